@@ -1,0 +1,162 @@
+"""ctypes bindings of the CPU checkers.  TEST INFRASTRUCTURE ONLY.
+
+  Oracle()     oracle/liboracle.so, the C restatement (peec_oracle.c)
+  Reference()  oracle/_ref/libpeec_ref.so, the reference's own sources
+               (only where they were compiled, i.e. not on the GPU host)
+
+Only tests/, the smoke check and the bench's CPU-baseline leg import this.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi  # noqa: E402  (struct layouts)
+
+ORACLE_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libpeec_ref.so")
+
+D = abi.c_double_p
+S = abi.c_size_t_p
+P = C.POINTER
+
+
+def _dp(a):
+    return a.ctypes.data_as(D)
+
+
+class Oracle:
+    def __init__(self, path=ORACLE_PATH):
+        if not os.path.exists(path):
+            raise RuntimeError("oracle library missing: run __graft_entry__.build()")
+        lib = C.CDLL(path)
+        sig = [
+            ("oracle_gauss_legendre_rule", C.c_int, [C.c_int, D, D]),
+            ("oracle_classify_pair", C.c_int, [P(abi.QuadPatch), P(abi.QuadPatch), C.c_double]),
+            ("oracle_patch_kernel", C.c_double,
+             [P(abi.QuadPatch), P(abi.QuadPatch), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
+            ("oracle_potential_evaluations", C.c_ulonglong, [C.c_int]),
+            ("oracle_inductance_matrix", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), P(C.c_int), C.c_double, C.c_double, C.c_int, D]),
+            ("oracle_inductance_rows", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), P(C.c_int), C.c_double, C.c_double, C.c_int,
+              C.c_size_t, C.c_size_t, D]),
+            ("oracle_potential_matrix", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), P(C.c_int), C.c_double, C.c_int, D]),
+            ("oracle_potential_rows", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), P(C.c_int), C.c_double, C.c_int, C.c_size_t,
+              C.c_size_t, D]),
+            ("oracle_lu_factorize", C.c_int,
+             [D, C.c_size_t, C.c_double, C.c_int, D, S, S, D]),
+            ("oracle_lu_solve", C.c_int, [D, S, C.c_size_t, D, D]),
+            ("oracle_complex_lu_factorize", C.c_int,
+             [D, C.c_size_t, C.c_double, C.c_int, D, S, S, D, D, D]),
+            ("oracle_complex_lu_solve", C.c_int, [D, S, D, D, C.c_size_t, D, D]),
+        ]
+        for name, res, args in sig:
+            f = getattr(lib, name)
+            f.restype, f.argtypes = res, args
+        self.lib = lib
+
+    @staticmethod
+    def _orders(o):
+        return (C.c_int * 4)(*o)
+
+    def gauss_legendre(self, order):
+        x, w = np.zeros(16), np.zeros(16)
+        if self.lib.oracle_gauss_legendre_rule(order, _dp(x), _dp(w)) != 0:
+            return None
+        return x[:order], w[:order]
+
+    def patch_kernel(self, a, b, orders=(4, 10, 12, 8), near_factor=0.5):
+        return self.lib.oracle_patch_kernel(C.byref(a), C.byref(b), *orders, near_factor)
+
+    def classify(self, a, b, near_factor=0.5):
+        return self.lib.oracle_classify_pair(C.byref(a), C.byref(b), near_factor)
+
+    def inductance(self, m, orders=(4, 10, 12, 8), near_factor=0.5, tol=1e-10, threads=None,
+                   rows=None):
+        n = m.n_edges
+        out = np.zeros((n, n))
+        threads = threads or os.cpu_count()
+        if rows is None:
+            s = self.lib.oracle_inductance_matrix(C.byref(m.mesh), C.byref(m.dual), self._orders(orders),
+                                                  near_factor, tol, threads, _dp(out))
+        else:
+            s = self.lib.oracle_inductance_rows(C.byref(m.mesh), C.byref(m.dual), self._orders(orders),
+                                                near_factor, tol, threads, rows[0], rows[1], _dp(out))
+        return s, out
+
+    def potential(self, m, orders=(4, 10, 12, 8), near_factor=0.5, threads=None, rows=None):
+        n = m.n_nodes
+        out = np.zeros((n, n))
+        threads = threads or os.cpu_count()
+        if rows is None:
+            s = self.lib.oracle_potential_matrix(C.byref(m.mesh), C.byref(m.dual), self._orders(orders),
+                                                 near_factor, threads, _dp(out))
+        else:
+            s = self.lib.oracle_potential_rows(C.byref(m.mesh), C.byref(m.dual), self._orders(orders),
+                                               near_factor, threads, rows[0], rows[1], _dp(out))
+        return s, out
+
+    def lu_factorize(self, a, tol=1e-14, threads=None):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        n = a.shape[0]
+        lu = np.zeros_like(a)
+        piv = np.zeros(n, dtype=np.uintp)
+        sc, scale = C.c_size_t(0), C.c_double(0)
+        s = self.lib.oracle_lu_factorize(_dp(a), n, tol, threads or os.cpu_count(), _dp(lu),
+                                         piv.ctypes.data_as(S), C.byref(sc), C.byref(scale))
+        return s, lu, piv, sc.value, scale.value
+
+    def lu_solve(self, lu, piv, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        s = self.lib.oracle_lu_solve(_dp(lu), piv.ctypes.data_as(S), lu.shape[0], _dp(b), _dp(x))
+        return s, x
+
+    def complex_lu_factorize(self, a, tol=1e-14, threads=None):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        n = a.shape[0]
+        lu = np.zeros_like(a)
+        piv = np.zeros(n, dtype=np.uintp)
+        rs, cs = np.zeros(n), np.zeros(n)
+        sc, scale = C.c_size_t(0), C.c_double(0)
+        s = self.lib.oracle_complex_lu_factorize(
+            a.ctypes.data_as(D), n, tol, threads or os.cpu_count(), lu.ctypes.data_as(D),
+            piv.ctypes.data_as(S), C.byref(sc), C.byref(scale), _dp(rs), _dp(cs))
+        return s, lu, piv, sc.value, scale.value, rs, cs
+
+    def complex_lu_solve(self, lu, piv, rs, cs, b):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b)
+        s = self.lib.oracle_complex_lu_solve(lu.ctypes.data_as(D), piv.ctypes.data_as(S), _dp(rs), _dp(cs),
+                                             lu.shape[0], b.ctypes.data_as(D), x.ctypes.data_as(D))
+        return s, x
+
+
+def reference_available():
+    return os.path.exists(REF_PATH)
+
+
+class Reference:
+    """The reference's own hot-path functions (same ABI as the drop-in)."""
+
+    def __init__(self, path=REF_PATH):
+        lib = C.CDLL(path)
+        abi._bind(lib, abi.DROP_IN_SYMBOLS)
+        extra = [
+            ("mesh_init", None, [P(abi.Mesh)]),
+            ("mesh_free", None, [P(abi.Mesh)]),
+            ("mesh_load_gmsh", C.c_int, [C.c_char_p, P(abi.Mesh)]),
+            ("mesh_build_topology", C.c_int, [P(abi.Mesh)]),
+            ("dual_mesh_init", None, [P(abi.DualMesh)]),
+            ("dual_mesh_free", None, [P(abi.DualMesh)]),
+            ("dual_mesh_build", C.c_int, [P(abi.Mesh), P(abi.DualMesh)]),
+        ]
+        abi._bind(lib, extra)
+        self.lib = lib

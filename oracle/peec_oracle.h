@@ -1,0 +1,83 @@
+/*
+ * CPU oracle for the PEEC hot path.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain C restatement of the reference algorithms (quadrature, Lp and P
+ * assembly, real and complex LU), written to follow the reference's
+ * operation order so that, built with ISO C flags (no FP contraction), it
+ * reproduces the reference bit for bit.  Only tests/, the smoke check and the
+ * bench's CPU baseline may load it; the GPU library never links or calls it.
+ *
+ * Every function cites the reference file:line it restates.
+ */
+#ifndef PEEC_ORACLE_H
+#define PEEC_ORACLE_H
+
+#include <stddef.h>
+
+#include "../include/complex_matrix.h"
+#include "../include/dual_mesh.h"
+#include "../include/mesh.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* quadrature.c:94-313 */
+int oracle_gauss_legendre_rule(int order, double *x, double *w);
+/* quadrature.c:550-607; returns 0 SELF, 1 TOUCHING, 2 NEAR, 3 FAR */
+int oracle_classify_pair(const QuadPatch *a, const QuadPatch *b, double near_factor);
+/* quadrature.c:975-1079 */
+double oracle_patch_kernel(const QuadPatch *a, const QuadPatch *b, int far_order,
+                           int near_order, int touching_order, int self_order,
+                           double near_factor);
+/* Number of triangle_potential_at() evaluations made by this thread since the
+ * last reset (work counter for the near-field roofline). */
+unsigned long long oracle_potential_evaluations(int reset);
+
+/* inductance.c:221-382 and :390-560.  orders[4] = far, near, touching, self.
+ * data must hold Ne*Ne doubles; threads >= 1 (OpenMP rows, dynamic). */
+int oracle_inductance_pair(const Mesh *mesh, const DualMesh *dual, size_t a, size_t b,
+                           const int orders[4], double near_factor,
+                           double direction_tolerance, double *value);
+int oracle_inductance_matrix(const Mesh *mesh, const DualMesh *dual, const int orders[4],
+                             double near_factor, double direction_tolerance,
+                             int threads, double *data);
+/* Same, for the rows [row_begin, row_end) only (upper triangle b >= a, both
+ * mirrors written): a bounded sample for CPU timing. */
+int oracle_inductance_rows(const Mesh *mesh, const DualMesh *dual, const int orders[4],
+                           double near_factor, double direction_tolerance, int threads,
+                           size_t row_begin, size_t row_end, double *data);
+
+/* potential.c:139-253 and :261-395 */
+int oracle_potential_pair(const Mesh *mesh, const DualMesh *dual, size_t i, size_t j,
+                          const int orders[4], double near_factor, double *value);
+int oracle_potential_matrix(const Mesh *mesh, const DualMesh *dual, const int orders[4],
+                            double near_factor, int threads, double *data);
+int oracle_potential_rows(const Mesh *mesh, const DualMesh *dual, const int orders[4],
+                          double near_factor, int threads, size_t row_begin,
+                          size_t row_end, double *data);
+
+/* lu.c:194-479: factor in place of a copy.  lu (n*n) receives packed L\U,
+ * pivots (n) the pivot rows.  Returns 0 / -1 / -2 like the reference. */
+int oracle_lu_factorize(const double *input, size_t n, double pivot_tolerance,
+                        int threads, double *lu, size_t *pivots, size_t *swap_count,
+                        double *matrix_scale);
+/* lu.c:494-653 */
+int oracle_lu_solve(const double *lu, const size_t *pivots, size_t n, const double *b,
+                    double *x);
+
+/* complex_lu.c:208-550 */
+int oracle_complex_lu_factorize(const Complex *input, size_t n, double pivot_tolerance,
+                                int threads, Complex *lu, size_t *pivots,
+                                size_t *swap_count, double *matrix_scale,
+                                double *row_scale, double *column_scale);
+/* complex_lu.c:598-778 */
+int oracle_complex_lu_solve(const Complex *lu, const size_t *pivots,
+                            const double *row_scale, const double *column_scale,
+                            size_t n, const Complex *b, Complex *x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

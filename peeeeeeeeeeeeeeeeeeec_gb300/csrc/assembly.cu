@@ -1,0 +1,1098 @@
+// Lp / P assembly on sm_103a: the 1/R panel integrals of the dual mesh.
+//
+// Reference path (paths inside the reference project):
+//   src/peec/inductance.c:221-560  Lp entries and matrix
+//   src/peec/potential.c:139-395   P entries and matrix
+//   src/peec/quadrature.c:550-1079 pair classification, far rule, analytic
+//                                  triangle potential, adaptive outer rule
+//
+// Pipeline for one matrix (all on the library stream):
+//   1. k_patch_prep      per patch: bounding box, longest side
+//   2. k_far_points      per patch: the far-rule points and weights of its two
+//                        triangles (x, y, z, w) -- reused by every pair
+//   3. k_near_scan       per patch i: every partner j of the upper triangle
+//                        whose class is not FAR (counted, scanned, filled:
+//                        a deterministic, i-major, j-sorted list)
+//   4. k_near_eval       one warp per (near pair, triangle pair, direction):
+//                        adaptive outer Gauss rule over the analytic inner
+//                        potential, depth-first with an explicit stack
+//   5. k_near_finalize   per near pair: the 4 triangle-pair values combined in
+//                        the reference's order (both orientations)
+//   6. k_assemble_tiles  one CTA per 32x32 tile of the upper triangle, one
+//                        warp per entry: sums its patch pairs in the
+//                        reference's (i, j) order, far pairs by the product
+//                        rule with a warp-shuffle reduction, near pairs from
+//                        step 5; the tile and its mirror are written with
+//                        coalesced row stores.
+// Everything is FP64.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/dual_mesh.h"
+#include "../../include/inductance.h"
+#include "../../include/mesh.h"
+#include "../../include/peec_gb300.h"
+#include "../../include/potential.h"
+#include "../../include/quadrature.h"
+#include "common.cuh"
+#include "geometry.cuh"
+
+namespace peec {
+
+static const double kMu0Over4Pi = 1.0e-7;               // inductance.c:24
+static const double kInv4PiEps0 = 8.987551792261171e9;  // potential.c:26
+
+__constant__ double c_gl_x[GL_NUM_ORDERS][16];
+__constant__ double c_gl_w[GL_NUM_ORDERS][16];
+
+static bool upload_gl_tables() {
+    static std::once_flag once;
+    static bool ok = false;
+    std::call_once(once, [] {
+        ok = cuda_ok(cudaMemcpyToSymbol(c_gl_x, GL_NODES, sizeof(GL_NODES)), "GL table") &&
+             cuda_ok(cudaMemcpyToSymbol(c_gl_w, GL_WEIGHTS, sizeof(GL_WEIGHTS)), "GL table");
+    });
+    return ok;
+}
+
+enum Kind { KIND_INDUCTANCE = 0, KIND_POTENTIAL = 1, KIND_RAW = 2 };
+
+// Device-resident region set: the patches of all edge (or node) regions,
+// region-contiguous, plus per-region scale data.
+struct RegionsDev {
+    int n = 0;             // regions
+    int np = 0;            // patches
+    int *off = nullptr;    // [n+1]
+    int *owner = nullptr;  // [np]
+    double *corner = nullptr;  // [np*12]
+    double *box = nullptr;     // [np*6]
+    double *size = nullptr;    // [np]
+    double *dir = nullptr;     // [n*3]   (inductance)
+    double *scale = nullptr;   // [n]     width w (inductance) or area S (potential); <= 0 marks a bad region
+    int *same_obj = nullptr;   // [np]    object id for the reference's pointer test
+};
+
+// one far-rule point: position and weight (32-byte aligned for vector loads)
+struct alignas(32) FarPt {
+    double x, y, z, w;
+};
+
+struct NearRec {
+    int i, j, cls, pad;
+};
+
+// ---------------------------------------------------------------------
+// 1-2. per-patch preparation
+// ---------------------------------------------------------------------
+__global__ void k_patch_prep(RegionsDev R) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= R.np) return;
+    const double *c = R.corner + 12 * (size_t)p;
+    patch_aabb(c, R.box + 6 * (size_t)p);
+    R.size[p] = patch_size(c);
+}
+
+// Far-rule points of patch p: triangle t (0: corners 0,1,2; 1: 0,2,3), point
+// (iu, iv) at index t*q*q + iu*q + iv; weight (0.5 w_iu)(0.5 w_iv) J
+// (reference quadrature.c:679-783 evaluates the same points per pair).
+__global__ void k_far_points(RegionsDev R, int q, int row, FarPt *pts) {
+    int np = R.np, per = 2 * q * q;
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)np * per) return;
+    int p = (int)(g / per), k = (int)(g % per);
+    int t = k / (q * q), iu = (k / q) % q, iv = k % q;
+    const double *c = R.corner + 12 * (size_t)p;
+    const double *p0 = c, *p1 = c + (t == 0 ? 3 : 6), *p2 = c + (t == 0 ? 6 : 9);
+    double u = 0.5 * (c_gl_x[row][iu] + 1.0), wu = 0.5 * c_gl_w[row][iu];
+    double v = 0.5 * (c_gl_x[row][iv] + 1.0), wv = 0.5 * c_gl_w[row][iv];
+    double r[3], jac;
+    tri_map(p0, p1, p2, u, v, r, &jac);
+    pts[g] = FarPt{r[0], r[1], r[2], wu * wv * jac};
+}
+
+// ---------------------------------------------------------------------
+// 3. near-pair discovery
+// ---------------------------------------------------------------------
+struct ScanArgs {
+    RegionsDev R;
+    int kind;
+    double near_factor;
+    double dir_tol;
+    int only_a, only_b;  // >= 0: restrict to the single entry (only_a, only_b)
+};
+
+__device__ __forceinline__ bool region_pair_skipped(const ScanArgs &s, int a, int b) {
+    if (s.only_a >= 0) {
+        int lo = s.only_a < s.only_b ? s.only_a : s.only_b, hi = s.only_a < s.only_b ? s.only_b : s.only_a;
+        if (!(a == lo && b == hi)) return true;
+    }
+    if (s.kind == KIND_INDUCTANCE) {
+        double d = dot3(s.R.dir + 3 * a, s.R.dir + 3 * b);
+        if (fabs(d) < s.dir_tol) return true;  // entry is exactly 0, no integral
+    }
+    return false;
+}
+
+// pass 0 counts, pass 1 writes (count[i] -> offsets in off[i])
+__global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, NearRec *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const RegionsDev &R = s.R;
+    if (i >= R.np) return;
+    int a = R.owner[i];
+    const double *ci = R.corner + 12 * (size_t)i, *bi = R.box + 6 * (size_t)i;
+    double hi = R.size[i];
+    int w = pass ? off[i] : 0, found = 0;
+    int b_prev = -1;
+    bool skip_b = false;
+    for (int j = R.off[a]; j < R.np; ++j) {
+        int b = R.owner[j];
+        if (b == a && j < i) continue;
+        if (b != b_prev) {
+            skip_b = region_pair_skipped(s, a, b);
+            b_prev = b;
+        }
+        if (skip_b) {
+            j = R.off[b + 1] - 1;  // jump to the next region
+            continue;
+        }
+        int cls = classify_pair(ci, bi, hi, R.corner + 12 * (size_t)j, R.box + 6 * (size_t)j, R.size[j],
+                                s.near_factor, R.same_obj[i] == R.same_obj[j]);
+        if (cls == CLS_FAR) continue;
+        if (pass) out[w + found] = NearRec{i, j, cls, 0};
+        ++found;
+    }
+    if (!pass) count[i] = found;
+}
+
+// exclusive scan of count[0..n) into off[0..n], single CTA of 1024 threads
+__global__ void k_exclusive_scan(const int *count, int *off, int n) {
+    __shared__ long long part[1024];
+    int t = threadIdx.x;
+    int chunk = (n + 1023) / 1024;
+    int lo = t * chunk, hi = min(n, lo + chunk);
+    long long s = 0;
+    for (int k = lo; k < hi; ++k) s += count[k];
+    part[t] = s;
+    __syncthreads();
+    for (int d = 1; d < 1024; d <<= 1) {
+        long long v = (t >= d) ? part[t - d] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long base = part[t] - s;
+    for (int k = lo; k < hi; ++k) {
+        off[k] = (int)base;
+        base += count[k];
+    }
+    if (t == 1023) off[n] = (int)part[1023];
+}
+
+// ---------------------------------------------------------------------
+// 4. analytic potential + adaptive outer rule (quadrature.c:842-938)
+// ---------------------------------------------------------------------
+struct TriPot {
+    double p[3][3], unit[3][3], outw[3][3], len[3], nrm[3];
+    double twice_area;
+};
+
+__device__ void tri_prepare(const double *v, TriPot &t) {
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) {
+            t.p[i][k] = v[3 * i + k];
+            t.unit[i][k] = v[3 * ((i + 1) % 3) + k] - v[3 * i + k];
+        }
+    cross3(t.unit[0], t.unit[1], t.nrm);
+    t.twice_area = norm3(t.nrm);
+    if (t.twice_area == 0.0) return;
+    for (int k = 0; k < 3; ++k) t.nrm[k] /= t.twice_area;
+    for (int i = 0; i < 3; ++i) {
+        t.len[i] = norm3(t.unit[i]);
+        for (int k = 0; k < 3; ++k) t.unit[i][k] /= t.len[i];
+        cross3(t.unit[i], t.nrm, t.outw[i]);
+    }
+}
+
+// \int_T 1/|r - r0| dS exactly: sum over edges of d_e * (asinh terms) minus
+// |h * solid angle| (van Oosterom's uniform-layer formula, as the reference).
+__device__ double tri_potential(const TriPot &t, const double *r) {
+    double v[3][3], rad[3];
+    for (int i = 0; i < 3; ++i) {
+        for (int k = 0; k < 3; ++k) v[i][k] = t.p[i][k] - r[k];
+        rad[i] = norm3(v[i]);
+    }
+    double h = dot3(v[0], t.nrm);
+    double acc = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        double d = dot3(v[i], t.outw[i]);
+        if (d == 0.0) continue;
+        double s = dot3(v[i], t.unit[i]);
+        double q = hypot(d, h);
+        double e = asinh((s + t.len[i]) / q) - asinh(s / q);
+        acc += d * e;
+    }
+    if (h != 0.0) {
+        double c[3];
+        cross3(v[1], v[2], c);
+        double den = rad[0] * rad[1] * rad[2] + dot3(v[0], v[1]) * rad[2] + dot3(v[1], v[2]) * rad[0] +
+                     dot3(v[2], v[0]) * rad[1];
+        double omega = 2.0 * atan2(dot3(v[0], c), den);
+        acc -= fabs(h * omega);
+    }
+    return acc;
+}
+
+struct AdaptNode {
+    double v[9];
+    double tol;
+    int depth;
+    int pad;
+};
+
+static const int kStackCap = 28;  // depth <= 24 => at most 26 pending nodes
+
+struct NearWarpSmem {
+    TriPot inner;
+    AdaptNode stack[kStackCap];
+};
+
+// Depth-first adaptive integration of triangle `outer` against the inner
+// potential, by one warp: the low and high rules of a node are spread over
+// the lanes and reduced with shuffles; accepted nodes add `high` left to
+// right.  Returns NaN if a rule is non-finite or depth 24 is exceeded
+// (reference quadrature.c:915-938).
+__device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order, double abs_tol,
+                                unsigned long long &evals) {
+    const int lane = threadIdx.x & 31;
+    const int ql = order <= 6 ? 3 : 4;
+    const int rl = gl_row(ql), rh = gl_row(order);
+    const int nlo = ql * ql, ntot = nlo + order * order;
+    if (lane == 0) {
+        for (int k = 0; k < 9; ++k) sm.stack[0].v[k] = outer[k];
+        sm.stack[0].tol = abs_tol;
+        sm.stack[0].depth = 0;
+    }
+    __syncwarp();
+    int sp = 1;
+    double acc = 0.0;
+    while (sp > 0) {
+        AdaptNode nd = sm.stack[sp - 1];
+        --sp;
+        __syncwarp();
+        const double *a0 = nd.v, *a1 = nd.v + 3, *a2 = nd.v + 6;
+        double lo = 0.0, hi = 0.0;
+        for (int k = lane; k < ntot; k += 32) {
+            int ord, row, idx;
+            if (k < nlo) {
+                ord = ql;
+                row = rl;
+                idx = k;
+            } else {
+                ord = order;
+                row = rh;
+                idx = k - nlo;
+            }
+            int i = idx / ord, j = idx % ord;
+            double xi = c_gl_x[row][i], xj = c_gl_x[row][j];
+            double wi = c_gl_w[row][i], wj = c_gl_w[row][j];
+            double r[3], jac;
+            tri_map(a0, a1, a2, 0.5 * (xi + 1.0), 0.5 * (xj + 1.0), r, &jac);
+            double val = 0.25 * wi * wj * jac * tri_potential(sm.inner, r);
+            if (k < nlo)
+                lo += val;
+            else
+                hi += val;
+        }
+        evals += (unsigned long long)ntot;
+        lo = warp_sum(lo);
+        hi = warp_sum(hi);
+        if (!isfinite(lo) || !isfinite(hi)) return nan("");
+        if (fabs(hi - lo) <= nd.tol + 2e-5 * fabs(hi)) {
+            acc += hi;
+            continue;
+        }
+        if (nd.depth >= 24 || sp + 2 > kStackCap) return nan("");
+        int e = 0;
+        double longest = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            double s = dist3(nd.v + 3 * i, nd.v + 3 * ((i + 1) % 3));
+            if (s > longest) {
+                longest = s;
+                e = i;
+            }
+        }
+        int j = (e + 1) % 3, k = (e + 2) % 3;
+        if (lane == 0) {
+            AdaptNode &left = sm.stack[sp + 1], &right = sm.stack[sp];
+            for (int d = 0; d < 3; ++d) {
+                double mid = 0.5 * (nd.v[3 * e + d] + nd.v[3 * j + d]);
+                left.v[d] = nd.v[3 * e + d];
+                left.v[3 + d] = mid;
+                left.v[6 + d] = nd.v[3 * k + d];
+                right.v[d] = mid;
+                right.v[3 + d] = nd.v[3 * j + d];
+                right.v[6 + d] = nd.v[3 * k + d];
+            }
+            left.tol = right.tol = nd.tol * 0.5;
+            left.depth = right.depth = nd.depth + 1;
+        }
+        __syncwarp();
+        sp += 2;
+    }
+    return acc;
+}
+
+// Triangle t of a patch: 0 -> corners (0,1,2), 1 -> (0,2,3).
+__device__ __forceinline__ void patch_triangle(const double *c, int t, double *v) {
+    const int idx[2][3] = {{0, 1, 2}, {0, 2, 3}};
+    for (int m = 0; m < 3; ++m)
+        for (int k = 0; k < 3; ++k) v[3 * m + k] = c[3 * idx[t][m] + k];
+}
+
+struct NearEvalArgs {
+    const double *corner;
+    const NearRec *rec;
+    int nrec;
+    int orders[4];  // far, near, touching, self
+    double *slot;   // [nrec*4*2]
+    int *kind;      // [nrec*4]: 0 adaptive, 1 zero area, 2 identical triangles
+    int *next_job;  // work counter
+    unsigned long long *evals;
+};
+
+// One warp per job (record, triangle pair t = s*2+u, direction d); warps
+// fetch jobs dynamically because refinement depth varies a lot.
+__global__ void __launch_bounds__(256) k_near_eval(NearEvalArgs A) {
+    extern __shared__ unsigned char smem_raw[];
+    NearWarpSmem *all = reinterpret_cast<NearWarpSmem *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    NearWarpSmem &sm = all[warp];
+    const long long njobs = (long long)A.nrec * 8;
+    unsigned long long evals = 0;
+    for (;;) {
+        long long job = 0;
+        if (lane == 0) job = atomicAdd(A.next_job, 1);
+        job = __shfl_sync(0xffffffffu, job, 0);
+        if (job >= njobs) break;
+        int r = (int)(job >> 3), t = (int)((job >> 1) & 3), d = (int)(job & 1);
+        NearRec rec = A.rec[r];
+        double ta[9], tb[9];
+        patch_triangle(A.corner + 12 * (size_t)rec.i, t >> 1, ta);
+        patch_triangle(A.corner + 12 * (size_t)rec.j, t & 1, tb);
+        // outer = the triangle integrated by the rule, inner = the potential source
+        const double *outer = d == 0 ? ta : tb, *inner = d == 0 ? tb : ta;
+        TriPot po;  // outer's own prepared form (area, identity test)
+        tri_prepare(outer, po);
+        if (lane == 0) tri_prepare(inner, sm.inner);
+        __syncwarp();
+        double out;
+        int kind;
+        if (po.twice_area == 0.0 || sm.inner.twice_area == 0.0) {
+            kind = 1;
+            out = 0.0;
+        } else {
+            bool identical = true;
+            for (int m = 0; m < 3; ++m) {
+                bool hit = false;
+                for (int q = 0; q < 3; ++q)
+                    if (same_point(ta + 3 * m, tb + 3 * q)) hit = true;
+                if (!hit) identical = false;
+            }
+            if (identical) {
+                // K(T,T) = (2 area / 3) * sum over the outer vertices of the
+                // inner potential (quadrature.c:948-956); d = 1 gives the
+                // value with the roles of the two triangles swapped.
+                kind = 2;
+                double s = 0.0;
+                for (int m = 0; m < 3; ++m) s += tri_potential(sm.inner, outer + 3 * m);
+                out = po.twice_area * s / 3.0;
+                evals += 3;
+            } else {
+                kind = 0;
+                int cls = rec.cls;
+                int order = cls == CLS_SELF ? A.orders[3] : cls == CLS_TOUCHING ? A.orders[2] : A.orders[1];
+                if (order < 6) order = 6;
+                double aa = d == 0 ? po.twice_area : sm.inner.twice_area;
+                double ab = d == 0 ? sm.inner.twice_area : po.twice_area;
+                double scale = aa * ab / sqrt(fmax(aa, ab));
+                out = warp_adaptive(outer, sm, order, 2e-5 * scale, evals);
+            }
+        }
+        if (lane == 0) {
+            A.slot[(size_t)r * 8 + t * 2 + d] = out;
+            if (d == 0) A.kind[(size_t)r * 4 + t] = kind;
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && evals) atomicAdd(A.evals, evals);
+}
+
+// K for each near record in both orientations (quadrature.c:1060-1076 sums
+// the triangle pairs (0,0),(0,1),(1,0),(1,1); the swapped patch order visits
+// the same values as (0,0),(1,0),(0,1),(1,1)).
+__global__ void k_near_finalize(int nrec, const double *slot, const int *kind, double2 *kval) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    double fwd[4], rev[4];
+    for (int t = 0; t < 4; ++t) {
+        double s0 = slot[(size_t)r * 8 + t * 2], s1 = slot[(size_t)r * 8 + t * 2 + 1];
+        int k = kind[(size_t)r * 4 + t];
+        if (k == 1) {
+            fwd[t] = rev[t] = 0.0;
+        } else if (k == 2) {
+            fwd[t] = s0;
+            rev[t] = s1;
+        } else {
+            fwd[t] = rev[t] = 0.5 * (s0 + s1);
+        }
+    }
+    double kf = 0.0, kr = 0.0;
+    const int rev_order[4] = {0, 2, 1, 3};
+    bool bad_f = false, bad_r = false;
+    for (int t = 0; t < 4; ++t) {
+        if (!isfinite(fwd[t])) bad_f = true;
+        kf += fwd[t];
+        double v = rev[rev_order[t]];
+        if (!isfinite(v)) bad_r = true;
+        kr += v;
+    }
+    kval[r] = make_double2(bad_f ? nan("") : kf, bad_r ? nan("") : kr);
+}
+
+// ---------------------------------------------------------------------
+// 6. tiled assembly
+// ---------------------------------------------------------------------
+struct TileArgs {
+    RegionsDev R;
+    int kind;
+    double dir_tol;
+    const FarPt *pts;
+    int npts;
+    const int *near_off;
+    const NearRec *near_rec;
+    const double2 *near_k;
+    double *out;  // n*n row-major
+    int n;
+    int only_a, only_b;
+    unsigned long long *err;  // min over failing entries of (a*n+b)+1, 0 = none
+};
+
+static const int kTile = 32;
+static const int kTileWarps = 8;
+
+// far-rule integral of one patch pair, all 4 triangle pairs at once:
+// sum_p W_p sum_q W_q / |r_p - r_q| over the 2q^2 points of each patch
+__device__ __forceinline__ double far_pair(const FarPt *pa, const FarPt *pb, int npts) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (int p = lane; p < npts; p += 32) {
+        FarPt A = pa[p];
+        double s = 0.0;
+#pragma unroll 4
+        for (int q = 0; q < npts; ++q) {
+            FarPt B = pb[q];
+            double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+            double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+            if (r2 > 0.0) s = fma(B.w, rsqrt(r2), s);
+        }
+        acc = fma(A.w, s, acc);
+    }
+    return warp_sum(acc);
+}
+
+__device__ __forceinline__ bool near_lookup(const TileArgs &T, int i, int j, double &k) {
+    int p = i, q = j;
+    bool rev = false;
+    if (T.R.owner[i] == T.R.owner[j] && i > j) {
+        p = j;
+        q = i;
+        rev = true;
+    }
+    int lo = T.near_off[p], hi = T.near_off[p + 1];
+    for (int m = lo; m < hi; ++m) {
+        int jj = T.near_rec[m].j;
+        if (jj == q) {
+            double2 kv = T.near_k[m];
+            k = rev ? kv.y : kv.x;
+            return true;
+        }
+        if (jj > q) break;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) {
+    __shared__ double tile[kTile][kTile + 1];
+    const int ta = blockIdx.y, tb = blockIdx.x;
+    if (tb < ta) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const RegionsDev &R = T.R;
+    const int n = T.n;
+    for (int e = warp; e < kTile * kTile; e += kTileWarps) {
+        int r = e / kTile, c = e % kTile;
+        int a = ta * kTile + r, b = tb * kTile + c;
+        double val = 0.0;
+        bool active = a < n && b < n && !(ta == tb && c < r);
+        if (active && T.only_a >= 0) {
+            int lo = min(T.only_a, T.only_b), hi = max(T.only_a, T.only_b);
+            active = (a == lo && b == hi);
+        }
+        if (active) {
+            double dot = 0.0, sa = R.scale[a], sb = R.scale[b];
+            bool skip = false;
+            if (T.kind == KIND_INDUCTANCE) {
+                dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
+                skip = fabs(dot) < T.dir_tol;
+            }
+            bool bad = false;
+            if (!skip) {
+                if (T.kind != KIND_RAW && (sa <= 0.0 || sb <= 0.0)) bad = true;
+                double integral = 0.0;
+                for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i)
+                    for (int j = R.off[b]; j < R.off[b + 1]; ++j) {
+                        double k;
+                        if (!near_lookup(T, i, j, k))
+                            k = far_pair(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
+                        if (!isfinite(k)) {
+                            bad = true;
+                            break;
+                        }
+                        integral += k;
+                    }
+                if (T.kind == KIND_INDUCTANCE)
+                    val = kMu0Over4Pi * dot * integral / (sa * sb);
+                else if (T.kind == KIND_POTENTIAL)
+                    val = kInv4PiEps0 * integral / (sa * sb);
+                else
+                    val = integral;
+                if (!isfinite(val)) bad = true;
+            }
+            if (bad) {
+                if (lane == 0) atomicMin(T.err, (unsigned long long)a * (unsigned long long)n + b + 1ull);
+                val = 0.0;
+            }
+        }
+        if (lane == 0) tile[r][c] = val;
+    }
+    __syncthreads();
+    // coalesced writes: the tile rows, then (off the diagonal) the mirror rows
+    const int rows = min(kTile, n - ta * kTile), cols = min(kTile, n - tb * kTile);
+    if (ta == tb) {
+        for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+            int r = e / kTile, c = e % kTile;
+            if (c < r) tile[r][c] = tile[c][r];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        int r = e / kTile, c = e % kTile;
+        if (r < rows && c < cols) T.out[(size_t)(ta * kTile + r) * n + tb * kTile + c] = tile[r][c];
+    }
+    if (ta != tb) {
+        for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+            int c = e / kTile, r = e % kTile;  // output row = column c of the tile
+            if (r < rows && c < cols) T.out[(size_t)(tb * kTile + c) * n + ta * kTile + r] = tile[r][c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------
+struct HostRegions {
+    std::vector<int> off, owner, same_obj;
+    std::vector<double> corner, dir, scale;
+    int n = 0;
+};
+
+// Gathers the patch lists of `kind` regions; `scale` <= 0 marks a region
+// whose entries must fail (no patches, or non-positive width / area).
+static bool gather_regions(const Mesh *mesh, const DualMesh *dual, int kind, HostRegions &H) {
+    bool edges = kind == KIND_INDUCTANCE;
+    size_t n = edges ? mesh->n_edges : mesh->n_nodes;
+    const PatchList *lists = edges ? dual->edge_patches : dual->node_patches;
+    if (!lists || n == 0 || n > 0x7fffffff) return false;
+    H.n = (int)n;
+    H.off.assign(n + 1, 0);
+    H.scale.assign(n, 0.0);
+    if (edges) H.dir.assign(3 * n, 0.0);
+    size_t total = 0;
+    for (size_t r = 0; r < n; ++r) {
+        H.off[r] = (int)total;
+        total += lists[r].count;
+        if (total > 0x7fffffff / 12) return false;
+    }
+    H.off[n] = (int)total;
+    H.corner.resize(12 * total);
+    H.owner.resize(total);
+    H.same_obj.resize(total);
+    for (size_t r = 0; r < n; ++r) {
+        const PatchList &L = lists[r];
+        for (size_t k = 0; k < L.count; ++k) {
+            size_t p = (size_t)H.off[r] + k;
+            memcpy(&H.corner[12 * p], L.patches[k].points, 12 * sizeof(double));
+            H.owner[p] = (int)r;
+            H.same_obj[p] = (int)p;
+        }
+        if (edges) {
+            double area = dual->edge_region_areas[r], length = mesh->edge_lengths[r];
+            double w = (area <= 0.0 || length <= 0.0) ? 0.0 : area / length;  // inductance.c:152-167
+            H.scale[r] = (L.count == 0) ? 0.0 : w;
+            for (int k = 0; k < 3; ++k) H.dir[3 * r + k] = mesh->edge_directions[3 * r + k];
+        } else {
+            double area = dual->node_region_areas[r];
+            H.scale[r] = (L.count == 0 || !(area > 0.0)) ? 0.0 : area;
+        }
+    }
+    return true;
+}
+
+struct DeviceRegions {
+    DBuf<int> off, owner, same_obj;
+    DBuf<double> corner, box, size, dir, scale;
+    RegionsDev view;
+    bool upload(const HostRegions &H) {
+        int np = H.off[H.n];
+        if (!off.alloc(H.n + 1) || !owner.alloc(np) || !same_obj.alloc(np) || !corner.alloc(12 * (size_t)np) ||
+            !box.alloc(6 * (size_t)np) || !size.alloc(np) || !scale.alloc(H.n) ||
+            !dir.alloc(H.dir.empty() ? 0 : H.dir.size()))
+            return false;
+        bool ok = off.upload(H.off.data(), H.off.size()) && scale.upload(H.scale.data(), H.scale.size());
+        if (np) ok = ok && owner.upload(H.owner.data(), np) && same_obj.upload(H.same_obj.data(), np) &&
+                     corner.upload(H.corner.data(), H.corner.size());
+        if (!H.dir.empty()) ok = ok && dir.upload(H.dir.data(), H.dir.size());
+        view.n = H.n;
+        view.np = np;
+        view.off = off.p;
+        view.owner = owner.p;
+        view.same_obj = same_obj.p;
+        view.corner = corner.p;
+        view.box = box.p;
+        view.size = size.p;
+        view.dir = dir.p;
+        view.scale = scale.p;
+        if (ok && np) {
+            PEEC_LAUNCH(k_patch_prep, (np + 127) / 128, 128, 0, view);
+            ok = launch_ok("patch preparation");
+        }
+        return ok;
+    }
+};
+
+struct AssemblyOptions {
+    int orders[4];  // far, near, touching, self
+    double near_factor;
+    double dir_tol;
+};
+
+static bool orders_valid(const AssemblyOptions &o) {
+    for (int k = 0; k < 4; ++k)
+        if (gl_row(o.orders[k]) < 0) return false;
+    return isfinite(o.near_factor) && o.near_factor >= 0.0;
+}
+
+// Runs steps 2-6 into d_out (n*n on the device).  Returns 0, or -1 with
+// *bad_entry = a*n+b of one failing entry (or -1 if the failure is not tied
+// to an entry).
+static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, double *d_out, int only_a,
+                        int only_b, long long *bad_entry, PeecAssemblyStats *stats) {
+    *bad_entry = -1;
+    if (!upload_gl_tables()) return -1;
+    const RegionsDev &R = D.view;
+    const int n = R.n, np = R.np;
+    const int q = o.orders[0], npts = 2 * q * q;
+    cudaEvent_t ev[4];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], stream());
+
+    DBuf<FarPt> pts((size_t)np * npts);
+    DBuf<int> count(np + 1), near_off(np + 1), counter(1);
+    DBuf<unsigned long long> err(1), evals(1);
+    if ((np && (!pts.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p) return -1;
+    cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), stream());
+    cudaMemsetAsync(evals.p, 0, sizeof(unsigned long long), stream());
+    cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
+    if (np) {
+        long long tot = (long long)np * npts;
+        PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p);
+        ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
+        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 0, count.p, nullptr, nullptr);
+        PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, count.p, near_off.p, np);
+    } else {
+        cudaMemsetAsync(near_off.p, 0, sizeof(int), stream());
+    }
+    int nrec = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&nrec, near_off.p + np, sizeof(int), cudaMemcpyDeviceToHost, stream()),
+                 "near count") ||
+        !sync("near-pair discovery"))
+        return -1;
+    DBuf<NearRec> rec(nrec);
+    DBuf<double> slot((size_t)nrec * 8);
+    DBuf<int> kindbuf((size_t)nrec * 4);
+    DBuf<double2> kval(nrec);
+    if (nrec && (!rec.p || !slot.p || !kindbuf.p || !kval.p)) return -1;
+    cudaEventRecord(ev[1], stream());
+    if (nrec) {
+        ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
+        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 1, nullptr, near_off.p, rec.p);
+        NearEvalArgs A;
+        A.corner = R.corner;
+        A.rec = rec.p;
+        A.nrec = nrec;
+        for (int k = 0; k < 4; ++k) A.orders[k] = o.orders[k];
+        A.slot = slot.p;
+        A.kind = kindbuf.p;
+        A.next_job = counter.p;
+        A.evals = evals.p;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        size_t smem = 8 * sizeof(NearWarpSmem);
+        static std::once_flag attr_once;
+        std::call_once(attr_once, [smem] {
+            cudaFuncSetAttribute(k_near_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        });
+        long long jobs = (long long)nrec * 8;
+        long long want = (jobs + 7) / 8;
+        int grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
+        PEEC_LAUNCH(k_near_eval, grid, 256, smem, A);
+        PEEC_LAUNCH(k_near_finalize, (nrec + 127) / 128, 128, 0, nrec, slot.p, kindbuf.p, kval.p);
+    }
+    cudaEventRecord(ev[2], stream());
+    TileArgs T;
+    T.R = R;
+    T.kind = kind;
+    T.dir_tol = o.dir_tol;
+    T.pts = pts.p;
+    T.npts = npts;
+    T.near_off = near_off.p;
+    T.near_rec = rec.p;
+    T.near_k = kval.p;
+    T.out = d_out;
+    T.n = n;
+    T.only_a = only_a;
+    T.only_b = only_b;
+    T.err = err.p;
+    int nt = (n + kTile - 1) / kTile;
+    PEEC_LAUNCH(k_assemble_tiles, dim3(nt, nt), kTileWarps * 32, 0, T);
+    cudaEventRecord(ev[3], stream());
+    if (!launch_ok("assembly kernels")) return -1;
+    unsigned long long e = 0, ne = 0;
+    cudaMemcpyAsync(&e, err.p, sizeof(e), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(&ne, evals.p, sizeof(ne), cudaMemcpyDeviceToHost, stream());
+    if (!sync("assembly")) return -1;
+    if (stats) {
+        float t01 = 0, t12 = 0, t23 = 0;
+        cudaEventElapsedTime(&t01, ev[0], ev[1]);
+        cudaEventElapsedTime(&t12, ev[1], ev[2]);
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        stats->near_pairs = (unsigned long long)nrec;
+        stats->potential_evaluations = ne;
+        stats->ms_prepare = t01;
+        stats->ms_near = t12;
+        stats->ms_far = t23;
+    }
+    for (auto &ev_ : ev) cudaEventDestroy(ev_);
+    if (e) {
+        *bad_entry = (long long)(e - 1);
+        return -1;
+    }
+    return 0;
+}
+
+// Counts the far-rule point evaluations of a matrix on the host from the
+// region sizes and the near list size (algorithmic work for the roofline).
+}  // namespace peec
+
+using namespace peec;
+
+// ---------------------------------------------------------------------
+// C ABI: quadrature.h
+// ---------------------------------------------------------------------
+extern "C" {
+
+int gauss_legendre_rule(int order, double *x, double *w) {
+    if (x == NULL || w == NULL) return -1;
+    int row = gl_row(order);
+    if (row < 0) {
+        fprintf(stderr, "ERROR: unsupported Gauss-Legendre order: %d.\n", order);
+        return -1;
+    }
+    for (int i = 0; i < order; ++i) {
+        x[i] = GL_NODES[row][i];
+        w[i] = GL_WEIGHTS[row][i];
+    }
+    return 0;
+}
+
+double triangle_area(const double p0[3], const double p1[3], const double p2[3]) {
+    double a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    double b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    double c[3];
+    cross3(a, b, c);
+    return 0.5 * norm3(c);
+}
+
+double quad_patch_area(const QuadPatch *patch) {
+    if (patch == NULL) return 0.0;
+    const double *c = patch->points;
+    return triangle_area(c, c + 3, c + 6) + triangle_area(c, c + 6, c + 9);
+}
+
+double quad_patch_size(const QuadPatch *patch) {
+    if (patch == NULL) return 0.0;
+    return patch_size(patch->points);
+}
+
+double quad_patch_min_vertex_distance(const QuadPatch *a, const QuadPatch *b) {
+    if (a == NULL || b == NULL) return 0.0;
+    double best = HUGE_VAL;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double d = dist3(a->points + 3 * i, b->points + 3 * j);
+            if (d < best) best = d;
+        }
+    return best;
+}
+
+QuadPairType quad_patch_classify_pair(const QuadPatch *a, const QuadPatch *b, double near_factor) {
+    if (a == NULL || b == NULL) return QUAD_PAIR_FAR;
+    double ba[6], bb[6];
+    patch_aabb(a->points, ba);
+    patch_aabb(b->points, bb);
+    return (QuadPairType)classify_pair(a->points, ba, patch_size(a->points), b->points, bb, patch_size(b->points),
+                                       near_factor, a == b);
+}
+
+double quad_patch_kernel_1_over_r(const QuadPatch *a, const QuadPatch *b, int far_order, int near_order,
+                                  int touching_order, int self_order, double near_factor) {
+    if (a == NULL || b == NULL) return nan("");
+    AssemblyOptions o = {{far_order, near_order, touching_order, self_order}, near_factor, 0.0};
+    if (!orders_valid(o)) return nan("");
+    HostRegions H;
+    bool same = (a == b);
+    H.n = same ? 1 : 2;
+    H.off = same ? std::vector<int>{0, 1} : std::vector<int>{0, 1, 2};
+    H.owner = same ? std::vector<int>{0} : std::vector<int>{0, 1};
+    H.same_obj = H.owner;
+    H.scale.assign(H.n, 1.0);
+    H.corner.assign(a->points, a->points + 12);
+    if (!same) H.corner.insert(H.corner.end(), b->points, b->points + 12);
+    DeviceRegions D;
+    if (!D.upload(H)) return nan("");
+    DBuf<double> out((size_t)H.n * H.n);
+    if (!out.p) return nan("");
+    long long bad = -1;
+    int oa = 0, ob = same ? 0 : 1;
+    if (run_assembly(D, KIND_RAW, o, out.p, oa, ob, &bad, nullptr) != 0) return nan("");
+    double v = 0.0;
+    if (!cuda_ok(cudaMemcpyAsync(&v, out.p + ob, sizeof(double), cudaMemcpyDeviceToHost, stream()), "copy") ||
+        !sync("pair kernel"))
+        return nan("");
+    return v;
+}
+
+// ---------------------------------------------------------------------
+// C ABI: inductance.h / potential.h
+// ---------------------------------------------------------------------
+void inductance_options_default(InductanceOptions *options, int parallel_threads) {
+    if (options == NULL) return;
+    options->far_order = 4;
+    options->near_order = 10;
+    options->touching_order = 12;
+    options->self_order = 8;
+    options->near_factor = 0.5;
+    options->parallel_threads = parallel_threads;
+    options->direction_tolerance = 1.0e-10;
+}
+
+void inductance_init(InductanceMatrix *L) {
+    if (L) memset(L, 0, sizeof(*L));
+}
+
+void inductance_free(InductanceMatrix *L) {
+    if (!L) return;
+    free(L->data);
+    inductance_init(L);
+}
+
+void potential_options_default(PotentialOptions *options, int parallel_threads) {
+    if (options == NULL) return;
+    options->far_order = 4;
+    options->near_order = 10;
+    options->touching_order = 12;
+    options->self_order = 8;
+    options->near_factor = 0.5;
+    options->parallel_threads = parallel_threads;
+}
+
+void potential_init(PotentialMatrix *P) {
+    if (P) memset(P, 0, sizeof(*P));
+}
+
+void potential_free(PotentialMatrix *P) {
+    if (!P) return;
+    free(P->data);
+    potential_init(P);
+}
+
+}  // extern "C"
+
+namespace peec {
+
+// Assemble one matrix of `kind` into host memory `host_out` (n*n), or into
+// device memory `dev_out` if given.  Single entry when only_a >= 0.
+static int assemble(const Mesh *mesh, const DualMesh *dual, int kind, const AssemblyOptions &o, double *host_out,
+                    double *dev_out, int only_a, int only_b, long long *bad, PeecAssemblyStats *stats) {
+    *bad = -1;
+    HostRegions H;
+    if (!gather_regions(mesh, dual, kind, H)) return -1;
+    DeviceRegions D;
+    if (!D.upload(H)) return -1;
+    size_t nn = (size_t)H.n * H.n;
+    DBuf<double> tmp;
+    double *d = dev_out;
+    if (!d) {
+        if (!tmp.alloc(nn)) return -1;
+        d = tmp.p;
+    }
+    if (run_assembly(D, kind, o, d, only_a, only_b, bad, stats) != 0) return -1;
+    if (host_out) {
+        if (only_a >= 0) {
+            size_t idx = (size_t)(only_a < only_b ? only_a : only_b) * H.n + (only_a < only_b ? only_b : only_a);
+            if (!cuda_ok(cudaMemcpyAsync(host_out, d + idx, sizeof(double), cudaMemcpyDeviceToHost, stream()),
+                         "copy"))
+                return -1;
+        } else if (!cuda_ok(cudaMemcpyAsync(host_out, d, nn * sizeof(double), cudaMemcpyDeviceToHost, stream()),
+                            "copy")) {
+            return -1;
+        }
+        if (!sync("matrix download")) return -1;
+    }
+    return 0;
+}
+
+}  // namespace peec
+
+extern "C" {
+
+int inductance_compute_pair(const Mesh *mesh, const DualMesh *dual, size_t edge_a, size_t edge_b,
+                            const InductanceOptions *options, double *value) {
+    if (!mesh || !dual || !options || !value) return -1;
+    if (edge_a >= mesh->n_edges || edge_b >= mesh->n_edges) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, options->direction_tolerance};
+    // orthogonal edges: exact zero before any integral (inductance.c:272-277)
+    double dot = dot3(&mesh->edge_directions[3 * edge_a], &mesh->edge_directions[3 * edge_b]);
+    if (fabs(dot) < options->direction_tolerance) {
+        *value = 0.0;
+        return 0;
+    }
+    if (!orders_valid(o)) return -1;
+    long long bad;
+    double v = 0.0;
+    if (assemble(mesh, dual, KIND_INDUCTANCE, o, &v, nullptr, (int)edge_a, (int)edge_b, &bad, nullptr) != 0)
+        return -1;
+    *value = v;
+    return 0;
+}
+
+int inductance_compute_matrix(const Mesh *mesh, const DualMesh *dual, const InductanceOptions *options,
+                              InductanceMatrix *L) {
+    if (!mesh || !dual || !options || !L) return -1;
+    if (mesh->n_edges == 0) return -1;
+    inductance_init(L);
+    size_t ne = mesh->n_edges;
+    L->n = ne;
+    L->data = (double *)calloc(ne * ne, sizeof(double));
+    if (!L->data) {
+        fprintf(stderr, "ERROR: cannot allocate inductance matrix.\n");
+        return -1;
+    }
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, options->direction_tolerance};
+    long long bad = -1;
+    int status = orders_valid(o) ? assemble(mesh, dual, KIND_INDUCTANCE, o, L->data, nullptr, -1, -1, &bad, nullptr)
+                                 : -1;
+    if (status != 0) {
+        if (bad >= 0)
+            fprintf(stderr, "\nERROR: inductance calculation failed for edges %zu, %zu.\n", (size_t)(bad / ne),
+                    (size_t)(bad % ne));
+        else
+            fprintf(stderr, "\nERROR: inductance calculation failed.\n");
+        inductance_free(L);
+        return -1;
+    }
+    return 0;
+}
+
+int potential_compute_pair(const Mesh *mesh, const DualMesh *dual, size_t node_i, size_t node_j,
+                           const PotentialOptions *options, double *value) {
+    if (!mesh || !dual || !options || !value) return -1;
+    if (node_i >= mesh->n_nodes || node_j >= mesh->n_nodes) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, 0.0};
+    if (!orders_valid(o)) return -1;
+    long long bad;
+    double v = 0.0;
+    if (assemble(mesh, dual, KIND_POTENTIAL, o, &v, nullptr, (int)node_i, (int)node_j, &bad, nullptr) != 0)
+        return -1;
+    *value = v;
+    return 0;
+}
+
+int potential_compute_matrix(const Mesh *mesh, const DualMesh *dual, const PotentialOptions *options,
+                             PotentialMatrix *P) {
+    if (!mesh || !dual || !options || !P) return -1;
+    if (mesh->n_nodes == 0) return -1;
+    potential_init(P);
+    size_t nv = mesh->n_nodes;
+    P->n = nv;
+    P->data = (double *)calloc(nv * nv, sizeof(double));
+    if (!P->data) {
+        fprintf(stderr, "ERROR: cannot allocate potential matrix.\n");
+        return -1;
+    }
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, 0.0};
+    long long bad = -1;
+    int status =
+        orders_valid(o) ? assemble(mesh, dual, KIND_POTENTIAL, o, P->data, nullptr, -1, -1, &bad, nullptr) : -1;
+    if (status != 0) {
+        if (bad >= 0)
+            fprintf(stderr, "\nERROR: potential calculation failed for nodes %zu, %zu.\n", (size_t)(bad / nv),
+                    (size_t)(bad % nv));
+        else
+            fprintf(stderr, "\nERROR: potential calculation failed.\n");
+        potential_free(P);
+        return -1;
+    }
+    return 0;
+}
+
+// Extension: assemble straight into device memory (n*n doubles).
+int peec_gb300_inductance_device(const Mesh *mesh, const DualMesh *dual, const InductanceOptions *options,
+                                 double *d_out, PeecAssemblyStats *stats) {
+    if (!mesh || !dual || !options || !d_out || mesh->n_edges == 0) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, options->direction_tolerance};
+    if (!orders_valid(o)) return -1;
+    long long bad;
+    return assemble(mesh, dual, KIND_INDUCTANCE, o, nullptr, d_out, -1, -1, &bad, stats);
+}
+
+int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual, const PotentialOptions *options,
+                                double *d_out, PeecAssemblyStats *stats) {
+    if (!mesh || !dual || !options || !d_out || mesh->n_nodes == 0) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, 0.0};
+    if (!orders_valid(o)) return -1;
+    long long bad;
+    return assemble(mesh, dual, KIND_POTENTIAL, o, nullptr, d_out, -1, -1, &bad, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,982 @@
+// Dense real and complex LU with partial pivoting on sm_103a (FP64).
+//
+// Reference path (paths inside the reference project):
+//   src/math/lu.c:194-479          real factorisation
+//   src/math/lu.c:494-724          pivots, forward/backward substitution, solves
+//   src/math/complex_lu.c:208-550  equilibration + complex factorisation
+//   src/math/complex_lu.c:598-840  complex solves
+//
+// Layout: the device keeps the matrix row-major, exactly as the host ABI
+// (data[i*n+j], complex interleaved {re, im}), so the packed L\U factor is
+// downloaded without any transpose.  Blocked right-looking algorithm with
+// panel width NB:
+//   k_panel     one CTA factors rows k0..n-1 of columns k0..k0+NB-1 column by
+//               column: argmax (first maximum wins, as the reference), row
+//               swap inside the panel, multipliers, rank-1 update of the
+//               remaining panel columns;
+//   k_laswp     replays the panel's row swaps on the columns left and right
+//               of the panel;
+//   k_trsm      U12 = L11^-1 A12 (one thread per column, L11 in shared memory);
+//   k_gemm_*    A22 -= L21 U12, register-tiled FP64 (complex: 4 real FMAs
+//               per complex multiply-add).
+// A device status word stops every later kernel after a singular pivot, so
+// the host synchronises once per factorisation.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <list>
+#include <mutex>
+#include <vector>
+
+#include "../../include/complex_lu.h"
+#include "../../include/lu.h"
+#include "../../include/peec_gb300.h"
+#include "common.cuh"
+
+namespace peec {
+
+static const int NB = 32;  // panel width
+
+struct cplx {
+    double re, im;
+};
+
+// ---- scalar traits --------------------------------------------------
+__device__ __forceinline__ double mag(double v) { return fabs(v); }
+__device__ __forceinline__ double mag(cplx v) { return hypot(v.re, v.im); }
+__device__ __forceinline__ double divide(double a, double b) { return a / b; }
+// complex_lu.c:168-190: (a conj(b)) / |b|^2 without scaling
+__device__ __forceinline__ cplx divide(cplx a, cplx b) {
+    double den = b.re * b.re + b.im * b.im;
+    cplx z;
+    z.re = (a.re * b.re + a.im * b.im) / den;
+    z.im = (a.im * b.re - a.re * b.im) / den;
+    return z;
+}
+// c - m*u
+__device__ __forceinline__ double msub(double c, double m, double u) { return fma(-m, u, c); }
+__device__ __forceinline__ cplx msub(cplx c, cplx m, cplx u) {
+    c.re = fma(-m.re, u.re, c.re);
+    c.re = fma(m.im, u.im, c.re);
+    c.im = fma(-m.re, u.im, c.im);
+    c.im = fma(-m.im, u.re, c.im);
+    return c;
+}
+
+struct Status {
+    int code;    // 0 ok, 2 singular / invalid pivot
+    int column;  // failing column
+    double value;
+};
+
+// ---- scale ----------------------------------------------------------
+// max over entries of |a| ignoring NaN (the reference's `if (v > max)` never
+// takes a NaN), as IEEE bits: non-negative doubles order like integers.
+template <class T>
+__global__ void k_max_mag(const T *a, size_t count, unsigned long long *out) {
+    double best = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x) {
+        double m = mag(a[t]);
+        if (m > best) best = m;
+    }
+    for (int s = 16; s > 0; s >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, s));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+// ---- panel ----------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(1024) k_panel(T *a, int n, int k0, int kb, double limit, long long *piv,
+                                                Status *st) {
+    __shared__ double s_val[32];
+    __shared__ int s_idx[32];
+    __shared__ int s_pivot;
+    __shared__ int s_fail;
+    __shared__ T s_row[NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nthr = blockDim.x;
+    if (st->code != 0) return;
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk;
+        // argmax |a[i][k]|, i >= k; ties -> lowest row; NaN below the diagonal
+        // never wins, a NaN diagonal is kept (and rejected below)
+        double best = -1.0;
+        int bi = n;
+        for (int i = k + tid; i < n; i += nthr) {
+            double m = mag(a[(size_t)i * n + k]);
+            if (i == k && isnan(m)) m = INFINITY;  // forces rejection
+            if (isnan(m)) continue;
+            if (m > best || (m == best && i < bi)) {
+                best = m;
+                bi = i;
+            }
+        }
+        for (int s = 16; s > 0; s >>= 1) {
+            double ov = __shfl_xor_sync(0xffffffffu, best, s);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, s);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_val[warp] = best;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int nw = nthr >> 5;
+            best = lane < nw ? s_val[lane] : -1.0;
+            bi = lane < nw ? s_idx[lane] : n;
+            for (int s = 16; s > 0; s >>= 1) {
+                double ov = __shfl_xor_sync(0xffffffffu, best, s);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, s);
+                if (ov > best || (ov == best && oi < bi)) {
+                    best = ov;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                double dm = mag(a[(size_t)k * n + k]);
+                double pv = isnan(dm) ? dm : best;
+                s_fail = 0;
+                if (!isfinite(pv) || pv <= limit || bi >= n) {
+                    s_fail = 1;
+                    st->code = 2;
+                    st->column = k;
+                    st->value = pv;
+                } else {
+                    piv[k] = bi;
+                }
+                s_pivot = bi;
+            }
+        }
+        __syncthreads();
+        if (s_fail) return;
+        const int p = s_pivot;
+        if (p != k) {
+            for (int j = k0 + tid; j < k0 + kb; j += nthr) {
+                T t = a[(size_t)k * n + j];
+                a[(size_t)k * n + j] = a[(size_t)p * n + j];
+                a[(size_t)p * n + j] = t;
+            }
+        }
+        __syncthreads();
+        if (k + 1 >= n) break;
+        for (int j = kk + tid; j < kb; j += nthr) s_row[j] = a[(size_t)k * n + k0 + j];
+        __syncthreads();
+        const T pivot = s_row[kk];
+        for (int i = k + 1 + tid; i < n; i += nthr) {
+            T *row = a + (size_t)i * n + k0;
+            T m = divide(row[kk], pivot);
+            row[kk] = m;
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], m, s_row[j]);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- row swaps outside the panel -------------------------------------
+template <class T>
+__global__ void k_laswp(T *a, int n, int k0, int kb, const long long *piv, const Status *st) {
+    if (st->code != 0) return;
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || (j >= k0 && j < k0 + kb)) return;
+    for (int kk = 0; kk < kb; ++kk) {
+        int k = k0 + kk;
+        int p = (int)piv[k];
+        if (p != k) {
+            T t = a[(size_t)k * n + j];
+            a[(size_t)k * n + j] = a[(size_t)p * n + j];
+            a[(size_t)p * n + j] = t;
+        }
+    }
+}
+
+// ---- U12 = L11^-1 A12 ------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, const Status *st) {
+    __shared__ T L[NB][NB];
+    if (st->code != 0) return;
+    for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+        int i = t / kb, m = t % kb;
+        L[i][m] = a[(size_t)(k0 + i) * n + k0 + m];
+    }
+    __syncthreads();
+    int j = k0 + kb + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    T x[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        if (i < kb) {
+            T v = a[(size_t)(k0 + i) * n + j];
+#pragma unroll
+            for (int m = 0; m < NB; ++m)
+                if (m < i) v = msub(v, L[i][m], x[m]);
+            x[i] = v;
+            a[(size_t)(k0 + i) * n + j] = v;
+        }
+    }
+}
+
+// ---- A22 -= L21 U12 --------------------------------------------------
+// Real: 64x64 C tile per 256-thread CTA, 4x4 per thread.
+__global__ void __launch_bounds__(256) k_gemm_real(double *a, int n, int k0, int kb, const Status *st) {
+    __shared__ double As[NB][64 + 1];
+    __shared__ double Bs[NB][64];
+    if (st->code != 0) return;
+    const int r0 = k0 + kb + blockIdx.y * 64, c0 = k0 + kb + blockIdx.x * 64;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    for (int t = threadIdx.x; t < 64 * NB; t += 256) {
+        int r = t / NB, m = t % NB;  // A tile: rows r0.., cols k0..
+        As[m][r] = (r0 + r < n && m < kb) ? a[(size_t)(r0 + r) * n + k0 + m] : 0.0;
+        int mm = t / 64, c = t % 64;  // B tile: rows k0.., cols c0..
+        Bs[mm][c] = (c0 + c < n && mm < kb) ? a[(size_t)(k0 + mm) * n + c0 + c] : 0.0;
+    }
+    __syncthreads();
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            acc[i][j] = (r < n && c < n) ? a[(size_t)r * n + c] : 0.0;
+        }
+#pragma unroll 8
+    for (int m = 0; m < NB; ++m) {
+        double av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = As[m][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = Bs[m][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(-av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            if (r < n && c < n) a[(size_t)r * n + c] = acc[i][j];
+        }
+}
+
+// Complex: 32x64 C tile per 256-thread CTA, 2x4 per thread.
+__global__ void __launch_bounds__(256) k_gemm_cplx(cplx *a, int n, int k0, int kb, const Status *st) {
+    __shared__ cplx As[NB][32 + 1];
+    __shared__ cplx Bs[NB][64];
+    if (st->code != 0) return;
+    const int r0 = k0 + kb + blockIdx.y * 32, c0 = k0 + kb + blockIdx.x * 64;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const cplx z = {0.0, 0.0};
+    for (int t = threadIdx.x; t < 32 * NB; t += 256) {
+        int r = t / NB, m = t % NB;
+        As[m][r] = (r0 + r < n && m < kb) ? a[(size_t)(r0 + r) * n + k0 + m] : z;
+    }
+    for (int t = threadIdx.x; t < 64 * NB; t += 256) {
+        int mm = t / 64, c = t % 64;
+        Bs[mm][c] = (c0 + c < n && mm < kb) ? a[(size_t)(k0 + mm) * n + c0 + c] : z;
+    }
+    __syncthreads();
+    cplx acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            acc[i][j] = (r < n && c < n) ? a[(size_t)r * n + c] : z;
+        }
+#pragma unroll 4
+    for (int m = 0; m < NB; ++m) {
+        cplx av[2], bv[4];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) av[i] = As[m][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = Bs[m][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = msub(acc[i][j], av[i], bv[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            if (r < n && c < n) a[(size_t)r * n + c] = acc[i][j];
+        }
+}
+
+// ---- final diagonal check (lu.c:455-476) -----------------------------
+template <class T>
+__global__ void k_check_diag(const T *a, int n, double limit, Status *st) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || st->code != 0) return;
+    double m = mag(a[(size_t)i * n + i]);
+    if (!isfinite(m) || m <= limit) {
+        if (atomicCAS(&st->code, 0, 3) == 0) {
+            st->column = i;
+            st->value = m;
+        }
+    }
+}
+
+// ---- complex equilibration (complex_lu.c:275-302) ---------------------
+// row scales: one warp per row, max of hypot; non-finite -> status 4,
+// zero row -> status 5
+__global__ void k_row_scale(const cplx *in, cplx *out, int n, double *row_scale, Status *st) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const cplx *row = in + (size_t)warp * n;
+    double s = 0.0;
+    int bad = 0;
+    for (int j = lane; j < n; j += 32) {
+        double m = hypot(row[j].re, row[j].im);
+        if (!isfinite(m)) bad = 1;
+        s = fmax(s, m);
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        s = fmax(s, __shfl_xor_sync(0xffffffffu, s, d));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, d);
+    }
+    if (bad || s == 0.0) {
+        if (lane == 0) atomicCAS(&st->code, 0, bad ? 4 : 5);
+        return;
+    }
+    if (lane == 0) row_scale[warp] = s;
+    cplx *orow = out + (size_t)warp * n;
+    for (int j = lane; j < n; j += 32) {
+        cplx v = row[j];
+        orow[j] = cplx{v.re / s, v.im / s};
+    }
+}
+
+// column scales on the row-scaled matrix: one thread per column
+__global__ void k_col_scale(cplx *a, int n, double *col_scale, Status *st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || st->code != 0) return;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = fmax(s, hypot(a[(size_t)i * n + j].re, a[(size_t)i * n + j].im));
+    if (s == 0.0) {
+        atomicCAS(&st->code, 0, 5);
+        return;
+    }
+    col_scale[j] = s;
+    for (int i = 0; i < n; ++i) {
+        cplx v = a[(size_t)i * n + j];
+        a[(size_t)i * n + j] = cplx{v.re / s, v.im / s};
+    }
+}
+
+// ---- solves ------------------------------------------------------------
+// permutation of the sequential swaps (lu.c:494-510), one thread in shared
+// memory: perm[i] = source row of position i after all swaps.
+__global__ void k_perm(const long long *piv, int n, int *perm) {
+    extern __shared__ int sp[];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n; ++k) {
+            int p = (int)piv[k];
+            if (p != k) {
+                int t = sp[k];
+                sp[k] = sp[p];
+                sp[p] = t;
+            }
+        }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
+}
+
+// x[r][i] = b[r][perm[i]] (real); complex also divides by row_scale first
+template <class T>
+__global__ void k_gather(const T *b, T *x, const int *perm, const double *row_scale, int n, int nrhs) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * nrhs) return;
+    int r = (int)(t / n), i = (int)(t % n);
+    int src = perm[i];
+    T v = b[(size_t)r * n + src];
+    if constexpr (sizeof(T) == sizeof(cplx)) {
+        cplx c = *reinterpret_cast<cplx *>(&v);
+        double s = row_scale[src];
+        c.re = c.re / s;
+        c.im = c.im / s;
+        v = *reinterpret_cast<T *>(&c);
+    }
+    x[(size_t)r * n + i] = v;
+}
+
+// diagonal block of the forward (unit L) or backward (U) substitution:
+// one warp per right-hand side, rows [k0, k0+kb); lane owns rows k0+lane
+__device__ __forceinline__ double mulv(double l, double x) { return l * x; }
+
+template <class T, bool LOWER>
+__global__ void k_trsv_diag(const T *a, int n, int k0, int kb, T *x, int nrhs) {
+    int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (r >= nrhs) return;
+    T *xr = x + (size_t)r * n;
+    T v;
+    if (lane < kb) v = xr[k0 + lane];
+    if (LOWER) {
+        for (int m = 0; m < kb; ++m) {
+            T xm;
+            double *pv = reinterpret_cast<double *>(&v);
+            double *pm = reinterpret_cast<double *>(&xm);
+#pragma unroll
+            for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pm[w] = __shfl_sync(0xffffffffu, pv[w], m);
+            if (lane > m && lane < kb) v = msub(v, a[(size_t)(k0 + lane) * n + k0 + m], xm);
+        }
+    } else {
+        for (int m = kb - 1; m >= 0; --m) {
+            if (lane == m) v = divide(v, a[(size_t)(k0 + m) * n + k0 + m]);
+            T xm;
+            double *pv = reinterpret_cast<double *>(&v);
+            double *pm = reinterpret_cast<double *>(&xm);
+#pragma unroll
+            for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pm[w] = __shfl_sync(0xffffffffu, pv[w], m);
+            if (lane < m) v = msub(v, a[(size_t)(k0 + lane) * n + k0 + m], xm);
+        }
+    }
+    if (lane < kb) xr[k0 + lane] = v;
+}
+
+// off-diagonal update: rows outside the block, x[i] -= sum_m A[i][k0+m] x[k0+m];
+// one warp per (row, rhs), lanes over m
+template <class T, bool LOWER>
+__global__ void k_trsv_update(const T *a, int n, int k0, int kb, T *x, int nrhs) {
+    size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int rows = LOWER ? n - (k0 + kb) : k0;
+    if (g >= (size_t)rows * nrhs) return;
+    int r = (int)(g / rows), i = (int)(g % rows) + (LOWER ? k0 + kb : 0);
+    T *xr = x + (size_t)r * n;
+    T acc;
+    memset(&acc, 0, sizeof(T));
+    if (lane < kb) {
+        T zero;
+        memset(&zero, 0, sizeof(T));
+        acc = msub(zero, a[(size_t)i * n + k0 + lane], xr[k0 + lane]);  // -A x
+    }
+    double *pa = reinterpret_cast<double *>(&acc);
+#pragma unroll
+    for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pa[w] = warp_sum(pa[w]);
+    if (lane == 0) {
+        T v = xr[i];
+        double *pv = reinterpret_cast<double *>(&v);
+#pragma unroll
+        for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pv[w] += pa[w];
+        xr[i] = v;
+    }
+}
+
+__global__ void k_col_unscale(cplx *x, const double *col_scale, int n, int nrhs) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * nrhs) return;
+    int i = (int)(t % n);
+    double s = col_scale[i];
+    x[t].re = x[t].re / s;
+    x[t].im = x[t].im / s;
+}
+
+// ---------------------------------------------------------------------
+// registry: device copies of factorisations, keyed by the host data
+// pointer and checked by a fingerprint before reuse
+// ---------------------------------------------------------------------
+struct Resident {
+    const void *host_data = nullptr;
+    size_t n = 0;
+    bool complex_ = false;
+    void *d_lu = nullptr;
+    long long *d_piv = nullptr;
+    int *d_perm = nullptr;
+    double *d_row = nullptr, *d_col = nullptr;
+    unsigned long long fingerprint = 0;
+    size_t bytes = 0;
+};
+
+static std::mutex g_reg_mu;
+static std::list<Resident> g_reg;
+static size_t g_reg_bytes = 0;
+static const size_t kRegLimit = (size_t)96 << 30;  // device bytes kept for reuse
+
+static unsigned long long mix(unsigned long long h, unsigned long long v) {
+    h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+// pivots, scales, the diagonal and a strided sample of the packed factor
+static unsigned long long fingerprint(const void *data, const size_t *piv, const double *rs, const double *cs,
+                                      size_t n, bool cx) {
+    unsigned long long h = n;
+    const unsigned long long *d = (const unsigned long long *)data;
+    size_t w = cx ? 2 : 1, total = n * n * w;
+    for (size_t k = 0; k < n; ++k) {
+        h = mix(h, piv[k]);
+        h = mix(h, d[(k * n + k) * w]);
+        if (cx) h = mix(h, d[(k * n + k) * w + 1]);
+        if (rs) h = mix(h, ((const unsigned long long *)rs)[k]);
+        if (cs) h = mix(h, ((const unsigned long long *)cs)[k]);
+    }
+    size_t step = total / 4093 + 1;
+    for (size_t t = 0; t < total; t += step) h = mix(h, d[t]);
+    return h;
+}
+
+static void release(Resident &r) {
+    dfree(r.d_lu);
+    dfree(r.d_piv);
+    dfree(r.d_perm);
+    dfree(r.d_row);
+    dfree(r.d_col);
+}
+
+static void registry_drop(const void *host_data) {
+    std::lock_guard<std::mutex> g(g_reg_mu);
+    for (auto it = g_reg.begin(); it != g_reg.end(); ++it)
+        if (it->host_data == host_data) {
+            g_reg_bytes -= it->bytes;
+            release(*it);
+            g_reg.erase(it);
+            return;
+        }
+}
+
+static void registry_put(Resident r) {
+    registry_drop(r.host_data);
+    std::lock_guard<std::mutex> g(g_reg_mu);
+    while (!g_reg.empty() && g_reg_bytes + r.bytes > kRegLimit) {
+        g_reg_bytes -= g_reg.back().bytes;
+        release(g_reg.back());
+        g_reg.pop_back();
+    }
+    g_reg_bytes += r.bytes;
+    g_reg.push_front(r);
+}
+
+static bool registry_get(const void *host_data, size_t n, bool cx, unsigned long long fp, Resident &out) {
+    std::lock_guard<std::mutex> g(g_reg_mu);
+    for (auto it = g_reg.begin(); it != g_reg.end(); ++it)
+        if (it->host_data == host_data) {
+            if (it->n != n || it->complex_ != cx || it->fingerprint != fp) return false;
+            g_reg.splice(g_reg.begin(), g_reg, it);
+            out = *it;
+            return true;
+        }
+    return false;
+}
+
+// ---------------------------------------------------------------------
+// factorisation driver
+// ---------------------------------------------------------------------
+template <class T>
+static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status *d_st) {
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        int kb = std::min(NB, n - k0);
+        PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
+        PEEC_LAUNCH(k_laswp<T>, (n + 255) / 256, 256, 0, d_a, n, k0, kb, d_piv, d_st);
+        int rest = n - (k0 + kb);
+        if (rest > 0) {
+            PEEC_LAUNCH(k_trsm<T>, (rest + 255) / 256, 256, 0, d_a, n, k0, kb, d_st);
+            if constexpr (sizeof(T) == sizeof(double)) {
+                dim3 g((rest + 63) / 64, (rest + 63) / 64);
+                PEEC_LAUNCH(k_gemm_real, g, 256, 0, (double *)d_a, n, k0, kb, d_st);
+            } else {
+                dim3 g((rest + 63) / 64, (rest + 31) / 32);
+                PEEC_LAUNCH(k_gemm_cplx, g, 256, 0, (cplx *)d_a, n, k0, kb, d_st);
+            }
+        }
+    }
+    PEEC_LAUNCH(k_check_diag<T>, (n + 255) / 256, 256, 0, d_a, n, limit, d_st);
+    return launch_ok("LU kernels");
+}
+
+template <class T>
+static bool solve_device(const T *d_lu, const int *d_perm, const double *d_row, const double *d_col, int n,
+                         const T *d_b, T *d_x, int nrhs) {
+    size_t tot = (size_t)n * nrhs;
+    PEEC_LAUNCH(k_gather<T>, (unsigned)((tot + 255) / 256), 256, 0, d_b, d_x, d_perm, d_row, n, nrhs);
+    int wpb = 8;
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        int kb = std::min(32, n - k0);
+        PEEC_LAUNCH((k_trsv_diag<T, true>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, d_lu, n, k0, kb, d_x, nrhs);
+        size_t rows = (size_t)(n - k0 - kb) * nrhs;
+        if (rows)
+            PEEC_LAUNCH((k_trsv_update<T, true>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, d_lu, n, k0, kb,
+                        d_x, nrhs);
+    }
+    int last = ((n - 1) / 32) * 32;
+    for (int k0 = last; k0 >= 0; k0 -= 32) {
+        int kb = std::min(32, n - k0);
+        PEEC_LAUNCH((k_trsv_diag<T, false>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, d_lu, n, k0, kb, d_x, nrhs);
+        size_t rows = (size_t)k0 * nrhs;
+        if (rows)
+            PEEC_LAUNCH((k_trsv_update<T, false>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, d_lu, n, k0, kb,
+                        d_x, nrhs);
+    }
+    if constexpr (sizeof(T) == sizeof(cplx))
+        PEEC_LAUNCH(k_col_unscale, (unsigned)((tot + 255) / 256), 256, 0, (cplx *)d_x, d_col, n, nrhs);
+    return launch_ok("LU solve kernels");
+}
+
+}  // namespace peec
+
+using namespace peec;
+
+// =====================================================================
+// C ABI: lu.h
+// =====================================================================
+extern "C" {
+
+void lu_options_default(LUOptions *options, int parallel_threads) {
+    if (!options) return;
+    options->parallel_threads = parallel_threads;
+    options->pivot_tolerance = 1.0e-14;
+    options->parallel_threshold = 64;
+}
+
+void lu_init(LUFactorization *lu) {
+    if (lu) memset(lu, 0, sizeof(*lu));
+}
+
+void lu_free(LUFactorization *lu) {
+    if (!lu) return;
+    if (lu->data) registry_drop(lu->data);
+    free(lu->data);
+    free(lu->pivots);
+    lu_init(lu);
+}
+
+}  // extern "C"
+
+namespace peec {
+
+// Shared host driver for both factorisations.  On success the factor stays
+// resident on the device (registry) for the solves.
+template <class T>
+static int factorize_common(const T *input, size_t n, double pivot_tolerance, bool cx, T *host_lu, size_t *host_piv,
+                            size_t *swap_count, double *matrix_scale, double *row_scale, double *col_scale) {
+    int ni = (int)n;
+    size_t nn = n * n;
+    Resident r;
+    r.n = n;
+    r.complex_ = cx;
+    r.bytes = nn * sizeof(T) + n * (sizeof(long long) + sizeof(int) + (cx ? 2 * sizeof(double) : 0));
+    r.d_lu = dalloc(nn * sizeof(T));
+    r.d_piv = (long long *)dalloc(n * sizeof(long long));
+    r.d_perm = (int *)dalloc(n * sizeof(int));
+    if (cx) {
+        r.d_row = (double *)dalloc(n * sizeof(double));
+        r.d_col = (double *)dalloc(n * sizeof(double));
+    }
+    DBuf<Status> st(1);
+    DBuf<unsigned long long> mx(1);
+    DBuf<T> staging;
+    bool ok = r.d_lu && r.d_piv && r.d_perm && st.p && mx.p && (!cx || (r.d_row && r.d_col));
+    if (ok && cx) ok = staging.alloc(nn);
+    if (!ok) {
+        release(r);
+        return -1;
+    }
+    T *d_a = (T *)r.d_lu;
+    cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
+    cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
+    if (!cuda_ok(cudaMemcpyAsync(cx ? staging.p : d_a, input, nn * sizeof(T), cudaMemcpyHostToDevice, stream()),
+                 "LU upload")) {
+        release(r);
+        return -1;
+    }
+    if (cx) {
+        // complex_lu.c:275-302: row scales, then column scales of the row-scaled matrix
+        PEEC_LAUNCH(k_row_scale, (unsigned)(((size_t)ni * 32 + 255) / 256), 256, 0, (const cplx *)staging.p,
+                    (cplx *)d_a, ni, r.d_row, st.p);
+        PEEC_LAUNCH(k_col_scale, (ni + 127) / 128, 128, 0, (cplx *)d_a, ni, r.d_col, st.p);
+    }
+    PEEC_LAUNCH(k_max_mag<T>, 152 * 8, 256, 0, d_a, nn, mx.p);
+    unsigned long long bits = 0;
+    Status hs;
+    cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+    if (!sync("LU scale")) {
+        release(r);
+        return -1;
+    }
+    staging.release();
+    if (hs.code != 0) {  // zero or non-finite row / column of the complex input
+        release(r);
+        return -2;
+    }
+    double scale;
+    memcpy(&scale, &bits, sizeof(scale));
+    *matrix_scale = scale;
+    if (!isfinite(scale) || scale <= 0.0) {
+        fprintf(stderr, cx ? "ERROR: complex LU input matrix is invalid or zero.\n"
+                           : "ERROR: LU input matrix is zero or contains invalid values.\n");
+        release(r);
+        return -2;
+    }
+    double limit = pivot_tolerance * scale;
+    if (!factor_device<T>(d_a, ni, limit, r.d_piv, st.p)) {
+        release(r);
+        return -1;
+    }
+    size_t perm_smem = n * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, ni, r.d_perm);
+    std::vector<long long> piv(n);
+    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+    bool copied = cuda_ok(cudaMemcpyAsync(host_lu, d_a, nn * sizeof(T), cudaMemcpyDeviceToHost, stream()), "LU download") &&
+                  cuda_ok(cudaMemcpyAsync(piv.data(), r.d_piv, n * sizeof(long long), cudaMemcpyDeviceToHost, stream()),
+                          "pivot download");
+    if (cx && copied)
+        copied = cuda_ok(cudaMemcpyAsync(row_scale, r.d_row, n * sizeof(double), cudaMemcpyDeviceToHost, stream()), "scale") &&
+                 cuda_ok(cudaMemcpyAsync(col_scale, r.d_col, n * sizeof(double), cudaMemcpyDeviceToHost, stream()), "scale");
+    if (!sync("LU factorisation") || !copied) {
+        release(r);
+        return -1;
+    }
+    size_t done = hs.code == 0 ? n : (size_t)hs.column;
+    size_t swaps = 0;
+    for (size_t k = 0; k < n; ++k) {
+        host_piv[k] = k < done ? (size_t)piv[k] : k;
+        if (k < done && host_piv[k] != k) ++swaps;
+    }
+    *swap_count = swaps;
+    if (hs.code != 0) {
+        if (hs.code == 2)
+            fprintf(stderr, cx ? "ERROR: complex LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n"
+                               : "ERROR: LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n",
+                    hs.column, hs.value);
+        else
+            fprintf(stderr, cx ? "ERROR: invalid complex U diagonal at [%d,%d], |Uii| = %.9e.\n"
+                               : "ERROR: invalid diagonal U[%d,%d] = %.9e.\n",
+                    hs.column, hs.column, hs.value);
+        release(r);
+        return -2;
+    }
+    r.host_data = host_lu;
+    r.fingerprint = fingerprint(host_lu, host_piv, cx ? row_scale : nullptr, cx ? col_scale : nullptr, n, cx);
+    registry_put(r);
+    return 0;
+}
+
+// Device copy of a host factorisation: the registry's if the fingerprint
+// matches, else uploaded now (and registered).
+template <class T>
+static bool resident_for(const T *data, const size_t *pivots, const double *rs, const double *cs, size_t n, bool cx,
+                         Resident &out) {
+    unsigned long long fp = fingerprint(data, pivots, rs, cs, n, cx);
+    if (registry_get(data, n, cx, fp, out)) return true;
+    Resident r;
+    r.host_data = data;
+    r.n = n;
+    r.complex_ = cx;
+    r.fingerprint = fp;
+    r.bytes = n * n * sizeof(T) + n * (sizeof(long long) + sizeof(int) + (cx ? 2 * sizeof(double) : 0));
+    r.d_lu = dalloc(n * n * sizeof(T));
+    r.d_piv = (long long *)dalloc(n * sizeof(long long));
+    r.d_perm = (int *)dalloc(n * sizeof(int));
+    if (cx) {
+        r.d_row = (double *)dalloc(n * sizeof(double));
+        r.d_col = (double *)dalloc(n * sizeof(double));
+    }
+    if (!r.d_lu || !r.d_piv || !r.d_perm || (cx && (!r.d_row || !r.d_col))) {
+        release(r);
+        return false;
+    }
+    std::vector<long long> piv(n);
+    for (size_t k = 0; k < n; ++k) {
+        if (pivots[k] >= n) {
+            release(r);
+            return false;
+        }
+        piv[k] = (long long)pivots[k];
+    }
+    bool ok = cuda_ok(cudaMemcpyAsync(r.d_lu, data, n * n * sizeof(T), cudaMemcpyHostToDevice, stream()), "factor upload") &&
+              cuda_ok(cudaMemcpyAsync(r.d_piv, piv.data(), n * sizeof(long long), cudaMemcpyHostToDevice, stream()),
+                      "pivot upload");
+    if (cx && ok)
+        ok = cuda_ok(cudaMemcpyAsync(r.d_row, rs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload") &&
+             cuda_ok(cudaMemcpyAsync(r.d_col, cs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload");
+    size_t perm_smem = n * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    if (ok) PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, (int)n, r.d_perm);
+    if (!ok || !sync("factor upload")) {
+        release(r);
+        return false;
+    }
+    registry_put(r);
+    out = r;
+    return true;
+}
+
+template <class T>
+static int solve_common(const T *data, const size_t *pivots, const double *rs, const double *cs, size_t n, bool cx,
+                        const T *B, T *X, size_t nrhs) {
+    if (n > (size_t)0x7fffffff || nrhs > (size_t)0x7fffffff) return -1;
+    Resident r;
+    if (!resident_for<T>(data, pivots, rs, cs, n, cx, r)) return -1;
+    size_t tot = n * nrhs;
+    DBuf<T> db(tot), dx(tot);
+    if (!db.p || !dx.p) return -1;
+    if (!db.upload(B, tot)) return -1;
+    if (!solve_device<T>((const T *)r.d_lu, r.d_perm, r.d_row, r.d_col, (int)n, db.p, dx.p, (int)nrhs)) return -1;
+    if (!dx.download(X, tot) || !sync("LU solve")) return -1;
+    for (size_t t = 0; t < tot; ++t) {
+        const double *v = (const double *)&X[t];
+        for (size_t w = 0; w < sizeof(T) / 8; ++w)
+            if (!isfinite(v[w])) return -1;  // zero / non-finite diagonal reached
+    }
+    return 0;
+}
+
+}  // namespace peec
+
+extern "C" {
+
+int lu_factorize(const double *input, size_t n, const LUOptions *options, LUFactorization *lu) {
+    if (!input || !options || !lu || n == 0) return -1;
+    if (options->parallel_threads < 1) return -1;
+    if (n > (size_t)0x7fffffff || n > SIZE_MAX / n || n * n > SIZE_MAX / sizeof(double)) {
+        fprintf(stderr, "ERROR: LU matrix size overflow.\n");
+        return -1;
+    }
+    lu_init(lu);
+    lu->n = n;
+    lu->data = (double *)malloc(n * n * sizeof(double));
+    lu->pivots = (size_t *)malloc(n * sizeof(size_t));
+    if (!lu->data || !lu->pivots) {
+        fprintf(stderr, "ERROR: cannot allocate LU factorization.\n");
+        lu_free(lu);
+        return -1;
+    }
+    int s = factorize_common<double>(input, n, options->pivot_tolerance, false, lu->data, lu->pivots,
+                                     &lu->swap_count, &lu->matrix_scale, nullptr, nullptr);
+    if (s == -1 || (s == -2 && !isfinite(lu->matrix_scale)) || (s == -2 && lu->matrix_scale <= 0.0)) {
+        lu_free(lu);
+        return s;
+    }
+    lu->factorized = s == 0;
+    return s;
+}
+
+int lu_solve(const LUFactorization *lu, const double *b, double *x) {
+    if (!lu || !b || !x || !lu->data || !lu->pivots || !lu->factorized) return -1;
+    return solve_common<double>(lu->data, lu->pivots, nullptr, nullptr, lu->n, false, b, x, 1);
+}
+
+int lu_solve_multiple(const LUFactorization *lu, const double *B, double *X, size_t rhs_count, int parallel_threads) {
+    if (!lu || !B || !X || rhs_count == 0 || parallel_threads < 1 || !lu->factorized) return -1;
+    if (!lu->data || !lu->pivots) return -1;
+    return solve_common<double>(lu->data, lu->pivots, nullptr, nullptr, lu->n, false, B, X, rhs_count);
+}
+
+double lu_determinant(const LUFactorization *lu) {
+    if (!lu || !lu->data || !lu->factorized) return NAN;
+    double det = (lu->swap_count % 2 == 0) ? 1.0 : -1.0;
+    for (size_t i = 0; i < lu->n; ++i) det *= lu->data[i * lu->n + i];
+    return det;
+}
+
+void lu_print_info(const LUFactorization *lu) {
+    if (!lu) return;
+    printf("\n========================================\n");
+    printf("LU FACTORIZATION (GPU)\n");
+    printf("========================================\n");
+    printf("Size         : %zu x %zu\n", lu->n, lu->n);
+    printf("Swap count   : %zu\n", lu->swap_count);
+    printf("Matrix scale : %.9e\n", lu->matrix_scale);
+    printf("Factorized   : %s\n", lu->factorized ? "yes" : "no");
+    if (lu->data && lu->n > 0)
+        printf("LU memory    : %.3f MiB\n", ((double)lu->n * (double)lu->n * sizeof(double)) / (1024.0 * 1024.0));
+    printf("========================================\n");
+}
+
+// =====================================================================
+// C ABI: complex_lu.h
+// =====================================================================
+void complex_lu_options_default(ComplexLUOptions *options, int parallel_threads) {
+    if (!options) return;
+    options->parallel_threads = parallel_threads;
+    options->pivot_tolerance = 1.0e-14;
+    options->parallel_threshold = 64;
+}
+
+void complex_lu_init(ComplexLUFactorization *lu) {
+    if (lu) memset(lu, 0, sizeof(*lu));
+}
+
+void complex_lu_free(ComplexLUFactorization *lu) {
+    if (!lu) return;
+    if (lu->data) registry_drop(lu->data);
+    free(lu->data);
+    free(lu->pivots);
+    free(lu->row_scale);
+    free(lu->column_scale);
+    complex_lu_init(lu);
+}
+
+int complex_lu_factorize(const Complex *input, size_t n, const ComplexLUOptions *options,
+                         ComplexLUFactorization *lu) {
+    if (!input || !options || !lu || n == 0 || options->parallel_threads < 1 || !isfinite(options->pivot_tolerance) ||
+        options->pivot_tolerance < 0.0)
+        return -1;
+    if (n > (size_t)0x7fffffff || n > SIZE_MAX / n || n * n > SIZE_MAX / sizeof(Complex)) {
+        fprintf(stderr, "ERROR: complex LU matrix size overflow.\n");
+        return -1;
+    }
+    complex_lu_init(lu);
+    lu->n = n;
+    lu->data = (Complex *)malloc(n * n * sizeof(Complex));
+    lu->pivots = (size_t *)malloc(n * sizeof(size_t));
+    lu->row_scale = (double *)malloc(n * sizeof(double));
+    lu->column_scale = (double *)malloc(n * sizeof(double));
+    if (!lu->data || !lu->pivots || !lu->row_scale || !lu->column_scale) {
+        fprintf(stderr, "ERROR: cannot allocate complex LU factorization.\n");
+        complex_lu_free(lu);
+        return -1;
+    }
+    lu->matrix_scale = 0.0;
+    int s = factorize_common<cplx>((const cplx *)input, n, options->pivot_tolerance, true, (cplx *)lu->data,
+                                   lu->pivots, &lu->swap_count, &lu->matrix_scale, lu->row_scale, lu->column_scale);
+    // equilibration / scale failures release everything (complex_lu.c:275-320);
+    // a singular pivot keeps the partial factor for the caller to free
+    if (s == -1 || (s == -2 && (!isfinite(lu->matrix_scale) || lu->matrix_scale <= 0.0))) {
+        complex_lu_free(lu);
+        return s;
+    }
+    lu->factorized = s == 0;
+    return s;
+}
+
+int complex_lu_solve(const ComplexLUFactorization *lu, const Complex *b, Complex *x) {
+    if (!lu || !b || !x || !lu->data || !lu->pivots || !lu->factorized) return -1;
+    if (!lu->row_scale || !lu->column_scale) return -1;
+    return solve_common<cplx>((const cplx *)lu->data, lu->pivots, lu->row_scale, lu->column_scale, lu->n, true,
+                              (const cplx *)b, (cplx *)x, 1);
+}
+
+int complex_lu_solve_multiple(const ComplexLUFactorization *lu, const Complex *B, Complex *X, size_t rhs_count,
+                              int parallel_threads) {
+    if (!lu || !B || !X || rhs_count == 0 || parallel_threads < 1 || !lu->factorized) return -1;
+    if (!lu->data || !lu->pivots || !lu->row_scale || !lu->column_scale) return -1;
+    return solve_common<cplx>((const cplx *)lu->data, lu->pivots, lu->row_scale, lu->column_scale, lu->n, true,
+                              (const cplx *)B, (cplx *)X, rhs_count);
+}
+
+void complex_lu_print_info(const ComplexLUFactorization *lu) {
+    if (!lu) return;
+    printf("\n========================================\n");
+    printf("COMPLEX LU FACTORIZATION (GPU)\n");
+    printf("========================================\n");
+    printf("Size         : %zu x %zu\n", lu->n, lu->n);
+    printf("Swap count   : %zu\n", lu->swap_count);
+    printf("Matrix scale : %.9e\n", lu->matrix_scale);
+    printf("Factorized   : %s\n", lu->factorized ? "yes" : "no");
+    if (lu->data && lu->n > 0)
+        printf("LU memory    : %.3f MiB\n", ((double)lu->n * (double)lu->n * sizeof(Complex)) / (1024.0 * 1024.0));
+    printf("========================================\n");
+}
+
+}  // extern "C"

@@ -1,0 +1,265 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own hot-path sources, compiled unchanged into
+oracle/_ref/libpeec_ref.so (`make -C oracle ref`), on small seeded inputs and
+stores inputs and outputs as .npz files.  The GPU machine has no copy of the
+reference, so the tests there compare against these files.
+
+    python tests/golden/make_golden.py        (needs oracle/_ref/libpeec_ref.so)
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi  # noqa: E402
+from oracle import Reference  # noqa: E402
+
+REF_MESH_DIR = os.environ.get("PEEC_REFERENCE_DIR", "/root/reference") + "/meshes"
+
+_libc = C.CDLL(None)
+_libc.malloc.restype = C.c_void_p
+_libc.malloc.argtypes = [C.c_size_t]
+
+
+def _c_copy(arr, ctype):
+    p = _libc.malloc(max(1, arr.nbytes))
+    C.memmove(p, arr.ctypes.data, arr.nbytes)
+    return C.cast(p, C.POINTER(ctype))
+
+
+def _arr(ptr, shape, dtype):
+    n = int(np.prod(shape))
+    ctype = C.c_double if dtype == np.float64 else C.c_int
+    return np.frombuffer(C.cast(ptr, C.POINTER(ctype * n)).contents, dtype=dtype).reshape(shape).copy()
+
+
+def plate_arrays(lx, ly, nx, ny):
+    xyz = np.zeros(((nx + 1) * (ny + 1), 3))
+    for j in range(ny + 1):
+        for i in range(nx + 1):
+            xyz[j * (nx + 1) + i] = (lx * i / nx, ly * j / ny, 0.0)
+    quads = []
+    for j in range(ny):
+        for i in range(nx):
+            v = j * (nx + 1) + i
+            quads.append((v, v + 1, v + 1 + nx + 1, v + nx + 1))
+    return xyz, np.array(quads, dtype=np.int32)
+
+
+def reference_case(R, xyz, quads, name, with_matrices=True):
+    m = abi.Mesh()
+    R.lib.mesh_init(C.byref(m))
+    m.n_nodes, m.n_quads = xyz.shape[0], quads.shape[0]
+    m.xyz = _c_copy(np.ascontiguousarray(xyz, np.float64), C.c_double)
+    m.quads = _c_copy(np.ascontiguousarray(quads, np.int32), C.c_int)
+    assert R.lib.mesh_build_topology(C.byref(m)) == 0
+    d = abi.DualMesh()
+    assert R.lib.dual_mesh_build(C.byref(m), C.byref(d)) == 0
+    ne, nv, nq = m.n_edges, m.n_nodes, m.n_quads
+    out = dict(
+        xyz=xyz, quads=quads,
+        edges=_arr(m.edges, (ne, 2), np.int32),
+        cell_edges=_arr(m.cell_edges, (nq, 4), np.int32),
+        cell_edge_signs=_arr(m.cell_edge_signs, (nq, 4), np.int32),
+        edge_lengths=_arr(m.edge_lengths, (ne,), np.float64),
+        edge_directions=_arr(m.edge_directions, (ne, 3), np.float64),
+        edge_region_areas=np.ctypeslib.as_array(d.edge_region_areas, shape=(ne,)).copy(),
+        node_region_areas=np.ctypeslib.as_array(d.node_region_areas, shape=(nv,)).copy(),
+        edge_patch_counts=np.array([d.edge_patches[r].count for r in range(ne)]),
+        node_patch_counts=np.array([d.node_patches[r].count for r in range(nv)]),
+    )
+    out["edge_patches"] = np.concatenate([
+        np.array([list(d.edge_patches[r].patches[k].points) for k in range(d.edge_patches[r].count)])
+        for r in range(ne)])
+    out["node_patches"] = np.concatenate([
+        np.array([list(d.node_patches[r].patches[k].points) for k in range(d.node_patches[r].count)])
+        for r in range(nv)])
+    if with_matrices:
+        lo = abi.InductanceOptions()
+        R.lib.inductance_options_default(C.byref(lo), os.cpu_count())
+        L = abi.InductanceMatrix()
+        assert R.lib.inductance_compute_matrix(C.byref(m), C.byref(d), C.byref(lo), C.byref(L)) == 0
+        out["L"] = np.ctypeslib.as_array(L.data, shape=(ne, ne)).copy()
+        po = abi.PotentialOptions()
+        R.lib.potential_options_default(C.byref(po), os.cpu_count())
+        Pm = abi.PotentialMatrix()
+        assert R.lib.potential_compute_matrix(C.byref(m), C.byref(d), C.byref(po), C.byref(Pm)) == 0
+        out["P"] = np.ctypeslib.as_array(Pm.data, shape=(nv, nv)).copy()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "Ne=%d Nv=%d" % (ne, nv))
+
+
+def box_arrays(lx, ly, lz, nx, ny, nz):
+    # same construction as the library's peec_synth_box (outward winding,
+    # first-seen vertex numbering over the faces -z, +z, -y, +y, -x, +x)
+    ids, xyz, quads = {}, [], []
+
+    def v(i, j, k):
+        if (i, j, k) not in ids:
+            ids[(i, j, k)] = len(xyz)
+            xyz.append((lx * i / nx, ly * j / ny, lz * k / nz))
+        return ids[(i, j, k)]
+
+    for j in range(ny):
+        for i in range(nx):
+            quads.append((v(i, j, 0), v(i, j + 1, 0), v(i + 1, j + 1, 0), v(i + 1, j, 0)))
+    for j in range(ny):
+        for i in range(nx):
+            quads.append((v(i, j, nz), v(i + 1, j, nz), v(i + 1, j + 1, nz), v(i, j + 1, nz)))
+    for k in range(nz):
+        for i in range(nx):
+            quads.append((v(i, 0, k), v(i + 1, 0, k), v(i + 1, 0, k + 1), v(i, 0, k + 1)))
+    for k in range(nz):
+        for i in range(nx):
+            quads.append((v(i, ny, k), v(i, ny, k + 1), v(i + 1, ny, k + 1), v(i + 1, ny, k)))
+    for k in range(nz):
+        for j in range(ny):
+            quads.append((v(0, j, k), v(0, j, k + 1), v(0, j + 1, k + 1), v(0, j + 1, k)))
+    for k in range(nz):
+        for j in range(ny):
+            quads.append((v(nx, j, k), v(nx, j + 1, k), v(nx, j + 1, k + 1), v(nx, j, k + 1)))
+    return np.array(xyz), np.array(quads, dtype=np.int32)
+
+
+def gmsh_case(R, path, name):
+    m = abi.Mesh()
+    R.lib.mesh_init(C.byref(m))
+    assert R.lib.mesh_load_gmsh(path.encode(), C.byref(m)) == 0
+    xyz = _arr(m.xyz, (m.n_nodes, 3), np.float64)
+    quads = _arr(m.quads, (m.n_quads, 4), np.int32)
+    reference_case(R, xyz, quads, name)
+
+
+def lu_cases(R):
+    rng = np.random.default_rng(20261203)
+    out = {}
+    for n in (1, 7, 40, 97):
+        a = rng.standard_normal((n, n))
+        if n == 40:
+            a[:, 3] *= 1e-3   # forces pivoting decisions away from the diagonal
+        b = rng.standard_normal(n)
+        o = abi.LUOptions()
+        R.lib.lu_options_default(C.byref(o), 1)
+        lu = abi.LUFactorization()
+        assert R.lib.lu_factorize(a.ctypes.data_as(abi.c_double_p), n, C.byref(o), C.byref(lu)) == 0
+        x = np.zeros(n)
+        assert R.lib.lu_solve(C.byref(lu), b.ctypes.data_as(abi.c_double_p), x.ctypes.data_as(abi.c_double_p)) == 0
+        out["real%d_a" % n] = a
+        out["real%d_b" % n] = b
+        out["real%d_lu" % n] = np.ctypeslib.as_array(lu.data, shape=(n, n)).copy()
+        out["real%d_piv" % n] = np.ctypeslib.as_array(lu.pivots, shape=(n,)).astype(np.int64)
+        out["real%d_x" % n] = x
+        out["real%d_det" % n] = np.array(R.lib.lu_determinant(C.byref(lu)))
+        R.lib.lu_free(C.byref(lu))
+    for n in (1, 5, 33, 80):
+        a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        a[0, :] *= 1e6  # unequal row scales exercise the equilibration
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        o = abi.ComplexLUOptions()
+        R.lib.complex_lu_options_default(C.byref(o), 1)
+        lu = abi.ComplexLUFactorization()
+        ac = np.ascontiguousarray(a)
+        assert R.lib.complex_lu_factorize(C.cast(ac.ctypes.data, C.POINTER(abi.Complex)), n, C.byref(o),
+                                          C.byref(lu)) == 0
+        x = np.zeros(n, dtype=np.complex128)
+        bc = np.ascontiguousarray(b)
+        assert R.lib.complex_lu_solve(C.byref(lu), C.cast(bc.ctypes.data, C.POINTER(abi.Complex)),
+                                      C.cast(x.ctypes.data, C.POINTER(abi.Complex))) == 0
+        raw = np.ctypeslib.as_array(C.cast(lu.data, abi.c_double_p), shape=(n * n * 2,)).copy()
+        out["cplx%d_a" % n] = a
+        out["cplx%d_b" % n] = b
+        out["cplx%d_lu" % n] = raw.view(np.complex128).reshape(n, n)
+        out["cplx%d_piv" % n] = np.ctypeslib.as_array(lu.pivots, shape=(n,)).astype(np.int64)
+        out["cplx%d_rs" % n] = np.ctypeslib.as_array(lu.row_scale, shape=(n,)).copy()
+        out["cplx%d_cs" % n] = np.ctypeslib.as_array(lu.column_scale, shape=(n,)).copy()
+        out["cplx%d_x" % n] = x
+        R.lib.complex_lu_free(C.byref(lu))
+    np.savez_compressed(os.path.join(HERE, "lu_cases.npz"), **out)
+    print("wrote lu_cases")
+
+
+def quadrature_cases(R):
+    """Single patch pairs in every class, including the reference tests'
+    rectangles and partitions, with the reference's K values."""
+    rng = np.random.default_rng(7)
+    pairs = []
+    sq = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0], float)
+    for aspect in (1.0, 10.0, 100.0):
+        p = np.array([0, 0, 0, aspect, 0, 0, aspect, 1, 0, 0, 1, 0], float)
+        pairs.append((p, p, 1))                 # same object (SELF by pointer)
+    pairs.append((sq, sq.copy(), 0))            # SELF by geometry
+    b = sq.copy()
+    b[0::3] += 1
+    pairs.append((sq, b, 0))                    # TOUCHING along an edge
+    pairs.append((b, sq, 0))
+    c = sq.copy()
+    c[0::3] += 1
+    c[1::3] += 1
+    pairs.append((sq, c, 0))                    # TOUCHING at a corner
+    d = sq.copy()
+    d[2::3] = 1e-7
+    pairs.append((sq, d, 0))                    # NEAR (stacked, tiny gap)
+    e = sq.copy()
+    e[0::3] += 1.3
+    pairs.append((sq, e, 0))                    # NEAR (gap 0.3 < 0.5)
+    f = sq.copy()
+    f[2::3] = 100.0
+    pairs.append((sq, f, 0))                    # FAR
+    for _ in range(12):                         # random skewed quads at random offsets
+        base = rng.uniform(-1, 1, 3)
+        q1 = (base + rng.uniform(0, 0.5, (4, 3)) * np.array([1, 1, 0.2])
+              + np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]])).ravel()
+        off = rng.uniform(-3, 3, 3)
+        q2 = (q1.reshape(4, 3) + off).ravel()
+        pairs.append((q1, q2, 0))
+    rot = np.array([0, 0, 0, 2, 0, 0, 2, 1, 0, 0, 1, 0], float)
+    e1, f1 = np.array([0.6, 0.8, 0]), np.array([-0.48, 0.36, 0.8])
+    rr = np.array([3.7 * (rot[3 * i] * e1 + rot[3 * i + 1] * f1) + np.array([1, 2, 3]) for i in range(4)]).ravel()
+    pairs.append((rr, rr, 1))
+    A, B, SAME, K, CLS = [], [], [], [], []
+    for pa, pb, same in pairs:
+        qa = abi.QuadPatch()
+        qb = abi.QuadPatch()
+        for t in range(12):
+            qa.points[t] = pa[t]
+            qb.points[t] = pb[t]
+        b_ref = qa if same else qb
+        K.append(R.lib.quad_patch_kernel_1_over_r(C.byref(qa), C.byref(b_ref), 4, 10, 12, 8, 0.5))
+        CLS.append(R.lib.quad_patch_classify_pair(C.byref(qa), C.byref(b_ref), 0.5))
+        A.append(pa)
+        B.append(pb)
+        SAME.append(same)
+    np.savez_compressed(os.path.join(HERE, "quadrature_cases.npz"), a=np.array(A), b=np.array(B),
+                        same=np.array(SAME), K=np.array(K), cls=np.array(CLS))
+    gl = {}
+    for q in (2, 3, 4, 5, 6, 8, 10, 12, 16):
+        x, w = np.zeros(16), np.zeros(16)
+        R.lib.gauss_legendre_rule(q, x.ctypes.data_as(abi.c_double_p), w.ctypes.data_as(abi.c_double_p))
+        gl["x%d" % q] = x[:q]
+        gl["w%d" % q] = w[:q]
+    np.savez_compressed(os.path.join(HERE, "gauss_legendre.npz"), **gl)
+    print("wrote quadrature_cases, gauss_legendre")
+
+
+def main():
+    R = Reference()
+    quadrature_cases(R)
+    lu_cases(R)
+    reference_case(R, *plate_arrays(1.0, 1.0, 4, 4), "plate4")
+    reference_case(R, *plate_arrays(1.0, 1.0, 8, 8), "plate8")
+    reference_case(R, *box_arrays(0.4, 0.2, 0.1, 4, 2, 1), "box421")
+    reference_case(R, *box_arrays(2.0, 1.0, 0.5, 40, 20, 10), "box_5cm_topology", with_matrices=False)
+    plate_msh = os.path.join(REF_MESH_DIR, "plate.msh")
+    if os.path.exists(plate_msh):
+        gmsh_case(R, plate_msh, "plate_msh")
+
+
+if __name__ == "__main__":
+    main()

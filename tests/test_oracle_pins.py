@@ -1,0 +1,179 @@
+"""Pins the CPU oracle before it is trusted as the checker.
+
+1. Against the reference's own unit-test identities (reference
+   tests/test_core.c): closed-form rectangle self integrals (aspect 1, 10,
+   100, tolerance 1e-3), rotation/translation/scale invariance, the touching
+   partition and reciprocity (< 1e-12), near-to-self and far bounds, the 3x3
+   real and 2x2 complex LU known answers (< 1e-11) and the singular complex
+   matrix.
+2. Against golden fixtures produced by the reference itself
+   (tests/golden/make_golden.py): Gauss-Legendre tables, single patch pairs
+   of every class, Lp and P of small plates, a box and the reference's own
+   meshes/plate.msh, and LU factors / pivots / solutions.
+3. Bit for bit against the reference library when it was compiled here.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from helpers import quad_patch, rel_err
+
+ALGEBRA_TOL = 1e-11
+QUAD_TOL = 1e-3
+
+
+def rectangle_reference(a, b):
+    """Closed form of the a x b rectangle self integral (reference
+    tests/test_core.c:179-192), evaluated in extended precision."""
+    a, b = np.longdouble(a), np.longdouble(b)
+    h = np.hypot(a, b)
+    i00 = a * np.arcsinh(b / a) + b * np.arcsinh(a / b)
+    ix = (b * h + a * a * np.arcsinh(b / a) - b * b) / 2
+    iy = (a * h + b * b * np.arcsinh(a / b) - a * a) / 2
+    ixy = (h * h * h - a * a * a - b * b * b) / 3
+    return 4 * (a * b * i00 - b * ix - a * iy + ixy)
+
+
+@pytest.mark.parametrize("aspect", [1.0, 10.0, 100.0])
+def test_rectangle_self_integral(oracle, aspect):
+    p = quad_patch([0, 0, 0, aspect, 0, 0, aspect, 1, 0, 0, 1, 0])
+    k = oracle.patch_kernel(p, p)
+    exact = rectangle_reference(aspect, 1.0)
+    assert np.isfinite(k) and k > 0
+    assert abs((np.longdouble(k) - exact) / exact) <= QUAD_TOL
+
+
+def test_geometry_invariance(oracle):
+    a = np.array([0, 0, 0, 2, 0, 0, 2, 1, 0, 0, 1, 0], float)
+    e, f = np.array([0.6, 0.8, 0]), np.array([-0.48, 0.36, 0.8])
+    b = np.array([3.7 * (a[3 * i] * e + a[3 * i + 1] * f) + np.array([1, 2, 3]) for i in range(4)]).ravel()
+    pb = quad_patch(b)
+    exact = float(rectangle_reference(2, 1)) * 3.7 ** 3
+    assert abs(oracle.patch_kernel(pb, pb) / exact - 1) < QUAD_TOL
+
+
+def test_touching_partition_and_reciprocity(oracle):
+    a = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0], float)
+    b = a.copy()
+    b[0::3] += 1
+    pa, pb = quad_patch(a), quad_patch(b)
+    ab, ba = oracle.patch_kernel(pa, pb), oracle.patch_kernel(pb, pa)
+    total = oracle.patch_kernel(pa, pa) + oracle.patch_kernel(pb, pb) + ab + ba
+    assert abs(total / float(rectangle_reference(2, 1)) - 1) < QUAD_TOL
+    assert abs(ab - ba) < 1e-12
+
+
+def test_near_and_far_bounds(oracle):
+    a = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0], float)
+    b = a.copy()
+    b[2::3] = 1e-7
+    near = oracle.patch_kernel(quad_patch(a), quad_patch(b))
+    assert abs(near / float(rectangle_reference(1, 1)) - 1) < QUAD_TOL
+    b[2::3] = 100
+    far = oracle.patch_kernel(quad_patch(a), quad_patch(b))
+    assert 1 / np.sqrt(10000.0 + 2) <= far <= 0.01
+
+
+def test_real_lu_known_answer(oracle):
+    a = np.array([0, 2, 1, 1, -2, -3, 2, 3, 1], float).reshape(3, 3)
+    exact = np.array([1, -2, 0.5])
+    s, lu, piv, _, _ = oracle.lu_factorize(a, threads=1)
+    assert s == 0
+    s, x = oracle.lu_solve(lu, piv, a @ exact)
+    assert s == 0 and np.max(np.abs(x - exact)) < ALGEBRA_TOL
+
+
+def test_complex_lu_known_answer(oracle):
+    a = np.array([[0, 2 + 1j], [1 - 1j, 3 + 0.5j]])
+    exact = np.array([1 + 2j, -0.5 + 0.75j])
+    s, lu, piv, _, _, rs, cs = oracle.complex_lu_factorize(a, threads=1)
+    assert s == 0
+    s, x = oracle.complex_lu_solve(lu, piv, rs, cs, a @ exact)
+    assert s == 0 and np.max(np.abs(x - exact)) < ALGEBRA_TOL
+
+
+def test_complex_lu_singular(oracle):
+    a = np.array([[1 + 1j, 2 + 2j], [2 + 2j, 4 + 4j]])
+    assert oracle.complex_lu_factorize(a, threads=1)[0] != 0
+
+
+def test_gauss_legendre_tables(oracle):
+    g = golden("gauss_legendre")
+    for q in (2, 3, 4, 5, 6, 8, 10, 12, 16):
+        x, w = oracle.gauss_legendre(q)
+        assert np.array_equal(x, g["x%d" % q]) and np.array_equal(w, g["w%d" % q])
+    assert oracle.gauss_legendre(7) is None
+
+
+def test_patch_pairs_against_reference_values(oracle):
+    q = golden("quadrature_cases")
+    for k in range(len(q["K"])):
+        a, b = quad_patch(q["a"][k]), quad_patch(q["b"][k])
+        bb = a if q["same"][k] else b
+        assert oracle.classify(a, bb) == q["cls"][k]
+        val = oracle.patch_kernel(a, bb)
+        # same algorithm; libm asinh/atan2 may differ by an ulp across CPUs
+        assert abs(val - q["K"][k]) <= 1e-13 * abs(q["K"][k]), k
+
+
+@pytest.mark.parametrize("name", ["plate4", "plate8", "box421", "plate_msh"])
+def test_matrices_against_reference(oracle, name):
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    g = golden(name)
+    with SynthMesh.from_arrays(g["xyz"], g["quads"]) as m:
+        s, L = oracle.inductance(m)
+        assert s == 0
+        assert np.array_equal(L == 0, g["L"] == 0)
+        assert rel_err(L, g["L"]) < 1e-13
+        s, P = oracle.potential(m)
+        assert s == 0
+        assert rel_err(P, g["P"]) < 1e-13
+
+
+def test_lu_cases_against_reference(oracle):
+    g = golden("lu_cases")
+    for n in (1, 7, 40, 97):
+        s, lu, piv, _, _ = oracle.lu_factorize(g["real%d_a" % n])
+        assert s == 0
+        assert np.array_equal(piv.astype(np.int64), g["real%d_piv" % n])
+        assert np.array_equal(lu, g["real%d_lu" % n])  # no reductions in the factorisation
+        s, x = oracle.lu_solve(lu, piv, g["real%d_b" % n])
+        assert rel_err(x, g["real%d_x" % n]) < 1e-13
+    for n in (1, 5, 33, 80):
+        s, lu, piv, _, _, rs, cs = oracle.complex_lu_factorize(g["cplx%d_a" % n])
+        assert s == 0
+        assert np.array_equal(piv.astype(np.int64), g["cplx%d_piv" % n])
+        assert rel_err(lu, g["cplx%d_lu" % n]) < 1e-14
+        s, x = oracle.complex_lu_solve(lu, piv, rs, cs, g["cplx%d_b" % n])
+        assert rel_err(x, g["cplx%d_x" % n]) < 1e-12
+
+
+def _reference():
+    from oracle import Reference, reference_available
+    if not reference_available():
+        pytest.skip("reference library not compiled on this machine")
+    return Reference()
+
+
+def test_bit_exact_against_reference_library(oracle):
+    """Same machine, same libm: the restatement reproduces every bit."""
+    R = _reference()
+    q = golden("quadrature_cases")
+    for k in range(len(q["K"])):
+        a, b = quad_patch(q["a"][k]), quad_patch(q["b"][k])
+        bb = a if q["same"][k] else b
+        assert oracle.patch_kernel(a, bb) == R.lib.quad_patch_kernel_1_over_r(
+            C.byref(a), C.byref(bb), 4, 10, 12, 8, 0.5)
+    from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    with SynthMesh.plate(1.0, 1.0, 6, 5) as m:
+        o = abi.InductanceOptions()
+        R.lib.inductance_options_default(C.byref(o), 4)
+        L = abi.InductanceMatrix()
+        assert R.lib.inductance_compute_matrix(C.byref(m.mesh), C.byref(m.dual), C.byref(o), C.byref(L)) == 0
+        ref = np.ctypeslib.as_array(L.data, shape=(L.n, L.n)).copy()
+        R.lib.inductance_free(C.byref(L))
+        assert np.array_equal(oracle.inductance(m)[1], ref)
