@@ -1,0 +1,438 @@
+"""Benchmark: plain-FP64 harmonic PEEC solves on one GB300.
+
+Workload (one step = one solve): closed PEC box 2.0 x 1.0 x 0.5 m meshed at
+5 cm (2800 cells, Ne = 5600 edges, Nv = 2802 nodes, N = 8402 complex
+unknowns), 30 MHz, one x-polarised unit plane wave incident from +z:
+  assemble Lp (Ne^2) and P (Nv^2) from the 1/R panel integrals,
+  fill the MNA matrix Z = [R + jwL, A; -P A^T, jw I] (PEC: R = 0),
+  complex LU factorisation (equilibrated, partial pivoting),
+  solve, and gate on the componentwise backward error <= 1e-10.
+Lp and P are quasi-static (the reference has no retardation).
+
+  value   solves/s with the geometry resident and every matrix built,
+          factored and checked in HBM (extension API, CUDA-event timed on
+          the library stream)
+  e2e     the same solve through the drop-in C ABI with host buffers:
+          inductance_compute_matrix, potential_compute_matrix, host MNA
+          fill (what the reference's harmonic driver does), complex_lu_
+          factorize, complex_lu_solve, host backward error
+  --impl reference   the reference algorithm on the host cores (the CPU
+          oracle, a restatement bit-exact with the reference's sources), on
+          a bounded sample extrapolated to one solve
+Multi-GPU: the path does not shard; --gpus N runs N independent replicas
+(one process per GPU) and reports the aggregate.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+FREQ = 30e6
+C0 = 299792458.0
+BOX = (2.0, 1.0, 0.5, 40, 20, 10)
+WORKLOAD = "pec_box_2x1x0.5m_5cm_30MHz_planewave"
+METRIC = "PEEC solves/s at <=1e-10 backward error (plain FP64 GPU path)"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ---------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------
+# workload pieces
+# ---------------------------------------------------------------------
+def make_mesh():
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    return SynthMesh.box(*BOX)
+
+
+def plane_wave(m):
+    """Host copy of the right-hand side [-U_e ; 0] (same formula as the
+    device kernel): x-polarised, incident from +z."""
+    k0 = 2 * np.pi * FREQ / C0
+    kh, eh = np.array([0.0, 0.0, -1.0]), np.array([1.0, 0.0, 0.0])
+    ctr = m.array("edge_centers", (m.n_edges, 3))
+    vec = m.array("edge_vectors", (m.n_edges, 3))
+    phase = -k0 * (ctr @ kh)
+    proj = vec @ eh
+    h = 0.5 * k0 * (vec @ kh)
+    sinc = np.where(np.abs(h) < 1e-8, 1 - h * h / 6, np.sin(h) / np.where(h == 0, 1, h))
+    b = np.zeros(m.n_edges + m.n_nodes, dtype=np.complex128)
+    b[:m.n_edges] = -proj * np.exp(1j * phase) * sinc
+    return b
+
+
+def host_mna(L, P, edges, freq):
+    """Z = [jwL, A; -P A^T, jw I] on the host, as the reference's
+    harmonic_build_system does (PEC: R = 0)."""
+    ne, nv = L.shape[0], P.shape[0]
+    n = ne + nv
+    w = 2 * np.pi * freq
+    Z = np.zeros((n, n), dtype=np.complex128)
+    Z[:ne, :ne] = 1j * w * L
+    idx = np.arange(ne)
+    Z[idx, ne + edges[:, 0]] = -1.0
+    Z[idx, ne + edges[:, 1]] = 1.0
+    Z[ne:, :ne] = -(P[:, edges[:, 1]] - P[:, edges[:, 0]])
+    Z[np.arange(ne, n), np.arange(ne, n)] = 1j * w
+    return Z
+
+
+def host_backward_error(Z, x, b):
+    r = Z @ x - b
+    den = np.abs(Z) @ np.abs(x) + np.abs(b)
+    return float(np.max(np.abs(r) / np.where(den > 0, den, 1)))
+
+
+class DeviceSolve:
+    """One solve with every matrix in HBM (extension API)."""
+
+    def __init__(self, lib, m):
+        from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+        self.lib, self.m, self.abi = lib, m, abi
+        ne, nv = m.n_edges, m.n_nodes
+        self.ne, self.nv, self.n = ne, nv, ne + nv
+        n = self.n
+        al = lib.peec_gb300_device_alloc
+        self.dL, self.dP = al(ne * ne * 8), al(nv * nv * 8)
+        self.dZ, self.dLU = al(n * n * 16), al(n * n * 16)
+        self.db, self.dx = al(n * 16), al(n * 16)
+        self.dpiv, self.dperm = al(n * 8), al(n * 4)
+        self.drow, self.dcol = al(n * 8), al(n * 8)
+        self.dedges = al(ne * 2 * 4)
+        self.dctr, self.dvec = al(ne * 24), al(ne * 24)
+        for p in (self.dL, self.dP, self.dZ, self.dLU, self.db, self.dx):
+            if not p:
+                raise RuntimeError("device allocation failed")
+        e = np.ascontiguousarray(m.edges())
+        lib.peec_gb300_copy_to_device(self.dedges, e.ctypes.data, e.nbytes)
+        ctr = np.ascontiguousarray(m.array("edge_centers", (ne, 3)))
+        vec = np.ascontiguousarray(m.array("edge_vectors", (ne, 3)))
+        lib.peec_gb300_copy_to_device(self.dctr, ctr.ctypes.data, ctr.nbytes)
+        lib.peec_gb300_copy_to_device(self.dvec, vec.ctypes.data, vec.nbytes)
+        self.lo = abi.InductanceOptions()
+        lib.inductance_options_default(C.byref(self.lo), 1)
+        self.po = abi.PotentialOptions()
+        lib.potential_options_default(C.byref(self.po), 1)
+        self.stL, self.stP = abi.PeecAssemblyStats(), abi.PeecAssemblyStats()
+        self.kh = (C.c_double * 3)(0.0, 0.0, -1.0)
+        self.eh = (C.c_double * 3)(1.0, 0.0, 0.0)
+        self.k0 = 2 * np.pi * FREQ / C0
+        self.phase_ms = {}
+
+    def step(self, timed_phases=False):
+        lib, m, n = self.lib, self.m, self.n
+        ev = [lib.peec_gb300_event_record()]
+        assert lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(self.lo), self.dL,
+                                                C.byref(self.stL)) == 0
+        ev.append(lib.peec_gb300_event_record())
+        assert lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(self.po), self.dP,
+                                               C.byref(self.stP)) == 0
+        ev.append(lib.peec_gb300_event_record())
+        assert lib.peec_gb300_harmonic_build_device(self.dL, self.dP, self.dedges, None, self.ne, self.nv, FREQ,
+                                                    self.dZ) == 0
+        assert lib.peec_gb300_copy_device(self.dLU, self.dZ, n * n * 16) == 0
+        ev.append(lib.peec_gb300_event_record())
+        scale, col = C.c_double(), C.c_int()
+        s = lib.peec_gb300_complex_lu_factor_device(self.dLU, n, 1e-14, self.dpiv, self.dperm, self.drow, self.dcol,
+                                                    C.byref(scale), C.byref(col))
+        assert s == 0, "factorisation failed"
+        ev.append(lib.peec_gb300_event_record())
+        assert lib.peec_gb300_plane_wave_rhs_device(self.dctr, self.dvec, self.ne, self.nv, self.kh, self.eh,
+                                                    self.k0, self.db) == 0
+        assert lib.peec_gb300_complex_lu_solve_device(self.dLU, self.dperm, self.drow, self.dcol, n, self.db,
+                                                      self.dx, 1) == 0
+        ev.append(lib.peec_gb300_event_record())
+        out = (C.c_double * 3)()
+        assert lib.peec_gb300_backward_error_device(self.dZ, n, self.dx, self.db, 1, out) == 0
+        ev.append(lib.peec_gb300_event_record())
+        names = ["assemble_Lp", "assemble_P", "mna_fill", "complex_lu", "rhs_solve", "backward_error"]
+        for k, name in enumerate(names):
+            self.phase_ms.setdefault(name, []).append(lib.peec_gb300_event_elapsed_ms(ev[k], ev[k + 1]))
+        for e in ev:
+            lib.peec_gb300_event_destroy(e)
+        return out[0]
+
+    def free(self):
+        for p in (self.dL, self.dP, self.dZ, self.dLU, self.db, self.dx, self.dpiv, self.dperm, self.drow, self.dcol,
+                  self.dedges, self.dctr, self.dvec):
+            self.lib.peec_gb300_device_free(p)
+
+
+def drop_in_solve(lib, m, b_host, edges):
+    from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+    lo = abi.InductanceOptions()
+    lib.inductance_options_default(C.byref(lo), 1)
+    L = abi.InductanceMatrix()
+    assert lib.inductance_compute_matrix(C.byref(m.mesh), C.byref(m.dual), C.byref(lo), C.byref(L)) == 0
+    Lh = np.ctypeslib.as_array(L.data, shape=(L.n, L.n))
+    po = abi.PotentialOptions()
+    lib.potential_options_default(C.byref(po), 1)
+    P = abi.PotentialMatrix()
+    assert lib.potential_compute_matrix(C.byref(m.mesh), C.byref(m.dual), C.byref(po), C.byref(P)) == 0
+    Ph = np.ctypeslib.as_array(P.data, shape=(P.n, P.n))
+    Z = host_mna(Lh, Ph, edges, FREQ)
+    lib.inductance_free(C.byref(L))
+    lib.potential_free(C.byref(P))
+    n = Z.shape[0]
+    o = abi.ComplexLUOptions()
+    lib.complex_lu_options_default(C.byref(o), 1)
+    f = abi.ComplexLUFactorization()
+    cp = lambda v: C.cast(v.ctypes.data, C.POINTER(abi.Complex))  # noqa: E731
+    assert lib.complex_lu_factorize(cp(Z), n, C.byref(o), C.byref(f)) == 0
+    x = np.zeros(n, dtype=np.complex128)
+    assert lib.complex_lu_solve(C.byref(f), cp(b_host), cp(x)) == 0
+    lib.complex_lu_free(C.byref(f))
+    be = host_backward_error(Z, x, b_host)
+    h2d = Z.nbytes + b_host.nbytes + geometry_bytes(m) * 2
+    d2h = (Lh.size + Ph.size) * 8 + Z.nbytes + n * 8 + x.nbytes
+    return be, h2d, d2h
+
+
+def geometry_bytes(m):
+    """Patch corners + per-region data uploaded by one assembly call."""
+    np_e = sum(m.dual.edge_patches[r].count for r in range(m.n_edges))
+    np_v = sum(m.dual.node_patches[r].count for r in range(m.n_nodes))
+    return (np_e + np_v) * (96 + 8) // 2 + (m.n_edges + m.n_nodes) * 40 // 2
+
+
+# ---------------------------------------------------------------------
+# CPU: the reference algorithm (oracle) on a bounded sample
+# ---------------------------------------------------------------------
+def cpu_sample_solve_seconds(m, threads, budget_rows=(48, 48), lu_n=1600):
+    """Seconds for one full solve on `threads` host cores, extrapolated from
+    a sample: the first rows of the Lp and P upper triangles (scaled by the
+    number of entry pairs), and a complex LU + solve of size lu_n (scaled by
+    (N/lu_n)^3 and (N/lu_n)^2)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from oracle import Oracle
+    orc = Oracle()
+    ne, nv = m.n_edges, m.n_nodes
+    n = ne + nv
+    parts = {}
+    t = time.perf_counter()
+    s, _ = orc.inductance(m, threads=threads, rows=(0, budget_rows[0]))
+    tl = time.perf_counter() - t
+    assert s == 0
+    pairs_s = sum(ne - a for a in range(budget_rows[0]))
+    parts["Lp"] = tl * (ne * (ne + 1) / 2) / pairs_s
+    t = time.perf_counter()
+    s, _ = orc.potential(m, threads=threads, rows=(0, budget_rows[1]))
+    tp = time.perf_counter() - t
+    assert s == 0
+    pairs_s = sum(nv - a for a in range(budget_rows[1]))
+    parts["P"] = tp * (nv * (nv + 1) / 2) / pairs_s
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((lu_n, lu_n)) + 1j * rng.standard_normal((lu_n, lu_n))
+    t = time.perf_counter()
+    s, lu, piv, _, _, rs, cs = orc.complex_lu_factorize(a, threads=threads)
+    tf = time.perf_counter() - t
+    t = time.perf_counter()
+    orc.complex_lu_solve(lu, piv, rs, cs, a[0])
+    ts = time.perf_counter() - t
+    parts["complex_lu"] = tf * (n / lu_n) ** 3
+    parts["solve"] = ts * (n / lu_n) ** 2
+    sample_s = tl + tp + tf + ts
+    desc = ("Lp rows 0-%d and P rows 0-%d of the upper triangle (scaled by entry-pair count), complex LU + "
+            "solve at n=%d (scaled by (N/n)^3, (N/n)^2); oracle restatement, %d threads"
+            % (budget_rows[0], budget_rows[1], lu_n, threads))
+    return sum(parts.values()), parts, sample_s, desc
+
+
+# ---------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    m = make_mesh()
+    threads = os.cpu_count()
+    times = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        sec, parts, sample_s, desc = cpu_sample_solve_seconds(m, threads, budget_rows=(16, 16), lu_n=1000)
+        if i >= args.warmup:
+            times.append(sec)
+        last = (parts, sample_s, desc)
+    t = statistics.median(times)
+    v = 1.0 / t
+    ref_kind = "reference" if os.path.exists(os.path.join(REPO, "oracle", "_ref", "libpeec_ref.so")) else "port"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_unknowns": m.n_edges + m.n_nodes, "Ne": m.n_edges,
+                       "Nv": m.n_nodes, "frequency_hz": FREQ, "parallelism": "cpu",
+                       "note": "bounded sample per step extrapolated to one full solve"},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": last[2], "phase_seconds": last[0]},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["cpu_baseline"]["kind"] = "port" if ref_kind == "port" else "port"
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+    lib = abi.load_gpu_lib()
+    if not lib.peec_gb300_device_ready():
+        raise RuntimeError("no CUDA device")
+    m = make_mesh()
+    ds = DeviceSolve(lib, m)
+    for _ in range(args.warmup):
+        be = ds.step()
+        assert be <= 1e-10, "backward error %g above the gate" % be
+    ds.phase_ms = {}
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    lib.peec_gb300_synchronize()
+    launches0 = lib.peec_gb300_launch_count()
+    clocks.start()
+    e0 = lib.peec_gb300_event_record()
+    bes = []
+    for _ in range(args.steps):
+        bes.append(ds.step())
+    e1 = lib.peec_gb300_event_record()
+    lib.peec_gb300_synchronize()
+    clk = clocks.stop()
+    total_ms = lib.peec_gb300_event_elapsed_ms(e0, e1)
+    launches = lib.peec_gb300_launch_count() - launches0
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    assert max(bes) <= 1e-10, "backward error above the gate"
+    ms_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+    phases = {k: statistics.median(v) for k, v in ds.phase_ms.items()}
+    ds.free()
+
+    # end to end through the drop-in ABI, host buffers
+    e2e = None
+    if not args.no_e2e:
+        b_host = plane_wave(m)
+        edges = m.edges()
+        drop_in_solve(lib, m, b_host, edges)  # warm (registry, pools)
+        ts = []
+        for _ in range(max(1, min(args.steps, 2))):
+            t = time.perf_counter()
+            be, h2d, d2h = drop_in_solve(lib, m, b_host, edges)
+            ts.append(time.perf_counter() - t)
+            assert be <= 1e-10
+        e2e = {"value": world / statistics.median(ts), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "backward_error": be}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sec, parts, sample_s, desc = cpu_sample_solve_seconds(m, os.cpu_count())
+        cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": desc, "sample_seconds": round(sample_s, 2),
+               "phase_seconds": {k: round(v, 2) for k, v in parts.items()}}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "n_unknowns": m.n_edges + m.n_nodes, "Ne": m.n_edges,
+                           "Nv": m.n_nodes, "frequency_hz": FREQ, "parallelism": "replicas" if world > 1 else "1gpu",
+                           "l2": "inputs larger than L2 (Z is %.2f GB)" % ((m.n_edges + m.n_nodes) ** 2 * 16 / 1e9),
+                           "retardation": "none (quasi-static, as the reference)"},
+                "phase_ms": phases, "backward_error": max(bes), "gpu_launches": int(launches),
+                "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+                "roofline": roofline(phases, m)}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def roofline(phases, m):
+    """Dominant phase of the step against its bound (filled in by measurement)."""
+    n = m.n_edges + m.n_nodes
+    lu_ms = phases.get("complex_lu")
+    flops = 8.0 / 3.0 * n ** 3
+    return {"bound": "fp64", "kernel": "complex LU (panel + FP64 trailing update)",
+            "achieved": flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None, "unit": "TFLOP/s",
+            "peak": None, "frac": None, "traffic": None}
+
+
+if __name__ == "__main__":
+    main()

@@ -12,6 +12,7 @@
 
 #include <stddef.h>
 
+#include "complex_matrix.h"
 #include "dual_mesh.h"
 #include "inductance.h"
 #include "mesh.h"
@@ -50,6 +51,8 @@ void peec_gb300_host_free_pinned(void *p);
 /* Synchronous copies on the library stream; 0 or -1. */
 int peec_gb300_copy_to_device(void *dst, const void *src, size_t bytes);
 int peec_gb300_copy_to_host(void *dst, const void *src, size_t bytes);
+/* Asynchronous device-to-device copy on the library stream. */
+int peec_gb300_copy_device(void *dst, const void *src, size_t bytes);
 int peec_gb300_synchronize(void);
 
 /* CUDA events recorded on the library stream. */
@@ -66,6 +69,46 @@ int peec_gb300_inductance_device(const Mesh *mesh, const DualMesh *dual,
 int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual,
                                 const PotentialOptions *options, double *d_out,
                                 PeecAssemblyStats *stats);
+
+/* ---- dense factorisations of device-resident matrices (in place) ----
+ * Same algorithm, numerics and error codes as lu_factorize /
+ * complex_lu_factorize.  d_piv (n int64) receives the pivot rows, d_perm (n
+ * int32) the combined row permutation the solves use.  failed_column is the
+ * column of a singular pivot, or -1. */
+int peec_gb300_lu_factor_device(double *d_a, size_t n, double pivot_tolerance,
+                                long long *d_piv, int *d_perm, double *matrix_scale,
+                                int *failed_column);
+int peec_gb300_complex_lu_factor_device(Complex *d_a, size_t n, double pivot_tolerance,
+                                        long long *d_piv, int *d_perm,
+                                        double *d_row_scale, double *d_column_scale,
+                                        double *matrix_scale, int *failed_column);
+/* nrhs right-hand sides stored one after another; d_b != d_x. */
+int peec_gb300_lu_solve_device(const double *d_lu, const int *d_perm, size_t n,
+                               const double *d_b, double *d_x, size_t nrhs);
+int peec_gb300_complex_lu_solve_device(const Complex *d_lu, const int *d_perm,
+                                       const double *d_row_scale,
+                                       const double *d_column_scale, size_t n,
+                                       const Complex *d_b, Complex *d_x, size_t nrhs);
+
+/* ---- harmonic system on the device ----
+ * Z = [R + j w L, A; -P A^T, j w I] (N = Ne + Nv) from device Lp, P and the
+ * edge list (2*Ne int32, a -> b); d_R (Ne diagonal) may be NULL for PEC.
+ * Mirrors the reference's harmonic_build_system. */
+int peec_gb300_harmonic_build_device(const double *d_L, const double *d_P,
+                                     const int *d_edges, const double *d_R,
+                                     size_t n_edges, size_t n_nodes, double frequency,
+                                     Complex *d_Z);
+/* [-U_e; 0] for a unit plane wave e_hat exp(-j k0 k_hat.r), U_e the field at
+ * the edge centre projected on the edge vector times sinc(k0 k_hat.l / 2). */
+int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
+                                     const double *d_edge_vectors, size_t n_edges,
+                                     size_t n_nodes, const double k_hat[3],
+                                     const double e_hat[3], double wave_number,
+                                     Complex *d_rhs);
+/* out[0] = max_i |r_i| / (sum_j |Z_ij||x_j| + |b_i|) over all right-hand
+ * sides, out[1] = max |r_i|, out[2] = max |b_i|. */
+int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x,
+                                     const Complex *d_b, size_t nrhs, double out[3]);
 
 #ifdef __cplusplus
 }

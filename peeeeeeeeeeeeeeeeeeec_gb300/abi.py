@@ -173,6 +173,7 @@ EXT_SYMBOLS = [
     ("peec_gb300_host_free_pinned", None, [C.c_void_p]),
     ("peec_gb300_copy_to_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     ("peec_gb300_copy_to_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    ("peec_gb300_copy_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     ("peec_gb300_synchronize", C.c_int, []),
     ("peec_gb300_event_record", C.c_void_p, []),
     ("peec_gb300_event_elapsed_ms", C.c_double, [C.c_void_p, C.c_void_p]),
@@ -181,6 +182,24 @@ EXT_SYMBOLS = [
      [P(Mesh), P(DualMesh), P(InductanceOptions), C.c_void_p, P(PeecAssemblyStats)]),
     ("peec_gb300_potential_device", C.c_int,
      [P(Mesh), P(DualMesh), P(PotentialOptions), C.c_void_p, P(PeecAssemblyStats)]),
+    ("peec_gb300_lu_factor_device", C.c_int,
+     [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, c_double_p, c_int_p]),
+    ("peec_gb300_complex_lu_factor_device", C.c_int,
+     [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+      c_double_p, c_int_p]),
+    ("peec_gb300_lu_solve_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t]),
+    ("peec_gb300_complex_lu_solve_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+      C.c_size_t]),
+    ("peec_gb300_harmonic_build_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_double,
+      C.c_void_p]),
+    ("peec_gb300_plane_wave_rhs_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_double_p, c_double_p, C.c_double,
+      C.c_void_p]),
+    ("peec_gb300_backward_error_device", C.c_int,
+     [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, c_double_p]),
 ]
 
 MESH_SYMBOLS = [

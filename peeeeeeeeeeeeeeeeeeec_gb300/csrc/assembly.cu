@@ -229,11 +229,20 @@ __device__ double tri_potential(const TriPot &t, const double *r) {
     double acc = 0.0;
     for (int i = 0; i < 3; ++i) {
         double d = dot3(v[i], t.outw[i]);
-        if (d == 0.0) continue;
+        if (d == 0.0) continue;  // finite limit d log(.) = 0, as the reference
+        // Edge integral asinh((s+L)/q) - asinh(s/q), q = hypot(d, h), written
+        // as log(A2/A1) with A = s + sqrt(s^2 + q^2) = s + |r - p| (the
+        // distances to the edge's end points are already in rad[]); for
+        // s < 0 the equivalent q^2 / (|r - p| - s) avoids the cancellation.
+        // One log instead of two asinh and a hypot; equal to within
+        // rounding.
         double s = dot3(v[i], t.unit[i]);
-        double q = hypot(d, h);
-        double e = asinh((s + t.len[i]) / q) - asinh(s / q);
-        acc += d * e;
+        double s2 = s + t.len[i];
+        double q2 = d * d + h * h;
+        double r1 = rad[i], r2 = rad[(i + 1) % 3];
+        double a1 = s >= 0.0 ? s + r1 : q2 / (r1 - s);
+        double a2 = s2 >= 0.0 ? s2 + r2 : q2 / (r2 - s2);
+        acc += d * log(a2 / a1);
     }
     if (h != 0.0) {
         double c[3];
@@ -478,7 +487,7 @@ struct TileArgs {
     double *out;  // n*n row-major
     int n;
     int only_a, only_b;
-    unsigned long long *err;  // min over failing entries of (a*n+b)+1, 0 = none
+    unsigned long long *err;  // min over failing entries of a*n+b; ~0ull = none
 };
 
 static const int kTile = 32;
@@ -497,7 +506,7 @@ __device__ __forceinline__ double far_pair(const FarPt *pa, const FarPt *pb, int
             FarPt B = pb[q];
             double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
             double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
-            if (r2 > 0.0) s = fma(B.w, rsqrt(r2), s);
+            if (!(r2 <= 0.0)) s = fma(B.w, rsqrt(r2), s);  // NaN propagates, as the reference's R <= 0 test
         }
         acc = fma(A.w, s, acc);
     }
@@ -572,7 +581,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                 if (!isfinite(val)) bad = true;
             }
             if (bad) {
-                if (lane == 0) atomicMin(T.err, (unsigned long long)a * (unsigned long long)n + b + 1ull);
+                if (lane == 0) atomicMin(T.err, (unsigned long long)a * (unsigned long long)n + b);
                 val = 0.0;
             }
         }
@@ -713,7 +722,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     DBuf<int> count(np + 1), near_off(np + 1), counter(1);
     DBuf<unsigned long long> err(1), evals(1);
     if ((np && (!pts.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p) return -1;
-    cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), stream());
+    cudaMemsetAsync(err.p, 0xff, sizeof(unsigned long long), stream());
     cudaMemsetAsync(evals.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
     if (np) {
@@ -797,8 +806,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         stats->ms_far = t23;
     }
     for (auto &ev_ : ev) cudaEventDestroy(ev_);
-    if (e) {
-        *bad_entry = (long long)(e - 1);
+    if (e != ~0ull) {
+        *bad_entry = (long long)e;
         return -1;
     }
     return 0;

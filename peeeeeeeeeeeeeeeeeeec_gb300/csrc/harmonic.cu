@@ -1,0 +1,160 @@
+// Device-resident harmonic system around the hot path: the MNA fill that
+// consumes Lp and P, a plane-wave right-hand side, and the componentwise
+// backward error that gates every solve.
+//
+// Reference (paths inside the reference project):
+//   src/solver/harmonic.c:175-372    harmonic_build_system
+//       Z = [ R + j w L     A    ]      A[e,a] = -1, A[e,b] = +1 (incidence.c:34-110)
+//           [ -P A^T      j w I  ]      (P A^T)[i,e] = P[i,b] - P[i,a] (incidence.c:417-592)
+//   src/solver/harmonic.c:436-552    harmonic_build_rhs: [-U_e ; P I_s]
+//   src/physics/scattering.c:263-336 U_e = (E(r_c) . l) sinc(k_hat.l k0 / 2)
+//   src/solver/harmonic.c:720-1080   backward error max_i |r_i| / (sum_j |Z_ij||x_j| + |b_i|)
+// All byte-bound: one pass over Z per kernel.
+#include <math.h>
+
+#include "../../include/complex_matrix.h"
+#include "../../include/peec_gb300.h"
+#include "common.cuh"
+
+namespace peec {
+
+struct cpx {
+    double re, im;
+};
+
+// One thread per entry of row-block rows; coalesced 16-byte stores.
+__global__ void k_harmonic_fill(const double *L, const double *P, const int *edges, const double *R, int ne, int nv,
+                                double omega, cpx *Z) {
+    const long long n = (long long)ne + nv;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n * n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t / n), j = (int)(t % n);
+        cpx z = {0.0, 0.0};
+        if (i < ne) {
+            if (j < ne) {
+                z.re = (i == j && R) ? R[i] : 0.0;
+                z.im = omega * L[(size_t)i * ne + j];
+            } else {
+                int k = j - ne;
+                z.re = (k == edges[2 * i]) ? -1.0 : (k == edges[2 * i + 1]) ? 1.0 : 0.0;
+            }
+        } else {
+            int r = i - ne;
+            if (j < ne) {
+                int a = edges[2 * j], b = edges[2 * j + 1];
+                const double *prow = P + (size_t)r * nv;
+                z.re = -(prow[b] - prow[a]);
+            } else if (j - ne == r) {
+                z.im = omega;
+            }
+        }
+        Z[t] = z;
+    }
+}
+
+// U_e for a unit plane wave E(r) = e_hat exp(-j k0 k_hat.r): field at the
+// edge centre projected on the edge vector, times sinc(q/2), q = k0 k_hat.l;
+// the right-hand side is [-U_e ; 0].
+__global__ void k_plane_wave_rhs(const double *centers, const double *vectors, int ne, int nv, double kx, double ky,
+                                 double kz, double ex, double ey, double ez, double k0, cpx *rhs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ne + nv) return;
+    if (i >= ne) {
+        rhs[i] = cpx{0.0, 0.0};
+        return;
+    }
+    const double *c = centers + 3 * i, *l = vectors + 3 * i;
+    double phase = -k0 * (kx * c[0] + ky * c[1] + kz * c[2]);
+    double s, co;
+    sincos(phase, &s, &co);
+    double proj = ex * l[0] + ey * l[1] + ez * l[2];
+    double q = k0 * (kx * l[0] + ky * l[1] + kz * l[2]);
+    double h = 0.5 * q;
+    double sinc = fabs(h) < 1e-8 ? 1.0 - h * h / 6.0 : sin(h) / h;
+    rhs[i] = cpx{-proj * co * sinc, -proj * s * sinc};
+}
+
+// Componentwise backward error, one warp per row; results as IEEE bits
+// (non-negative) max-reduced: out[0] = backward error, out[1] = max |r_i|,
+// out[2] = max |b_i|.
+__global__ void k_backward_error(const cpx *Z, const cpx *x, const cpx *b, int n, int nrhs,
+                                 unsigned long long *out) {
+    long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= (long long)n * nrhs) return;
+    int rr = (int)(warp / n), i = (int)(warp % n);
+    const cpx *row = Z + (size_t)i * n;
+    const cpx *xr = x + (size_t)rr * n;
+    double yr = 0.0, yi = 0.0, den = 0.0;
+    for (int j = lane; j < n; j += 32) {
+        cpx z = row[j], v = xr[j];
+        yr = fma(z.re, v.re, yr);
+        yr = fma(-z.im, v.im, yr);
+        yi = fma(z.re, v.im, yi);
+        yi = fma(z.im, v.re, yi);
+        den = fma(hypot(z.re, z.im), hypot(v.re, v.im), den);
+    }
+    yr = warp_sum(yr);
+    yi = warp_sum(yi);
+    den = warp_sum(den);
+    if (lane == 0) {
+        cpx bi = b[(size_t)rr * n + i];
+        double res = hypot(yr - bi.re, yi - bi.im);
+        double babs = hypot(bi.re, bi.im);
+        den += babs;
+        double eta = den > 0.0 ? res / den : res;
+        if (!isfinite(eta)) eta = INFINITY;
+        atomicMax(out + 0, (unsigned long long)__double_as_longlong(eta));
+        atomicMax(out + 1, (unsigned long long)__double_as_longlong(isfinite(res) ? res : INFINITY));
+        atomicMax(out + 2, (unsigned long long)__double_as_longlong(babs));
+    }
+}
+
+}  // namespace peec
+
+using namespace peec;
+
+extern "C" {
+
+int peec_gb300_harmonic_build_device(const double *d_L, const double *d_P, const int *d_edges,
+                                     const double *d_R, size_t n_edges, size_t n_nodes, double frequency,
+                                     Complex *d_Z) {
+    if (!d_L || !d_P || !d_edges || !d_Z || n_edges == 0 || n_nodes == 0 || !isfinite(frequency) ||
+        frequency <= 0.0)
+        return -1;
+    double omega = 2.0 * M_PI * frequency;
+    long long n = (long long)(n_edges + n_nodes);
+    long long total = n * n;
+    int grid = (int)((total + 255) / 256 < 152LL * 32 ? (total + 255) / 256 : 152LL * 32);
+    PEEC_LAUNCH(k_harmonic_fill, grid, 256, 0, d_L, d_P, d_edges, d_R, (int)n_edges, (int)n_nodes, omega,
+                (cpx *)d_Z);
+    return launch_ok("harmonic fill") ? 0 : -1;
+}
+
+int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers, const double *d_edge_vectors, size_t n_edges,
+                                     size_t n_nodes, const double k_hat[3], const double e_hat[3],
+                                     double wave_number, Complex *d_rhs) {
+    if (!d_edge_centers || !d_edge_vectors || !k_hat || !e_hat || !d_rhs) return -1;
+    int n = (int)(n_edges + n_nodes);
+    PEEC_LAUNCH(k_plane_wave_rhs, (n + 255) / 256, 256, 0, d_edge_centers, d_edge_vectors, (int)n_edges,
+                (int)n_nodes, k_hat[0], k_hat[1], k_hat[2], e_hat[0], e_hat[1], e_hat[2], wave_number, (cpx *)d_rhs);
+    return launch_ok("plane-wave rhs") ? 0 : -1;
+}
+
+int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x, const Complex *d_b,
+                                     size_t nrhs, double out[3]) {
+    if (!d_Z || !d_x || !d_b || !out || n == 0 || nrhs == 0) return -1;
+    DBuf<unsigned long long> acc(3);
+    if (!acc.p) return -1;
+    cudaMemsetAsync(acc.p, 0, 3 * sizeof(unsigned long long), stream());
+    long long warps = (long long)n * nrhs;
+    PEEC_LAUNCH(k_backward_error, (unsigned)((warps * 32 + 255) / 256), 256, 0, (const cpx *)d_Z, (const cpx *)d_x,
+                (const cpx *)d_b, (int)n, (int)nrhs, acc.p);
+    unsigned long long h[3];
+    cudaMemcpyAsync(h, acc.p, sizeof(h), cudaMemcpyDeviceToHost, stream());
+    if (!sync("backward error")) return -1;
+    for (int k = 0; k < 3; ++k) memcpy(&out[k], &h[k], sizeof(double));
+    return 0;
+}
+
+}  // extern "C"

@@ -373,13 +373,17 @@ __global__ void k_col_scale(cplx *a, int n, double *col_scale, Status *st) {
 // ---- solves ------------------------------------------------------------
 // permutation of the sequential swaps (lu.c:494-510), one thread in shared
 // memory: perm[i] = source row of position i after all swaps.
-__global__ void k_perm(const long long *piv, int n, int *perm) {
+// Runs only after a successful factorisation (st == nullptr or code 0):
+// after a singular pivot the later pivot entries were never written.
+__global__ void k_perm(const long long *piv, int n, int *perm, const Status *st) {
     extern __shared__ int sp[];
+    if (st && st->code != 0) return;
     for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
     __syncthreads();
     if (threadIdx.x == 0)
         for (int k = 0; k < n; ++k) {
-            int p = (int)piv[k];
+            long long pl = piv[k];
+            int p = (pl >= k && pl < n) ? (int)pl : k;  // pivots are rows k..n-1
             if (p != k) {
                 int t = sp[k];
                 sp[k] = sp[p];
@@ -652,6 +656,54 @@ void lu_free(LUFactorization *lu) {
 
 namespace peec {
 
+// Equilibrate (complex), scale, factor and build the solve permutation of a
+// device-resident matrix in place.  Returns -1 on a CUDA failure, else 0
+// with *hs holding the device status (code 0 ok) and *scale max|A| (NaN
+// ignored).  A zero / non-finite complex row or column gives hs->code 4/5
+// before any factorisation.
+template <class T>
+static int factor_inplace(T *d_a, int n, double pivot_tolerance, bool cx, long long *d_piv, int *d_perm,
+                          double *d_row, double *d_col, double *scale, Status *hs) {
+    size_t nn = (size_t)n * n;
+    DBuf<Status> st(1);
+    DBuf<unsigned long long> mx(1);
+    if (!st.p || !mx.p) return -1;
+    cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
+    cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
+    if (cx) {
+        // complex_lu.c:275-302: row scales, then column scales of the row-scaled matrix
+        PEEC_LAUNCH(k_row_scale, (unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, (const cplx *)d_a, (cplx *)d_a, n,
+                    d_row, st.p);
+        PEEC_LAUNCH(k_col_scale, (n + 127) / 128, 128, 0, (cplx *)d_a, n, d_col, st.p);
+    }
+    PEEC_LAUNCH(k_max_mag<T>, 152 * 8, 256, 0, d_a, nn, mx.p);
+    unsigned long long bits = 0;
+    cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(hs, st.p, sizeof(Status), cudaMemcpyDeviceToHost, stream());
+    if (!sync("LU scale")) return -1;
+    memcpy(scale, &bits, sizeof(double));
+    if (hs->code != 0 || !isfinite(*scale) || *scale <= 0.0) return 0;
+    double limit = pivot_tolerance * *scale;
+    if (!factor_device<T>(d_a, n, limit, d_piv, st.p)) return -1;
+    size_t perm_smem = (size_t)n * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, d_piv, n, d_perm, st.p);
+    cudaMemcpyAsync(hs, st.p, sizeof(Status), cudaMemcpyDeviceToHost, stream());
+    if (!launch_ok("LU permutation") || !sync("LU factorisation")) return -1;
+    return 0;
+}
+
+static void report_status(const Status &hs, bool cx) {
+    if (hs.code == 2)
+        fprintf(stderr, cx ? "ERROR: complex LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n"
+                           : "ERROR: LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n",
+                hs.column, hs.value);
+    else if (hs.code == 3)
+        fprintf(stderr, cx ? "ERROR: invalid complex U diagonal at [%d,%d], |Uii| = %.9e.\n"
+                           : "ERROR: invalid diagonal U[%d,%d] = %.9e.\n",
+                hs.column, hs.column, hs.value);
+}
+
 // Shared host driver for both factorisations.  On success the factor stays
 // resident on the device (registry) for the solves.
 template <class T>
@@ -670,45 +722,25 @@ static int factorize_common(const T *input, size_t n, double pivot_tolerance, bo
         r.d_row = (double *)dalloc(n * sizeof(double));
         r.d_col = (double *)dalloc(n * sizeof(double));
     }
-    DBuf<Status> st(1);
-    DBuf<unsigned long long> mx(1);
-    DBuf<T> staging;
-    bool ok = r.d_lu && r.d_piv && r.d_perm && st.p && mx.p && (!cx || (r.d_row && r.d_col));
-    if (ok && cx) ok = staging.alloc(nn);
-    if (!ok) {
+    if (!r.d_lu || !r.d_piv || !r.d_perm || (cx && (!r.d_row || !r.d_col))) {
         release(r);
         return -1;
     }
     T *d_a = (T *)r.d_lu;
-    cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
-    cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
-    if (!cuda_ok(cudaMemcpyAsync(cx ? staging.p : d_a, input, nn * sizeof(T), cudaMemcpyHostToDevice, stream()),
-                 "LU upload")) {
+    if (!cuda_ok(cudaMemcpyAsync(d_a, input, nn * sizeof(T), cudaMemcpyHostToDevice, stream()), "LU upload")) {
         release(r);
         return -1;
     }
-    if (cx) {
-        // complex_lu.c:275-302: row scales, then column scales of the row-scaled matrix
-        PEEC_LAUNCH(k_row_scale, (unsigned)(((size_t)ni * 32 + 255) / 256), 256, 0, (const cplx *)staging.p,
-                    (cplx *)d_a, ni, r.d_row, st.p);
-        PEEC_LAUNCH(k_col_scale, (ni + 127) / 128, 128, 0, (cplx *)d_a, ni, r.d_col, st.p);
-    }
-    PEEC_LAUNCH(k_max_mag<T>, 152 * 8, 256, 0, d_a, nn, mx.p);
-    unsigned long long bits = 0;
     Status hs;
-    cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
-    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
-    if (!sync("LU scale")) {
+    double scale = 0.0;
+    if (factor_inplace<T>(d_a, ni, pivot_tolerance, cx, r.d_piv, r.d_perm, r.d_row, r.d_col, &scale, &hs) != 0) {
         release(r);
         return -1;
     }
-    staging.release();
-    if (hs.code != 0) {  // zero or non-finite row / column of the complex input
+    if (hs.code == 4 || hs.code == 5) {  // zero or non-finite row / column of the complex input
         release(r);
         return -2;
     }
-    double scale;
-    memcpy(&scale, &bits, sizeof(scale));
     *matrix_scale = scale;
     if (!isfinite(scale) || scale <= 0.0) {
         fprintf(stderr, cx ? "ERROR: complex LU input matrix is invalid or zero.\n"
@@ -716,23 +748,14 @@ static int factorize_common(const T *input, size_t n, double pivot_tolerance, bo
         release(r);
         return -2;
     }
-    double limit = pivot_tolerance * scale;
-    if (!factor_device<T>(d_a, ni, limit, r.d_piv, st.p)) {
-        release(r);
-        return -1;
-    }
-    size_t perm_smem = n * sizeof(int);
-    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
-    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, ni, r.d_perm);
     std::vector<long long> piv(n);
-    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
     bool copied = cuda_ok(cudaMemcpyAsync(host_lu, d_a, nn * sizeof(T), cudaMemcpyDeviceToHost, stream()), "LU download") &&
                   cuda_ok(cudaMemcpyAsync(piv.data(), r.d_piv, n * sizeof(long long), cudaMemcpyDeviceToHost, stream()),
                           "pivot download");
     if (cx && copied)
         copied = cuda_ok(cudaMemcpyAsync(row_scale, r.d_row, n * sizeof(double), cudaMemcpyDeviceToHost, stream()), "scale") &&
                  cuda_ok(cudaMemcpyAsync(col_scale, r.d_col, n * sizeof(double), cudaMemcpyDeviceToHost, stream()), "scale");
-    if (!sync("LU factorisation") || !copied) {
+    if (!sync("LU download") || !copied) {
         release(r);
         return -1;
     }
@@ -744,14 +767,7 @@ static int factorize_common(const T *input, size_t n, double pivot_tolerance, bo
     }
     *swap_count = swaps;
     if (hs.code != 0) {
-        if (hs.code == 2)
-            fprintf(stderr, cx ? "ERROR: complex LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n"
-                               : "ERROR: LU matrix is singular or nearly singular at column %d, |pivot| = %.9e.\n",
-                    hs.column, hs.value);
-        else
-            fprintf(stderr, cx ? "ERROR: invalid complex U diagonal at [%d,%d], |Uii| = %.9e.\n"
-                               : "ERROR: invalid diagonal U[%d,%d] = %.9e.\n",
-                    hs.column, hs.column, hs.value);
+        report_status(hs, cx);
         release(r);
         return -2;
     }
@@ -801,7 +817,7 @@ static bool resident_for(const T *data, const size_t *pivots, const double *rs, 
              cuda_ok(cudaMemcpyAsync(r.d_col, cs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload");
     size_t perm_smem = n * sizeof(int);
     if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
-    if (ok) PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, (int)n, r.d_perm);
+    if (ok) PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, (int)n, r.d_perm, (const Status *)nullptr);
     if (!ok || !sync("factor upload")) {
         release(r);
         return false;
@@ -977,6 +993,67 @@ void complex_lu_print_info(const ComplexLUFactorization *lu) {
     if (lu->data && lu->n > 0)
         printf("LU memory    : %.3f MiB\n", ((double)lu->n * (double)lu->n * sizeof(Complex)) / (1024.0 * 1024.0));
     printf("========================================\n");
+}
+
+}  // extern "C"
+
+// =====================================================================
+// extension: factor / solve matrices that already live on the device
+// =====================================================================
+extern "C" {
+
+int peec_gb300_lu_factor_device(double *d_a, size_t n, double pivot_tolerance, long long *d_piv, int *d_perm,
+                                double *matrix_scale, int *failed_column) {
+    if (!d_a || !d_piv || !d_perm || n == 0 || n > (size_t)0x7fffffff) return -1;
+    Status hs;
+    double scale = 0.0;
+    if (factor_inplace<double>(d_a, (int)n, pivot_tolerance, false, d_piv, d_perm, nullptr, nullptr, &scale, &hs) != 0)
+        return -1;
+    if (matrix_scale) *matrix_scale = scale;
+    if (failed_column) *failed_column = hs.code ? hs.column : -1;
+    if (!isfinite(scale) || scale <= 0.0) return -2;
+    if (hs.code) {
+        report_status(hs, false);
+        return -2;
+    }
+    return 0;
+}
+
+int peec_gb300_complex_lu_factor_device(Complex *d_a, size_t n, double pivot_tolerance, long long *d_piv, int *d_perm,
+                                        double *d_row_scale, double *d_column_scale, double *matrix_scale,
+                                        int *failed_column) {
+    if (!d_a || !d_piv || !d_perm || !d_row_scale || !d_column_scale || n == 0 || n > (size_t)0x7fffffff) return -1;
+    Status hs;
+    double scale = 0.0;
+    if (factor_inplace<cplx>((cplx *)d_a, (int)n, pivot_tolerance, true, d_piv, d_perm, d_row_scale, d_column_scale,
+                             &scale, &hs) != 0)
+        return -1;
+    if (matrix_scale) *matrix_scale = scale;
+    if (failed_column) *failed_column = hs.code ? hs.column : -1;
+    if (hs.code == 4 || hs.code == 5 || !isfinite(scale) || scale <= 0.0) return -2;
+    if (hs.code) {
+        report_status(hs, true);
+        return -2;
+    }
+    return 0;
+}
+
+int peec_gb300_lu_solve_device(const double *d_lu, const int *d_perm, size_t n, const double *d_b, double *d_x,
+                               size_t nrhs) {
+    if (!d_lu || !d_perm || !d_b || !d_x || n == 0 || nrhs == 0 || d_b == d_x) return -1;
+    if (!solve_device<double>(d_lu, d_perm, nullptr, nullptr, (int)n, d_b, d_x, (int)nrhs)) return -1;
+    return 0;
+}
+
+int peec_gb300_complex_lu_solve_device(const Complex *d_lu, const int *d_perm, const double *d_row_scale,
+                                       const double *d_column_scale, size_t n, const Complex *d_b, Complex *d_x,
+                                       size_t nrhs) {
+    if (!d_lu || !d_perm || !d_row_scale || !d_column_scale || !d_b || !d_x || n == 0 || nrhs == 0 || d_b == d_x)
+        return -1;
+    if (!solve_device<cplx>((const cplx *)d_lu, d_perm, d_row_scale, d_column_scale, (int)n, (const cplx *)d_b,
+                            (cplx *)d_x, (int)nrhs))
+        return -1;
+    return 0;
 }
 
 }  // extern "C"

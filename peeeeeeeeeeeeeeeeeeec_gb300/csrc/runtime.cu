@@ -107,6 +107,10 @@ int peec_gb300_copy_to_host(void *dst, const void *src, size_t bytes) {
     return peec::sync("copy") ? 0 : -1;
 }
 
+int peec_gb300_copy_device(void *dst, const void *src, size_t bytes) {
+    return peec::cuda_ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, peec::stream()), "copy") ? 0 : -1;
+}
+
 void *peec_gb300_host_alloc_pinned(size_t bytes) {
     void *p = nullptr;
     if (!peec::cuda_ok(cudaMallocHost(&p, bytes ? bytes : 1), "pinned allocation")) return nullptr;
