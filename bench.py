@@ -208,6 +208,11 @@ class DeviceSolve:
         names = ["assemble_Lp", "assemble_P", "mna_fill", "complex_lu", "rhs_solve", "backward_error"]
         for k, name in enumerate(names):
             self.phase_ms.setdefault(name, []).append(lib.peec_gb300_event_elapsed_ms(ev[k], ev[k + 1]))
+        for tag, st in (("Lp", self.stL), ("P", self.stP)):
+            for f in ("ms_prepare", "ms_near", "ms_far"):
+                self.phase_ms.setdefault(tag + "_" + f[3:], []).append(getattr(st, f))
+        self.work = {"Lp_near_pairs": self.stL.near_pairs, "Lp_potential_evals": self.stL.potential_evaluations,
+                     "P_near_pairs": self.stP.near_pairs, "P_potential_evals": self.stP.potential_evaluations}
         for e in ev:
             lib.peec_gb300_event_destroy(e)
         return out[0]
@@ -415,7 +420,7 @@ def main():
                            "Nv": m.n_nodes, "frequency_hz": FREQ, "parallelism": "replicas" if world > 1 else "1gpu",
                            "l2": "inputs larger than L2 (Z is %.2f GB)" % ((m.n_edges + m.n_nodes) ** 2 * 16 / 1e9),
                            "retardation": "none (quasi-static, as the reference)"},
-                "phase_ms": phases, "backward_error": max(bes), "gpu_launches": int(launches),
+                "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
                 "roofline": roofline(phases, m)}
         print(json.dumps(line))

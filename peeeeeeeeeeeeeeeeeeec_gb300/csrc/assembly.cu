@@ -81,6 +81,17 @@ struct alignas(32) FarPt {
     double x, y, z, w;
 };
 
+// The same point as unevaluated float pairs (hi + lo == the double to 2^-48
+// relative): the far rule runs on the FP32 pipes in double-float arithmetic.
+struct alignas(32) FarPtF {
+    float xh, yh, zh, wh, xl, yl, zl, wl;
+};
+
+__device__ __forceinline__ void split_df(double v, float &h, float &l) {
+    h = __double2float_rn(v);
+    l = __double2float_rn(v - (double)h);
+}
+
 struct NearRec {
     int i, j, cls, pad;
 };
@@ -99,7 +110,7 @@ __global__ void k_patch_prep(RegionsDev R) {
 // Far-rule points of patch p: triangle t (0: corners 0,1,2; 1: 0,2,3), point
 // (iu, iv) at index t*q*q + iu*q + iv; weight (0.5 w_iu)(0.5 w_iv) J
 // (reference quadrature.c:679-783 evaluates the same points per pair).
-__global__ void k_far_points(RegionsDev R, int q, int row, FarPt *pts) {
+__global__ void k_far_points(RegionsDev R, int q, int row, FarPt *pts, FarPtF *ptf) {
     int np = R.np, per = 2 * q * q;
     long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)np * per) return;
@@ -111,7 +122,14 @@ __global__ void k_far_points(RegionsDev R, int q, int row, FarPt *pts) {
     double v = 0.5 * (c_gl_x[row][iv] + 1.0), wv = 0.5 * c_gl_w[row][iv];
     double r[3], jac;
     tri_map(p0, p1, p2, u, v, r, &jac);
-    pts[g] = FarPt{r[0], r[1], r[2], wu * wv * jac};
+    double w = wu * wv * jac;
+    pts[g] = FarPt{r[0], r[1], r[2], w};
+    FarPtF f;
+    split_df(r[0], f.xh, f.xl);
+    split_df(r[1], f.yh, f.yl);
+    split_df(r[2], f.zh, f.zl);
+    split_df(w, f.wh, f.wl);
+    ptf[g] = f;
 }
 
 // ---------------------------------------------------------------------
@@ -230,19 +248,27 @@ __device__ double tri_potential(const TriPot &t, const double *r) {
     for (int i = 0; i < 3; ++i) {
         double d = dot3(v[i], t.outw[i]);
         if (d == 0.0) continue;  // finite limit d log(.) = 0, as the reference
-        // Edge integral asinh((s+L)/q) - asinh(s/q), q = hypot(d, h), written
-        // as log(A2/A1) with A = s + sqrt(s^2 + q^2) = s + |r - p| (the
-        // distances to the edge's end points are already in rad[]); for
-        // s < 0 the equivalent q^2 / (|r - p| - s) avoids the cancellation.
-        // One log instead of two asinh and a hypot; equal to within
-        // rounding.
+        // Edge integral asinh((s+L)/q) - asinh(s/q), q = hypot(d, h), as
+        // log(A2/A1) with A = s + sqrt(s^2 + q^2) (= q e^asinh(s/q)); for
+        // s < 0 the equal form q^2 / (sqrt(s^2 + q^2) - s) avoids the
+        // cancellation.  The square roots use the same s and q as the
+        // asinh arguments (not the vertex distances, which disagree by
+        // rounding when the point lies on the edge's line).  One log and two
+        // square roots instead of two asinh and a hypot.
         double s = dot3(v[i], t.unit[i]);
         double s2 = s + t.len[i];
         double q2 = d * d + h * h;
-        double r1 = rad[i], r2 = rad[(i + 1) % 3];
-        double a1 = s >= 0.0 ? s + r1 : q2 / (r1 - s);
-        double a2 = s2 >= 0.0 ? s2 + r2 : q2 / (r2 - s2);
-        acc += d * log(a2 / a1);
+        double e;
+        if (q2 > 1e-280) {
+            double r1 = sqrt(fma(s, s, q2)), r2 = sqrt(fma(s2, s2, q2));
+            double a1 = s >= 0.0 ? s + r1 : q2 / (r1 - s);
+            double a2 = s2 >= 0.0 ? s2 + r2 : q2 / (r2 - s2);
+            e = log(a2 / a1);
+        } else {  // q^2 underflows: the reference's form
+            double q = hypot(d, h);
+            e = asinh(s2 / q) - asinh(s / q);
+        }
+        acc += d * e;
     }
     if (h != 0.0) {
         double c[3];
@@ -375,7 +401,7 @@ struct NearEvalArgs {
 
 // One warp per job (record, triangle pair t = s*2+u, direction d); warps
 // fetch jobs dynamically because refinement depth varies a lot.
-__global__ void __launch_bounds__(256) k_near_eval(NearEvalArgs A) {
+__global__ void __launch_bounds__(256, 2) k_near_eval(NearEvalArgs A) {
     extern __shared__ unsigned char smem_raw[];
     NearWarpSmem *all = reinterpret_cast<NearWarpSmem *>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -480,7 +506,9 @@ struct TileArgs {
     int kind;
     double dir_tol;
     const FarPt *pts;
+    const FarPtF *ptf;
     int npts;
+    int far_df;  // 1: double-float far rule, 0: FP64
     const int *near_off;
     const NearRec *near_rec;
     const double2 *near_k;
@@ -495,7 +523,9 @@ static const int kTileWarps = 8;
 
 // far-rule integral of one patch pair, all 4 triangle pairs at once:
 // sum_p W_p sum_q W_q / |r_p - r_q| over the 2q^2 points of each patch
-__device__ __forceinline__ double far_pair(const FarPt *pa, const FarPt *pb, int npts) {
+// (reference quadrature.c:679-783 sums the same products per triangle pair).
+// FP64 form: kept for comparison runs (PEEC_GB300_FAR=fp64).
+__device__ __forceinline__ double far_pair_fp64(const FarPt *pa, const FarPt *pb, int npts) {
     const int lane = threadIdx.x & 31;
     double acc = 0.0;
     for (int p = lane; p < npts; p += 32) {
@@ -509,6 +539,83 @@ __device__ __forceinline__ double far_pair(const FarPt *pa, const FarPt *pb, int
             if (!(r2 <= 0.0)) s = fma(B.w, rsqrt(r2), s);  // NaN propagates, as the reference's R <= 0 test
         }
         acc = fma(A.w, s, acc);
+    }
+    return warp_sum(acc);
+}
+
+// ---- double-float arithmetic (Dekker / Knuth error-free transforms) ----
+// The library is built without implicit FMA contraction, so a + b and a * b
+// below round exactly as written; fmaf() is explicit.
+struct f2 {
+    float h, l;
+};
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+    float s = a + b, v = s - a;
+    return f2{s, (a - (s - v)) + (b - v)};
+}
+__device__ __forceinline__ f2 quick_two_sum(float a, float b) {  // |a| >= |b|
+    float s = a + b;
+    return f2{s, b - (s - a)};
+}
+__device__ __forceinline__ f2 df_sub(f2 a, f2 b) {
+    f2 s = two_sum(a.h, -b.h);
+    return quick_two_sum(s.h, s.l + (a.l - b.l));
+}
+__device__ __forceinline__ f2 df_add(f2 a, f2 b) {
+    f2 s = two_sum(a.h, b.h);
+    return quick_two_sum(s.h, s.l + (a.l + b.l));
+}
+__device__ __forceinline__ f2 df_sqr(f2 a) {
+    float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(a.h + a.h, a.l, e);
+    return quick_two_sum(p, e);
+}
+__device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return quick_two_sum(p, e);
+}
+// 1/sqrt(x) for x > 0 to ~1e-14 relative: hardware rsqrtf seed y, residual
+// r = 1 - x y^2 in double-float, one Halley step y (1 + r/2 + 3 r^2 / 8)
+// (third-order convergence from the 2^-22 seed).
+__device__ __forceinline__ f2 df_rsqrt(f2 x) {
+    float y = rsqrtf(x.h);
+    float yy = y * y;
+    f2 y2 = f2{yy, fmaf(y, y, -yy)};
+    f2 t = df_mul(x, y2);
+    float r = (1.0f - t.h) - t.l;
+    float c = y * fmaf(0.375f * r, r, 0.5f * r);
+    return quick_two_sum(y, c);
+}
+
+// Double-float form of the same sum: every point difference, square, the
+// reciprocal square root and the accumulation carry ~48 significant bits,
+// on the FP32 pipes; per-lane partial sums are combined in FP64.
+__device__ __forceinline__ double far_pair_df(const FarPtF *pa, const FarPtF *pb, int npts) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (int p = lane; p < npts; p += 32) {
+        FarPtF A = pa[p];
+        f2 ax = {A.xh, A.xl}, ay = {A.yh, A.yl}, az = {A.zh, A.zl};
+        f2 s = {0.0f, 0.0f};
+        bool bad = false;
+#pragma unroll 2
+        for (int q = 0; q < npts; ++q) {
+            FarPtF B = pb[q];
+            f2 dx = df_sub(ax, f2{B.xh, B.xl});
+            f2 dy = df_sub(ay, f2{B.yh, B.yl});
+            f2 dz = df_sub(az, f2{B.zh, B.zl});
+            f2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+            if (r2.h <= 0.0f) continue;  // the reference skips R <= 0
+            if (!(r2.h == r2.h) || !(B.wh == B.wh)) bad = true;  // NaN, as the reference propagates it
+            s = df_add(s, df_mul(f2{B.wh, B.wl}, df_rsqrt(r2)));
+        }
+        double sd = (double)s.h + (double)s.l;
+        if (bad) sd = nan("");
+        acc = fma((double)A.wh + (double)A.wl, sd, acc);
     }
     return warp_sum(acc);
 }
@@ -565,7 +672,8 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                     for (int j = R.off[b]; j < R.off[b + 1]; ++j) {
                         double k;
                         if (!near_lookup(T, i, j, k))
-                            k = far_pair(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
+                            k = T.far_df ? far_pair_df(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts)
+                                         : far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
                         if (!isfinite(k)) {
                             bad = true;
                             break;
@@ -698,6 +806,17 @@ struct AssemblyOptions {
     double dir_tol;
 };
 
+// Far rule arithmetic: double-float on the FP32 pipes (default), or native
+// FP64 when PEEC_GB300_FAR=fp64 (for comparison runs).
+static int far_mode_df() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char *e = getenv("PEEC_GB300_FAR");
+        mode = (e && strcmp(e, "fp64") == 0) ? 0 : 1;
+    }
+    return mode;
+}
+
 static bool orders_valid(const AssemblyOptions &o) {
     for (int k = 0; k < 4; ++k)
         if (gl_row(o.orders[k]) < 0) return false;
@@ -719,15 +838,16 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     cudaEventRecord(ev[0], stream());
 
     DBuf<FarPt> pts((size_t)np * npts);
+    DBuf<FarPtF> ptf((size_t)np * npts);
     DBuf<int> count(np + 1), near_off(np + 1), counter(1);
     DBuf<unsigned long long> err(1), evals(1);
-    if ((np && (!pts.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p) return -1;
+    if ((np && (!pts.p || !ptf.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p) return -1;
     cudaMemsetAsync(err.p, 0xff, sizeof(unsigned long long), stream());
     cudaMemsetAsync(evals.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
     if (np) {
         long long tot = (long long)np * npts;
-        PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p);
+        PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p, ptf.p);
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
         PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 0, count.p, nullptr, nullptr);
         PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, count.p, near_off.p, np);
@@ -777,7 +897,9 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     T.kind = kind;
     T.dir_tol = o.dir_tol;
     T.pts = pts.p;
+    T.ptf = ptf.p;
     T.npts = npts;
+    T.far_df = far_mode_df();
     T.near_off = near_off.p;
     T.near_rec = rec.p;
     T.near_k = kval.p;

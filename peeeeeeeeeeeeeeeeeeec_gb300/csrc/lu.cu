@@ -176,6 +176,205 @@ __global__ void __launch_bounds__(1024) k_panel(T *a, int n, int k0, int kb, dou
     }
 }
 
+// ---- cooperative panel ------------------------------------------------
+// The panel (rows k0..n-1, columns k0..k0+kb-1) spread over G co-resident
+// CTAs, each holding a contiguous block of rows in shared memory, so the
+// rank-1 panel updates use every SM's FP64 units.  One grid barrier per
+// column: before it every CTA publishes its best candidate (value, row and
+// the candidate row's panel segment) and the owner of row k publishes row k;
+// after it every CTA picks the same pivot (first maximum wins), the two
+// owners exchange rows k and p, and all update their rows.  Publication
+// slots alternate by column parity so a CTA that runs ahead never
+// overwrites slots still being read.  The barrier spin is bounded: on
+// timeout the status word reports it and every CTA leaves.
+// loads that bypass L1 (other SMs wrote the data this barrier epoch)
+template <class T>
+__device__ __forceinline__ T ld_volatile(const T *p) {
+    if constexpr (sizeof(T) == 8) {
+        long long v = __ldcg(reinterpret_cast<const long long *>(p));
+        return *reinterpret_cast<T *>(&v);
+    } else if constexpr (sizeof(T) == 16) {
+        longlong2 v = __ldcg(reinterpret_cast<const longlong2 *>(p));
+        return *reinterpret_cast<T *>(&v);
+    } else {
+        int v = __ldcg(reinterpret_cast<const int *>(p));
+        return *reinterpret_cast<T *>(&v);
+    }
+}
+
+struct PanelSlots {
+    unsigned int count;
+    unsigned int gen;
+    int timeout;
+    int pad;
+};
+
+static const long long kSpinLimit = 1LL << 26;
+
+__device__ __forceinline__ bool grid_barrier(PanelSlots *ps, unsigned int nblocks, unsigned int &gen) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &ps->gen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&ps->count, 1u);
+        int ok = 1;
+        if (arrived == nblocks - 1) {
+            ps->count = 0;
+            __threadfence();
+            atomicExch(&ps->gen, gen + 1);
+        } else {
+            long long spins = 0;
+            while (*vgen == gen) {
+                if (++spins > kSpinLimit || *(volatile int *)&ps->timeout) {
+                    atomicExch(&ps->timeout, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    ++gen;
+    return s_ok;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb, int rows_per_cta, double limit,
+                                                    long long *piv, Status *st, PanelSlots *ps, double *cand_val,
+                                                    int *cand_idx, T *cand_row, T *krow) {
+    extern __shared__ unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);  // [rows_per_cta][NB]
+    __shared__ T s_prow[NB];
+    __shared__ double s_val[8];
+    __shared__ int s_idx[8];
+    __shared__ int s_p, s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned int G = gridDim.x;
+    const int c = blockIdx.x;
+    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform across CTAs (set before launch)
+    unsigned int gen = *(volatile unsigned int *)&ps->gen;  // stable between launches
+    for (int t = tid; t < nrows * kb; t += blockDim.x) {
+        int i = t / kb, j = t % kb;
+        tile[i * NB + j] = a[(size_t)(r0 + i) * n + k0 + j];
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk, par = kk & 1;
+        // local argmax over this CTA's rows i >= k (NaN below the diagonal
+        // never wins; a NaN diagonal becomes +inf and is rejected)
+        double best = -1.0;
+        int bi = n;
+        for (int i = max(r0, k) + tid; i < r1; i += blockDim.x) {
+            double m = mag(tile[(i - r0) * NB + kk]);
+            if (i == k && isnan(m)) m = INFINITY;
+            if (isnan(m)) continue;
+            if (m > best || (m == best && i < bi)) {
+                best = m;
+                bi = i;
+            }
+        }
+        for (int s = 16; s > 0; s >>= 1) {
+            double ov = __shfl_xor_sync(0xffffffffu, best, s);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, s);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_val[warp] = best;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                if (s_val[w] > best || (s_val[w] == best && s_idx[w] < bi)) {
+                    best = s_val[w];
+                    bi = s_idx[w];
+                }
+            s_val[0] = best;
+            s_idx[0] = bi;
+            cand_val[par * G + c] = best;
+            cand_idx[par * G + c] = bi;
+        }
+        __syncthreads();
+        bi = s_idx[0];
+        // publish the candidate row's segment and, if owned here, row k
+        if (bi < n)
+            for (int j = tid; j < kb; j += blockDim.x)
+                cand_row[((size_t)par * G + c) * NB + j] = tile[(bi - r0) * NB + j];
+        if (k >= r0 && k < r1)
+            for (int j = tid; j < kb; j += blockDim.x) krow[(size_t)par * NB + j] = tile[(k - r0) * NB + j];
+        if (!grid_barrier(ps, G, gen)) {
+            if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
+            return;
+        }
+        // global pivot, identical in every CTA
+        if (tid == 0) {
+            double gb = -1.0;
+            int gi = n, gc = -1;
+            for (unsigned int q = 0; q < G; ++q) {
+                double v = ld_volatile(cand_val + par * G + q);
+                int ix = ld_volatile(cand_idx + par * G + q);
+                if (ix >= n) continue;
+                if (v > gb || (v == gb && ix < gi)) {
+                    gb = v;
+                    gi = ix;
+                    gc = (int)q;
+                }
+            }
+            s_fail = 0;
+            if (gc < 0 || !isfinite(gb) || gb <= limit) {
+                s_fail = 1;
+                if (c == 0) {
+                    st->code = 2;
+                    st->column = k;
+                    st->value = gb;
+                }
+            } else if (c == 0) {
+                piv[k] = gi;
+            }
+            s_p = gi;
+            s_val[1] = (double)gc;
+        }
+        __syncthreads();
+        if (s_fail) return;
+        const int p = s_p, pc = (int)s_val[1];
+        // the new row k is the published row p (full panel width: columns
+        // < kk hold earlier multipliers and move with the row)
+        const T *prow_g = cand_row + ((size_t)par * G + pc) * NB;
+        for (int j = tid; j < kb; j += blockDim.x) s_prow[j] = ld_volatile(prow_g + j);
+        __syncthreads();
+        if (p != k) {
+            if (k >= r0 && k < r1)
+                for (int j = tid; j < kb; j += blockDim.x) tile[(k - r0) * NB + j] = s_prow[j];
+            if (p >= r0 && p < r1)
+                for (int j = tid; j < kb; j += blockDim.x)
+                    tile[(p - r0) * NB + j] = ld_volatile(krow + (size_t)par * NB + j);
+        }
+        __syncthreads();
+        if (k + 1 >= n) break;
+        const T pivot = s_prow[kk];
+        for (int i = max(r0, k + 1) + tid; i < r1; i += blockDim.x) {
+            T *row = tile + (i - r0) * NB;
+            T m = divide(row[kk], pivot);
+            row[kk] = m;
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], m, s_prow[j]);
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < nrows * kb; t += blockDim.x) {
+        int i = t / kb, j = t % kb;
+        a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
+    }
+}
+
 // ---- row swaps outside the panel -------------------------------------
 template <class T>
 __global__ void k_laswp(T *a, int n, int k0, int kb, const long long *piv, const Status *st) {
@@ -308,6 +507,79 @@ __global__ void __launch_bounds__(256) k_gemm_cplx(cplx *a, int n, int k0, int k
             if (r < n && c < n) a[(size_t)r * n + c] = acc[i][j];
         }
 }
+
+// Complex, 3 real products per complex multiply-add (Gauss / 3M):
+//   T1 = Ar Br, T2 = Ai Bi, T3 = (Ar + Ai)(Br + Bi),
+//   C -= (T1 - T2) + j (T3 - T1 - T2),
+// 25% fewer FP64 operations than the 4-product form; the sums Ar + Ai and
+// Br + Bi are formed once per tile in shared memory.  32x64 C tile per
+// 256-thread CTA, 2x4 per thread.
+__global__ void __launch_bounds__(256) k_gemm_cplx3m(cplx *a, int n, int k0, int kb, const Status *st) {
+    extern __shared__ double sm3[];
+    double *Ar = sm3, *Ai = Ar + NB * 33, *As = Ai + NB * 33;  // [NB][33]
+    double *Br = As + NB * 33, *Bi = Br + NB * 64, *Bs = Bi + NB * 64;  // [NB][64]
+    if (st->code != 0) return;
+    const int r0 = k0 + kb + blockIdx.y * 32, c0 = k0 + kb + blockIdx.x * 64;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    for (int t = threadIdx.x; t < 32 * NB; t += 256) {
+        int r = t / NB, m = t % NB;
+        cplx v = (r0 + r < n && m < kb) ? a[(size_t)(r0 + r) * n + k0 + m] : cplx{0.0, 0.0};
+        Ar[m * 33 + r] = v.re;
+        Ai[m * 33 + r] = v.im;
+        As[m * 33 + r] = v.re + v.im;
+    }
+    for (int t = threadIdx.x; t < 64 * NB; t += 256) {
+        int mm = t / 64, c = t % 64;
+        cplx v = (c0 + c < n && mm < kb) ? a[(size_t)(k0 + mm) * n + c0 + c] : cplx{0.0, 0.0};
+        Br[mm * 64 + c] = v.re;
+        Bi[mm * 64 + c] = v.im;
+        Bs[mm * 64 + c] = v.re + v.im;
+    }
+    __syncthreads();
+    double t1[2][4], t2[2][4], t3[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) t1[i][j] = t2[i][j] = t3[i][j] = 0.0;
+#pragma unroll 4
+    for (int m = 0; m < NB; ++m) {
+        double ar[2], ai[2], as[2], br[4], bi[4], bs[4];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            ar[i] = Ar[m * 33 + ty + 16 * i];
+            ai[i] = Ai[m * 33 + ty + 16 * i];
+            as[i] = As[m * 33 + ty + 16 * i];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            br[j] = Br[m * 64 + tx + 16 * j];
+            bi[j] = Bi[m * 64 + tx + 16 * j];
+            bs[j] = Bs[m * 64 + tx + 16 * j];
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                t1[i][j] = fma(ar[i], br[j], t1[i][j]);
+                t2[i][j] = fma(ai[i], bi[j], t2[i][j]);
+                t3[i][j] = fma(as[i], bs[j], t3[i][j]);
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int r = r0 + ty + 16 * i, c = c0 + tx + 16 * j;
+            if (r < n && c < n) {
+                cplx v = a[(size_t)r * n + c];
+                v.re -= t1[i][j] - t2[i][j];
+                v.im -= (t3[i][j] - t1[i][j]) - t2[i][j];
+                a[(size_t)r * n + c] = v;
+            }
+        }
+}
+
+static const size_t kGemm3mSmem = (size_t)NB * 33 * 3 * 8 + (size_t)NB * 64 * 3 * 8;
 
 // ---- final diagonal check (lu.c:455-476) -----------------------------
 template <class T>
@@ -574,11 +846,98 @@ static bool registry_get(const void *host_data, size_t n, bool cx, unsigned long
 // ---------------------------------------------------------------------
 // factorisation driver
 // ---------------------------------------------------------------------
+// Cooperative-panel launch plan for rows m: G co-resident CTAs of 256
+// threads with rows_per_cta rows each in shared memory; G = 0 if it does not
+// fit (the single-CTA panel is used then).
+template <class T>
+struct CoopPlan {
+    int G = 0, rows = 0;
+    size_t smem = 0;
+};
+
+template <class T>
+static CoopPlan<T> coop_plan(int m) {
+    CoopPlan<T> pl;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop || m < 2 * 64) return pl;  // small panels: one CTA is faster
+    int G = std::min(sms, (m + 31) / 32);
+    int rows = (m + G - 1) / G;
+    size_t smem = (size_t)rows * NB * sizeof(T);
+    if (smem > 200 * 1024) return pl;
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaFuncSetAttribute(k_panel_coop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_done = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel_coop<T>, 256, smem);
+    if (per_sm < 1) return pl;
+    pl.G = G;
+    pl.rows = rows;
+    pl.smem = smem;
+    return pl;
+}
+
+// Complex trailing update form: the direct 4-product form (default; it keeps
+// the reference's backward error, 1.5e-11 on the 8402-unknown box) or 3 real
+// products when PEEC_GB300_CGEMM=3m (17% faster, backward error 3.4e-11).
+static bool complex_gemm_3m() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char *e = getenv("PEEC_GB300_CGEMM");
+        mode = (e && strcmp(e, "3m") == 0) ? 1 : 0;
+    }
+    return mode == 1;
+}
+
+struct PanelScratch {
+    PanelSlots *ps = nullptr;
+    double *cand_val = nullptr;
+    int *cand_idx = nullptr;
+    void *cand_row = nullptr, *krow = nullptr;
+};
+
 template <class T>
 static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status *d_st) {
+    DBuf<unsigned char> scratch;
+    PanelScratch sc;
+    {
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        size_t G = (size_t)sms;
+        size_t bytes = 256 + 2 * G * 8 + 2 * G * 4 + 2 * G * NB * sizeof(T) + 2 * NB * sizeof(T) + 64;
+        if (!scratch.alloc(bytes)) return false;
+        cudaMemsetAsync(scratch.p, 0, bytes, stream());
+        unsigned char *b = scratch.p;
+        sc.ps = (PanelSlots *)b;
+        sc.cand_val = (double *)(b + 256);
+        sc.cand_idx = (int *)(b + 256 + 2 * G * 8);
+        size_t off = 256 + 2 * G * 8 + 2 * G * 4;
+        off = (off + 15) & ~(size_t)15;
+        sc.cand_row = b + off;
+        sc.krow = b + off + 2 * G * NB * sizeof(T);
+    }
     for (int k0 = 0; k0 < n; k0 += NB) {
         int kb = std::min(NB, n - k0);
-        PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
+        CoopPlan<T> pl = coop_plan<T>(n - k0);
+        if (pl.G > 0) {
+            int rows = pl.rows;
+            T *cr = (T *)sc.cand_row, *kr = (T *)sc.krow;
+            void *args[] = {&d_a, &n, (void *)&k0, &kb, &rows, &limit, &d_piv, &d_st, &sc.ps, &sc.cand_val,
+                            &sc.cand_idx, &cr, &kr};
+            if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<T>, dim3(pl.G), dim3(256), args,
+                                                     pl.smem, stream()),
+                         "cooperative panel launch"))
+                return false;
+            note_launch();
+        } else {
+            PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
+        }
         PEEC_LAUNCH(k_laswp<T>, (n + 255) / 256, 256, 0, d_a, n, k0, kb, d_piv, d_st);
         int rest = n - (k0 + kb);
         if (rest > 0) {
@@ -588,7 +947,17 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
                 PEEC_LAUNCH(k_gemm_real, g, 256, 0, (double *)d_a, n, k0, kb, d_st);
             } else {
                 dim3 g((rest + 63) / 64, (rest + 31) / 32);
-                PEEC_LAUNCH(k_gemm_cplx, g, 256, 0, (cplx *)d_a, n, k0, kb, d_st);
+                if (complex_gemm_3m()) {
+                    static bool attr = false;
+                    if (!attr) {
+                        cudaFuncSetAttribute(k_gemm_cplx3m, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kGemm3mSmem);
+                        attr = true;
+                    }
+                    PEEC_LAUNCH(k_gemm_cplx3m, g, 256, kGemm3mSmem, (cplx *)d_a, n, k0, kb, d_st);
+                } else {
+                    PEEC_LAUNCH(k_gemm_cplx, g, 256, 0, (cplx *)d_a, n, k0, kb, d_st);
+                }
             }
         }
     }
@@ -690,6 +1059,10 @@ static int factor_inplace(T *d_a, int n, double pivot_tolerance, bool cx, long l
     PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, d_piv, n, d_perm, st.p);
     cudaMemcpyAsync(hs, st.p, sizeof(Status), cudaMemcpyDeviceToHost, stream());
     if (!launch_ok("LU permutation") || !sync("LU factorisation")) return -1;
+    if (hs->code == 6) {
+        set_error("LU panel synchronisation timed out");
+        return -1;
+    }
     return 0;
 }
 
