@@ -82,6 +82,21 @@ int peec_gb300_complex_lu_factor_device(Complex *d_a, size_t n, double pivot_tol
                                         long long *d_piv, int *d_perm,
                                         double *d_row_scale, double *d_column_scale,
                                         double *matrix_scale, int *failed_column);
+/* Same as peec_gb300_lu_factor_device, but allocates no device memory (no
+ * cudaMalloc, cudaFree or allocating library call), for callers that own all
+ * device memory through their own pool or hard budget, or that must not let
+ * cudaMalloc / cudaFree synchronise the device inside a solver loop.  Its
+ * scratch (status, scale reduction, panel exchange slots) lives in one
+ * 256 KiB static device array that every GPU loading the library keeps until
+ * the process exits; n is limited to 50000 (larger n returns -1 with a
+ * message, see peec_gb300_last_error).  The first call on each device looks
+ * up the array's device address with that device current: make that first
+ * call before any stream capture.  Every call reuses the same array and
+ * clears it on entry, so calls that overlap on the GPU (for instance from two
+ * host threads) race with each other: serialise them. */
+int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double pivot_tolerance,
+                                        long long *d_piv, int *d_perm,
+                                        double *matrix_scale, int *failed_column);
 /* nrhs right-hand sides stored one after another; d_b != d_x. */
 int peec_gb300_lu_solve_device(const double *d_lu, const int *d_perm, size_t n,
                                const double *d_b, double *d_x, size_t nrhs);

@@ -184,6 +184,8 @@ EXT_SYMBOLS = [
      [P(Mesh), P(DualMesh), P(PotentialOptions), C.c_void_p, P(PeecAssemblyStats)]),
     ("peec_gb300_lu_factor_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, c_double_p, c_int_p]),
+    ("peec_gb300_lu_factor_device_noalloc", C.c_int,
+     [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, c_double_p, c_int_p]),
     ("peec_gb300_complex_lu_factor_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
       c_double_p, c_int_p]),

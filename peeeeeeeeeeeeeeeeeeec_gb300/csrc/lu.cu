@@ -1430,3 +1430,131 @@ int peec_gb300_complex_lu_solve_device(const Complex *d_lu, const int *d_perm, c
 }
 
 }  // extern "C"
+
+// =====================================================================
+// Allocation-free real factorisation
+//
+// Some callers cannot let a library allocate device memory: applications
+// that own every byte of the GPU through their own pool or hard budget (a
+// hidden cudaMalloc would break their accounting or fail under the cap), and
+// tight solver loops where cudaMalloc / cudaFree would synchronise the
+// device.  For them peec_gb300_lu_factor_device_noalloc keeps all of its
+// scratch -- the status word, the scale reduction and the cooperative
+// panel's exchange slots -- in one file-scope device array of fixed size,
+// which every GPU that loads this library holds until the process exits.
+// =====================================================================
+namespace peec {
+
+static const size_t kNoAllocScratchBytes = 256 * 1024;
+static const size_t kNoAllocMaxN = 50000;  // the permutation kernel keeps n ints in shared memory
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64];  // device address of g_noalloc_scratch, per device ordinal
+
+// Host-side name of the array is not a device address: resolve it once per
+// device with that device current.
+static unsigned char *noalloc_scratch(int dev) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress of the static LU scratch failed: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    return (unsigned char *)g_noalloc_ptr[dev];
+}
+
+}  // namespace peec
+
+extern "C" int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double pivot_tolerance, long long *d_piv,
+                                                   int *d_perm, double *matrix_scale, int *failed_column) {
+    if (!d_a || !d_piv || !d_perm || n == 0) return -1;
+    if (n > kNoAllocMaxN) {
+        set_error("peec_gb300_lu_factor_device_noalloc: n = %zu exceeds the maximum %zu", n, kNoAllocMaxN);
+        return -1;
+    }
+    int dev = 0, sms = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "current device") ||
+        !cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
+        return -1;
+    // layout: status | scale word | panel slots | candidates | candidate rows | row k
+    const size_t G = (size_t)sms;
+    const size_t off_mx = 64, off_ps = 128, off_val = 256, off_idx = off_val + 2 * G * 8;
+    const size_t off_row = (off_idx + 2 * G * 4 + 15) & ~(size_t)15;
+    const size_t off_krow = off_row + 2 * G * NB * sizeof(double);
+    const size_t need = off_krow + 2 * NB * sizeof(double);
+    if (need > kNoAllocScratchBytes) {
+        set_error("peec_gb300_lu_factor_device_noalloc: %d SMs need %zu scratch bytes, the maximum is %zu", sms, need,
+                  kNoAllocScratchBytes);
+        return -1;
+    }
+    unsigned char *base = noalloc_scratch(dev);
+    if (!base) return -1;
+    Status *st = (Status *)base;
+    unsigned long long *mx = (unsigned long long *)(base + off_mx);
+    PanelScratch sc;
+    sc.ps = (PanelSlots *)(base + off_ps);
+    sc.cand_val = (double *)(base + off_val);
+    sc.cand_idx = (int *)(base + off_idx);
+    sc.cand_row = base + off_row;
+    sc.krow = base + off_krow;
+    // the array keeps the previous call's contents: clear what must start at zero
+    if (!cuda_ok(cudaMemsetAsync(base, 0, need, stream()), "scratch reset")) return -1;
+    const int ni = (int)n;
+    PEEC_LAUNCH(k_max_mag<double>, 152 * 8, 256, 0, d_a, n * n, mx);
+    unsigned long long bits = 0;
+    Status hs;
+    cudaMemcpyAsync(&bits, mx, sizeof(bits), cudaMemcpyDeviceToHost, stream());
+    if (!sync("LU scale")) return -1;
+    double scale;
+    memcpy(&scale, &bits, sizeof(scale));
+    if (matrix_scale) *matrix_scale = scale;
+    if (failed_column) *failed_column = -1;
+    if (!isfinite(scale) || scale <= 0.0) return -2;
+    double limit = pivot_tolerance * scale;
+    for (int k0 = 0; k0 < ni; k0 += NB) {
+        int kb = std::min(NB, ni - k0);
+        CoopPlan<double> pl = coop_plan<double>(ni - k0);
+        if (pl.G > 0) {
+            int rows = pl.rows;
+            double *cr = (double *)sc.cand_row, *kr = (double *)sc.krow;
+            void *args[] = {&d_a, (void *)&ni, (void *)&k0, &kb, &rows, &limit, &d_piv, &st, &sc.ps, &sc.cand_val,
+                            &sc.cand_idx, &cr, &kr};
+            if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<double>, dim3(pl.G), dim3(256), args,
+                                                     pl.smem, stream()),
+                         "cooperative panel launch"))
+                return -1;
+            note_launch();
+        } else {
+            PEEC_LAUNCH(k_panel<double>, 1, 1024, 0, d_a, ni, k0, kb, limit, d_piv, st);
+        }
+        PEEC_LAUNCH(k_laswp<double>, (ni + 255) / 256, 256, 0, d_a, ni, k0, kb, d_piv, st);
+        int rest = ni - (k0 + kb);
+        if (rest > 0) {
+            PEEC_LAUNCH(k_trsm<double>, (rest + 255) / 256, 256, 0, d_a, ni, k0, kb, st);
+            dim3 g((rest + 63) / 64, (rest + 63) / 64);
+            PEEC_LAUNCH(k_gemm_real, g, 256, 0, d_a, ni, k0, kb, st);
+        }
+    }
+    PEEC_LAUNCH(k_check_diag<double>, (ni + 255) / 256, 256, 0, d_a, ni, limit, st);
+    size_t perm_smem = n * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, d_piv, ni, d_perm, st);
+    cudaMemcpyAsync(&hs, st, sizeof(Status), cudaMemcpyDeviceToHost, stream());
+    if (!launch_ok("LU kernels") || !sync("LU factorisation")) return -1;
+    if (hs.code == 6) {
+        set_error("LU panel synchronisation timed out");
+        return -1;
+    }
+    if (failed_column) *failed_column = hs.code ? hs.column : -1;
+    if (hs.code) {
+        report_status(hs, false);
+        return -2;
+    }
+    return 0;
+}
