@@ -105,6 +105,14 @@ def make_mesh():
     return SynthMesh.box(*BOX)
 
 
+def set_box(spec):
+    """--box lx,ly,lz,nx,ny,nz (a smaller case for profiling runs)."""
+    global BOX, WORKLOAD
+    v = spec.split(",")
+    BOX = (float(v[0]), float(v[1]), float(v[2]), int(v[3]), int(v[4]), int(v[5]))
+    WORKLOAD = "pec_box_%gx%gx%gm_%dx%dx%d_cells_30MHz_planewave" % BOX
+
+
 def plane_wave(m):
     """Host copy of the right-hand side [-U_e ; 0] (same formula as the
     device kernel): x-polarised, incident from +z."""
@@ -178,6 +186,8 @@ class DeviceSolve:
         self.eh = (C.c_double * 3)(1.0, 0.0, 0.0)
         self.k0 = 2 * np.pi * FREQ / C0
         self.phase_ms = {}
+        self.phase_ms_mixed = {}
+        self.mixed_iters = 0
 
     def step(self, timed_phases=False):
         lib, m, n = self.lib, self.m, self.n
@@ -212,10 +222,50 @@ class DeviceSolve:
             for f in ("ms_prepare", "ms_near", "ms_far"):
                 self.phase_ms.setdefault(tag + "_" + f[3:], []).append(getattr(st, f))
         self.work = {"Lp_near_pairs": self.stL.near_pairs, "Lp_potential_evals": self.stL.potential_evaluations,
-                     "P_near_pairs": self.stP.near_pairs, "P_potential_evals": self.stP.potential_evaluations}
+                     "Lp_far_point_pairs": self.stL.far_point_pairs,
+                     "P_near_pairs": self.stP.near_pairs, "P_potential_evals": self.stP.potential_evaluations,
+                     "P_far_point_pairs": self.stP.far_point_pairs}
         for e in ev:
             lib.peec_gb300_event_destroy(e)
         return out[0]
+
+    def step_mixed(self):
+        """The mixed-precision solve of the same system: FP32 far field (the
+        near field stays FP64), FP32 LU with split-BF16x3 tcgen05 trailing
+        updates, FP64 iterative refinement to the same 1e-10 gate."""
+        lib, m, n = self.lib, self.m, self.n
+        prev = lib.peec_gb300_set_far_precision(2)
+        ev = [lib.peec_gb300_event_record()]
+        assert lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(self.lo), self.dL,
+                                                C.byref(self.stL)) == 0
+        ev.append(lib.peec_gb300_event_record())
+        assert lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(self.po), self.dP,
+                                               C.byref(self.stP)) == 0
+        ev.append(lib.peec_gb300_event_record())
+        lib.peec_gb300_set_far_precision(prev)
+        assert lib.peec_gb300_harmonic_build_device(self.dL, self.dP, self.dedges, None, self.ne, self.nv, FREQ,
+                                                    self.dZ) == 0
+        assert lib.peec_gb300_plane_wave_rhs_device(self.dctr, self.dvec, self.ne, self.nv, self.kh, self.eh,
+                                                    self.k0, self.db) == 0
+        ev.append(lib.peec_gb300_event_record())
+        be, it = C.c_double(), C.c_int()
+        s = lib.peec_gb300_complex_solve_mixed_device(self.dZ, n, self.db, self.dx, 1, 1e-10, 30, C.byref(be),
+                                                      C.byref(it))
+        assert s == 0, "mixed solve did not converge: status %d, backward error %g" % (s, be.value)
+        ev.append(lib.peec_gb300_event_record())
+        names = ["assemble_Lp", "assemble_P", "mna_fill_rhs", "mixed_solve"]
+        for k, name in enumerate(names):
+            self.phase_ms_mixed.setdefault(name, []).append(lib.peec_gb300_event_elapsed_ms(ev[k], ev[k + 1]))
+        for tag, st in (("Lp", self.stL), ("P", self.stP)):
+            for f in ("ms_near", "ms_far"):
+                self.phase_ms_mixed.setdefault(tag + "_" + f[3:], []).append(getattr(st, f))
+        mp, mf, mr = C.c_double(), C.c_double(), C.c_double()
+        self.mixed_iters = lib.peec_gb300_mixed_timing(C.byref(mp), C.byref(mf), C.byref(mr))
+        for name, v in (("solve_prepare", mp), ("solve_factor", mf), ("solve_refine", mr)):
+            self.phase_ms_mixed.setdefault(name, []).append(v.value)
+        for e in ev:
+            lib.peec_gb300_event_destroy(e)
+        return be.value
 
     def free(self):
         for p in (self.dL, self.dP, self.dZ, self.dLU, self.db, self.dx, self.dpiv, self.dperm, self.drow, self.dcol,
@@ -340,7 +390,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--box", default=None, help="lx,ly,lz,nx,ny,nz (default: the 5 cm box)")
     args = ap.parse_args()
+    if args.box:
+        set_box(args.box)
     rank, world, local = dist_env()
     dist = None
     if world > 1:
@@ -388,6 +442,33 @@ def main():
     ms_step = total_ms / args.steps
     value = world * args.steps / (total_ms / 1e3)
     phases = {k: statistics.median(v) for k, v in ds.phase_ms.items()}
+    # mixed-precision path on the same system (CUDA-event timed, same gate)
+    mixed = None
+    if not args.no_mixed:
+        for _ in range(args.warmup):
+            ds.step_mixed()
+        ds.phase_ms_mixed = {}
+        lib.peec_gb300_synchronize()
+        m0 = lib.peec_gb300_event_record()
+        mbes = [ds.step_mixed() for _ in range(args.steps)]
+        m1 = lib.peec_gb300_event_record()
+        mixed_ms = lib.peec_gb300_event_elapsed_ms(m0, m1) / args.steps
+        mixed = {"value": world * 1000.0 / mixed_ms, "unit": "solves/s", "ms_per_step": mixed_ms,
+                 "vs_plain_fp64_gpu": (1000.0 / mixed_ms) / (1000.0 / ms_step),
+                 "backward_error": max(mbes), "refinement_iterations": ds.mixed_iters,
+                 "phase_ms": {k: statistics.median(v) for k, v in ds.phase_ms_mixed.items()},
+                 "precision": "FP32 far field (near field FP64), FP32 LU with split-BF16x3 tcgen05 trailing "
+                              "update (FP32 accumulation), FP64 iterative refinement"}
+    # one more solve, outside the timed region, with the LU phase timing on
+    lib.peec_gb300_lu_timing_enable(1)
+    ds.step()
+    lu_t = [C.c_double() for _ in range(4)]
+    lib.peec_gb300_lu_timing(*[C.byref(x) for x in lu_t])
+    lib.peec_gb300_lu_timing_enable(0)
+    lu_phases = {"panel_ms": lu_t[0].value, "swap_trsm_ms": lu_t[1].value, "update_ms": lu_t[2].value,
+                 "update_flops": lu_t[3].value}
+    p64, p32 = C.c_double(), C.c_double()
+    lib.peec_gb300_pipe_peaks(C.byref(p64), C.byref(p32))
     ds.free()
 
     # end to end through the drop-in ABI, host buffers
@@ -412,6 +493,7 @@ def main():
                "sample": desc, "sample_seconds": round(sample_s, 2),
                "phase_seconds": {k: round(v, 2) for k, v in parts.items()}}
 
+    roofs = roofline(phases, lu_phases, m, p64.value, p32.value, ds.work)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -422,21 +504,75 @@ def main():
                            "retardation": "none (quasi-static, as the reference)"},
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-                "roofline": roofline(phases, m)}
+                "lu_phases": lu_phases, "mixed": mixed,
+                "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
+                                      "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
+                "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}
         print(json.dumps(line))
     if dist:
         dist.barrier()
         dist.destroy_process_group()
 
 
-def roofline(phases, m):
-    """Dominant phase of the step against its bound (filled in by measurement)."""
-    n = m.n_edges + m.n_nodes
-    lu_ms = phases.get("complex_lu")
-    flops = 8.0 / 3.0 * n ** 3
-    return {"bound": "fp64", "kernel": "complex LU (panel + FP64 trailing update)",
-            "achieved": flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None, "unit": "TFLOP/s",
-            "peak": None, "frac": None, "traffic": None}
+DF_FP32_INSTR_PER_PAIR = 106  # double-float far rule: FP32 instructions per point pair (csrc/assembly.cu)
+
+
+def load_traffic():
+    """DRAM bytes per launch of the profiled kernels, from the committed ncu
+    summary (profiles/traffic.json), or {} if absent."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def roofline(phases, lu, m, fp64_peak, fp32_peak, work):
+    """The dominant kernel of the step against the pipe that bounds it, plus
+    the other phases.  Peaks: HBM from MEASURED_PEAKS.json, FP64/FP32 pipes
+    measured by bench.py's own FMA loops on the same GPU."""
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    ne, nv = m.n_edges, m.n_nodes
+    n = ne + nv
+    traffic = load_traffic()
+    out = []
+    if lu.get("update_ms"):
+        a = lu["update_flops"] / (lu["update_ms"] * 1e-3) / 1e12
+        out.append({"kernel": "k_gemm_cplx (complex LU trailing update, FP64 FMA)", "bound": "fp64",
+                    "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s", "frac": a / fp64_peak if fp64_peak else None,
+                    "ms": lu["update_ms"], "traffic": traffic.get("k_gemm_cplx"),
+                    "peak_source": "measured (bench FMA loop)"})
+    far_pairs = {"Lp": work.get("Lp_far_point_pairs", 0), "P": work.get("P_far_point_pairs", 0)}
+    for tag in ("Lp", "P"):
+        ms = phases.get(tag + "_far")
+        if ms:
+            a = far_pairs[tag] / (ms * 1e-3) / 1e9
+            pk = fp32_peak * 1e12 / 2 / DF_FP32_INSTR_PER_PAIR / 1e9
+            out.append({"kernel": "k_assemble_tiles far rule, %s (double-float on the FP32 pipe)" % tag,
+                        "bound": "fp32", "achieved": a, "peak": pk, "unit": "Gpoint-pairs/s", "frac": a / pk,
+                        "ms": ms, "traffic": traffic.get("k_assemble_tiles"),
+                        "peak_source": "measured FP32 FMA rate / %d FP32 instructions per point pair"
+                                       % DF_FP32_INSTR_PER_PAIR})
+    if phases.get("mna_fill"):
+        b = 16.0 * n * n + 8.0 * ne * ne
+        a = b / (phases["mna_fill"] * 1e-3) / 1e9
+        out.append({"kernel": "k_harmonic_fill (MNA matrix Z)", "bound": "hbm", "achieved": a, "peak": hbm,
+                    "unit": "GB/s", "frac": a / hbm, "ms": phases["mna_fill"], "traffic": traffic.get("k_harmonic_fill"),
+                    "peak_source": "measured (MEASURED_PEAKS.json)"})
+    if phases.get("backward_error"):
+        b = 16.0 * n * n
+        a = b / (phases["backward_error"] * 1e-3) / 1e9
+        out.append({"kernel": "k_backward_error (FP64 residual, one pass over Z)", "bound": "hbm", "achieved": a,
+                    "peak": hbm, "unit": "GB/s", "frac": a / hbm, "ms": phases["backward_error"],
+                    "traffic": traffic.get("k_backward_error"), "peak_source": "measured (MEASURED_PEAKS.json)"})
+    return out
 
 
 if __name__ == "__main__":

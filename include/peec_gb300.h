@@ -27,6 +27,7 @@ typedef struct
 {
     unsigned long long near_pairs;             /* non-FAR patch pairs integrated analytically */
     unsigned long long potential_evaluations;  /* analytic triangle-potential evaluations     */
+    unsigned long long far_point_pairs;        /* far-rule 1/R point pairs (FAR patch pairs x (2q^2)^2) */
     double ms_prepare;                         /* patch prep + near-pair discovery (CUDA events) */
     double ms_near;                            /* adaptive near-field kernels                 */
     double ms_far;                             /* tiled far-field + combine kernel            */
@@ -70,6 +71,12 @@ int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual,
                                 const PotentialOptions *options, double *d_out,
                                 PeecAssemblyStats *stats);
 
+/* Far-rule arithmetic of later assemblies (all entry points): 0 native FP64,
+ * 1 double-float on the FP32 pipes (default; FP64-accurate, parity 1e-12),
+ * 2 FP32 with FP32 accumulation (mixed-precision path, ~1e-7 relative).
+ * Returns the previous mode.  Not thread-safe against concurrent assemblies. */
+int peec_gb300_set_far_precision(int mode);
+
 /* ---- dense factorisations of device-resident matrices (in place) ----
  * Same algorithm, numerics and error codes as lu_factorize /
  * complex_lu_factorize.  d_piv (n int64) receives the pivot rows, d_perm (n
@@ -104,6 +111,39 @@ int peec_gb300_complex_lu_solve_device(const Complex *d_lu, const int *d_perm,
                                        const double *d_row_scale,
                                        const double *d_column_scale, size_t n,
                                        const Complex *d_b, Complex *d_x, size_t nrhs);
+
+/* Per-phase timing of the allocating factorisations (events around each
+ * block column's panel, swaps + triangular solve, trailing update).
+ * peec_gb300_lu_timing returns -1 unless enabled. */
+void peec_gb300_lu_timing_enable(int on);
+int peec_gb300_lu_timing(double *ms_panel, double *ms_swap_trsm, double *ms_update,
+                         double *update_flops);
+
+/* Measured FMA issue rates of this GPU's FP64 and FP32 pipes (TFLOP/s). */
+int peec_gb300_pipe_peaks(double *fp64_tflops, double *fp32_tflops);
+
+/* ---- tensor-core building block ----
+ * C_j (FP32, row-major, leading dimension ldc) -= A B_j^T for device BF16
+ * matrices A [m][k] and B_j [n][k] (K contiguous), j < J (J = 1 or 2), on
+ * tcgen05 with TMA-fed operands and FP32 accumulation in tensor memory.
+ * k must be a multiple of 64; A, B_j 16-byte aligned. */
+int peec_gb300_tc_gemm(const void *d_a, const void *d_b0, const void *d_b1, float *d_c0,
+                       float *d_c1, int m, int n, int k, long long ldc, int J);
+
+/* ---- mixed precision complex solve ----
+ * Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
+ * another) to a componentwise backward error <= tol: FP64 equilibration as
+ * complex_lu_factorize, FP32 LU whose trailing updates run on the tensor
+ * cores as split-BF16x3 products (FP32 accumulation), then FP64 iterative
+ * refinement r = B - Z X.  d_Z and d_b are not modified.  Returns 0 when
+ * converged, 1 when max_iter refinements did not reach tol (X holds the last
+ * iterate), -2 for a zero / non-finite row or column or a singular FP32
+ * pivot, -1 on other errors.  backward_error / iterations may be NULL. */
+int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Complex *d_b,
+                                          Complex *d_x, size_t nrhs, double tol, int max_iter,
+                                          double *backward_error, int *iterations);
+/* Phase times (ms) of the last mixed solve; returns its iteration count. */
+int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine);
 
 /* ---- harmonic system on the device ----
  * Z = [R + j w L, A; -P A^T, j w I] (N = Ne + Nv) from device Lp, P and the

@@ -156,7 +156,8 @@ __device__ __forceinline__ bool region_pair_skipped(const ScanArgs &s, int a, in
 }
 
 // pass 0 counts, pass 1 writes (count[i] -> offsets in off[i])
-__global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, NearRec *out) {
+__global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, NearRec *out,
+                            unsigned long long *far_pairs) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const RegionsDev &R = s.R;
     if (i >= R.np) return;
@@ -164,6 +165,7 @@ __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, Ne
     const double *ci = R.corner + 12 * (size_t)i, *bi = R.box + 6 * (size_t)i;
     double hi = R.size[i];
     int w = pass ? off[i] : 0, found = 0;
+    unsigned long long nfar = 0;
     int b_prev = -1;
     bool skip_b = false;
     for (int j = R.off[a]; j < R.np; ++j) {
@@ -179,11 +181,17 @@ __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, Ne
         }
         int cls = classify_pair(ci, bi, hi, R.corner + 12 * (size_t)j, R.box + 6 * (size_t)j, R.size[j],
                                 s.near_factor, R.same_obj[i] == R.same_obj[j]);
-        if (cls == CLS_FAR) continue;
+        if (cls == CLS_FAR) {
+            ++nfar;
+            continue;
+        }
         if (pass) out[w + found] = NearRec{i, j, cls, 0};
         ++found;
     }
-    if (!pass) count[i] = found;
+    if (!pass) {
+        count[i] = found;
+        if (far_pairs && nfar) atomicAdd(far_pairs, nfar);
+    }
 }
 
 // exclusive scan of count[0..n) into off[0..n], single CTA of 1024 threads
@@ -508,7 +516,7 @@ struct TileArgs {
     const FarPt *pts;
     const FarPtF *ptf;
     int npts;
-    int far_df;  // 1: double-float far rule, 0: FP64
+    int far_df;  // 1: double-float far rule, 0: FP64, 2: FP32
     const int *near_off;
     const NearRec *near_rec;
     const double2 *near_k;
@@ -591,6 +599,70 @@ __device__ __forceinline__ f2 df_rsqrt(f2 x) {
     return quick_two_sum(y, c);
 }
 
+// FP32 form (the mixed-precision path): hi parts only, FP32 rsqrt and
+// per-lane FP32 accumulation, combined across lanes in FP64.  Relative error
+// of an entry ~1e-7.
+__device__ __forceinline__ double far_pair_f32(const FarPtF *pa, const FarPtF *pb, int npts) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (int p = lane; p < npts; p += 32) {
+        FarPtF A = pa[p];
+        float s = 0.0f;
+#pragma unroll 4
+        for (int q = 0; q < npts; ++q) {
+            FarPtF B = pb[q];
+            float dx = A.xh - B.xh, dy = A.yh - B.yh, dz = A.zh - B.zh;
+            float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (!(r2 <= 0.0f)) s = fmaf(B.wh, rsqrtf(r2), s);
+        }
+        acc = fma((double)A.wh, (double)s, acc);
+    }
+    return warp_sum(acc);
+}
+
+// Double-float form, accumulating into this lane's running sum `acc` (the
+// entry's far part is reduced across lanes once, after all its patch pairs):
+// every point difference, square, the reciprocal square root and the sums
+// carry ~48 significant bits on the FP32 pipes; two independent partial sums
+// per lane keep the dependent add chains short.  `bad` is set for a NaN.
+__device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *pb, int npts, f2 &acc, bool &bad) {
+    const int lane = threadIdx.x & 31;
+    for (int p = lane; p < npts; p += 32) {
+        FarPtF A = pa[p];
+        f2 ax = {A.xh, A.xl}, ay = {A.yh, A.yl}, az = {A.zh, A.zl};
+        f2 s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+        for (int q = 0; q < npts; q += 2) {
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (q + u >= npts) break;
+                FarPtF B = pb[q + u];
+                f2 dx = df_sub(ax, f2{B.xh, B.xl});
+                f2 dy = df_sub(ay, f2{B.yh, B.yl});
+                f2 dz = df_sub(az, f2{B.zh, B.zl});
+                f2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+                if (r2.h <= 0.0f) continue;  // the reference skips R <= 0
+                if (!(r2.h == r2.h) || !(B.wh == B.wh)) bad = true;
+                f2 t = df_mul(f2{B.wh, B.wl}, df_rsqrt(r2));
+                if (u == 0)
+                    s0 = df_add(s0, t);
+                else
+                    s1 = df_add(s1, t);
+            }
+        }
+        if (!(A.wh == A.wh)) bad = true;
+        acc = df_add(acc, df_mul(f2{A.wh, A.wl}, df_add(s0, s1)));
+    }
+}
+
+__device__ __forceinline__ double warp_sum_df(f2 v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+        f2 o = {__shfl_xor_sync(0xffffffffu, v.h, m), __shfl_xor_sync(0xffffffffu, v.l, m)};
+        v = df_add(v, o);
+    }
+    return (double)v.h + (double)v.l;
+}
+
 // Double-float form of the same sum: every point difference, square, the
 // reciprocal square root and the accumulation carry ~48 significant bits,
 // on the FP32 pipes; per-lane partial sums are combined in FP64.
@@ -668,18 +740,35 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
             if (!skip) {
                 if (T.kind != KIND_RAW && (sa <= 0.0 || sb <= 0.0)) bad = true;
                 double integral = 0.0;
+                // double-float mode: far patch pairs accumulate per lane and
+                // are reduced across the warp once per entry; near pairs (and
+                // the other modes) add in the reference's (i, j) order
+                f2 facc = {0.0f, 0.0f};
+                bool fbad = false;
                 for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i)
                     for (int j = R.off[b]; j < R.off[b + 1]; ++j) {
                         double k;
-                        if (!near_lookup(T, i, j, k))
-                            k = T.far_df ? far_pair_df(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts)
-                                         : far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
+                        if (!near_lookup(T, i, j, k)) {
+                            if (T.far_df == 1) {
+                                far_pair_df_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, facc,
+                                                fbad);
+                                continue;
+                            }
+                            k = T.far_df == 2 ? far_pair_f32(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts)
+                                              : far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
+                        }
                         if (!isfinite(k)) {
                             bad = true;
                             break;
                         }
                         integral += k;
                     }
+                if (T.far_df == 1) {
+                    fbad = __any_sync(0xffffffffu, fbad);
+                    double far = warp_sum_df(facc);
+                    if (fbad || !isfinite(far)) bad = true;
+                    integral += far;
+                }
                 if (T.kind == KIND_INDUCTANCE)
                     val = kMu0Over4Pi * dot * integral / (sa * sb);
                 else if (T.kind == KIND_POTENTIAL)
@@ -806,15 +895,16 @@ struct AssemblyOptions {
     double dir_tol;
 };
 
-// Far rule arithmetic: double-float on the FP32 pipes (default), or native
-// FP64 when PEEC_GB300_FAR=fp64 (for comparison runs).
+// Far rule arithmetic: 1 double-float on the FP32 pipes (default), 0 native
+// FP64 (PEEC_GB300_FAR=fp64), 2 FP32 (PEEC_GB300_FAR=fp32, or
+// peec_gb300_set_far_precision for the mixed-precision path).
+static int g_far_mode = -1;
 static int far_mode_df() {
-    static int mode = -1;
-    if (mode < 0) {
+    if (g_far_mode < 0) {
         const char *e = getenv("PEEC_GB300_FAR");
-        mode = (e && strcmp(e, "fp64") == 0) ? 0 : 1;
+        g_far_mode = (e && strcmp(e, "fp64") == 0) ? 0 : (e && strcmp(e, "fp32") == 0) ? 2 : 1;
     }
-    return mode;
+    return g_far_mode;
 }
 
 static bool orders_valid(const AssemblyOptions &o) {
@@ -840,8 +930,10 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     DBuf<FarPt> pts((size_t)np * npts);
     DBuf<FarPtF> ptf((size_t)np * npts);
     DBuf<int> count(np + 1), near_off(np + 1), counter(1);
-    DBuf<unsigned long long> err(1), evals(1);
-    if ((np && (!pts.p || !ptf.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p) return -1;
+    DBuf<unsigned long long> err(1), evals(1), farcount(1);
+    if ((np && (!pts.p || !ptf.p || !count.p || !near_off.p)) || !counter.p || !err.p || !evals.p || !farcount.p)
+        return -1;
+    cudaMemsetAsync(farcount.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(err.p, 0xff, sizeof(unsigned long long), stream());
     cudaMemsetAsync(evals.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
@@ -849,7 +941,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         long long tot = (long long)np * npts;
         PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p, ptf.p);
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
-        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 0, count.p, nullptr, nullptr);
+        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 0, count.p, nullptr, nullptr, farcount.p);
         PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, count.p, near_off.p, np);
     } else {
         cudaMemsetAsync(near_off.p, 0, sizeof(int), stream());
@@ -867,7 +959,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     cudaEventRecord(ev[1], stream());
     if (nrec) {
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
-        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 1, nullptr, near_off.p, rec.p);
+        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 1, nullptr, near_off.p, rec.p, nullptr);
         NearEvalArgs A;
         A.corner = R.corner;
         A.rec = rec.p;
@@ -912,7 +1004,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     PEEC_LAUNCH(k_assemble_tiles, dim3(nt, nt), kTileWarps * 32, 0, T);
     cudaEventRecord(ev[3], stream());
     if (!launch_ok("assembly kernels")) return -1;
-    unsigned long long e = 0, ne = 0;
+    unsigned long long e = 0, ne = 0, nf = 0;
+    cudaMemcpyAsync(&nf, farcount.p, sizeof(nf), cudaMemcpyDeviceToHost, stream());
     cudaMemcpyAsync(&e, err.p, sizeof(e), cudaMemcpyDeviceToHost, stream());
     cudaMemcpyAsync(&ne, evals.p, sizeof(ne), cudaMemcpyDeviceToHost, stream());
     if (!sync("assembly")) return -1;
@@ -923,6 +1016,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         cudaEventElapsedTime(&t23, ev[2], ev[3]);
         stats->near_pairs = (unsigned long long)nrec;
         stats->potential_evaluations = ne;
+        stats->far_point_pairs = nf * (unsigned long long)npts * (unsigned long long)npts;
         stats->ms_prepare = t01;
         stats->ms_near = t12;
         stats->ms_far = t23;
@@ -1227,3 +1321,12 @@ int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual, const Po
 }
 
 }  // extern "C"
+
+// Select the far-rule arithmetic of later assemblies: 0 FP64, 1 double-float
+// (default, FP64-accurate), 2 FP32 (mixed-precision path).  Returns the
+// previous mode.
+extern "C" int peec_gb300_set_far_precision(int mode) {
+    int prev = far_mode_df();
+    if (mode >= 0 && mode <= 2) g_far_mode = mode;
+    return prev;
+}

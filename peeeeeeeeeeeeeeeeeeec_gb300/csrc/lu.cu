@@ -33,6 +33,8 @@
 #include "../../include/complex_lu.h"
 #include "../../include/lu.h"
 #include "../../include/peec_gb300.h"
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace peec {
@@ -64,6 +66,44 @@ __device__ __forceinline__ cplx msub(cplx c, cplx m, cplx u) {
     c.im = fma(-m.im, u.re, c.im);
     return c;
 }
+
+// FP32 complex, for the mixed-precision factorisation
+struct cplxf {
+    float re, im;
+};
+__device__ __forceinline__ double mag(cplxf v) { return (double)hypotf(v.re, v.im); }
+__device__ __forceinline__ cplxf divide(cplxf a, cplxf b) {
+    float den = b.re * b.re + b.im * b.im;
+    cplxf z;
+    z.re = (a.re * b.re + a.im * b.im) / den;
+    z.im = (a.im * b.re - a.re * b.im) / den;
+    return z;
+}
+__device__ __forceinline__ cplxf msub(cplxf c, cplxf m, cplxf u) {
+    c.re = fmaf(-m.re, u.re, c.re);
+    c.re = fmaf(m.im, u.im, c.re);
+    c.im = fmaf(-m.re, u.im, c.im);
+    c.im = fmaf(-m.im, u.re, c.im);
+    return c;
+}
+// component-wise warp sums and additions
+__device__ __forceinline__ double warp_sum_t(double v) { return warp_sum(v); }
+__device__ __forceinline__ cplx warp_sum_t(cplx v) {
+    v.re = warp_sum(v.re);
+    v.im = warp_sum(v.im);
+    return v;
+}
+__device__ __forceinline__ cplxf warp_sum_t(cplxf v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+        v.re += __shfl_xor_sync(0xffffffffu, v.re, m);
+        v.im += __shfl_xor_sync(0xffffffffu, v.im, m);
+    }
+    return v;
+}
+__device__ __forceinline__ double addv(double a, double b) { return a + b; }
+__device__ __forceinline__ cplx addv(cplx a, cplx b) { return cplx{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cplxf addv(cplxf a, cplxf b) { return cplxf{a.re + b.re, a.im + b.im}; }
 
 struct Status {
     int code;    // 0 ok, 2 singular / invalid pivot
@@ -251,6 +291,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
     __shared__ T s_prow[NB];
     __shared__ double s_val[8];
     __shared__ int s_idx[8];
+    __shared__ int s_cta[8];
     __shared__ int s_p, s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned int G = gridDim.x;
@@ -315,11 +356,12 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
             if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
             return;
         }
-        // global pivot, identical in every CTA
-        if (tid == 0) {
+        // global pivot, identical in every CTA: the G candidates are loaded
+        // in parallel and reduced (largest value, then lowest row)
+        {
             double gb = -1.0;
             int gi = n, gc = -1;
-            for (unsigned int q = 0; q < G; ++q) {
+            for (unsigned int q = tid; q < G; q += blockDim.x) {
                 double v = ld_volatile(cand_val + par * G + q);
                 int ix = ld_volatile(cand_idx + par * G + q);
                 if (ix >= n) continue;
@@ -329,6 +371,33 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                     gc = (int)q;
                 }
             }
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                double ov = __shfl_xor_sync(0xffffffffu, gb, sh);
+                int oi = __shfl_xor_sync(0xffffffffu, gi, sh);
+                int oc = __shfl_xor_sync(0xffffffffu, gc, sh);
+                if (ov > gb || (ov == gb && oi < gi)) {
+                    gb = ov;
+                    gi = oi;
+                    gc = oc;
+                }
+            }
+            __syncthreads();  // s_val / s_idx of the local argmax are consumed
+            if (lane == 0) {
+                s_val[warp] = gb;
+                s_idx[warp] = gi;
+                s_cta[warp] = gc;
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            double gb = s_val[0];
+            int gi = s_idx[0], gc = s_cta[0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                if (s_val[w] > gb || (s_val[w] == gb && s_idx[w] < gi)) {
+                    gb = s_val[w];
+                    gi = s_idx[w];
+                    gc = s_cta[w];
+                }
             s_fail = 0;
             if (gc < 0 || !isfinite(gb) || gb <= limit) {
                 s_fail = 1;
@@ -625,20 +694,32 @@ __global__ void k_row_scale(const cplx *in, cplx *out, int n, double *row_scale,
     }
 }
 
-// column scales on the row-scaled matrix: one thread per column
-__global__ void k_col_scale(cplx *a, int n, double *col_scale, Status *st) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n || st->code != 0) return;
+// column scales on the row-scaled matrix: one CTA per 32 columns, its 8
+// warps striding over the rows (coalesced 32-column row segments), max
+// reduced in shared memory; then every entry is divided by its column scale.
+__global__ void __launch_bounds__(256) k_col_max(const cplx *a, int n, double *col_scale, Status *st) {
+    __shared__ double part[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane;
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s = fmax(s, hypot(a[(size_t)i * n + j].re, a[(size_t)i * n + j].im));
-    if (s == 0.0) {
-        atomicCAS(&st->code, 0, 5);
-        return;
+    if (j < n)
+        for (int i = warp; i < n; i += 8) s = fmax(s, hypot(a[(size_t)i * n + j].re, a[(size_t)i * n + j].im));
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && j < n) {
+        for (int w = 1; w < 8; ++w) s = fmax(s, part[w][lane]);
+        if (s == 0.0) atomicCAS(&st->code, 0, 5);
+        col_scale[j] = s;
     }
-    col_scale[j] = s;
-    for (int i = 0; i < n; ++i) {
-        cplx v = a[(size_t)i * n + j];
-        a[(size_t)i * n + j] = cplx{v.re / s, v.im / s};
+}
+
+__global__ void k_col_divide(cplx *a, int n, const double *col_scale, const Status *st) {
+    if (st->code != 0) return;
+    size_t nn = (size_t)n * n;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn; t += (size_t)gridDim.x * blockDim.x) {
+        double c = col_scale[t % n];
+        cplx v = a[t];
+        a[t] = cplx{v.re / c, v.im / c};
     }
 }
 
@@ -735,16 +816,8 @@ __global__ void k_trsv_update(const T *a, int n, int k0, int kb, T *x, int nrhs)
         memset(&zero, 0, sizeof(T));
         acc = msub(zero, a[(size_t)i * n + k0 + lane], xr[k0 + lane]);  // -A x
     }
-    double *pa = reinterpret_cast<double *>(&acc);
-#pragma unroll
-    for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pa[w] = warp_sum(pa[w]);
-    if (lane == 0) {
-        T v = xr[i];
-        double *pv = reinterpret_cast<double *>(&v);
-#pragma unroll
-        for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pv[w] += pa[w];
-        xr[i] = v;
-    }
+    acc = warp_sum_t(acc);
+    if (lane == 0) xr[i] = addv(xr[i], acc);
 }
 
 __global__ void k_col_unscale(cplx *x, const double *col_scale, int n, int nrhs) {
@@ -901,8 +974,33 @@ struct PanelScratch {
     void *cand_row = nullptr, *krow = nullptr;
 };
 
+// Optional phase timing of factor_device (extension: peec_gb300_lu_timing):
+// CUDA events around the panel, swap + triangular solve, and trailing update
+// launches of every block column, summed at the end of the factorisation.
+struct LuTiming {
+    bool enabled = false;
+    double ms[3] = {0, 0, 0};        // panel, swaps + trsm, trailing update
+    double flops_update = 0.0;       // algorithmic flops of the trailing updates
+    std::vector<cudaEvent_t> ev;
+};
+static LuTiming g_lu_timing;
+
+static void lu_mark(std::vector<cudaEvent_t> &ev) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream());
+    ev.push_back(e);
+}
+
 template <class T>
 static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status *d_st) {
+    LuTiming &tm = g_lu_timing;
+    if (tm.enabled) {
+        for (auto e : tm.ev) cudaEventDestroy(e);
+        tm.ev.clear();
+        tm.ms[0] = tm.ms[1] = tm.ms[2] = 0.0;
+        tm.flops_update = 0.0;
+    }
     DBuf<unsigned char> scratch;
     PanelScratch sc;
     {
@@ -924,6 +1022,7 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
     }
     for (int k0 = 0; k0 < n; k0 += NB) {
         int kb = std::min(NB, n - k0);
+        if (tm.enabled) lu_mark(tm.ev);
         CoopPlan<T> pl = coop_plan<T>(n - k0);
         if (pl.G > 0) {
             int rows = pl.rows;
@@ -938,10 +1037,17 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
         } else {
             PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
         }
+        if (tm.enabled) lu_mark(tm.ev);
         PEEC_LAUNCH(k_laswp<T>, (n + 255) / 256, 256, 0, d_a, n, k0, kb, d_piv, d_st);
         int rest = n - (k0 + kb);
         if (rest > 0) {
             PEEC_LAUNCH(k_trsm<T>, (rest + 255) / 256, 256, 0, d_a, n, k0, kb, d_st);
+        }
+        if (tm.enabled) {
+            lu_mark(tm.ev);
+            tm.flops_update += (sizeof(T) == sizeof(double) ? 2.0 : 8.0) * (double)rest * rest * kb;
+        }
+        if (rest > 0) {
             if constexpr (sizeof(T) == sizeof(double)) {
                 dim3 g((rest + 63) / 64, (rest + 63) / 64);
                 PEEC_LAUNCH(k_gemm_real, g, 256, 0, (double *)d_a, n, k0, kb, d_st);
@@ -959,6 +1065,15 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
                     PEEC_LAUNCH(k_gemm_cplx, g, 256, 0, (cplx *)d_a, n, k0, kb, d_st);
                 }
             }
+        }
+    }
+    if (tm.enabled) {
+        lu_mark(tm.ev);
+        cudaEventSynchronize(tm.ev.back());
+        for (size_t i = 0; i + 1 < tm.ev.size(); ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
+            tm.ms[i % 3] += ms;
         }
     }
     PEEC_LAUNCH(k_check_diag<T>, (n + 255) / 256, 256, 0, d_a, n, limit, d_st);
@@ -1043,7 +1158,8 @@ static int factor_inplace(T *d_a, int n, double pivot_tolerance, bool cx, long l
         // complex_lu.c:275-302: row scales, then column scales of the row-scaled matrix
         PEEC_LAUNCH(k_row_scale, (unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, (const cplx *)d_a, (cplx *)d_a, n,
                     d_row, st.p);
-        PEEC_LAUNCH(k_col_scale, (n + 127) / 128, 128, 0, (cplx *)d_a, n, d_col, st.p);
+        PEEC_LAUNCH(k_col_max, (n + 31) / 32, 256, 0, (const cplx *)d_a, n, d_col, st.p);
+        PEEC_LAUNCH(k_col_divide, 152 * 16, 256, 0, (cplx *)d_a, n, d_col, st.p);
     }
     PEEC_LAUNCH(k_max_mag<T>, 152 * 8, 256, 0, d_a, nn, mx.p);
     unsigned long long bits = 0;
@@ -1557,4 +1673,369 @@ extern "C" int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double
         return -2;
     }
     return 0;
+}
+
+extern "C" {
+
+// Turn per-phase timing of the allocating factorisations on (1) or off (0).
+void peec_gb300_lu_timing_enable(int on) { g_lu_timing.enabled = on != 0; }
+
+// Phase times of the last timed factorisation (ms) and the algorithmic
+// flops of its trailing updates.
+int peec_gb300_lu_timing(double *ms_panel, double *ms_swap_trsm, double *ms_update, double *update_flops) {
+    if (!g_lu_timing.enabled) return -1;
+    if (ms_panel) *ms_panel = g_lu_timing.ms[0];
+    if (ms_swap_trsm) *ms_swap_trsm = g_lu_timing.ms[1];
+    if (ms_update) *ms_update = g_lu_timing.ms[2];
+    if (update_flops) *update_flops = g_lu_timing.flops_update;
+    return 0;
+}
+
+}  // extern "C"
+
+// =====================================================================
+// Mixed precision: FP32 complex LU with a split-BF16x3 tensor-core
+// trailing update, then FP64 iterative refinement against the FP64 matrix.
+//
+//   equilibrate in FP64 as complex_lu_factorize does (row scales, then
+//   column scales of the row-scaled matrix), round to FP32 complex;
+//   per block column: cooperative FP32 panel (same pivot rule), row swaps,
+//   U12 = L11^-1 A12 in FP32, then split L21 and U12 into BF16 hi/lo parts,
+//     A'  = [Lr_h Lr_h Lr_l Li_h Li_h Li_l]            (K' = 6 x 32)
+//     Br' = [Ur_h Ur_l Ur_h -Ui_h -Ui_l -Ui_h]
+//     Bi' = [Ui_h Ui_l Ui_h  Ur_h  Ur_l  Ur_h]
+//   so that one tcgen05 GEMM with two TMEM accumulators gives
+//     C -= (Lr Ur - Li Ui) + j (Lr Ui + Li Ur)   to ~2^-16 per product;
+//   refinement: x = 0, r = b; repeat { d = LU^-1 r (FP32); x += d;
+//     r = b - Z x (FP64); stop when the componentwise backward error
+//     max |r_i| / (sum_j |Z_ij||x_j| + |b_i|) <= tol }.
+// =====================================================================
+namespace peec {
+
+bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c, int m, int n, int k, int row0,
+                         int col0, long long ldc, int *d_err);
+
+__global__ void k_eq_row_scale(const cplx *z, int n, double *rs, Status *st) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const cplx *row = z + (size_t)warp * n;
+    double s = 0.0;
+    int bad = 0;
+    for (int j = lane; j < n; j += 32) {
+        double m = hypot(row[j].re, row[j].im);
+        if (!isfinite(m)) bad = 1;
+        s = fmax(s, m);
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        s = fmax(s, __shfl_xor_sync(0xffffffffu, s, d));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, d);
+    }
+    if (lane == 0) {
+        if (bad || s == 0.0) atomicCAS(&st->code, 0, bad ? 4 : 5);
+        rs[warp] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_eq_col_scale(const cplx *z, int n, const double *rs, double *cs,
+                                                      Status *st) {
+    __shared__ double part[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane;
+    double s = 0.0;
+    if (j < n)
+        for (int i = warp; i < n; i += 8) {
+            cplx v = z[(size_t)i * n + j];
+            double r = rs[i];
+            s = fmax(s, hypot(v.re / r, v.im / r));
+        }
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && j < n) {
+        for (int w = 1; w < 8; ++w) s = fmax(s, part[w][lane]);
+        if (s == 0.0) atomicCAS(&st->code, 0, 5);
+        cs[j] = s;
+    }
+}
+
+__global__ void k_eq_to_float(const cplx *z, int n, const double *rs, const double *cs, cplxf *f) {
+    size_t nn = (size_t)n * n;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn; t += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(t / n), j = (int)(t % n);
+        cplx v = z[t];
+        double r = rs[i], c = cs[j];
+        f[t] = cplxf{(float)((v.re / r) / c), (float)((v.im / r) / c)};
+    }
+}
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &h, __nv_bfloat16 &l) {
+    h = __float2bfloat16_rn(x);
+    l = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// A' rows r = 0..m-1 <- L21 row k0+kb+r, columns k0..k0+kb-1 (zero-padded to NB)
+__global__ void k_split_a(const cplxf *a, int n, int k0, int kb, int m, __nv_bfloat16 *out) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)m * NB) return;
+    int r = (int)(t / NB), c = (int)(t % NB);
+    cplxf x = c < kb ? a[(size_t)(k0 + kb + r) * n + k0 + c] : cplxf{0.0f, 0.0f};
+    __nv_bfloat16 rh, rl, ih, il;
+    split_bf16(x.re, rh, rl);
+    split_bf16(x.im, ih, il);
+    __nv_bfloat16 *row = out + (size_t)r * 6 * NB;
+    row[c] = rh;
+    row[NB + c] = rh;
+    row[2 * NB + c] = rl;
+    row[3 * NB + c] = ih;
+    row[4 * NB + c] = ih;
+    row[5 * NB + c] = il;
+}
+
+// Br', Bi' rows j = 0..nc-1 <- U12 column k0+kb+j, rows k0..k0+kb-1
+__global__ void k_split_b(const cplxf *a, int n, int k0, int kb, int nc, __nv_bfloat16 *br, __nv_bfloat16 *bi) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nc * NB) return;
+    int c = (int)(t / nc), j = (int)(t % nc);  // consecutive threads read consecutive columns
+    cplxf x = c < kb ? a[(size_t)(k0 + c) * n + k0 + kb + j] : cplxf{0.0f, 0.0f};
+    __nv_bfloat16 rh, rl, ih, il;
+    split_bf16(x.re, rh, rl);
+    split_bf16(x.im, ih, il);
+    __nv_bfloat16 *r = br + (size_t)j * 6 * NB, *q = bi + (size_t)j * 6 * NB;
+    r[c] = rh;
+    r[NB + c] = rl;
+    r[2 * NB + c] = rh;
+    r[3 * NB + c] = __hneg(ih);
+    r[4 * NB + c] = __hneg(il);
+    r[5 * NB + c] = __hneg(ih);
+    q[c] = ih;
+    q[NB + c] = il;
+    q[2 * NB + c] = ih;
+    q[3 * NB + c] = rh;
+    q[4 * NB + c] = rl;
+    q[5 * NB + c] = rh;
+}
+
+// y = P D_r^-1 r in FP32 (the permuted, row-scaled residual)
+__global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int n, int nrhs, cplxf *y) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * nrhs) return;
+    int q = (int)(t / n), i = (int)(t % n), src = perm[i];
+    cplx v = r[(size_t)q * n + src];
+    double s = rs[src];
+    y[t] = cplxf{(float)(v.re / s), (float)(v.im / s)};
+}
+
+// x += D_c^-1 y  (FP64 accumulation of the FP32 correction)
+__global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * nrhs) return;
+    int i = (int)(t % n);
+    double s = cs[i];
+    x[t].re += (double)y[t].re / s;
+    x[t].im += (double)y[t].im / s;
+}
+
+// r = b - Z x in FP64 (one warp per row and right-hand side) and the
+// componentwise backward error, max-reduced as IEEE bits.
+__global__ void k_residual(const cplx *Z, const cplx *x, const cplx *b, int n, int nrhs, cplx *r,
+                           unsigned long long *be) {
+    long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= (long long)n * nrhs) return;
+    int q = (int)(warp / n), i = (int)(warp % n);
+    const cplx *row = Z + (size_t)i * n, *xr = x + (size_t)q * n;
+    double yr = 0.0, yi = 0.0, den = 0.0;
+    for (int j = lane; j < n; j += 32) {
+        cplx z = row[j], v = xr[j];
+        yr = fma(z.re, v.re, yr);
+        yr = fma(-z.im, v.im, yr);
+        yi = fma(z.re, v.im, yi);
+        yi = fma(z.im, v.re, yi);
+        den = fma(hypot(z.re, z.im), hypot(v.re, v.im), den);
+    }
+    yr = warp_sum(yr);
+    yi = warp_sum(yi);
+    den = warp_sum(den);
+    if (lane == 0) {
+        cplx bi = b[(size_t)q * n + i];
+        cplx ri = cplx{bi.re - yr, bi.im - yi};
+        r[(size_t)q * n + i] = ri;
+        double res = hypot(ri.re, ri.im), babs = hypot(bi.re, bi.im);
+        den += babs;
+        double eta = den > 0.0 ? res / den : res;
+        if (!isfinite(eta)) eta = INFINITY;
+        atomicMax(be, (unsigned long long)__double_as_longlong(eta));
+    }
+}
+
+struct MixedTiming {
+    double ms_prepare = 0, ms_factor = 0, ms_refine = 0;
+    int iterations = 0;
+};
+static MixedTiming g_mixed_timing;
+
+}  // namespace peec
+
+extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x,
+                                                     size_t nrhs_, double tol, int max_iter, double *backward_error,
+                                                     int *iterations) {
+    using namespace peec;
+    if (!d_Z || !d_b || !d_x || n_ == 0 || nrhs_ == 0 || n_ > (size_t)0x7fffffff || max_iter < 1) return -1;
+    const int n = (int)n_, nrhs = (int)nrhs_;
+    const size_t nn = n_ * n_, nv = n_ * nrhs_;
+    const cplx *Z = (const cplx *)d_Z;
+    const cplx *b = (const cplx *)d_b;
+    cplx *x = (cplx *)d_x;
+    DBuf<cplxf> f(nn), y(nv);
+    DBuf<cplx> r(nv);
+    DBuf<double> rs(n), cs(n);
+    DBuf<long long> piv(n);
+    DBuf<int> perm(n), err(1);
+    DBuf<Status> st(1);
+    DBuf<unsigned long long> mx(1), be(1);
+    DBuf<__nv_bfloat16> ap((size_t)n * 6 * NB), bpr((size_t)n * 6 * NB), bpi((size_t)n * 6 * NB);
+    DBuf<unsigned char> scratch;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t G = (size_t)sms;
+    size_t sbytes = 256 + 2 * G * 8 + 2 * G * 4 + 16 + 2 * G * NB * sizeof(cplxf) + 2 * NB * sizeof(cplxf) + 64;
+    if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
+        !bpr.p || !bpi.p || !scratch.alloc(sbytes))
+        return -1;
+    cudaEvent_t ev[4];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], stream());
+    cudaMemsetAsync(scratch.p, 0, sbytes, stream());
+    cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
+    cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
+    cudaMemsetAsync(err.p, 0, sizeof(int), stream());
+    PanelScratch sc;
+    {
+        unsigned char *bb = scratch.p;
+        sc.ps = (PanelSlots *)bb;
+        sc.cand_val = (double *)(bb + 256);
+        sc.cand_idx = (int *)(bb + 256 + 2 * G * 8);
+        size_t off = (256 + 2 * G * 8 + 2 * G * 4 + 15) & ~(size_t)15;
+        sc.cand_row = bb + off;
+        sc.krow = bb + off + 2 * G * NB * sizeof(cplxf);
+    }
+    // equilibrate in FP64, round to FP32
+    PEEC_LAUNCH(k_eq_row_scale, (unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, Z, n, rs.p, st.p);
+    PEEC_LAUNCH(k_eq_col_scale, (n + 31) / 32, 256, 0, Z, n, rs.p, cs.p, st.p);
+    PEEC_LAUNCH(k_eq_to_float, 152 * 16, 256, 0, Z, n, rs.p, cs.p, f.p);
+    PEEC_LAUNCH(k_max_mag<cplxf>, 152 * 8, 256, 0, f.p, nn, mx.p);
+    unsigned long long bits = 0;
+    Status hs;
+    cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+    if (!sync("mixed equilibration")) return -1;
+    if (hs.code != 0) return -2;
+    double scale;
+    memcpy(&scale, &bits, sizeof(scale));
+    if (!isfinite(scale) || scale <= 0.0) return -2;
+    const double limit = 1e-14 * scale;
+    cudaEventRecord(ev[1], stream());
+    // FP32 factorisation, trailing updates on the tensor cores
+    cplxf *a = f.p;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        int kb = std::min(NB, n - k0);
+        CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
+        if (pl.G > 0) {
+            int rows = pl.rows;
+            cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
+            Status *stp = st.p;
+            long long *pivp = piv.p;
+            void *args[] = {&a, (void *)&n, (void *)&k0, &kb, &rows, (void *)&limit, &pivp, &stp, &sc.ps,
+                            &sc.cand_val, &sc.cand_idx, &cr, &kr};
+            if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<cplxf>, dim3(pl.G), dim3(256), args,
+                                                     pl.smem, stream()),
+                         "cooperative panel launch"))
+                return -1;
+            note_launch();
+        } else {
+            PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
+        }
+        PEEC_LAUNCH(k_laswp<cplxf>, (n + 255) / 256, 256, 0, a, n, k0, kb, piv.p, st.p);
+        int rest = n - (k0 + kb);
+        if (rest > 0) {
+            PEEC_LAUNCH(k_trsm<cplxf>, (rest + 255) / 256, 256, 0, a, n, k0, kb, st.p);
+            PEEC_LAUNCH(k_split_a, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, ap.p);
+            PEEC_LAUNCH(k_split_b, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, bpr.p,
+                        bpi.p);
+            if (!tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, rest, rest, 6 * NB, k0 + kb, k0 + kb, n, err.p))
+                return -1;
+        }
+    }
+    PEEC_LAUNCH(k_check_diag<cplxf>, (n + 255) / 256, 256, 0, a, n, limit, st.p);
+    size_t perm_smem = n_ * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, piv.p, n, perm.p, st.p);
+    int herr = 0;
+    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+    cudaEventRecord(ev[2], stream());
+    if (!launch_ok("mixed factorisation") || !sync("mixed factorisation")) return -1;
+    if (herr) {
+        set_error("tcgen05 trailing update: a pipeline wait timed out");
+        return -1;
+    }
+    if (hs.code == 6) {
+        set_error("LU panel synchronisation timed out");
+        return -1;
+    }
+    if (hs.code != 0) return -2;
+    // FP64 iterative refinement
+    cudaMemsetAsync(x, 0, nv * sizeof(cplx), stream());
+    cudaMemcpyAsync(r.p, b, nv * sizeof(cplx), cudaMemcpyDeviceToDevice, stream());
+    double eta = INFINITY;
+    int it = 0;
+    const int wpb = 8;
+    for (it = 1; it <= max_iter; ++it) {
+        PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            int kb = std::min(32, n - k0);
+            PEEC_LAUNCH((k_trsv_diag<cplxf, true>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, a, n, k0, kb, y.p, nrhs);
+            size_t rows = (size_t)(n - k0 - kb) * nrhs;
+            if (rows)
+                PEEC_LAUNCH((k_trsv_update<cplxf, true>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, a, n, k0,
+                            kb, y.p, nrhs);
+        }
+        for (int k0 = ((n - 1) / 32) * 32; k0 >= 0; k0 -= 32) {
+            int kb = std::min(32, n - k0);
+            PEEC_LAUNCH((k_trsv_diag<cplxf, false>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, a, n, k0, kb, y.p, nrhs);
+            size_t rows = (size_t)k0 * nrhs;
+            if (rows)
+                PEEC_LAUNCH((k_trsv_update<cplxf, false>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, a, n, k0,
+                            kb, y.p, nrhs);
+        }
+        PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs);
+        cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+        PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, x, b, n, nrhs, r.p, be.p);
+        unsigned long long hb = 0;
+        cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
+        if (!launch_ok("refinement") || !sync("refinement")) return -1;
+        memcpy(&eta, &hb, sizeof(eta));
+        if (eta <= tol) break;
+    }
+    cudaEventRecord(ev[3], stream());
+    cudaEventSynchronize(ev[3]);
+    float t01, t12, t23;
+    cudaEventElapsedTime(&t01, ev[0], ev[1]);
+    cudaEventElapsedTime(&t12, ev[1], ev[2]);
+    cudaEventElapsedTime(&t23, ev[2], ev[3]);
+    g_mixed_timing.ms_prepare = t01;
+    g_mixed_timing.ms_factor = t12;
+    g_mixed_timing.ms_refine = t23;
+    g_mixed_timing.iterations = it > max_iter ? max_iter : it;
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (backward_error) *backward_error = eta;
+    if (iterations) *iterations = it > max_iter ? max_iter : it;
+    return eta <= tol ? 0 : 1;
+}
+
+extern "C" int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine) {
+    if (ms_prepare) *ms_prepare = peec::g_mixed_timing.ms_prepare;
+    if (ms_factor) *ms_factor = peec::g_mixed_timing.ms_factor;
+    if (ms_refine) *ms_refine = peec::g_mixed_timing.ms_refine;
+    return peec::g_mixed_timing.iterations;
 }

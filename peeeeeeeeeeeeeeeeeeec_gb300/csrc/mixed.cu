@@ -1,0 +1,133 @@
+// Mixed-precision building blocks on the tensor cores (tcgen05 + TMA).
+//
+//   tensor maps      cuTensorMapEncodeTiled through the runtime's driver entry
+//                    point (no link-time dependency on libcuda)
+//   tc_gemm_update   C_j[row0.., col0..] -= A B_j^T with BF16 operands and FP32
+//                    accumulation in TMEM (tc_gemm.cuh)
+//   split kernels    FP32 -> BF16 hi + lo, the hi/lo parts laid out along K so
+//                    that one GEMM computes the split-BF16x3 product
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <math.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "../../include/peec_gb300.h"
+#include "common.cuh"
+#include "tc_gemm.cuh"
+
+namespace peec {
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static bool encoder() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    });
+    if (!g_encode) set_error("cuTensorMapEncodeTiled is not available");
+    return g_encode != nullptr;
+}
+
+// 2-D BF16 K-major matrix [rows][k], box {64, box_rows}, 128-byte swizzle.
+static bool make_map_bf16(CUtensorMap *map, const void *base, int rows, int k, int box_rows) {
+    if (!encoder()) return false;
+    if (((uintptr_t)base & 15) || (k * 2) % 16 != 0) {
+        set_error("tensor map: base must be 16-byte aligned and the row pitch a multiple of 16 bytes");
+        return false;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)k * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
+                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return false;
+    }
+    return true;
+}
+
+template <int BN, int J>
+static bool launch_tc(const void *a, const void *b0, const void *b1, float *c0, float *c1, int m, int n, int k,
+                      int row0, int col0, long long ldc, int *d_err, int interleaved = 0) {
+    CUtensorMap ma, mb0, mb1;
+    if (!make_map_bf16(&ma, a, m, k, tc::kBM) || !make_map_bf16(&mb0, b0, n, k, BN)) return false;
+    if (!make_map_bf16(&mb1, J > 1 ? b1 : b0, n, k, BN)) return false;
+    tc::GemmArgs g;
+    g.m = m;
+    g.n = n;
+    g.k = k;
+    g.row0 = row0;
+    g.col0 = col0;
+    g.c[0] = c0;
+    g.c[1] = c1;
+    g.ldc = ldc;
+    g.interleaved = interleaved;
+    g.error = d_err;
+    constexpr size_t smem = tc::smem_bytes<BN, J>();
+    static bool attr = false;
+    if (!attr) {
+        if (!cuda_ok(cudaFuncSetAttribute(tc::k_tc_gemm<BN, J>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                     "tcgen05 GEMM smem attribute"))
+            return false;
+        attr = true;
+    }
+    dim3 grid((n + BN - 1) / BN, (m + tc::kBM - 1) / tc::kBM);
+    PEEC_LAUNCH((tc::k_tc_gemm<BN, J>), grid, 128, smem, ma, mb0, mb1, g);
+    return launch_ok("tcgen05 GEMM");
+}
+
+// C_j -= A B_j^T; J = 1 or 2; K multiple of 64; returns false on failure.
+bool tc_gemm_update(const void *a, const void *b0, const void *b1, float *c0, float *c1, int m, int n, int k,
+                    int row0, int col0, long long ldc, int J, int *d_err) {
+    if (k % tc::kBK != 0 || m <= 0 || n <= 0) {
+        set_error("tcgen05 GEMM: K must be a positive multiple of 64");
+        return false;
+    }
+    if (J == 1) return launch_tc<128, 1>(a, b0, nullptr, c0, nullptr, m, n, k, row0, col0, ldc, d_err);
+    return launch_tc<128, 2>(a, b0, b1, c0, c1, m, n, k, row0, col0, ldc, d_err);
+}
+
+// Complex C (interleaved FP32, leading dimension ldc complex elements)
+// [row0.., col0..] -= (A Br^T) + j (A Bi^T).
+bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c, int m, int n, int k, int row0,
+                         int col0, long long ldc, int *d_err) {
+    if (k % tc::kBK != 0 || m <= 0 || n <= 0) {
+        set_error("tcgen05 GEMM: K must be a positive multiple of 64");
+        return false;
+    }
+    return launch_tc<128, 2>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
+}
+
+}  // namespace peec
+
+using namespace peec;
+
+// Test / building-block entry point: C_j (FP32 row-major, ld = ldc) -= A B_j^T
+// for device BF16 matrices A [m][k] and B_j [n][k].
+extern "C" int peec_gb300_tc_gemm(const void *d_a, const void *d_b0, const void *d_b1, float *d_c0, float *d_c1,
+                                  int m, int n, int k, long long ldc, int J) {
+    if (!d_a || !d_b0 || !d_c0 || (J == 2 && (!d_b1 || !d_c1)) || (J != 1 && J != 2)) return -1;
+    DBuf<int> err(1);
+    if (!err.p) return -1;
+    cudaMemsetAsync(err.p, 0, sizeof(int), stream());
+    if (!tc_gemm_update(d_a, d_b0, d_b1, d_c0, d_c1, m, n, k, 0, 0, ldc, J, err.p)) return -1;
+    int h = 0;
+    cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+    if (!sync("tcgen05 GEMM")) return -1;
+    if (h) {
+        set_error("tcgen05 GEMM: a pipeline wait timed out");
+        return -1;
+    }
+    return 0;
+}

@@ -146,3 +146,65 @@ void peec_gb300_event_destroy(void *e) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------
+// FP64 / FP32 issue-rate probes: the roofline denominators for the FP64-
+// and FP32-pipe kernels (the machine's measured peaks cover HBM and BF16 only).
+// Independent FMA chains per thread, 8 CTAs per SM, CUDA-event timed.
+// ---------------------------------------------------------------------
+namespace peec {
+__global__ void k_probe_dfma(double *out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b);
+        x1 = fma(x1, a, b);
+        x2 = fma(x2, a, b);
+        x3 = fma(x3, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
+__global__ void k_probe_ffma(float *out, int iters, float a, float b) {
+    float x[8];
+    for (int j = 0; j < 8; ++j) x[j] = threadIdx.x * 1e-3f + j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fmaf(x[j], a, b);
+    }
+    float s = 0;
+    for (int j = 0; j < 8; ++j) s += x[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace peec
+
+extern "C" int peec_gb300_pipe_peaks(double *fp64_tflops, double *fp32_tflops) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int blocks = sms * 8, threads = 256;
+    size_t n = (size_t)blocks * threads;
+    peec::DBuf<double> d(n);
+    peec::DBuf<float> f(n);
+    if (!d.p || !f.p) return -1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms = 0;
+    const int itd = 2048, itf = 32768;
+    PEEC_LAUNCH(peec::k_probe_dfma, blocks, threads, 0, d.p, 16, 1.0000001, 1e-9);
+    cudaEventRecord(e0, peec::stream());
+    PEEC_LAUNCH(peec::k_probe_dfma, blocks, threads, 0, d.p, itd, 1.0000001, 1e-9);
+    cudaEventRecord(e1, peec::stream());
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (fp64_tflops) *fp64_tflops = 2.0 * 4 * itd * (double)n / (ms * 1e9);
+    PEEC_LAUNCH(peec::k_probe_ffma, blocks, threads, 0, f.p, 16, 1.0000001f, 1e-9f);
+    cudaEventRecord(e0, peec::stream());
+    PEEC_LAUNCH(peec::k_probe_ffma, blocks, threads, 0, f.p, itf, 1.0000001f, 1e-9f);
+    cudaEventRecord(e1, peec::stream());
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (fp32_tflops) *fp32_tflops = 2.0 * 8 * itf * (double)n / (ms * 1e9);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return peec::sync("pipe peak probe") ? 0 : -1;
+}

@@ -1,0 +1,286 @@
+// tcgen05 tensor-core GEMM for sm_103a: TMA-fed shared-memory operands, FP32
+// accumulators in tensor memory (TMEM), one elected thread issuing the MMAs.
+//
+//   D_j[128 x BN] = A[128 x K] * B_j[BN x K]^T      (j < J, BF16 in, FP32 acc)
+//   C_j[rows, cols] -= D_j                            (epilogue, FP32 in HBM)
+//
+// A and every B_j are K-major BF16 matrices in global memory described by TMA
+// tensor maps (box 64 x rows, 128-byte swizzle).  Splitting FP32 operands
+// into BF16 hi/lo parts and concatenating the parts along K turns one call
+// into the split-BF16x3 product  Ah Bh + Ah Bl + Al Bh  (FP32-equivalent),
+// and stacking real / imaginary parts along K gives the complex update with
+// J = 2 accumulators that share the A tile.
+//
+// Warp roles (4 warps, 128 threads): warp 0 allocates TMEM and one of its
+// lanes drives TMA; one lane of warp 1 issues tcgen05.mma; after the last MMA
+// commits, all four warps read their 32 TMEM lanes (tcgen05.ld 32x32b) and
+// update C.  Every mbarrier wait is bounded: on timeout the kernel records
+// an error, stops issuing work, waits (bounded) for what it issued, frees
+// TMEM and returns.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace peec {
+namespace tc {
+
+static const int kBM = 128;       // rows per tile (one TMEM lane each)
+static const int kBK = 64;        // K per stage: 64 BF16 = one 128-byte swizzle row
+static const int kStages = 4;
+static const long long kWaitLimit = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+    for (long long i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 1023) == 1023 && *abort_flag) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *smem_dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major, 128-byte swizzle: 8-row groups of
+// 128-byte rows, 1024 bytes apart (SBO); start address in 16-byte units.
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void *smem) {
+    uint64_t addr = smem_u32(smem);
+    uint64_t d = 0;
+    d |= (addr >> 4) & 0x3FFFull;        // start address
+    d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+    d |= (uint64_t)1 << 46;              // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;              // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+    return (1u << 4)                       // D format F32
+           | (1u << 7)                     // A format BF16
+           | (1u << 10)                    // B format BF16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *smem_result, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(smem_result)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmArgs {
+    int m, n;           // rows of A / C block and rows of B / columns of the C block
+    int k;              // K (multiple of 64)
+    int row0, col0;     // offset of the updated block in C (A and B start at row 0)
+    float *c[2];        // C_j, row-major
+    long long ldc;      // leading dimension of C (in complex elements when interleaved)
+    int interleaved;    // 1: J = 2 accumulators are the re / im parts of one complex C
+    int *error;         // set to 1 on a wait timeout
+};
+
+// grid: (ceil(n / BN), ceil(m / 128)); block 128; dynamic smem = smem_bytes<BN, J>()
+template <int BN, int J>
+__host__ __device__ constexpr size_t smem_bytes() {
+    return (size_t)kStages * ((size_t)kBM * kBK * 2 + (size_t)J * BN * kBK * 2) + 1024 + 256;
+}
+
+template <int BN, int J>
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b0,
+              const __grid_constant__ CUtensorMap map_b1, GemmArgs args) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // stage buffers on a 1024-byte boundary (128-byte swizzle atoms)
+    unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const size_t a_bytes = (size_t)kBM * kBK * 2, b_bytes = (size_t)BN * kBK * 2;
+    const size_t stage_bytes = a_bytes + J * b_bytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + kStages * stage_bytes);
+    uint64_t *empty = full + kStages;
+    uint64_t *done = empty + kStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile_n = blockIdx.x * BN, tile_m = blockIdx.y * kBM;
+    const int ktiles = args.k / kBK;
+    constexpr uint32_t kTmemCols = (J * BN <= 32) ? 32 : (J * BN <= 64) ? 64 : (J * BN <= 128) ? 128 : (J * BN <= 256) ? 256 : 512;
+
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    volatile int *abort_flag = &s_abort;
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer
+        for (int kt = 0; kt < ktiles; ++kt) {
+            int s = kt % kStages;
+            if (kt >= kStages) {
+                if (!mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, abort_flag)) {
+                    s_abort = 1;
+                    break;
+                }
+            }
+            unsigned char *sa = base + s * stage_bytes;
+            mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+            tma_load_2d(sa, &map_a, kt * kBK, tile_m, &full[s]);
+            tma_load_2d(sa + a_bytes, &map_b0, kt * kBK, tile_n, &full[s]);
+            if (J > 1) tma_load_2d(sa + a_bytes + b_bytes, &map_b1, kt * kBK, tile_n, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = idesc_bf16_f32(kBM, BN);
+        for (int kt = 0; kt < ktiles; ++kt) {
+            int s = kt % kStages;
+            if (!mbar_wait(&full[s], (kt / kStages) & 1, abort_flag)) {
+                s_abort = 1;
+                break;
+            }
+            fence_after_sync();
+            unsigned char *sa = base + s * stage_bytes;
+            uint64_t ad = smem_desc_sw128(sa);
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                uint64_t bd = smem_desc_sw128(sa + a_bytes + j * b_bytes);
+#pragma unroll
+                for (int kk = 0; kk < kBK / 16; ++kk) {
+                    // +32 bytes along K inside the swizzle row = +2 in 16-byte units
+                    mma_bf16(tmem + j * BN, ad + 2 * kk, bd + 2 * kk, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(&empty[s]);
+        }
+        mma_commit(done);
+    }
+    __syncwarp();
+    // epilogue: wait for the accumulators
+    bool ok = mbar_wait(done, 0, abort_flag);
+    if (!ok) s_abort = 1;
+    fence_after_sync();
+    __syncthreads();
+    if (!s_abort) {
+        const int row = tile_m + warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(lane_addr + j * BN + c0, v);
+                if (row < args.m) {
+                    int lim = args.n - (tile_n + c0);
+                    if (args.interleaved) {
+                        float *crow =
+                            args.c[0] + ((size_t)(args.row0 + row) * args.ldc + args.col0 + tile_n + c0) * 2 + j;
+#pragma unroll
+                        for (int t = 0; t < 32; ++t)
+                            if (t < lim) crow[2 * t] -= v[t];
+                    } else {
+                        float *crow = args.c[j] + (size_t)(args.row0 + row) * args.ldc + args.col0 + tile_n + c0;
+#pragma unroll
+                        for (int t = 0; t < 32; ++t)
+                            if (t < lim) crow[t] -= v[t];
+                    }
+                }
+            }
+        }
+    } else {
+        if (threadIdx.x == 0) atomicExch(args.error, 1);
+        // give copies already issued time to land before the CTA's shared
+        // memory and TMEM are released (bounded)
+        for (int i = 0; i < 20000; ++i) __nanosleep(1000);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+}  // namespace tc
+}  // namespace peec

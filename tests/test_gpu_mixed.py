@@ -1,0 +1,134 @@
+"""Mixed-precision complex solve (FP32 LU with a split-BF16x3 tcgen05 trailing
+update, FP64 iterative refinement) against the FP64 path.
+
+Gate: componentwise backward error <= 1e-10 (the harmonic driver's
+acceptance test), and the refined solution agrees with the plain FP64 LU
+solution to the accuracy that backward error allows."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import ComplexLU, rel_err
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+
+pytestmark = pytest.mark.gpu
+
+
+def dev_put(lib, arr):
+    p = lib.peec_gb300_device_alloc(arr.nbytes)
+    assert lib.peec_gb300_copy_to_device(p, arr.ctypes.data, arr.nbytes) == 0
+    return p
+
+
+def mixed_solve(lib, Z, B, tol=1e-10, max_iter=30):
+    Z = np.ascontiguousarray(Z, dtype=np.complex128)
+    B = np.ascontiguousarray(B, dtype=np.complex128)
+    n = Z.shape[0]
+    nrhs = 1 if B.ndim == 1 else B.shape[0]
+    dZ, dB = dev_put(lib, Z), dev_put(lib, B)
+    dX = lib.peec_gb300_device_alloc(B.nbytes)
+    be, it = C.c_double(), C.c_int()
+    s = lib.peec_gb300_complex_solve_mixed_device(dZ, n, dB, dX, nrhs, tol, max_iter, C.byref(be), C.byref(it))
+    X = np.zeros_like(B)
+    lib.peec_gb300_copy_to_host(X.ctypes.data, dX, X.nbytes)
+    Zback = np.zeros_like(Z)
+    lib.peec_gb300_copy_to_host(Zback.ctypes.data, dZ, Z.nbytes)
+    for p in (dZ, dB, dX):
+        lib.peec_gb300_device_free(p)
+    assert np.array_equal(Zback, Z)  # the input matrix is not modified
+    return s, X, be.value, it.value
+
+
+def backward_error(Z, x, b):
+    r = Z @ x - b
+    return np.max(np.abs(r) / (np.abs(Z) @ np.abs(x) + np.abs(b)))
+
+
+@pytest.mark.parametrize("n", [64, 300, 513])
+def test_random_systems(gpu_lib, n):
+    rng = np.random.default_rng(n)
+    Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + n ** 0.5 * np.eye(n)
+    Z *= np.logspace(-4, 4, n)[:, None]  # badly scaled rows: equilibration matters
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    s, x, be, it = mixed_solve(gpu_lib, Z, b)
+    assert s == 0, (be, it)
+    assert be <= 1e-10 and backward_error(Z, x, b) <= 1e-10
+    assert rel_err(x, np.linalg.solve(Z, b)) < 1e-8
+
+
+def test_multiple_right_hand_sides(gpu_lib):
+    rng = np.random.default_rng(7)
+    n, k = 200, 4
+    Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 10 * np.eye(n)
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    s, X, be, it = mixed_solve(gpu_lib, Z, B)
+    assert s == 0
+    for q in range(k):
+        assert backward_error(Z, X[q], B[q]) <= 1e-10
+
+
+def test_peec_box_system_matches_plain_fp64(gpu_lib):
+    """Harmonic MNA matrix of a small PEC box at 30 MHz (assembled on the
+    GPU): the mixed solve reaches the 1e-10 gate and agrees with the plain
+    FP64 complex LU."""
+    with SynthMesh.box(0.4, 0.2, 0.1, 16, 8, 4) as m:
+        ne, nv = m.n_edges, m.n_nodes
+        n = ne + nv
+        lo = abi.InductanceOptions()
+        gpu_lib.inductance_options_default(C.byref(lo), 1)
+        po = abi.PotentialOptions()
+        gpu_lib.potential_options_default(C.byref(po), 1)
+        dL = gpu_lib.peec_gb300_device_alloc(ne * ne * 8)
+        dP = gpu_lib.peec_gb300_device_alloc(nv * nv * 8)
+        dZ = gpu_lib.peec_gb300_device_alloc(n * n * 16)
+        edges = np.ascontiguousarray(m.edges())
+        dE = dev_put(gpu_lib, edges)
+        assert gpu_lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(lo), dL, None) == 0
+        assert gpu_lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(po), dP, None) == 0
+        assert gpu_lib.peec_gb300_harmonic_build_device(dL, dP, dE, None, ne, nv, 30e6, dZ) == 0
+        Z = np.zeros((n, n), dtype=np.complex128)
+        gpu_lib.peec_gb300_copy_to_host(Z.ctypes.data, dZ, Z.nbytes)
+        for p in (dL, dP, dZ, dE):
+            gpu_lib.peec_gb300_device_free(p)
+    rng = np.random.default_rng(3)
+    b = np.zeros(n, dtype=np.complex128)
+    b[:ne] = rng.standard_normal(ne) + 1j * rng.standard_normal(ne)
+    s, x, be, it = mixed_solve(gpu_lib, Z, b)
+    assert s == 0, (be, it)
+    assert backward_error(Z, x, b) <= 1e-10
+    f = ComplexLU(gpu_lib, Z)
+    assert f.status == 0
+    _, xp = f.solve(b)
+    f.free()
+    assert rel_err(x, xp) < 1e-7
+
+
+def test_singular_and_bad_input(gpu_lib):
+    Z = np.eye(40, dtype=np.complex128)
+    Z[5, :] = 0
+    s, _, _, _ = mixed_solve(gpu_lib, Z, np.ones(40, dtype=np.complex128))
+    assert s == -2
+
+
+def test_fp32_far_field_assembly_error(gpu_lib, oracle):
+    """Mixed path assembly: FP32 far rule (near field still FP64).  The error
+    against the FP64 oracle is stated: below 1e-6 relative per entry."""
+    from helpers import inductance, potential
+    with SynthMesh.box(0.3, 0.2, 0.1, 6, 4, 2) as m:
+        prev = gpu_lib.peec_gb300_set_far_precision(2)
+        try:
+            s, L = inductance(gpu_lib, m)
+            s2, P = potential(gpu_lib, m)
+        finally:
+            gpu_lib.peec_gb300_set_far_precision(prev)
+        assert s == 0 and s2 == 0
+        Lo, Po = oracle.inductance(m)[1], oracle.potential(m)[1]
+        nz = Lo != 0
+        assert np.array_equal(L != 0, nz)
+        assert np.max(np.abs(L[nz] - Lo[nz]) / np.abs(Lo[nz])) < 1e-6
+        assert np.max(np.abs(P - Po) / np.abs(Po)) < 1e-6
+        # and the default mode is back to FP64-accurate
+        s, L2 = inductance(gpu_lib, m)
+        assert np.max(np.abs(L2[nz] - Lo[nz]) / np.abs(Lo[nz])) < 1e-12
