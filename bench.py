@@ -221,7 +221,9 @@ class DeviceSolve:
         for tag, st in (("Lp", self.stL), ("P", self.stP)):
             for f in ("ms_prepare", "ms_near", "ms_far"):
                 self.phase_ms.setdefault(tag + "_" + f[3:], []).append(getattr(st, f))
-        self.work = {"Lp_near_pairs": self.stL.near_pairs, "Lp_potential_evals": self.stL.potential_evaluations,
+        self.work = {"Lp_near_pairs": self.stL.near_pairs, "Lp_near_pairs_evaluated": self.stL.near_pairs_evaluated,
+                     "P_near_pairs_evaluated": self.stP.near_pairs_evaluated,
+                     "Lp_potential_evals": self.stL.potential_evaluations,
                      "Lp_far_point_pairs": self.stL.far_point_pairs,
                      "P_near_pairs": self.stP.near_pairs, "P_potential_evals": self.stP.potential_evaluations,
                      "P_far_point_pairs": self.stP.far_point_pairs}
@@ -453,9 +455,17 @@ def main():
         mbes = [ds.step_mixed() for _ in range(args.steps)]
         m1 = lib.peec_gb300_event_record()
         mixed_ms = lib.peec_gb300_event_elapsed_ms(m0, m1) / args.steps
+        # one more mixed solve with the factorisation's phase timing on
+        lib.peec_gb300_lu_timing_enable(1)
+        ds.step_mixed()
+        mt = [C.c_double() for _ in range(4)]
+        lib.peec_gb300_lu_timing(*[C.byref(x) for x in mt])
+        lib.peec_gb300_lu_timing_enable(0)
+        mixed_lu = {"panel_ms": mt[0].value, "swap_trsm_split_ms": mt[1].value, "tc_update_ms": mt[2].value,
+                    "tc_update_issued_bf16_flops": mt[3].value}
         mixed = {"value": world * 1000.0 / mixed_ms, "unit": "solves/s", "ms_per_step": mixed_ms,
                  "vs_plain_fp64_gpu": (1000.0 / mixed_ms) / (1000.0 / ms_step),
-                 "backward_error": max(mbes), "refinement_iterations": ds.mixed_iters,
+                 "backward_error": max(mbes), "refinement_iterations": ds.mixed_iters, "lu_phases": mixed_lu,
                  "phase_ms": {k: statistics.median(v) for k, v in ds.phase_ms_mixed.items()},
                  "precision": "FP32 far field (near field FP64), FP32 LU with split-BF16x3 tcgen05 trailing "
                               "update (FP32 accumulation), FP64 iterative refinement"}
@@ -494,6 +504,20 @@ def main():
                "phase_seconds": {k: round(v, 2) for k, v in parts.items()}}
 
     roofs = roofline(phases, lu_phases, m, p64.value, p32.value, ds.work)
+    if mixed and mixed["lu_phases"].get("tc_update_ms"):
+        ml = mixed["lu_phases"]
+        bf16 = 1933.8
+        try:
+            with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+                bf16 = json.load(f).get("bf16_tflops", bf16)
+        except Exception:
+            pass
+        a = ml["tc_update_issued_bf16_flops"] / (ml["tc_update_ms"] * 1e-3) / 1e12
+        roofs.append({"kernel": "k_tc_gemm (mixed path: tcgen05 split-BF16x3 complex trailing update)",
+                      "bound": "tensor", "achieved": a, "peak": bf16, "unit": "TFLOP/s", "frac": a / bf16,
+                      "ms": ml["tc_update_ms"], "traffic": load_traffic().get("k_tc_gemm"),
+                      "peak_source": "measured (MEASURED_PEAKS.json, cuBLAS BF16 burst)",
+                      "note": "issued BF16 flops: 2 accumulators x 2 x m x n x 192 per block column"})
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -28,6 +28,7 @@ typedef struct
     unsigned long long near_pairs;             /* non-FAR patch pairs integrated analytically */
     unsigned long long potential_evaluations;  /* analytic triangle-potential evaluations     */
     unsigned long long far_point_pairs;        /* far-rule 1/R point pairs (FAR patch pairs x (2q^2)^2) */
+    unsigned long long near_pairs_evaluated;   /* near pairs integrated (the rest reuse a translated copy) */
     double ms_prepare;                         /* patch prep + near-pair discovery (CUDA events) */
     double ms_near;                            /* adaptive near-field kernels                 */
     double ms_far;                             /* tiled far-field + combine kernel            */
@@ -76,6 +77,11 @@ int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual,
  * 2 FP32 with FP32 accumulation (mixed-precision path, ~1e-7 relative).
  * Returns the previous mode.  Not thread-safe against concurrent assemblies. */
 int peec_gb300_set_far_precision(int mode);
+
+/* Reuse of translated near pairs (default on): near patch pairs whose
+ * corners are translated copies of each other (to a few ulps of the largest
+ * coordinate) share one adaptive evaluation.  Returns the previous setting. */
+int peec_gb300_set_near_reuse(int on);
 
 /* ---- dense factorisations of device-resident matrices (in place) ----
  * Same algorithm, numerics and error codes as lu_factorize /

@@ -158,7 +158,7 @@ DROP_IN_SYMBOLS = [
 
 class PeecAssemblyStats(C.Structure):
     _fields_ = [("near_pairs", C.c_ulonglong), ("potential_evaluations", C.c_ulonglong),
-                ("far_point_pairs", C.c_ulonglong),
+                ("far_point_pairs", C.c_ulonglong), ("near_pairs_evaluated", C.c_ulonglong),
                 ("ms_prepare", C.c_double), ("ms_near", C.c_double), ("ms_far", C.c_double)]
 
 
@@ -184,6 +184,7 @@ EXT_SYMBOLS = [
     ("peec_gb300_potential_device", C.c_int,
      [P(Mesh), P(DualMesh), P(PotentialOptions), C.c_void_p, P(PeecAssemblyStats)]),
     ("peec_gb300_set_far_precision", C.c_int, [C.c_int]),
+    ("peec_gb300_set_near_reuse", C.c_int, [C.c_int]),
     ("peec_gb300_lu_factor_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_double, C.c_void_p, C.c_void_p, c_double_p, c_int_p]),
     ("peec_gb300_lu_factor_device_noalloc", C.c_int,

@@ -74,6 +74,7 @@ struct RegionsDev {
     double *dir = nullptr;     // [n*3]   (inductance)
     double *scale = nullptr;   // [n]     width w (inductance) or area S (potential); <= 0 marks a bad region
     int *same_obj = nullptr;   // [np]    object id for the reference's pointer test
+    double cmax = 0.0;         // largest |corner coordinate| (scale of the rounding noise)
 };
 
 // one far-rule point: position and weight (32-byte aligned for vector loads)
@@ -309,7 +310,7 @@ struct NearWarpSmem {
 // right.  Returns NaN if a rule is non-finite or depth 24 is exceeded
 // (reference quadrature.c:915-938).
 __device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order, double abs_tol,
-                                unsigned long long &evals) {
+                                unsigned long long &evals, bool &marginal) {
     const int lane = threadIdx.x & 31;
     const int ql = order <= 6 ? 3 : 4;
     const int rl = gl_row(ql), rh = gl_row(order);
@@ -354,20 +355,29 @@ __device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order
         lo = warp_sum(lo);
         hi = warp_sum(hi);
         if (!isfinite(lo) || !isfinite(hi)) return nan("");
+        // a decision within 1e-6 of its threshold could go the other way for
+        // a copy of this pair that differs only by rounding of its corners
+        double thr = nd.tol + 2e-5 * fabs(hi), gap = fabs(hi - lo);
+        if (fabs(gap - thr) <= 1e-6 * thr) marginal = true;
         if (fabs(hi - lo) <= nd.tol + 2e-5 * fabs(hi)) {
             acc += hi;
             continue;
         }
         if (nd.depth >= 24 || sp + 2 > kStackCap) return nan("");
         int e = 0;
-        double longest = 0.0;
+        double longest = 0.0, len[3];
         for (int i = 0; i < 3; ++i) {
             double s = dist3(nd.v + 3 * i, nd.v + 3 * ((i + 1) % 3));
+            len[i] = s;
             if (s > longest) {
                 longest = s;
                 e = i;
             }
         }
+        // two (nearly) equal longest edges: which one is bisected is decided
+        // by rounding, so a translated copy may subdivide differently
+        for (int i = 0; i < 3; ++i)
+            if (i != e && len[i] >= longest * (1.0 - 1e-10)) marginal = true;
         int j = (e + 1) % 3, k = (e + 2) % 3;
         if (lane == 0) {
             AdaptNode &left = sm.stack[sp + 1], &right = sm.stack[sp];
@@ -399,12 +409,14 @@ __device__ __forceinline__ void patch_triangle(const double *c, int t, double *v
 struct NearEvalArgs {
     const double *corner;
     const NearRec *rec;
-    int nrec;
+    const int *job_rec;  // records to evaluate (representatives), or null for all
+    int nrec;            // number of records to evaluate
     int orders[4];  // far, near, touching, self
     double *slot;   // [nrec*4*2]
     int *kind;      // [nrec*4]: 0 adaptive, 1 zero area, 2 identical triangles
     int *next_job;  // work counter
     unsigned long long *evals;
+    int *marginal;  // [nrec] set to 1 if an adaptive decision was within 1e-6 of its threshold
 };
 
 // One warp per job (record, triangle pair t = s*2+u, direction d); warps
@@ -422,6 +434,7 @@ __global__ void __launch_bounds__(256, 2) k_near_eval(NearEvalArgs A) {
         job = __shfl_sync(0xffffffffu, job, 0);
         if (job >= njobs) break;
         int r = (int)(job >> 3), t = (int)((job >> 1) & 3), d = (int)(job & 1);
+        if (A.job_rec) r = A.job_rec[r];
         NearRec rec = A.rec[r];
         double ta[9], tb[9];
         patch_triangle(A.corner + 12 * (size_t)rec.i, t >> 1, ta);
@@ -462,7 +475,9 @@ __global__ void __launch_bounds__(256, 2) k_near_eval(NearEvalArgs A) {
                 double aa = d == 0 ? po.twice_area : sm.inner.twice_area;
                 double ab = d == 0 ? sm.inner.twice_area : po.twice_area;
                 double scale = aa * ab / sqrt(fmax(aa, ab));
-                out = warp_adaptive(outer, sm, order, 2e-5 * scale, evals);
+                bool marg = false;
+                out = warp_adaptive(outer, sm, order, 2e-5 * scale, evals, marg);
+                if (marg && lane == 0 && A.marginal) atomicOr(A.marginal + r, 1);
             }
         }
         if (lane == 0) {
@@ -504,6 +519,132 @@ __global__ void k_near_finalize(int nrec, const double *slot, const int *kind, d
         kr += v;
     }
     kval[r] = make_double2(bad_f ? nan("") : kf, bad_r ? nan("") : kr);
+}
+
+// ---------------------------------------------------------------------
+// 5b. reuse of translated near pairs
+//
+// The near-pair integral depends only on the two patches' corners relative
+// to each other.  On meshes with repeated cells most near pairs are
+// translated copies of a few hundred configurations (5 cm box: 56 k P pairs,
+// 251 distinct; 69 k Lp pairs, 318 distinct).  Each record gets a key: its
+// 21 corner offsets relative to corner 0 of patch i, quantised to delta (a
+// few ulps of the largest coordinate, so copies that differ only by rounding
+// share a key), plus its class and same-object flag.  Records with equal
+// keys share one evaluation: the representative is the lowest record index
+// of the group (deterministic), and a full-key comparison guards against
+// hash collisions.  Copies differ from their representative by at most
+// delta in each offset, far below the parity tolerance.
+// ---------------------------------------------------------------------
+static const int kKeyLen = 21;
+
+// strided int fill (used to initialise the representative field of the table)
+__global__ void k_fill_int(int *base, long long count, int stride_ints, int value) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) base[t * stride_ints] = value;
+}
+
+struct MemoSlot {
+    unsigned long long hash;  // 0 = empty
+    int rep;
+    int pad;
+};
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long h, unsigned long long v) {
+    h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    h *= 0xff51afd7ed558ccdull;
+    return h ^ (h >> 29);
+}
+
+// keys[r*22]: 21 quantised offsets + (cls | same_object << 8); ok[r] = 0 if
+// an offset does not fit the quantisation range (the record is then never
+// shared)
+__global__ void k_memo_keys(const double *corner, const int *same_obj, const NearRec *rec, int nrec, double delta,
+                            long long *keys, unsigned long long *hash, int *ok) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    NearRec q = rec[r];
+    const double *ci = corner + 12 * (size_t)q.i, *cj = corner + 12 * (size_t)q.j;
+    long long *key = keys + (size_t)r * (kKeyLen + 1);
+    unsigned long long h = 0x1234567ull;
+    int good = 1;
+    for (int t = 0; t < kKeyLen; ++t) {
+        double v = t < 9 ? ci[3 + t] - ci[t % 3] : cj[t - 9] - ci[(t - 9) % 3];
+        double qv = rint(v / delta);
+        if (!(fabs(qv) < 9.0e15)) {
+            good = 0;
+            qv = 0.0;
+        }
+        key[t] = (long long)qv;
+        h = mix64(h, (unsigned long long)key[t]);
+    }
+    long long tag = (long long)q.cls | ((long long)(same_obj[q.i] == same_obj[q.j]) << 8);
+    key[kKeyLen] = tag;
+    h = mix64(h, (unsigned long long)tag);
+    hash[r] = h | 1ull;
+    ok[r] = good;
+}
+
+__global__ void k_memo_insert(int nrec, const unsigned long long *hash, const int *ok, MemoSlot *tab,
+                              unsigned long long mask, int *slot_of) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    if (!ok[r]) {
+        slot_of[r] = -1;
+        return;
+    }
+    unsigned long long h = hash[r], s = h & mask;
+    for (unsigned long long probe = 0; probe <= mask; ++probe) {  // bounded: the table is never full
+        unsigned long long prev = atomicCAS(&tab[s].hash, 0ull, h);
+        if (prev == 0ull || prev == h) {
+            atomicMin(&tab[s].rep, r);
+            slot_of[r] = (int)s;
+            return;
+        }
+        s = (s + 1) & mask;
+    }
+    slot_of[r] = -1;
+}
+
+// rep[r] = representative record; is_rep[r] = 1 for representatives
+__global__ void k_memo_resolve(int nrec, const long long *keys, const MemoSlot *tab, const int *slot_of, int *rep,
+                               int *is_rep) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    int rr = r;
+    if (slot_of[r] >= 0) {
+        int r0 = tab[slot_of[r]].rep;
+        if (r0 != r) {
+            const long long *a = keys + (size_t)r * (kKeyLen + 1), *b = keys + (size_t)r0 * (kKeyLen + 1);
+            bool same = true;
+            for (int t = 0; t <= kKeyLen; ++t)
+                if (a[t] != b[t]) same = false;
+            if (same) rr = r0;
+        }
+    }
+    rep[r] = rr;
+    is_rep[r] = rr == r;
+}
+
+__global__ void k_memo_compact(int nrec, const int *is_rep, const int *off, int *list) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec || !is_rep[r]) return;
+    list[off[r]] = r;
+}
+
+// copies of a marginal representative are evaluated on their own
+__global__ void k_memo_recheck(int nrec, const int *rep, const int *marginal, int *flag) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    int r0 = rep[r];
+    flag[r] = (r0 != r && marginal[r0]) ? 1 : 0;
+}
+
+__global__ void k_memo_scatter(int nrec, const int *rep, const int *marginal, double2 *kval) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    int r0 = rep[r];
+    if (r0 != r && !marginal[r0]) kval[r] = kval[r0];
 }
 
 // ---------------------------------------------------------------------
@@ -881,6 +1022,8 @@ struct DeviceRegions {
         view.size = size.p;
         view.dir = dir.p;
         view.scale = scale.p;
+        view.cmax = 0.0;
+        for (double v : H.corner) view.cmax = fmax(view.cmax, fabs(v));
         if (ok && np) {
             PEEC_LAUNCH(k_patch_prep, (np + 127) / 128, 128, 0, view);
             ok = launch_ok("patch preparation");
@@ -898,6 +1041,17 @@ struct AssemblyOptions {
 // Far rule arithmetic: 1 double-float on the FP32 pipes (default), 0 native
 // FP64 (PEEC_GB300_FAR=fp64), 2 FP32 (PEEC_GB300_FAR=fp32, or
 // peec_gb300_set_far_precision for the mixed-precision path).
+static int g_near_reuse = -1;
+// Reuse of translated near pairs: on unless PEEC_GB300_NEAR_REUSE=0 or
+// peec_gb300_set_near_reuse(0).
+static bool near_reuse_enabled() {
+    if (g_near_reuse < 0) {
+        const char *e = getenv("PEEC_GB300_NEAR_REUSE");
+        g_near_reuse = (e && strcmp(e, "0") == 0) ? 0 : 1;
+    }
+    return g_near_reuse == 1;
+}
+
 static int g_far_mode = -1;
 static int far_mode_df() {
     if (g_far_mode < 0) {
@@ -957,13 +1111,48 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     DBuf<double2> kval(nrec);
     if (nrec && (!rec.p || !slot.p || !kindbuf.p || !kval.p)) return -1;
     cudaEventRecord(ev[1], stream());
+    DBuf<long long> mkeys;
+    DBuf<unsigned long long> mhash;
+    DBuf<int> mok, mslot, mrep, misrep, moff, mlist;
+    DBuf<MemoSlot> mtab;
+    int njobrec = nrec;
+    const int *job_rec = nullptr;
     if (nrec) {
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
         PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 1, nullptr, near_off.p, rec.p, nullptr);
+        if (near_reuse_enabled() && nrec > 1) {
+            unsigned long long cap = 1;
+            while (cap < 4ull * (unsigned long long)nrec) cap <<= 1;
+            double delta = 8.0 * 2.220446049250313e-16 * (R.cmax > 0.0 ? R.cmax : 1.0);
+            bool ok = mkeys.alloc((size_t)nrec * (kKeyLen + 1)) && mhash.alloc(nrec) && mok.alloc(nrec) &&
+                      mslot.alloc(nrec) && mrep.alloc(nrec) && misrep.alloc(nrec) && moff.alloc(nrec + 1) &&
+                      mtab.alloc(cap);
+            if (!ok) return -1;
+            cudaMemsetAsync(mtab.p, 0, cap * sizeof(MemoSlot), stream());
+            PEEC_LAUNCH(k_fill_int, (unsigned)((cap + 255) / 256), 256, 0, &mtab.p[0].rep, (long long)cap,
+                        (int)sizeof(MemoSlot) / (int)sizeof(int), 0x7fffffff);
+            unsigned g = (nrec + 255) / 256;
+            PEEC_LAUNCH(k_memo_keys, g, 256, 0, R.corner, R.same_obj, rec.p, nrec, delta, mkeys.p, mhash.p, mok.p);
+            PEEC_LAUNCH(k_memo_insert, g, 256, 0, nrec, mhash.p, mok.p, mtab.p, cap - 1, mslot.p);
+            PEEC_LAUNCH(k_memo_resolve, g, 256, 0, nrec, mkeys.p, mtab.p, mslot.p, mrep.p, misrep.p);
+            PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, misrep.p, moff.p, nrec);
+            int nreps = 0;
+            cudaMemcpyAsync(&nreps, moff.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            if (!sync("near-pair reuse")) return -1;
+            if (!mlist.alloc(nreps > 0 ? nreps : 1)) return -1;
+            PEEC_LAUNCH(k_memo_compact, g, 256, 0, nrec, misrep.p, moff.p, mlist.p);
+            njobrec = nreps;
+            job_rec = mlist.p;
+        }
+        DBuf<int> marginal(nrec);
+        if (!marginal.p) return -1;
+        cudaMemsetAsync(marginal.p, 0, (size_t)nrec * sizeof(int), stream());
         NearEvalArgs A;
         A.corner = R.corner;
         A.rec = rec.p;
-        A.nrec = nrec;
+        A.job_rec = job_rec;
+        A.nrec = njobrec;
+        A.marginal = marginal.p;
         for (int k = 0; k < 4; ++k) A.orders[k] = o.orders[k];
         A.slot = slot.p;
         A.kind = kindbuf.p;
@@ -977,11 +1166,38 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         std::call_once(attr_once, [smem] {
             cudaFuncSetAttribute(k_near_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         });
-        long long jobs = (long long)nrec * 8;
-        long long want = (jobs + 7) / 8;
-        int grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
-        PEEC_LAUNCH(k_near_eval, grid, 256, smem, A);
+        auto launch_eval = [&](int nj) {
+            long long jobs = (long long)nj * 8;
+            long long want = (jobs + 7) / 8;
+            int grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
+            if (grid > 0) PEEC_LAUNCH(k_near_eval, grid, 256, smem, A);
+        };
+        launch_eval(njobrec);
+        DBuf<int> rflag, roff, rlist;
+        if (job_rec) {
+            // second pass: copies of representatives with a marginal decision
+            unsigned g = (nrec + 255) / 256;
+            if (!rflag.alloc(nrec) || !roff.alloc(nrec + 1)) return -1;
+            PEEC_LAUNCH(k_memo_recheck, g, 256, 0, nrec, mrep.p, marginal.p, rflag.p);
+            PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, rflag.p, roff.p, nrec);
+            int nre = 0;
+            cudaMemcpyAsync(&nre, roff.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            if (!sync("near-pair reuse check")) return -1;
+            if (nre > 0) {
+                if (!rlist.alloc(nre)) return -1;
+                PEEC_LAUNCH(k_memo_compact, g, 256, 0, nrec, rflag.p, roff.p, rlist.p);
+                cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
+                A.job_rec = rlist.p;
+                A.nrec = nre;
+                A.marginal = nullptr;
+                launch_eval(nre);
+            }
+            if (stats) stats->near_pairs_evaluated = (unsigned long long)(njobrec + nre);
+        } else if (stats) {
+            stats->near_pairs_evaluated = (unsigned long long)nrec;
+        }
         PEEC_LAUNCH(k_near_finalize, (nrec + 127) / 128, 128, 0, nrec, slot.p, kindbuf.p, kval.p);
+        if (job_rec) PEEC_LAUNCH(k_memo_scatter, (nrec + 255) / 256, 256, 0, nrec, mrep.p, marginal.p, kval.p);
     }
     cudaEventRecord(ev[2], stream());
     TileArgs T;
@@ -1328,5 +1544,13 @@ int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual, const Po
 extern "C" int peec_gb300_set_far_precision(int mode) {
     int prev = far_mode_df();
     if (mode >= 0 && mode <= 2) g_far_mode = mode;
+    return prev;
+}
+
+// Turn the reuse of translated near pairs on (1) or off (0) for later
+// assemblies; returns the previous setting.
+extern "C" int peec_gb300_set_near_reuse(int on) {
+    int prev = near_reuse_enabled() ? 1 : 0;
+    g_near_reuse = on ? 1 : 0;
     return prev;
 }

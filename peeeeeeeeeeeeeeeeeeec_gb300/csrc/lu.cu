@@ -1937,8 +1937,16 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     cudaEventRecord(ev[1], stream());
     // FP32 factorisation, trailing updates on the tensor cores
     cplxf *a = f.p;
+    LuTiming &tm = g_lu_timing;
+    if (tm.enabled) {
+        for (auto e : tm.ev) cudaEventDestroy(e);
+        tm.ev.clear();
+        tm.ms[0] = tm.ms[1] = tm.ms[2] = 0.0;
+        tm.flops_update = 0.0;
+    }
     for (int k0 = 0; k0 < n; k0 += NB) {
         int kb = std::min(NB, n - k0);
+        if (tm.enabled) lu_mark(tm.ev);
         CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
         if (pl.G > 0) {
             int rows = pl.rows;
@@ -1955,6 +1963,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         } else {
             PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
         }
+        if (tm.enabled) lu_mark(tm.ev);
         PEEC_LAUNCH(k_laswp<cplxf>, (n + 255) / 256, 256, 0, a, n, k0, kb, piv.p, st.p);
         int rest = n - (k0 + kb);
         if (rest > 0) {
@@ -1962,8 +1971,22 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             PEEC_LAUNCH(k_split_a, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, ap.p);
             PEEC_LAUNCH(k_split_b, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, bpr.p,
                         bpi.p);
-            if (!tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, rest, rest, 6 * NB, k0 + kb, k0 + kb, n, err.p))
-                return -1;
+        }
+        if (tm.enabled) {
+            lu_mark(tm.ev);
+            tm.flops_update += 2.0 * 2.0 * (double)rest * rest * (6 * NB);  // issued BF16 tensor flops
+        }
+        if (rest > 0 &&
+            !tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, rest, rest, 6 * NB, k0 + kb, k0 + kb, n, err.p))
+            return -1;
+    }
+    if (tm.enabled) {
+        lu_mark(tm.ev);
+        cudaEventSynchronize(tm.ev.back());
+        for (size_t i = 0; i + 1 < tm.ev.size(); ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
+            tm.ms[i % 3] += ms;
         }
     }
     PEEC_LAUNCH(k_check_diag<cplxf>, (n + 255) / 256, 256, 0, a, n, limit, st.p);
@@ -1990,7 +2013,10 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     double eta = INFINITY;
     int it = 0;
     const int wpb = 8;
-    for (it = 1; it <= max_iter; ++it) {
+    // one refinement sweep (FP32 correction solve, FP64 update, FP64
+    // residual + backward error) is ~1000 launches: capture it once as a
+    // CUDA graph and replay it per iteration
+    auto sweep = [&]() {
         PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
         for (int k0 = 0; k0 < n; k0 += 32) {
             int kb = std::min(32, n - k0);
@@ -2011,12 +2037,40 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs);
         cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
         PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, x, b, n, nrhs, r.p, be.p);
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    if (!sync("refinement setup")) return -1;
+    unsigned long long sweep_launches = 0;
+    if (cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        unsigned long long l0 = launch_count();
+        sweep();
+        sweep_launches = launch_count() - l0;
+        if (cudaStreamEndCapture(stream(), &graph) != cudaSuccess ||
+            cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {
+            gexec = nullptr;
+        }
+    }
+    cudaGetLastError();  // a failed capture falls back to direct launches
+    for (it = 1; it <= max_iter; ++it) {
+        if (gexec) {
+            if (!cuda_ok(cudaGraphLaunch(gexec, stream()), "refinement graph")) break;
+            note_launch((int)sweep_launches);  // the replayed kernels
+        } else {
+            sweep();
+        }
         unsigned long long hb = 0;
         cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
-        if (!launch_ok("refinement") || !sync("refinement")) return -1;
+        if (!launch_ok("refinement") || !sync("refinement")) {
+            if (gexec) cudaGraphExecDestroy(gexec);
+            if (graph) cudaGraphDestroy(graph);
+            return -1;
+        }
         memcpy(&eta, &hb, sizeof(eta));
         if (eta <= tol) break;
     }
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
     cudaEventRecord(ev[3], stream());
     cudaEventSynchronize(ev[3]);
     float t01, t12, t23;

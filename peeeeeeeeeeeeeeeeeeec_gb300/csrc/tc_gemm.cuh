@@ -246,7 +246,30 @@ __global__ void __launch_bounds__(128, 1)
     if (!ok) s_abort = 1;
     fence_after_sync();
     __syncthreads();
-    if (!s_abort) {
+    if (!s_abort && J == 2 && args.interleaved) {
+        // complex C: both accumulators of 32 columns, one float2 read-modify-
+        // write per element (256 contiguous bytes per thread)
+        const int row = tile_m + warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            float vr[32], vi[32];
+            tmem_ld32(lane_addr + c0, vr);
+            tmem_ld32(lane_addr + BN + c0, vi);
+            if (row < args.m) {
+                int lim = args.n - (tile_n + c0);
+                float2 *crow = reinterpret_cast<float2 *>(args.c[0]) + (size_t)(args.row0 + row) * args.ldc +
+                               args.col0 + tile_n + c0;
+#pragma unroll
+                for (int t = 0; t < 32; ++t)
+                    if (t < lim) {
+                        float2 v = crow[t];
+                        v.x -= vr[t];
+                        v.y -= vi[t];
+                        crow[t] = v;
+                    }
+            }
+        }
+    } else if (!s_abort) {
         const int row = tile_m + warp * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll

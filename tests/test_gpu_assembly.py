@@ -182,3 +182,53 @@ def test_potential_helpers(gpu_lib):
     assert gpu_lib.potential_build_self_capacitance(C.byref(pm2), F.ctypes.data_as(abi.c_double_p)) == -1
     assert gpu_lib.potential_self_voltage_to_full_potential(C.byref(pm2), v.ctypes.data_as(abi.c_double_p),
                                                             phi.ctypes.data_as(abi.c_double_p)) == -1
+
+
+def _assembly_stats(gpu_lib, m, which):
+    n = m.n_edges if which == "L" else m.n_nodes
+    d = gpu_lib.peec_gb300_device_alloc(n * n * 8)
+    st = abi.PeecAssemblyStats()
+    if which == "L":
+        o = abi.InductanceOptions()
+        gpu_lib.inductance_options_default(C.byref(o), 1)
+        assert gpu_lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(o), d, C.byref(st)) == 0
+    else:
+        o = abi.PotentialOptions()
+        gpu_lib.potential_options_default(C.byref(o), 1)
+        assert gpu_lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(o), d, C.byref(st)) == 0
+    gpu_lib.peec_gb300_device_free(d)
+    return st
+
+
+def test_near_reuse_matches_individual_evaluation(gpu_lib):
+    """Translated copies of a near pair share one evaluation unless one of its
+    adaptive decisions is within 1e-6 of the threshold; the result agrees
+    with evaluating every pair on its own."""
+    with SynthMesh.box(0.4, 0.2, 0.1, 16, 8, 4) as m:
+        prev = gpu_lib.peec_gb300_set_near_reuse(0)
+        try:
+            _, L0 = inductance(gpu_lib, m)
+            _, P0 = potential(gpu_lib, m)
+            st0 = _assembly_stats(gpu_lib, m, "P")
+        finally:
+            gpu_lib.peec_gb300_set_near_reuse(prev)
+        gpu_lib.peec_gb300_set_near_reuse(1)
+        _, L1 = inductance(gpu_lib, m)
+        _, P1 = potential(gpu_lib, m)
+        st1 = _assembly_stats(gpu_lib, m, "P")
+        gpu_lib.peec_gb300_set_near_reuse(prev)
+        assert elem_rel_err(L1, L0) < 1e-13
+        assert elem_rel_err(P1, P0) < 1e-13
+        assert st0.near_pairs_evaluated == st0.near_pairs
+        assert st1.near_pairs == st0.near_pairs
+        assert st1.near_pairs_evaluated * 10 < st1.near_pairs
+
+
+def test_box_against_oracle_with_reuse(gpu_lib, oracle):
+    """1.0 x 0.5 x 0.25 m PEC box at 5 cm (Ne = 1400, Nv = 702): every entry
+    within 1e-12 of the oracle with near-pair reuse on (the default)."""
+    with SynthMesh.box(1.0, 0.5, 0.25, 20, 10, 5) as m:
+        s, L = inductance(gpu_lib, m)
+        assert s == 0 and elem_rel_err(L, oracle.inductance(m)[1]) < TOL
+        s, P = potential(gpu_lib, m)
+        assert s == 0 and elem_rel_err(P, oracle.potential(m)[1]) < TOL
