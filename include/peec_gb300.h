@@ -43,7 +43,9 @@ const char *peec_gb300_last_error(void);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long peec_gb300_launch_count(void);
 
-/* The library's CUDA stream (cudaStream_t), on which every call enqueues. */
+/* The calling host thread's CUDA stream (cudaStream_t): each host thread has
+ * its own, every call from that thread enqueues on it, and calls from
+ * different threads overlap on the device. */
 void *peec_gb300_stream(void);
 
 void *peec_gb300_device_alloc(size_t bytes);
@@ -170,6 +172,49 @@ int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
  * sides, out[1] = max |r_i|, out[2] = max |b_i|. */
 int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x,
                                      const Complex *d_b, size_t nrhs, double out[3]);
+
+/* ---- serving loop ----
+ * A server admits harmonic solve requests from a FIFO onto worker threads,
+ * each with its own CUDA stream, as soon as a worker is free and the
+ * request's device-memory estimate fits the HBM budget.  Lp and P assembled
+ * for one mesh_key stay in device memory and serve every later request with
+ * that key (any frequency) until evicted, least recently used first, to make
+ * room.  Each request builds Z = harmonic_build_system(frequency), nrhs
+ * plane-wave right-hand sides, and solves by the plain FP64 complex LU
+ * (mixed = 0) or the mixed-precision solve (mixed = 1, tolerance 0 means
+ * 1e-10), then copies X to the caller's host array. */
+typedef struct
+{
+    const Mesh *mesh;            /* read when the key is first assembled: keep valid until done */
+    const DualMesh *dual;
+    unsigned long long mesh_key; /* same key = same mesh (the caller's promise) */
+    double frequency;            /* Hz, > 0 */
+    size_t nrhs;                 /* plane waves                               */
+    const double *k_hat;         /* [3*nrhs] propagation directions (copied at submit) */
+    const double *e_hat;         /* [3*nrhs] polarisations (copied at submit)  */
+    int mixed;                   /* 0 plain FP64 LU, 1 mixed precision         */
+    double tolerance;            /* mixed: backward-error target (0 = 1e-10)   */
+    Complex *x;                  /* host output [nrhs][Ne+Nv]                  */
+} PeecHarmonicRequest;
+
+typedef struct
+{
+    int status;            /* 0 solved, 1 mixed refinement did not converge, -2 singular, -1 error */
+    int iterations;        /* mixed refinement iterations (0 for plain)     */
+    double backward_error; /* componentwise, over all right-hand sides      */
+    double t_submit, t_start, t_end; /* seconds on the server's clock       */
+} PeecRequestResult;
+
+/* Returns NULL on failure.  workers >= 1 host threads (and streams). */
+void *peec_gb300_server_create(size_t hbm_budget_bytes, int workers);
+/* Ticket >= 0, or -1 for an invalid request or one that can never fit. */
+long long peec_gb300_server_submit(void *server, const PeecHarmonicRequest *request);
+/* Blocks until the request is done; 0, or -1 for an unknown ticket. */
+int peec_gb300_server_wait(void *server, long long ticket, PeecRequestResult *result);
+/* Seconds since the server was created (the clock of the result times). */
+double peec_gb300_server_clock(void *server);
+/* Finishes every queued request, then stops the workers and frees the cache. */
+void peec_gb300_server_destroy(void *server);
 
 #ifdef __cplusplus
 }

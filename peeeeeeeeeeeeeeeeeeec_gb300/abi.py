@@ -162,6 +162,18 @@ class PeecAssemblyStats(C.Structure):
                 ("ms_prepare", C.c_double), ("ms_near", C.c_double), ("ms_far", C.c_double)]
 
 
+class PeecHarmonicRequest(C.Structure):
+    _fields_ = [("mesh", P(Mesh)), ("dual", P(DualMesh)), ("mesh_key", C.c_ulonglong),
+                ("frequency", C.c_double), ("nrhs", C.c_size_t), ("k_hat", c_double_p),
+                ("e_hat", c_double_p), ("mixed", C.c_int), ("tolerance", C.c_double),
+                ("x", P(Complex))]
+
+
+class PeecRequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("backward_error", C.c_double),
+                ("t_submit", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double)]
+
+
 # include/peec_gb300.h
 EXT_SYMBOLS = [
     ("peec_gb300_device_ready", C.c_int, []),
@@ -215,6 +227,11 @@ EXT_SYMBOLS = [
       C.c_void_p]),
     ("peec_gb300_backward_error_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, c_double_p]),
+    ("peec_gb300_server_create", C.c_void_p, [C.c_size_t, C.c_int]),
+    ("peec_gb300_server_submit", C.c_longlong, [C.c_void_p, P(PeecHarmonicRequest)]),
+    ("peec_gb300_server_wait", C.c_int, [C.c_void_p, C.c_longlong, P(PeecRequestResult)]),
+    ("peec_gb300_server_clock", C.c_double, [C.c_void_p]),
+    ("peec_gb300_server_destroy", None, [C.c_void_p]),
 ]
 
 MESH_SYMBOLS = [

@@ -29,6 +29,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -309,8 +310,13 @@ struct NearWarpSmem {
 // the lanes and reduced with shuffles; accepted nodes add `high` left to
 // right.  Returns NaN if a rule is non-finite or depth 24 is exceeded
 // (reference quadrature.c:915-938).
+// Decision flags for the reuse of translated copies (see 5b below).
+enum : int { MARG_THRESHOLD = 1, MARG_TIE = 2, MARG_TRACE_FULL = 4 };
+static const int kTraceCap = 256;       // decisions recorded per job
+static const unsigned char kAccept = 0xFF;
+
 __device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order, double abs_tol,
-                                unsigned long long &evals, bool &marginal) {
+                                unsigned long long &evals, int &mflags, unsigned char *trace, int &trace_len) {
     const int lane = threadIdx.x & 31;
     const int ql = order <= 6 ? 3 : 4;
     const int rl = gl_row(ql), rh = gl_row(order);
@@ -358,9 +364,17 @@ __device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order
         // a decision within 1e-6 of its threshold could go the other way for
         // a copy of this pair that differs only by rounding of its corners
         double thr = nd.tol + 2e-5 * fabs(hi), gap = fabs(hi - lo);
-        if (fabs(gap - thr) <= 1e-6 * thr) marginal = true;
+        if (fabs(gap - thr) <= 1e-6 * thr) mflags |= MARG_THRESHOLD;
         if (fabs(hi - lo) <= nd.tol + 2e-5 * fabs(hi)) {
             acc += hi;
+            if (trace) {
+                if (trace_len < kTraceCap) {
+                    if (lane == 0) trace[trace_len] = kAccept;
+                    ++trace_len;
+                } else {
+                    mflags |= MARG_TRACE_FULL;
+                }
+            }
             continue;
         }
         if (nd.depth >= 24 || sp + 2 > kStackCap) return nan("");
@@ -377,7 +391,15 @@ __device__ double warp_adaptive(const double *outer, NearWarpSmem &sm, int order
         // two (nearly) equal longest edges: which one is bisected is decided
         // by rounding, so a translated copy may subdivide differently
         for (int i = 0; i < 3; ++i)
-            if (i != e && len[i] >= longest * (1.0 - 1e-10)) marginal = true;
+            if (i != e && len[i] >= longest * (1.0 - 1e-10)) mflags |= MARG_TIE;
+        if (trace) {
+            if (trace_len < kTraceCap) {
+                if (lane == 0) trace[trace_len] = (unsigned char)e;
+                ++trace_len;
+            } else {
+                mflags |= MARG_TRACE_FULL;
+            }
+        }
         int j = (e + 1) % 3, k = (e + 2) % 3;
         if (lane == 0) {
             AdaptNode &left = sm.stack[sp + 1], &right = sm.stack[sp];
@@ -412,11 +434,13 @@ struct NearEvalArgs {
     const int *job_rec;  // records to evaluate (representatives), or null for all
     int nrec;            // number of records to evaluate
     int orders[4];  // far, near, touching, self
-    double *slot;   // [nrec*4*2]
+    double *slot;   // [records*4*2]
     int *kind;      // [nrec*4]: 0 adaptive, 1 zero area, 2 identical triangles
     int *next_job;  // work counter
     unsigned long long *evals;
-    int *marginal;  // [nrec] set to 1 if an adaptive decision was within 1e-6 of its threshold
+    int *marginal;  // [nrec] MARG_* flags of the record's jobs (null: not recorded)
+    unsigned char *trace;  // [jobs * kTraceCap] decision traces (null: not recorded)
+    int *trace_len;        // [jobs]
 };
 
 // One warp per job (record, triangle pair t = s*2+u, direction d); warps
@@ -475,14 +499,17 @@ __global__ void __launch_bounds__(256, 2) k_near_eval(NearEvalArgs A) {
                 double aa = d == 0 ? po.twice_area : sm.inner.twice_area;
                 double ab = d == 0 ? sm.inner.twice_area : po.twice_area;
                 double scale = aa * ab / sqrt(fmax(aa, ab));
-                bool marg = false;
-                out = warp_adaptive(outer, sm, order, 2e-5 * scale, evals, marg);
-                if (marg && lane == 0 && A.marginal) atomicOr(A.marginal + r, 1);
+                int mflags = 0, tlen = 0;
+                unsigned char *tr = A.trace ? A.trace + (size_t)job * kTraceCap : nullptr;
+                out = warp_adaptive(outer, sm, order, 2e-5 * scale, evals, mflags, tr, tlen);
+                if (lane == 0 && A.marginal && mflags) atomicOr(A.marginal + r, mflags);
+                if (lane == 0 && A.trace_len) A.trace_len[job] = tlen;
             }
         }
         if (lane == 0) {
             A.slot[(size_t)r * 8 + t * 2 + d] = out;
             if (d == 0) A.kind[(size_t)r * 4 + t] = kind;
+            if (kind != 0 && A.trace_len) A.trace_len[job] = 0;
         }
         __syncwarp();
     }
@@ -632,19 +659,85 @@ __global__ void k_memo_compact(int nrec, const int *is_rep, const int *off, int 
     list[off[r]] = r;
 }
 
-// copies of a marginal representative are evaluated on their own
+// Copies of a representative with an accept decision near its threshold
+// (or an overflowing trace) are evaluated on their own.
 __global__ void k_memo_recheck(int nrec, const int *rep, const int *marginal, int *flag) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     int r0 = rep[r];
-    flag[r] = (r0 != r && marginal[r0]) ? 1 : 0;
+    flag[r] = (r0 != r && (marginal[r0] & (MARG_THRESHOLD | MARG_TRACE_FULL))) ? 1 : 0;
 }
 
-__global__ void k_memo_scatter(int nrec, const int *rep, const int *marginal, double2 *kval) {
+// Copies of a representative whose only marginal decisions are bisection-
+// edge ties replay the representative's decision trace on their own
+// corners (geometry only, one thread per job): the copy reuses the value
+// only if it bisects the same edge at every refined node, i.e. follows the
+// same subdivision tree.
+__global__ void k_memo_replay(int nrec, const int *rep, const int *marginal, const int *rep_pos,
+                              const double *corner, const NearRec *rec, const unsigned char *trace,
+                              const int *trace_len, int *flag) {
+    long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= (long long)nrec * 8) return;
+    int r = (int)(g >> 3), t = (int)((g >> 1) & 3), d = (int)(g & 1);
+    int r0 = rep[r];
+    if (r0 == r || !(marginal[r0] & MARG_TIE) || (marginal[r0] & (MARG_THRESHOLD | MARG_TRACE_FULL))) return;
+    long long job = (long long)rep_pos[r0] * 8 + t * 2 + d;
+    int len = trace_len[job];
+    if (len <= 0) return;
+    const unsigned char *tr = trace + (size_t)job * kTraceCap;
+    NearRec q = rec[r];
+    double ta[9], tb[9];
+    patch_triangle(corner + 12 * (size_t)q.i, t >> 1, ta);
+    patch_triangle(corner + 12 * (size_t)q.j, t & 1, tb);
+    double stack[kStackCap][9];
+    for (int k = 0; k < 9; ++k) stack[0][k] = d == 0 ? ta[k] : tb[k];
+    int sp = 1, pos = 0;
+    bool ok = true;
+    while (sp > 0) {
+        double v[9];
+        --sp;
+        for (int k = 0; k < 9; ++k) v[k] = stack[sp][k];
+        if (pos >= len) {
+            ok = false;
+            break;
+        }
+        unsigned char c = tr[pos++];
+        if (c == kAccept) continue;
+        int e = 0;
+        double longest = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            double s = dist3(v + 3 * i, v + 3 * ((i + 1) % 3));
+            if (s > longest) {
+                longest = s;
+                e = i;
+            }
+        }
+        if (e != (int)c || sp + 2 > kStackCap) {
+            ok = false;
+            break;
+        }
+        int j = (e + 1) % 3, k = (e + 2) % 3;
+        double *left = stack[sp + 1], *right = stack[sp];
+        for (int dd = 0; dd < 3; ++dd) {
+            double mid = 0.5 * (v[3 * e + dd] + v[3 * j + dd]);
+            left[dd] = v[3 * e + dd];
+            left[3 + dd] = mid;
+            left[6 + dd] = v[3 * k + dd];
+            right[dd] = mid;
+            right[3 + dd] = v[3 * j + dd];
+            right[6 + dd] = v[3 * k + dd];
+        }
+        sp += 2;
+    }
+    if (pos != len) ok = false;
+    if (!ok) atomicOr(flag + r, 1);
+}
+
+__global__ void k_memo_scatter(int nrec, const int *rep, const int *flag, double2 *kval) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     int r0 = rep[r];
-    if (r0 != r && !marginal[r0]) kval[r] = kval[r0];
+    if (r0 != r && !flag[r]) kval[r] = kval[r0];
 }
 
 // ---------------------------------------------------------------------
@@ -1041,7 +1134,7 @@ struct AssemblyOptions {
 // Far rule arithmetic: 1 double-float on the FP32 pipes (default), 0 native
 // FP64 (PEEC_GB300_FAR=fp64), 2 FP32 (PEEC_GB300_FAR=fp32, or
 // peec_gb300_set_far_precision for the mixed-precision path).
-static int g_near_reuse = -1;
+static std::atomic<int> g_near_reuse{-1};
 // Reuse of translated near pairs: on unless PEEC_GB300_NEAR_REUSE=0 or
 // peec_gb300_set_near_reuse(0).
 static bool near_reuse_enabled() {
@@ -1052,7 +1145,7 @@ static bool near_reuse_enabled() {
     return g_near_reuse == 1;
 }
 
-static int g_far_mode = -1;
+static std::atomic<int> g_far_mode{-1};
 static int far_mode_df() {
     if (g_far_mode < 0) {
         const char *e = getenv("PEEC_GB300_FAR");
@@ -1147,12 +1240,20 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         DBuf<int> marginal(nrec);
         if (!marginal.p) return -1;
         cudaMemsetAsync(marginal.p, 0, (size_t)nrec * sizeof(int), stream());
+        DBuf<unsigned char> trace;
+        DBuf<int> trace_len;
+        if (job_rec) {
+            if (!trace.alloc((size_t)njobrec * 8 * kTraceCap) || !trace_len.alloc((size_t)njobrec * 8)) return -1;
+            cudaMemsetAsync(trace_len.p, 0, (size_t)njobrec * 8 * sizeof(int), stream());
+        }
         NearEvalArgs A;
         A.corner = R.corner;
         A.rec = rec.p;
         A.job_rec = job_rec;
         A.nrec = njobrec;
         A.marginal = marginal.p;
+        A.trace = job_rec ? trace.p : nullptr;
+        A.trace_len = job_rec ? trace_len.p : nullptr;
         for (int k = 0; k < 4; ++k) A.orders[k] = o.orders[k];
         A.slot = slot.p;
         A.kind = kindbuf.p;
@@ -1179,6 +1280,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
             unsigned g = (nrec + 255) / 256;
             if (!rflag.alloc(nrec) || !roff.alloc(nrec + 1)) return -1;
             PEEC_LAUNCH(k_memo_recheck, g, 256, 0, nrec, mrep.p, marginal.p, rflag.p);
+            PEEC_LAUNCH(k_memo_replay, (unsigned)(((long long)nrec * 8 + 127) / 128), 128, 0, nrec, mrep.p,
+                        marginal.p, moff.p, R.corner, rec.p, trace.p, trace_len.p, rflag.p);
             PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, rflag.p, roff.p, nrec);
             int nre = 0;
             cudaMemcpyAsync(&nre, roff.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
@@ -1190,6 +1293,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
                 A.job_rec = rlist.p;
                 A.nrec = nre;
                 A.marginal = nullptr;
+                A.trace = nullptr;
+                A.trace_len = nullptr;
                 launch_eval(nre);
             }
             if (stats) stats->near_pairs_evaluated = (unsigned long long)(njobrec + nre);
@@ -1197,7 +1302,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
             stats->near_pairs_evaluated = (unsigned long long)nrec;
         }
         PEEC_LAUNCH(k_near_finalize, (nrec + 127) / 128, 128, 0, nrec, slot.p, kindbuf.p, kval.p);
-        if (job_rec) PEEC_LAUNCH(k_memo_scatter, (nrec + 255) / 256, 256, 0, nrec, mrep.p, marginal.p, kval.p);
+        if (job_rec) PEEC_LAUNCH(k_memo_scatter, (nrec + 255) / 256, 256, 0, nrec, mrep.p, rflag.p, kval.p);
     }
     cudaEventRecord(ev[2], stream());
     TileArgs T;

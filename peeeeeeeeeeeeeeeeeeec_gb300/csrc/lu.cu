@@ -941,11 +941,9 @@ static CoopPlan<T> coop_plan(int m) {
     int rows = (m + G - 1) / G;
     size_t smem = (size_t)rows * NB * sizeof(T);
     if (smem > 200 * 1024) return pl;
-    static bool attr_done = false;
-    if (!attr_done) {
+    static const cudaError_t attr =  // once per type (thread-safe static initialisation)
         cudaFuncSetAttribute(k_panel_coop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_done = true;
-    }
+    if (attr != cudaSuccess) return pl;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel_coop<T>, 256, smem);
     if (per_sm < 1) return pl;
@@ -983,7 +981,7 @@ struct LuTiming {
     double flops_update = 0.0;       // algorithmic flops of the trailing updates
     std::vector<cudaEvent_t> ev;
 };
-static LuTiming g_lu_timing;
+static thread_local LuTiming g_lu_timing;  // per host thread, like the stream
 
 static void lu_mark(std::vector<cudaEvent_t> &ev) {
     cudaEvent_t e;
@@ -1871,7 +1869,7 @@ struct MixedTiming {
     double ms_prepare = 0, ms_factor = 0, ms_refine = 0;
     int iterations = 0;
 };
-static MixedTiming g_mixed_timing;
+static thread_local MixedTiming g_mixed_timing;  // last mixed solve of this host thread
 
 }  // namespace peec
 

@@ -37,6 +37,8 @@ static bool encoder() {
 }
 
 // 2-D BF16 K-major matrix [rows][k], box {64, box_rows}, 128-byte swizzle.
+static bool launch_tc_ok() { return launch_ok("tcgen05 GEMM"); }
+
 static bool make_map_bf16(CUtensorMap *map, const void *base, int rows, int k, int box_rows) {
     if (!encoder()) return false;
     if (((uintptr_t)base & 15) || (k * 2) % 16 != 0) {
@@ -57,7 +59,7 @@ static bool make_map_bf16(CUtensorMap *map, const void *base, int rows, int k, i
     return true;
 }
 
-template <int BN, int J>
+template <int BN, int J, int S>
 static bool launch_tc(const void *a, const void *b0, const void *b1, float *c0, float *c1, int m, int n, int k,
                       int row0, int col0, long long ldc, int *d_err, int interleaved = 0) {
     CUtensorMap ma, mb0, mb1;
@@ -74,17 +76,14 @@ static bool launch_tc(const void *a, const void *b0, const void *b1, float *c0, 
     g.ldc = ldc;
     g.interleaved = interleaved;
     g.error = d_err;
-    constexpr size_t smem = tc::smem_bytes<BN, J>();
-    static bool attr = false;
-    if (!attr) {
-        if (!cuda_ok(cudaFuncSetAttribute(tc::k_tc_gemm<BN, J>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                     "tcgen05 GEMM smem attribute"))
-            return false;
-        attr = true;
-    }
+    constexpr size_t smem = tc::smem_bytes<BN, J, S>();
+    // set once per instantiation (thread-safe static initialisation)
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(tc::k_tc_gemm<BN, J, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!cuda_ok(attr, "tcgen05 GEMM smem attribute")) return false;
     dim3 grid((n + BN - 1) / BN, (m + tc::kBM - 1) / tc::kBM);
-    PEEC_LAUNCH((tc::k_tc_gemm<BN, J>), grid, 128, smem, ma, mb0, mb1, g);
-    return launch_ok("tcgen05 GEMM");
+    PEEC_LAUNCH((tc::k_tc_gemm<BN, J, S>), grid, 128, smem, ma, mb0, mb1, g);
+    return launch_tc_ok();
 }
 
 // C_j -= A B_j^T; J = 1 or 2; K multiple of 64; returns false on failure.
@@ -94,8 +93,8 @@ bool tc_gemm_update(const void *a, const void *b0, const void *b1, float *c0, fl
         set_error("tcgen05 GEMM: K must be a positive multiple of 64");
         return false;
     }
-    if (J == 1) return launch_tc<128, 1>(a, b0, nullptr, c0, nullptr, m, n, k, row0, col0, ldc, d_err);
-    return launch_tc<128, 2>(a, b0, b1, c0, c1, m, n, k, row0, col0, ldc, d_err);
+    if (J == 1) return launch_tc<128, 1, 4>(a, b0, nullptr, c0, nullptr, m, n, k, row0, col0, ldc, d_err);
+    return launch_tc<128, 2, 4>(a, b0, b1, c0, c1, m, n, k, row0, col0, ldc, d_err);
 }
 
 // Complex C (interleaved FP32, leading dimension ldc complex elements)
@@ -106,7 +105,9 @@ bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c
         set_error("tcgen05 GEMM: K must be a positive multiple of 64");
         return false;
     }
-    return launch_tc<128, 2>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
+    // the LU's K is 192: three stages, 64-column tiles -> two CTAs per SM
+    if (k == 192) return launch_tc<64, 2, 3>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
+    return launch_tc<128, 2, 4>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
 }
 
 }  // namespace peec

@@ -13,15 +13,24 @@
 
 namespace peec {
 
-static std::once_flag g_stream_once;
-static cudaStream_t g_stream = nullptr;
+static std::once_flag g_pool_once;
 static std::atomic<unsigned long long> g_launches{0};
 static thread_local char g_err[512] = "";
 
+// One non-blocking stream per host thread: calls from different threads (the
+// serving loop's workers) overlap on the device; every entry point
+// synchronises its own thread's stream before it returns host results.
+struct ThreadStream {
+    cudaStream_t s = nullptr;
+    ~ThreadStream() {
+        if (s) cudaStreamDestroy(s);
+    }
+};
+static thread_local ThreadStream t_stream;
+
 cudaStream_t stream() {
-    std::call_once(g_stream_once, [] {
-        if (cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking) != cudaSuccess) g_stream = nullptr;
-        // keep freed blocks in the pool between calls
+    std::call_once(g_pool_once, [] {
+        // keep freed blocks in the stream-ordered pool between calls
         cudaMemPool_t pool;
         int dev = 0;
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
@@ -29,7 +38,9 @@ cudaStream_t stream() {
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
         }
     });
-    return g_stream;
+    if (!t_stream.s && cudaStreamCreateWithFlags(&t_stream.s, cudaStreamNonBlocking) != cudaSuccess)
+        t_stream.s = nullptr;
+    return t_stream.s;
 }
 
 void set_error(const char *fmt, ...) {

@@ -28,7 +28,7 @@ namespace tc {
 
 static const int kBM = 128;       // rows per tile (one TMEM lane each)
 static const int kBK = 64;        // K per stage: 64 BF16 = one 128-byte swizzle row
-static const int kStages = 4;
+static const int kMaxStages = 4;
 static const long long kWaitLimit = 1LL << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -157,13 +157,14 @@ struct GemmArgs {
     int *error;         // set to 1 on a wait timeout
 };
 
-// grid: (ceil(n / BN), ceil(m / 128)); block 128; dynamic smem = smem_bytes<BN, J>()
-template <int BN, int J>
+// grid: (ceil(n / BN), ceil(m / 128)); block 128; dynamic smem =
+// smem_bytes<BN, J, S>() for an S-stage pipeline (S = min(4, K / 64))
+template <int BN, int J, int S>
 __host__ __device__ constexpr size_t smem_bytes() {
-    return (size_t)kStages * ((size_t)kBM * kBK * 2 + (size_t)J * BN * kBK * 2) + 1024 + 256;
+    return (size_t)S * ((size_t)kBM * kBK * 2 + (size_t)J * BN * kBK * 2) + 1024 + 256;
 }
 
-template <int BN, int J>
+template <int BN, int J, int kStages>
 __global__ void __launch_bounds__(128, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b0,
               const __grid_constant__ CUtensorMap map_b1, GemmArgs args) {
@@ -247,8 +248,9 @@ __global__ void __launch_bounds__(128, 1)
     fence_after_sync();
     __syncthreads();
     if (!s_abort && J == 2 && args.interleaved) {
-        // complex C: both accumulators of 32 columns, one float2 read-modify-
-        // write per element (256 contiguous bytes per thread)
+        // complex C: both accumulators of 32 columns, then one float2 read-
+        // modify-write per element (256 contiguous bytes per thread; all
+        // loads issued before the first store)
         const int row = tile_m + warp * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
         for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -259,14 +261,26 @@ __global__ void __launch_bounds__(128, 1)
                 int lim = args.n - (tile_n + c0);
                 float2 *crow = reinterpret_cast<float2 *>(args.c[0]) + (size_t)(args.row0 + row) * args.ldc +
                                args.col0 + tile_n + c0;
+                if (lim >= 32) {
+                    float2 cv[32];
 #pragma unroll
-                for (int t = 0; t < 32; ++t)
-                    if (t < lim) {
-                        float2 v = crow[t];
-                        v.x -= vr[t];
-                        v.y -= vi[t];
-                        crow[t] = v;
+                    for (int t = 0; t < 32; ++t) cv[t] = crow[t];
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) {
+                        cv[t].x -= vr[t];
+                        cv[t].y -= vi[t];
+                        crow[t] = cv[t];
                     }
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 32; ++t)
+                        if (t < lim) {
+                            float2 v = crow[t];
+                            v.x -= vr[t];
+                            v.y -= vi[t];
+                            crow[t] = v;
+                        }
+                }
             }
         }
     } else if (!s_abort) {
