@@ -56,6 +56,16 @@ class Oracle:
             ("oracle_complex_lu_factorize", C.c_int,
              [D, C.c_size_t, C.c_double, C.c_int, D, S, S, D, D, D]),
             ("oracle_complex_lu_solve", C.c_int, [D, S, D, D, C.c_size_t, D, D]),
+            ("oracle_transient_stage1_matrix", C.c_int,
+             [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, D, D, D]),
+            ("oracle_transient_rhs_stage1", C.c_int,
+             [D, D, D, D, P(C.c_int), C.c_size_t, C.c_size_t, C.c_int, C.c_double, D, D, D, D, D]),
+            ("oracle_lightning_current", C.c_double,
+             [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
+            ("oracle_transient_lightning", C.c_int,
+             [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, C.c_double,
+              C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_size_t, D, D,
+              P(C.c_int), C.c_size_t, P(C.c_int), C.c_size_t, D]),
         ]
         for name, res, args in sig:
             f = getattr(lib, name)
@@ -138,6 +148,44 @@ class Oracle:
                                              lu.shape[0], b.ctypes.data_as(D), x.ctypes.data_as(D))
         return s, x
 
+    def transient_matrix(self, L, P_, edges, R, scheme, dt):
+        ne, nv = L.shape[0], P_.shape[0]
+        nt = ne + nv
+        M, F, AS = np.zeros((nt, nt)), np.zeros(nv), np.zeros((ne, nv))
+        s = self.lib.oracle_transient_stage1_matrix(
+            _dp(L), _dp(P_), _ip(edges), None if R is None else _dp(R), ne, nv, scheme, dt,
+            _dp(M), _dp(F), _dp(AS))
+        return s, M, F, AS
+
+    def transient_lightning(self, L, P_, edges, R, scheme, dt, source, n_steps, I=None, V=None,
+                            probe_nodes=(), probe_edges=()):
+        return _transient_lightning(self.lib.oracle_transient_lightning, L, P_, edges, R, scheme,
+                                    dt, source, n_steps, I, V, probe_nodes, probe_edges)
+
+
+def _ip(a):
+    return a.ctypes.data_as(P(C.c_int))
+
+
+def _transient_lightning(fn, L, P_, edges, R, scheme, dt, source, n_steps, I, V, probe_nodes,
+                         probe_edges):
+    """source = (K, alpha, beta, delay, strike_node, return_node).  Returns
+    (status, I, V, probes [n_steps][len(probe_nodes) + len(probe_edges)])."""
+    L = np.ascontiguousarray(L, dtype=np.float64)
+    P_ = np.ascontiguousarray(P_, dtype=np.float64)
+    edges = np.ascontiguousarray(edges, dtype=np.int32)
+    ne, nv = L.shape[0], P_.shape[0]
+    I = np.zeros(ne) if I is None else np.array(I, dtype=np.float64)
+    V = np.zeros(nv) if V is None else np.array(V, dtype=np.float64)
+    pn = np.ascontiguousarray(probe_nodes, dtype=np.int32)
+    pe = np.ascontiguousarray(probe_edges, dtype=np.int32)
+    probes = np.zeros((n_steps, len(pn) + len(pe)))
+    Rp = None if R is None else _dp(np.ascontiguousarray(R, dtype=np.float64))
+    K, alpha, beta, delay, strike, ret = source
+    s = fn(_dp(L), _dp(P_), _ip(edges), Rp, ne, nv, scheme, dt, K, alpha, beta, delay, strike, ret,
+           n_steps, _dp(I), _dp(V), _ip(pn), len(pn), _ip(pe), len(pe), _dp(probes))
+    return s, I, V, probes
+
 
 def reference_available():
     return os.path.exists(REF_PATH)
@@ -159,4 +207,13 @@ class Reference:
             ("dual_mesh_build", C.c_int, [P(abi.Mesh), P(abi.DualMesh)]),
         ]
         abi._bind(lib, extra)
+        f = lib.ref_transient_lightning
+        f.restype, f.argtypes = C.c_int, [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, C.c_double,
+              C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_size_t, D, D,
+              P(C.c_int), C.c_size_t, P(C.c_int), C.c_size_t, D]
         self.lib = lib
+
+    def transient_lightning(self, L, P_, edges, R, scheme, dt, source, n_steps, I=None, V=None,
+                            probe_nodes=(), probe_edges=()):
+        return _transient_lightning(self.lib.ref_transient_lightning, L, P_, edges, R, scheme, dt,
+                                    source, n_steps, I, V, probe_nodes, probe_edges)

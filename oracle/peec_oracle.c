@@ -727,3 +727,157 @@ int oracle_complex_lu_solve(const Complex *a, const size_t *piv, const double *r
     }
     return 0;
 }
+
+
+/* ===================================================================== */
+/* transient stage 1                                                      */
+/* ===================================================================== */
+
+/* transient.c:19-35 */
+static double transient_theta(int scheme)
+{
+    return scheme == 1 ? 1.0 : scheme == 2 ? 0.5 : NAN;
+}
+
+/* dense incidence row e: A[e][a] = -1, A[e][b] = +1 (incidence.c:34-115) */
+static double incidence_entry(const int *edges, size_t e, size_t j)
+{
+    if ((size_t)edges[2 * e + 1] == j) return 1.0;
+    if ((size_t)edges[2 * e + 0] == j) return -1.0;
+    return 0.0;
+}
+
+int oracle_transient_stage1_matrix(const double *L, const double *P, const int *edges,
+                                   const double *R, size_t ne, size_t nv, int scheme,
+                                   double dt, double *M, double *F, double *AS)
+{
+    double theta = transient_theta(scheme);
+    if (!L || !P || !edges || !M || !F || !AS || ne == 0 || nv == 0 || isnan(theta) ||
+        !isfinite(dt) || dt <= 0.0)
+        return -1;
+    size_t nt = ne + nv;
+    /* potential.c:483-520 */
+    for (size_t j = 0; j < nv; ++j) {
+        double d = P[j * nv + j];
+        if (!isfinite(d) || d <= 0.0) return -1;
+        F[j] = 1.0 / d;
+    }
+    /* incidence.c:593-741: AS[e][a] = (P[plus][a] - P[minus][a]) / P[a][a] */
+    for (size_t e = 0; e < ne; ++e) {
+        int a = edges[2 * e + 0], b = edges[2 * e + 1];
+        if (a < 0 || b < 0 || (size_t)a >= nv || (size_t)b >= nv || a == b) return -1;
+        for (size_t k = 0; k < nv; ++k)
+            AS[e * nv + k] = (P[(size_t)b * nv + k] - P[(size_t)a * nv + k]) / P[k * nv + k];
+    }
+    memset(M, 0, nt * nt * sizeof(double));
+    for (size_t i = 0; i < ne; ++i)
+        for (size_t j = 0; j < ne; ++j) {
+            double v = L[i * ne + j] / dt;
+            if (i == j) v += theta * (R ? R[i] : 0.0);
+            M[i * nt + j] = v;
+        }
+    for (size_t e = 0; e < ne; ++e)
+        for (size_t j = 0; j < nv; ++j) M[e * nt + ne + j] = theta * AS[e * nv + j];
+    for (size_t j = 0; j < nv; ++j)
+        for (size_t e = 0; e < ne; ++e) M[(ne + j) * nt + e] = -theta * incidence_entry(edges, e, j);
+    for (size_t r = 0; r < nv; ++r)
+        for (size_t c = 0; c < nv; ++c) {
+            double v = 0.0;
+            if (r == c) v += F[r];
+            M[(ne + r) * nt + ne + c] = v / dt;
+        }
+    return 0;
+}
+
+int oracle_transient_rhs_stage1(const double *L, const double *R, const double *AS,
+                                const double *F, const int *edges, size_t ne, size_t nv,
+                                int scheme, double dt, const double *I, const double *V,
+                                const double *Jn, const double *Jnp1, double *rhs)
+{
+    double theta = transient_theta(scheme);
+    if (!L || !AS || !F || !edges || !I || !V || !rhs || isnan(theta)) return -1;
+    double omt = 1.0 - theta;
+    for (size_t i = 0; i < ne; ++i) {
+        double v = 0.0;
+        for (size_t j = 0; j < ne; ++j) v += L[i * ne + j] * I[j] / dt;
+        v -= omt * (R ? R[i] : 0.0) * I[i];
+        for (size_t j = 0; j < nv; ++j) v -= omt * AS[i * nv + j] * V[j];
+        rhs[i] = v;
+    }
+    for (size_t j = 0; j < nv; ++j) {
+        double v = F[j] * V[j] / dt;
+        for (size_t e = 0; e < ne; ++e) v += omt * incidence_entry(edges, e, j) * I[e];
+        if (Jn) v += omt * Jn[j];
+        if (Jnp1) v += theta * Jnp1[j];
+        rhs[ne + j] = v;
+    }
+    return 0;
+}
+
+double oracle_lightning_current(double K, double alpha, double beta, double delay, double t)
+{
+    if (!isfinite(t)) return NAN;
+    if (t < delay) return 0.0;
+    double tau = t - delay;
+    return K * (exp(-alpha * tau) - exp(-beta * tau));
+}
+
+int oracle_transient_lightning(const double *L, const double *P, const int *edges,
+                               const double *R, size_t ne, size_t nv, int scheme, double dt,
+                               double K, double alpha, double beta, double delay,
+                               size_t strike_node, size_t return_node, size_t n_steps,
+                               double *I, double *V, const int *probe_nodes,
+                               size_t n_probe_nodes, const int *probe_edges,
+                               size_t n_probe_edges, double *probe_out)
+{
+    if (strike_node >= nv || return_node >= nv || strike_node == return_node) return -1;
+    size_t nt = ne + nv;
+    double *M = malloc(nt * nt * sizeof(double)), *F = malloc(nv * sizeof(double));
+    double *AS = malloc(ne * nv * sizeof(double)), *lu = malloc(nt * nt * sizeof(double));
+    double *rhs = malloc(nt * sizeof(double)), *x = malloc(nt * sizeof(double));
+    double *Jn = calloc(nv, sizeof(double)), *Jnp1 = calloc(nv, sizeof(double));
+    size_t *piv = malloc(nt * sizeof(size_t));
+    int status = -1;
+    if (!M || !F || !AS || !lu || !rhs || !x || !Jn || !Jnp1 || !piv) goto done;
+    if (oracle_transient_stage1_matrix(L, P, edges, R, ne, nv, scheme, dt, M, F, AS) != 0) goto done;
+    size_t swaps;
+    double scale;
+    status = oracle_lu_factorize(M, nt, 1.0e-14, 1, lu, piv, &swaps, &scale);
+    if (status != 0) goto done;
+    size_t np = n_probe_nodes + n_probe_edges;
+    for (size_t step = 0; step < n_steps; ++step) {
+        double tn = step * dt, tnp1 = (step + 1) * dt;
+        /* lightning.c:310-373 */
+        double cn = oracle_lightning_current(K, alpha, beta, delay, tn);
+        double cnp1 = oracle_lightning_current(K, alpha, beta, delay, tnp1);
+        memset(Jn, 0, nv * sizeof(double));
+        memset(Jnp1, 0, nv * sizeof(double));
+        Jn[strike_node] = cn;
+        Jn[return_node] = -cn;
+        Jnp1[strike_node] = cnp1;
+        Jnp1[return_node] = -cnp1;
+        oracle_transient_rhs_stage1(L, R, AS, F, edges, ne, nv, scheme, dt, I, V, Jn, Jnp1, rhs);
+        if (oracle_lu_solve(lu, piv, nt, rhs, x) != 0) {
+            status = -1;
+            goto done;
+        }
+        memcpy(I, x, ne * sizeof(double));
+        memcpy(V, x + ne, nv * sizeof(double));
+        if (probe_out) {
+            for (size_t k = 0; k < n_probe_nodes; ++k) probe_out[step * np + k] = V[probe_nodes[k]];
+            for (size_t k = 0; k < n_probe_edges; ++k)
+                probe_out[step * np + n_probe_nodes + k] = I[probe_edges[k]];
+        }
+    }
+done:
+    free(M);
+    free(F);
+    free(AS);
+    free(lu);
+    free(rhs);
+    free(x);
+    free(Jn);
+    free(Jnp1);
+    free(piv);
+    return status;
+}

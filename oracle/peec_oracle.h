@@ -76,6 +76,37 @@ int oracle_complex_lu_solve(const Complex *lu, const size_t *pivots,
                             const double *row_scale, const double *column_scale,
                             size_t n, const Complex *b, Complex *x);
 
+/* ---- transient stage 1 (lightning current at nodes) ----
+ * scheme 1 backward Euler (theta 1), 2 trapezoidal (theta 1/2); edges holds
+ * (a, b) per edge (current a -> b); R is the edge resistance diagonal or
+ * NULL for PEC (zeros).
+ *
+ * transient.c:1020-1110 stage-1 blocks, with F = 1/diag(P)
+ * (potential.c:483-520) and AS = A S (incidence.c:593-741):
+ * M = [L/dt + theta R, theta AS; -theta A^T, F/dt], nt = ne + nv.
+ * F (nv) and AS (ne x nv) are returned as well. */
+int oracle_transient_stage1_matrix(const double *L, const double *P, const int *edges,
+                                   const double *R, size_t ne, size_t nv, int scheme,
+                                   double dt, double *M, double *F, double *AS);
+/* transient.c:1421-1631 (edge voltages absent): rhs (nt) of one step */
+int oracle_transient_rhs_stage1(const double *L, const double *R, const double *AS,
+                                const double *F, const int *edges, size_t ne, size_t nv,
+                                int scheme, double dt, const double *I, const double *V,
+                                const double *Jn, const double *Jnp1, double *rhs);
+/* lightning.c:184-212: K (exp(-alpha tau) - exp(-beta tau)), tau = t - delay */
+double oracle_lightning_current(double K, double alpha, double beta, double delay, double t);
+/* main.c:3139-3400: factor M once, then n_steps of source, rhs, solve and
+ * extract, starting from I and V (updated in place).  probe_out receives,
+ * after every step, V at the probe nodes then I at the probe edges
+ * ([n_steps][n_probe_nodes + n_probe_edges]); it may be NULL. */
+int oracle_transient_lightning(const double *L, const double *P, const int *edges,
+                               const double *R, size_t ne, size_t nv, int scheme, double dt,
+                               double K, double alpha, double beta, double delay,
+                               size_t strike_node, size_t return_node, size_t n_steps,
+                               double *I, double *V, const int *probe_nodes,
+                               size_t n_probe_nodes, const int *probe_edges,
+                               size_t n_probe_edges, double *probe_out);
+
 #ifdef __cplusplus
 }
 #endif

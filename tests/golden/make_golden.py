@@ -248,6 +248,31 @@ def quadrature_cases(R):
     print("wrote quadrature_cases, gauss_legendre")
 
 
+# Stage-1 lightning transient on the fixtures' own Lp / P (the reference's
+# transient.c / lightning.c driven by oracle/ref_transient.c): every step's
+# node self-voltages and edge currents, for backward Euler and trapezoidal.
+TRANSIENT_SOURCE = (102900.0, 1500.0, 1.0e6, 0.0)  # the reference's default waveform
+TRANSIENT_DT = 1.0e-7
+
+
+def transient_case(R, name, n_steps, strike, ret, r_edge=1.0e-3):
+    f = np.load(os.path.join(HERE, name + ".npz"))
+    L, P, edges = f["L"], f["P"], f["edges"].astype(np.int32)
+    ne, nv = L.shape[0], P.shape[0]
+    Rd = np.full(ne, r_edge)
+    out = dict(R=Rd, strike=strike, ret=ret, dt=TRANSIENT_DT, source=np.array(TRANSIENT_SOURCE),
+               n_steps=n_steps)
+    for scheme in (1, 2):
+        s, I, V, probes = R.transient_lightning(L, P, edges, Rd, scheme, TRANSIENT_DT,
+                                                TRANSIENT_SOURCE + (strike, ret), n_steps,
+                                                probe_nodes=range(nv), probe_edges=range(ne))
+        assert s == 0
+        out["V%d" % scheme] = probes[:, :nv]
+        out["I%d" % scheme] = probes[:, nv:]
+    np.savez_compressed(os.path.join(HERE, "transient_" + name + ".npz"), **out)
+    print("wrote transient_" + name, n_steps, "steps")
+
+
 def main():
     R = Reference()
     quadrature_cases(R)
@@ -256,6 +281,8 @@ def main():
     reference_case(R, *plate_arrays(1.0, 1.0, 8, 8), "plate8")
     reference_case(R, *box_arrays(0.4, 0.2, 0.1, 4, 2, 1), "box421")
     reference_case(R, *box_arrays(2.0, 1.0, 0.5, 40, 20, 10), "box_5cm_topology", with_matrices=False)
+    transient_case(R, "plate4", 300, 0, 24)
+    transient_case(R, "box421", 200, 0, 5)
     plate_msh = os.path.join(REF_MESH_DIR, "plate.msh")
     if os.path.exists(plate_msh):
         gmsh_case(R, plate_msh, "plate_msh")
