@@ -169,9 +169,40 @@ int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
                                      const double e_hat[3], double wave_number,
                                      Complex *d_rhs);
 /* out[0] = max_i |r_i| / (sum_j |Z_ij||x_j| + |b_i|) over all right-hand
- * sides, out[1] = max |r_i|, out[2] = max |b_i|. */
+ * sides (r = b - Z x in FP64; the denominator's sum from FP32 magnitudes,
+ * ~1e-7 relative, which only matters for a gate on eta), out[1] = max |r_i|,
+ * out[2] = max |b_i|. */
 int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x,
                                      const Complex *d_b, size_t nrhs, double out[3]);
+
+/* ---- stage-1 transient (lightning) on the device ----
+ * The reference's transient_system_create_stage1 + transient_factorize
+ * (transient.c:385-480, 1020-1110, 2014-2066): M = [L/dt + theta R,
+ * theta A S; -theta A^T, F/dt] built from device Lp (kept by pointer: it
+ * must stay valid while the system lives), P, the edge list (2*Ne int32,
+ * a -> b) and the edge resistance diagonal d_R (NULL: PEC), then factorised
+ * and kept on the device.  scheme 1 backward Euler, 2 trapezoidal.  Returns
+ * 0, -1 (invalid input or CUDA error), -2 (singular system). */
+int peec_gb300_transient_create(const double *d_L, const double *d_P, const int *d_edges,
+                                const double *d_R, size_t n_edges, size_t n_nodes, int scheme,
+                                double dt, void **system);
+/* n_steps steps starting at t = step0*dt under the double-exponential
+ * lightning current K (exp(-alpha tau) - exp(-beta tau)), tau = t - delay,
+ * injected at strike_node and returned at return_node (per step:
+ * lightning_build_node_current at t_n and t_n+1, transient_build_rhs_stage1,
+ * transient_solve_step).  d_I (Ne) and d_V (Nv, node self-voltages) hold the
+ * state on entry and on exit.  d_probes, if the probe counts are not zero,
+ * receives after every step V at the probe nodes then I at the probe edges
+ * ([n_steps][n_probe_nodes + n_probe_edges]; an index outside the mesh
+ * records NaN).  Several runs may use one system at once (each call keeps
+ * its own state and scratch). */
+int peec_gb300_transient_lightning(void *system, double K, double alpha, double beta,
+                                   double delay, size_t strike_node, size_t return_node,
+                                   size_t step0, size_t n_steps, double *d_I, double *d_V,
+                                   const int *d_probe_nodes, size_t n_probe_nodes,
+                                   const int *d_probe_edges, size_t n_probe_edges,
+                                   double *d_probes);
+void peec_gb300_transient_destroy(void *system);
 
 /* ---- serving loop ----
  * A server admits harmonic solve requests from a FIFO onto worker threads,
@@ -205,11 +236,40 @@ typedef struct
     double t_submit, t_start, t_end; /* seconds on the server's clock       */
 } PeecRequestResult;
 
+/* A lightning run on a PEC mesh (R = 0): n_steps of the stage-1 transient
+ * (scheme 1 backward Euler, 2 trapezoidal, step dt) from rest, under the
+ * double-exponential current K (exp(-alpha tau) - exp(-beta tau)),
+ * tau = t - delay, injected at strike_node and returned at return_node.
+ * The factorised system of (mesh_key, scheme, dt) stays resident for later
+ * runs.  Probe lists are copied at submit; probes (host [n_steps][n_probe_
+ * nodes + n_probe_edges]), I (Ne) and V (Nv) receive the waveforms and the
+ * final state when not NULL. */
+typedef struct
+{
+    const Mesh *mesh;
+    const DualMesh *dual;
+    unsigned long long mesh_key;
+    int scheme;
+    double dt;
+    size_t n_steps;
+    double K, alpha, beta, delay;
+    size_t strike_node, return_node;
+    const int *probe_nodes;
+    size_t n_probe_nodes;
+    const int *probe_edges;
+    size_t n_probe_edges;
+    double *probes;
+    double *I;
+    double *V;
+} PeecTransientRequest;
+
 /* Returns NULL on failure.  workers >= 1 host threads (and streams). */
 void *peec_gb300_server_create(size_t hbm_budget_bytes, int workers);
 /* Ticket >= 0, or -1 for an invalid request or one that can never fit. */
 long long peec_gb300_server_submit(void *server, const PeecHarmonicRequest *request);
-/* Blocks until the request is done; 0, or -1 for an unknown ticket. */
+long long peec_gb300_server_submit_transient(void *server, const PeecTransientRequest *request);
+/* Blocks until the request is done; 0, or -1 for an unknown ticket.  For a
+ * transient request iterations is the step count and backward_error 0. */
 int peec_gb300_server_wait(void *server, long long ticket, PeecRequestResult *result);
 /* Seconds since the server was created (the clock of the result times). */
 double peec_gb300_server_clock(void *server);

@@ -169,6 +169,16 @@ class PeecHarmonicRequest(C.Structure):
                 ("x", P(Complex))]
 
 
+class PeecTransientRequest(C.Structure):
+    _fields_ = [("mesh", P(Mesh)), ("dual", P(DualMesh)), ("mesh_key", C.c_ulonglong),
+                ("scheme", C.c_int), ("dt", C.c_double), ("n_steps", C.c_size_t),
+                ("K", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("delay", C.c_double),
+                ("strike_node", C.c_size_t), ("return_node", C.c_size_t),
+                ("probe_nodes", P(C.c_int)), ("n_probe_nodes", C.c_size_t),
+                ("probe_edges", P(C.c_int)), ("n_probe_edges", C.c_size_t),
+                ("probes", c_double_p), ("I", c_double_p), ("V", c_double_p)]
+
+
 class PeecRequestResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("backward_error", C.c_double),
                 ("t_submit", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double)]
@@ -227,8 +237,17 @@ EXT_SYMBOLS = [
       C.c_void_p]),
     ("peec_gb300_backward_error_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, c_double_p]),
+    ("peec_gb300_transient_create", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_int, C.c_double,
+      P(C.c_void_p)]),
+    ("peec_gb300_transient_lightning", C.c_int,
+     [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t,
+      C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+      C.c_size_t, C.c_void_p]),
+    ("peec_gb300_transient_destroy", None, [C.c_void_p]),
     ("peec_gb300_server_create", C.c_void_p, [C.c_size_t, C.c_int]),
     ("peec_gb300_server_submit", C.c_longlong, [C.c_void_p, P(PeecHarmonicRequest)]),
+    ("peec_gb300_server_submit_transient", C.c_longlong, [C.c_void_p, P(PeecTransientRequest)]),
     ("peec_gb300_server_wait", C.c_int, [C.c_void_p, C.c_longlong, P(PeecRequestResult)]),
     ("peec_gb300_server_clock", C.c_double, [C.c_void_p]),
     ("peec_gb300_server_destroy", None, [C.c_void_p]),

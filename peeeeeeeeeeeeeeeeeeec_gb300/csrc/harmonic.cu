@@ -74,10 +74,24 @@ __global__ void k_plane_wave_rhs(const double *centers, const double *vectors, i
     rhs[i] = cpx{-proj * co * sinc, -proj * s * sinc};
 }
 
+// |z| in FP32 for the denominator sum |Z||x| + |b| of the backward error (a
+// gate, not a result: FP32 rounding moves eta by ~1e-7 of itself).  Parts
+// are clamped to 1e19 so the square cannot overflow; clamping and underflow
+// can only shrink the denominator, i.e. overstate eta.
+__device__ __forceinline__ float abs_f32_fast(cpx z) {
+    float ar = fminf(fabsf((float)z.re), 1e19f), ai = fminf(fabsf((float)z.im), 1e19f);
+    return sqrtf(fmaf(ar, ar, ai * ai));
+}
+
+__global__ void k_abs_vector(const cpx *x, size_t count, float *out) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t < count) out[t] = abs_f32_fast(x[t]);
+}
+
 // Componentwise backward error, one warp per row; results as IEEE bits
 // (non-negative) max-reduced: out[0] = backward error, out[1] = max |r_i|,
-// out[2] = max |b_i|.
-__global__ void k_backward_error(const cpx *Z, const cpx *x, const cpx *b, int n, int nrhs,
+// out[2] = max |b_i|.  The residual is FP64, the denominator FP32.
+__global__ void k_backward_error(const cpx *Z, const cpx *x, const float *absx, const cpx *b, int n, int nrhs,
                                  unsigned long long *out) {
     long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -85,24 +99,27 @@ __global__ void k_backward_error(const cpx *Z, const cpx *x, const cpx *b, int n
     int rr = (int)(warp / n), i = (int)(warp % n);
     const cpx *row = Z + (size_t)i * n;
     const cpx *xr = x + (size_t)rr * n;
-    double yr = 0.0, yi = 0.0, den = 0.0;
+    const float *ax = absx + (size_t)rr * n;
+    double yr = 0.0, yi = 0.0;
+    float den = 0.0f;
     for (int j = lane; j < n; j += 32) {
         cpx z = row[j], v = xr[j];
         yr = fma(z.re, v.re, yr);
         yr = fma(-z.im, v.im, yr);
         yi = fma(z.re, v.im, yi);
         yi = fma(z.im, v.re, yi);
-        den = fma(hypot(z.re, z.im), hypot(v.re, v.im), den);
+        den = fmaf(abs_f32_fast(z), ax[j], den);
     }
     yr = warp_sum(yr);
     yi = warp_sum(yi);
-    den = warp_sum(den);
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) den += __shfl_xor_sync(0xffffffffu, den, m);
     if (lane == 0) {
         cpx bi = b[(size_t)rr * n + i];
         double res = hypot(yr - bi.re, yi - bi.im);
         double babs = hypot(bi.re, bi.im);
-        den += babs;
-        double eta = den > 0.0 ? res / den : res;
+        double d = (double)den + babs;
+        double eta = d > 0.0 ? res / d : res;
         if (!isfinite(eta)) eta = INFINITY;
         atomicMax(out + 0, (unsigned long long)__double_as_longlong(eta));
         atomicMax(out + 1, (unsigned long long)__double_as_longlong(isfinite(res) ? res : INFINITY));
@@ -145,11 +162,13 @@ int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex
                                      size_t nrhs, double out[3]) {
     if (!d_Z || !d_x || !d_b || !out || n == 0 || nrhs == 0) return -1;
     DBuf<unsigned long long> acc(3);
-    if (!acc.p) return -1;
+    DBuf<float> absx(n * nrhs);
+    if (!acc.p || !absx.p) return -1;
     cudaMemsetAsync(acc.p, 0, 3 * sizeof(unsigned long long), stream());
+    PEEC_LAUNCH(k_abs_vector, (unsigned)((n * nrhs + 255) / 256), 256, 0, (const cpx *)d_x, n * nrhs, absx.p);
     long long warps = (long long)n * nrhs;
     PEEC_LAUNCH(k_backward_error, (unsigned)((warps * 32 + 255) / 256), 256, 0, (const cpx *)d_Z, (const cpx *)d_x,
-                (const cpx *)d_b, (int)n, (int)nrhs, acc.p);
+                absx.p, (const cpx *)d_b, (int)n, (int)nrhs, acc.p);
     unsigned long long h[3];
     cudaMemcpyAsync(h, acc.p, sizeof(h), cudaMemcpyDeviceToHost, stream());
     if (!sync("backward error")) return -1;

@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <list>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/complex_lu.h"
@@ -36,6 +37,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "solve.cuh"
 
 namespace peec {
 
@@ -747,86 +749,384 @@ __global__ void k_perm(const long long *piv, int n, int *perm, const Status *st)
     for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
 }
 
-// x[r][i] = b[r][perm[i]] (real); complex also divides by row_scale first
+// ---------------------------------------------------------------------
+// wavefront triangular solves: one cooperative launch does the forward
+// (unit L) and backward (U) substitution for all right-hand sides, NR at a
+// time.  Row blocks of kRB rows are owned round-robin by the CTAs (forward
+// in increasing, backward in decreasing block order).  A block streams its
+// off-diagonal tiles from HBM as soon as the x block they multiply is
+// published (the tile itself is loaded before waiting), then applies the
+// precomputed inverse of its diagonal block (k_diag_inverse) as one more
+// tile and publishes x with a per-block ready flag.  The inverse turns the
+// 64-step dependent substitution, which on one warp would run at a quarter
+// of the SM's small FP64 rate, into a product spread over all warps.
+// Every task waits only on earlier tasks of the global order (forward
+// 0..nb-1, then backward nb-1..0) and each CTA runs its tasks in that order,
+// so with all CTAs co-resident the earliest unfinished task can always
+// proceed.  Waits are bounded: on timeout the kernel records code 6 in
+// *error and returns.
+// ---------------------------------------------------------------------
+static const int kRB = 64;
+static const int kRS = kRB + 1;  // padded row stride of a block in shared memory
+
 template <class T>
-__global__ void k_gather(const T *b, T *x, const int *perm, const double *row_scale, int n, int nrhs) {
-    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (t >= (size_t)n * nrhs) return;
-    int r = (int)(t / n), i = (int)(t % n);
-    int src = perm[i];
-    T v = b[(size_t)r * n + src];
-    if constexpr (sizeof(T) == sizeof(cplx)) {
-        cplx c = *reinterpret_cast<cplx *>(&v);
-        double s = row_scale[src];
-        c.re = c.re / s;
-        c.im = c.im / s;
-        v = *reinterpret_cast<T *>(&c);
-    }
-    x[(size_t)r * n + i] = v;
+struct WaveArgs {
+    const T *lu;
+    const T *dinv;            // [nb][2][kRB][kRB]: L_bb^-1, U_bb^-1 (k_diag_inverse)
+    int n, nb, nrhs;
+    const int *perm;          // forward rhs_i = b[perm[i]] (NULL: b[i])
+    const double *row_scale;  // complex: rhs divided by row_scale[perm[i]]
+    const double *col_scale;  // if set, out[i] = x[i] / col_scale[i]
+    const T *b;
+    T *x;                     // working solution (may equal b when perm is NULL)
+    T *out;                   // unscaled copy (col_scale set), else unused
+    unsigned *flags;          // [nchunks][2][nb], zero on entry
+    int *error;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// diagonal block of the forward (unit L) or backward (U) substitution:
-// one warp per right-hand side, rows [k0, k0+kb); lane owns rows k0+lane
-__device__ __forceinline__ double mulv(double l, double x) { return l * x; }
+template <class T>
+__device__ __forceinline__ T zero_t() {
+    T z;
+    memset(&z, 0, sizeof(T));
+    return z;
+}
+__device__ __forceinline__ double one_t(double) { return 1.0; }
+__device__ __forceinline__ cplx one_t(cplx) { return cplx{1.0, 0.0}; }
+__device__ __forceinline__ cplxf one_t(cplxf) { return cplxf{1.0f, 0.0f}; }
+__device__ __forceinline__ double neg_t(double v) { return -v; }
+__device__ __forceinline__ cplx neg_t(cplx v) { return cplx{-v.re, -v.im}; }
+__device__ __forceinline__ cplxf neg_t(cplxf v) { return cplxf{-v.re, -v.im}; }
+__device__ __forceinline__ double ldcg_t(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ cplx ldcg_t(const cplx *p) {
+    double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
+    return cplx{v.x, v.y};
+}
+__device__ __forceinline__ cplxf ldcg_t(const cplxf *p) {
+    float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+    return cplxf{v.x, v.y};
+}
+__device__ __forceinline__ double scale_div(double v, double s) { return v / s; }
+__device__ __forceinline__ cplx scale_div(cplx v, double s) { return cplx{v.re / s, v.im / s}; }
+__device__ __forceinline__ cplxf scale_div(cplxf v, double s) {
+    return cplxf{(float)(v.re / s), (float)(v.im / s)};
+}
 
-template <class T, bool LOWER>
-__global__ void k_trsv_diag(const T *a, int n, int k0, int kb, T *x, int nrhs) {
-    int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (r >= nrhs) return;
-    T *xr = x + (size_t)r * n;
-    T v;
-    if (lane < kb) v = xr[k0 + lane];
-    if (LOWER) {
-        for (int m = 0; m < kb; ++m) {
-            T xm;
-            double *pv = reinterpret_cast<double *>(&v);
-            double *pm = reinterpret_cast<double *>(&xm);
-#pragma unroll
-            for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pm[w] = __shfl_sync(0xffffffffu, pv[w], m);
-            if (lane > m && lane < kb) v = msub(v, a[(size_t)(k0 + lane) * n + k0 + m], xm);
+// Inverses of the diagonal blocks of a packed LU factor, one CTA per block:
+// threads 0..63 each solve one column of L_bb X = I (unit lower), threads
+// 64..127 one column of U_bb X = I, from the block staged in shared memory.
+// Entries outside the matrix are zero.
+template <class T>
+__global__ void __launch_bounds__(128) k_diag_inverse(const T *lu, int n, T *dinv) {
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    T *blk = reinterpret_cast<T *>(inv_smem);  // kRB x kRS
+    T *XL = blk + kRB * kRS, *XU = XL + kRB * kRS;
+    const int b = blockIdx.x, r0 = b * kRB, nrow = min(kRB, n - r0);
+    for (int t = threadIdx.x; t < kRB * kRB; t += blockDim.x) {
+        int i = t / kRB, j = t % kRB;
+        blk[i * kRS + j] = (i < nrow && j < nrow) ? lu[(size_t)(r0 + i) * n + r0 + j] : zero_t<T>();
+        XL[i * kRS + j] = zero_t<T>();
+        XU[i * kRS + j] = zero_t<T>();
+    }
+    __syncthreads();
+    const int c = threadIdx.x & (kRB - 1);
+    if (c < nrow) {
+        if (threadIdx.x < kRB) {  // column c of L^-1: rows c..nrow-1
+            XL[c * kRS + c] = one_t(T{});
+            for (int i = c + 1; i < nrow; ++i) {
+                T s = zero_t<T>();
+                for (int k = c; k < i; ++k) s = msub(s, blk[i * kRS + k], XL[k * kRS + c]);
+                XL[i * kRS + c] = s;
+            }
+        } else {  // column c of U^-1: rows c..0
+            XU[c * kRS + c] = divide(one_t(T{}), blk[c * kRS + c]);
+            for (int i = c - 1; i >= 0; --i) {
+                T s = zero_t<T>();
+                for (int k = i + 1; k <= c; ++k) s = msub(s, blk[i * kRS + k], XU[k * kRS + c]);
+                XU[i * kRS + c] = divide(s, blk[i * kRS + i]);
+            }
         }
-    } else {
-        for (int m = kb - 1; m >= 0; --m) {
-            if (lane == m) v = divide(v, a[(size_t)(k0 + m) * n + k0 + m]);
-            T xm;
-            double *pv = reinterpret_cast<double *>(&v);
-            double *pm = reinterpret_cast<double *>(&xm);
+    }
+    __syncthreads();
+    T *dl = dinv + (size_t)b * 2 * kRB * kRB, *du = dl + kRB * kRB;
+    for (int t = threadIdx.x; t < kRB * kRB; t += blockDim.x) {
+        int i = t / kRB, j = t % kRB;
+        dl[t] = XL[i * kRS + j];
+        du[t] = XU[i * kRS + j];
+    }
+}
+
+// bounded wait for *flag != 0 by one thread; false on timeout / abort
+__device__ __forceinline__ bool wave_wait(const unsigned *flag, int *error) {
+    long long spins = 0;
+    while (ld_acquire_u32(flag) == 0u) {
+        if (++spins > kSpinLimit || *(volatile int *)error) {
+            atomicExch(error, 6);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
+}
+
+// c + m*u
+__device__ __forceinline__ double mac(double c, double m, double u) { return fma(m, u, c); }
+__device__ __forceinline__ cplx mac(cplx c, cplx m, cplx u) {
+    c.re = fma(m.re, u.re, c.re);
+    c.re = fma(-m.im, u.im, c.re);
+    c.im = fma(m.re, u.im, c.im);
+    c.im = fma(m.im, u.re, c.im);
+    return c;
+}
+__device__ __forceinline__ cplxf mac(cplxf c, cplxf m, cplxf u) {
+    c.re = fmaf(m.re, u.re, c.re);
+    c.re = fmaf(-m.im, u.im, c.re);
+    c.im = fmaf(m.re, u.im, c.im);
+    c.im = fmaf(m.im, u.re, c.im);
+    return c;
+}
+template <class T>
+__device__ __forceinline__ T shfl_xor_t(T v, int m) {
+    T r;
+    const unsigned *pv = reinterpret_cast<const unsigned *>(&v);
+    unsigned *pr = reinterpret_cast<unsigned *>(&r);
 #pragma unroll
-            for (int w = 0; w < (int)(sizeof(T) / 8); ++w) pm[w] = __shfl_sync(0xffffffffu, pv[w], m);
-            if (lane < m) v = msub(v, a[(size_t)(k0 + lane) * n + k0 + m], xm);
+    for (int w = 0; w < (int)(sizeof(T) / 4); ++w) pr[w] = __shfl_xor_sync(0xffffffffu, pv[w], m);
+    return r;
+}
+
+// shared memory of one wavefront CTA: the diagonal-block inverse (staged by
+// cp.async while the off-diagonal tiles stream), the per-lane partial sums
+// and the block's right-hand sides
+static const int kDS = kRB + 4;  // row stride of the staged inverse (bank-conflict free)
+template <class T, int NR>
+struct WaveSmem {
+    T dinv[kRB * kDS];
+    T part[NR][kRB][33];
+    T y[NR][kRB];
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <class T, int NR, bool LOWER>
+__device__ bool wave_block(const WaveArgs<T> &A, int blk, int c0, int nr, unsigned *flags, WaveSmem<T, NR> &S,
+                           int *s_ok) {
+    constexpr int RPW = kRB / 8;  // rows per warp in the tile loop
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = A.n, nb = A.nb;
+    const int r0 = blk * kRB, nrow = min(kRB, n - r0);
+    // stage the inverse of the diagonal block (64 x 64, 16-byte pieces)
+    {
+        const T *D = A.dinv + ((size_t)blk * 2 + (LOWER ? 0 : 1)) * kRB * kRB;
+        constexpr int per_row = kRB * (int)sizeof(T) / 16;
+        for (int t = threadIdx.x; t < kRB * per_row; t += blockDim.x) {
+            const int r = t / per_row, c = t % per_row;
+            cp_async16(reinterpret_cast<char *>(S.dinv + r * kDS) + 16 * c,
+                       reinterpret_cast<const char *>(D + r * kRB) + 16 * c);
         }
     }
-    if (lane < kb) xr[k0 + lane] = v;
-}
-
-// off-diagonal update: rows outside the block, x[i] -= sum_m A[i][k0+m] x[k0+m];
-// one warp per (row, rhs), lanes over m
-template <class T, bool LOWER>
-__global__ void k_trsv_update(const T *a, int n, int k0, int kb, T *x, int nrhs) {
-    size_t g = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    int rows = LOWER ? n - (k0 + kb) : k0;
-    if (g >= (size_t)rows * nrhs) return;
-    int r = (int)(g / rows), i = (int)(g % rows) + (LOWER ? k0 + kb : 0);
-    T *xr = x + (size_t)r * n;
-    T acc;
-    memset(&acc, 0, sizeof(T));
-    if (lane < kb) {
-        T zero;
-        memset(&zero, 0, sizeof(T));
-        acc = msub(zero, a[(size_t)i * n + k0 + lane], xr[k0 + lane]);  // -A x
+    T acc[RPW][NR];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[r][q] = zero_t<T>();
+    // off-diagonal tiles: forward j = 0..blk-1, backward j = nb-1..blk+1
+    const int ntiles = LOWER ? blk : nb - 1 - blk;
+    for (int t = 0; t < ntiles; ++t) {
+        const int jb = LOWER ? t : nb - 1 - t;
+        const int c = jb * kRB + lane;
+        T a0[RPW], a1[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            const int row = r0 + warp * RPW + r;
+            const bool ok = row < r0 + nrow;
+            const T *ar = A.lu + (size_t)(ok ? row : r0) * n;
+            a0[r] = (ok && c < n) ? ar[c] : zero_t<T>();
+            a1[r] = (ok && c + 32 < n) ? ar[c + 32] : zero_t<T>();
+        }
+        if (threadIdx.x == 0) *s_ok = wave_wait(flags + jb, A.error);
+        __syncthreads();
+        if (!*s_ok) return false;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            if (q >= nr) break;
+            const T *xr = A.x + (size_t)(c0 + q) * n;
+            T x0 = c < n ? ldcg_t(xr + c) : zero_t<T>();
+            T x1 = c + 32 < n ? ldcg_t(xr + c + 32) : zero_t<T>();
+#pragma unroll
+            for (int r = 0; r < RPW; ++r) {
+                acc[r][q] = msub(acc[r][q], a0[r], x0);
+                acc[r][q] = msub(acc[r][q], a1[r], x1);
+            }
+        }
     }
-    acc = warp_sum_t(acc);
-    if (lane == 0) xr[i] = addv(xr[i], acc);
+    // lane partials -> shared memory (no FP64 shuffle trees: the FP64 pipe
+    // is the scarce resource here)
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        if (q >= nr) break;
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) S.part[q][warp * RPW + r][lane] = acc[r][q];
+    }
+    __syncthreads();
+    // row sums: four threads per row, eight partials each, then two shuffles
+    const int row = threadIdx.x >> 2, qq = threadIdx.x & 3;
+    for (int q = 0; q < nr; ++q) {
+        T s = S.part[q][row][qq * 8];
+#pragma unroll
+        for (int l = 1; l < 8; ++l) s = addv(s, S.part[q][row][qq * 8 + l]);
+        s = addv(s, shfl_xor_t(s, 1));
+        s = addv(s, shfl_xor_t(s, 2));
+        if (qq == 0) {
+            T v = zero_t<T>();
+            if (row < nrow) {
+                const int i = r0 + row;
+                T rhs;
+                if (LOWER && A.perm) {
+                    const int src = A.perm[i];
+                    rhs = ldcg_t(A.b + (size_t)(c0 + q) * n + src);
+                    if (A.row_scale) rhs = scale_div(rhs, A.row_scale[src]);
+                } else if (LOWER) {
+                    rhs = ldcg_t(A.b + (size_t)(c0 + q) * n + i);
+                } else {
+                    rhs = ldcg_t(A.x + (size_t)(c0 + q) * n + i);
+                }
+                v = addv(rhs, s);
+            }
+            S.y[q][row] = v;
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // x_b = D_b^-1 y: four threads per row, interleaved columns qq + 4k
+    for (int q = 0; q < nr; ++q) {
+        T v = zero_t<T>();
+#pragma unroll
+        for (int k = 0; k < kRB / 4; ++k) v = mac(v, S.dinv[row * kDS + qq + 4 * k], S.y[q][qq + 4 * k]);
+        v = addv(v, shfl_xor_t(v, 1));
+        v = addv(v, shfl_xor_t(v, 2));
+        if (qq == 0 && row < nrow) {
+            A.x[(size_t)(c0 + q) * n + r0 + row] = v;
+            if (!LOWER && A.col_scale) A.out[(size_t)(c0 + q) * n + r0 + row] = scale_div(v, A.col_scale[r0 + row]);
+        }
+    }
+    __threadfence();
+    __syncthreads();  // every x of the block written; shared memory free for reuse
+    if (threadIdx.x == 0) st_release_u32(flags + blk, 1u);
+    return true;
 }
 
-__global__ void k_col_unscale(cplx *x, const double *col_scale, int n, int nrhs) {
-    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (t >= (size_t)n * nrhs) return;
-    int i = (int)(t % n);
-    double s = col_scale[i];
-    x[t].re = x[t].re / s;
-    x[t].im = x[t].im / s;
+template <class T, int NR>
+__global__ void __launch_bounds__(256) k_trsv_wave(WaveArgs<T> A) {
+    extern __shared__ __align__(16) unsigned char wave_smem[];
+    WaveSmem<T, NR> &S = *reinterpret_cast<WaveSmem<T, NR> *>(wave_smem);
+    __shared__ int s_ok;
+    const int nb = A.nb;
+    for (int c0 = 0, chunk = 0; c0 < A.nrhs; c0 += NR, ++chunk) {
+        const int nr = min(NR, A.nrhs - c0);
+        unsigned *ff = A.flags + (size_t)chunk * 2 * nb, *bf = ff + nb;
+        for (int blk = blockIdx.x; blk < nb; blk += gridDim.x)
+            if (!wave_block<T, NR, true>(A, blk, c0, nr, ff, S, &s_ok)) return;
+        for (int q = blockIdx.x; q < nb; q += gridDim.x) {
+            const int blk = nb - 1 - q;
+            // the last block's backward step also needs the whole forward pass
+            if (blk == nb - 1) {
+                if (threadIdx.x == 0) s_ok = wave_wait(ff + nb - 1, A.error);
+                __syncthreads();
+                if (!s_ok) return;
+            }
+            if (!wave_block<T, NR, false>(A, blk, c0, nr, bf, S, &s_ok)) return;
+        }
+    }
+}
+
+template <class T>
+static constexpr int wave_nr() {
+    return std::is_same<T, double>::value ? 4 : 2;
+}
+
+// Flag words of one wavefront solve of n unknowns and nrhs right-hand sides.
+template <class T>
+static size_t wave_flag_count(int n, int nrhs) {
+    int nb = (n + kRB - 1) / kRB;
+    return (size_t)((nrhs + wave_nr<T>() - 1) / wave_nr<T>()) * 2 * nb;
+}
+
+// Elements of the diagonal-block inverses of an n x n factor.
+static size_t wave_dinv_count(int n) {
+    int nb = (n + kRB - 1) / kRB;
+    return (size_t)nb * 2 * kRB * kRB;
+}
+
+// Computes the diagonal-block inverses of the factor into dinv.
+template <class T>
+static bool wave_prepare(const T *lu, int n, T *dinv) {
+    constexpr size_t smem = (size_t)3 * kRB * kRS * sizeof(T);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_diag_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!cuda_ok(attr, "diagonal block inverse smem attribute")) return false;
+    int nb = (n + kRB - 1) / kRB;
+    PEEC_LAUNCH(k_diag_inverse<T>, nb, 128, smem, lu, n, dinv);
+    return launch_ok("diagonal block inverses");
+}
+
+// Launches the wavefront solve (A.dinv from wave_prepare; flags / error as
+// wave_flag_count words and one int).  Returns false on a launch failure.
+template <class T>
+static bool wave_solve(WaveArgs<T> A) {
+    constexpr int NR = wave_nr<T>();
+    static int capacity = [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(k_trsv_wave<T, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(WaveSmem<T, NR>));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_wave<T, NR>, 256, sizeof(WaveSmem<T, NR>));
+        return sms * per_sm;
+    }();
+    if (capacity < 1) {
+        set_error("triangular solve: kernel does not fit on an SM");
+        return false;
+    }
+    A.nb = (A.n + kRB - 1) / kRB;
+    int grid = std::min(A.nb, capacity);
+    cudaMemsetAsync(A.flags, 0, wave_flag_count<T>(A.n, A.nrhs) * sizeof(unsigned), stream());
+    void *args[] = {&A};
+    note_launch();
+    return cuda_ok(cudaLaunchCooperativeKernel((const void *)k_trsv_wave<T, NR>, dim3(grid), dim3(256), args,
+                                               sizeof(WaveSmem<T, NR>), stream()),
+                   "triangular solve launch");
+}
+
+size_t wave_flag_words_real(int n, int nrhs) { return wave_flag_count<double>(n, nrhs); }
+size_t wave_dinv_words_real(int n) { return wave_dinv_count(n); }
+bool wave_prepare_real(const double *lu, int n, double *dinv) { return wave_prepare(lu, n, dinv); }
+
+bool wave_solve_real(const double *lu, const double *dinv, const int *perm, int n, const double *b, double *x,
+                     int nrhs, unsigned *flags, int *err) {
+    WaveArgs<double> A{};
+    A.lu = lu;
+    A.dinv = dinv;
+    A.n = n;
+    A.nrhs = nrhs;
+    A.perm = perm;
+    A.b = b;
+    A.x = x;
+    A.flags = flags;
+    A.error = err;
+    return wave_solve(A);
 }
 
 // ---------------------------------------------------------------------
@@ -1081,29 +1381,35 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
 template <class T>
 static bool solve_device(const T *d_lu, const int *d_perm, const double *d_row, const double *d_col, int n,
                          const T *d_b, T *d_x, int nrhs) {
-    size_t tot = (size_t)n * nrhs;
-    PEEC_LAUNCH(k_gather<T>, (unsigned)((tot + 255) / 256), 256, 0, d_b, d_x, d_perm, d_row, n, nrhs);
-    int wpb = 8;
-    for (int k0 = 0; k0 < n; k0 += 32) {
-        int kb = std::min(32, n - k0);
-        PEEC_LAUNCH((k_trsv_diag<T, true>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, d_lu, n, k0, kb, d_x, nrhs);
-        size_t rows = (size_t)(n - k0 - kb) * nrhs;
-        if (rows)
-            PEEC_LAUNCH((k_trsv_update<T, true>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, d_lu, n, k0, kb,
-                        d_x, nrhs);
+    constexpr bool cx = sizeof(T) == sizeof(cplx);
+    DBuf<unsigned> flags(wave_flag_count<T>(n, nrhs));
+    DBuf<int> err(1);
+    DBuf<T> work(cx ? (size_t)n * nrhs : 0), dinv(wave_dinv_count(n));
+    if (!flags.p || !err.p || (cx && !work.p) || !dinv.p) return false;
+    if (!cuda_ok(cudaMemsetAsync(err.p, 0, sizeof(int), stream()), "solve scratch")) return false;
+    if (!wave_prepare(d_lu, n, dinv.p)) return false;
+    WaveArgs<T> A{};
+    A.lu = d_lu;
+    A.dinv = dinv.p;
+    A.n = n;
+    A.nrhs = nrhs;
+    A.perm = d_perm;
+    A.row_scale = cx ? d_row : nullptr;
+    A.col_scale = cx ? d_col : nullptr;
+    A.b = d_b;
+    A.x = cx ? work.p : d_x;  // complex: scaled solution in scratch, unscaled into d_x
+    A.out = d_x;
+    A.flags = flags.p;
+    A.error = err.p;
+    if (!wave_solve(A)) return false;
+    int herr = 0;
+    cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+    if (!launch_ok("LU solve kernels") || !sync("LU solve")) return false;
+    if (herr) {
+        set_error("triangular solve: a wait for an earlier row block timed out");
+        return false;
     }
-    int last = ((n - 1) / 32) * 32;
-    for (int k0 = last; k0 >= 0; k0 -= 32) {
-        int kb = std::min(32, n - k0);
-        PEEC_LAUNCH((k_trsv_diag<T, false>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, d_lu, n, k0, kb, d_x, nrhs);
-        size_t rows = (size_t)k0 * nrhs;
-        if (rows)
-            PEEC_LAUNCH((k_trsv_update<T, false>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, d_lu, n, k0, kb,
-                        d_x, nrhs);
-    }
-    if constexpr (sizeof(T) == sizeof(cplx))
-        PEEC_LAUNCH(k_col_unscale, (unsigned)((tot + 255) / 256), 256, 0, (cplx *)d_x, d_col, n, nrhs);
-    return launch_ok("LU solve kernels");
+    return true;
 }
 
 }  // namespace peec
@@ -1823,43 +2129,64 @@ __global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int 
 }
 
 // x += D_c^-1 y  (FP64 accumulation of the FP32 correction)
-__global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs) {
+// |z| rounded to FP32 for the backward error's denominator sum |Z||x| + |b|
+// (a stopping test: FP32 relative error there moves eta by ~1e-7 of itself);
+// values beyond the FP32 range clamp to 3e38, which can only shrink the
+// denominator, i.e. overstate eta.
+__device__ __forceinline__ float abs_f32(cplx z) {
+    double m = sqrt(fma(z.re, z.re, z.im * z.im));
+    return m < 3.0e38 ? (float)m : 3.0e38f;
+}
+
+__global__ void k_abs_matrix(const cplx *Z, size_t count, float *out) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
+        out[t] = abs_f32(Z[t]);
+}
+
+__global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs, float *absx) {
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)n * nrhs) return;
     int i = (int)(t % n);
     double s = cs[i];
-    x[t].re += (double)y[t].re / s;
-    x[t].im += (double)y[t].im / s;
+    cplx v = x[t];
+    v.re += (double)y[t].re / s;
+    v.im += (double)y[t].im / s;
+    x[t] = v;
+    absx[t] = abs_f32(v);
 }
 
 // r = b - Z x in FP64 (one warp per row and right-hand side) and the
-// componentwise backward error, max-reduced as IEEE bits.
-__global__ void k_residual(const cplx *Z, const cplx *x, const cplx *b, int n, int nrhs, cplx *r,
-                           unsigned long long *be) {
+// componentwise backward error |r_i| / (sum_j |Z_ij||x_j| + |b_i|), the
+// denominator from FP32 magnitudes, max-reduced as IEEE bits.
+__global__ void k_residual(const cplx *Z, const float *absZ, const cplx *x, const float *absx, const cplx *b, int n,
+                           int nrhs, cplx *r, unsigned long long *be) {
     long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= (long long)n * nrhs) return;
     int q = (int)(warp / n), i = (int)(warp % n);
     const cplx *row = Z + (size_t)i * n, *xr = x + (size_t)q * n;
-    double yr = 0.0, yi = 0.0, den = 0.0;
+    const float *arow = absZ + (size_t)i * n, *ax = absx + (size_t)q * n;
+    double yr = 0.0, yi = 0.0;
+    float den = 0.0f;
     for (int j = lane; j < n; j += 32) {
         cplx z = row[j], v = xr[j];
         yr = fma(z.re, v.re, yr);
         yr = fma(-z.im, v.im, yr);
         yi = fma(z.re, v.im, yi);
         yi = fma(z.im, v.re, yi);
-        den = fma(hypot(z.re, z.im), hypot(v.re, v.im), den);
+        den = fmaf(arow[j], ax[j], den);
     }
     yr = warp_sum(yr);
     yi = warp_sum(yi);
-    den = warp_sum(den);
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) den += __shfl_xor_sync(0xffffffffu, den, m);
     if (lane == 0) {
         cplx bi = b[(size_t)q * n + i];
         cplx ri = cplx{bi.re - yr, bi.im - yi};
         r[(size_t)q * n + i] = ri;
-        double res = hypot(ri.re, ri.im), babs = hypot(bi.re, bi.im);
-        den += babs;
-        double eta = den > 0.0 ? res / den : res;
+        double res = sqrt(fma(ri.re, ri.re, ri.im * ri.im)), babs = hypot(bi.re, bi.im);
+        double d = (double)den + babs;
+        double eta = d > 0.0 ? res / d : res;
         if (!isfinite(eta)) eta = INFINITY;
         atomicMax(be, (unsigned long long)__double_as_longlong(eta));
     }
@@ -2010,31 +2337,33 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     cudaMemcpyAsync(r.p, b, nv * sizeof(cplx), cudaMemcpyDeviceToDevice, stream());
     double eta = INFINITY;
     int it = 0;
-    const int wpb = 8;
+    DBuf<unsigned> wflags(wave_flag_count<cplxf>(n, nrhs));
+    DBuf<int> werr(1);
+    DBuf<cplxf> wdinv(wave_dinv_count(n));
+    DBuf<float> absZ(nn), absx(nv);
+    if (!wflags.p || !werr.p || !wdinv.p || !absZ.p || !absx.p) return -1;
+    PEEC_LAUNCH(k_abs_matrix, 152 * 8, 256, 0, Z, nn, absZ.p);
+    cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
+    if (!wave_prepare(a, n, wdinv.p)) return -1;
     // one refinement sweep (FP32 correction solve, FP64 update, FP64
-    // residual + backward error) is ~1000 launches: capture it once as a
-    // CUDA graph and replay it per iteration
+    // residual + backward error): captured once as a CUDA graph and
+    // replayed per iteration
     auto sweep = [&]() {
         PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
-        for (int k0 = 0; k0 < n; k0 += 32) {
-            int kb = std::min(32, n - k0);
-            PEEC_LAUNCH((k_trsv_diag<cplxf, true>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, a, n, k0, kb, y.p, nrhs);
-            size_t rows = (size_t)(n - k0 - kb) * nrhs;
-            if (rows)
-                PEEC_LAUNCH((k_trsv_update<cplxf, true>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, a, n, k0,
-                            kb, y.p, nrhs);
-        }
-        for (int k0 = ((n - 1) / 32) * 32; k0 >= 0; k0 -= 32) {
-            int kb = std::min(32, n - k0);
-            PEEC_LAUNCH((k_trsv_diag<cplxf, false>), (nrhs + wpb - 1) / wpb, wpb * 32, 0, a, n, k0, kb, y.p, nrhs);
-            size_t rows = (size_t)k0 * nrhs;
-            if (rows)
-                PEEC_LAUNCH((k_trsv_update<cplxf, false>), (unsigned)((rows + wpb - 1) / wpb), wpb * 32, 0, a, n, k0,
-                            kb, y.p, nrhs);
-        }
-        PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs);
+        WaveArgs<cplxf> W{};
+        W.lu = a;
+        W.dinv = wdinv.p;
+        W.n = n;
+        W.nrhs = nrhs;
+        W.b = y.p;  // already permuted and row-scaled by k_mix_rhs
+        W.x = y.p;
+        W.flags = wflags.p;
+        W.error = werr.p;
+        wave_solve(W);
+        PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs, absx.p);
         cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
-        PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, x, b, n, nrhs, r.p, be.p);
+        PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, b, n, nrhs, r.p,
+                    be.p);
     };
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -2058,8 +2387,11 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             sweep();
         }
         unsigned long long hb = 0;
+        int hw = 0;
         cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
-        if (!launch_ok("refinement") || !sync("refinement")) {
+        cudaMemcpyAsync(&hw, werr.p, sizeof(hw), cudaMemcpyDeviceToHost, stream());
+        if (!launch_ok("refinement") || !sync("refinement") || hw) {
+            if (hw) set_error("triangular solve: a wait for an earlier row block timed out");
             if (gexec) cudaGraphExecDestroy(gexec);
             if (graph) cudaGraphDestroy(graph);
             return -1;

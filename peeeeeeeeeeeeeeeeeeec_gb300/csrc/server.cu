@@ -1,21 +1,23 @@
-// Serving loop: continuous batching of harmonic solves on one GPU.
+// Serving loop: continuous admission of harmonic and transient requests on
+// one GPU.
 //
-// Requests (mesh, frequency, plane-wave right-hand sides, plain or mixed
-// precision) enter a FIFO.  Worker threads -- each with its own CUDA stream,
+// Requests enter a FIFO.  Worker threads -- each with its own CUDA stream,
 // so admitted requests overlap on the device -- admit the head request as
 // soon as a worker is free and its HBM estimate fits the remaining budget.
 // Assembled Lp / P stay device-resident per mesh key and are reused by every
-// later request on that mesh (any frequency); the cache is evicted least-
-// recently-used when a new request needs the memory.  Each request records
-// submit / start / end times for latency percentiles.
+// later request on that mesh (any frequency); a transient system (its
+// factorised MNA matrix) stays resident per mesh, scheme and time step and
+// is reused by every later lightning run on it.  Cached meshes are evicted,
+// least recently used first, when a new request needs the memory.  Each
+// request records submit / start / end times for latency percentiles.
 #include <math.h>
 #include <string.h>
 
 #include <chrono>
 #include <condition_variable>
 #include <deque>
-#include <memory>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -25,26 +27,47 @@
 
 namespace peec {
 
+struct TransientEntry {
+    void *sys = nullptr;
+    size_t bytes = 0;
+    bool ready = false;
+    int status = 0;
+};
+
 struct MeshEntry {
     unsigned long long key = 0;
     double *L = nullptr, *P = nullptr, *ctr = nullptr, *vec = nullptr;
     int *edges = nullptr;
-    size_t ne = 0, nv = 0, bytes = 0;
+    size_t ne = 0, nv = 0, bytes = 0;  // bytes: Lp / P / geometry plus every transient system
     int users = 0;
     bool ready = false;
     int status = 0;
     unsigned long long last_use = 0;
+    std::map<std::pair<int, double>, TransientEntry> transient;  // (scheme, dt)
 };
 
 struct Job {
-    long long ticket;
-    PeecHarmonicRequest req;
-    std::vector<double> k_hat, e_hat;  // copies
-    size_t bytes = 0;                  // per-request device estimate (mesh cache excluded)
-    size_t mesh_bytes = 0;
+    long long ticket = 0;
+    int kind = 0;  // 0 harmonic, 1 transient lightning
+    PeecHarmonicRequest req{};
+    PeecTransientRequest treq{};
+    std::vector<double> k_hat, e_hat;           // harmonic: copies
+    std::vector<int> probe_nodes, probe_edges;  // transient: copies
+    const Mesh *mesh = nullptr;
+    const DualMesh *dual = nullptr;
+    unsigned long long mesh_key = 0;
+    size_t bytes = 0;       // per-request device estimate (caches excluded)
+    size_t mesh_bytes = 0;  // Lp / P / geometry of the mesh
+    size_t sys_bytes = 0;   // transient system of (scheme, dt)
     PeecRequestResult res{};
     bool done = false;
 };
+
+// factor + A S + diagonal-block inverses + vectors of a transient system
+static size_t transient_system_bytes(size_t ne, size_t nv) {
+    size_t nt = ne + nv, nb = (nt + 63) / 64;
+    return 8 * nt * nt + 8 * ne * nv + 8 * nb * 2 * 64 * 64 + 64 * nt + 16 * ne;
+}
 
 class Server {
   public:
@@ -75,24 +98,42 @@ class Server {
             return -1;
         }
         auto j = std::make_shared<Job>();
+        j->kind = 0;
         j->req = *r;
+        j->mesh = r->mesh;
+        j->dual = r->dual;
+        j->mesh_key = r->mesh_key;
         j->k_hat.assign(r->k_hat, r->k_hat + 3 * r->nrhs);
         j->e_hat.assign(r->e_hat, r->e_hat + 3 * r->nrhs);
         size_t ne = r->mesh->n_edges, nv = r->mesh->n_nodes, n = ne + nv;
-        j->mesh_bytes = 8 * (ne * ne + nv * nv) + 56 * ne;
-        // Z + working copy (FP32 LU for mixed, FP64 LU for plain) + vectors
-        j->bytes = 16 * n * n + (r->mixed ? 8 * n * n + 6 * n * 192 : 16 * n * n) + 64 * n * r->nrhs + (64 << 20);
-        if (j->bytes + j->mesh_bytes > budget_) {
-            set_error("server: request needs more device memory than the server's budget");
+        j->mesh_bytes = mesh_bytes(ne, nv);
+        // Z + working copy (FP32 LU + FP32 |Z| for mixed, FP64 LU for plain) + vectors + scratch
+        j->bytes = 16 * n * n + (r->mixed ? 12 * n * n + 6 * n * 192 : 16 * n * n) + 96 * n * r->nrhs + (64 << 20);
+        return enqueue(j);
+    }
+
+    long long submit(const PeecTransientRequest *r) {
+        if (!r || !r->mesh || !r->dual || r->n_steps == 0 || r->mesh->n_edges == 0 || r->mesh->n_nodes == 0 ||
+            (r->scheme != 1 && r->scheme != 2) || !(r->dt > 0.0) || !isfinite(r->dt) ||
+            (r->n_probe_nodes && !r->probe_nodes) || (r->n_probe_edges && !r->probe_edges) ||
+            ((r->n_probe_nodes || r->n_probe_edges) && !r->probes)) {
+            set_error("server: invalid request");
             return -1;
         }
-        std::lock_guard<std::mutex> g(mu_);
-        j->ticket = next_ticket_++;
-        j->res.t_submit = clock();
-        jobs_[j->ticket] = j;
-        queue_.push_back(j);
-        cv_.notify_all();
-        return j->ticket;
+        auto j = std::make_shared<Job>();
+        j->kind = 1;
+        j->treq = *r;
+        j->mesh = r->mesh;
+        j->dual = r->dual;
+        j->mesh_key = r->mesh_key;
+        j->probe_nodes.assign(r->probe_nodes, r->probe_nodes + r->n_probe_nodes);
+        j->probe_edges.assign(r->probe_edges, r->probe_edges + r->n_probe_edges);
+        size_t ne = r->mesh->n_edges, nv = r->mesh->n_nodes, nt = ne + nv;
+        size_t np = r->n_probe_nodes + r->n_probe_edges;
+        j->mesh_bytes = mesh_bytes(ne, nv);
+        j->sys_bytes = transient_system_bytes(ne, nv);
+        j->bytes = 8 * r->n_steps * np + 64 * nt + 4 * np + (64 << 20);
+        return enqueue(j);
     }
 
     int wait(long long ticket, PeecRequestResult *out) {
@@ -120,18 +161,40 @@ class Server {
     unsigned long long tick_ = 0;
     bool stop_ = false;
 
+    static size_t mesh_bytes(size_t ne, size_t nv) { return 8 * (ne * ne + nv * nv) + 56 * ne; }
+
+    long long enqueue(const std::shared_ptr<Job> &j) {
+        if (j->bytes + j->mesh_bytes + j->sys_bytes > budget_) {
+            set_error("server: request needs more device memory than the server's budget");
+            return -1;
+        }
+        std::lock_guard<std::mutex> g(mu_);
+        j->ticket = next_ticket_++;
+        j->res.t_submit = clock();
+        jobs_[j->ticket] = j;
+        queue_.push_back(j);
+        cv_.notify_all();
+        return j->ticket;
+    }
+
     // stream-ordered free on the calling thread's stream: an entry is freed
     // only when no request uses it and every user has synchronised
     static void free_mesh(MeshEntry &m) {
+        for (auto &t : m.transient)
+            if (t.second.sys) peec_gb300_transient_destroy(t.second.sys);
+        m.transient.clear();
         for (void *p : {(void *)m.L, (void *)m.P, (void *)m.ctr, (void *)m.vec, (void *)m.edges}) dfree(p);
         m.L = m.P = m.ctr = m.vec = nullptr;
         m.edges = nullptr;
     }
 
-    // bytes the head job needs now (its own + the mesh entry if not cached)
+    // bytes the job needs now: its own, plus the mesh and the transient
+    // system when they are not cached
     size_t need(const Job &j) {
-        auto it = meshes_.find(j.req.mesh_key);
-        return j.bytes + (it == meshes_.end() ? j.mesh_bytes : 0);
+        auto it = meshes_.find(j.mesh_key);
+        if (it == meshes_.end()) return j.bytes + j.mesh_bytes + j.sys_bytes;
+        if (j.kind == 1 && !it->second.transient.count({j.treq.scheme, j.treq.dt})) return j.bytes + j.sys_bytes;
+        return j.bytes;
     }
 
     // evict unused cached meshes (least recently used first, never `keep`)
@@ -155,30 +218,43 @@ class Server {
         for (;;) {
             std::shared_ptr<Job> j;
             MeshEntry *me = nullptr;
-            bool build_mesh = false;
+            TransientEntry *te = nullptr;
+            bool build_mesh = false, build_sys = false;
             {
                 std::unique_lock<std::mutex> g(mu_);
                 for (;;) {
                     if (stop_ && queue_.empty()) return;
                     if (!queue_.empty()) {
                         size_t nb = need(*queue_.front());
-                        make_room(nb, queue_.front()->req.mesh_key);
+                        make_room(nb, queue_.front()->mesh_key);
                         if (used_ + nb <= budget_) break;
                     }
                     cv_.wait(g);
                 }
                 j = queue_.front();
                 queue_.pop_front();
-                auto it = meshes_.find(j->req.mesh_key);
+                auto it = meshes_.find(j->mesh_key);
                 if (it == meshes_.end()) {
                     MeshEntry e;
-                    e.key = j->req.mesh_key;
+                    e.key = j->mesh_key;
                     e.bytes = j->mesh_bytes;
                     it = meshes_.emplace(e.key, e).first;
                     used_ += j->mesh_bytes;
                     build_mesh = true;
                 }
                 me = &it->second;
+                if (j->kind == 1) {
+                    auto key = std::make_pair(j->treq.scheme, j->treq.dt);
+                    auto ti = me->transient.find(key);
+                    if (ti == me->transient.end()) {
+                        ti = me->transient.emplace(key, TransientEntry()).first;
+                        ti->second.bytes = j->sys_bytes;
+                        me->bytes += j->sys_bytes;
+                        used_ += j->sys_bytes;
+                        build_sys = true;
+                    }
+                    te = &ti->second;
+                }
                 me->users++;
                 me->last_use = ++tick_;
                 used_ += j->bytes;
@@ -186,7 +262,7 @@ class Server {
             }
             cv_.notify_all();
             if (build_mesh) {
-                int s = assemble_mesh(*me, j->req);
+                int s = assemble_mesh(*me, j->mesh, j->dual);
                 std::lock_guard<std::mutex> g(mu_);
                 me->status = s;
                 me->ready = true;
@@ -195,14 +271,32 @@ class Server {
                 std::unique_lock<std::mutex> g(mu_);
                 cv_.wait(g, [&] { return me->ready; });
             }
-            int status = me->status == 0 ? solve(*me, *j) : -1;
+            int status = me->status == 0 ? 0 : -1;
+            if (status == 0 && j->kind == 1) {
+                if (build_sys) {
+                    void *sys = nullptr;
+                    int s = peec_gb300_transient_create(me->L, me->P, me->edges, nullptr, me->ne, me->nv,
+                                                        j->treq.scheme, j->treq.dt, &sys);
+                    std::lock_guard<std::mutex> g(mu_);
+                    te->sys = sys;
+                    te->status = s;
+                    te->ready = true;
+                    cv_.notify_all();
+                } else {
+                    std::unique_lock<std::mutex> g(mu_);
+                    cv_.wait(g, [&] { return te->ready; });
+                }
+                status = te->status;
+            }
+            if (status == 0) status = j->kind == 0 ? solve(*me, *j) : run_transient(*me, *te, *j);
             {
                 std::lock_guard<std::mutex> g(mu_);
                 j->res.status = status;
                 j->res.t_end = clock();
                 used_ -= j->bytes;
                 me->users--;
-                if (me->status != 0 && me->users == 0) {  // a failed assembly is not kept
+                if ((me->status != 0 || (te && te->status != 0)) && me->users == 0) {
+                    // a failed assembly or factorisation is not kept
                     used_ -= me->bytes;
                     free_mesh(*me);
                     meshes_.erase(me->key);
@@ -214,8 +308,7 @@ class Server {
         }
     }
 
-    int assemble_mesh(MeshEntry &e, const PeecHarmonicRequest &r) {
-        const Mesh *m = r.mesh;
+    int assemble_mesh(MeshEntry &e, const Mesh *m, const DualMesh *dual) {
         e.ne = m->n_edges;
         e.nv = m->n_nodes;
         e.L = static_cast<double *>(dalloc(8 * e.ne * e.ne));
@@ -228,8 +321,8 @@ class Server {
         inductance_options_default(&lo, 1);
         PotentialOptions po;
         potential_options_default(&po, 1);
-        if (peec_gb300_inductance_device(m, r.dual, &lo, e.L, nullptr) != 0) return -1;
-        if (peec_gb300_potential_device(m, r.dual, &po, e.P, nullptr) != 0) return -1;
+        if (peec_gb300_inductance_device(m, dual, &lo, e.L, nullptr) != 0) return -1;
+        if (peec_gb300_potential_device(m, dual, &po, e.P, nullptr) != 0) return -1;
         if (peec_gb300_copy_to_device(e.ctr, m->edge_centers, 24 * e.ne) != 0 ||
             peec_gb300_copy_to_device(e.vec, m->edge_vectors, 24 * e.ne) != 0 ||
             peec_gb300_copy_to_device(e.edges, m->edges, 8 * e.ne) != 0)
@@ -268,13 +361,32 @@ class Server {
                 status = peec_gb300_complex_lu_solve_device(W.p, perm.p, rs.p, cs.p, n, B.p, X.p, nrhs);
             double out[3];
             if (status == 0 && peec_gb300_backward_error_device(Z.p, n, X.p, B.p, nrhs, out) == 0) be = out[0];
-            iters = 0;
         }
         j.res.backward_error = be;
         j.res.iterations = iters;
         if (status < 0) return status;
         if (!X.download(r.x, n * nrhs) || !sync("serving result")) return -1;
         return status;
+    }
+
+    int run_transient(const MeshEntry &e, const TransientEntry &t, Job &j) {
+        const PeecTransientRequest &r = j.treq;
+        const size_t npn = j.probe_nodes.size(), npe = j.probe_edges.size(), np = npn + npe;
+        DBuf<double> I(e.ne), V(e.nv), probes(r.n_steps * np);
+        DBuf<int> pn(npn), pe(npe);
+        if (!I.p || !V.p || (np && !probes.p) || (npn && !pn.p) || (npe && !pe.p)) return -1;
+        cudaMemsetAsync(I.p, 0, 8 * e.ne, stream());
+        cudaMemsetAsync(V.p, 0, 8 * e.nv, stream());
+        if ((npn && !pn.upload(j.probe_nodes.data(), npn)) || (npe && !pe.upload(j.probe_edges.data(), npe)))
+            return -1;
+        int s = peec_gb300_transient_lightning(t.sys, r.K, r.alpha, r.beta, r.delay, r.strike_node, r.return_node, 0,
+                                               r.n_steps, I.p, V.p, pn.p, npn, pe.p, npe, probes.p);
+        j.res.iterations = (int)r.n_steps;
+        if (s != 0) return s;
+        if ((np && !probes.download(r.probes, r.n_steps * np)) || (r.I && !I.download(r.I, e.ne)) ||
+            (r.V && !V.download(r.V, e.nv)) || !sync("transient result"))
+            return -1;
+        return 0;
     }
 };
 
@@ -291,6 +403,10 @@ void *peec_gb300_server_create(size_t hbm_budget_bytes, int workers) {
 }
 
 long long peec_gb300_server_submit(void *server, const PeecHarmonicRequest *request) {
+    return server ? static_cast<peec::Server *>(server)->submit(request) : -1;
+}
+
+long long peec_gb300_server_submit_transient(void *server, const PeecTransientRequest *request) {
     return server ? static_cast<peec::Server *>(server)->submit(request) : -1;
 }
 

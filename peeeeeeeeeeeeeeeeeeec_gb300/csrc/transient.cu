@@ -1,0 +1,369 @@
+// Stage-1 transient stepping on the device: the reference's
+// transient_system_create_stage1 + transient_factorize (transient.c:385-480,
+// 1020-1110, 2014-2066) and, per step, lightning_build_node_current
+// (lightning.c:184-373), transient_build_rhs_stage1 (transient.c:1421-1660)
+// and transient_solve_step (transient.c:2068-2097).
+//
+// The system matrix M = [L/dt + theta R, theta AS; -theta A^T, F/dt] is
+// filled and LU-factorised once on the device and stays resident; every step
+// then reads Lp and AS once (the right-hand side, an HBM-bound GEMV with the
+// node rows gathered through a node -> edge adjacency instead of the dense
+// incidence) and the factor once (one cooperative wavefront solve).  The
+// state x = [I; V] never leaves HBM between steps.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/peec_gb300.h"
+#include "common.cuh"
+#include "solve.cuh"
+
+namespace peec {
+
+struct TransientSystem {
+    int ne = 0, nv = 0, nt = 0, scheme = 0;
+    double theta = 0.0, dt = 0.0;
+    const double *L = nullptr;  // caller's Lp (kept by pointer)
+    double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
+    long long *piv = nullptr;
+    int *perm = nullptr, *edges = nullptr;
+    int *adj_ptr = nullptr, *adj = nullptr;  // node j: edges +(e+1) entering (b = j), -(e+1) leaving (a = j)
+    void release() {
+        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)piv, (void *)perm,
+                        (void *)edges, (void *)adj_ptr, (void *)adj})
+            dfree(p);
+        R = F = AS = lu = dinv = nullptr;
+        piv = nullptr;
+        perm = edges = adj_ptr = adj = nullptr;
+    }
+};
+
+// F_j = 1 / P_jj (potential.c:483-520); a non-finite or non-positive
+// diagonal sets *bad
+__global__ void k_self_capacitance(const double *P, int nv, double *F, int *bad) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nv) return;
+    double d = P[(size_t)j * nv + j];
+    if (!isfinite(d) || d <= 0.0) {
+        atomicExch(bad, 1);
+        F[j] = NAN;
+        return;
+    }
+    F[j] = 1.0 / d;
+}
+
+// AS[e][k] = (P[b][k] - P[a][k]) / P[k][k] (incidence.c:593-741), k fastest
+__global__ void k_as_build(const double *P, const int *edges, int ne, int nv, double *AS) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)ne * nv) return;
+    int e = (int)(t / nv), k = (int)(t % nv);
+    int a = edges[2 * e], b = edges[2 * e + 1];
+    AS[t] = (P[(size_t)b * nv + k] - P[(size_t)a * nv + k]) / P[(size_t)k * nv + k];
+}
+
+// M, row-major nt x nt (transient.c:1020-1110, stage 1)
+__global__ void k_transient_fill(const double *L, const double *R, const double *AS, const double *F, const int *edges,
+                                 int ne, int nv, double theta, double dt, double *M) {
+    const int nt = ne + nv;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)nt * nt;
+         t += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(t / nt), j = (int)(t % nt);
+        double v;
+        if (i < ne && j < ne) {
+            v = L[(size_t)i * ne + j] / dt;
+            if (i == j) v += theta * R[i];
+        } else if (i < ne) {
+            v = theta * AS[(size_t)i * nv + (j - ne)];
+        } else if (j < ne) {
+            int node = i - ne;
+            double a = edges[2 * j + 1] == node ? 1.0 : edges[2 * j] == node ? -1.0 : 0.0;
+            v = -theta * a;
+        } else {
+            v = (i == j ? F[i - ne] : 0.0) / dt;
+        }
+        M[t] = v;
+    }
+}
+
+struct LightningArgs {
+    double K, alpha, beta, delay;
+    int strike, ret;
+};
+
+// lightning.c:184-212
+__device__ __forceinline__ double lightning_current(const LightningArgs &s, double t) {
+    if (t < s.delay) return 0.0;
+    double tau = t - s.delay;
+    return s.K * (exp(-s.alpha * tau) - exp(-s.beta * tau));
+}
+
+struct StepArgs {
+    const double *L, *R, *AS, *F;
+    const int *adj_ptr, *adj;
+    int ne, nv;
+    double theta, dt;
+    const double *x;  // state [I; V] after the previous step
+    double *rhs;
+    LightningArgs src;
+    long long step;
+    // probes of the previous step's state (record_row >= 0)
+    const int *probe_nodes, *probe_edges;
+    int n_probe_nodes, n_probe_edges;
+    double *probes;
+    long long record_row;
+};
+
+__device__ __forceinline__ void record_probes(const StepArgs &A, long long row) {
+    const int np = A.n_probe_nodes + A.n_probe_edges;
+    for (int k = threadIdx.x; k < np; k += blockDim.x) {
+        double v = NAN;  // an index outside the mesh records NaN
+        if (k < A.n_probe_nodes) {
+            int j = A.probe_nodes[k];
+            if (j >= 0 && j < A.nv) v = A.x[A.ne + j];
+        } else {
+            int e = A.probe_edges[k - A.n_probe_nodes];
+            if (e >= 0 && e < A.ne) v = A.x[e];
+        }
+        A.probes[row * np + k] = v;
+    }
+}
+
+// Right-hand side of one step (transient.c:1421-1631, edge voltages absent):
+// blocks [0, eb) take the edge rows, one warp each; the rest the node rows.
+__global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
+    const double omt = 1.0 - A.theta;
+    if (blockIdx.x == 0 && A.probes && A.record_row >= 0) record_probes(A, A.record_row);
+    if ((int)blockIdx.x < eb) {
+        const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+        if (i >= A.ne) return;
+        const double *I = A.x, *V = A.x + A.ne;
+        const double *Lr = A.L + (size_t)i * A.ne;
+        double s = 0.0;
+        for (int j = lane; j < A.ne; j += 32) s = fma(Lr[j], I[j], s);
+        s = warp_sum(s);
+        double sa = 0.0;
+        if (omt != 0.0) {
+            const double *Ar = A.AS + (size_t)i * A.nv;
+            for (int j = lane; j < A.nv; j += 32) sa = fma(Ar[j], V[j], sa);
+            sa = warp_sum(sa);
+        }
+        if (lane == 0) A.rhs[i] = s / A.dt - omt * A.R[i] * I[i] - omt * sa;
+        return;
+    }
+    const int j = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
+    if (j >= A.nv) return;
+    const double tn = (double)A.step * A.dt, tnp1 = (double)(A.step + 1) * A.dt;
+    double jn = 0.0, jnp1 = 0.0;
+    if (j == A.src.strike || j == A.src.ret) {
+        jn = lightning_current(A.src, tn);
+        jnp1 = lightning_current(A.src, tnp1);
+        if (j == A.src.ret) {
+            jn = -jn;
+            jnp1 = -jnp1;
+        }
+    }
+    double v = A.F[j] * A.x[A.ne + j] / A.dt;
+    double at = 0.0;  // (A^T I)_j
+    for (int k = A.adj_ptr[j]; k < A.adj_ptr[j + 1]; ++k) {
+        int s = A.adj[k];
+        at += s > 0 ? A.x[s - 1] : -A.x[-s - 1];
+    }
+    v += omt * at;
+    v += omt * jn;
+    v += A.theta * jnp1;
+    A.rhs[A.ne + j] = v;
+}
+
+__global__ void k_transient_probe(StepArgs A) { record_probes(A, A.record_row); }
+
+static int create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R, size_t ne_, size_t nv_,
+                  int scheme, double dt, TransientSystem &S) {
+    if (!d_L || !d_P || !d_edges || ne_ == 0 || nv_ == 0 || ne_ + nv_ > 200000 || (scheme != 1 && scheme != 2) ||
+        !isfinite(dt) || dt <= 0.0) {
+        set_error("transient: invalid arguments (scheme 1 or 2, dt > 0, non-empty mesh)");
+        return -1;
+    }
+    const int ne = (int)ne_, nv = (int)nv_, nt = ne + nv;
+    S.ne = ne;
+    S.nv = nv;
+    S.nt = nt;
+    S.scheme = scheme;
+    S.theta = scheme == 1 ? 1.0 : 0.5;
+    S.dt = dt;
+    S.L = d_L;
+    // edge list on the host for the node -> edge adjacency (A^T)
+    std::vector<int> edges(2 * (size_t)ne);
+    if (!cuda_ok(cudaMemcpyAsync(edges.data(), d_edges, edges.size() * sizeof(int), cudaMemcpyDeviceToHost, stream()),
+                 "transient edges") ||
+        !sync("transient edges"))
+        return -1;
+    std::vector<int> ptr(nv + 1, 0), adj(2 * (size_t)ne);
+    for (int e = 0; e < ne; ++e) {
+        int a = edges[2 * e], b = edges[2 * e + 1];
+        if (a < 0 || b < 0 || a >= nv || b >= nv || a == b) {
+            set_error("transient: edge with an invalid node pair");
+            return -1;
+        }
+        ptr[a + 1]++;
+        ptr[b + 1]++;
+    }
+    for (int j = 0; j < nv; ++j) ptr[j + 1] += ptr[j];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int e = 0; e < ne; ++e) {  // increasing edge order within each node
+        adj[fill[edges[2 * e]]++] = -(e + 1);
+        adj[fill[edges[2 * e + 1]]++] = e + 1;
+    }
+    S.R = static_cast<double *>(dalloc(sizeof(double) * ne));
+    S.F = static_cast<double *>(dalloc(sizeof(double) * nv));
+    S.AS = static_cast<double *>(dalloc(sizeof(double) * (size_t)ne * nv));
+    S.lu = static_cast<double *>(dalloc(sizeof(double) * (size_t)nt * nt));
+    S.piv = static_cast<long long *>(dalloc(sizeof(long long) * nt));
+    S.perm = static_cast<int *>(dalloc(sizeof(int) * nt));
+    S.edges = static_cast<int *>(dalloc(sizeof(int) * 2 * (size_t)ne));
+    S.adj_ptr = static_cast<int *>(dalloc(sizeof(int) * (nv + 1)));
+    S.adj = static_cast<int *>(dalloc(sizeof(int) * 2 * (size_t)ne));
+    DBuf<int> bad(1);
+    if (!S.R || !S.F || !S.AS || !S.lu || !S.piv || !S.perm || !S.edges || !S.adj_ptr || !S.adj || !bad.p) return -1;
+    cudaStream_t st = stream();
+    if (d_R)
+        cudaMemcpyAsync(S.R, d_R, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st);
+    else
+        cudaMemsetAsync(S.R, 0, sizeof(double) * ne, st);
+    cudaMemcpyAsync(S.edges, edges.data(), edges.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(S.adj_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(S.adj, adj.data(), adj.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(bad.p, 0, sizeof(int), st);
+    PEEC_LAUNCH(k_self_capacitance, (nv + 255) / 256, 256, 0, d_P, nv, S.F, bad.p);
+    size_t nas = (size_t)ne * nv;
+    PEEC_LAUNCH(k_as_build, (unsigned)((nas + 255) / 256), 256, 0, d_P, S.edges, ne, nv, S.AS);
+    PEEC_LAUNCH(k_transient_fill, 152 * 16, 256, 0, d_L, S.R, S.AS, S.F, S.edges, ne, nv, S.theta, dt, S.lu);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!launch_ok("transient system") || !sync("transient system")) return -1;
+    if (hbad) {
+        set_error("transient: invalid diagonal of P (non-finite or not positive)");
+        return -1;
+    }
+    double scale;
+    int col;
+    int s = peec_gb300_lu_factor_device(S.lu, nt, 1.0e-14, S.piv, S.perm, &scale, &col);
+    if (s != 0) return s == -2 ? -2 : -1;
+    // diagonal-block inverses for the per-step solves, once per factor
+    S.dinv = static_cast<double *>(dalloc(sizeof(double) * wave_dinv_words_real(nt)));
+    if (!S.dinv || !wave_prepare_real(S.lu, nt, S.dinv) || !sync("transient factor")) return -1;
+    return 0;
+}
+
+static int run_lightning(const TransientSystem &S, const LightningArgs &src, long long step0, long long n_steps,
+                         double *d_I, double *d_V, const int *probe_nodes, int n_probe_nodes, const int *probe_edges,
+                         int n_probe_edges, double *probes) {
+    const int ne = S.ne, nv = S.nv, nt = S.nt;
+    DBuf<double> x(nt), rhs(nt);
+    DBuf<unsigned> flags(wave_flag_words_real(nt, 1));
+    DBuf<int> err(1);
+    if (!x.p || !rhs.p || !flags.p || !err.p) return -1;
+    cudaStream_t st = stream();
+    cudaMemcpyAsync(x.p, d_I, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(x.p + ne, d_V, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(err.p, 0, sizeof(int), st);
+    StepArgs A{};
+    A.L = S.L;
+    A.R = S.R;
+    A.AS = S.AS;
+    A.F = S.F;
+    A.adj_ptr = S.adj_ptr;
+    A.adj = S.adj;
+    A.ne = ne;
+    A.nv = nv;
+    A.theta = S.theta;
+    A.dt = S.dt;
+    A.x = x.p;
+    A.rhs = rhs.p;
+    A.src = src;
+    A.probe_nodes = probe_nodes;
+    A.probe_edges = probe_edges;
+    A.n_probe_nodes = n_probe_nodes;
+    A.n_probe_edges = n_probe_edges;
+    A.probes = (n_probe_nodes + n_probe_edges) > 0 ? probes : nullptr;
+    const int eb = (ne + 7) / 8, grid = eb + (nv + 255) / 256;
+    for (long long k = 0; k < n_steps; ++k) {
+        A.step = step0 + k;
+        A.record_row = k - 1;
+        PEEC_LAUNCH(k_transient_rhs, grid, 256, 0, A, eb);
+        if (!wave_solve_real(S.lu, S.dinv, S.perm, nt, rhs.p, x.p, 1, flags.p, err.p)) return -1;
+        if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
+    }
+    if (A.probes && n_steps > 0) {
+        A.record_row = n_steps - 1;
+        PEEC_LAUNCH(k_transient_probe, 1, 256, 0, A);
+    }
+    cudaMemcpyAsync(d_I, x.p, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(d_V, x.p + ne, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!launch_ok("transient steps") || !sync("transient steps")) return -1;
+    if (herr) {
+        set_error("transient: a triangular-solve wait timed out");
+        return -1;
+    }
+    return 0;
+}
+
+}  // namespace peec
+
+using namespace peec;
+
+extern "C" {
+
+int peec_gb300_transient_create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R,
+                                size_t n_edges, size_t n_nodes, int scheme, double dt, void **system) {
+    if (!system) return -1;
+    *system = nullptr;
+    auto *S = new TransientSystem();
+    int s = create(d_L, d_P, d_edges, d_R, n_edges, n_nodes, scheme, dt, *S);
+    if (s != 0) {
+        S->release();
+        sync("transient release");
+        delete S;
+        return s;
+    }
+    *system = S;
+    return 0;
+}
+
+int peec_gb300_transient_lightning(void *system, double K, double alpha, double beta, double delay,
+                                   size_t strike_node, size_t return_node, size_t step0, size_t n_steps, double *d_I,
+                                   double *d_V, const int *d_probe_nodes, size_t n_probe_nodes,
+                                   const int *d_probe_edges, size_t n_probe_edges, double *d_probes) {
+    auto *S = static_cast<TransientSystem *>(system);
+    if (!S || !d_I || !d_V) {
+        set_error("transient: missing system or state");
+        return -1;
+    }
+    // lightning.c:66-171
+    if (!isfinite(K) || K <= 0.0 || !isfinite(alpha) || !isfinite(beta) || alpha <= 0.0 || beta <= 0.0 ||
+        beta <= alpha || !isfinite(delay) || delay < 0.0 || strike_node >= (size_t)S->nv ||
+        return_node >= (size_t)S->nv || strike_node == return_node) {
+        set_error("transient: invalid lightning source (K > 0, 0 < alpha < beta, delay >= 0, two distinct nodes)");
+        return -1;
+    }
+    if ((n_probe_nodes && !d_probe_nodes) || (n_probe_edges && !d_probe_edges) ||
+        ((n_probe_nodes || n_probe_edges) && !d_probes) || n_probe_nodes + n_probe_edges > (1u << 20)) {
+        set_error("transient: probe arrays missing");
+        return -1;
+    }
+    LightningArgs src{K, alpha, beta, delay, (int)strike_node, (int)return_node};
+    return run_lightning(*S, src, (long long)step0, (long long)n_steps, d_I, d_V, d_probe_nodes, (int)n_probe_nodes,
+                         d_probe_edges, (int)n_probe_edges, d_probes);
+}
+
+void peec_gb300_transient_destroy(void *system) {
+    auto *S = static_cast<TransientSystem *>(system);
+    if (!S) return;
+    S->release();
+    sync("transient release");
+    delete S;
+}
+
+}  // extern "C"

@@ -149,3 +149,38 @@ def test_refused_requests(gpu_lib, meshes):
     with Server(GB, 1) as s:
         with pytest.raises(ValueError, match="invalid"):
             s.submit(meshes[0], 0, -1.0, [0, 0, 1], [1, 0, 0])
+
+
+def test_transient_requests_alone_and_in_the_mix(gpu_lib, meshes):
+    """Lightning runs through the server (the factorised transient system
+    cached per mesh, scheme and dt) equal a direct device run bit for bit,
+    alone and mixed with harmonic requests."""
+    from test_gpu_transient import DeviceTransient
+    from helpers import inductance, potential
+    m = meshes[0]
+    src = (102900.0, 1500.0, 1.0e6, 0.0, 3, 20)
+    pn, pe = [0, 3, 20], [1, 5]
+    s1, L = inductance(gpu_lib, m)
+    s2, P = potential(gpu_lib, m)
+    direct = DeviceTransient(gpu_lib, L, P, m.edges(), None, 2, 1e-7)
+    try:
+        assert direct.status == 0
+        s, I, V, probes = direct.run(src, 300, probe_nodes=pn, probe_edges=pe)
+        assert s == 0
+    finally:
+        direct.close()
+    with Server(8 * GB, 1) as srv:
+        (pa, Ia, Va), ra = srv.wait(srv.submit_transient(m, 0, 300, src, probe_nodes=pn, probe_edges=pe))
+    assert ra["status"] == 0 and ra["iterations"] == 300
+    assert np.array_equal(pa, probes) and np.array_equal(Ia, I) and np.array_equal(Va, V)
+    reqs = requests()[:6]
+    with Server(8 * GB, 4) as srv:
+        tt = [srv.submit_transient(m, 0, 300, src, probe_nodes=pn, probe_edges=pe) for _ in range(2)]
+        th = [srv.submit(meshes[r["mesh"]], r["mesh"], r["frequency"], r["k_hat"], r["e_hat"], mixed=r["mixed"])
+              for r in reqs]
+        outs = [srv.wait(t) for t in tt]
+        hs = [srv.wait(t) for t in th]
+    for (pb, Ib, Vb), rb in outs:
+        assert rb["status"] == 0
+        assert np.array_equal(pb, probes) and np.array_equal(Ib, I)
+    assert all(h[1]["status"] == 0 for h in hs)
