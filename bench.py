@@ -275,6 +275,96 @@ class DeviceSolve:
             self.lib.peec_gb300_device_free(p)
 
 
+def transient_leg(lib, ds, n_steps):
+    """Lightning transient on the same box (PEC, trapezoidal, dt 0.1 us): the
+    10/350 us 100 kA first stroke injected at a seeded top-face node and
+    returned at node 0, every step's right-hand side and solve on the device
+    with the factorised system resident.  CUDA-event timed."""
+    from peeeeeeeeeeeeeeeeeeec_gb300.workloads import LIGHTNING_10_350 as W
+    m = ds.m
+    xyz = m.array("xyz", (m.n_nodes, 3))
+    top = np.flatnonzero(xyz[:, 2] >= xyz[:, 2].max() - 1e-12)
+    strike = int(np.random.default_rng(3).choice(top))
+    h = C.c_void_p()
+    e0 = lib.peec_gb300_event_record()
+    s = lib.peec_gb300_transient_create(ds.dL, ds.dP, ds.dedges, None, ds.ne, ds.nv, 2, 1e-7, C.byref(h))
+    e1 = lib.peec_gb300_event_record()
+    lib.peec_gb300_synchronize()
+    assert s == 0, "transient system failed"
+    create_ms = lib.peec_gb300_event_elapsed_ms(e0, e1)
+    al = lib.peec_gb300_device_alloc
+    dI, dV = al(ds.ne * 8), al(ds.nv * 8)
+    probes = np.array([strike, 0], dtype=np.int32)
+    dpn, dpr = al(8), al(n_steps * 2 * 8)
+    lib.peec_gb300_copy_to_device(dpn, probes.ctypes.data, probes.nbytes)
+    out = {}
+    for rep in range(2):  # the first run warms the pools
+        z = np.zeros(max(ds.ne, ds.nv))
+        lib.peec_gb300_copy_to_device(dI, z.ctypes.data, ds.ne * 8)
+        lib.peec_gb300_copy_to_device(dV, z.ctypes.data, ds.nv * 8)
+        steps = n_steps if rep else 16
+        l0 = lib.peec_gb300_launch_count()
+        e0 = lib.peec_gb300_event_record()
+        s = lib.peec_gb300_transient_lightning(h, W["K"], W["alpha"], W["beta"], W["delay"], strike, 0, 0, steps,
+                                               dI, dV, dpn, 2, None, 0, dpr)
+        e1 = lib.peec_gb300_event_record()
+        lib.peec_gb300_synchronize()
+        assert s == 0, "transient run failed"
+        ms = lib.peec_gb300_event_elapsed_ms(e0, e1)
+        out = {"value": steps / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / steps, "steps": steps,
+               "system_create_ms": create_ms, "gpu_launches": int(lib.peec_gb300_launch_count() - l0),
+               "scheme": "trapezoidal", "dt_s": 1e-7, "strike_node": strike, "return_node": 0,
+               "source": "10/350 us, 100 kA: K %.6g A, alpha %.6g 1/s, beta %.6g 1/s" % (W["K"], W["alpha"],
+                                                                                     W["beta"])}
+    V = np.zeros((n_steps, 2))
+    lib.peec_gb300_copy_to_host(V.ctypes.data, dpr, V.nbytes)
+    out["peak_strike_node_self_voltage_V"] = float(np.max(np.abs(V[:, 0])))
+    lib.peec_gb300_transient_destroy(h)
+    for p in (dI, dV, dpn, dpr):
+        lib.peec_gb300_device_free(p)
+    return out
+
+
+def serving_leg(lib, window_s, workers):
+    """Poisson arrivals at 200 requests/s over window_s of harmonic requests
+    (seeded boxes / plates of 500-12000 unknowns, 1-100 MHz, 1-64 plane
+    waves), replayed once with the mixed-precision solve and once with the
+    plain FP64 LU through one server (150 GB budget) whose Lp / P cache was
+    warmed first.  Latency = completion - submission on the server clock."""
+    from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
+    from peeeeeeeeeeeeeeeeeeec_gb300.server import Server
+    pool = W.serving_meshes(seed=5, count=6)
+    reqs = W.harmonic_requests(seed=7, n_meshes=len(pool), rate_hz=200.0, window_s=window_s)
+    out = {"arrivals": "Poisson 200/s over %.2f s: %d requests" % (window_s, len(reqs)),
+           "meshes": ["%s, N=%d" % (d, m.n_edges + m.n_nodes) for m, d in pool], "workers": workers,
+           "hbm_budget_gb": 150}
+    with Server(150 << 30, workers) as srv:
+        warm = [srv.submit(m, i, 30e6, [[0.0, 0.0, -1.0]], [[1.0, 0.0, 0.0]], mixed=True)
+                for i, (m, _) in enumerate(pool)]
+        for t in warm:
+            srv.wait(t)
+        for mode in ("mixed", "plain"):
+            t0 = time.perf_counter()
+            tickets = []
+            for (ta, mi, f, k, e) in reqs:
+                d = t0 + ta - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                tickets.append(srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed")))
+            res = [srv.wait(t)[1] for t in tickets]
+            lat = np.array([r["t_end"] - r["t_submit"] for r in res])
+            span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
+            ok = sum(1 for r in res if r["status"] == 0 and r["backward_error"] <= 1e-10)
+            out[mode] = {"value": ok / span, "unit": "solves/s", "completed_at_gate": ok, "requests": len(res),
+                         "p50_latency_s": float(np.percentile(lat, 50)),
+                         "p99_latency_s": float(np.percentile(lat, 99)), "makespan_s": span,
+                         "max_backward_error": max(r["backward_error"] for r in res)}
+    out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
+    for m, _ in pool:
+        m.close()
+    return out
+
+
 def drop_in_solve(lib, m, b_host, edges):
     from peeeeeeeeeeeeeeeeeeec_gb300 import abi
     lo = abi.InductanceOptions()
@@ -394,6 +484,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--box", default=None, help="lx,ly,lz,nx,ny,nz (default: the 5 cm box)")
+    ap.add_argument("--transient-steps", type=int, default=4096)
+    ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
     if args.box:
         set_box(args.box)
@@ -479,7 +572,9 @@ def main():
                  "update_flops": lu_t[3].value}
     p64, p32 = C.c_double(), C.c_double()
     lib.peec_gb300_pipe_peaks(C.byref(p64), C.byref(p32))
+    transient = transient_leg(lib, ds, args.transient_steps) if args.transient_steps > 0 else None
     ds.free()
+    serving = serving_leg(lib, args.serve_window, args.serve_workers) if args.serve_window > 0 else None
 
     # end to end through the drop-in ABI, host buffers
     e2e = None
@@ -528,7 +623,7 @@ def main():
                            "retardation": "none (quasi-static, as the reference)"},
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-                "lu_phases": lu_phases, "mixed": mixed,
+                "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "transient": transient,
                 "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
                                       "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
                 "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}
