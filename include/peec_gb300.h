@@ -232,6 +232,9 @@ typedef struct
 {
     int status;            /* 0 solved, 1 mixed refinement did not converge, -2 singular, -1 error */
     int iterations;        /* mixed refinement iterations (0 for plain)     */
+    int fallback;          /* 1: the mixed solve did not reach the tolerance
+                              (or met a singular FP32 pivot) and the request
+                              was solved again by the plain FP64 LU          */
     double backward_error; /* componentwise, over all right-hand sides      */
     double t_submit, t_start, t_end; /* seconds on the server's clock       */
 } PeecRequestResult;

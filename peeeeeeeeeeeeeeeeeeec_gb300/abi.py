@@ -180,7 +180,7 @@ class PeecTransientRequest(C.Structure):
 
 
 class PeecRequestResult(C.Structure):
-    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("backward_error", C.c_double),
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("fallback", C.c_int), ("backward_error", C.c_double),
                 ("t_submit", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double)]
 
 

@@ -465,7 +465,7 @@ __global__ void k_laswp(T *a, int n, int k0, int kb, const long long *piv, const
 
 // ---- U12 = L11^-1 A12 ------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, const Status *st) {
+__global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, int c0, int c1, const Status *st) {
     __shared__ T L[NB][NB];
     if (st->code != 0) return;
     for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
@@ -473,8 +473,8 @@ __global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, const
         L[i][m] = a[(size_t)(k0 + i) * n + k0 + m];
     }
     __syncthreads();
-    int j = k0 + kb + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+    int j = c0 + blockIdx.x * blockDim.x + threadIdx.x;  // columns c0 .. c1-1 (all right of the panel)
+    if (j >= c1) return;
     T x[NB];
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
@@ -1053,8 +1053,8 @@ __global__ void __launch_bounds__(256) k_trsv_wave(WaveArgs<T> A) {
 }
 
 template <class T>
-static constexpr int wave_nr() {
-    return std::is_same<T, double>::value ? 4 : 2;
+static constexpr int wave_nr() {  // right-hand sides per wave: 8-byte scalars 4, FP64 complex 2
+    return sizeof(T) == 8 ? 4 : 2;
 }
 
 // Flag words of one wavefront solve of n unknowns and nrhs right-hand sides.
@@ -1277,28 +1277,41 @@ struct PanelScratch {
 // launches of every block column, summed at the end of the factorisation.
 struct LuTiming {
     bool enabled = false;
-    double ms[3] = {0, 0, 0};        // panel, swaps + trsm, trailing update
-    double flops_update = 0.0;       // algorithmic flops of the trailing updates
+    double ms[3] = {0, 0, 0};   // panel, swaps + trsm (+ splits), trailing update
+    double flops_update = 0.0;  // flops of the trailing updates (algorithmic, or issued BF16 for the mixed path)
     std::vector<cudaEvent_t> ev;
+    std::vector<int> cat;       // category of the interval that ends at each event (-1: none)
+    void reset() {
+        for (auto e : ev) cudaEventDestroy(e);
+        ev.clear();
+        cat.clear();
+        ms[0] = ms[1] = ms[2] = 0.0;
+        flops_update = 0.0;
+    }
+    void mark(int c) {
+        if (!enabled) return;
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, stream());
+        ev.push_back(e);
+        cat.push_back(c);
+    }
+    void finish() {
+        if (!enabled || ev.empty()) return;
+        cudaEventSynchronize(ev.back());
+        for (size_t i = 1; i < ev.size(); ++i) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[i - 1], ev[i]);
+            if (cat[i] >= 0) ms[cat[i]] += t;
+        }
+    }
 };
 static thread_local LuTiming g_lu_timing;  // per host thread, like the stream
-
-static void lu_mark(std::vector<cudaEvent_t> &ev) {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    cudaEventRecord(e, stream());
-    ev.push_back(e);
-}
 
 template <class T>
 static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status *d_st) {
     LuTiming &tm = g_lu_timing;
-    if (tm.enabled) {
-        for (auto e : tm.ev) cudaEventDestroy(e);
-        tm.ev.clear();
-        tm.ms[0] = tm.ms[1] = tm.ms[2] = 0.0;
-        tm.flops_update = 0.0;
-    }
+    if (tm.enabled) tm.reset();
     DBuf<unsigned char> scratch;
     PanelScratch sc;
     {
@@ -1320,7 +1333,7 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
     }
     for (int k0 = 0; k0 < n; k0 += NB) {
         int kb = std::min(NB, n - k0);
-        if (tm.enabled) lu_mark(tm.ev);
+        tm.mark(2);
         CoopPlan<T> pl = coop_plan<T>(n - k0);
         if (pl.G > 0) {
             int rows = pl.rows;
@@ -1335,16 +1348,14 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
         } else {
             PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
         }
-        if (tm.enabled) lu_mark(tm.ev);
+        tm.mark(0);
         PEEC_LAUNCH(k_laswp<T>, (n + 255) / 256, 256, 0, d_a, n, k0, kb, d_piv, d_st);
         int rest = n - (k0 + kb);
         if (rest > 0) {
-            PEEC_LAUNCH(k_trsm<T>, (rest + 255) / 256, 256, 0, d_a, n, k0, kb, d_st);
+            PEEC_LAUNCH(k_trsm<T>, (rest + 255) / 256, 256, 0, d_a, n, k0, kb, k0 + kb, n, d_st);
         }
-        if (tm.enabled) {
-            lu_mark(tm.ev);
-            tm.flops_update += (sizeof(T) == sizeof(double) ? 2.0 : 8.0) * (double)rest * rest * kb;
-        }
+        tm.mark(1);
+        if (tm.enabled) tm.flops_update += (sizeof(T) == sizeof(double) ? 2.0 : 8.0) * (double)rest * rest * kb;
         if (rest > 0) {
             if constexpr (sizeof(T) == sizeof(double)) {
                 dim3 g((rest + 63) / 64, (rest + 63) / 64);
@@ -1352,12 +1363,9 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
             } else {
                 dim3 g((rest + 63) / 64, (rest + 31) / 32);
                 if (complex_gemm_3m()) {
-                    static bool attr = false;
-                    if (!attr) {
-                        cudaFuncSetAttribute(k_gemm_cplx3m, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kGemm3mSmem);
-                        attr = true;
-                    }
+                    static const cudaError_t attr = cudaFuncSetAttribute(
+                        k_gemm_cplx3m, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemm3mSmem);
+                    (void)attr;
                     PEEC_LAUNCH(k_gemm_cplx3m, g, 256, kGemm3mSmem, (cplx *)d_a, n, k0, kb, d_st);
                 } else {
                     PEEC_LAUNCH(k_gemm_cplx, g, 256, 0, (cplx *)d_a, n, k0, kb, d_st);
@@ -1365,15 +1373,8 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
             }
         }
     }
-    if (tm.enabled) {
-        lu_mark(tm.ev);
-        cudaEventSynchronize(tm.ev.back());
-        for (size_t i = 0; i + 1 < tm.ev.size(); ++i) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
-            tm.ms[i % 3] += ms;
-        }
-    }
+    tm.mark(2);
+    tm.finish();
     PEEC_LAUNCH(k_check_diag<T>, (n + 255) / 256, 256, 0, d_a, n, limit, d_st);
     return launch_ok("LU kernels");
 }
@@ -1956,7 +1957,7 @@ extern "C" int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double
         PEEC_LAUNCH(k_laswp<double>, (ni + 255) / 256, 256, 0, d_a, ni, k0, kb, d_piv, st);
         int rest = ni - (k0 + kb);
         if (rest > 0) {
-            PEEC_LAUNCH(k_trsm<double>, (rest + 255) / 256, 256, 0, d_a, ni, k0, kb, st);
+            PEEC_LAUNCH(k_trsm<double>, (rest + 255) / 256, 256, 0, d_a, ni, k0, kb, k0 + kb, ni, st);
             dim3 g((rest + 63) / 64, (rest + 63) / 64);
             PEEC_LAUNCH(k_gemm_real, g, 256, 0, d_a, ni, k0, kb, st);
         }
@@ -2076,46 +2077,51 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &h, __nv_bfloa
     l = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
-// A' rows r = 0..m-1 <- L21 row k0+kb+r, columns k0..k0+kb-1 (zero-padded to NB)
-__global__ void k_split_a(const cplxf *a, int n, int k0, int kb, int m, __nv_bfloat16 *out) {
+// Split-BF16x3 operands of one complex trailing update C -= L U, K = 6 KW:
+// A' row r (0..m-1) <- L[row0 + r][col0 .. col0+kw-1] (zero-padded to KW) as
+// the planes [re_h | re_h | re_l | im_h | im_h | im_l], KW wide each.
+__global__ void k_split_a(const cplxf *a, int n, int row0, int m, int col0, int kw, int KW, __nv_bfloat16 *out) {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)m * NB) return;
-    int r = (int)(t / NB), c = (int)(t % NB);
-    cplxf x = c < kb ? a[(size_t)(k0 + kb + r) * n + k0 + c] : cplxf{0.0f, 0.0f};
+    if (t >= (long long)m * KW) return;
+    int r = (int)(t / KW), c = (int)(t % KW);
+    cplxf x = c < kw ? a[(size_t)(row0 + r) * n + col0 + c] : cplxf{0.0f, 0.0f};
     __nv_bfloat16 rh, rl, ih, il;
     split_bf16(x.re, rh, rl);
     split_bf16(x.im, ih, il);
-    __nv_bfloat16 *row = out + (size_t)r * 6 * NB;
+    __nv_bfloat16 *row = out + (size_t)r * 6 * KW;
     row[c] = rh;
-    row[NB + c] = rh;
-    row[2 * NB + c] = rl;
-    row[3 * NB + c] = ih;
-    row[4 * NB + c] = ih;
-    row[5 * NB + c] = il;
+    row[KW + c] = rh;
+    row[2 * KW + c] = rl;
+    row[3 * KW + c] = ih;
+    row[4 * KW + c] = ih;
+    row[5 * KW + c] = il;
 }
 
-// Br', Bi' rows j = 0..nc-1 <- U12 column k0+kb+j, rows k0..k0+kb-1
-__global__ void k_split_b(const cplxf *a, int n, int k0, int kb, int nc, __nv_bfloat16 *br, __nv_bfloat16 *bi) {
+// Br', Bi' row j (0..nc-1) <- U[row0 .. row0+kw-1][col0 + j]:
+// Br' = [re_h | re_l | re_h | -im_h | -im_l | -im_h], Bi' = [im_h | im_l | im_h | re_h | re_l | re_h],
+// so that A' Br' = Re(L U) and A' Bi' = Im(L U) to FP32 accuracy.
+__global__ void k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int col0, int nc, __nv_bfloat16 *br,
+                          __nv_bfloat16 *bi) {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)nc * NB) return;
+    if (t >= (long long)nc * KW) return;
     int c = (int)(t / nc), j = (int)(t % nc);  // consecutive threads read consecutive columns
-    cplxf x = c < kb ? a[(size_t)(k0 + c) * n + k0 + kb + j] : cplxf{0.0f, 0.0f};
+    cplxf x = c < kw ? a[(size_t)(row0 + c) * n + col0 + j] : cplxf{0.0f, 0.0f};
     __nv_bfloat16 rh, rl, ih, il;
     split_bf16(x.re, rh, rl);
     split_bf16(x.im, ih, il);
-    __nv_bfloat16 *r = br + (size_t)j * 6 * NB, *q = bi + (size_t)j * 6 * NB;
+    __nv_bfloat16 *r = br + (size_t)j * 6 * KW, *q = bi + (size_t)j * 6 * KW;
     r[c] = rh;
-    r[NB + c] = rl;
-    r[2 * NB + c] = rh;
-    r[3 * NB + c] = __hneg(ih);
-    r[4 * NB + c] = __hneg(il);
-    r[5 * NB + c] = __hneg(ih);
+    r[KW + c] = rl;
+    r[2 * KW + c] = rh;
+    r[3 * KW + c] = __hneg(ih);
+    r[4 * KW + c] = __hneg(il);
+    r[5 * KW + c] = __hneg(ih);
     q[c] = ih;
-    q[NB + c] = il;
-    q[2 * NB + c] = ih;
-    q[3 * NB + c] = rh;
-    q[4 * NB + c] = rl;
-    q[5 * NB + c] = rh;
+    q[KW + c] = il;
+    q[2 * KW + c] = ih;
+    q[3 * KW + c] = rh;
+    q[4 * KW + c] = rl;
+    q[5 * KW + c] = rh;
 }
 
 // y = P D_r^-1 r in FP32 (the permuted, row-scaled residual)
@@ -2217,7 +2223,10 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     DBuf<int> perm(n), err(1);
     DBuf<Status> st(1);
     DBuf<unsigned long long> mx(1), be(1);
-    DBuf<__nv_bfloat16> ap((size_t)n * 6 * NB), bpr((size_t)n * 6 * NB), bpi((size_t)n * 6 * NB);
+    // two-level blocking: 32-column panels inside 256-column outer blocks, so
+    // the bulk of the trailing update runs with K = 6 x 256 on the tensor cores
+    const int OB = 256;
+    DBuf<__nv_bfloat16> ap((size_t)n * 6 * OB), bpr((size_t)n * 6 * OB), bpi((size_t)n * 6 * OB);
     DBuf<unsigned char> scratch;
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -2263,57 +2272,62 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     // FP32 factorisation, trailing updates on the tensor cores
     cplxf *a = f.p;
     LuTiming &tm = g_lu_timing;
-    if (tm.enabled) {
-        for (auto e : tm.ev) cudaEventDestroy(e);
-        tm.ev.clear();
-        tm.ms[0] = tm.ms[1] = tm.ms[2] = 0.0;
-        tm.flops_update = 0.0;
+    if (tm.enabled) tm.reset();
+    // C[row0.., col0..] -= L[row0.., kc..kc+kw) U[kc..kc+kw, col0..), split-BF16x3
+    auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw) -> bool {
+        if (m <= 0 || nc <= 0) return true;
+        const int KW = (kw + 31) / 32 * 32;
+        PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
+        PEEC_LAUNCH(k_split_b, (unsigned)(((long long)nc * KW + 255) / 256), 256, 0, a, n, kc, kw, KW, col0, nc,
+                    bpr.p, bpi.p);
+        if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
+        return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
+    };
+    for (int K0 = 0; K0 < n; K0 += OB) {
+        const int E = std::min(n, K0 + OB);  // the outer block is columns [K0, E)
+        for (int k0 = K0; k0 < E; k0 += NB) {
+            const int kb = std::min(NB, E - k0);
+            tm.mark(2);
+            CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
+            if (pl.G > 0) {
+                int rows = pl.rows;
+                cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
+                Status *stp = st.p;
+                long long *pivp = piv.p;
+                int kbv = kb;
+                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, &rows, (void *)&limit, &pivp, &stp, &sc.ps,
+                                &sc.cand_val, &sc.cand_idx, &cr, &kr};
+                if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<cplxf>, dim3(pl.G), dim3(256),
+                                                         args, pl.smem, stream()),
+                             "cooperative panel launch"))
+                    return -1;
+                note_launch();
+            } else {
+                PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
+            }
+            tm.mark(0);
+            PEEC_LAUNCH(k_laswp<cplxf>, (n + 255) / 256, 256, 0, a, n, k0, kb, piv.p, st.p);
+            // the rest of the outer block's columns: U12 rows, then the narrow update
+            const int rin = E - (k0 + kb);
+            if (rin > 0) PEEC_LAUNCH(k_trsm<cplxf>, (rin + 255) / 256, 256, 0, a, n, k0, kb, k0 + kb, E, st.p);
+            tm.mark(1);
+            if (!tc_update(k0 + kb, n - (k0 + kb), k0 + kb, rin, k0, kb)) return -1;
+        }
+        if (E < n) {
+            // U12 of the outer block for the columns right of it, block by block
+            for (int k0 = K0; k0 < E; k0 += NB) {
+                const int kb = std::min(NB, E - k0);
+                PEEC_LAUNCH(k_trsm<cplxf>, (n - E + 255) / 256, 256, 0, a, n, k0, kb, E, n, st.p);
+                tm.mark(1);
+                if (!tc_update(k0 + kb, E - (k0 + kb), E, n - E, k0, kb)) return -1;
+                tm.mark(2);
+            }
+            // trailing update with K = 6 x (E - K0)
+            if (!tc_update(E, n - E, E, n - E, K0, E - K0)) return -1;
+        }
     }
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        int kb = std::min(NB, n - k0);
-        if (tm.enabled) lu_mark(tm.ev);
-        CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
-        if (pl.G > 0) {
-            int rows = pl.rows;
-            cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
-            Status *stp = st.p;
-            long long *pivp = piv.p;
-            void *args[] = {&a, (void *)&n, (void *)&k0, &kb, &rows, (void *)&limit, &pivp, &stp, &sc.ps,
-                            &sc.cand_val, &sc.cand_idx, &cr, &kr};
-            if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<cplxf>, dim3(pl.G), dim3(256), args,
-                                                     pl.smem, stream()),
-                         "cooperative panel launch"))
-                return -1;
-            note_launch();
-        } else {
-            PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
-        }
-        if (tm.enabled) lu_mark(tm.ev);
-        PEEC_LAUNCH(k_laswp<cplxf>, (n + 255) / 256, 256, 0, a, n, k0, kb, piv.p, st.p);
-        int rest = n - (k0 + kb);
-        if (rest > 0) {
-            PEEC_LAUNCH(k_trsm<cplxf>, (rest + 255) / 256, 256, 0, a, n, k0, kb, st.p);
-            PEEC_LAUNCH(k_split_a, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, ap.p);
-            PEEC_LAUNCH(k_split_b, (unsigned)(((long long)rest * NB + 255) / 256), 256, 0, a, n, k0, kb, rest, bpr.p,
-                        bpi.p);
-        }
-        if (tm.enabled) {
-            lu_mark(tm.ev);
-            tm.flops_update += 2.0 * 2.0 * (double)rest * rest * (6 * NB);  // issued BF16 tensor flops
-        }
-        if (rest > 0 &&
-            !tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, rest, rest, 6 * NB, k0 + kb, k0 + kb, n, err.p))
-            return -1;
-    }
-    if (tm.enabled) {
-        lu_mark(tm.ev);
-        cudaEventSynchronize(tm.ev.back());
-        for (size_t i = 0; i + 1 < tm.ev.size(); ++i) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, tm.ev[i], tm.ev[i + 1]);
-            tm.ms[i % 3] += ms;
-        }
-    }
+    tm.mark(2);
+    tm.finish();
     PEEC_LAUNCH(k_check_diag<cplxf>, (n + 255) / 256, 256, 0, a, n, limit, st.p);
     size_t perm_smem = n_ * sizeof(int);
     if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);

@@ -107,8 +107,10 @@ class Server {
         j->e_hat.assign(r->e_hat, r->e_hat + 3 * r->nrhs);
         size_t ne = r->mesh->n_edges, nv = r->mesh->n_nodes, n = ne + nv;
         j->mesh_bytes = mesh_bytes(ne, nv);
-        // Z + working copy (FP32 LU + FP32 |Z| for mixed, FP64 LU for plain) + vectors + scratch
-        j->bytes = 16 * n * n + (r->mixed ? 12 * n * n + 6 * n * 192 : 16 * n * n) + 96 * n * r->nrhs + (64 << 20);
+        // Z + working copy (mixed: FP32 LU + FP32 |Z| + BF16 splits, or the
+        // FP64 LU of a fallback, whichever is larger; plain: FP64 LU) +
+        // vectors + scratch
+        j->bytes = 32 * n * n + (r->mixed ? 9216 * n : 0) + 96 * n * r->nrhs + (64 << 20);
         return enqueue(j);
     }
 
@@ -348,7 +350,11 @@ class Server {
         if (r.mixed) {
             double tol = r.tolerance > 0.0 ? r.tolerance : 1e-10;
             status = peec_gb300_complex_solve_mixed_device(Z.p, n, B.p, X.p, nrhs, tol, 30, &be, &iters);
-        } else {
+            // refinement that stalls (ill-conditioned systems, e.g. very low
+            // frequencies) or an FP32 pivot breakdown: solve again in FP64
+            if (status == 1 || status == -2) j.res.fallback = 1;
+        }
+        if (!r.mixed || j.res.fallback) {
             DBuf<long long> piv(n);
             DBuf<int> perm(n);
             DBuf<double> rs(n), cs(n);

@@ -70,7 +70,7 @@ class Server:
         if self.lib.peec_gb300_server_wait(self.handle, ticket, C.byref(r)) != 0:
             raise KeyError(ticket)
         x = self._pending.pop(ticket)[0]
-        return x, {"status": r.status, "iterations": r.iterations,
+        return x, {"status": r.status, "iterations": r.iterations, "fallback": r.fallback,
                    "backward_error": r.backward_error, "t_submit": r.t_submit,
                    "t_start": r.t_start, "t_end": r.t_end}
 
