@@ -175,6 +175,27 @@ int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
 int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x,
                                      const Complex *d_b, size_t nrhs, double out[3]);
 
+/* ---- retarded Lp / P (no reference counterpart: the reference's
+ * retardation.c is empty) ----
+ * Lp and P with the kernel exp(-jkR)/R, k = wave_number (rad/m, >= 0),
+ * n x n complex in device memory.  Each patch-pair integral is the static
+ * one of peec_gb300_inductance_device / _potential_device (exact near field,
+ * FP64) plus the integral of (exp(-jkR) - 1)/R -- smooth and bounded -- by
+ * the far product rule over every patch pair, evaluated on the FP32 pipes
+ * (~1e-6 relative error on that correction).  k = 0 gives the static
+ * matrices exactly, with zero imaginary parts. */
+int peec_gb300_inductance_retarded_device(const Mesh *mesh, const DualMesh *dual,
+                                          const InductanceOptions *options, double wave_number,
+                                          Complex *d_out, PeecAssemblyStats *stats);
+int peec_gb300_potential_retarded_device(const Mesh *mesh, const DualMesh *dual,
+                                         const PotentialOptions *options, double wave_number,
+                                         Complex *d_out, PeecAssemblyStats *stats);
+/* Z of peec_gb300_harmonic_build_device from complex Lp and P. */
+int peec_gb300_harmonic_build_retarded_device(const Complex *d_L, const Complex *d_P,
+                                              const int *d_edges, const double *d_R,
+                                              size_t n_edges, size_t n_nodes, double frequency,
+                                              Complex *d_Z);
+
 /* ---- stage-1 transient (lightning) on the device ----
  * The reference's transient_system_create_stage1 + transient_factorize
  * (transient.c:385-480, 1020-1110, 2014-2066): M = [L/dt + theta R,

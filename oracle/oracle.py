@@ -56,6 +56,9 @@ class Oracle:
             ("oracle_complex_lu_factorize", C.c_int,
              [D, C.c_size_t, C.c_double, C.c_int, D, S, S, D, D, D]),
             ("oracle_complex_lu_solve", C.c_int, [D, S, D, D, C.c_size_t, D, D]),
+            ("oracle_retarded_matrix", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), C.c_int, P(C.c_int), C.c_double, C.c_double, C.c_double,
+              C.c_int, D]),
             ("oracle_transient_stage1_matrix", C.c_int,
              [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, D, D, D]),
             ("oracle_transient_rhs_stage1", C.c_int,
@@ -147,6 +150,16 @@ class Oracle:
         s = self.lib.oracle_complex_lu_solve(lu.ctypes.data_as(D), piv.ctypes.data_as(S), _dp(rs), _dp(cs),
                                              lu.shape[0], b.ctypes.data_as(D), x.ctypes.data_as(D))
         return s, x
+
+    def retarded(self, m, kind, wave_number, orders=(4, 10, 12, 8), near_factor=0.5, tol=1e-10,
+                 threads=None):
+        """kind 0: Lp, 1: P with the exp(-jkR)/R kernel (complex n x n)."""
+        n = m.n_edges if kind == 0 else m.n_nodes
+        out = np.zeros((n, n), dtype=np.complex128)
+        s = self.lib.oracle_retarded_matrix(C.byref(m.mesh), C.byref(m.dual), kind, self._orders(orders),
+                                            near_factor, tol, wave_number, threads or os.cpu_count(),
+                                            out.ctypes.data_as(D))
+        return s, out
 
     def transient_matrix(self, L, P_, edges, R, scheme, dt):
         ne, nv = L.shape[0], P_.shape[0]

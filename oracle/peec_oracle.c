@@ -881,3 +881,121 @@ done:
     free(piv);
     return status;
 }
+
+
+/* ===================================================================== */
+/* retarded kernel (extension; the reference's retardation.c is empty)    */
+/* ===================================================================== */
+
+/* far-rule points of a patch: triangles (0,1,2), (0,2,3), order^2 mapped
+ * Gauss points each with weight w_u w_v J (quadrature.c:632-666) */
+static int patch_points(const QuadPatch *p, int order, double *pts /* [2 order^2][4] */)
+{
+    double x[16], w[16];
+    if (order <= 0 || order > 16 || oracle_gauss_legendre_rule(order, x, w) != 0) return -1;
+    double c[4][3];
+    for (int i = 0; i < 4; ++i) corner(p, i, c[i]);
+    int k = 0;
+    for (int t = 0; t < 2; ++t) {
+        const double *p0 = c[0], *p1 = c[t == 0 ? 1 : 2], *p2 = c[t == 0 ? 2 : 3];
+        for (int iu = 0; iu < order; ++iu)
+            for (int iv = 0; iv < order; ++iv, ++k) {
+                double u = 0.5 * (x[iu] + 1.0), wu = 0.5 * w[iu];
+                double v = 0.5 * (x[iv] + 1.0), wv = 0.5 * w[iv];
+                double r[3], jac;
+                tri_point(p0, p1, p2, u, v, r, &jac);
+                pts[4 * k + 0] = r[0];
+                pts[4 * k + 1] = r[1];
+                pts[4 * k + 2] = r[2];
+                pts[4 * k + 3] = wu * wv * jac;
+            }
+    }
+    return k;
+}
+
+/* sum over point pairs of w_a w_b (exp(-jkR) - 1) / R
+ * = w_a w_b (-2 sin^2(kR/2) - j sin kR) / R, limit -jk w_a w_b at R = 0 */
+static int retard_correction(const QuadPatch *a, const QuadPatch *b, int order, double k,
+                             double *re, double *im)
+{
+    double pa[2 * 16 * 16 * 4], pb[2 * 16 * 16 * 4];
+    int na = patch_points(a, order, pa), nb = patch_points(b, order, pb);
+    if (na < 0 || nb < 0) return -1;
+    double sr = 0.0, si = 0.0;
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j) {
+            double d[3] = {pa[4 * i] - pb[4 * j], pa[4 * i + 1] - pb[4 * j + 1], pa[4 * i + 2] - pb[4 * j + 2]};
+            double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            double ww = pa[4 * i + 3] * pb[4 * j + 3];
+            if (R <= 0.0) {
+                si += -k * ww;
+                continue;
+            }
+            double s = sin(0.5 * k * R), c = cos(0.5 * k * R);
+            sr += ww * (-2.0 * s * s) / R;
+            si += ww * (-2.0 * s * c) / R;
+        }
+    *re = sr;
+    *im = si;
+    return 0;
+}
+
+int oracle_retarded_matrix(const Mesh *mesh, const DualMesh *dual, int kind, const int orders[4],
+                           double near_factor, double direction_tolerance, double wave_number,
+                           int threads, double *out)
+{
+    if (!mesh || !dual || !orders || !out || threads < 1 || (kind != 0 && kind != 1) ||
+        !isfinite(wave_number) || wave_number < 0.0)
+        return -1;
+    size_t n = kind == 0 ? mesh->n_edges : mesh->n_nodes;
+    double *stat = malloc(n * n * sizeof(double));
+    if (!stat) return -1;
+    int s = kind == 0 ? oracle_inductance_matrix(mesh, dual, orders, near_factor, direction_tolerance,
+                                                 threads, stat)
+                      : oracle_potential_matrix(mesh, dual, orders, near_factor, threads, stat);
+    if (s != 0) {
+        free(stat);
+        return -1;
+    }
+    int failed = 0;
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+    for (long long as = 0; as < (long long)n; ++as) {
+        size_t a = (size_t)as;
+        for (size_t b = a; b < n; ++b) {
+            double scale, dre = 0.0, dim = 0.0;
+            const PatchList *ra, *rb;
+            if (kind == 0) {
+                double dot = v_dot(&mesh->edge_directions[3 * a], &mesh->edge_directions[3 * b]);
+                double wa = dual->edge_region_areas[a] / mesh->edge_lengths[a];
+                double wb = dual->edge_region_areas[b] / mesh->edge_lengths[b];
+                scale = fabs(dot) < direction_tolerance ? 0.0 : MU0_OVER_4PI * dot / (wa * wb);
+                ra = &dual->edge_patches[a];
+                rb = &dual->edge_patches[b];
+            } else {
+                scale = INV_4PI_EPS0 / (dual->node_region_areas[a] * dual->node_region_areas[b]);
+                ra = &dual->node_patches[a];
+                rb = &dual->node_patches[b];
+            }
+            if (scale != 0.0 && wave_number != 0.0) {
+                for (size_t i = 0; i < ra->count; ++i)
+                    for (size_t j = 0; j < rb->count; ++j) {
+                        double r, m;
+                        if (retard_correction(&ra->patches[i], &rb->patches[j], orders[0], wave_number,
+                                              &r, &m) != 0) {
+#pragma omp atomic write
+                            failed = 1;
+                        }
+                        dre += r;
+                        dim += m;
+                    }
+            }
+            double vr = stat[a * n + b] + scale * dre, vi = scale * dim;
+            out[2 * (a * n + b)] = vr;
+            out[2 * (a * n + b) + 1] = vi;
+            out[2 * (b * n + a)] = vr;
+            out[2 * (b * n + a) + 1] = vi;
+        }
+    }
+    free(stat);
+    return failed ? -1 : 0;
+}

@@ -107,6 +107,18 @@ int oracle_transient_lightning(const double *L, const double *P, const int *edge
                                size_t n_probe_nodes, const int *probe_edges,
                                size_t n_probe_edges, double *probe_out);
 
+/* ---- retarded kernel exp(-jkR)/R (no reference counterpart) ----
+ * K_k = K_0 + D_k: K_0 the static patch-pair integral above (exact near
+ * field), D_k the integral of (exp(-jkR) - 1)/R, smooth and bounded (limit
+ * -jk at R = 0), by the far product rule of order far_order over both
+ * patches' triangles for every patch pair.  Entries are scaled as Lp
+ * (kind 0, zero for orthogonal edges) or P (kind 1).  out: n x n complex,
+ * interleaved.  Parity unpinned: the reference has no retarded kernel; at
+ * k = 0 this is the static matrix exactly. */
+int oracle_retarded_matrix(const Mesh *mesh, const DualMesh *dual, int kind, const int orders[4],
+                           double near_factor, double direction_tolerance, double wave_number,
+                           int threads, double *out);
+
 #ifdef __cplusplus
 }
 #endif

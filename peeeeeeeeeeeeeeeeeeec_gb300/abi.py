@@ -237,6 +237,12 @@ EXT_SYMBOLS = [
       C.c_void_p]),
     ("peec_gb300_backward_error_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, c_double_p]),
+    ("peec_gb300_inductance_retarded_device", C.c_int,
+     [P(Mesh), P(DualMesh), P(InductanceOptions), C.c_double, C.c_void_p, P(PeecAssemblyStats)]),
+    ("peec_gb300_potential_retarded_device", C.c_int,
+     [P(Mesh), P(DualMesh), P(PotentialOptions), C.c_double, C.c_void_p, P(PeecAssemblyStats)]),
+    ("peec_gb300_harmonic_build_retarded_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_double, C.c_void_p]),
     ("peec_gb300_transient_create", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_int, C.c_double,
       P(C.c_void_p)]),

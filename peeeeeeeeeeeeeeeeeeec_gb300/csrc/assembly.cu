@@ -1350,6 +1350,136 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     return 0;
 }
 
+// ---------------------------------------------------------------------
+// 7. retarded kernel exp(-jkR)/R (extension; the reference has none)
+//
+// K_k = K_0 + D_k with K_0 the static integral of this pipeline (exact near
+// field, FP64) and D_k = integral of (exp(-jkR) - 1)/R, which is smooth and
+// bounded (limit -jk at R = 0), by the far product rule over every patch
+// pair, on the FP32 pipes: (exp(-jkR) - 1)/R = (-2 sin^2(kR/2) - j sin kR)/R
+// from one sincosf, per-lane FP32 sums combined in FP64.  D_k carries ~1e-6
+// relative FP32 error; at k = 0 the result is the static matrix exactly.
+// ---------------------------------------------------------------------
+struct Cplx {
+    double re, im;
+};
+
+struct RetardArgs {
+    RegionsDev R;
+    const FarPtF *ptf;
+    int npts, n, kind;
+    double dir_tol;
+    float k;
+    const double *stat;  // static matrix, n x n
+    Cplx *out;           // n x n complex
+};
+
+__device__ __forceinline__ void retard_pair(const FarPtF *pa, const FarPtF *pb, int npts, float k, double &re,
+                                            double &im) {
+    const int lane = threadIdx.x & 31;
+    for (int p = lane; p < npts; p += 32) {
+        FarPtF A = pa[p];
+        float sr = 0.0f, si = 0.0f;
+#pragma unroll 4
+        for (int q = 0; q < npts; ++q) {
+            FarPtF B = pb[q];
+            float dx = A.xh - B.xh, dy = A.yh - B.yh, dz = A.zh - B.zh;
+            float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (r2 > 0.0f) {
+                float inv = rsqrtf(r2), sn, cs;
+                sincosf(0.5f * k * (r2 * inv), &sn, &cs);
+                float wi = B.wh * inv;
+                sr = fmaf(wi, -2.0f * sn * sn, sr);
+                si = fmaf(wi, -2.0f * sn * cs, si);
+            } else {
+                si = fmaf(B.wh, -k, si);
+            }
+        }
+        re = fma((double)A.wh, (double)sr, re);
+        im = fma((double)A.wh, (double)si, im);
+    }
+}
+
+__global__ void __launch_bounds__(kTileWarps * 32) k_retard_tiles(RetardArgs T) {
+    __shared__ Cplx tile[kTile][kTile + 1];
+    const int ta = blockIdx.y, tb = blockIdx.x;
+    if (tb < ta) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const RegionsDev &R = T.R;
+    const int n = T.n;
+    for (int e = warp; e < kTile * kTile; e += kTileWarps) {
+        int r = e / kTile, c = e % kTile;
+        int a = ta * kTile + r, b = tb * kTile + c;
+        Cplx val = {0.0, 0.0};
+        if (a < n && b < n && !(ta == tb && c < r)) {
+            double scale;
+            if (T.kind == KIND_INDUCTANCE) {
+                double dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
+                scale = fabs(dot) < T.dir_tol ? 0.0 : kMu0Over4Pi * dot / (R.scale[a] * R.scale[b]);
+            } else {
+                scale = kInv4PiEps0 / (R.scale[a] * R.scale[b]);
+            }
+            double dre = 0.0, dim = 0.0;
+            if (scale != 0.0 && T.k != 0.0f)
+                for (int i = R.off[a]; i < R.off[a + 1]; ++i)
+                    for (int j = R.off[b]; j < R.off[b + 1]; ++j)
+                        retard_pair(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, T.k, dre, dim);
+            dre = warp_sum(dre);
+            dim = warp_sum(dim);
+            val.re = T.stat[(size_t)a * n + b] + scale * dre;
+            val.im = scale * dim;
+        }
+        if (lane == 0) tile[r][c] = val;
+    }
+    __syncthreads();
+    const int rows = min(kTile, n - ta * kTile), cols = min(kTile, n - tb * kTile);
+    if (ta == tb) {
+        for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+            int r = e / kTile, c = e % kTile;
+            if (c < r) tile[r][c] = tile[c][r];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        int r = e / kTile, c = e % kTile;
+        if (r < rows && c < cols) T.out[(size_t)(ta * kTile + r) * n + tb * kTile + c] = tile[r][c];
+    }
+    if (ta != tb) {
+        for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+            int c = e / kTile, r = e % kTile;
+            if (r < rows && c < cols) T.out[(size_t)(tb * kTile + c) * n + ta * kTile + r] = tile[r][c];
+        }
+    }
+}
+
+static int assemble_retarded(const Mesh *mesh, const DualMesh *dual, int kind, const AssemblyOptions &o,
+                             double wave_number, Complex *d_out, PeecAssemblyStats *stats) {
+    if (!isfinite(wave_number) || wave_number < 0.0) {
+        set_error("retarded assembly: the wave number must be finite and >= 0");
+        return -1;
+    }
+    HostRegions H;
+    if (!gather_regions(mesh, dual, kind, H)) return -1;
+    DeviceRegions D;
+    if (!D.upload(H)) return -1;
+    const int n = H.n, q = o.orders[0], npts = 2 * q * q;
+    DBuf<double> stat((size_t)n * n);
+    if (!stat.p) return -1;
+    long long bad;
+    if (run_assembly(D, kind, o, stat.p, -1, -1, &bad, stats) != 0) return -1;
+    const RegionsDev &R = D.view;
+    DBuf<FarPt> pts((size_t)R.np * npts);
+    DBuf<FarPtF> ptf((size_t)R.np * npts);
+    if (R.np && (!pts.p || !ptf.p)) return -1;
+    long long tot = (long long)R.np * npts;
+    if (tot) PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p, ptf.p);
+    RetardArgs T{R, ptf.p, npts, n, kind, o.dir_tol, (float)wave_number, stat.p, reinterpret_cast<Cplx *>(d_out)};
+    int nt = (n + kTile - 1) / kTile;
+    PEEC_LAUNCH(k_retard_tiles, dim3(nt, nt), kTileWarps * 32, 0, T);
+    if (!launch_ok("retarded assembly") || !sync("retarded assembly")) return -1;
+    return 0;
+}
+
 // Counts the far-rule point evaluations of a matrix on the host from the
 // region sizes and the near list size (algorithmic work for the roofline).
 }  // namespace peec
@@ -1642,6 +1772,26 @@ int peec_gb300_potential_device(const Mesh *mesh, const DualMesh *dual, const Po
 }
 
 }  // extern "C"
+
+extern "C" int peec_gb300_inductance_retarded_device(const Mesh *mesh, const DualMesh *dual,
+                                                    const InductanceOptions *options, double wave_number,
+                                                    Complex *d_out, PeecAssemblyStats *stats) {
+    if (!mesh || !dual || !options || !d_out || mesh->n_edges == 0) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, options->direction_tolerance};
+    if (!orders_valid(o)) return -1;
+    return assemble_retarded(mesh, dual, KIND_INDUCTANCE, o, wave_number, d_out, stats);
+}
+
+extern "C" int peec_gb300_potential_retarded_device(const Mesh *mesh, const DualMesh *dual,
+                                                   const PotentialOptions *options, double wave_number,
+                                                   Complex *d_out, PeecAssemblyStats *stats) {
+    if (!mesh || !dual || !options || !d_out || mesh->n_nodes == 0) return -1;
+    AssemblyOptions o = {{options->far_order, options->near_order, options->touching_order, options->self_order},
+                         options->near_factor, 0.0};
+    if (!orders_valid(o)) return -1;
+    return assemble_retarded(mesh, dual, KIND_POTENTIAL, o, wave_number, d_out, stats);
+}
 
 // Select the far-rule arithmetic of later assemblies: 0 FP64, 1 double-float
 // (default, FP64-accurate), 2 FP32 (mixed-precision path).  Returns the

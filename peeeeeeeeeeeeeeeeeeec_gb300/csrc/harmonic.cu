@@ -52,6 +52,39 @@ __global__ void k_harmonic_fill(const double *L, const double *P, const int *edg
     }
 }
 
+// The same system from retarded (complex) Lp and P: j w (Lr + j Li) and
+// -(P A^T) with complex P.
+__global__ void k_harmonic_fill_complex(const cpx *L, const cpx *P, const int *edges, const double *R, int ne, int nv,
+                                        double omega, cpx *Z) {
+    const long long n = (long long)ne + nv;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n * n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t / n), j = (int)(t % n);
+        cpx z = {0.0, 0.0};
+        if (i < ne) {
+            if (j < ne) {
+                cpx l = L[(size_t)i * ne + j];
+                z.re = ((i == j && R) ? R[i] : 0.0) - omega * l.im;
+                z.im = omega * l.re;
+            } else {
+                int k = j - ne;
+                z.re = (k == edges[2 * i]) ? -1.0 : (k == edges[2 * i + 1]) ? 1.0 : 0.0;
+            }
+        } else {
+            int r = i - ne;
+            if (j < ne) {
+                int a = edges[2 * j], b = edges[2 * j + 1];
+                const cpx *prow = P + (size_t)r * nv;
+                z.re = -(prow[b].re - prow[a].re);
+                z.im = -(prow[b].im - prow[a].im);
+            } else if (j - ne == r) {
+                z.im = omega;
+            }
+        }
+        Z[t] = z;
+    }
+}
+
 // U_e for a unit plane wave E(r) = e_hat exp(-j k0 k_hat.r): field at the
 // edge centre projected on the edge vector, times sinc(q/2), q = k0 k_hat.l;
 // the right-hand side is [-U_e ; 0].
@@ -146,6 +179,21 @@ int peec_gb300_harmonic_build_device(const double *d_L, const double *d_P, const
     PEEC_LAUNCH(k_harmonic_fill, grid, 256, 0, d_L, d_P, d_edges, d_R, (int)n_edges, (int)n_nodes, omega,
                 (cpx *)d_Z);
     return launch_ok("harmonic fill") ? 0 : -1;
+}
+
+int peec_gb300_harmonic_build_retarded_device(const Complex *d_L, const Complex *d_P, const int *d_edges,
+                                              const double *d_R, size_t n_edges, size_t n_nodes, double frequency,
+                                              Complex *d_Z) {
+    if (!d_L || !d_P || !d_edges || !d_Z || n_edges == 0 || n_nodes == 0 || !isfinite(frequency) ||
+        frequency <= 0.0)
+        return -1;
+    double omega = 2.0 * M_PI * frequency;
+    long long n = (long long)(n_edges + n_nodes);
+    long long total = n * n;
+    int grid = (int)((total + 255) / 256 < 152LL * 32 ? (total + 255) / 256 : 152LL * 32);
+    PEEC_LAUNCH(k_harmonic_fill_complex, grid, 256, 0, (const cpx *)d_L, (const cpx *)d_P, d_edges, d_R,
+                (int)n_edges, (int)n_nodes, omega, (cpx *)d_Z);
+    return launch_ok("retarded harmonic fill") ? 0 : -1;
 }
 
 int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers, const double *d_edge_vectors, size_t n_edges,

@@ -257,3 +257,48 @@ def test_transient_against_reference_library(oracle):
     # same source node on both ends is refused (lightning.c:160-170)
     assert oracle.transient_lightning(f["L"], f["P"], f["edges"], Rd, 1, 1e-7,
                                       src[:4] + (3, 3), 5)[0] == -1
+
+
+# Retarded kernel exp(-jkR)/R: no reference implementation exists (the
+# reference's retardation.c is empty), so the restatement is checked against
+# its own limits: k = 0 is the static matrix bit for bit, first order in k is
+# -jk |S_a| |S_b| (the integral of -jk over both regions), and a far entry of
+# two small patches carries the phase exp(-jkd) of their distance.
+def test_retarded_oracle_limits(oracle):
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    with SynthMesh.plate(1.0, 1.0, 4, 4) as m:
+        sL, L0 = oracle.inductance(m)
+        sP, P0 = oracle.potential(m)
+        s, Lk = oracle.retarded(m, 0, 0.0)
+        assert s == 0 and np.array_equal(Lk.real, L0) and not Lk.imag.any()
+        s, Pk = oracle.retarded(m, 1, 0.0)
+        assert s == 0 and np.array_equal(Pk.real, P0) and not Pk.imag.any()
+        k = 1e-4
+        s, Pk = oracle.retarded(m, 1, k)
+        S = m.region_areas("node")
+        # P_ij = 1/(4 pi eps0) K / (S_i S_j): Im -> -k / (4 pi eps0)
+        assert np.allclose(Pk.imag, -k * 8.987551792261171e9, rtol=1e-6, atol=0)
+        assert np.max(np.abs(Pk.real - P0) / np.abs(P0)) < 1e-7  # second order in k
+        s, Lk = oracle.retarded(m, 0, k)
+        nz = L0 != 0
+        # Lp_ab = 1e-7 (e_a . e_b) K / (w_a w_b), w = S / l
+        d = m.edge_directions()
+        S = m.region_areas("edge")
+        w = S / m.edge_lengths()
+        expect = -k * 1e-7 * (d @ d.T) * np.outer(S, S) / np.outer(w, w)
+        assert np.allclose(Lk.imag[nz], expect[nz], rtol=1e-6, atol=0)
+        assert np.array_equal(Lk == 0, L0 == 0)
+    # two small plates 2 m apart: K_k / K_0 ~ exp(-j k d)
+    xyz = np.array([[0, 0, 0], [0.01, 0, 0], [0.01, 0.01, 0], [0, 0.01, 0],
+                    [2, 0, 0], [2.01, 0, 0], [2.01, 0.01, 0], [2, 0.01, 0]], dtype=float)
+    quads = np.array([[0, 1, 2, 3], [4, 5, 6, 7]], dtype=np.int32)
+    with SynthMesh.from_arrays(xyz, quads) as m:
+        s0, P0 = oracle.potential(m)
+        k = 1.7
+        s, Pk = oracle.retarded(m, 1, k)
+        # node regions of the two plates: entries between a node of each
+        i = 0
+        j = m.n_nodes - 1
+        ratio = Pk[i, j] / P0[i, j]
+        d = np.linalg.norm(m.array("xyz", (m.n_nodes, 3))[i] - m.array("xyz", (m.n_nodes, 3))[j])
+        assert abs(ratio - np.exp(-1j * k * d)) < 2e-2
