@@ -406,6 +406,38 @@ def serving_leg(lib, window_s, workers):
     return out
 
 
+def batched_leg(lib, n_meshes, n_freqs, workers):
+    """Many meshes x many frequencies (config-4 shape, scaled): seeded boxes /
+    plates of 300-4000 unknowns, each at n_freqs log-spaced frequencies from
+    1 kHz to 100 MHz with 4 plane waves, all submitted at once to one server
+    (its Lp / P cache warmed first), mixed solve then plain FP64 LU.
+    Throughput = systems reaching the 1e-10 gate / makespan."""
+    from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
+    from peeeeeeeeeeeeeeeeeeec_gb300.server import Server
+    pool = W.serving_meshes(seed=11, count=n_meshes, lo=300, hi=4000)
+    systems = W.batch_systems(seed=13, n_meshes=n_meshes, n_freqs=n_freqs)
+    out = {"systems": "%d meshes x %d frequencies (1 kHz - 100 MHz, log) x 4 plane waves" % (n_meshes, n_freqs),
+           "unknowns": [m.n_edges + m.n_nodes for m, _ in pool], "workers": workers}
+    with Server(150 << 30, workers) as srv:
+        for t in [srv.submit(m, i, 30e6, [[0.0, 0.0, -1.0]], [[1.0, 0.0, 0.0]]) for i, (m, _) in enumerate(pool)]:
+            srv.wait(t)
+        for mode in ("mixed", "plain"):
+            tickets = [srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed")) for (mi, f, k, e) in systems]
+            res = [srv.wait(t)[1] for t in tickets]
+            span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
+            ok = sum(1 for r in res if r["status"] == 0 and r["backward_error"] <= 1e-10)
+            lat = np.array([r["t_end"] - r["t_submit"] for r in res])
+            out[mode] = {"value": ok / span, "unit": "systems/s", "at_gate": ok, "systems": len(res),
+                         "makespan_s": span, "fallbacks_to_fp64": sum(r.get("fallback", 0) for r in res),
+                         "p50_latency_s": float(np.percentile(lat, 50)),
+                         "p99_latency_s": float(np.percentile(lat, 99)),
+                         "max_backward_error": max(r["backward_error"] for r in res)}
+    out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
+    for m, _ in pool:
+        m.close()
+    return out
+
+
 def drop_in_solve(lib, m, b_host, edges):
     from peeeeeeeeeeeeeeeeeeec_gb300 import abi
     lo = abi.InductanceOptions()
@@ -529,6 +561,7 @@ def main():
     ap.add_argument("--no-retarded", action="store_true")
     ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--batch", default="8x8", help="meshes x frequencies of the batched leg (0: skip)")
     args = ap.parse_args()
     if args.box:
         set_box(args.box)
@@ -618,6 +651,10 @@ def main():
     retarded = None if args.no_retarded else retarded_leg(lib, ds)
     ds.free()
     serving = serving_leg(lib, args.serve_window, args.serve_workers) if args.serve_window > 0 else None
+    batched = None
+    if args.batch not in ("0", ""):
+        bm, bf = (int(v) for v in args.batch.split("x"))
+        batched = batched_leg(lib, bm, bf, args.serve_workers)
 
     # end to end through the drop-in ABI, host buffers
     e2e = None
@@ -667,7 +704,7 @@ def main():
                                           "the retarded kernel is the 'retarded' leg"},
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-                "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "transient": transient, "retarded": retarded,
+                "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "batched": batched, "transient": transient, "retarded": retarded,
                 "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
                                       "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
                 "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}

@@ -150,6 +150,16 @@ int peec_gb300_tc_gemm(const void *d_a, const void *d_b0, const void *d_b1, floa
 int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Complex *d_b,
                                           Complex *d_x, size_t nrhs, double tol, int max_iter,
                                           double *backward_error, int *iterations);
+/* FP64 iterative refinement of d_x (in: a solution, out: the refined one)
+ * with an FP64 factor of Z from peec_gb300_complex_lu_factor_device:
+ * r = b - Z x, x += (LU)^-1 r until the componentwise backward error
+ * <= tol.  Returns 0 when reached, 1 when not after max_iter corrections,
+ * -1 on errors.  The server uses it when a mixed solve falls back to FP64. */
+int peec_gb300_complex_refine_device(const Complex *d_Z, const Complex *d_lu, const int *d_perm,
+                                     const double *d_row_scale, const double *d_column_scale,
+                                     size_t n, const Complex *d_b, Complex *d_x, size_t nrhs,
+                                     double tol, int max_iter, double *backward_error,
+                                     int *iterations);
 /* Phase times (ms) of the last mixed solve; returns its iteration count. */
 int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine);
 
@@ -223,6 +233,20 @@ int peec_gb300_transient_lightning(void *system, double K, double alpha, double 
                                    const int *d_probe_nodes, size_t n_probe_nodes,
                                    const int *d_probe_edges, size_t n_probe_edges,
                                    double *d_probes);
+/* nrun (1 to 8) lightning runs on one system stepped together: run r has
+ * its own source (K[r], alpha[r], beta[r], delay[r], strike_node[r],
+ * return_node[r]) and state d_X + r (Ne + Nv) = [I; V] (in and out); every
+ * step reads Lp, A S and the factor once for all runs (the runs are the
+ * right-hand sides of one wavefront solve).  d_probes:
+ * [n_steps][nrun][n_probe_nodes + n_probe_edges].  Each run's result is the
+ * one a single run gives, to rounding. */
+int peec_gb300_transient_lightning_batch(void *system, int nrun, const double *K,
+                                         const double *alpha, const double *beta,
+                                         const double *delay, const size_t *strike_node,
+                                         const size_t *return_node, size_t step0, size_t n_steps,
+                                         double *d_X, const int *d_probe_nodes,
+                                         size_t n_probe_nodes, const int *d_probe_edges,
+                                         size_t n_probe_edges, double *d_probes);
 void peec_gb300_transient_destroy(void *system);
 
 /* ---- serving loop ----

@@ -228,6 +228,9 @@ EXT_SYMBOLS = [
     ("peec_gb300_complex_solve_mixed_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, c_double_p,
       c_int_p]),
+    ("peec_gb300_complex_refine_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+      C.c_size_t, C.c_double, C.c_int, c_double_p, c_int_p]),
     ("peec_gb300_mixed_timing", C.c_int, [c_double_p, c_double_p, c_double_p]),
     ("peec_gb300_harmonic_build_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_double,
@@ -250,6 +253,9 @@ EXT_SYMBOLS = [
      [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t,
       C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
       C.c_size_t, C.c_void_p]),
+    ("peec_gb300_transient_lightning_batch", C.c_int,
+     [C.c_void_p, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p, P(C.c_size_t), P(C.c_size_t),
+      C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p]),
     ("peec_gb300_transient_destroy", None, [C.c_void_p]),
     ("peec_gb300_server_create", C.c_void_p, [C.c_size_t, C.c_int]),
     ("peec_gb300_server_submit", C.c_longlong, [C.c_void_p, P(PeecHarmonicRequest)]),

@@ -1357,8 +1357,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
 // field, FP64) and D_k = integral of (exp(-jkR) - 1)/R, which is smooth and
 // bounded (limit -jk at R = 0), by the far product rule over every patch
 // pair, on the FP32 pipes: (exp(-jkR) - 1)/R = (-2 sin^2(kR/2) - j sin kR)/R
-// from one sincosf, per-lane FP32 sums combined in FP64.  D_k carries ~1e-6
-// relative FP32 error; at k = 0 the result is the static matrix exactly.
+// from one sincosf, FP32 sums per lane and across the warp.  D_k carries
+// ~1e-6 relative FP32 error; at k = 0 the result is the static matrix exactly.
 // ---------------------------------------------------------------------
 struct Cplx {
     double re, im;
@@ -1374,8 +1374,10 @@ struct RetardArgs {
     Cplx *out;           // n x n complex
 };
 
-__device__ __forceinline__ void retard_pair(const FarPtF *pa, const FarPtF *pb, int npts, float k, double &re,
-                                            double &im) {
+// per-lane FP32 sums of one patch pair's correction (no FP64 instructions in
+// the point loop: on GB300 they would cost 64 cycles per warp each)
+__device__ __forceinline__ void retard_pair(const FarPtF *pa, const FarPtF *pb, int npts, float k, float &re,
+                                            float &im) {
     const int lane = threadIdx.x & 31;
     for (int p = lane; p < npts; p += 32) {
         FarPtF A = pa[p];
@@ -1395,8 +1397,8 @@ __device__ __forceinline__ void retard_pair(const FarPtF *pa, const FarPtF *pb, 
                 si = fmaf(B.wh, -k, si);
             }
         }
-        re = fma((double)A.wh, (double)sr, re);
-        im = fma((double)A.wh, (double)si, im);
+        re = fmaf(A.wh, sr, re);
+        im = fmaf(A.wh, si, im);
     }
 }
 
@@ -1419,15 +1421,18 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_retard_tiles(RetardArgs T) 
             } else {
                 scale = kInv4PiEps0 / (R.scale[a] * R.scale[b]);
             }
-            double dre = 0.0, dim = 0.0;
+            float fre = 0.0f, fim = 0.0f;
             if (scale != 0.0 && T.k != 0.0f)
                 for (int i = R.off[a]; i < R.off[a + 1]; ++i)
                     for (int j = R.off[b]; j < R.off[b + 1]; ++j)
-                        retard_pair(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, T.k, dre, dim);
-            dre = warp_sum(dre);
-            dim = warp_sum(dim);
-            val.re = T.stat[(size_t)a * n + b] + scale * dre;
-            val.im = scale * dim;
+                        retard_pair(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, T.k, fre, fim);
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) {
+                fre += __shfl_xor_sync(0xffffffffu, fre, m);
+                fim += __shfl_xor_sync(0xffffffffu, fim, m);
+            }
+            val.re = T.stat[(size_t)a * n + b] + scale * (double)fre;
+            val.im = scale * (double)fim;
         }
         if (lane == 0) tile[r][c] = val;
     }

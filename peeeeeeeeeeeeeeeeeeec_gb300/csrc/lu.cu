@@ -34,6 +34,7 @@
 #include "../../include/complex_lu.h"
 #include "../../include/lu.h"
 #include "../../include/peec_gb300.h"
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -244,6 +245,21 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
     }
 }
 
+// Pivot magnitudes: FP64 hypot for the FP64 factorisations (the reference's
+// pivot choice), FP32 for the FP32 factorisation of the mixed path (no FP64
+// instructions there: on GB300 one warp-wide FP64 compare costs 64 cycles).
+template <class T>
+struct MagType {
+    using type = double;
+};
+template <>
+struct MagType<cplxf> {
+    using type = float;
+};
+__device__ __forceinline__ double mag_t(double v) { return fabs(v); }
+__device__ __forceinline__ double mag_t(cplx v) { return hypot(v.re, v.im); }
+__device__ __forceinline__ float mag_t(cplxf v) { return hypotf(v.re, v.im); }
+
 struct PanelSlots {
     unsigned int count;
     unsigned int gen;
@@ -290,11 +306,13 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                                                     int *cand_idx, T *cand_row, T *krow) {
     extern __shared__ unsigned char smem_raw[];
     T *tile = reinterpret_cast<T *>(smem_raw);  // [rows_per_cta][NB]
+    using M = typename MagType<T>::type;  // FP32 magnitudes for the FP32 factorisation
+    M *cval = reinterpret_cast<M *>(cand_val);
     __shared__ T s_prow[NB];
-    __shared__ double s_val[8];
+    __shared__ M s_val[8];
     __shared__ int s_idx[8];
     __shared__ int s_cta[8];
-    __shared__ int s_p, s_fail;
+    __shared__ int s_p, s_fail, s_pc;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned int G = gridDim.x;
     const int c = blockIdx.x;
@@ -311,10 +329,10 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         const int k = k0 + kk, par = kk & 1;
         // local argmax over this CTA's rows i >= k (NaN below the diagonal
         // never wins; a NaN diagonal becomes +inf and is rejected)
-        double best = -1.0;
+        M best = -1;
         int bi = n;
         for (int i = max(r0, k) + tid; i < r1; i += blockDim.x) {
-            double m = mag(tile[(i - r0) * NB + kk]);
+            M m = mag_t(tile[(i - r0) * NB + kk]);
             if (i == k && isnan(m)) m = INFINITY;
             if (isnan(m)) continue;
             if (m > best || (m == best && i < bi)) {
@@ -323,7 +341,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
             }
         }
         for (int s = 16; s > 0; s >>= 1) {
-            double ov = __shfl_xor_sync(0xffffffffu, best, s);
+            M ov = __shfl_xor_sync(0xffffffffu, best, s);
             int oi = __shfl_xor_sync(0xffffffffu, bi, s);
             if (ov > best || (ov == best && oi < bi)) {
                 best = ov;
@@ -343,7 +361,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                 }
             s_val[0] = best;
             s_idx[0] = bi;
-            cand_val[par * G + c] = best;
+            cval[par * G + c] = best;
             cand_idx[par * G + c] = bi;
         }
         __syncthreads();
@@ -361,10 +379,10 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         // global pivot, identical in every CTA: the G candidates are loaded
         // in parallel and reduced (largest value, then lowest row)
         {
-            double gb = -1.0;
+            M gb = -1;
             int gi = n, gc = -1;
             for (unsigned int q = tid; q < G; q += blockDim.x) {
-                double v = ld_volatile(cand_val + par * G + q);
+                M v = ld_volatile(cval + par * G + q);
                 int ix = ld_volatile(cand_idx + par * G + q);
                 if (ix >= n) continue;
                 if (v > gb || (v == gb && ix < gi)) {
@@ -374,7 +392,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                 }
             }
             for (int sh = 16; sh > 0; sh >>= 1) {
-                double ov = __shfl_xor_sync(0xffffffffu, gb, sh);
+                M ov = __shfl_xor_sync(0xffffffffu, gb, sh);
                 int oi = __shfl_xor_sync(0xffffffffu, gi, sh);
                 int oc = __shfl_xor_sync(0xffffffffu, gc, sh);
                 if (ov > gb || (ov == gb && oi < gi)) {
@@ -392,7 +410,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
             __syncthreads();
         }
         if (tid == 0) {
-            double gb = s_val[0];
+            M gb = s_val[0];
             int gi = s_idx[0], gc = s_cta[0];
             for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
                 if (s_val[w] > gb || (s_val[w] == gb && s_idx[w] < gi)) {
@@ -401,22 +419,22 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                     gc = s_cta[w];
                 }
             s_fail = 0;
-            if (gc < 0 || !isfinite(gb) || gb <= limit) {
+            if (gc < 0 || !isfinite(gb) || (double)gb <= limit) {
                 s_fail = 1;
                 if (c == 0) {
                     st->code = 2;
                     st->column = k;
-                    st->value = gb;
+                    st->value = (double)gb;
                 }
             } else if (c == 0) {
                 piv[k] = gi;
             }
             s_p = gi;
-            s_val[1] = (double)gc;
+            s_pc = gc;
         }
         __syncthreads();
         if (s_fail) return;
-        const int p = s_p, pc = (int)s_val[1];
+        const int p = s_p, pc = s_pc;
         // the new row k is the published row p (full panel width: columns
         // < kk hold earlier multipliers and move with the row)
         const T *prow_g = cand_row + ((size_t)par * G + pc) * NB;
@@ -444,6 +462,168 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         int i = t / kb, j = t % kb;
         a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
     }
+}
+
+// ---- cluster panel ----------------------------------------------------
+// The same partial-pivoting panel (first maximum wins, NaN never wins, the
+// same swaps and updates, so the same pivots as the reference) on one
+// thread-block cluster of up to 16 CTAs: the panel rows sit in the CTAs'
+// shared memory, candidates are exchanged through distributed shared memory
+// and each column costs one hardware cluster barrier instead of a grid
+// barrier through global memory.  Slots alternate by column parity, so a
+// CTA that runs ahead never overwrites a slot another CTA still reads (it
+// cannot pass the next barrier before the slower one arrives).  Used while
+// the panel fits (rows per CTA x 32 elements in shared memory).
+template <class T>
+struct ClusterSlot {
+    T cand_row[2][NB];  // this CTA's candidate row, by column parity
+    T krow[2][NB];      // row k when owned here
+    double val[2];      // candidate magnitude (as double: exact for float)
+    int idx[2];         // candidate row, n if none
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) k_panel_cluster(T *a, int n, int k0, int kb, int rows_per_cta, double limit,
+                                                       long long *piv, Status *st) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    using M = typename MagType<T>::type;
+    extern __shared__ __align__(16) unsigned char cl_smem[];
+    ClusterSlot<T> &slot = *reinterpret_cast<ClusterSlot<T> *>(cl_smem);
+    T *tile = reinterpret_cast<T *>(cl_smem + ((sizeof(ClusterSlot<T>) + 15) & ~(size_t)15));  // [rows][NB]
+    __shared__ T s_prow[NB];
+    __shared__ M s_val[8];
+    __shared__ int s_idx[8];
+    __shared__ int s_p, s_pc, s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int C = (int)cluster.num_blocks(), c = (int)cluster.block_rank();
+    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform across the cluster (set before launch)
+    for (int t = tid; t < nrows * kb; t += blockDim.x) {
+        int i = t / kb, j = t % kb;
+        tile[i * NB + j] = a[(size_t)(r0 + i) * n + k0 + j];
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk, par = kk & 1;
+        M best = -1;
+        int bi = n;
+        for (int i = max(r0, k) + tid; i < r1; i += blockDim.x) {
+            M m = mag_t(tile[(i - r0) * NB + kk]);
+            if (i == k && isnan(m)) m = INFINITY;
+            if (isnan(m)) continue;
+            if (m > best || (m == best && i < bi)) {
+                best = m;
+                bi = i;
+            }
+        }
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            M ov = __shfl_xor_sync(0xffffffffu, best, sh);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_val[warp] = best;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                if (s_val[w] > best || (s_val[w] == best && s_idx[w] < bi)) {
+                    best = s_val[w];
+                    bi = s_idx[w];
+                }
+            slot.val[par] = (double)best;
+            slot.idx[par] = bi;
+            s_idx[0] = bi;
+        }
+        __syncthreads();
+        bi = s_idx[0];
+        if (bi < n)
+            for (int j = tid; j < kb; j += blockDim.x) slot.cand_row[par][j] = tile[(bi - r0) * NB + j];
+        if (k >= r0 && k < r1)
+            for (int j = tid; j < kb; j += blockDim.x) slot.krow[par][j] = tile[(k - r0) * NB + j];
+        cluster.sync();
+        // global pivot from the C slots (distributed shared memory)
+        if (warp == 0) {
+            double gb = -1.0;
+            int gi = n, gc = -1;
+            if (lane < C) {
+                ClusterSlot<T> *rs = cluster.map_shared_rank(&slot, lane);
+                int ix = rs->idx[par];
+                double v = rs->val[par];
+                if (ix < n) {
+                    gb = v;
+                    gi = ix;
+                    gc = lane;
+                }
+            }
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                double ov = __shfl_xor_sync(0xffffffffu, gb, sh);
+                int oi = __shfl_xor_sync(0xffffffffu, gi, sh);
+                int oc = __shfl_xor_sync(0xffffffffu, gc, sh);
+                if (ov > gb || (ov == gb && oi < gi)) {
+                    gb = ov;
+                    gi = oi;
+                    gc = oc;
+                }
+            }
+            if (lane == 0) {
+                s_fail = 0;
+                if (gc < 0 || !isfinite(gb) || gb <= limit) {
+                    s_fail = 1;
+                    if (c == 0) {
+                        st->code = 2;
+                        st->column = k;
+                        st->value = gb;
+                    }
+                } else if (c == 0) {
+                    piv[k] = gi;
+                }
+                s_p = gi;
+                s_pc = gc;
+            }
+        }
+        __syncthreads();
+        if (s_fail) {  // identical decision in every CTA of the cluster
+            cluster.sync();  // every CTA has read the slots before any leaves
+            return;
+        }
+        const int p = s_p, pc = s_pc;
+        {
+            ClusterSlot<T> *ps = cluster.map_shared_rank(&slot, pc);
+            for (int j = tid; j < kb; j += blockDim.x) s_prow[j] = ps->cand_row[par][j];
+        }
+        __syncthreads();
+        if (p != k) {
+            if (k >= r0 && k < r1)
+                for (int j = tid; j < kb; j += blockDim.x) tile[(k - r0) * NB + j] = s_prow[j];
+            if (p >= r0 && p < r1) {
+                const int kc = (k - k0) / rows_per_cta;  // owner of row k
+                ClusterSlot<T> *ks = cluster.map_shared_rank(&slot, kc);
+                for (int j = tid; j < kb; j += blockDim.x) tile[(p - r0) * NB + j] = ks->krow[par][j];
+            }
+        }
+        __syncthreads();
+        if (k + 1 >= n) break;
+        const T pivot = s_prow[kk];
+        for (int i = max(r0, k + 1) + tid; i < r1; i += blockDim.x) {
+            T *row = tile + (i - r0) * NB;
+            T m = divide(row[kk], pivot);
+            row[kk] = m;
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], m, s_prow[j]);
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < nrows * kb; t += blockDim.x) {
+        int i = t / kb, j = t % kb;
+        a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its slots
 }
 
 // ---- row swaps outside the panel -------------------------------------
@@ -1228,6 +1408,57 @@ struct CoopPlan {
     size_t smem = 0;
 };
 
+// Cluster panel: C CTAs (16 where the device allows non-portable clusters,
+// else 8) when the m panel rows fit their shared memory.  Returns false
+// when the cluster panel does not apply; the caller then uses the
+// cooperative grid panel.
+template <class T>
+static bool launch_cluster_panel(T *a, int n, int k0, int kb, double limit, long long *piv, Status *st) {
+    const int m = n - k0;
+    if (m < 2 * 64) return false;  // small panels: one CTA is faster
+    static const size_t kMaxSmem = 220 * 1024;
+    static const size_t head = (sizeof(ClusterSlot<T>) + 15) & ~(size_t)15;
+    static const int max_c = [] {
+        cudaFuncSetAttribute(k_panel_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+        cudaFuncSetAttribute(k_panel_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = kMaxSmem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int c = 0;
+        if (cudaOccupancyMaxPotentialClusterSize(&c, k_panel_cluster<T>, &cfg) != cudaSuccess) c = 0;
+        cudaGetLastError();
+        return c >= 16 ? 16 : c >= 8 ? 8 : 0;
+    }();
+    if (max_c == 0) return false;
+    const int C = max_c;
+    const int rows = (m + C - 1) / C;
+    const size_t smem = head + (size_t)rows * NB * sizeof(T);
+    if (smem > kMaxSmem) return false;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream();
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    note_launch();
+    return cuda_ok(cudaLaunchKernelEx(&cfg, k_panel_cluster<T>, a, n, k0, kb, rows, limit, piv, st),
+                   "cluster panel launch");
+}
+
 template <class T>
 static CoopPlan<T> coop_plan(int m) {
     CoopPlan<T> pl;
@@ -1251,6 +1482,21 @@ static CoopPlan<T> coop_plan(int m) {
     pl.rows = rows;
     pl.smem = smem;
     return pl;
+}
+
+// Panel form: the cooperative grid panel by default; PEEC_GB300_PANEL=cluster
+// selects the 16-CTA cluster panel where it fits.  Measured on GB300 (8402
+// unknowns) the cluster form is slower -- the mixed panel 68 ms against 55 ms,
+// the plain 116 ms against 105 ms: its dependent distributed-shared-memory
+// reads and the larger per-CTA row count cost more per column than the grid
+// barrier saves -- so it stays an alternative, checked to give the same
+// factors bit for bit.
+static bool cluster_panel_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PEEC_GB300_PANEL");
+        return e && strcmp(e, "cluster") == 0;
+    }();
+    return on;
 }
 
 // Complex trailing update form: the direct 4-product form (default; it keeps
@@ -1335,7 +1581,8 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
         int kb = std::min(NB, n - k0);
         tm.mark(2);
         CoopPlan<T> pl = coop_plan<T>(n - k0);
-        if (pl.G > 0) {
+        if (cluster_panel_enabled() && launch_cluster_panel<T>(d_a, n, k0, kb, limit, d_piv, d_st)) {
+        } else if (pl.G > 0) {
             int rows = pl.rows;
             T *cr = (T *)sc.cand_row, *kr = (T *)sc.krow;
             void *args[] = {&d_a, &n, (void *)&k0, &kb, &rows, &limit, &d_piv, &d_st, &sc.ps, &sc.cand_val,
@@ -2198,6 +2445,18 @@ __global__ void k_residual(const cplx *Z, const float *absZ, const cplx *x, cons
     }
 }
 
+__global__ void k_abs_x(const cplx *x, size_t count, float *absx) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t < count) absx[t] = abs_f32(x[t]);
+}
+
+__global__ void k_add_cplx(cplx *x, const cplx *dx, size_t count) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    x[t].re += dx[t].re;
+    x[t].im += dx[t].im;
+}
+
 struct MixedTiming {
     double ms_prepare = 0, ms_factor = 0, ms_refine = 0;
     int iterations = 0;
@@ -2205,6 +2464,48 @@ struct MixedTiming {
 static thread_local MixedTiming g_mixed_timing;  // last mixed solve of this host thread
 
 }  // namespace peec
+
+// FP64 iterative refinement of a solution from an FP64 complex factor of Z
+// (peec_gb300_complex_lu_factor_device): r = b - Z x, x += LU^-1 r until the
+// componentwise backward error <= tol.  Returns 0 when reached, 1 when not
+// after max_iter corrections (x holds the last iterate), -1 on errors.
+extern "C" int peec_gb300_complex_refine_device(const Complex *d_Z, const Complex *d_lu, const int *d_perm,
+                                                const double *d_row_scale, const double *d_column_scale, size_t n_,
+                                                const Complex *d_b, Complex *d_x, size_t nrhs_, double tol,
+                                                int max_iter, double *backward_error, int *iterations) {
+    using namespace peec;
+    if (!d_Z || !d_lu || !d_perm || !d_row_scale || !d_column_scale || !d_b || !d_x || n_ == 0 || nrhs_ == 0 ||
+        n_ > (size_t)0x7fffffff || max_iter < 0)
+        return -1;
+    const int n = (int)n_, nrhs = (int)nrhs_;
+    const size_t nn = n_ * n_, nv = n_ * nrhs_;
+    const cplx *Z = (const cplx *)d_Z;
+    cplx *x = (cplx *)d_x;
+    DBuf<float> absZ(nn), absx(nv);
+    DBuf<cplx> r(nv), dx(nv);
+    DBuf<unsigned long long> be(1);
+    if (!absZ.p || !absx.p || !r.p || !dx.p || !be.p) return -1;
+    PEEC_LAUNCH(k_abs_matrix, 152 * 8, 256, 0, Z, nn, absZ.p);
+    double eta = INFINITY;
+    int it = 0;
+    for (;; ++it) {
+        cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+        PEEC_LAUNCH(k_abs_x, (unsigned)((nv + 255) / 256), 256, 0, x, nv, absx.p);
+        PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, (const cplx *)d_b, n,
+                    nrhs, r.p, be.p);
+        unsigned long long hb = 0;
+        cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
+        if (!launch_ok("refinement") || !sync("refinement")) return -1;
+        memcpy(&eta, &hb, sizeof(eta));
+        if (eta <= tol || it >= max_iter) break;
+        if (!solve_device<cplx>((const cplx *)d_lu, d_perm, d_row_scale, d_column_scale, n, r.p, dx.p, nrhs))
+            return -1;
+        PEEC_LAUNCH(k_add_cplx, (unsigned)((nv + 255) / 256), 256, 0, x, dx.p, nv);
+    }
+    if (backward_error) *backward_error = eta;
+    if (iterations) *iterations = it;
+    return eta <= tol ? 0 : 1;
+}
 
 extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x,
                                                      size_t nrhs_, double tol, int max_iter, double *backward_error,
@@ -2289,7 +2590,8 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             const int kb = std::min(NB, E - k0);
             tm.mark(2);
             CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
-            if (pl.G > 0) {
+            if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
+            } else if (pl.G > 0) {
                 int rows = pl.rows;
                 cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
                 Status *stp = st.p;

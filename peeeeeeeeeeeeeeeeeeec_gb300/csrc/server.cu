@@ -219,6 +219,7 @@ class Server {
         cudaSetDevice(device_);
         for (;;) {
             std::shared_ptr<Job> j;
+            std::vector<std::shared_ptr<Job>> batch;  // transient runs stepped with j
             MeshEntry *me = nullptr;
             TransientEntry *te = nullptr;
             bool build_mesh = false, build_sys = false;
@@ -261,6 +262,26 @@ class Server {
                 me->last_use = ++tick_;
                 used_ += j->bytes;
                 j->res.t_start = clock();
+                if (j->kind == 1) {
+                    // continuous batching of lightning runs: queued runs on the
+                    // same system with the same length and probes join this one
+                    // (up to 8 runs per step), as far as the budget allows
+                    for (auto q = queue_.begin(); q != queue_.end() && batch.size() < 7;) {
+                        const Job &o = **q;
+                        if (o.kind == 1 && o.mesh_key == j->mesh_key && o.treq.scheme == j->treq.scheme &&
+                            o.treq.dt == j->treq.dt && o.treq.n_steps == j->treq.n_steps &&
+                            o.probe_nodes == j->probe_nodes && o.probe_edges == j->probe_edges &&
+                            used_ + o.bytes <= budget_) {
+                            used_ += o.bytes;
+                            me->users++;
+                            (*q)->res.t_start = j->res.t_start;
+                            batch.push_back(*q);
+                            q = queue_.erase(q);
+                        } else {
+                            ++q;
+                        }
+                    }
+                }
             }
             cv_.notify_all();
             if (build_mesh) {
@@ -290,13 +311,18 @@ class Server {
                 }
                 status = te->status;
             }
-            if (status == 0) status = j->kind == 0 ? solve(*me, *j) : run_transient(*me, *te, *j);
+            batch.insert(batch.begin(), j);
+            if (status == 0) status = j->kind == 0 ? solve(*me, *j) : run_transient(*me, *te, batch);
             {
                 std::lock_guard<std::mutex> g(mu_);
-                j->res.status = status;
-                j->res.t_end = clock();
-                used_ -= j->bytes;
-                me->users--;
+                for (auto &b : batch) {
+                    b->res.status = status;
+                    b->res.t_end = clock();
+                    b->res.iterations = j->kind == 1 ? (int)b->treq.n_steps : b->res.iterations;
+                    used_ -= b->bytes;
+                    me->users--;
+                    if (b != j) b->done = true;
+                }
                 if ((me->status != 0 || (te && te->status != 0)) && me->users == 0) {
                     // a failed assembly or factorisation is not kept
                     used_ -= me->bytes;
@@ -365,8 +391,15 @@ class Server {
             status = peec_gb300_complex_lu_factor_device(W.p, n, 1e-14, piv.p, perm.p, rs.p, cs.p, &scale, &col);
             if (status == 0)
                 status = peec_gb300_complex_lu_solve_device(W.p, perm.p, rs.p, cs.p, n, B.p, X.p, nrhs);
-            double out[3];
-            if (status == 0 && peec_gb300_backward_error_device(Z.p, n, X.p, B.p, nrhs, out) == 0) be = out[0];
+            if (status == 0 && j.res.fallback) {
+                // the fallback refines in FP64 with the FP64 factor to the gate
+                double tol = r.tolerance > 0.0 ? r.tolerance : 1e-10;
+                status = peec_gb300_complex_refine_device(Z.p, W.p, perm.p, rs.p, cs.p, n, B.p, X.p, nrhs, tol, 5,
+                                                          &be, &iters);
+            } else {
+                double out[3];
+                if (status == 0 && peec_gb300_backward_error_device(Z.p, n, X.p, B.p, nrhs, out) == 0) be = out[0];
+            }
         }
         j.res.backward_error = be;
         j.res.iterations = iters;
@@ -375,23 +408,46 @@ class Server {
         return status;
     }
 
-    int run_transient(const MeshEntry &e, const TransientEntry &t, Job &j) {
-        const PeecTransientRequest &r = j.treq;
-        const size_t npn = j.probe_nodes.size(), npe = j.probe_edges.size(), np = npn + npe;
-        DBuf<double> I(e.ne), V(e.nv), probes(r.n_steps * np);
+    // the lightning runs of `jobs` (same system, length and probes) stepped
+    // together; each job gets its own waveforms and final state
+    int run_transient(const MeshEntry &e, const TransientEntry &t, const std::vector<std::shared_ptr<Job>> &jobs) {
+        const Job &j0 = *jobs[0];
+        const int nrun = (int)jobs.size();
+        const size_t nt = e.ne + e.nv, n_steps = j0.treq.n_steps;
+        const size_t npn = j0.probe_nodes.size(), npe = j0.probe_edges.size(), np = npn + npe;
+        DBuf<double> X(nt * nrun), probes(n_steps * nrun * np);
         DBuf<int> pn(npn), pe(npe);
-        if (!I.p || !V.p || (np && !probes.p) || (npn && !pn.p) || (npe && !pe.p)) return -1;
-        cudaMemsetAsync(I.p, 0, 8 * e.ne, stream());
-        cudaMemsetAsync(V.p, 0, 8 * e.nv, stream());
-        if ((npn && !pn.upload(j.probe_nodes.data(), npn)) || (npe && !pe.upload(j.probe_edges.data(), npe)))
+        if (!X.p || (np && !probes.p) || (npn && !pn.p) || (npe && !pe.p)) return -1;
+        cudaMemsetAsync(X.p, 0, 8 * nt * nrun, stream());
+        if ((npn && !pn.upload(j0.probe_nodes.data(), npn)) || (npe && !pe.upload(j0.probe_edges.data(), npe)))
             return -1;
-        int s = peec_gb300_transient_lightning(t.sys, r.K, r.alpha, r.beta, r.delay, r.strike_node, r.return_node, 0,
-                                               r.n_steps, I.p, V.p, pn.p, npn, pe.p, npe, probes.p);
-        j.res.iterations = (int)r.n_steps;
+        std::vector<double> K(nrun), al(nrun), be(nrun), de(nrun);
+        std::vector<size_t> sk(nrun), rt(nrun);
+        for (int r = 0; r < nrun; ++r) {
+            const PeecTransientRequest &q = jobs[r]->treq;
+            K[r] = q.K;
+            al[r] = q.alpha;
+            be[r] = q.beta;
+            de[r] = q.delay;
+            sk[r] = q.strike_node;
+            rt[r] = q.return_node;
+        }
+        int s = peec_gb300_transient_lightning_batch(t.sys, nrun, K.data(), al.data(), be.data(), de.data(),
+                                                     sk.data(), rt.data(), 0, n_steps, X.p, pn.p, npn, pe.p, npe,
+                                                     probes.p);
         if (s != 0) return s;
-        if ((np && !probes.download(r.probes, r.n_steps * np)) || (r.I && !I.download(r.I, e.ne)) ||
-            (r.V && !V.download(r.V, e.nv)) || !sync("transient result"))
+        std::vector<double> hx(nt * nrun), hp(n_steps * nrun * np);
+        if (!X.download(hx.data(), nt * nrun) || (np && !probes.download(hp.data(), hp.size())) ||
+            !sync("transient result"))
             return -1;
+        for (int r = 0; r < nrun; ++r) {
+            const PeecTransientRequest &q = jobs[r]->treq;
+            if (np && q.probes)
+                for (size_t k = 0; k < n_steps; ++k)
+                    memcpy(q.probes + k * np, hp.data() + (k * nrun + r) * np, np * sizeof(double));
+            if (q.I) memcpy(q.I, hx.data() + r * nt, e.ne * sizeof(double));
+            if (q.V) memcpy(q.V, hx.data() + r * nt + e.ne, e.nv * sizeof(double));
+        }
         return 0;
     }
 };

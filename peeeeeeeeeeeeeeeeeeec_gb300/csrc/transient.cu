@@ -98,16 +98,22 @@ __device__ __forceinline__ double lightning_current(const LightningArgs &s, doub
     return s.K * (exp(-s.alpha * tau) - exp(-s.beta * tau));
 }
 
+// Several lightning runs on one system are stepped together (up to kMaxRuns):
+// the right-hand-side kernel reads each Lp / A S row once for all runs and
+// the wavefront solve takes the runs as right-hand sides, so the factor is
+// read once per step for all of them.
+static const int kMaxRuns = 8;
+
 struct StepArgs {
     const double *L, *R, *AS, *F;
     const int *adj_ptr, *adj;
-    int ne, nv;
+    int ne, nv, nrun;
     double theta, dt;
-    const double *x;  // state [I; V] after the previous step
-    double *rhs;
-    LightningArgs src;
+    const double *x;  // states [nrun][I; V] after the previous step
+    double *rhs;      // [nrun][ne + nv]
+    LightningArgs src[kMaxRuns];
     long long step;
-    // probes of the previous step's state (record_row >= 0)
+    // probes of the previous step's state (record_row >= 0): [row][run][np]
     const int *probe_nodes, *probe_edges;
     int n_probe_nodes, n_probe_edges;
     double *probes;
@@ -115,64 +121,99 @@ struct StepArgs {
 };
 
 __device__ __forceinline__ void record_probes(const StepArgs &A, long long row) {
-    const int np = A.n_probe_nodes + A.n_probe_edges;
-    for (int k = threadIdx.x; k < np; k += blockDim.x) {
+    const int np = A.n_probe_nodes + A.n_probe_edges, nt = A.ne + A.nv;
+    for (int t = threadIdx.x; t < np * A.nrun; t += blockDim.x) {
+        const int r = t / np, k = t % np;
+        const double *x = A.x + (size_t)r * nt;
         double v = NAN;  // an index outside the mesh records NaN
         if (k < A.n_probe_nodes) {
             int j = A.probe_nodes[k];
-            if (j >= 0 && j < A.nv) v = A.x[A.ne + j];
+            if (j >= 0 && j < A.nv) v = x[A.ne + j];
         } else {
             int e = A.probe_edges[k - A.n_probe_nodes];
-            if (e >= 0 && e < A.ne) v = A.x[e];
+            if (e >= 0 && e < A.ne) v = x[e];
         }
-        A.probes[row * np + k] = v;
+        A.probes[(row * A.nrun + r) * np + k] = v;
     }
 }
 
-// Right-hand side of one step (transient.c:1421-1631, edge voltages absent):
-// blocks [0, eb) take the edge rows, one warp each; the rest the node rows.
+// this lane's part of row . x_r for every run r < nrun: each row element is
+// loaded once (streamed from HBM), two loads in flight per lane; the states
+// stay in L1 / L2
+template <int R>
+__device__ __forceinline__ void row_dot_runs(const double *row, const double *x, size_t ldx, int n, int lane,
+                                             double *acc) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = 0.0;
+    int j = lane;
+    for (; j + 32 < n; j += 64) {
+        const double a0 = __ldcs(row + j), a1 = __ldcs(row + j + 32);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            acc[r] = fma(a0, x[r * ldx + j], acc[r]);
+            acc[r] = fma(a1, x[r * ldx + j + 32], acc[r]);
+        }
+    }
+    for (; j < n; j += 32) {
+        const double a0 = row[j];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = fma(a0, x[r * ldx + j], acc[r]);
+    }
+}
+
+// Right-hand side of one step for every run (transient.c:1421-1631, edge
+// voltages absent): blocks [0, eb) take the edge rows, one warp per row and
+// all runs; the rest the (node, run) pairs.
+template <int R>
 __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
     const double omt = 1.0 - A.theta;
+    const int nt = A.ne + A.nv;
     if (blockIdx.x == 0 && A.probes && A.record_row >= 0) record_probes(A, A.record_row);
     if ((int)blockIdx.x < eb) {
         const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
         if (i >= A.ne) return;
-        const double *I = A.x, *V = A.x + A.ne;
-        const double *Lr = A.L + (size_t)i * A.ne;
-        double s = 0.0;
-        for (int j = lane; j < A.ne; j += 32) s = fma(Lr[j], I[j], s);
-        s = warp_sum(s);
-        double sa = 0.0;
-        if (omt != 0.0) {
-            const double *Ar = A.AS + (size_t)i * A.nv;
-            for (int j = lane; j < A.nv; j += 32) sa = fma(Ar[j], V[j], sa);
-            sa = warp_sum(sa);
+        double s[R], sa[R];
+        row_dot_runs<R>(A.L + (size_t)i * A.ne, A.x, nt, A.ne, lane, s);
+        if (omt != 0.0)
+            row_dot_runs<R>(A.AS + (size_t)i * A.nv, A.x + A.ne, nt, A.nv, lane, sa);
+        else
+#pragma unroll
+            for (int r = 0; r < R; ++r) sa[r] = 0.0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const double ls = warp_sum(s[r]), as = omt != 0.0 ? warp_sum(sa[r]) : 0.0;
+            if (lane == 0 && r < A.nrun) {
+                const double *I = A.x + (size_t)r * nt;
+                A.rhs[(size_t)r * nt + i] = ls / A.dt - omt * A.R[i] * I[i] - omt * as;
+            }
         }
-        if (lane == 0) A.rhs[i] = s / A.dt - omt * A.R[i] * I[i] - omt * sa;
         return;
     }
-    const int j = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
-    if (j >= A.nv) return;
+    const int t = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
+    if (t >= A.nv * A.nrun) return;
+    const int r = t / A.nv, j = t % A.nv;
+    const double *x = A.x + (size_t)r * nt;
+    const LightningArgs &src = A.src[r];
     const double tn = (double)A.step * A.dt, tnp1 = (double)(A.step + 1) * A.dt;
     double jn = 0.0, jnp1 = 0.0;
-    if (j == A.src.strike || j == A.src.ret) {
-        jn = lightning_current(A.src, tn);
-        jnp1 = lightning_current(A.src, tnp1);
-        if (j == A.src.ret) {
+    if (j == src.strike || j == src.ret) {
+        jn = lightning_current(src, tn);
+        jnp1 = lightning_current(src, tnp1);
+        if (j == src.ret) {
             jn = -jn;
             jnp1 = -jnp1;
         }
     }
-    double v = A.F[j] * A.x[A.ne + j] / A.dt;
+    double v = A.F[j] * x[A.ne + j] / A.dt;
     double at = 0.0;  // (A^T I)_j
     for (int k = A.adj_ptr[j]; k < A.adj_ptr[j + 1]; ++k) {
-        int s = A.adj[k];
-        at += s > 0 ? A.x[s - 1] : -A.x[-s - 1];
+        int e = A.adj[k];
+        at += e > 0 ? x[e - 1] : -x[-e - 1];
     }
     v += omt * at;
     v += omt * jn;
     v += A.theta * jnp1;
-    A.rhs[A.ne + j] = v;
+    A.rhs[(size_t)r * nt + A.ne + j] = v;
 }
 
 __global__ void k_transient_probe(StepArgs A) { record_probes(A, A.record_row); }
@@ -255,17 +296,31 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     return 0;
 }
 
-static int run_lightning(const TransientSystem &S, const LightningArgs &src, long long step0, long long n_steps,
-                         double *d_I, double *d_V, const int *probe_nodes, int n_probe_nodes, const int *probe_edges,
-                         int n_probe_edges, double *probes) {
+static void launch_rhs(const StepArgs &A, int grid, int eb) {
+    switch (A.nrun) {
+        case 1: PEEC_LAUNCH(k_transient_rhs<1>, grid, 256, 0, A, eb); break;
+        case 2: PEEC_LAUNCH(k_transient_rhs<2>, grid, 256, 0, A, eb); break;
+        case 3:
+        case 4: PEEC_LAUNCH(k_transient_rhs<4>, grid, 256, 0, A, eb); break;
+        default: PEEC_LAUNCH(k_transient_rhs<8>, grid, 256, 0, A, eb); break;
+    }
+}
+
+// nrun runs (states d_X[r] = [I; V], sources src[r]) stepped together
+static int run_lightning(const TransientSystem &S, const LightningArgs *src, int nrun, long long step0,
+                         long long n_steps, double *d_X, const int *probe_nodes, int n_probe_nodes,
+                         const int *probe_edges, int n_probe_edges, double *probes) {
     const int ne = S.ne, nv = S.nv, nt = S.nt;
-    DBuf<double> x(nt), rhs(nt);
-    DBuf<unsigned> flags(wave_flag_words_real(nt, 1));
+    // the right-hand-side kernel is instantiated for 1, 2, 4 or 8 runs and
+    // reads that many states: pad with zero states
+    const int cap = nrun <= 1 ? 1 : nrun <= 2 ? 2 : nrun <= 4 ? 4 : 8;
+    DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * nrun);
+    DBuf<unsigned> flags(wave_flag_words_real(nt, nrun));
     DBuf<int> err(1);
     if (!x.p || !rhs.p || !flags.p || !err.p) return -1;
     cudaStream_t st = stream();
-    cudaMemcpyAsync(x.p, d_I, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(x.p + ne, d_V, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
+    if (cap > nrun) cudaMemsetAsync(x.p + (size_t)nt * nrun, 0, sizeof(double) * nt * (cap - nrun), st);
+    cudaMemcpyAsync(x.p, d_X, sizeof(double) * nt * nrun, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(err.p, 0, sizeof(int), st);
     StepArgs A{};
     A.L = S.L;
@@ -276,30 +331,30 @@ static int run_lightning(const TransientSystem &S, const LightningArgs &src, lon
     A.adj = S.adj;
     A.ne = ne;
     A.nv = nv;
+    A.nrun = nrun;
     A.theta = S.theta;
     A.dt = S.dt;
     A.x = x.p;
     A.rhs = rhs.p;
-    A.src = src;
+    for (int r = 0; r < nrun; ++r) A.src[r] = src[r];
     A.probe_nodes = probe_nodes;
     A.probe_edges = probe_edges;
     A.n_probe_nodes = n_probe_nodes;
     A.n_probe_edges = n_probe_edges;
     A.probes = (n_probe_nodes + n_probe_edges) > 0 ? probes : nullptr;
-    const int eb = (ne + 7) / 8, grid = eb + (nv + 255) / 256;
+    const int eb = (ne + 7) / 8, grid = eb + (nv * nrun + 255) / 256;
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
         A.record_row = k - 1;
-        PEEC_LAUNCH(k_transient_rhs, grid, 256, 0, A, eb);
-        if (!wave_solve_real(S.lu, S.dinv, S.perm, nt, rhs.p, x.p, 1, flags.p, err.p)) return -1;
+        launch_rhs(A, grid, eb);
+        if (!wave_solve_real(S.lu, S.dinv, S.perm, nt, rhs.p, x.p, nrun, flags.p, err.p)) return -1;
         if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
     }
     if (A.probes && n_steps > 0) {
         A.record_row = n_steps - 1;
         PEEC_LAUNCH(k_transient_probe, 1, 256, 0, A);
     }
-    cudaMemcpyAsync(d_I, x.p, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(d_V, x.p + ne, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(d_X, x.p, sizeof(double) * nt * nrun, cudaMemcpyDeviceToDevice, st);
     int herr = 0;
     cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (!launch_ok("transient steps") || !sync("transient steps")) return -1;
@@ -308,6 +363,14 @@ static int run_lightning(const TransientSystem &S, const LightningArgs &src, lon
         return -1;
     }
     return 0;
+}
+
+// lightning.c:66-171
+static bool source_ok(const TransientSystem &S, double K, double alpha, double beta, double delay, size_t strike,
+                      size_t ret) {
+    return isfinite(K) && K > 0.0 && isfinite(alpha) && isfinite(beta) && alpha > 0.0 && beta > 0.0 &&
+           beta > alpha && isfinite(delay) && delay >= 0.0 && strike < (size_t)S.nv && ret < (size_t)S.nv &&
+           strike != ret;
 }
 
 }  // namespace peec
@@ -341,20 +404,45 @@ int peec_gb300_transient_lightning(void *system, double K, double alpha, double 
         set_error("transient: missing system or state");
         return -1;
     }
-    // lightning.c:66-171
-    if (!isfinite(K) || K <= 0.0 || !isfinite(alpha) || !isfinite(beta) || alpha <= 0.0 || beta <= 0.0 ||
-        beta <= alpha || !isfinite(delay) || delay < 0.0 || strike_node >= (size_t)S->nv ||
-        return_node >= (size_t)S->nv || strike_node == return_node) {
-        set_error("transient: invalid lightning source (K > 0, 0 < alpha < beta, delay >= 0, two distinct nodes)");
+    DBuf<double> X((size_t)S->nt);
+    if (!X.p) return -1;
+    cudaMemcpyAsync(X.p, d_I, sizeof(double) * S->ne, cudaMemcpyDeviceToDevice, stream());
+    cudaMemcpyAsync(X.p + S->ne, d_V, sizeof(double) * S->nv, cudaMemcpyDeviceToDevice, stream());
+    size_t strike = strike_node, ret = return_node;
+    int s = peec_gb300_transient_lightning_batch(system, 1, &K, &alpha, &beta, &delay, &strike, &ret, step0, n_steps,
+                                                 X.p, d_probe_nodes, n_probe_nodes, d_probe_edges, n_probe_edges,
+                                                 d_probes);
+    if (s != 0) return s;
+    cudaMemcpyAsync(d_I, X.p, sizeof(double) * S->ne, cudaMemcpyDeviceToDevice, stream());
+    cudaMemcpyAsync(d_V, X.p + S->ne, sizeof(double) * S->nv, cudaMemcpyDeviceToDevice, stream());
+    return sync("transient state") ? 0 : -1;
+}
+
+int peec_gb300_transient_lightning_batch(void *system, int nrun, const double *K, const double *alpha,
+                                         const double *beta, const double *delay, const size_t *strike_node,
+                                         const size_t *return_node, size_t step0, size_t n_steps, double *d_X,
+                                         const int *d_probe_nodes, size_t n_probe_nodes, const int *d_probe_edges,
+                                         size_t n_probe_edges, double *d_probes) {
+    auto *S = static_cast<TransientSystem *>(system);
+    if (!S || !d_X || nrun < 1 || nrun > kMaxRuns || !K || !alpha || !beta || !delay || !strike_node ||
+        !return_node) {
+        set_error("transient: missing system, state or sources (1 to 8 runs)");
         return -1;
+    }
+    LightningArgs src[kMaxRuns];
+    for (int r = 0; r < nrun; ++r) {
+        if (!source_ok(*S, K[r], alpha[r], beta[r], delay[r], strike_node[r], return_node[r])) {
+            set_error("transient: invalid lightning source (K > 0, 0 < alpha < beta, delay >= 0, two distinct nodes)");
+            return -1;
+        }
+        src[r] = LightningArgs{K[r], alpha[r], beta[r], delay[r], (int)strike_node[r], (int)return_node[r]};
     }
     if ((n_probe_nodes && !d_probe_nodes) || (n_probe_edges && !d_probe_edges) ||
         ((n_probe_nodes || n_probe_edges) && !d_probes) || n_probe_nodes + n_probe_edges > (1u << 20)) {
         set_error("transient: probe arrays missing");
         return -1;
     }
-    LightningArgs src{K, alpha, beta, delay, (int)strike_node, (int)return_node};
-    return run_lightning(*S, src, (long long)step0, (long long)n_steps, d_I, d_V, d_probe_nodes, (int)n_probe_nodes,
+    return run_lightning(*S, src, nrun, (long long)step0, (long long)n_steps, d_X, d_probe_nodes, (int)n_probe_nodes,
                          d_probe_edges, (int)n_probe_edges, d_probes);
 }
 

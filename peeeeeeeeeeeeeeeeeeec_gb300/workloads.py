@@ -12,6 +12,8 @@ reference's).
   size chosen so that the unknown count N = Ne + Nv is near a U(lo, hi) draw.
 * harmonic_requests: frequency U(1, 100) MHz, 1-64 plane waves with random
   directions and transverse polarisations, Poisson arrival times.
+* batch_systems: every mesh of a pool at log-spaced frequencies with a
+  fixed number of plane waves (the many-meshes x many-frequencies sweep).
 """
 import numpy as np
 
@@ -92,3 +94,15 @@ def harmonic_requests(seed, n_meshes, rate_hz, window_s, max_rhs=64):
         q = int(rng.integers(1, max_rhs + 1))
         k, e = plane_waves(rng, q)
         out.append((t, int(rng.integers(0, n_meshes)), float(rng.uniform(1e6, 100e6)), k, e))
+
+
+def batch_systems(seed, n_meshes, n_freqs, f_lo=1e3, f_hi=1e8, nrhs=4):
+    """[(mesh index, frequency, k_hat (nrhs, 3), e_hat (nrhs, 3))] for every
+    mesh at n_freqs log-spaced frequencies in [f_lo, f_hi]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for mi in range(n_meshes):
+        for f in np.logspace(np.log10(f_lo), np.log10(f_hi), n_freqs):
+            k, e = plane_waves(rng, nrhs)
+            out.append((mi, float(f), k, e))
+    return out

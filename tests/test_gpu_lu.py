@@ -179,3 +179,46 @@ def test_solve_with_caller_built_factor(gpu_lib):
     assert gpu_lib.lu_solve(C.byref(g), dp(b), dp(x)) == 0
     assert np.array_equal(x, b)
     f.free()
+
+
+_PANEL_PROBE = r"""
+import ctypes as C, hashlib, sys
+import numpy as np
+sys.path.insert(0, {repo!r}); sys.path.insert(0, {tests!r})
+from helpers import ComplexLU, RealLU
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+lib = abi.load_gpu_lib()
+rng = np.random.default_rng(5)
+h = hashlib.sha256()
+for n in (700, 1500):
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    f = ComplexLU(lib, a)
+    lu, piv, rs, cs = f.factors()
+    h.update(lu.tobytes()); h.update(piv.tobytes()); f.free()
+    r = RealLU(lib, a.real)
+    lu, piv = r.factors()
+    h.update(lu.tobytes()); h.update(piv.tobytes()); r.free()
+print(h.hexdigest())
+"""
+
+
+def test_cluster_and_grid_panels_agree():
+    """The cooperative grid panel (default) and the thread-block-cluster
+    panel (PEEC_GB300_PANEL=cluster) make the same pivot choices and the same
+    arithmetic: the factors agree bit for bit."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = _PANEL_PROBE.format(repo=os.path.dirname(here), tests=here)
+    out = {}
+    for mode in ("cluster", "grid"):
+        env = dict(os.environ)
+        if mode == "cluster":
+            env["PEEC_GB300_PANEL"] = "cluster"
+        else:
+            env.pop("PEEC_GB300_PANEL", None)
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out[mode] = r.stdout.strip()
+    assert out["cluster"] == out["grid"]

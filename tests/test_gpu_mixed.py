@@ -132,3 +132,45 @@ def test_fp32_far_field_assembly_error(gpu_lib, oracle):
         # and the default mode is back to FP64-accurate
         s, L2 = inductance(gpu_lib, m)
         assert np.max(np.abs(L2[nz] - Lo[nz]) / np.abs(Lo[nz])) < 1e-12
+
+
+def test_fp64_refinement_reaches_the_gate_at_low_frequency(gpu_lib):
+    """At 1 kHz the MNA matrix of a small box is badly conditioned and the
+    plain FP64 LU solution misses the 1e-10 backward-error gate on some right-
+    hand sides; FP64 iterative refinement with the same factor reaches it."""
+    with SynthMesh.box(0.4, 0.2, 0.1, 8, 4, 2) as m:
+        ne, nv = m.n_edges, m.n_nodes
+        n = ne + nv
+        lo = abi.InductanceOptions()
+        gpu_lib.inductance_options_default(C.byref(lo), 1)
+        po = abi.PotentialOptions()
+        gpu_lib.potential_options_default(C.byref(po), 1)
+        dL = gpu_lib.peec_gb300_device_alloc(ne * ne * 8)
+        dP = gpu_lib.peec_gb300_device_alloc(nv * nv * 8)
+        dZ = gpu_lib.peec_gb300_device_alloc(n * n * 16)
+        dE = dev_put(gpu_lib, np.ascontiguousarray(m.edges()))
+        assert gpu_lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(lo), dL, None) == 0
+        assert gpu_lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(po), dP, None) == 0
+        assert gpu_lib.peec_gb300_harmonic_build_device(dL, dP, dE, None, ne, nv, 1e3, dZ) == 0
+    rng = np.random.default_rng(9)
+    B = np.zeros((4, n), dtype=np.complex128)
+    B[:, :ne] = rng.standard_normal((4, ne)) + 1j * rng.standard_normal((4, ne))
+    dB, dX = dev_put(gpu_lib, B), gpu_lib.peec_gb300_device_alloc(B.nbytes)
+    dLU = gpu_lib.peec_gb300_device_alloc(n * n * 16)
+    assert gpu_lib.peec_gb300_copy_device(dLU, dZ, n * n * 16) == 0
+    piv, perm = gpu_lib.peec_gb300_device_alloc(n * 8), gpu_lib.peec_gb300_device_alloc(n * 4)
+    rs, cs = gpu_lib.peec_gb300_device_alloc(n * 8), gpu_lib.peec_gb300_device_alloc(n * 8)
+    sc, col = C.c_double(), C.c_int()
+    assert gpu_lib.peec_gb300_complex_lu_factor_device(dLU, n, 1e-14, piv, perm, rs, cs, C.byref(sc), C.byref(col)) == 0
+    assert gpu_lib.peec_gb300_complex_lu_solve_device(dLU, perm, rs, cs, n, dB, dX, 4) == 0
+    be, it = C.c_double(), C.c_int()
+    s = gpu_lib.peec_gb300_complex_refine_device(dZ, dLU, perm, rs, cs, n, dB, dX, 4, 1e-10, 5, C.byref(be), C.byref(it))
+    X = np.zeros_like(B)
+    gpu_lib.peec_gb300_copy_to_host(X.ctypes.data, dX, X.nbytes)
+    Z = np.zeros((n, n), dtype=np.complex128)
+    gpu_lib.peec_gb300_copy_to_host(Z.ctypes.data, dZ, Z.nbytes)
+    for p in (dL, dP, dZ, dE, dB, dX, dLU, piv, perm, rs, cs):
+        gpu_lib.peec_gb300_device_free(p)
+    assert s == 0, (be.value, it.value)
+    for q in range(4):
+        assert backward_error(Z, X[q], B[q]) <= 1e-10

@@ -185,3 +185,33 @@ def test_transient_requests_alone_and_in_the_mix(gpu_lib, meshes):
         assert rb["status"] == 0
         assert np.array_equal(pb, probes) and np.array_equal(Ib, I)
     assert all(h[1]["status"] == 0 for h in hs)
+
+
+def test_queued_transient_runs_are_batched(gpu_lib, meshes):
+    """Lightning runs that queue up behind other work on the same system are
+    stepped together by one worker; each still equals its own direct run."""
+    from test_gpu_transient import DeviceTransient
+    from helpers import inductance, potential
+    m = meshes[0]
+    srcs = [(102900.0, 1500.0, 1.0e6, 0.0, 3, 20), (105139.0, 2127.18, 246066.0, 0.0, 7, 0),
+            (6.0e4, 1800.0, 4.0e5, 1e-7, 12, 25)]
+    pn, pe = [0, 3, 20], [1, 5]
+    s1, L = inductance(gpu_lib, m)
+    s2, P = potential(gpu_lib, m)
+    direct = DeviceTransient(gpu_lib, L, P, m.edges(), None, 2, 1e-7)
+    try:
+        ref = [direct.run(src, 200, probe_nodes=pn, probe_edges=pe) for src in srcs]
+    finally:
+        direct.close()
+    r = requests()[0]
+    with Server(8 * GB, 1) as srv:
+        busy = srv.submit(meshes[r["mesh"]], r["mesh"], r["frequency"], r["k_hat"], r["e_hat"], mixed=r["mixed"])
+        tt = [srv.submit_transient(m, 0, 200, src, probe_nodes=pn, probe_edges=pe) for src in srcs]
+        outs = [srv.wait(t) for t in tt]
+        srv.wait(busy)
+    starts = {o[1]["t_start"] for o in outs}
+    assert len(starts) <= 2  # the queued runs started together with the first or right after it
+    for (pb, Ib, Vb), rb in outs:
+        assert rb["status"] == 0
+    for ((pb, Ib, Vb), rb), (s, I, V, p) in zip(outs, ref):
+        assert np.array_equal(pb, p) and np.array_equal(Ib, I) and np.array_equal(Vb, V)

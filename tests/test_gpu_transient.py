@@ -167,3 +167,40 @@ def test_invalid_inputs(gpu_lib):
         assert s == 0 and np.isfinite(probes[:, 0]).all() and np.isnan(probes[:, 1:]).all()
     finally:
         t.close()
+
+
+def test_batched_runs_equal_single_runs(gpu_lib):
+    """Three runs with different sources stepped together (one right-hand
+    side kernel and one wavefront solve per step for all) give each run's
+    single-run waveforms bit for bit; bad sources and run counts are refused."""
+    f, g = golden("box421"), golden("transient_box421")
+    ne, nv = f["L"].shape[0], f["P"].shape[0]
+    nt = ne + nv
+    srcs = [(102900.0, 1500.0, 1.0e6, 0.0, 0, 5), (105139.0, 2127.18, 246066.0, 2e-7, 3, 17),
+            (5.0e4, 1000.0, 5.0e5, 0.0, 11, 2)]
+    t = DeviceTransient(gpu_lib, f["L"], f["P"], f["edges"], g["R"], 2, 1e-7)
+    try:
+        single = [t.run(src, 120, probe_nodes=range(nv), probe_edges=range(ne)) for src in srcs]
+        n = len(srcs)
+        X = np.zeros((n, nt))
+        dX = t.put(X)
+        pn, pe = t.put(np.arange(nv, dtype=np.int32)), t.put(np.arange(ne, dtype=np.int32))
+        dpr = gpu_lib.peec_gb300_device_alloc(120 * n * nt * 8)
+        t.bufs.append(dpr)
+        col = lambda k: (C.c_double * n)(*[s[k] for s in srcs])
+        sz = lambda k: (C.c_size_t * n)(*[s[k] for s in srcs])
+        st = gpu_lib.peec_gb300_transient_lightning_batch(t.h, n, col(0), col(1), col(2), col(3), sz(4), sz(5), 0, 120,
+                                                          dX, pn, nv, pe, ne, dpr)
+        assert st == 0
+        probes = np.zeros((120, n, nt))
+        gpu_lib.peec_gb300_copy_to_host(probes.ctypes.data, dpr, probes.nbytes)
+        gpu_lib.peec_gb300_copy_to_host(X.ctypes.data, dX, X.nbytes)
+        for r, (s, I, V, p1) in enumerate(single):
+            assert s == 0
+            assert np.array_equal(probes[:, r, :], p1)
+            assert np.array_equal(X[r, :ne], I) and np.array_equal(X[r, ne:], V)
+        bad = gpu_lib.peec_gb300_transient_lightning_batch(t.h, 9, col(0), col(1), col(2), col(3), sz(4), sz(5), 0, 5,
+                                                           dX, None, 0, None, 0, None)
+        assert bad == -1
+    finally:
+        t.close()
