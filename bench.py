@@ -222,6 +222,7 @@ class DeviceSolve:
             for f in ("ms_prepare", "ms_near", "ms_far"):
                 self.phase_ms.setdefault(tag + "_" + f[3:], []).append(getattr(st, f))
         self.work = {"Lp_near_pairs": self.stL.near_pairs, "Lp_near_pairs_evaluated": self.stL.near_pairs_evaluated,
+                     "Lp_near_pairs_reevaluated": self.stL.near_pairs_reevaluated,
                      "P_near_pairs_evaluated": self.stP.near_pairs_evaluated,
                      "Lp_potential_evals": self.stL.potential_evaluations,
                      "Lp_far_point_pairs": self.stL.far_point_pairs,

@@ -29,6 +29,8 @@ typedef struct
     unsigned long long potential_evaluations;  /* analytic triangle-potential evaluations     */
     unsigned long long far_point_pairs;        /* far-rule 1/R point pairs (FAR patch pairs x (2q^2)^2) */
     unsigned long long near_pairs_evaluated;   /* near pairs integrated (the rest reuse a translated copy) */
+    unsigned long long near_pairs_reevaluated; /* of those: copies integrated again because their
+                                                  representative's adaptive decisions were marginal */
     double ms_prepare;                         /* patch prep + near-pair discovery (CUDA events) */
     double ms_near;                            /* adaptive near-field kernels                 */
     double ms_far;                             /* tiled far-field + combine kernel            */

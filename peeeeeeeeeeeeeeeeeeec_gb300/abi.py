@@ -159,6 +159,7 @@ DROP_IN_SYMBOLS = [
 class PeecAssemblyStats(C.Structure):
     _fields_ = [("near_pairs", C.c_ulonglong), ("potential_evaluations", C.c_ulonglong),
                 ("far_point_pairs", C.c_ulonglong), ("near_pairs_evaluated", C.c_ulonglong),
+                ("near_pairs_reevaluated", C.c_ulonglong),
                 ("ms_prepare", C.c_double), ("ms_near", C.c_double), ("ms_far", C.c_double)]
 
 

@@ -1297,9 +1297,13 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
                 A.trace_len = nullptr;
                 launch_eval(nre);
             }
-            if (stats) stats->near_pairs_evaluated = (unsigned long long)(njobrec + nre);
+            if (stats) {
+                stats->near_pairs_evaluated = (unsigned long long)(njobrec + nre);
+                stats->near_pairs_reevaluated = (unsigned long long)nre;
+            }
         } else if (stats) {
             stats->near_pairs_evaluated = (unsigned long long)nrec;
+            stats->near_pairs_reevaluated = 0;
         }
         PEEC_LAUNCH(k_near_finalize, (nrec + 127) / 128, 128, 0, nrec, slot.p, kindbuf.p, kval.p);
         if (job_rec) PEEC_LAUNCH(k_memo_scatter, (nrec + 255) / 256, 256, 0, nrec, mrep.p, rflag.p, kval.p);
@@ -1414,15 +1418,22 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_retard_tiles(RetardArgs T) 
         int a = ta * kTile + r, b = tb * kTile + c;
         Cplx val = {0.0, 0.0};
         if (a < n && b < n && !(ta == tb && c < r)) {
-            double scale;
-            if (T.kind == KIND_INDUCTANCE) {
-                double dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
-                scale = fabs(dot) < T.dir_tol ? 0.0 : kMu0Over4Pi * dot / (R.scale[a] * R.scale[b]);
-            } else {
-                scale = kInv4PiEps0 / (R.scale[a] * R.scale[b]);
+            // the entry's FP64 scale in lane 0 only: FP64 instructions are
+            // scarce on GB300, the point loop below is all FP32
+            double scale = 0.0;
+            int skip = 0;
+            if (lane == 0) {
+                if (T.kind == KIND_INDUCTANCE) {
+                    double dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
+                    scale = fabs(dot) < T.dir_tol ? 0.0 : kMu0Over4Pi * dot / (R.scale[a] * R.scale[b]);
+                } else {
+                    scale = kInv4PiEps0 / (R.scale[a] * R.scale[b]);
+                }
+                skip = scale == 0.0 || T.k == 0.0f;
             }
+            skip = __shfl_sync(0xffffffffu, skip, 0);
             float fre = 0.0f, fim = 0.0f;
-            if (scale != 0.0 && T.k != 0.0f)
+            if (!skip)
                 for (int i = R.off[a]; i < R.off[a + 1]; ++i)
                     for (int j = R.off[b]; j < R.off[b + 1]; ++j)
                         retard_pair(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, T.k, fre, fim);
@@ -1431,8 +1442,10 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_retard_tiles(RetardArgs T) 
                 fre += __shfl_xor_sync(0xffffffffu, fre, m);
                 fim += __shfl_xor_sync(0xffffffffu, fim, m);
             }
-            val.re = T.stat[(size_t)a * n + b] + scale * (double)fre;
-            val.im = scale * (double)fim;
+            if (lane == 0) {
+                val.re = T.stat[(size_t)a * n + b] + scale * (double)fre;
+                val.im = scale * (double)fim;
+            }
         }
         if (lane == 0) tile[r][c] = val;
     }

@@ -2371,6 +2371,32 @@ __global__ void k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int c
     q[5 * KW + c] = rh;
 }
 
+// N = I - L^-1 for the unit lower triangle L = a[K0 + i][K0 + k] (i, k < kw,
+// kw <= 256), FP32 complex, row-major kw x kw: one warp per column c solves
+// L x = e_c by forward substitution (lane-parallel dot products, FP32
+// shuffles); N is strictly lower (N[i][c] = -x_i for i > c).
+__global__ void __launch_bounds__(256) k_lower_inv(const cplxf *a, int n, int K0, int kw, cplxf *N) {
+    __shared__ cplxf xs[8][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * 8 + warp;
+    if (c >= kw) return;
+    cplxf *x = xs[warp];
+    for (int i = lane; i < kw; i += 32) x[i] = cplxf{i == c ? 1.0f : 0.0f, 0.0f};
+    __syncwarp();
+    for (int i = c + 1; i < kw; ++i) {
+        const cplxf *li = a + (size_t)(K0 + i) * n + K0;
+        cplxf s = {0.0f, 0.0f};
+        for (int k = c + lane; k < i; k += 32) s = mac(s, li[k], x[k]);
+        s = warp_sum_t(s);
+        if (lane == 0) x[i] = cplxf{-s.re, -s.im};
+        __syncwarp();
+    }
+    for (int i = lane; i < kw; i += 32) {
+        cplxf v = i > c ? cplxf{-x[i].re, -x[i].im} : cplxf{0.0f, 0.0f};
+        N[(size_t)i * kw + c] = v;
+    }
+}
+
 // y = P D_r^-1 r in FP32 (the permuted, row-scaled residual)
 __global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int n, int nrhs, cplxf *y) {
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -2528,6 +2554,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     // the bulk of the trailing update runs with K = 6 x 256 on the tensor cores
     const int OB = 256;
     DBuf<__nv_bfloat16> ap((size_t)n * 6 * OB), bpr((size_t)n * 6 * OB), bpi((size_t)n * 6 * OB);
+    DBuf<cplxf> linv((size_t)OB * OB);  // I - L11^-1 of one outer block
     DBuf<unsigned char> scratch;
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -2535,7 +2562,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     const size_t G = (size_t)sms;
     size_t sbytes = 256 + 2 * G * 8 + 2 * G * 4 + 16 + 2 * G * NB * sizeof(cplxf) + 2 * NB * sizeof(cplxf) + 64;
     if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
-        !bpr.p || !bpi.p || !scratch.alloc(sbytes))
+        !bpr.p || !bpi.p || !linv.p || !scratch.alloc(sbytes))
         return -1;
     cudaEvent_t ev[4];
     for (auto &e : ev) cudaEventCreate(&e);
@@ -2575,6 +2602,19 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     LuTiming &tm = g_lu_timing;
     if (tm.enabled) tm.reset();
     // C[row0.., col0..] -= L[row0.., kc..kc+kw) U[kc..kc+kw, col0..), split-BF16x3
+    // (the L operand may come from another matrix: lsrc with leading dimension
+    // ld, its rows lrow0.., columns lcol0..)
+    auto tc_update_from = [&](const cplxf *lsrc, int ld, int lrow0, int lcol0, int row0, int m, int col0, int nc,
+                              int kc, int kw) -> bool {
+        if (m <= 0 || nc <= 0) return true;
+        const int KW = (kw + 31) / 32 * 32;
+        PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
+                    ap.p);
+        PEEC_LAUNCH(k_split_b, (unsigned)(((long long)nc * KW + 255) / 256), 256, 0, a, n, kc, kw, KW, col0, nc,
+                    bpr.p, bpi.p);
+        if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
+        return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
+    };
     auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw) -> bool {
         if (m <= 0 || nc <= 0) return true;
         const int KW = (kw + 31) / 32 * 32;
@@ -2616,14 +2656,13 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             if (!tc_update(k0 + kb, n - (k0 + kb), k0 + kb, rin, k0, kb)) return -1;
         }
         if (E < n) {
-            // U12 of the outer block for the columns right of it, block by block
-            for (int k0 = K0; k0 < E; k0 += NB) {
-                const int kb = std::min(NB, E - k0);
-                PEEC_LAUNCH(k_trsm<cplxf>, (n - E + 255) / 256, 256, 0, a, n, k0, kb, E, n, st.p);
-                tm.mark(1);
-                if (!tc_update(k0 + kb, E - (k0 + kb), E, n - E, k0, kb)) return -1;
-                tm.mark(2);
-            }
+            // U12 of the outer block for the columns right of it in one
+            // tensor-core update: U12 = L11^-1 A12 = A12 - (I - L11^-1) A12
+            const int kw = E - K0;
+            PEEC_LAUNCH(k_lower_inv, (kw + 7) / 8, 256, 0, a, n, K0, kw, linv.p);
+            tm.mark(1);
+            if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
+            tm.mark(2);
             // trailing update with K = 6 x (E - K0)
             if (!tc_update(E, n - E, E, n - E, K0, E - K0)) return -1;
         }
