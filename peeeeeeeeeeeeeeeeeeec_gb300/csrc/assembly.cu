@@ -659,31 +659,50 @@ __global__ void k_memo_compact(int nrec, const int *is_rep, const int *off, int 
     list[off[r]] = r;
 }
 
-// Copies of a representative with an accept decision near its threshold
-// (or an overflowing trace) are evaluated on their own.
-__global__ void k_memo_recheck(int nrec, const int *rep, const int *marginal, int *flag) {
+// ---- multi-round reuse ------------------------------------------------
+// A copy whose replay of its representative's trace fails takes the
+// representative's value only if it follows the same subdivision tree, so
+// copies that fail are regrouped by (representative, first divergence:
+// job, trace position, the copy's own edge choice); each new group's
+// lowest record is integrated with traces on, and the remaining members
+// replay against it -- a few rounds settle almost every tie pattern, and
+// what is left is integrated directly.  src[r] is the record whose value r
+// takes (r itself when integrated).
+static const int kNoFail = 0x7fffffff;
+
+// copies whose representative was integrated in this round: classify
+__global__ void k_round_classify(int nrec, const int *rep, const int *rep_pos, const int *marginal, int *src,
+                                 int *eval, int *replay, int *fcode) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
+    replay[r] = 0;
+    if (src[r] >= 0) return;  // decided (a representative or an earlier round)
     int r0 = rep[r];
-    flag[r] = (r0 != r && (marginal[r0] & (MARG_THRESHOLD | MARG_TRACE_FULL))) ? 1 : 0;
+    if (r0 == r || rep_pos[r0] < 0) return;  // representative not integrated in this round
+    int m = marginal[r0];
+    if (m & (MARG_THRESHOLD | MARG_TRACE_FULL)) {
+        src[r] = r;
+        eval[r] = 1;
+    } else if (!(m & MARG_TIE)) {
+        src[r] = r0;
+    } else {
+        replay[r] = 1;
+        fcode[r] = kNoFail;
+    }
 }
 
-// Copies of a representative whose only marginal decisions are bisection-
-// edge ties replay the representative's decision trace on their own
-// corners (geometry only, one thread per job): the copy reuses the value
-// only if it bisects the same edge at every refined node, i.e. follows the
-// same subdivision tree.
-__global__ void k_memo_replay(int nrec, const int *rep, const int *marginal, const int *rep_pos,
-                              const double *corner, const NearRec *rec, const unsigned char *trace,
-                              const int *trace_len, int *flag) {
+// replay of the representative's trace per (record, job); the first
+// divergence (lowest job, then trace position) goes to fcode
+__global__ void k_round_replay(int nrec, const int *rep, const int *rep_pos, const int *replay, const double *corner,
+                               const NearRec *rec, const unsigned char *trace, const int *trace_len, int *fcode) {
     long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= (long long)nrec * 8) return;
-    int r = (int)(g >> 3), t = (int)((g >> 1) & 3), d = (int)(g & 1);
+    int r = (int)(g >> 3), jb = (int)(g & 7), t = jb >> 1, d = jb & 1;
+    if (!replay[r]) return;
     int r0 = rep[r];
-    if (r0 == r || !(marginal[r0] & MARG_TIE) || (marginal[r0] & (MARG_THRESHOLD | MARG_TRACE_FULL))) return;
-    long long job = (long long)rep_pos[r0] * 8 + t * 2 + d;
+    long long job = (long long)rep_pos[r0] * 8 + jb;
     int len = trace_len[job];
-    if (len <= 0) return;
+    if (len <= 0) return;  // zero-area or identical triangles: no subdivision
     const unsigned char *tr = trace + (size_t)job * kTraceCap;
     NearRec q = rec[r];
     double ta[9], tb[9];
@@ -691,31 +710,34 @@ __global__ void k_memo_replay(int nrec, const int *rep, const int *marginal, con
     patch_triangle(corner + 12 * (size_t)q.j, t & 1, tb);
     double stack[kStackCap][9];
     for (int k = 0; k < 9; ++k) stack[0][k] = d == 0 ? ta[k] : tb[k];
-    int sp = 1, pos = 0;
-    bool ok = true;
+    int sp = 1, pos = 0, code = kNoFail;
     while (sp > 0) {
         double v[9];
         --sp;
         for (int k = 0; k < 9; ++k) v[k] = stack[sp][k];
         if (pos >= len) {
-            ok = false;
+            code = (jb << 12) | (pos << 2) | 3;
             break;
         }
-        unsigned char c = tr[pos++];
-        if (c == kAccept) continue;
+        unsigned char c = tr[pos];
+        if (c == kAccept) {
+            ++pos;
+            continue;
+        }
         int e = 0;
         double longest = 0.0;
         for (int i = 0; i < 3; ++i) {
-            double s = dist3(v + 3 * i, v + 3 * ((i + 1) % 3));
-            if (s > longest) {
-                longest = s;
+            double sl = dist3(v + 3 * i, v + 3 * ((i + 1) % 3));
+            if (sl > longest) {
+                longest = sl;
                 e = i;
             }
         }
         if (e != (int)c || sp + 2 > kStackCap) {
-            ok = false;
+            code = (jb << 12) | (pos << 2) | (e & 3);
             break;
         }
+        ++pos;
         int j = (e + 1) % 3, k = (e + 2) % 3;
         double *left = stack[sp + 1], *right = stack[sp];
         for (int dd = 0; dd < 3; ++dd) {
@@ -729,15 +751,91 @@ __global__ void k_memo_replay(int nrec, const int *rep, const int *marginal, con
         }
         sp += 2;
     }
-    if (pos != len) ok = false;
-    if (!ok) atomicOr(flag + r, 1);
+    if (code == kNoFail && pos != len) code = (jb << 12) | (pos << 2) | 3;
+    if (code != kNoFail) atomicMin(fcode + r, code);
 }
 
-__global__ void k_memo_scatter(int nrec, const int *rep, const int *flag, double2 *kval) {
+// after the replay: reuse, or join a new group keyed by (rep, fcode)
+__global__ void k_round_regroup(int nrec, const int *replay, const int *fcode, const int *rep, int *src, int *failed,
+                                unsigned long long *key) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
-    int r0 = rep[r];
-    if (r0 != r && !flag[r]) kval[r] = kval[r0];
+    failed[r] = 0;
+    if (!replay[r]) return;
+    if (fcode[r] == kNoFail) {
+        src[r] = rep[r];
+        return;
+    }
+    failed[r] = 1;
+    key[r] = ((unsigned long long)(unsigned)rep[r] << 32) | (unsigned)fcode[r];
+}
+
+// exact-key hash insert of the failed records: lowest record per key
+struct RoundSlot {
+    unsigned long long key;  // ~0 = empty
+    int rep;
+    int pad;
+};
+__global__ void k_round_insert(int nrec, const int *failed, const unsigned long long *key, RoundSlot *tab,
+                               unsigned long long mask, int *slot_of) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec || !failed[r]) return;
+    unsigned long long kk = key[r], s = mix64(0x51ull, kk) & mask;
+    for (unsigned long long probe = 0; probe <= mask; ++probe) {  // bounded: the table is never full
+        unsigned long long prev = atomicCAS(&tab[s].key, ~0ull, kk);
+        if (prev == ~0ull || prev == kk) {
+            atomicMin(&tab[s].rep, r);
+            slot_of[r] = (int)s;
+            return;
+        }
+        s = (s + 1) & mask;
+    }
+    slot_of[r] = -1;
+}
+
+// new representatives of the failed records (integrated next, src = self)
+__global__ void k_round_resolve(int nrec, const int *failed, const RoundSlot *tab, const int *slot_of, int *rep,
+                                int *src, int *is_new, int *eval) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    is_new[r] = 0;
+    if (!failed[r]) return;
+    if (slot_of[r] < 0) {  // (cannot happen: the table has 4x the records) integrate directly
+        src[r] = r;
+        eval[r] = 1;
+        return;
+    }
+    int r0 = tab[slot_of[r]].rep;
+    rep[r] = r0;
+    if (r0 == r) {
+        src[r] = r;
+        is_new[r] = 1;
+    }
+}
+
+// representatives integrated in round 1 take their own value
+__global__ void k_round_self(int nrec, const int *rep_pos, int *src) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nrec && rep_pos[r] >= 0) src[r] = r;
+}
+
+__global__ void k_round_fail_to_eval(int nrec, const int *failed, int *src, int *eval) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec || !failed[r]) return;
+    src[r] = r;
+    eval[r] = 1;
+}
+
+__global__ void k_round_scatter(int nrec, const int *src, double2 *kval) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    int s = src[r];
+    if (s >= 0 && s != r) kval[r] = kval[s];
+}
+
+__global__ void k_round_positions(const int *list, int n, int *pos) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pos[list[i]] = i;
 }
 
 // ---------------------------------------------------------------------
@@ -1274,39 +1372,95 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
             if (grid > 0) PEEC_LAUNCH(k_near_eval, grid, 256, smem, A);
         };
         launch_eval(njobrec);
-        DBuf<int> rflag, roff, rlist;
+        DBuf<int> src, evalf, rpos, replay, fcode, failed, slot_of2, isnew, off2, list2, elist;
+        DBuf<unsigned long long> key2;
+        DBuf<RoundSlot> tab2;
+        unsigned long long evaluated = (unsigned long long)njobrec;
         if (job_rec) {
-            // second pass: copies of representatives with a marginal decision
-            unsigned g = (nrec + 255) / 256;
-            if (!rflag.alloc(nrec) || !roff.alloc(nrec + 1)) return -1;
-            PEEC_LAUNCH(k_memo_recheck, g, 256, 0, nrec, mrep.p, marginal.p, rflag.p);
-            PEEC_LAUNCH(k_memo_replay, (unsigned)(((long long)nrec * 8 + 127) / 128), 128, 0, nrec, mrep.p,
-                        marginal.p, moff.p, R.corner, rec.p, trace.p, trace_len.p, rflag.p);
-            PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, rflag.p, roff.p, nrec);
+            const unsigned g = (nrec + 255) / 256;
+            unsigned long long cap = 1;
+            while (cap < 4ull * (unsigned long long)nrec) cap <<= 1;
+            if (!src.alloc(nrec) || !evalf.alloc(nrec) || !rpos.alloc(nrec) || !replay.alloc(nrec) ||
+                !fcode.alloc(nrec) || !failed.alloc(nrec) || !slot_of2.alloc(nrec) || !isnew.alloc(nrec) ||
+                !off2.alloc(nrec + 1) || !key2.alloc(nrec) || !tab2.alloc(cap))
+                return -1;
+            // round 1: the representatives just integrated decide for themselves
+            PEEC_LAUNCH(k_fill_int, g, 256, 0, src.p, (long long)nrec, 1, -1);
+            PEEC_LAUNCH(k_fill_int, g, 256, 0, rpos.p, (long long)nrec, 1, -1);
+            cudaMemsetAsync(evalf.p, 0, (size_t)nrec * sizeof(int), stream());
+            PEEC_LAUNCH(k_round_positions, (njobrec + 255) / 256, 256, 0, job_rec, njobrec, rpos.p);
+            PEEC_LAUNCH(k_round_self, g, 256, 0, nrec, rpos.p, src.p);
+            DBuf<unsigned char> rtrace;
+            DBuf<int> rtrace_len;
+            const unsigned char *cur_trace = trace.p;
+            const int *cur_len = trace_len.p;
+            const int kRounds = 6;
+            for (int round = 1; round <= kRounds; ++round) {
+                PEEC_LAUNCH(k_round_classify, g, 256, 0, nrec, mrep.p, rpos.p, marginal.p, src.p, evalf.p, replay.p,
+                            fcode.p);
+                PEEC_LAUNCH(k_round_replay, (unsigned)(((long long)nrec * 8 + 127) / 128), 128, 0, nrec, mrep.p,
+                            rpos.p, replay.p, R.corner, rec.p, cur_trace, cur_len, fcode.p);
+                PEEC_LAUNCH(k_round_regroup, g, 256, 0, nrec, replay.p, fcode.p, mrep.p, src.p, failed.p, key2.p);
+                if (round == kRounds) {
+                    // last round: what still fails is integrated directly
+                    PEEC_LAUNCH(k_round_fail_to_eval, g, 256, 0, nrec, failed.p, src.p, evalf.p);
+                    break;
+                }
+                cudaMemsetAsync(tab2.p, 0xff, cap * sizeof(RoundSlot), stream());
+                PEEC_LAUNCH(k_fill_int, (unsigned)((cap + 255) / 256), 256, 0, &tab2.p[0].rep, (long long)cap,
+                            (int)sizeof(RoundSlot) / (int)sizeof(int), 0x7fffffff);
+                PEEC_LAUNCH(k_round_insert, g, 256, 0, nrec, failed.p, key2.p, tab2.p, cap - 1, slot_of2.p);
+                PEEC_LAUNCH(k_round_resolve, g, 256, 0, nrec, failed.p, tab2.p, slot_of2.p, mrep.p, src.p, isnew.p,
+                            evalf.p);
+                PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, isnew.p, off2.p, nrec);
+                int nnew = 0;
+                cudaMemcpyAsync(&nnew, off2.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
+                if (!sync("near-pair reuse round")) return -1;
+                if (nnew == 0) break;
+                if (!list2.alloc(nnew) || !rtrace.alloc((size_t)nnew * 8 * kTraceCap) ||
+                    !rtrace_len.alloc((size_t)nnew * 8))
+                    return -1;
+                PEEC_LAUNCH(k_memo_compact, g, 256, 0, nrec, isnew.p, off2.p, list2.p);
+                PEEC_LAUNCH(k_fill_int, g, 256, 0, rpos.p, (long long)nrec, 1, -1);
+                PEEC_LAUNCH(k_round_positions, (nnew + 255) / 256, 256, 0, list2.p, nnew, rpos.p);
+                cudaMemsetAsync(rtrace_len.p, 0, (size_t)nnew * 8 * sizeof(int), stream());
+                cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
+                A.job_rec = list2.p;
+                A.nrec = nnew;
+                A.trace = rtrace.p;
+                A.trace_len = rtrace_len.p;
+                launch_eval(nnew);
+                evaluated += (unsigned long long)nnew;
+                cur_trace = rtrace.p;
+                cur_len = rtrace_len.p;
+            }
+            // records marked for direct integration
+            PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, evalf.p, off2.p, nrec);
             int nre = 0;
-            cudaMemcpyAsync(&nre, roff.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            cudaMemcpyAsync(&nre, off2.p + nrec, sizeof(int), cudaMemcpyDeviceToHost, stream());
             if (!sync("near-pair reuse check")) return -1;
             if (nre > 0) {
-                if (!rlist.alloc(nre)) return -1;
-                PEEC_LAUNCH(k_memo_compact, g, 256, 0, nrec, rflag.p, roff.p, rlist.p);
+                if (!elist.alloc(nre)) return -1;
+                PEEC_LAUNCH(k_memo_compact, g, 256, 0, nrec, evalf.p, off2.p, elist.p);
                 cudaMemsetAsync(counter.p, 0, sizeof(int), stream());
-                A.job_rec = rlist.p;
+                A.job_rec = elist.p;
                 A.nrec = nre;
                 A.marginal = nullptr;
                 A.trace = nullptr;
                 A.trace_len = nullptr;
                 launch_eval(nre);
+                evaluated += (unsigned long long)nre;
             }
             if (stats) {
-                stats->near_pairs_evaluated = (unsigned long long)(njobrec + nre);
-                stats->near_pairs_reevaluated = (unsigned long long)nre;
+                stats->near_pairs_evaluated = evaluated;
+                stats->near_pairs_reevaluated = evaluated - (unsigned long long)njobrec;
             }
         } else if (stats) {
             stats->near_pairs_evaluated = (unsigned long long)nrec;
             stats->near_pairs_reevaluated = 0;
         }
         PEEC_LAUNCH(k_near_finalize, (nrec + 127) / 128, 128, 0, nrec, slot.p, kindbuf.p, kval.p);
-        if (job_rec) PEEC_LAUNCH(k_memo_scatter, (nrec + 255) / 256, 256, 0, nrec, mrep.p, rflag.p, kval.p);
+        if (job_rec) PEEC_LAUNCH(k_round_scatter, (nrec + 255) / 256, 256, 0, nrec, src.p, kval.p);
     }
     cudaEventRecord(ev[2], stream());
     TileArgs T;

@@ -43,6 +43,7 @@
 namespace peec {
 
 static const int NB = 32;  // panel width
+static const int kPS = NB + 1;  // padded row stride of panel rows in shared memory
 
 struct cplx {
     double re, im;
@@ -305,7 +306,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
                                                     long long *piv, Status *st, PanelSlots *ps, double *cand_val,
                                                     int *cand_idx, T *cand_row, T *krow) {
     extern __shared__ unsigned char smem_raw[];
-    T *tile = reinterpret_cast<T *>(smem_raw);  // [rows_per_cta][NB]
+    T *tile = reinterpret_cast<T *>(smem_raw);  // [rows_per_cta][kPS] (padded rows: no bank conflicts)
     using M = typename MagType<T>::type;  // FP32 magnitudes for the FP32 factorisation
     M *cval = reinterpret_cast<M *>(cand_val);
     __shared__ T s_prow[NB];
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
     unsigned int gen = *(volatile unsigned int *)&ps->gen;  // stable between launches
     for (int t = tid; t < nrows * kb; t += blockDim.x) {
         int i = t / kb, j = t % kb;
-        tile[i * NB + j] = a[(size_t)(r0 + i) * n + k0 + j];
+        tile[i * kPS + j] = a[(size_t)(r0 + i) * n + k0 + j];
     }
     __syncthreads();
     for (int kk = 0; kk < kb; ++kk) {
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         M best = -1;
         int bi = n;
         for (int i = max(r0, k) + tid; i < r1; i += blockDim.x) {
-            M m = mag_t(tile[(i - r0) * NB + kk]);
+            M m = mag_t(tile[(i - r0) * kPS + kk]);
             if (i == k && isnan(m)) m = INFINITY;
             if (isnan(m)) continue;
             if (m > best || (m == best && i < bi)) {
@@ -369,9 +370,9 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         // publish the candidate row's segment and, if owned here, row k
         if (bi < n)
             for (int j = tid; j < kb; j += blockDim.x)
-                cand_row[((size_t)par * G + c) * NB + j] = tile[(bi - r0) * NB + j];
+                cand_row[((size_t)par * G + c) * NB + j] = tile[(bi - r0) * kPS + j];
         if (k >= r0 && k < r1)
-            for (int j = tid; j < kb; j += blockDim.x) krow[(size_t)par * NB + j] = tile[(k - r0) * NB + j];
+            for (int j = tid; j < kb; j += blockDim.x) krow[(size_t)par * NB + j] = tile[(k - r0) * kPS + j];
         if (!grid_barrier(ps, G, gen)) {
             if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
             return;
@@ -442,16 +443,16 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
         __syncthreads();
         if (p != k) {
             if (k >= r0 && k < r1)
-                for (int j = tid; j < kb; j += blockDim.x) tile[(k - r0) * NB + j] = s_prow[j];
+                for (int j = tid; j < kb; j += blockDim.x) tile[(k - r0) * kPS + j] = s_prow[j];
             if (p >= r0 && p < r1)
                 for (int j = tid; j < kb; j += blockDim.x)
-                    tile[(p - r0) * NB + j] = ld_volatile(krow + (size_t)par * NB + j);
+                    tile[(p - r0) * kPS + j] = ld_volatile(krow + (size_t)par * NB + j);
         }
         __syncthreads();
         if (k + 1 >= n) break;
         const T pivot = s_prow[kk];
         for (int i = max(r0, k + 1) + tid; i < r1; i += blockDim.x) {
-            T *row = tile + (i - r0) * NB;
+            T *row = tile + (i - r0) * kPS;
             T m = divide(row[kk], pivot);
             row[kk] = m;
             for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], m, s_prow[j]);
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
     }
     for (int t = tid; t < nrows * kb; t += blockDim.x) {
         int i = t / kb, j = t % kb;
-        a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
+        a[(size_t)(r0 + i) * n + k0 + j] = tile[i * kPS + j];
     }
 }
 
@@ -624,6 +625,291 @@ __global__ void __launch_bounds__(256) k_panel_cluster(T *a, int n, int k0, int 
         a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
     }
     cluster.sync();  // no CTA leaves while another may still read its slots
+}
+
+// ---- tournament-pivoting panel (mixed path) ----------------------------
+// Communication-avoiding LU of the FP32 panel (rows k0..n-1, columns
+// k0..k0+kb-1) with tournament pivoting: each CTA factors its own rows with
+// partial pivoting and nominates the rows it picked; groups of 8 CTAs
+// merge their nominees the same way, then CTA 0 merges the group winners and
+// factors the final pivot rows.  Four bounded grid barriers per panel
+// instead of one per column (plus one before the panel is written back).
+// The pivots differ from partial pivoting (so
+// this is used only by the FP32 factorisation, whose result is refined in
+// FP64); every non-pivot row becomes L21 = A21 U11^-1 from its original
+// values.  piv[] receives the equivalent sequential swaps.
+static const int kCaluGroup = 8;          // CTAs whose nominees one leader merges
+static const int kCaluRows = 256;         // rows per CTA in the first two phases (local rows, group nominees)
+static const int kCaluMaxRows = 640;      // group winners merged by CTA 0 (up to 160 CTAs)
+
+struct CaluScratch {
+    PanelSlots *ps;
+    cplxf *cand;     // [G][NB][NB] nominated rows (original values)
+    int *cand_idx;   // [G][NB] their rows, -1 = none
+    cplxf *cand2;    // [groups][NB][NB]
+    int *cand2_idx;  // [groups][NB]
+    cplxf *top;      // [NB][NB] factored pivot rows (L11 \ U11)
+    int *fpiv;       // [NB] final pivot rows in order
+};
+
+// Partial-pivoting LU of the m x kb block W (rows of NB in shared memory,
+// ids[] the rows they came from): after the call the first min(m, kb) rows
+// are the chosen pivot rows in order (ids permuted with them).  NaN never
+// wins; a row whose magnitude is NaN at the diagonal counts as +inf (as the
+// reference's panel).  All threads of the CTA call it.
+__device__ void calu_block_lu(cplxf *W, int *ids, int m, int kb) {
+    __shared__ float s_v[8];
+    __shared__ int s_i[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int steps = min(m, kb);
+    for (int j = 0; j < steps; ++j) {
+        float best = -1.0f;
+        int bi = m;
+        for (int r = j + tid; r < m; r += blockDim.x) {
+            float v = mag_t(W[r * kPS + j]);
+            if (r == j && isnan(v)) v = INFINITY;
+            if (isnan(v)) continue;
+            if (v > best || (v == best && r < bi)) {
+                best = v;
+                bi = r;
+            }
+        }
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            float ov = __shfl_xor_sync(0xffffffffu, best, sh);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_v[warp] = best;
+            s_i[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                if (s_v[w] > best || (s_v[w] == best && s_i[w] < bi)) {
+                    best = s_v[w];
+                    bi = s_i[w];
+                }
+            s_i[0] = bi < m ? bi : j;  // no candidate (all NaN): keep row j
+        }
+        __syncthreads();
+        const int p = s_i[0];
+        if (p != j) {
+            for (int c = tid; c < NB; c += blockDim.x) {
+                cplxf t = W[j * kPS + c];
+                W[j * kPS + c] = W[p * kPS + c];
+                W[p * kPS + c] = t;
+            }
+            if (tid == 0) {
+                int t = ids[j];
+                ids[j] = ids[p];
+                ids[p] = t;
+            }
+        }
+        __syncthreads();
+        const cplxf piv = W[j * kPS + j];
+        for (int r = j + 1 + tid; r < m; r += blockDim.x) {
+            cplxf *row = W + r * kPS;
+            cplxf l = divide(row[j], piv);
+            row[j] = l;
+            for (int c = j + 1; c < kb; ++c) row[c] = msub(row[c], l, W[j * kPS + c]);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_panel_calu(cplxf *a, int n, int k0, int kb, int rows_per_cta, double limit,
+                                                    long long *piv, Status *st, CaluScratch S) {
+    extern __shared__ __align__(16) unsigned char calu_smem[];
+    // W: work rows; O: the same rows' original values (phases 1-2 only, so
+    // phase 3 may use the whole buffer for W)
+    cplxf *W = reinterpret_cast<cplxf *>(calu_smem);                 // [kCaluMaxRows][kPS]
+    cplxf *O = W + kCaluRows * kPS;                                  // [kCaluRows][kPS]
+    int *ids = reinterpret_cast<int *>(W + kCaluMaxRows * kPS);      // [kCaluMaxRows]
+    __shared__ int s_prow[2 * NB], s_pos[2 * NB], s_nt;              // touched rows and where they end
+    __shared__ cplxf s_top[NB * NB];
+    const int tid = threadIdx.x;
+    const unsigned G = gridDim.x;
+    const int c = blockIdx.x;
+    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform (set before launch)
+    unsigned int gen = *(volatile unsigned int *)&S.ps->gen;
+    // 1. local partial pivoting on this CTA's rows, nominate its pivot rows
+    for (int t = tid; t < nrows * NB; t += blockDim.x) {
+        int i = t / NB, j = t % NB;
+        cplxf v = j < kb ? a[(size_t)(r0 + i) * n + k0 + j] : cplxf{0.0f, 0.0f};
+        W[i * kPS + j] = v;
+        O[i * kPS + j] = v;
+    }
+    for (int i = tid; i < nrows; i += blockDim.x) ids[i] = i;  // local index into O
+    __syncthreads();
+    calu_block_lu(W, ids, nrows, kb);
+    const int nc = min(nrows, kb);
+    for (int t = tid; t < NB * NB; t += blockDim.x) {
+        int i = t / NB, j = t % NB;
+        S.cand[((size_t)c * NB + i) * NB + j] = i < nc ? O[ids[i] * kPS + j] : cplxf{0.0f, 0.0f};
+    }
+    for (int i = tid; i < NB; i += blockDim.x) S.cand_idx[c * NB + i] = i < nc ? r0 + ids[i] : -1;
+    if (!grid_barrier(S.ps, G, gen)) {
+        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
+        return;
+    }
+    // 2. group leaders merge the nominees of their 8 CTAs
+    const int groups = (int)((G + kCaluGroup - 1) / kCaluGroup);
+    __shared__ int s_off[kCaluMaxRows / NB + 1];  // compaction offsets (phase 2: CTAs, phase 3: groups)
+    __shared__ int s_gr[kCaluMaxRows];  // global row of each gathered candidate
+    if (c % kCaluGroup == 0) {
+        const int g = c / kCaluGroup, nq = min((int)G, c + kCaluGroup) - c;
+        // valid nominees of CTA q are its first count(q) slots: compaction offsets
+        if (tid < nq) {
+            int cnt = 0;
+            for (int i = 0; i < NB; ++i) cnt += ld_volatile(S.cand_idx + (c + tid) * NB + i) >= 0;
+            s_off[tid + 1] = cnt;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_off[0] = 0;
+            for (int q = 0; q < nq; ++q) s_off[q + 1] += s_off[q];
+        }
+        __syncthreads();
+        const int m = s_off[nq];
+        for (int t = tid; t < nq * NB * NB; t += blockDim.x) {
+            const int q = t / (NB * NB), i = (t / NB) % NB, j = t % NB;
+            if (i < s_off[q + 1] - s_off[q]) {
+                cplxf v = ld_volatile(S.cand + ((size_t)(c + q) * NB + i) * NB + j);
+                W[(s_off[q] + i) * kPS + j] = v;
+                O[(s_off[q] + i) * kPS + j] = v;
+                if (j == 0) s_gr[s_off[q] + i] = ld_volatile(S.cand_idx + (c + q) * NB + i);
+            }
+        }
+        for (int i = tid; i < m; i += blockDim.x) ids[i] = i;
+        __syncthreads();
+        calu_block_lu(W, ids, m, kb);
+        const int w2 = min(m, kb);
+        for (int t = tid; t < NB * NB; t += blockDim.x) {
+            int i = t / NB, j = t % NB;
+            S.cand2[((size_t)g * NB + i) * NB + j] = i < w2 ? O[ids[i] * kPS + j] : cplxf{0.0f, 0.0f};
+        }
+        for (int i = tid; i < NB; i += blockDim.x) S.cand2_idx[g * NB + i] = i < w2 ? s_gr[ids[i]] : -1;
+    }
+    if (!grid_barrier(S.ps, G, gen)) {
+        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
+        return;
+    }
+    // 3. CTA 0 merges the group winners and factors the pivot rows
+    if (c == 0) {
+        if (tid < groups) {
+            int cnt = 0;
+            for (int i = 0; i < NB; ++i) cnt += ld_volatile(S.cand2_idx + tid * NB + i) >= 0;
+            s_off[tid + 1] = cnt;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_off[0] = 0;
+            for (int q = 0; q < groups; ++q) s_off[q + 1] += s_off[q];
+        }
+        __syncthreads();
+        const int m = s_off[groups];
+        for (int t = tid; t < groups * NB * NB; t += blockDim.x) {
+            const int q = t / (NB * NB), i = (t / NB) % NB, j = t % NB;
+            if (i < s_off[q + 1] - s_off[q]) {
+                W[(s_off[q] + i) * kPS + j] = ld_volatile(S.cand2 + ((size_t)q * NB + i) * NB + j);
+                if (j == 0) s_gr[s_off[q] + i] = ld_volatile(S.cand2_idx + q * NB + i);
+            }
+        }
+        for (int i = tid; i < m; i += blockDim.x) ids[i] = i;
+        __syncthreads();
+        calu_block_lu(W, ids, m, kb);
+        if (tid == 0) {
+            for (int i = 0; i < kb; ++i) {
+                const double dm = i < m ? (double)mag_t(W[i * kPS + i]) : 0.0;
+                if (i >= m || !isfinite(dm) || dm <= limit) {
+                    st->code = 2;
+                    st->column = k0 + i;
+                    st->value = dm;
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < NB * NB; t += blockDim.x) S.top[t] = W[(t / NB) * kPS + t % NB];
+        for (int i = tid; i < NB; i += blockDim.x) S.fpiv[i] = i < kb && i < m ? s_gr[ids[i]] : -1;
+    }
+    if (!grid_barrier(S.ps, G, gen)) {
+        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
+        return;
+    }
+    if (ld_volatile(&st->code) != 0) return;  // a singular pivot block: every CTA leaves here
+    // the merges overwrote the shared buffers: reload this CTA's original
+    // rows (nothing has written the panel yet) before anyone writes it
+    cplxf *Own = W;
+    for (int t = tid; t < nrows * NB; t += blockDim.x) {
+        int i = t / NB, j = t % NB;
+        Own[i * kPS + j] = j < kb ? a[(size_t)(r0 + i) * n + k0 + j] : cplxf{0.0f, 0.0f};
+    }
+    // 4. sequential swaps equivalent to moving fpiv[i] to row k0 + i (piv[]),
+    //    and where every touched row ends: entries (row s_prow[t] at
+    //    position s_pos[t]); untouched rows stay where they are
+    if (tid == 0) {
+        int nt = 0;
+        for (int i = 0; i < kb; ++i) {
+            const int r = ld_volatile(S.fpiv + i), p = k0 + i;
+            int tr = -1, tp = -1;
+            for (int t = 0; t < nt; ++t) {
+                if (s_prow[t] == r) tr = t;
+                if (s_pos[t] == p) tp = t;
+            }
+            const int q = tr >= 0 ? s_pos[tr] : r;  // current position of row r
+            if (c == 0) piv[p] = q;
+            if (q == p) continue;
+            const int rp = tp >= 0 ? s_prow[tp] : p;  // the row now at p moves to q
+            if (tr < 0) {
+                tr = nt++;
+                s_prow[tr] = r;
+            }
+            if (tp < 0) {
+                tp = nt++;
+                s_prow[tp] = rp;
+            }
+            s_pos[tr] = p;
+            s_pos[tp] = q;
+        }
+        s_nt = nt;
+    }
+    for (int t = tid; t < NB * NB; t += blockDim.x) s_top[t] = ld_volatile(S.top + t);
+    if (!grid_barrier(S.ps, G, gen)) {  // every CTA holds its originals
+        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
+        return;
+    }
+    // 5. write this CTA's original rows at their final positions: pivot rows
+    //    get L11 \ U11 (from CTA 0's factorisation), the others
+    //    L21 = A21 U11^-1 (forward substitution along the row)
+    for (int i = tid; i < nrows; i += blockDim.x) {
+        const int r = r0 + i;
+        int pos = r;
+        for (int t = 0; t < s_nt; ++t)
+            if (s_prow[t] == r) pos = s_pos[t];
+        cplxf *dst = a + (size_t)pos * n + k0;
+        if (pos < k0 + kb) {
+            const cplxf *src = s_top + (pos - k0) * NB;
+            for (int j = 0; j < kb; ++j) dst[j] = src[j];
+        } else {
+            cplxf x[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                if (j < kb) {
+                    cplxf v = Own[i * kPS + j];
+                    for (int q = 0; q < j; ++q) v = msub(v, x[q], s_top[q * NB + j]);
+                    x[j] = divide(v, s_top[j * NB + j]);
+                    dst[j] = x[j];
+                }
+            }
+        }
+    }
 }
 
 // ---- row swaps outside the panel -------------------------------------
@@ -1408,6 +1694,34 @@ struct CoopPlan {
     size_t smem = 0;
 };
 
+// Tournament panel for the FP32 factorisation: G CTAs (one per SM) when the
+// panel has enough rows; false when it does not apply.
+static bool launch_calu_panel(cplxf *a, int n, int k0, int kb, double limit, long long *piv, Status *st,
+                              const CaluScratch &S, int sms) {
+    const int m = n - k0;
+    if (m < 2 * 64) return false;
+    const int G = std::min(sms, std::min(kCaluMaxRows / NB * kCaluGroup, (m + NB - 1) / NB));
+    const int rows = (m + G - 1) / G;
+    if (rows > kCaluRows) return false;
+    constexpr size_t smem = (size_t)kCaluMaxRows * kPS * sizeof(cplxf) + kCaluMaxRows * sizeof(int);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_panel_calu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return false;
+    static const int per_sm = [] {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_panel_calu, 256, smem);
+        return v;
+    }();
+    if (per_sm < 1) return false;
+    int rows_v = rows, kb_v = kb, n_v = n, k0_v = k0;
+    double lim = limit;
+    CaluScratch sv = S;
+    void *args[] = {&a, &n_v, &k0_v, &kb_v, &rows_v, &lim, &piv, &st, &sv};
+    note_launch();
+    return cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_calu, dim3(G), dim3(256), args, smem, stream()),
+                   "tournament panel launch");
+}
+
 // Cluster panel: C CTAs (16 where the device allows non-portable clusters,
 // else 8) when the m panel rows fit their shared memory.  Returns false
 // when the cluster panel does not apply; the caller then uses the
@@ -1470,7 +1784,7 @@ static CoopPlan<T> coop_plan(int m) {
     if (!coop || m < 2 * 64) return pl;  // small panels: one CTA is faster
     int G = std::min(sms, (m + 31) / 32);
     int rows = (m + G - 1) / G;
-    size_t smem = (size_t)rows * NB * sizeof(T);
+    size_t smem = (size_t)rows * kPS * sizeof(T);
     if (smem > 200 * 1024) return pl;
     static const cudaError_t attr =  // once per type (thread-safe static initialisation)
         cudaFuncSetAttribute(k_panel_coop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -1495,6 +1809,21 @@ static bool cluster_panel_enabled() {
     static const bool on = [] {
         const char *e = getenv("PEEC_GB300_PANEL");
         return e && strcmp(e, "cluster") == 0;
+    }();
+    return on;
+}
+
+// FP32 panels of the mixed path by tournament pivoting when
+// PEEC_GB300_MIXED_PANEL=calu; partial pivoting otherwise.  Measured on
+// GB300 (8402 unknowns) the tournament panel takes 75 ms per factorisation
+// against 49 ms for the cooperative partial-pivoting panel: its four grid
+// barriers per panel are cheaper than 32, but every CTA's local LU of 256+
+// rows and the two merge levels serialise more FP32 work than the barriers
+// save at 32-column panels.
+static bool calu_panel_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PEEC_GB300_MIXED_PANEL");
+        return e && strcmp(e, "calu") == 0;
     }();
     return on;
 }
@@ -2555,6 +2884,11 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     const int OB = 256;
     DBuf<__nv_bfloat16> ap((size_t)n * 6 * OB), bpr((size_t)n * 6 * OB), bpi((size_t)n * 6 * OB);
     DBuf<cplxf> linv((size_t)OB * OB);  // I - L11^-1 of one outer block
+    // tournament panel scratch (nominees of every CTA and group, the pivot block)
+    const int kMaxCta = kCaluMaxRows / NB * kCaluGroup;
+    DBuf<cplxf> calu_rows((size_t)(kMaxCta + kMaxCta / kCaluGroup + 1) * NB * NB);
+    DBuf<int> calu_idx((size_t)(kMaxCta + kMaxCta / kCaluGroup + 1) * NB);
+    DBuf<PanelSlots> calu_ps(1);
     DBuf<unsigned char> scratch;
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -2562,7 +2896,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     const size_t G = (size_t)sms;
     size_t sbytes = 256 + 2 * G * 8 + 2 * G * 4 + 16 + 2 * G * NB * sizeof(cplxf) + 2 * NB * sizeof(cplxf) + 64;
     if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
-        !bpr.p || !bpi.p || !linv.p || !scratch.alloc(sbytes))
+        !bpr.p || !bpi.p || !linv.p || !calu_rows.p || !calu_idx.p || !calu_ps.p || !scratch.alloc(sbytes))
         return -1;
     cudaEvent_t ev[4];
     for (auto &e : ev) cudaEventCreate(&e);
@@ -2571,6 +2905,15 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
     cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(err.p, 0, sizeof(int), stream());
+    cudaMemsetAsync(calu_ps.p, 0, sizeof(PanelSlots), stream());
+    CaluScratch cs_calu;
+    cs_calu.ps = calu_ps.p;
+    cs_calu.cand = calu_rows.p;
+    cs_calu.cand_idx = calu_idx.p;
+    cs_calu.cand2 = calu_rows.p + (size_t)kMaxCta * NB * NB;
+    cs_calu.cand2_idx = calu_idx.p + (size_t)kMaxCta * NB;
+    cs_calu.top = cs_calu.cand2 + (size_t)(kMaxCta / kCaluGroup) * NB * NB;
+    cs_calu.fpiv = cs_calu.cand2_idx + (size_t)(kMaxCta / kCaluGroup) * NB;
     PanelScratch sc;
     {
         unsigned char *bb = scratch.p;
@@ -2630,7 +2973,8 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             const int kb = std::min(NB, E - k0);
             tm.mark(2);
             CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
-            if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
+            if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
+            } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
             } else if (pl.G > 0) {
                 int rows = pl.rows;
                 cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
