@@ -2676,53 +2676,132 @@ __global__ void k_split_a(const cplxf *a, int n, int row0, int m, int col0, int 
 // Br', Bi' row j (0..nc-1) <- U[row0 .. row0+kw-1][col0 + j]:
 // Br' = [re_h | re_l | re_h | -im_h | -im_l | -im_h], Bi' = [im_h | im_l | im_h | re_h | re_l | re_h],
 // so that A' Br' = Re(L U) and A' Bi' = Im(L U) to FP32 accuracy.
-__global__ void k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int col0, int nc, __nv_bfloat16 *br,
-                          __nv_bfloat16 *bi) {
-    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)nc * KW) return;
-    int c = (int)(t / nc), j = (int)(t % nc);  // consecutive threads read consecutive columns
-    cplxf x = c < kw ? a[(size_t)(row0 + c) * n + col0 + j] : cplxf{0.0f, 0.0f};
-    __nv_bfloat16 rh, rl, ih, il;
-    split_bf16(x.re, rh, rl);
-    split_bf16(x.im, ih, il);
-    __nv_bfloat16 *r = br + (size_t)j * 6 * KW, *q = bi + (size_t)j * 6 * KW;
-    r[c] = rh;
-    r[KW + c] = rl;
-    r[2 * KW + c] = rh;
-    r[3 * KW + c] = __hneg(ih);
-    r[4 * KW + c] = __hneg(il);
-    r[5 * KW + c] = __hneg(ih);
-    q[c] = ih;
-    q[KW + c] = il;
-    q[2 * KW + c] = ih;
-    q[3 * KW + c] = rh;
-    q[4 * KW + c] = rl;
-    q[5 * KW + c] = rh;
+// A 64 (K) x 32 (columns) tile per CTA goes through shared memory: rows of U
+// are read along the columns (coalesced), the four BF16 parts are kept as
+// K-contiguous planes, and the K-major outputs are written as 128-byte
+// segments of 16-byte stores.  grid (ceil(nc / 32), ceil(KW / 64)), 256 threads.
+static const int kSbK = 64, kSbJ = 32, kSbPad = 72;  // plane row: 72 BF16 = 144 bytes (16-byte aligned)
+__global__ void __launch_bounds__(256) k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int col0, int nc,
+                                                 __nv_bfloat16 *br, __nv_bfloat16 *bi) {
+    __shared__ __align__(16) __nv_bfloat16 pl[4][kSbJ][kSbPad];  // re_h, re_l, im_h, im_l
+    const int t = threadIdx.x, j0 = blockIdx.x * kSbJ, c0 = blockIdx.y * kSbK;
+    {
+        const int j = t & 31;
+        for (int rr = 0; rr < kSbK / 8; ++rr) {
+            const int c = rr * 8 + (t >> 5);
+            cplxf x = (c0 + c < kw && j0 + j < nc) ? a[(size_t)(row0 + c0 + c) * n + col0 + j0 + j]
+                                                   : cplxf{0.0f, 0.0f};
+            __nv_bfloat16 rh, rl, ih, il;
+            split_bf16(x.re, rh, rl);
+            split_bf16(x.im, ih, il);
+            pl[0][j][c] = rh;
+            pl[1][j][c] = rl;
+            pl[2][j][c] = ih;
+            pl[3][j][c] = il;
+        }
+    }
+    __syncthreads();
+    // output segment seg (0..11): br planes 0..5, bi planes 6..11; within
+    // six, parts (h, l, h) of the first then the second component
+    for (int q = t; q < 12 * kSbJ * (kSbK / 8); q += blockDim.x) {
+        const int e = q & 7, j = (q >> 3) & (kSbJ - 1), seg = q >> 8;
+        const int c = c0 + 8 * e;
+        if (j0 + j >= nc || c >= KW) continue;
+        const int s6 = seg % 6, second = s6 / 3, lo = (s6 % 3) == 1;
+        const int imag = (seg < 6) ? second : 1 - second;
+        uint4 v = *reinterpret_cast<const uint4 *>(&pl[2 * imag + lo][j][8 * e]);
+        const unsigned m = (seg < 6 && second) ? 0x80008000u : 0u;
+        v.x ^= m;
+        v.y ^= m;
+        v.z ^= m;
+        v.w ^= m;
+        __nv_bfloat16 *out = (seg < 6 ? br : bi) + (size_t)(j0 + j) * 6 * KW + (seg % 6) * KW + c;
+        *reinterpret_cast<uint4 *>(out) = v;
+    }
 }
 
 // N = I - L^-1 for the unit lower triangle L = a[K0 + i][K0 + k] (i, k < kw,
-// kw <= 256), FP32 complex, row-major kw x kw: one warp per column c solves
-// L x = e_c by forward substitution (lane-parallel dot products, FP32
-// shuffles); N is strictly lower (N[i][c] = -x_i for i > c).
+// kw <= 256), FP32 complex, row-major kw x kw; N is strictly lower.
+// Blocked in 32 x 32 blocks: CTA (jb, g) computes the columns 32 jb + 8 g ..
+// +7 of X = L^-1.  Phase 1: warp w inverts the diagonal block D = L_ii^-1,
+// i = jb + w (one lane per column, forward substitution in registers).
+// Phase 2, block rows i = jb+1 ..: X_i = -D_i sum_{k<i} L_ik X_k (the sum in
+// shared memory, one output per thread).  grid (ceil(kw / 32), 4), 256
+// threads, dynamic shared memory k_lower_inv_smem().
+static const int kLiPad = 33, kLiX = 9, kLiRow = 225;
+static constexpr size_t k_lower_inv_smem() {
+    return sizeof(cplxf) * ((size_t)8 * 32 * kLiPad + 256 * kLiX + 32 * kLiRow + 32 * kLiX);
+}
 __global__ void __launch_bounds__(256) k_lower_inv(const cplxf *a, int n, int K0, int kw, cplxf *N) {
-    __shared__ cplxf xs[8][256];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * 8 + warp;
-    if (c >= kw) return;
-    cplxf *x = xs[warp];
-    for (int i = lane; i < kw; i += 32) x[i] = cplxf{i == c ? 1.0f : 0.0f, 0.0f};
-    __syncwarp();
-    for (int i = c + 1; i < kw; ++i) {
-        const cplxf *li = a + (size_t)(K0 + i) * n + K0;
-        cplxf s = {0.0f, 0.0f};
-        for (int k = c + lane; k < i; k += 32) s = mac(s, li[k], x[k]);
-        s = warp_sum_t(s);
-        if (lane == 0) x[i] = cplxf{-s.re, -s.im};
-        __syncwarp();
+    extern __shared__ __align__(16) unsigned char li_smem[];
+    cplxf *blk = reinterpret_cast<cplxf *>(li_smem);  // [8][32][kLiPad]: L_ii, then L_ii^-1
+    cplxf *X = blk + 8 * 32 * kLiPad;                 // [256][kLiX]: rows 32 jb.., this CTA's 8 columns
+    cplxf *Lr = X + 256 * kLiX;                       // [32][kLiRow]: L_i,jb..i-1
+    cplxf *S = Lr + 32 * kLiRow;                      // [32][kLiX]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int jb = blockIdx.x, g = blockIdx.y, nb = (kw + 31) / 32;
+    // phase 1: diagonal block inverses (rows past kw: identity)
+    {
+        const int i = jb + warp;
+        if (i < nb) {
+            cplxf *B = blk + warp * 32 * kLiPad;
+            for (int r = 0; r < 32; ++r) {
+                const int gr = 32 * i + r, gq = 32 * i + lane;
+                B[r * kLiPad + lane] = (lane < r && gr < kw) ? a[(size_t)(K0 + gr) * n + K0 + gq] : cplxf{0.0f, 0.0f};
+            }
+            __syncwarp();
+            cplxf d[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                cplxf s = {r == lane ? 1.0f : 0.0f, 0.0f};
+#pragma unroll
+                for (int q = 0; q < r; ++q) {
+                    const cplxf l = B[r * kLiPad + q];
+                    s.re = fmaf(-l.re, d[q].re, s.re);
+                    s.re = fmaf(l.im, d[q].im, s.re);
+                    s.im = fmaf(-l.re, d[q].im, s.im);
+                    s.im = fmaf(-l.im, d[q].re, s.im);
+                }
+                d[r] = r >= lane ? s : cplxf{0.0f, 0.0f};
+            }
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < 32; ++r) B[r * kLiPad + lane] = d[r];
+        }
     }
-    for (int i = lane; i < kw; i += 32) {
-        cplxf v = i > c ? cplxf{-x[i].re, -x[i].im} : cplxf{0.0f, 0.0f};
-        N[(size_t)i * kw + c] = v;
+    __syncthreads();
+    const int r = tid >> 3, cc = tid & 7;
+    X[r * kLiX + cc] = blk[r * kLiPad + 8 * g + cc];  // X_jb = columns of D_jb
+    for (int i = jb + 1; i < nb; ++i) {
+        const int len = 32 * (i - jb);
+        for (int q = tid; q < 32 * len; q += blockDim.x) {
+            const int rr = q / len, qq = q % len, gr = 32 * i + rr;
+            Lr[rr * kLiRow + qq] = gr < kw ? a[(size_t)(K0 + gr) * n + K0 + 32 * jb + qq] : cplxf{0.0f, 0.0f};
+        }
+        __syncthreads();
+        cplxf s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+        for (int q = 0; q < len; q += 2) {
+            s0 = mac(s0, Lr[r * kLiRow + q], X[q * kLiX + cc]);
+            s1 = mac(s1, Lr[r * kLiRow + q + 1], X[(q + 1) * kLiX + cc]);
+        }
+        S[r * kLiX + cc] = cplxf{s0.re + s1.re, s0.im + s1.im};
+        __syncthreads();
+        const cplxf *D = blk + (i - jb) * 32 * kLiPad;
+        cplxf x = {0.0f, 0.0f};
+        for (int q = 0; q < 32; ++q) x = mac(x, D[r * kLiPad + q], S[q * kLiX + cc]);
+        X[(len + r) * kLiX + cc] = cplxf{-x.re, -x.im};
+        __syncthreads();
+    }
+    // N[row][col] = -X for row > col, 0 otherwise (rows above the block: 0)
+    const int col = 32 * jb + 8 * g + cc;
+    if (col >= kw) return;
+    for (int row = r; row < kw; row += 32) {
+        cplxf v = {0.0f, 0.0f};
+        if (row > col) {
+            const cplxf xv = X[(row - 32 * jb) * kLiX + cc];
+            v = cplxf{-xv.re, -xv.im};
+        }
+        N[(size_t)row * kw + col] = v;
     }
 }
 
@@ -2953,7 +3032,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         const int KW = (kw + 31) / 32 * 32;
         PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
                     ap.p);
-        PEEC_LAUNCH(k_split_b, (unsigned)(((long long)nc * KW + 255) / 256), 256, 0, a, n, kc, kw, KW, col0, nc,
+        PEEC_LAUNCH(k_split_b, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
                     bpr.p, bpi.p);
         if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
         return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
@@ -2962,7 +3041,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         if (m <= 0 || nc <= 0) return true;
         const int KW = (kw + 31) / 32 * 32;
         PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
-        PEEC_LAUNCH(k_split_b, (unsigned)(((long long)nc * KW + 255) / 256), 256, 0, a, n, kc, kw, KW, col0, nc,
+        PEEC_LAUNCH(k_split_b, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
                     bpr.p, bpi.p);
         if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
         return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
@@ -3003,7 +3082,10 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             // U12 of the outer block for the columns right of it in one
             // tensor-core update: U12 = L11^-1 A12 = A12 - (I - L11^-1) A12
             const int kw = E - K0;
-            PEEC_LAUNCH(k_lower_inv, (kw + 7) / 8, 256, 0, a, n, K0, kw, linv.p);
+            static const cudaError_t li_attr = cudaFuncSetAttribute(
+                k_lower_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k_lower_inv_smem());
+            if (!cuda_ok(li_attr, "lower-inverse smem attribute")) return -1;
+            PEEC_LAUNCH(k_lower_inv, dim3((kw + 31) / 32, 4), 256, k_lower_inv_smem(), a, n, K0, kw, linv.p);
             tm.mark(1);
             if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
             tm.mark(2);
