@@ -140,6 +140,14 @@ int peec_gb300_pipe_peaks(double *fp64_tflops, double *fp32_tflops);
 int peec_gb300_tc_gemm(const void *d_a, const void *d_b0, const void *d_b1, float *d_c0,
                        float *d_c1, int m, int n, int k, long long ldc, int J);
 
+/* Complex form used by the mixed-precision LU: C (interleaved FP32 complex,
+ * leading dimension ldc complex elements) [row0 + i][col0 + j] -=
+ * (A Br^T)[i][j] + j (A Bi^T)[i][j] for i < m, j < n; BF16 A [m][k],
+ * Br / Bi [n][k].  A 16-byte aligned block with an even ldc runs on the
+ * persistent kernel (TMEM double-buffered accumulators, TMA epilogue). */
+int peec_gb300_tc_gemm_cplx(const void *d_a, const void *d_br, const void *d_bi, float *d_c, int m,
+                            int n, int k, int row0, int col0, long long ldc);
+
 /* ---- mixed precision complex solve ----
  * Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
  * another) to a componentwise backward error <= tol: FP64 equilibration as

@@ -10,8 +10,10 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/peec_gb300.h"
@@ -97,6 +99,69 @@ bool tc_gemm_update(const void *a, const void *b0, const void *b1, float *c0, fl
     return launch_tc<128, 2, 4>(a, b0, b1, c0, c1, m, n, k, row0, col0, ldc, d_err);
 }
 
+// FP32 interleaved complex block C[row0.., col0..] (m x n, leading dimension
+// ldc complex) as a 2-D FP32 map, box 32 floats x 128 rows, 128-byte swizzle.
+static bool make_map_c(CUtensorMap *map, float *c, long long ldc, int row0, int col0, int m, int n) {
+    if (!encoder()) return false;
+    float *base = c + 2 * ((size_t)row0 * ldc + col0);
+    if (((uintptr_t)base & 15) || (ldc * 8) % 16 != 0) {
+        set_error("tensor map: C block must start 16-byte aligned with an even leading dimension");
+        return false;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)2 * n, (cuuint64_t)m};
+    cuuint64_t strides[1] = {(cuuint64_t)ldc * 8};
+    cuuint32_t box[2] = {32, (cuuint32_t)tc::kBM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (C) failed (%d)", (int)r);
+        return false;
+    }
+    return true;
+}
+
+// Persistent form (tc_gemm.cuh): one CTA per SM, TMEM double-buffered
+// accumulators, TMA epilogue.  Needs the C block 16-byte aligned.
+static bool persistent_ok(const float *c, long long ldc, int row0, int col0) {
+    const float *base = c + 2 * ((size_t)row0 * ldc + col0);
+    return ((uintptr_t)base & 15) == 0 && (ldc & 1) == 0;
+}
+
+static bool launch_tc_persistent(const void *a, const void *br, const void *bi, float *c, int m, int n, int k,
+                                 int row0, int col0, long long ldc, int *d_err) {
+    constexpr int BN = 128, S = 4;
+    CUtensorMap ma, mbr, mbi, mc;
+    if (!make_map_bf16(&ma, a, m, k, tc::kBM) || !make_map_bf16(&mbr, br, n, k, BN) ||
+        !make_map_bf16(&mbi, bi, n, k, BN) || !make_map_c(&mc, c, ldc, row0, col0, m, n))
+        return false;
+    constexpr size_t smem = tc::smem_bytes_persistent<BN, S>();
+    static const cudaError_t attr = cudaFuncSetAttribute(tc::k_tc_gemm_cplx_persistent<BN, S>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!cuda_ok(attr, "tcgen05 persistent GEMM smem attribute")) return false;
+    static const int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    const long long tiles = (long long)((m + tc::kBM - 1) / tc::kBM) * ((n + BN - 1) / BN);
+    const int grid = (int)std::min<long long>(tiles, sms);
+    tc::PersistentArgs g{m, n, k, d_err};
+    PEEC_LAUNCH((tc::k_tc_gemm_cplx_persistent<BN, S>), grid, 192, smem, ma, mbr, mbi, mc, g);
+    return launch_tc_ok();
+}
+
+// PEEC_GB300_TC_PERSISTENT=0 keeps the one-tile-per-CTA kernel everywhere.
+static bool persistent_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PEEC_GB300_TC_PERSISTENT");
+        return !(e && strcmp(e, "0") == 0);
+    }();
+    return on;
+}
+
 // Complex C (interleaved FP32, leading dimension ldc complex elements)
 // [row0.., col0..] -= (A Br^T) + j (A Bi^T).
 bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c, int m, int n, int k, int row0,
@@ -107,12 +172,33 @@ bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c
     }
     // the LU's K is 192: three stages, 64-column tiles -> two CTAs per SM
     if (k == 192) return launch_tc<64, 2, 3>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
+    if (persistent_enabled() && persistent_ok(c, ldc, row0, col0))
+        return launch_tc_persistent(a, br, bi, c, m, n, k, row0, col0, ldc, d_err);
     return launch_tc<128, 2, 4>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
 }
 
 }  // namespace peec
 
 using namespace peec;
+
+// Test / building-block entry point: complex C (interleaved FP32, leading
+// dimension ldc complex) [row0.., col0..] -= A Br^T + j A Bi^T, m x n block.
+extern "C" int peec_gb300_tc_gemm_cplx(const void *d_a, const void *d_br, const void *d_bi, float *d_c, int m, int n,
+                                       int k, int row0, int col0, long long ldc) {
+    if (!d_a || !d_br || !d_bi || !d_c || m <= 0 || n <= 0 || row0 < 0 || col0 < 0 || ldc < col0 + n) return -1;
+    DBuf<int> err(1);
+    if (!err.p) return -1;
+    cudaMemsetAsync(err.p, 0, sizeof(int), stream());
+    if (!tc_gemm_update_cplx(d_a, d_br, d_bi, d_c, m, n, k, row0, col0, ldc, err.p)) return -1;
+    int h = 0;
+    cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+    if (!sync("tcgen05 complex GEMM")) return -1;
+    if (h) {
+        set_error("tcgen05 complex GEMM: a pipeline wait timed out");
+        return -1;
+    }
+    return 0;
+}
 
 // Test / building-block entry point: C_j (FP32 row-major, ld = ldc) -= A B_j^T
 // for device BF16 matrices A [m][k] and B_j [n][k].

@@ -319,5 +319,269 @@ __global__ void __launch_bounds__(128, 1)
     if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
+// ---------------------------------------------------------------------
+// Persistent complex update with an overlapped TMA epilogue.
+//
+//   C[row0 + i][col0 + j] -= (A Br^T)[i][j] + i (A Bi^T)[i][j]
+//
+// C is interleaved complex FP32 (described by its own tensor map over the
+// m x n block, so stores clip at the block's edge).  One CTA per SM loops
+// over 128 x BN tiles (t = blockIdx.x, + gridDim.x, ...).  Six warps:
+//   warp 0   lane 0 TMA producer of the A / B stages (runs ahead across tiles)
+//   warp 1   lane 0 MMA issuer; the two accumulators (re, im) of a tile live
+//            in one of two TMEM buffers, so the MMAs of tile t+1 run while
+//            the epilogue drains tile t
+//   warps 2-5 epilogue: C is brought into shared memory by TMA in 16-column
+//            chunks (128 rows x 128 bytes, 128-byte swizzle, double
+//            buffered), each thread subtracts its TMEM row, and the chunk
+//            goes back by a TMA store -- C is read and written once, in
+//            full lines.
+// Every wait is bounded; a timeout stops all roles at the next uniform
+// point, records the error, lets work in flight drain, and frees TMEM.
+static const int kEpiCols = 16;  // complex columns per C chunk (32 floats = one 128-byte row)
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y, const void *smem_src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(smem_u32(smem_src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN, int S>
+__host__ __device__ constexpr size_t smem_bytes_persistent() {
+    return (size_t)S * ((size_t)kBM * kBK * 2 + (size_t)2 * BN * kBK * 2) + (size_t)2 * kBM * 128 + 1024 + 256;
+}
+
+struct PersistentArgs {
+    int m, n, k;  // C block m x n, K
+    int *error;
+};
+
+template <int BN, int kStages>
+__global__ void __launch_bounds__(192, 1)
+    k_tc_gemm_cplx_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_br,
+                              const __grid_constant__ CUtensorMap map_bi, const __grid_constant__ CUtensorMap map_c,
+                              PersistentArgs args) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    constexpr size_t a_bytes = (size_t)kBM * kBK * 2, b_bytes = (size_t)BN * kBK * 2;
+    constexpr size_t stage_bytes = a_bytes + 2 * b_bytes;
+    constexpr uint32_t chunk_bytes = kBM * 128;
+    unsigned char *cbuf = base + kStages * stage_bytes;  // 2 x [128 rows][128 bytes], swizzled
+    uint64_t *full = reinterpret_cast<uint64_t *>(cbuf + 2 * chunk_bytes);
+    uint64_t *empty = full + kStages;
+    uint64_t *tfull = empty + kStages;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *cfull = tempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(cfull + 2);
+    __shared__ int s_abort, s_epi_fail;
+    constexpr uint32_t kTmemCols = 4 * BN;  // two buffers x (re, im)
+    static_assert(kTmemCols <= 512 && (kTmemCols & (kTmemCols - 1)) == 0, "TMEM columns");
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_m = (args.m + kBM - 1) / kBM, tiles_n = (args.n + BN - 1) / BN;
+    const int ntiles = tiles_m * tiles_n, ktiles = args.k / kBK;
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        s_epi_fail = 0;
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 4);
+            mbar_init(&cfull[b], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    volatile int *abort_flag = &s_abort;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            long long it = 0;
+            for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+                const int tm = (t / tiles_n) * kBM, tn = (t % tiles_n) * BN;
+                for (int kt = 0; kt < ktiles; ++kt, ++it) {
+                    const int s = (int)(it % kStages);
+                    if (it >= kStages && !mbar_wait(&empty[s], (uint32_t)((it / kStages) - 1) & 1, abort_flag)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    unsigned char *sa = base + s * stage_bytes;
+                    mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+                    tma_load_2d(sa, &map_a, kt * kBK, tm, &full[s]);
+                    tma_load_2d(sa + a_bytes, &map_br, kt * kBK, tn, &full[s]);
+                    tma_load_2d(sa + a_bytes + b_bytes, &map_bi, kt * kBK, tn, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16_f32(kBM, BN);
+            long long it = 0;
+            int lt = 0;
+            for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
+                const int b = lt & 1;
+                if (lt >= 2 && !mbar_wait(&tempty[b], (uint32_t)((lt >> 1) - 1) & 1, abort_flag)) {
+                    s_abort = 1;
+                    break;
+                }
+                fence_after_sync();
+                const uint32_t acc = tmem + (uint32_t)(b * 2 * BN);
+                bool ok = true;
+                for (int kt = 0; kt < ktiles; ++kt, ++it) {
+                    const int s = (int)(it % kStages);
+                    if (!mbar_wait(&full[s], (uint32_t)(it / kStages) & 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after_sync();
+                    unsigned char *sa = base + s * stage_bytes;
+                    const uint64_t ad = smem_desc_sw128(sa);
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const uint64_t bd = smem_desc_sw128(sa + a_bytes + j * b_bytes);
+#pragma unroll
+                        for (int kk = 0; kk < kBK / 16; ++kk)
+                            mma_bf16(acc + j * BN, ad + 2 * kk, bd + 2 * kk, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) {
+                    s_abort = 1;
+                    break;
+                }
+                mma_commit(&tfull[b]);
+            }
+        }
+    } else {
+        // epilogue warps 2..5: TMEM lanes 32 (warp % 4) .. + 31.  A failed
+        // wait is made uniform over the 128 epilogue threads (flag written
+        // before one named barrier, read between it and the next) so that
+        // they leave the loop together.
+        const int q = warp & 3;
+        const int row = 32 * q + lane;  // row within the tile
+        const bool leader = (warp == 2 && lane == 0);
+        const int chunks = BN / kEpiCols;
+        long long gi = 0;  // C chunk sequence number (buffer gi & 1)
+        int lt = 0;
+        int t = blockIdx.x;
+        auto uniform_fail = [&](bool ok) -> bool {
+            if (!ok) {
+                s_epi_fail = 1;
+                s_abort = 1;
+            }
+            if (leader && s_abort) s_epi_fail = 1;
+            __syncwarp();
+            epi_barrier();
+            const bool f = s_epi_fail != 0;
+            epi_barrier();
+            return f;
+        };
+        // prefetch the first chunk
+        if (leader && t < ntiles) {
+            mbar_expect_tx(&cfull[0], chunk_bytes);
+            tma_load_2d(cbuf, &map_c, 2 * ((t % tiles_n) * BN), (t / tiles_n) * kBM, &cfull[0]);
+        }
+        for (; t < ntiles; t += gridDim.x, ++lt) {
+            const int b = lt & 1;
+            const int tm = (t / tiles_n) * kBM, tn = (t % tiles_n) * BN;
+            if (uniform_fail(mbar_wait(&tfull[b], (uint32_t)(lt >> 1) & 1, abort_flag))) break;
+            fence_after_sync();
+            const uint32_t acc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 2 * BN);
+            bool failed = false;
+            for (int ch = 0; ch < chunks; ++ch, ++gi) {
+                // issue the next chunk's load once its buffer's previous store has read it
+                if (leader) {
+                    bulk_wait_read0();
+                    int nt = t, nch = ch + 1;
+                    if (nch == chunks) {
+                        nch = 0;
+                        nt = t + gridDim.x;
+                    }
+                    if (nt < ntiles) {
+                        const int nb = (int)((gi + 1) & 1);
+                        mbar_expect_tx(&cfull[nb], chunk_bytes);
+                        tma_load_2d(cbuf + nb * chunk_bytes, &map_c, 2 * ((nt % tiles_n) * BN + nch * kEpiCols),
+                                    (nt / tiles_n) * kBM, &cfull[nb]);
+                    }
+                }
+                __syncwarp();
+                float vr[kEpiCols], vi[kEpiCols];
+                tmem_ld16(acc + ch * kEpiCols, vr);
+                tmem_ld16(acc + BN + ch * kEpiCols, vi);
+                const int cb = (int)(gi & 1);
+                if (uniform_fail(mbar_wait(&cfull[cb], (uint32_t)(gi >> 1) & 1, abort_flag))) {
+                    failed = true;
+                    break;
+                }
+                unsigned char *rowp = cbuf + cb * chunk_bytes + row * 128;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    float4 *p = reinterpret_cast<float4 *>(rowp + ((u ^ (row & 7)) << 4));
+                    float4 v = *p;
+                    v.x -= vr[2 * u];
+                    v.y -= vi[2 * u];
+                    v.z -= vr[2 * u + 1];
+                    v.w -= vi[2 * u + 1];
+                    *p = v;
+                }
+                fence_proxy_async_smem();
+                __syncwarp();
+                epi_barrier();
+                if (leader) {
+                    tma_store_2d(&map_c, 2 * (tn + ch * kEpiCols), tm, cbuf + cb * chunk_bytes);
+                    bulk_commit();
+                }
+            }
+            if (failed) break;
+            // this tile's accumulators are read: hand the TMEM buffer back
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
+        }
+        if (leader) bulk_wait0();
+    }
+    __syncwarp();
+    __syncthreads();
+    if (s_abort) {
+        if (threadIdx.x == 0) atomicExch(args.error, 1);
+        for (int i = 0; i < 20000; ++i) __nanosleep(1000);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
 }  // namespace tc
 }  // namespace peec

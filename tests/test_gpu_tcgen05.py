@@ -60,3 +60,50 @@ def test_tc_gemm_matches_fp64(gpu_lib, m, n, k, J):
 
 def test_tc_gemm_rejects_bad_k(gpu_lib):
     assert gpu_lib.peec_gb300_tc_gemm(1, 1, 1, 1, 1, 128, 128, 100, 128, 1) == -1
+
+
+def run_cplx(lib, m, n, k, row0, col0, ldc, rows, seed):
+    """C (rows x ldc interleaved complex FP32) block [row0.., col0..] -= A Br^T + j A Bi^T;
+    everything outside the block must be untouched bit for bit."""
+    rng = np.random.default_rng(seed)
+    A = to_bf16_bits(rng.standard_normal((m, k)).astype(np.float32))
+    Br = to_bf16_bits(rng.standard_normal((n, k)).astype(np.float32))
+    Bi = to_bf16_bits(rng.standard_normal((n, k)).astype(np.float32))
+    C0 = rng.standard_normal((rows, 2 * ldc)).astype(np.float32)
+    dev = []
+
+    def up(arr):
+        p = lib.peec_gb300_device_alloc(arr.nbytes)
+        assert lib.peec_gb300_copy_to_device(p, arr.ctypes.data, arr.nbytes) == 0
+        dev.append(p)
+        return p
+    dA, dBr, dBi, dC = up(A), up(Br), up(Bi), up(C0)
+    s = lib.peec_gb300_tc_gemm_cplx(dA, dBr, dBi, dC, m, n, k, row0, col0, ldc)
+    out = np.zeros_like(C0)
+    lib.peec_gb300_copy_to_host(out.ctypes.data, dC, out.nbytes)
+    for p in dev:
+        lib.peec_gb300_device_free(p)
+    assert s == 0
+    Af, Brf, Bif = bf16_bits_to_f64(A), bf16_bits_to_f64(Br), bf16_bits_to_f64(Bi)
+    blk = (slice(row0, row0 + m), slice(2 * col0, 2 * (col0 + n)))
+    ref = C0.astype(np.float64).copy()
+    ref[blk[0], blk[1].start:blk[1].stop:2] -= Af @ Brf.T
+    ref[blk[0], blk[1].start + 1:blk[1].stop:2] -= Af @ Bif.T
+    scale = np.abs(C0).astype(np.float64)
+    scale[blk[0], blk[1].start:blk[1].stop:2] += np.abs(Af) @ np.abs(Brf).T
+    scale[blk[0], blk[1].start + 1:blk[1].stop:2] += np.abs(Af) @ np.abs(Bif).T
+    err = np.max(np.abs(out - ref) / scale)
+    assert err < 1e-5, (m, n, k, err)
+    mask = np.ones(C0.shape, dtype=bool)
+    mask[blk] = False
+    assert np.array_equal(out[mask], C0[mask])
+
+
+# (m, n, k, row0, col0, ldc, rows): even ldc and an aligned block take the
+# persistent kernel (several tiles per CTA at the larger sizes, ragged edges);
+# odd ldc and K = 192 take the one-tile-per-CTA kernel.
+@pytest.mark.parametrize("m,n,k,row0,col0,ldc,rows", [
+    (128, 128, 384, 0, 0, 128, 128), (300, 260, 1536, 5, 6, 600, 320), (1000, 700, 768, 2, 4, 800, 1010),
+    (4000, 2600, 256, 32, 64, 2700, 4040), (200, 150, 384, 1, 3, 301, 210), (500, 100, 192, 0, 32, 200, 510)])
+def test_tc_gemm_cplx_block(gpu_lib, m, n, k, row0, col0, ldc, rows):
+    run_cplx(gpu_lib, m, n, k, row0, col0, ldc, rows, seed=m + n + k)
