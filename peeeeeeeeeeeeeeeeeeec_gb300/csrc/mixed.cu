@@ -129,9 +129,9 @@ static bool persistent_ok(const float *c, long long ldc, int row0, int col0) {
     return ((uintptr_t)base & 15) == 0 && (ldc & 1) == 0;
 }
 
+template <int BN, int S>
 static bool launch_tc_persistent(const void *a, const void *br, const void *bi, float *c, int m, int n, int k,
                                  int row0, int col0, long long ldc, int *d_err) {
-    constexpr int BN = 128, S = 4;
     CUtensorMap ma, mbr, mbi, mc;
     if (!make_map_bf16(&ma, a, m, k, tc::kBM) || !make_map_bf16(&mbr, br, n, k, BN) ||
         !make_map_bf16(&mbi, bi, n, k, BN) || !make_map_c(&mc, c, ldc, row0, col0, m, n))
@@ -171,9 +171,12 @@ bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c
         return false;
     }
     // the LU's K is 192: three stages, 64-column tiles -> two CTAs per SM
-    if (k == 192) return launch_tc<64, 2, 3>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
+    // narrow updates (the panel's K = 6 x 32 columns): 64-column tiles
+    const bool narrow = k <= 192;
     if (persistent_enabled() && persistent_ok(c, ldc, row0, col0))
-        return launch_tc_persistent(a, br, bi, c, m, n, k, row0, col0, ldc, d_err);
+        return narrow ? launch_tc_persistent<64, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err)
+                      : launch_tc_persistent<128, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err);
+    if (narrow) return launch_tc<64, 2, 3>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
     return launch_tc<128, 2, 4>(a, br, bi, c, c, m, n, k, row0, col0, ldc, d_err, 1);
 }
 

@@ -346,6 +346,33 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int 
                  "r"(x), "r"(y), "r"(smem_u32(smem_src))
                  : "memory");
 }
+// L2 policies: the A / B operands are re-read by every tile row / column and
+// should stay in L2 while C streams through once.
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void tma_load_2d_hint(void *smem_dst, const CUtensorMap *map, int x, int y, uint64_t *bar,
+                                                 uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+        "%3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_2d_hint(const CUtensorMap *map, int x, int y, const void *smem_src,
+                                                  uint64_t policy) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%1, %2}], [%3], %4;" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(smem_u32(smem_src)), "l"(policy)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
@@ -429,6 +456,7 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 0) {
         if (lane == 0) {
             long long it = 0;
+            const uint64_t keep = policy_evict_last();
             for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
                 const int tm = (t / tiles_n) * kBM, tn = (t % tiles_n) * BN;
                 for (int kt = 0; kt < ktiles; ++kt, ++it) {
@@ -439,9 +467,9 @@ __global__ void __launch_bounds__(192, 1)
                     }
                     unsigned char *sa = base + s * stage_bytes;
                     mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
-                    tma_load_2d(sa, &map_a, kt * kBK, tm, &full[s]);
-                    tma_load_2d(sa + a_bytes, &map_br, kt * kBK, tn, &full[s]);
-                    tma_load_2d(sa + a_bytes + b_bytes, &map_bi, kt * kBK, tn, &full[s]);
+                    tma_load_2d_hint(sa, &map_a, kt * kBK, tm, &full[s], keep);
+                    tma_load_2d_hint(sa + a_bytes, &map_br, kt * kBK, tn, &full[s], keep);
+                    tma_load_2d_hint(sa + a_bytes + b_bytes, &map_bi, kt * kBK, tn, &full[s], keep);
                 }
             }
         }
@@ -496,6 +524,7 @@ __global__ void __launch_bounds__(192, 1)
         long long gi = 0;  // C chunk sequence number (buffer gi & 1)
         int lt = 0;
         int t = blockIdx.x;
+        const uint64_t stream_c = policy_evict_first();
         auto uniform_fail = [&](bool ok) -> bool {
             if (!ok) {
                 s_epi_fail = 1;
@@ -511,7 +540,7 @@ __global__ void __launch_bounds__(192, 1)
         // prefetch the first chunk
         if (leader && t < ntiles) {
             mbar_expect_tx(&cfull[0], chunk_bytes);
-            tma_load_2d(cbuf, &map_c, 2 * ((t % tiles_n) * BN), (t / tiles_n) * kBM, &cfull[0]);
+            tma_load_2d_hint(cbuf, &map_c, 2 * ((t % tiles_n) * BN), (t / tiles_n) * kBM, &cfull[0], stream_c);
         }
         for (; t < ntiles; t += gridDim.x, ++lt) {
             const int b = lt & 1;
@@ -532,8 +561,8 @@ __global__ void __launch_bounds__(192, 1)
                     if (nt < ntiles) {
                         const int nb = (int)((gi + 1) & 1);
                         mbar_expect_tx(&cfull[nb], chunk_bytes);
-                        tma_load_2d(cbuf + nb * chunk_bytes, &map_c, 2 * ((nt % tiles_n) * BN + nch * kEpiCols),
-                                    (nt / tiles_n) * kBM, &cfull[nb]);
+                        tma_load_2d_hint(cbuf + nb * chunk_bytes, &map_c, 2 * ((nt % tiles_n) * BN + nch * kEpiCols),
+                                         (nt / tiles_n) * kBM, &cfull[nb], stream_c);
                     }
                 }
                 __syncwarp();
@@ -560,7 +589,7 @@ __global__ void __launch_bounds__(192, 1)
                 __syncwarp();
                 epi_barrier();
                 if (leader) {
-                    tma_store_2d(&map_c, 2 * (tn + ch * kEpiCols), tm, cbuf + cb * chunk_bytes);
+                    tma_store_2d_hint(&map_c, 2 * (tn + ch * kEpiCols), tm, cbuf + cb * chunk_bytes, stream_c);
                     bulk_commit();
                 }
             }
