@@ -128,6 +128,10 @@ int peec_gb300_complex_lu_solve_device(const Complex *d_lu, const int *d_perm,
 void peec_gb300_lu_timing_enable(int on);
 int peec_gb300_lu_timing(double *ms_panel, double *ms_swap_trsm, double *ms_update,
                          double *update_flops);
+/* Of the last timed mixed-precision factorisation: the time (ms) and issued
+ * BF16 tensor flops of the outer-block trailing GEMMs alone (K = 6 x 256,
+ * operand splits excluded); -1 unless timing is enabled. */
+int peec_gb300_lu_timing_trailing(double *ms, double *issued_flops);
 
 /* Measured FMA issue rates of this GPU's FP64 and FP32 pipes (TFLOP/s). */
 int peec_gb300_pipe_peaks(double *fp64_tflops, double *fp32_tflops);

@@ -222,6 +222,7 @@ EXT_SYMBOLS = [
       C.c_size_t]),
     ("peec_gb300_lu_timing_enable", None, [C.c_int]),
     ("peec_gb300_lu_timing", C.c_int, [c_double_p, c_double_p, c_double_p, c_double_p]),
+    ("peec_gb300_lu_timing_trailing", C.c_int, [c_double_p, c_double_p]),
     ("peec_gb300_pipe_peaks", C.c_int, [c_double_p, c_double_p]),
     ("peec_gb300_tc_gemm", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,

@@ -29,6 +29,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -75,6 +76,7 @@ struct RegionsDev {
     double *dir = nullptr;     // [n*3]   (inductance)
     double *scale = nullptr;   // [n]     width w (inductance) or area S (potential); <= 0 marks a bad region
     int *same_obj = nullptr;   // [np]    object id for the reference's pointer test
+    float4 *boxf = nullptr;    // [np*2]  box rounded to FP32: (lo, size), (hi, 0) -- the scan's far filter
     double cmax = 0.0;         // largest |corner coordinate| (scale of the rounding noise)
 };
 
@@ -105,8 +107,11 @@ __global__ void k_patch_prep(RegionsDev R) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= R.np) return;
     const double *c = R.corner + 12 * (size_t)p;
-    patch_aabb(c, R.box + 6 * (size_t)p);
+    double *b = R.box + 6 * (size_t)p;
+    patch_aabb(c, b);
     R.size[p] = patch_size(c);
+    R.boxf[2 * p] = make_float4((float)b[0], (float)b[1], (float)b[2], (float)R.size[p]);
+    R.boxf[2 * p + 1] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
 }
 
 // Far-rule points of patch p: triangle t (0: corners 0,1,2; 1: 0,2,3), point
@@ -167,6 +172,14 @@ __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, Ne
     const double *ci = R.corner + 12 * (size_t)i, *bi = R.box + 6 * (size_t)i;
     double hi = R.size[i];
     int w = pass ? off[i] : 0, found = 0;
+    // FP32 filter: a pair whose FP32 gap exceeds the FP32 threshold by more
+    // than the rounding of both (boxes rounded to FP32 move by <= 2^-24 cmax
+    // per coordinate; the margins below are 4x the worst case) is FAR in the
+    // exact FP64 test as well; every other pair takes the exact test.
+    const float4 la = R.boxf[2 * i], ha4 = R.boxf[2 * i + 1];
+    const float nf = (float)s.near_factor;
+    const float slack = (float)(9.5367431640625e-07 * R.cmax);  // 2^-20 cmax
+    const int same_i = R.same_obj[i];
     unsigned long long nfar = 0;
     int b_prev = -1;
     bool skip_b = false;
@@ -181,8 +194,21 @@ __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, Ne
             j = R.off[b + 1] - 1;  // jump to the next region
             continue;
         }
+        const bool same = same_i == R.same_obj[j];
+        if (!same) {
+            const float4 lb = R.boxf[2 * j], hb4 = R.boxf[2 * j + 1];
+            float gx = fmaxf(0.0f, fmaxf(la.x - hb4.x, lb.x - ha4.x));
+            float gy = fmaxf(0.0f, fmaxf(la.y - hb4.y, lb.y - ha4.y));
+            float gz = fmaxf(0.0f, fmaxf(la.z - hb4.z, lb.z - ha4.z));
+            float gap = sqrtf(gx * gx + gy * gy + gz * gz);
+            float h = fmaxf(la.w, lb.w);
+            if (gap * (1.0f - 9.5367431640625e-07f) - slack > nf * h * (1.0f + 9.5367431640625e-07f)) {
+                ++nfar;
+                continue;
+            }
+        }
         int cls = classify_pair(ci, bi, hi, R.corner + 12 * (size_t)j, R.box + 6 * (size_t)j, R.size[j],
-                                s.near_factor, R.same_obj[i] == R.same_obj[j]);
+                                s.near_factor, same);
         if (cls == CLS_FAR) {
             ++nfar;
             continue;
@@ -546,6 +572,345 @@ __global__ void k_near_finalize(int nrec, const double *slot, const int *kind, d
         kr += v;
     }
     kval[r] = make_double2(bad_f ? nan("") : kf, bad_r ? nan("") : kr);
+}
+
+// ---------------------------------------------------------------------
+// 5a. level-synchronous form of the adaptive rule
+//
+// The depth-first warp above serialises a job's whole refinement tree, and a
+// few deep jobs (edge- and vertex-touching pairs refine towards the shared
+// edge to depth ~20) set the time of the launch.  Here the trees of all
+// jobs grow one level per launch: every node of the level is one warp (the
+// same low / high rules and decisions as the reference's recursion), accepted
+// nodes keep `high`, refined nodes append their two children to the next
+// level.  The value is then formed bottom-up exactly as the recursion returns
+// it, value(node) = value(left) + value(right) (quadrature.c:936-937), and a
+// top-down pass numbers the nodes in depth-first order to write the decision
+// trace the reuse replay reads.  The critical path is the tree depth
+// (<= 24 levels) instead of the largest tree's node count.
+struct LevelJob {
+    TriPot inner;
+    int order;
+    int slot;  // r * 8 + t * 2 + d
+    int rec;   // record (marginal flags)
+};
+
+struct LevelNode {
+    double v[9];
+    double tol;
+    double val;
+    int job;    // index into the chunk's LevelJob array
+    int depth;
+    int child;  // first child (left; right = child + 1) or -1
+    int size;   // nodes in the subtree
+    int pos;    // depth-first position in the job's tree
+    int edge;   // bisected edge of a refined node
+};
+
+struct LevelArgs {
+    const double *corner;
+    const NearRec *rec;
+    const int *job_rec;
+    long long job0, njob;  // jobs [job0, job0 + njob) of the launch's job numbering
+    int orders[4];
+    double *slot;
+    int *kind;
+    int *marginal;
+    unsigned char *trace;  // [jobs * kTraceCap] or null
+    int *trace_len;
+    LevelJob *jobs;        // [njob]
+    LevelNode *pool;
+    int *count;            // nodes appended to the next level
+    int *overflow;
+    unsigned long long *evals;
+};
+
+// One thread per job: zero-area and identical-triangle jobs are finished
+// here (as in k_near_eval); adaptive jobs get their root node.
+__global__ void k_level_init(LevelArgs A, int base0, int cap) {
+    long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= A.njob) return;
+    const long long job = A.job0 + g;
+    int r = (int)(job >> 3), t = (int)((job >> 1) & 3), d = (int)(job & 1);
+    if (A.job_rec) r = A.job_rec[r];
+    NearRec rec = A.rec[r];
+    double ta[9], tb[9];
+    patch_triangle(A.corner + 12 * (size_t)rec.i, t >> 1, ta);
+    patch_triangle(A.corner + 12 * (size_t)rec.j, t & 1, tb);
+    const double *outer = d == 0 ? ta : tb, *inner = d == 0 ? tb : ta;
+    LevelJob &J = A.jobs[g];
+    TriPot po;
+    tri_prepare(outer, po);
+    tri_prepare(inner, J.inner);
+    J.slot = r * 8 + t * 2 + d;
+    J.rec = r;
+    int kind;
+    if (po.twice_area == 0.0 || J.inner.twice_area == 0.0) {
+        kind = 1;
+        A.slot[J.slot] = 0.0;
+    } else {
+        bool identical = true;
+        for (int m = 0; m < 3; ++m) {
+            bool hit = false;
+            for (int q = 0; q < 3; ++q)
+                if (same_point(ta + 3 * m, tb + 3 * q)) hit = true;
+            if (!hit) identical = false;
+        }
+        if (identical) {
+            kind = 2;
+            double s = 0.0;
+            for (int m = 0; m < 3; ++m) s += tri_potential(J.inner, outer + 3 * m);
+            A.slot[J.slot] = po.twice_area * s / 3.0;
+            atomicAdd(A.evals, 3ull);
+        } else {
+            kind = 0;
+            int order = rec.cls == CLS_SELF ? A.orders[3] : rec.cls == CLS_TOUCHING ? A.orders[2] : A.orders[1];
+            if (order < 6) order = 6;
+            J.order = order;
+            double aa = d == 0 ? po.twice_area : J.inner.twice_area;
+            double ab = d == 0 ? J.inner.twice_area : po.twice_area;
+            double scale = aa * ab / sqrt(fmax(aa, ab));
+            int at = atomicAdd(A.count, 1);
+            if (at >= cap) {
+                atomicExch(A.overflow, 1);
+            } else {
+                LevelNode &nd = A.pool[base0 + at];
+                for (int k = 0; k < 9; ++k) nd.v[k] = outer[k];
+                nd.tol = 2e-5 * scale;
+                nd.job = (int)g;
+                nd.depth = 0;
+                nd.child = -1;
+                nd.pos = 0;
+            }
+        }
+    }
+    if (d == 0) A.kind[(size_t)r * 4 + t] = kind;
+    if (kind != 0 && A.trace_len) A.trace_len[job] = 0;
+}
+
+// One warp per node of one level.
+__global__ void __launch_bounds__(256, 2) k_level_eval(LevelArgs A, int base, int n, int next_base, int cap) {
+    __shared__ TriPot s_inner[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = blockIdx.x * 8ll + warp;
+    if (w >= n) return;
+    LevelNode &nd = A.pool[base + w];
+    const LevelJob &J = A.jobs[nd.job];
+    TriPot &inner = s_inner[warp];
+    {
+        const double *src = reinterpret_cast<const double *>(&J.inner);
+        double *dst = reinterpret_cast<double *>(&inner);
+        for (int k = lane; k < (int)(sizeof(TriPot) / sizeof(double)); k += 32) dst[k] = src[k];
+    }
+    double v[9];
+    for (int k = 0; k < 9; ++k) v[k] = nd.v[k];
+    const double tol = nd.tol;
+    const int depth = nd.depth, order = J.order;
+    __syncwarp();
+    const int ql = order <= 6 ? 3 : 4;
+    const int rl = gl_row(ql), rh = gl_row(order);
+    const int nlo = ql * ql, ntot = nlo + order * order;
+    double lo = 0.0, hi = 0.0;
+    for (int k = lane; k < ntot; k += 32) {
+        int ord, row, idx;
+        if (k < nlo) {
+            ord = ql;
+            row = rl;
+            idx = k;
+        } else {
+            ord = order;
+            row = rh;
+            idx = k - nlo;
+        }
+        int i = idx / ord, j = idx % ord;
+        double xi = c_gl_x[row][i], xj = c_gl_x[row][j];
+        double wi = c_gl_w[row][i], wj = c_gl_w[row][j];
+        double r[3], jac;
+        tri_map(v, v + 3, v + 6, 0.5 * (xi + 1.0), 0.5 * (xj + 1.0), r, &jac);
+        double val = 0.25 * wi * wj * jac * tri_potential(inner, r);
+        if (k < nlo)
+            lo += val;
+        else
+            hi += val;
+    }
+    lo = warp_sum(lo);
+    hi = warp_sum(hi);
+    if (lane != 0) return;
+    atomicAdd(A.evals, (unsigned long long)ntot);
+    nd.child = -1;
+    if (!isfinite(lo) || !isfinite(hi)) {
+        nd.val = nan("");
+        return;
+    }
+    int mflags = 0;
+    double thr = tol + 2e-5 * fabs(hi), gap = fabs(hi - lo);
+    if (fabs(gap - thr) <= 1e-6 * thr) mflags |= MARG_THRESHOLD;
+    if (gap <= thr) {
+        nd.val = hi;
+    } else if (depth >= 24) {
+        nd.val = nan("");  // quadrature.c:922
+    } else {
+        int e = 0;
+        double longest = 0.0, len[3];
+        for (int i = 0; i < 3; ++i) {
+            double sl = dist3(v + 3 * i, v + 3 * ((i + 1) % 3));
+            len[i] = sl;
+            if (sl > longest) {
+                longest = sl;
+                e = i;
+            }
+        }
+        for (int i = 0; i < 3; ++i)
+            if (i != e && len[i] >= longest * (1.0 - 1e-10)) mflags |= MARG_TIE;
+        nd.edge = e;
+        int at = atomicAdd(A.count, 2);
+        if (at + 2 > cap) {
+            atomicExch(A.overflow, 1);
+            nd.val = nan("");
+        } else {
+            nd.child = next_base + at;
+            LevelNode &left = A.pool[next_base + at], &right = A.pool[next_base + at + 1];
+            int j = (e + 1) % 3, k = (e + 2) % 3;
+            for (int dd = 0; dd < 3; ++dd) {
+                double mid = 0.5 * (v[3 * e + dd] + v[3 * j + dd]);
+                left.v[dd] = v[3 * e + dd];
+                left.v[3 + dd] = mid;
+                left.v[6 + dd] = v[3 * k + dd];
+                right.v[dd] = mid;
+                right.v[3 + dd] = v[3 * j + dd];
+                right.v[6 + dd] = v[3 * k + dd];
+            }
+            left.tol = right.tol = tol * 0.5;
+            left.depth = right.depth = depth + 1;
+            left.job = right.job = nd.job;
+            left.child = right.child = -1;
+        }
+    }
+    if (mflags && A.marginal) atomicOr(A.marginal + J.rec, mflags);
+}
+
+// value(node) = value(left) + value(right); subtree sizes
+__global__ void k_level_up(LevelNode *pool, int base, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    LevelNode &nd = pool[base + i];
+    if (nd.child >= 0) {
+        const LevelNode &l = pool[nd.child], &r = pool[nd.child + 1];
+        nd.val = l.val + r.val;
+        nd.size = 1 + l.size + r.size;
+    } else {
+        nd.size = 1;
+    }
+}
+
+// depth-first positions of the children; the decision trace
+__global__ void k_level_down(LevelArgs A, int base, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const LevelNode &nd = A.pool[base + i];
+    if (A.trace && nd.pos < kTraceCap)
+        A.trace[(size_t)(A.job0 + nd.job) * kTraceCap + nd.pos] = nd.child >= 0 ? (unsigned char)nd.edge : kAccept;
+    if (nd.child >= 0) {
+        LevelNode &l = A.pool[nd.child], &r = A.pool[nd.child + 1];
+        l.pos = nd.pos + 1;
+        r.pos = nd.pos + 1 + l.size;
+    }
+}
+
+// roots: the job's value, trace length, full-trace flag
+__global__ void k_level_roots(LevelArgs A, int base, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const LevelNode &nd = A.pool[base + i];
+    const LevelJob &J = A.jobs[nd.job];
+    A.slot[J.slot] = nd.val;
+    if (A.trace_len) A.trace_len[A.job0 + nd.job] = nd.size < kTraceCap ? nd.size : kTraceCap;
+    if (A.marginal && A.trace && nd.size > kTraceCap) atomicOr(A.marginal + J.rec, MARG_TRACE_FULL);
+}
+
+// PEEC_GB300_NEAR_LEVELS=0 keeps the depth-first warp form (k_near_eval).
+static bool near_levels_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PEEC_GB300_NEAR_LEVELS");
+        return !(e && strcmp(e, "0") == 0);
+    }();
+    return on;
+}
+
+// All 8 jobs of the first nrec records of E's list, level by level, in
+// chunks whose trees fit the node pool (a chunk that overflows is retried
+// with half the jobs).
+static bool near_eval_levels(const NearEvalArgs &E, int nrec) {
+    static const int kPoolNodes = 1 << 21;
+    const long long total = (long long)nrec * 8;
+    if (total == 0) return true;
+    long long chunk = total < (1 << 16) ? total : (1 << 16);
+    DBuf<LevelNode> pool(kPoolNodes);
+    DBuf<LevelJob> jobs((size_t)chunk);
+    DBuf<int> cnt(1), ovf(1);
+    if (!pool.p || !jobs.p || !cnt.p || !ovf.p) return false;
+    LevelArgs L;
+    L.corner = E.corner;
+    L.rec = E.rec;
+    L.job_rec = E.job_rec;
+    for (int k = 0; k < 4; ++k) L.orders[k] = E.orders[k];
+    L.slot = E.slot;
+    L.kind = E.kind;
+    L.marginal = E.marginal;
+    L.trace = E.trace;
+    L.trace_len = E.trace_len;
+    L.jobs = jobs.p;
+    L.pool = pool.p;
+    L.count = cnt.p;
+    L.overflow = ovf.p;
+    L.evals = E.evals;
+    std::vector<int> base, cnt_l;
+    for (long long job0 = 0; job0 < total;) {
+        const long long nj = std::min(chunk, total - job0);
+        L.job0 = job0;
+        L.njob = nj;
+        base.assign(1, 0);
+        cnt_l.clear();
+        int h[2] = {0, 0};
+        cudaMemsetAsync(cnt.p, 0, sizeof(int), stream());
+        cudaMemsetAsync(ovf.p, 0, sizeof(int), stream());
+        PEEC_LAUNCH(k_level_init, (unsigned)((nj + 127) / 128), 128, 0, L, 0, kPoolNodes);
+        cudaMemcpyAsync(&h[0], cnt.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+        cudaMemcpyAsync(&h[1], ovf.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+        if (!sync("near-field roots")) return false;
+        bool overflow = h[1] != 0;
+        cnt_l.push_back(h[0]);
+        while (!overflow && cnt_l.back() > 0) {
+            const int lv = (int)cnt_l.size() - 1;
+            const int next_base = base[lv] + cnt_l[lv];
+            cudaMemsetAsync(cnt.p, 0, sizeof(int), stream());
+            PEEC_LAUNCH(k_level_eval, (unsigned)((cnt_l[lv] + 7) / 8), 256, 0, L, base[lv], cnt_l[lv], next_base,
+                        kPoolNodes - next_base);
+            cudaMemcpyAsync(&h[0], cnt.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            cudaMemcpyAsync(&h[1], ovf.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            if (!sync("near-field level")) return false;
+            overflow = h[1] != 0;
+            base.push_back(next_base);
+            cnt_l.push_back(h[0]);
+        }
+        if (overflow) {
+            if (nj == 1) {
+                set_error("near-field quadrature: one refinement tree exceeds %d nodes", kPoolNodes);
+                return false;
+            }
+            chunk = (nj + 1) / 2;
+            continue;
+        }
+        const int levels = (int)cnt_l.size() - 1;  // the last level is empty
+        for (int lv = levels - 1; lv >= 0; --lv)
+            PEEC_LAUNCH(k_level_up, (unsigned)((cnt_l[lv] + 255) / 256), 256, 0, pool.p, base[lv], cnt_l[lv]);
+        for (int lv = 0; lv < levels; ++lv)
+            PEEC_LAUNCH(k_level_down, (unsigned)((cnt_l[lv] + 255) / 256), 256, 0, L, base[lv], cnt_l[lv]);
+        if (cnt_l[0] > 0) PEEC_LAUNCH(k_level_roots, (unsigned)((cnt_l[0] + 255) / 256), 256, 0, L, base[0], cnt_l[0]);
+        if (!launch_ok("near-field levels")) return false;
+        job0 += nj;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------
@@ -1192,11 +1557,12 @@ static bool gather_regions(const Mesh *mesh, const DualMesh *dual, int kind, Hos
 struct DeviceRegions {
     DBuf<int> off, owner, same_obj;
     DBuf<double> corner, box, size, dir, scale;
+    DBuf<float4> boxf;
     RegionsDev view;
     bool upload(const HostRegions &H) {
         int np = H.off[H.n];
         if (!off.alloc(H.n + 1) || !owner.alloc(np) || !same_obj.alloc(np) || !corner.alloc(12 * (size_t)np) ||
-            !box.alloc(6 * (size_t)np) || !size.alloc(np) || !scale.alloc(H.n) ||
+            !box.alloc(6 * (size_t)np) || !size.alloc(np) || !scale.alloc(H.n) || !boxf.alloc(2 * (size_t)np) ||
             !dir.alloc(H.dir.empty() ? 0 : H.dir.size()))
             return false;
         bool ok = off.upload(H.off.data(), H.off.size()) && scale.upload(H.scale.data(), H.scale.size());
@@ -1211,6 +1577,7 @@ struct DeviceRegions {
         view.corner = corner.p;
         view.box = box.p;
         view.size = size.p;
+        view.boxf = boxf.p;
         view.dir = dir.p;
         view.scale = scale.p;
         view.cmax = 0.0;
@@ -1365,13 +1732,15 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         std::call_once(attr_once, [smem] {
             cudaFuncSetAttribute(k_near_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         });
-        auto launch_eval = [&](int nj) {
+        auto launch_eval = [&](int nj) -> bool {
+            if (near_levels_enabled()) return near_eval_levels(A, nj);
             long long jobs = (long long)nj * 8;
             long long want = (jobs + 7) / 8;
             int grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
             if (grid > 0) PEEC_LAUNCH(k_near_eval, grid, 256, smem, A);
+            return true;
         };
-        launch_eval(njobrec);
+        if (!launch_eval(njobrec)) return -1;
         DBuf<int> src, evalf, rpos, replay, fcode, failed, slot_of2, isnew, off2, list2, elist;
         DBuf<unsigned long long> key2;
         DBuf<RoundSlot> tab2;
@@ -1429,7 +1798,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
                 A.nrec = nnew;
                 A.trace = rtrace.p;
                 A.trace_len = rtrace_len.p;
-                launch_eval(nnew);
+                if (!launch_eval(nnew)) return -1;
                 evaluated += (unsigned long long)nnew;
                 cur_trace = rtrace.p;
                 cur_len = rtrace_len.p;
@@ -1448,7 +1817,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
                 A.marginal = nullptr;
                 A.trace = nullptr;
                 A.trace_len = nullptr;
-                launch_eval(nre);
+                if (!launch_eval(nre)) return -1;
                 evaluated += (unsigned long long)nre;
             }
             if (stats) {

@@ -1852,16 +1852,17 @@ struct PanelScratch {
 // launches of every block column, summed at the end of the factorisation.
 struct LuTiming {
     bool enabled = false;
-    double ms[3] = {0, 0, 0};   // panel, swaps + trsm (+ splits), trailing update
-    double flops_update = 0.0;  // flops of the trailing updates (algorithmic, or issued BF16 for the mixed path)
+    double ms[4] = {0, 0, 0, 0};  // panel, swaps + trsm (+ splits), update, outer-block trailing GEMM
+    double flops_update = 0.0;    // flops of the trailing updates (algorithmic, or issued BF16 for the mixed path)
+    double flops_outer = 0.0;     // issued BF16 flops of the mixed path's outer-block trailing GEMMs
     std::vector<cudaEvent_t> ev;
     std::vector<int> cat;       // category of the interval that ends at each event (-1: none)
     void reset() {
         for (auto e : ev) cudaEventDestroy(e);
         ev.clear();
         cat.clear();
-        ms[0] = ms[1] = ms[2] = 0.0;
-        flops_update = 0.0;
+        ms[0] = ms[1] = ms[2] = ms[3] = 0.0;
+        flops_update = flops_outer = 0.0;
     }
     void mark(int c) {
         if (!enabled) return;
@@ -2567,8 +2568,17 @@ int peec_gb300_lu_timing(double *ms_panel, double *ms_swap_trsm, double *ms_upda
     if (!g_lu_timing.enabled) return -1;
     if (ms_panel) *ms_panel = g_lu_timing.ms[0];
     if (ms_swap_trsm) *ms_swap_trsm = g_lu_timing.ms[1];
-    if (ms_update) *ms_update = g_lu_timing.ms[2];
+    if (ms_update) *ms_update = g_lu_timing.ms[2] + g_lu_timing.ms[3];
     if (update_flops) *update_flops = g_lu_timing.flops_update;
+    return 0;
+}
+
+// Of the last timed mixed factorisation: time (ms) and issued BF16 flops of
+// the outer-block trailing GEMMs alone (K = 6 x 256; no operand splits).
+int peec_gb300_lu_timing_trailing(double *ms, double *issued_flops) {
+    if (!g_lu_timing.enabled) return -1;
+    if (ms) *ms = g_lu_timing.ms[3];
+    if (issued_flops) *issued_flops = g_lu_timing.flops_outer;
     return 0;
 }
 
@@ -3037,14 +3047,19 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
         return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
     };
-    auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw) -> bool {
+    auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw, bool outer = false) -> bool {
         if (m <= 0 || nc <= 0) return true;
         const int KW = (kw + 31) / 32 * 32;
         PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
         PEEC_LAUNCH(k_split_b, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
                     bpr.p, bpi.p);
         if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
-        return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
+        if (!outer) return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
+        tm.mark(2);
+        if (tm.enabled) tm.flops_outer += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);
+        const bool ok = tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
+        tm.mark(3);
+        return ok;
     };
     for (int K0 = 0; K0 < n; K0 += OB) {
         const int E = std::min(n, K0 + OB);  // the outer block is columns [K0, E)
@@ -3090,7 +3105,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
             tm.mark(2);
             // trailing update with K = 6 x (E - K0)
-            if (!tc_update(E, n - E, E, n - E, K0, E - K0)) return -1;
+            if (!tc_update(E, n - E, E, n - E, K0, E - K0, true)) return -1;
         }
     }
     tm.mark(2);
