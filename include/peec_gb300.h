@@ -154,13 +154,19 @@ int peec_gb300_tc_gemm_cplx(const void *d_a, const void *d_br, const void *d_bi,
 
 /* ---- mixed precision complex solve ----
  * Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
- * another) to a componentwise backward error <= tol: FP64 equilibration as
- * complex_lu_factorize, FP32 LU whose trailing updates run on the tensor
+ * another) to a componentwise backward error <= tol: row and column
+ * equilibration by powers of two, FP32 LU whose trailing updates run on the tensor
  * cores as split-BF16x3 products (FP32 accumulation), then FP64 iterative
  * refinement r = B - Z X.  d_Z and d_b are not modified.  Returns 0 when
  * converged, 1 when max_iter refinements did not reach tol (X holds the last
  * iterate), -2 for a zero / non-finite row or column or a singular FP32
  * pivot, -1 on other errors.  backward_error / iterations may be NULL. */
+/* The FP32 rounding used by the mixed-precision solve's equilibration:
+ * d_y[i] = d_x[i] * 2^-shift rounded to the nearest FP32 (ties to even) by
+ * integer operations on the FP64 bits; results below 2^-126 flush to zero,
+ * beyond the FP32 range give +-inf, NaN stays NaN. */
+int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, size_t count, int shift);
+
 int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Complex *d_b,
                                           Complex *d_x, size_t nrhs, double tol, int max_iter,
                                           double *backward_error, int *iterations);

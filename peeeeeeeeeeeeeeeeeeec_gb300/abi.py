@@ -230,6 +230,7 @@ EXT_SYMBOLS = [
     ("peec_gb300_tc_gemm_cplx", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
       C.c_longlong]),
+    ("peec_gb300_round_to_f32_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]),
     ("peec_gb300_complex_solve_mixed_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, c_double_p,
       c_int_p]),

@@ -2588,8 +2588,8 @@ int peec_gb300_lu_timing_trailing(double *ms, double *issued_flops) {
 // Mixed precision: FP32 complex LU with a split-BF16x3 tensor-core
 // trailing update, then FP64 iterative refinement against the FP64 matrix.
 //
-//   equilibrate in FP64 as complex_lu_factorize does (row scales, then
-//   column scales of the row-scaled matrix), round to FP32 complex;
+//   equilibrate by powers of two (row scales, then column scales of the
+//   row-scaled matrix, in integer exponent arithmetic), round to FP32 complex;
 //   per block column: cooperative FP32 panel (same pivot rule), row swaps,
 //   U12 = L11^-1 A12 in FP32, then split L21 and U12 into BF16 hi/lo parts,
 //     A'  = [Lr_h Lr_h Lr_l Li_h Li_h Li_l]            (K' = 6 x 32)
@@ -2606,55 +2606,98 @@ namespace peec {
 bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c, int m, int n, int k, int row0,
                          int col0, long long ldc, int *d_err);
 
-__global__ void k_eq_row_scale(const cplx *z, int n, double *rs, Status *st) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+// x * 2^-shift rounded to FP32 (nearest, ties to even) by integer operations
+// on the bits: no FP64 instruction (one warp-wide FP64 operation costs ~64
+// cycles on GB300).  Zero and subnormal inputs and results below 2^-126
+// give (signed) zero; results beyond the FP32 range give +-inf; NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32_scaled(double x, int shift) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    if (ex == 0x7ff) return __uint_as_float(sign | (m ? 0x7fc00000u : 0x7f800000u));
+    if (ex == 0) return __uint_as_float(sign);
+    int e = ex - 1023 - shift;
+    if (e < -126) return __uint_as_float(sign);
+    unsigned m23 = (unsigned)(m >> 29);
+    const unsigned long long rem = m & 0x1FFFFFFFull;
+    if (rem > 0x10000000ull || (rem == 0x10000000ull && (m23 & 1u))) {
+        if (++m23 == 0x800000u) {
+            m23 = 0;
+            ++e;
+        }
+    }
+    if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)(e + 127) << 23) | m23);
+}
+
+// |z| in FP32 for the backward error's denominator sum |Z||x| + |b| (a
+// stopping test: FP32 relative error there moves eta by ~1e-7 of itself);
+// values beyond the FP32 range clamp to 3e38, which can only shrink the
+// denominator, i.e. overstate eta.
+__device__ __forceinline__ float abs_f32(cplx z) {
+    const float m = hypotf(f64_to_f32_scaled(z.re, 0), f64_to_f32_scaled(z.im, 0));
+    return m < 3.0e38f ? m : 3.0e38f;
+}
+
+// Equilibration of the mixed path with power-of-two scales, in integer
+// exponent arithmetic: R_i = the largest exponent of row i (of max(|re|,
+// |im|)), C_j = max_i (E_ij - R_i) <= 0 over column j; the scaled entries
+// z 2^-(R_i + C_j) have magnitude < 2 with every column's largest >= 1, and
+// the scalings are exact.  Status 4: a non-finite entry; 5: a zero row or
+// column (as the FP64 equilibration).
+__device__ __forceinline__ int exp_of(double x) { return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff); }
+
+__global__ void k_eq2_row(const cplx *z, int n, int *er, double *rs, Status *st) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= n) return;
     const cplx *row = z + (size_t)warp * n;
-    double s = 0.0;
-    int bad = 0;
-    for (int j = lane; j < n; j += 32) {
-        double m = hypot(row[j].re, row[j].im);
-        if (!isfinite(m)) bad = 1;
-        s = fmax(s, m);
-    }
-    for (int d = 16; d > 0; d >>= 1) {
-        s = fmax(s, __shfl_xor_sync(0xffffffffu, s, d));
-        bad |= __shfl_xor_sync(0xffffffffu, bad, d);
-    }
+    int e = 0;
+    for (int j = lane; j < n; j += 32) e = max(e, max(exp_of(row[j].re), exp_of(row[j].im)));
+    for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
     if (lane == 0) {
-        if (bad || s == 0.0) atomicCAS(&st->code, 0, bad ? 4 : 5);
-        rs[warp] = s;
+        if (e == 0x7ff || e == 0) atomicCAS(&st->code, 0, e ? 4 : 5);
+        const int ee = (e == 0x7ff || e == 0) ? 1023 : e;
+        er[warp] = ee;
+        rs[warp] = __longlong_as_double((long long)ee << 52);  // 2^(R_i)
     }
 }
 
-__global__ void __launch_bounds__(256) k_eq_col_scale(const cplx *z, int n, const double *rs, double *cs,
-                                                      Status *st) {
-    __shared__ double part[8][32];
+__global__ void __launch_bounds__(256) k_eq2_col(const cplx *z, int n, const int *er, int *ec, double *cs,
+                                                 Status *st) {
+    __shared__ int part[8][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + lane;
-    double s = 0.0;
+    int c = -100000;
     if (j < n)
         for (int i = warp; i < n; i += 8) {
-            cplx v = z[(size_t)i * n + j];
-            double r = rs[i];
-            s = fmax(s, hypot(v.re / r, v.im / r));
+            const cplx v = z[(size_t)i * n + j];
+            const int e = max(exp_of(v.re), exp_of(v.im));
+            if (e != 0) c = max(c, e - er[i]);
         }
-    part[warp][lane] = s;
+    part[warp][lane] = c;
     __syncthreads();
     if (warp == 0 && j < n) {
-        for (int w = 1; w < 8; ++w) s = fmax(s, part[w][lane]);
-        if (s == 0.0) atomicCAS(&st->code, 0, 5);
-        cs[j] = s;
+        for (int w = 1; w < 8; ++w) c = max(c, part[w][lane]);
+        if (c < -1022) {
+            atomicCAS(&st->code, 0, 5);
+            c = 0;
+        }
+        ec[j] = c;
+        cs[j] = __longlong_as_double((long long)(c + 1023) << 52);  // 2^(C_j)
     }
 }
 
-__global__ void k_eq_to_float(const cplx *z, int n, const double *rs, const double *cs, cplxf *f) {
-    size_t nn = (size_t)n * n;
+// f = z 2^-(R_i + C_j) in FP32 and |z| in FP32 (the backward error's
+// denominator), one pass over Z
+__global__ void k_eq2_to_float(const cplx *z, int n, const int *er, const int *ec, cplxf *f, float *absz) {
+    const size_t nn = (size_t)n * n;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn; t += (size_t)gridDim.x * blockDim.x) {
-        int i = (int)(t / n), j = (int)(t % n);
-        cplx v = z[t];
-        double r = rs[i], c = cs[j];
-        f[t] = cplxf{(float)((v.re / r) / c), (float)((v.im / r) / c)};
+        const int i = (int)(t / n), j = (int)(t % n);
+        const cplx v = z[t];
+        const int shift = (er[i] - 1023) + ec[j];
+        f[t] = cplxf{f64_to_f32_scaled(v.re, shift), f64_to_f32_scaled(v.im, shift)};
+        if (absz) absz[t] = abs_f32(v);
     }
 }
 
@@ -2825,21 +2868,12 @@ __global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int 
     y[t] = cplxf{(float)(v.re / s), (float)(v.im / s)};
 }
 
-// x += D_c^-1 y  (FP64 accumulation of the FP32 correction)
-// |z| rounded to FP32 for the backward error's denominator sum |Z||x| + |b|
-// (a stopping test: FP32 relative error there moves eta by ~1e-7 of itself);
-// values beyond the FP32 range clamp to 3e38, which can only shrink the
-// denominator, i.e. overstate eta.
-__device__ __forceinline__ float abs_f32(cplx z) {
-    double m = sqrt(fma(z.re, z.re, z.im * z.im));
-    return m < 3.0e38 ? (float)m : 3.0e38f;
-}
-
 __global__ void k_abs_matrix(const cplx *Z, size_t count, float *out) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
         out[t] = abs_f32(Z[t]);
 }
 
+// x += D_c^-1 y  (FP64 accumulation of the FP32 correction)
 __global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs, float *absx) {
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)n * nrhs) return;
@@ -3013,10 +3047,13 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         sc.cand_row = bb + off;
         sc.krow = bb + off + 2 * G * NB * sizeof(cplxf);
     }
-    // equilibrate in FP64, round to FP32
-    PEEC_LAUNCH(k_eq_row_scale, (unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, Z, n, rs.p, st.p);
-    PEEC_LAUNCH(k_eq_col_scale, (n + 31) / 32, 256, 0, Z, n, rs.p, cs.p, st.p);
-    PEEC_LAUNCH(k_eq_to_float, 152 * 16, 256, 0, Z, n, rs.p, cs.p, f.p);
+    // equilibrate by powers of two, round to FP32; |Z| in FP32 in the same pass
+    DBuf<int> er(n), ec(n);
+    DBuf<float> absZ(nn);
+    if (!er.p || !ec.p || !absZ.p) return -1;
+    PEEC_LAUNCH(k_eq2_row, (unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, Z, n, er.p, rs.p, st.p);
+    PEEC_LAUNCH(k_eq2_col, (n + 31) / 32, 256, 0, Z, n, er.p, ec.p, cs.p, st.p);
+    PEEC_LAUNCH(k_eq2_to_float, 152 * 16, 256, 0, Z, n, er.p, ec.p, f.p, absZ.p);
     PEEC_LAUNCH(k_max_mag<cplxf>, 152 * 8, 256, 0, f.p, nn, mx.p);
     unsigned long long bits = 0;
     Status hs;
@@ -3136,9 +3173,8 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     DBuf<unsigned> wflags(wave_flag_count<cplxf>(n, nrhs));
     DBuf<int> werr(1);
     DBuf<cplxf> wdinv(wave_dinv_count(n));
-    DBuf<float> absZ(nn), absx(nv);
-    if (!wflags.p || !werr.p || !wdinv.p || !absZ.p || !absx.p) return -1;
-    PEEC_LAUNCH(k_abs_matrix, 152 * 8, 256, 0, Z, nn, absZ.p);
+    DBuf<float> absx(nv);
+    if (!wflags.p || !werr.p || !wdinv.p || !absx.p) return -1;
     cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
     if (!wave_prepare(a, n, wdinv.p)) return -1;
     // one refinement sweep (FP32 correction solve, FP64 update, FP64
@@ -3211,6 +3247,23 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     if (backward_error) *backward_error = eta;
     if (iterations) *iterations = it > max_iter ? max_iter : it;
     return eta <= tol ? 0 : 1;
+}
+
+namespace peec {
+__global__ void k_round_f32(const double *x, float *y, size_t count, int shift) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
+        y[t] = f64_to_f32_scaled(x[t], shift);
+}
+}  // namespace peec
+
+// The FP32 rounding of the mixed path's equilibration: y = x 2^-shift to the
+// nearest FP32 (ties to even), subnormal results flushed to zero.
+extern "C" int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, size_t count, int shift) {
+    using namespace peec;
+    if ((!d_x || !d_y) && count) return -1;
+    if (!count) return 0;
+    PEEC_LAUNCH(k_round_f32, 152 * 4, 256, 0, d_x, d_y, count, shift);
+    return sync("FP32 rounding") ? 0 : -1;
 }
 
 extern "C" int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine) {

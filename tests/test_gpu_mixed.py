@@ -174,3 +174,35 @@ def test_fp64_refinement_reaches_the_gate_at_low_frequency(gpu_lib):
     assert s == 0, (be.value, it.value)
     for q in range(4):
         assert backward_error(Z, X[q], B[q]) <= 1e-10
+
+
+def test_fp32_rounding_matches_ieee(gpu_lib):
+    """The integer-arithmetic FP64 -> FP32 rounding of the equilibration
+    against IEEE round-to-nearest-even (numpy), with ties, carries into the
+    exponent, overflow, the subnormal flush, zeros, inf and NaN."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([
+        rng.standard_normal(20000) * 10.0 ** rng.uniform(-30, 30, 20000),
+        np.float64(np.float32(rng.standard_normal(2000))) * (1 + 2.0 ** -24),   # exact ties
+        np.float64(np.float32(rng.standard_normal(2000))) * (1 - 2.0 ** -25),
+        np.array([0.0, -0.0, 1.0, -1.0, 2.0 ** -126, 2.0 ** -127, 2.0 ** -149, 3.4028234663852886e38,
+                  3.4028235677973366e38, 1e39, -1e39, np.inf, -np.inf, np.nan, 1.9999999999999998,
+                  1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, 5e-324])])
+    for shift in (0, 7, -5):
+        n = x.size
+        dx = gpu_lib.peec_gb300_device_alloc(x.nbytes)
+        dy = gpu_lib.peec_gb300_device_alloc(n * 4)
+        gpu_lib.peec_gb300_copy_to_device(dx, x.ctypes.data, x.nbytes)
+        assert gpu_lib.peec_gb300_round_to_f32_device(dx, dy, n, shift) == 0
+        y = np.zeros(n, dtype=np.float32)
+        gpu_lib.peec_gb300_copy_to_host(y.ctypes.data, dy, y.nbytes)
+        gpu_lib.peec_gb300_device_free(dx)
+        gpu_lib.peec_gb300_device_free(dy)
+        with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+            ref = (x * 2.0 ** -shift).astype(np.float32)
+        tiny = np.abs(ref) < np.float32(2.0 ** -126)
+        ref[tiny] = np.copysign(np.float32(0.0), ref[tiny])
+        # a subnormal FP64 input (the last one) is flushed too
+        ref[np.abs(x) < 2.0 ** -1022] = np.copysign(np.float32(0.0), x[np.abs(x) < 2.0 ** -1022])
+        assert np.array_equal(y.view(np.uint32)[~np.isnan(ref)], ref.view(np.uint32)[~np.isnan(ref)]), shift
+        assert np.all(np.isnan(y[np.isnan(ref)]))
