@@ -1296,25 +1296,36 @@ __device__ __forceinline__ f2 df_rsqrt(f2 x) {
     return quick_two_sum(y, c);
 }
 
-// FP32 form (the mixed-precision path): hi parts only, FP32 rsqrt and
-// per-lane FP32 accumulation, combined across lanes in FP64.  Relative error
-// of an entry ~1e-7.
-__device__ __forceinline__ double far_pair_f32(const FarPtF *pa, const FarPtF *pb, int npts) {
+// FP32 form accumulating into this lane's running double-float sum `acc`
+// (reduced across the warp once per entry): each lane's point sum over the
+// partner patch is FP32; adding it into a (hi, lo) pair keeps the entry's
+// sum of ~16 k products at FP32 accuracy.  NaN propagates into `acc`.
+__device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF *pb, int npts, f2 &acc) {
     const int lane = threadIdx.x & 31;
-    double acc = 0.0;
     for (int p = lane; p < npts; p += 32) {
-        FarPtF A = pa[p];
-        float s = 0.0f;
-#pragma unroll 4
-        for (int q = 0; q < npts; ++q) {
-            FarPtF B = pb[q];
-            float dx = A.xh - B.xh, dy = A.yh - B.yh, dz = A.zh - B.zh;
+        const float4 A = *reinterpret_cast<const float4 *>(pa + p);  // xh, yh, zh, wh
+        float s0 = 0.0f, s1 = 0.0f;
+        int q = 0;
+        for (; q + 1 < npts; q += 2) {
+            const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
+            const float4 B1 = *reinterpret_cast<const float4 *>(pb + q + 1);
+            float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
             float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (!(r2 <= 0.0f)) s = fmaf(B.wh, rsqrtf(r2), s);
+            if (!(r2 <= 0.0f)) s0 = fmaf(B0.w, rsqrtf(r2), s0);
+            dx = A.x - B1.x;
+            dy = A.y - B1.y;
+            dz = A.z - B1.z;
+            r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (!(r2 <= 0.0f)) s1 = fmaf(B1.w, rsqrtf(r2), s1);
         }
-        acc = fma((double)A.wh, (double)s, acc);
+        if (q < npts) {
+            const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
+            float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
+            float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (!(r2 <= 0.0f)) s0 = fmaf(B0.w, rsqrtf(r2), s0);
+        }
+        acc = df_add(acc, two_sum(A.w * s0, A.w * s1));
     }
-    return warp_sum(acc);
 }
 
 // Double-float form, accumulating into this lane's running sum `acc` (the
@@ -1442,17 +1453,39 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                 // the other modes) add in the reference's (i, j) order
                 f2 facc = {0.0f, 0.0f};
                 bool fbad = false;
-                for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i)
+                for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i) {
+                    // i's near partners are sorted by j (the scan's list):
+                    // a cursor from the first partner in region b
+                    const int mhi = T.near_off[i + 1];
+                    int m = T.near_off[i];
+                    for (int hi = mhi; m < hi;) {
+                        const int mid = (m + hi) >> 1;
+                        if (T.near_rec[mid].j < R.off[b])
+                            m = mid + 1;
+                        else
+                            hi = mid;
+                    }
                     for (int j = R.off[b]; j < R.off[b + 1]; ++j) {
                         double k;
-                        if (!near_lookup(T, i, j, k)) {
+                        bool near;
+                        if (a == b && i > j) {
+                            near = near_lookup(T, i, j, k);  // (j, i), reversed, in j's list
+                        } else {
+                            while (m < mhi && T.near_rec[m].j < j) ++m;
+                            near = m < mhi && T.near_rec[m].j == j;
+                            if (near) k = T.near_k[m].x;
+                        }
+                        if (!near) {
                             if (T.far_df == 1) {
                                 far_pair_df_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, facc,
                                                 fbad);
                                 continue;
                             }
-                            k = T.far_df == 2 ? far_pair_f32(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts)
-                                              : far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
+                            if (T.far_df == 2) {
+                                far_pair_f32_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, facc);
+                                continue;
+                            }
+                            k = far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
                         }
                         if (!isfinite(k)) {
                             bad = true;
@@ -1460,7 +1493,8 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                         }
                         integral += k;
                     }
-                if (T.far_df == 1) {
+                }
+                if (T.far_df == 1 || T.far_df == 2) {
                     fbad = __any_sync(0xffffffffu, fbad);
                     double far = warp_sum_df(facc);
                     if (fbad || !isfinite(far)) bad = true;

@@ -465,6 +465,202 @@ __global__ void __launch_bounds__(256) k_panel_coop(T *a, int n, int k0, int kb,
     }
 }
 
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// ---- lean FP32 panel (the mixed path) ------------------------------
+// The same partial pivoting (first maximum of |z| in FP32 wins) with the
+// per-column critical path cut down, from measurements of the cooperative
+// panel on GB300 (8402 rows, 152 CTAs, per column: local argmax + publish
+// 0.94 us, grid barrier 2.3 us, candidate read + selection by 256 threads
+// 1.4 us, pivot row 0.2 us, update 0.6 us):
+//  * 64 threads per CTA, one row each: the argmax is a warp shuffle plus one
+//    two-warp exchange, and the next column's magnitude comes out of the
+//    update itself;
+//  * no grid barrier: each CTA publishes its candidate (row segment, index)
+//    and then one epoch-tagged flag word carrying the FP32 magnitude; one
+//    warp polls the G flags (a flag per 128-byte line), which synchronises
+//    and delivers the magnitudes in one step;
+//  * multipliers by one complex reciprocal of the pivot instead of a
+//    division per row.
+// Epochs grow monotonically (base from the slots word, advanced by CTA 0 at
+// the end), so flags of earlier columns or launches never match.  Every
+// wait is bounded (status 6).
+static const int kLeanThreads = 64;
+static const int kLeanFlagStride = 16;  // u64 words per flag: one 128-byte line each
+
+__device__ __forceinline__ float lean_mag(cplxf v, bool diag) {
+    float m = hypotf(v.re, v.im);
+    if (isnan(m)) m = diag ? INFINITY : -1.0f;  // NaN below the diagonal never wins; on it, +inf is rejected
+    return m;
+}
+
+__global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, int k0, int kb, double limit,
+                                                             long long *piv, Status *st, PanelSlots *ps,
+                                                             unsigned long long *flag, int *cand_idx,
+                                                             cplxf *cand_row, cplxf *krow) {
+    __shared__ cplxf tile[kLeanThreads][kPS];
+    __shared__ cplxf s_prow[NB];
+    __shared__ float s_wv[2], s_fb;
+    __shared__ int s_wi[2], s_gc, s_p, s_timeout;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned G = gridDim.x;
+    const int c = blockIdx.x;
+    const int r0 = k0 + c * kLeanThreads, r1 = min(n, r0 + kLeanThreads);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform across CTAs (set before launch)
+    const unsigned gen0 = *(volatile unsigned *)&ps->gen;
+    for (int t = tid; t < nrows * kb; t += kLeanThreads) {
+        const int i = t / kb, j = t % kb;
+        tile[i][j] = a[(size_t)(r0 + i) * n + k0 + j];
+    }
+    if (tid == 0) s_timeout = 0;
+    __syncthreads();
+    const int i = r0 + tid;
+    const bool mine = tid < nrows;
+    cplxf *row = tile[tid];
+    float mv = mine ? lean_mag(row[0], i == k0) : -1.0f;
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk, par = kk & 1;
+        const unsigned epoch = gen0 + (unsigned)kk + 1u;
+        // this CTA's candidate: largest magnitude, lowest row
+        float bv = (mine && i >= k) ? mv : -1.0f;
+        int bi = bv >= 0.0f ? i : n;
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, sh);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_wv[warp] = bv;
+            s_wi[warp] = bi;
+        }
+        __syncthreads();
+        if (s_wv[1] > s_wv[0] || (s_wv[1] == s_wv[0] && s_wi[1] < s_wi[0])) {
+            bv = s_wv[1];
+            bi = s_wi[1];
+        } else {
+            bv = s_wv[0];
+            bi = s_wi[0];
+        }
+        // publish the candidate row and, if owned here, row k; then the flag
+        if (warp == 0 && bi < n && lane < kb) cand_row[((size_t)par * G + c) * NB + lane] = tile[bi - r0][lane];
+        if (warp == 1 && k >= r0 && k < r1 && lane < kb) krow[(size_t)par * NB + lane] = tile[k - r0][lane];
+        if (tid == 0) cand_idx[par * G + c] = bi;
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_relaxed_u64(flag + (size_t)(par * G + c) * kLeanFlagStride,
+                           ((unsigned long long)epoch << 32) | __float_as_uint(bi < n ? bv : -1.0f));
+        }
+        // warp 0 polls the G flags: (largest magnitude, lowest CTA)
+        if (warp == 0) {
+            float fb = -2.0f;
+            int fq = -1;
+            bool ok = true;
+            for (unsigned q = lane; q < G && ok; q += 32) {
+                unsigned long long v = 0;
+                ok = false;
+                for (long long spin = 0; spin < kSpinLimit; ++spin) {
+                    v = ld_acquire_u64(flag + (size_t)(par * G + q) * kLeanFlagStride);
+                    if ((unsigned)(v >> 32) == epoch) {
+                        ok = true;
+                        break;
+                    }
+                    if ((spin & 1023) == 1023 && *(volatile int *)&ps->timeout) break;
+                }
+                const float f = __uint_as_float((unsigned)v);
+                if (ok && f >= 0.0f && (f > fb || (f == fb && (int)q < fq))) {
+                    fb = f;
+                    fq = (int)q;
+                }
+            }
+            if (!ok) atomicExch(&ps->timeout, 1);
+            const bool any_fail = __any_sync(0xffffffffu, !ok);
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const float ov = __shfl_xor_sync(0xffffffffu, fb, sh);
+                const int oq = __shfl_xor_sync(0xffffffffu, fq, sh);
+                if (oq >= 0 && (fq < 0 || ov > fb || (ov == fb && oq < fq))) {
+                    fb = ov;
+                    fq = oq;
+                }
+            }
+            if (lane == 0) {
+                s_gc = fq;
+                s_fb = fb;
+                s_timeout = any_fail ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        if (s_timeout) {
+            if (tid == 0) atomicCAS(&st->code, 0, 6);
+            return;
+        }
+        const int gc = s_gc;
+        const float gb = s_fb;
+        if (gc < 0 || !isfinite(gb) || (double)gb <= limit) {
+            if (c == 0 && tid == 0) {
+                st->code = 2;
+                st->column = k;
+                st->value = gc < 0 ? -1.0 : (double)gb;
+            }
+            return;
+        }
+        // the winner's row segment and index; the owner of p takes row k
+        cplxf kval = {0.0f, 0.0f};
+        if (gc == c) {
+            if (warp == 0 && lane < kb) s_prow[lane] = tile[bi - r0][lane];
+            if (tid == 0) s_p = bi;
+            if (warp == 1 && bi != k && lane < kb) kval = ld_volatile(krow + (size_t)par * NB + lane);
+        } else {
+            if (warp == 0 && lane < kb) s_prow[lane] = ld_volatile(cand_row + ((size_t)par * G + gc) * NB + lane);
+            if (warp == 1 && lane == 0) s_p = ld_volatile(cand_idx + par * G + gc);
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p != k) {
+            if (warp == 0 && k >= r0 && k < r1 && lane < kb) tile[k - r0][lane] = s_prow[lane];
+            if (warp == 1 && gc == c && lane < kb) tile[p - r0][lane] = kval;
+        }
+        if (c == 0 && tid == 0) piv[k] = p;
+        __syncthreads();
+        if (k + 1 >= n) break;
+        // update this thread's row; the next column's magnitude on the way
+        if (mine && i > k) {
+            const cplxf pv = s_prow[kk];
+            const float den = pv.re * pv.re + pv.im * pv.im;
+            const cplxf inv = {pv.re / den, -pv.im / den};
+            const cplxf x = row[kk];
+            const cplxf mlt = {x.re * inv.re - x.im * inv.im, x.re * inv.im + x.im * inv.re};
+            row[kk] = mlt;
+#pragma unroll 8
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mlt, s_prow[j]);
+            mv = kk + 1 < kb ? lean_mag(row[kk + 1], i == k + 1) : -1.0f;
+        } else {
+            mv = -1.0f;
+        }
+    }
+    __syncthreads();
+    for (int t = tid; t < nrows * kb; t += kLeanThreads) {
+        const int ii = t / kb, j = t % kb;
+        a[(size_t)(r0 + ii) * n + k0 + j] = tile[ii][j];
+    }
+    // every CTA read the base epoch before publishing column 0, and CTA 0
+    // gets here only after every CTA published the last column
+    if (c == 0 && tid == 0) atomicExch(&ps->gen, gen0 + (unsigned)kb);
+}
+
 // ---- cluster panel ----------------------------------------------------
 // The same partial-pivoting panel (first maximum wins, NaN never wins, the
 // same swaps and updates, so the same pivots as the reference) on one
@@ -1813,6 +2009,25 @@ static bool cluster_panel_enabled() {
     return on;
 }
 
+// CTAs of the lean FP32 panel for m rows (0: use another form).  Off with
+// PEEC_GB300_MIXED_PANEL=coop; the grid must be co-resident.
+static int lean_panel_ctas(int m) {
+    static const int cap = [] {
+        const char *e = getenv("PEEC_GB300_MIXED_PANEL");
+        if (e && strcmp(e, "coop") == 0) return 0;
+        int dev = 0, sms = 0, coop = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel_lean, kLeanThreads, 0) != cudaSuccess)
+            return 0;
+        return per_sm * sms;
+    }();
+    if (m < 2 * kLeanThreads) return 0;  // small panels: one CTA
+    const int g = (m + kLeanThreads - 1) / kLeanThreads;
+    return g <= cap ? g : 0;
+}
+
 // FP32 panels of the mixed path by tournament pivoting when
 // PEEC_GB300_MIXED_PANEL=calu; partial pivoting otherwise.  Measured on
 // GB300 (8402 unknowns) the tournament panel takes 75 ms per factorisation
@@ -3018,9 +3233,16 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t G = (size_t)sms;
     size_t sbytes = 256 + 2 * G * 8 + 2 * G * 4 + 16 + 2 * G * NB * sizeof(cplxf) + 2 * NB * sizeof(cplxf) + 64;
+    // lean panel slots: G_lean = ceil(n / 64) CTAs at most
+    const size_t GL = (size_t)(n + kLeanThreads - 1) / kLeanThreads;
+    DBuf<unsigned long long> lean_flag(2 * GL * kLeanFlagStride);
+    DBuf<int> lean_idx(2 * GL);
+    DBuf<cplxf> lean_rows(2 * GL * NB + 2 * NB);
     if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
-        !bpr.p || !bpi.p || !linv.p || !calu_rows.p || !calu_idx.p || !calu_ps.p || !scratch.alloc(sbytes))
+        !bpr.p || !bpi.p || !linv.p || !calu_rows.p || !calu_idx.p || !calu_ps.p || !scratch.alloc(sbytes) ||
+        !lean_flag.p || !lean_idx.p || !lean_rows.p)
         return -1;
+    cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
     cudaEvent_t ev[4];
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], stream());
@@ -3104,8 +3326,23 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             const int kb = std::min(NB, E - k0);
             tm.mark(2);
             CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
+            const int lean_g = lean_panel_ctas(n - k0);
             if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
             } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
+            } else if (lean_g > 0) {
+                Status *stp = st.p;
+                long long *pivp = piv.p;
+                int kbv = kb;
+                unsigned long long *fl = lean_flag.p;
+                int *li = lean_idx.p;
+                cplxf *lr = lean_rows.p, *lk = lean_rows.p + 2 * GL * NB;
+                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, (void *)&limit, &pivp, &stp, &sc.ps, &fl, &li, &lr,
+                                &lk};
+                if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_lean, dim3(lean_g), dim3(kLeanThreads),
+                                                         args, 0, stream()),
+                             "lean panel launch"))
+                    return -1;
+                note_launch();
             } else if (pl.G > 0) {
                 int rows = pl.rows;
                 cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
