@@ -493,7 +493,18 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned l
 // the end), so flags of earlier columns or launches never match.  Every
 // wait is bounded (status 6).
 static const int kLeanThreads = 64;
-static const int kLeanFlagStride = 16;  // u64 words per flag: one 128-byte line each
+static const int kLeanPoll = 8;  // flags per polling lane (two per 16-byte load): at most 256 CTAs
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acquire_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ void ld_relaxed_v2u64(const unsigned long long *p, unsigned long long &a,
+                                                 unsigned long long &b) {
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
 
 __device__ __forceinline__ float lean_mag(cplxf v, bool diag) {
     float m = hypotf(v.re, v.im);
@@ -503,10 +514,10 @@ __device__ __forceinline__ float lean_mag(cplxf v, bool diag) {
 
 __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, int k0, int kb, double limit,
                                                              long long *piv, Status *st, PanelSlots *ps,
-                                                             unsigned long long *flag, int *cand_idx,
-                                                             cplxf *cand_row, cplxf *krow) {
+                                                             unsigned long long *flag, int flag_stride,
+                                                             int *cand_idx, cplxf *cand_row, cplxf *krow) {
     __shared__ cplxf tile[kLeanThreads][kPS];
-    __shared__ cplxf s_prow[NB];
+    __shared__ cplxf s_prow[2][NB];  // pivot rows of the current and the previous column
     __shared__ float s_wv[2], s_fb;
     __shared__ int s_wi[2], s_gc, s_p, s_timeout;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -517,8 +528,8 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
     if (st->code != 0) return;  // uniform across CTAs (set before launch)
     const unsigned gen0 = *(volatile unsigned *)&ps->gen;
     for (int t = tid; t < nrows * kb; t += kLeanThreads) {
-        const int i = t / kb, j = t % kb;
-        tile[i][j] = a[(size_t)(r0 + i) * n + k0 + j];
+        const int ii = t / kb, j = t % kb;
+        tile[ii][j] = a[(size_t)(r0 + ii) * n + k0 + j];
     }
     if (tid == 0) s_timeout = 0;
     __syncthreads();
@@ -526,10 +537,12 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
     const bool mine = tid < nrows;
     cplxf *row = tile[tid];
     float mv = mine ? lean_mag(row[0], i == k0) : -1.0f;
+    cplxf mreg = {0.0f, 0.0f};  // this row's multiplier of the previous column (its update is deferred)
     for (int kk = 0; kk < kb; ++kk) {
         const int k = k0 + kk, par = kk & 1;
         const unsigned epoch = gen0 + (unsigned)kk + 1u;
-        // this CTA's candidate: largest magnitude, lowest row
+        const cplxf *pprev = s_prow[par ^ 1];  // pivot row of column kk - 1
+        // this CTA's candidate (column kk is up to date): largest magnitude, lowest row
         float bv = (mine && i >= k) ? mv : -1.0f;
         int bi = bv >= 0.0f ? i : n;
 #pragma unroll
@@ -553,36 +566,55 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
             bv = s_wv[0];
             bi = s_wi[0];
         }
-        // publish the candidate row and, if owned here, row k; then the flag
+        // publish the candidate row and, if owned here, row k as they are
+        // (columns > kk still lack the previous column's update, which the
+        // readers apply), then the flag with the magnitude
         if (warp == 0 && bi < n && lane < kb) cand_row[((size_t)par * G + c) * NB + lane] = tile[bi - r0][lane];
         if (warp == 1 && k >= r0 && k < r1 && lane < kb) krow[(size_t)par * NB + lane] = tile[k - r0][lane];
         if (tid == 0) cand_idx[par * G + c] = bi;
         __syncthreads();
         if (tid == 0) {
             __threadfence();
-            st_relaxed_u64(flag + (size_t)(par * G + c) * kLeanFlagStride,
+            st_relaxed_u64(flag + (size_t)par * flag_stride + c,
                            ((unsigned long long)epoch << 32) | __float_as_uint(bi < n ? bv : -1.0f));
         }
-        // warp 0 polls the G flags: (largest magnitude, lowest CTA)
+        // the previous column's deferred update of this CTA's rows, while
+        // the flags travel
+        if (kk > 0 && mine && i >= k) {
+#pragma unroll 4
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mreg, pprev[j]);
+        }
+        // warp 0 polls the G flags (dense: a sweep is a few coalesced 16-byte
+        // loads per lane, flags q = 64 u + 2 lane + {0, 1}), then one acquire
+        // fence: (largest magnitude, lowest CTA)
         if (warp == 0) {
             float fb = -2.0f;
             int fq = -1;
-            bool ok = true;
-            for (unsigned q = lane; q < G && ok; q += 32) {
-                unsigned long long v = 0;
-                ok = false;
-                for (long long spin = 0; spin < kSpinLimit; ++spin) {
-                    v = ld_acquire_u64(flag + (size_t)(par * G + q) * kLeanFlagStride);
-                    if ((unsigned)(v >> 32) == epoch) {
-                        ok = true;
-                        break;
-                    }
-                    if ((spin & 1023) == 1023 && *(volatile int *)&ps->timeout) break;
-                }
-                const float f = __uint_as_float((unsigned)v);
-                if (ok && f >= 0.0f && (f > fb || (f == fb && (int)q < fq))) {
+            unsigned long long v[kLeanPoll];
+            unsigned pending = 0;
+#pragma unroll
+            for (int u = 0; u < kLeanPoll; ++u)
+                if (64 * (u >> 1) + 2 * lane + (u & 1) < (int)G) pending |= 1u << u;
+            for (long long spin = 0; pending && spin < kSpinLimit; ++spin) {
+#pragma unroll
+                for (int u = 0; u < kLeanPoll; u += 2)
+                    if (pending & (3u << u))
+                        ld_relaxed_v2u64(flag + (size_t)par * flag_stride + 64 * (u >> 1) + 2 * lane, v[u], v[u + 1]);
+#pragma unroll
+                for (int u = 0; u < kLeanPoll; ++u)
+                    if ((pending & (1u << u)) && (unsigned)(v[u] >> 32) == epoch) pending &= ~(1u << u);
+                if ((spin & 1023) == 1023 && *(volatile int *)&ps->timeout) break;
+            }
+            fence_acquire_gpu();
+            const bool ok = pending == 0;
+#pragma unroll
+            for (int u = 0; u < kLeanPoll; ++u) {
+                const int q = 64 * (u >> 1) + 2 * lane + (u & 1);
+                if (q >= (int)G) continue;
+                const float f = __uint_as_float((unsigned)v[u]);
+                if (ok && f >= 0.0f && (f > fb || (f == fb && q < fq))) {
                     fb = f;
-                    fq = (int)q;
+                    fq = q;
                 }
             }
             if (!ok) atomicExch(&ps->timeout, 1);
@@ -617,36 +649,59 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
             }
             return;
         }
-        // the winner's row segment and index; the owner of p takes row k
+        // the winner's row (with the pending update applied, exactly as its
+        // owner applied it) and index; the owner of p takes row k
+        cplxf *pcur = s_prow[par];
         cplxf kval = {0.0f, 0.0f};
         if (gc == c) {
-            if (warp == 0 && lane < kb) s_prow[lane] = tile[bi - r0][lane];
+            if (warp == 0 && lane < kb) pcur[lane] = tile[bi - r0][lane];
             if (tid == 0) s_p = bi;
-            if (warp == 1 && bi != k && lane < kb) kval = ld_volatile(krow + (size_t)par * NB + lane);
+            if (warp == 1 && bi != k && lane < kb) {
+                if (k >= r0 && k < r1) {
+                    kval = tile[k - r0][lane];  // updated above by its own thread
+                } else {
+                    kval = ld_volatile(krow + (size_t)par * NB + lane);
+                    if (kk > 0 && lane > kk) {
+                        const cplxf km = ld_volatile(krow + (size_t)par * NB + kk - 1);
+                        kval = msub(kval, km, pprev[lane]);
+                    }
+                }
+            }
         } else {
-            if (warp == 0 && lane < kb) s_prow[lane] = ld_volatile(cand_row + ((size_t)par * G + gc) * NB + lane);
+            if (warp == 0 && lane < kb) {
+                cplxf v = ld_volatile(cand_row + ((size_t)par * G + gc) * NB + lane);
+                if (kk > 0 && lane > kk) {
+                    const cplxf cm = ld_volatile(cand_row + ((size_t)par * G + gc) * NB + kk - 1);
+                    v = msub(v, cm, pprev[lane]);
+                }
+                pcur[lane] = v;
+            }
             if (warp == 1 && lane == 0) s_p = ld_volatile(cand_idx + par * G + gc);
         }
         __syncthreads();
         const int p = s_p;
         if (p != k) {
-            if (warp == 0 && k >= r0 && k < r1 && lane < kb) tile[k - r0][lane] = s_prow[lane];
+            if (warp == 0 && k >= r0 && k < r1 && lane < kb) tile[k - r0][lane] = pcur[lane];
             if (warp == 1 && gc == c && lane < kb) tile[p - r0][lane] = kval;
         }
         if (c == 0 && tid == 0) piv[k] = p;
         __syncthreads();
         if (k + 1 >= n) break;
-        // update this thread's row; the next column's magnitude on the way
+        // this row's multiplier and its next column (the rest of the row is
+        // updated in the next step, off the critical path)
         if (mine && i > k) {
-            const cplxf pv = s_prow[kk];
+            const cplxf pv = pcur[kk];
             const float den = pv.re * pv.re + pv.im * pv.im;
             const cplxf inv = {pv.re / den, -pv.im / den};
             const cplxf x = row[kk];
-            const cplxf mlt = {x.re * inv.re - x.im * inv.im, x.re * inv.im + x.im * inv.re};
-            row[kk] = mlt;
-#pragma unroll 8
-            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mlt, s_prow[j]);
-            mv = kk + 1 < kb ? lean_mag(row[kk + 1], i == k + 1) : -1.0f;
+            mreg = cplxf{x.re * inv.re - x.im * inv.im, x.re * inv.im + x.im * inv.re};
+            row[kk] = mreg;
+            if (kk + 1 < kb) {
+                row[kk + 1] = msub(row[kk + 1], mreg, pcur[kk + 1]);
+                mv = lean_mag(row[kk + 1], i == k + 1);
+            } else {
+                mv = -1.0f;
+            }
         } else {
             mv = -1.0f;
         }
@@ -659,6 +714,246 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
     // every CTA read the base epoch before publishing column 0, and CTA 0
     // gets here only after every CTA published the last column
     if (c == 0 && tid == 0) atomicExch(&ps->gen, gen0 + (unsigned)kb);
+}
+
+// ---- cluster FP32 panel (the mixed path) ---------------------------
+// The lean panel's per-column exchange still crosses the GPU: measured on
+// GB300, a release store takes ~2 us to reach pollers on other SMs, while a
+// thread-block cluster barrier takes 0.2 us and a distributed-shared-memory
+// load 0.1 us.  Here the whole panel lives in one cluster of C (16) CTAs,
+// one row per thread (up to 1024 rows per CTA), candidates in each CTA's
+// shared memory: per column a CTA argmax, one split cluster barrier (the
+// previous column's deferred update runs between arrive and wait), the
+// winner read from its CTA's shared memory, the swap, and the multiplier
+// plus next column of every row.  Published rows are copied before the
+// deferred update; readers apply it (the row's multiplier in column kk-1
+// times the previous pivot row), exactly as the owner does.  The pivot rule
+// is the lean panel's (first maximum of |z| in FP32, lowest row on ties).
+struct ClSlot {
+    cplxf row[2][NB];   // candidate row, by column parity
+    cplxf krow[2][NB];  // row k when owned here
+    float val[2];
+    int idx[2];
+};
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+__global__ void __launch_bounds__(1024) k_panel_cl(cplxf *a, int n, int k0, int kb, int rows_per_cta, double limit,
+                                                   long long *piv, Status *st) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char cl_smem[];
+    cplxf(*tile)[kPS] = reinterpret_cast<cplxf(*)[kPS]>(cl_smem);  // [rows_per_cta][kPS]
+    __shared__ ClSlot slot;
+    __shared__ cplxf s_prow[2][NB];
+    __shared__ float s_wv[32], s_gb;
+    __shared__ int s_wi[32], s_gc, s_p;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int C = (int)cluster.num_blocks(), c = (int)cluster.block_rank();
+    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform over the cluster (set before launch)
+    for (int t = tid; t < nrows * kb; t += blockDim.x) {
+        const int ii = t / kb, j = t % kb;
+        tile[ii][j] = a[(size_t)(r0 + ii) * n + k0 + j];
+    }
+    __syncthreads();
+    const int i = r0 + tid;
+    const bool mine = tid < nrows;
+    cplxf *row = tile[mine ? tid : 0];
+    float mv = mine ? lean_mag(row[0], i == k0) : -1.0f;
+    cplxf mreg = {0.0f, 0.0f};
+    bool failed = false;
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk, par = kk & 1;
+        const cplxf *pprev = s_prow[par ^ 1];
+        // CTA candidate (largest magnitude, lowest row)
+        float bv = (mine && i >= k) ? mv : -1.0f;
+        int bi = bv >= 0.0f ? i : n;
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, sh);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_wv[warp] = bv;
+            s_wi[warp] = bi;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            bv = lane < nwarps ? s_wv[lane] : -1.0f;
+            bi = lane < nwarps ? s_wi[lane] : n;
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const float ov = __shfl_xor_sync(0xffffffffu, bv, sh);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            // publish: the candidate as it is (pending the previous column's update)
+            if (lane < kb) slot.row[par][lane] = bi < n ? tile[bi - r0][lane] : cplxf{0.0f, 0.0f};
+            if (lane == 0) {
+                slot.val[par] = bi < n ? bv : -1.0f;
+                slot.idx[par] = bi;
+            }
+        }
+        if (warp == 1 && k >= r0 && k < r1 && lane < kb) slot.krow[par][lane] = tile[k - r0][lane];
+        __syncthreads();
+        cluster_arrive();
+        // the previous column's deferred update, between arrive and wait
+        if (kk > 0 && mine && i >= k) {
+#pragma unroll 4
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mreg, pprev[j]);
+        }
+        __syncwarp();
+        cluster_wait();
+
+        // the winner over the cluster
+        if (warp == 0) {
+            float fv = -1.0f;
+            int fi = n, fq = -1;
+            if (lane < C) {
+                const ClSlot *rs = cluster.map_shared_rank(&slot, lane);
+                fv = rs->val[par];
+                fi = rs->idx[par];
+                fq = fi < n ? lane : -1;
+                if (fq < 0) fv = -1.0f;
+            }
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const float ov = __shfl_xor_sync(0xffffffffu, fv, sh);
+                const int oi = __shfl_xor_sync(0xffffffffu, fi, sh);
+                const int oq = __shfl_xor_sync(0xffffffffu, fq, sh);
+                if (oq >= 0 && (fq < 0 || ov > fv || (ov == fv && oi < fi))) {
+                    fv = ov;
+                    fi = oi;
+                    fq = oq;
+                }
+            }
+            if (lane == 0) {
+                s_gc = fq;
+                s_gb = fv;
+                s_p = fi;
+            }
+        }
+        __syncthreads();
+        const int gc = s_gc, p = s_p;
+        const float gb = s_gb;
+        if (gc < 0 || !isfinite(gb) || (double)gb <= limit) {
+            if (c == 0 && tid == 0) {
+                st->code = 2;
+                st->column = k;
+                st->value = gc < 0 ? -1.0 : (double)gb;
+            }
+            failed = true;
+            break;  // uniform over the cluster: every CTA read the same slots
+        }
+        // the pivot row, and row k for the owner of p, with the pending update
+        cplxf *pcur = s_prow[par];
+        cplxf kval = {0.0f, 0.0f};
+        if (warp == 0 && lane < kb) {
+            const ClSlot *ws = cluster.map_shared_rank(&slot, gc);
+            cplxf v = ws->row[par][lane];
+            if (kk > 0 && lane > kk) v = msub(v, ws->row[par][kk - 1], pprev[lane]);
+            pcur[lane] = v;
+        }
+        if (warp == 1 && gc == c && p != k && lane < kb) {
+            const ClSlot *ks = cluster.map_shared_rank(&slot, (k - k0) / rows_per_cta);
+            kval = ks->krow[par][lane];
+            if (kk > 0 && lane > kk) kval = msub(kval, ks->krow[par][kk - 1], pprev[lane]);
+        }
+        __syncthreads();
+        if (p != k) {
+            if (warp == 0 && k >= r0 && k < r1 && lane < kb) tile[k - r0][lane] = pcur[lane];
+            if (warp == 1 && gc == c && lane < kb) tile[p - r0][lane] = kval;
+        }
+        if (c == 0 && tid == 0) piv[k] = p;
+        __syncthreads();
+        if (k + 1 >= n) break;
+        if (mine && i > k) {
+            const cplxf pv = pcur[kk];
+            const float den = pv.re * pv.re + pv.im * pv.im;
+            const cplxf inv = {pv.re / den, -pv.im / den};
+            const cplxf x = row[kk];
+            mreg = cplxf{x.re * inv.re - x.im * inv.im, x.re * inv.im + x.im * inv.re};
+            row[kk] = mreg;
+            if (kk + 1 < kb) {
+                row[kk + 1] = msub(row[kk + 1], mreg, pcur[kk + 1]);
+                mv = lean_mag(row[kk + 1], i == k + 1);
+            } else {
+                mv = -1.0f;
+            }
+        } else {
+            mv = -1.0f;
+        }
+    }
+    if (!failed) {
+        __syncthreads();
+        for (int t = tid; t < nrows * kb; t += blockDim.x) {
+            const int ii = t / kb, j = t % kb;
+            a[(size_t)(r0 + ii) * n + k0 + j] = tile[ii][j];
+        }
+    }
+    // no CTA leaves while another may still read its shared memory
+    __syncthreads();
+    cluster_arrive();
+    cluster_wait();
+}
+
+
+// Cluster FP32 panel for m rows: C = 16 CTAs (8 where 16 is not
+// available), one row per thread; false when it does not apply.
+static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long long *piv, Status *st) {
+    const int m = n - k0;
+    if (m < 2 * 64) return false;
+    static const size_t kMaxSmem = 200 * 1024;
+    static const int max_c = [] {
+        cudaFuncSetAttribute(k_panel_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+        cudaFuncSetAttribute(k_panel_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = kMaxSmem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int c = 0;
+        if (cudaOccupancyMaxPotentialClusterSize(&c, k_panel_cl, &cfg) != cudaSuccess) c = 0;
+        cudaGetLastError();
+        return c >= 16 ? 16 : c >= 8 ? 8 : 0;
+    }();
+    if (max_c == 0) return false;
+    const int C = max_c;
+    const int rows = (m + C - 1) / C;
+    if (rows > 1024) return false;
+    const size_t smem = (size_t)rows * kPS * sizeof(cplxf);
+    if (smem > kMaxSmem) return false;
+    const int threads = std::max(64, (rows + 31) / 32 * 32);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream();
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    note_launch();
+    return cuda_ok(cudaLaunchKernelEx(&cfg, k_panel_cl, a, n, k0, kb, rows, limit, piv, st), "cluster FP32 panel launch");
 }
 
 // ---- cluster panel ----------------------------------------------------
@@ -2009,8 +2304,19 @@ static bool cluster_panel_enabled() {
     return on;
 }
 
-// CTAs of the lean FP32 panel for m rows (0: use another form).  Off with
-// PEEC_GB300_MIXED_PANEL=coop; the grid must be co-resident.
+// FP32 panel of the mixed path: the cluster panel (k_panel_cl) where the
+// panel fits one cluster's shared memory, else the lean grid panel, else the
+// cooperative one.  PEEC_GB300_MIXED_PANEL=lean / coop / calu selects a form.
+static bool cl_panel_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PEEC_GB300_MIXED_PANEL");
+        return !(e && (strcmp(e, "lean") == 0 || strcmp(e, "coop") == 0 || strcmp(e, "calu") == 0));
+    }();
+    return on;
+}
+
+// CTAs of the lean FP32 panel for m rows (0: use another form); the grid
+// must be co-resident.
 static int lean_panel_ctas(int m) {
     static const int cap = [] {
         const char *e = getenv("PEEC_GB300_MIXED_PANEL");
@@ -2025,7 +2331,7 @@ static int lean_panel_ctas(int m) {
     }();
     if (m < 2 * kLeanThreads) return 0;  // small panels: one CTA
     const int g = (m + kLeanThreads - 1) / kLeanThreads;
-    return g <= cap ? g : 0;
+    return g <= cap && g <= 32 * kLeanPoll ? g : 0;
 }
 
 // FP32 panels of the mixed path by tournament pivoting when
@@ -3235,7 +3541,8 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     size_t sbytes = 256 + 2 * G * 8 + 2 * G * 4 + 16 + 2 * G * NB * sizeof(cplxf) + 2 * NB * sizeof(cplxf) + 64;
     // lean panel slots: G_lean = ceil(n / 64) CTAs at most
     const size_t GL = (size_t)(n + kLeanThreads - 1) / kLeanThreads;
-    DBuf<unsigned long long> lean_flag(2 * GL * kLeanFlagStride);
+    const int lean_stride = (int)((GL + 63) / 64 * 64);  // flags of one parity, a multiple of 64 (16-byte loads)
+    DBuf<unsigned long long> lean_flag(2 * (size_t)lean_stride);
     DBuf<int> lean_idx(2 * GL);
     DBuf<cplxf> lean_rows(2 * GL * NB + 2 * NB);
     if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
@@ -3329,6 +3636,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             const int lean_g = lean_panel_ctas(n - k0);
             if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
             } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
+            } else if (cl_panel_enabled() && launch_cl_panel(a, n, k0, kb, limit, piv.p, st.p)) {
             } else if (lean_g > 0) {
                 Status *stp = st.p;
                 long long *pivp = piv.p;
@@ -3336,8 +3644,9 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
                 unsigned long long *fl = lean_flag.p;
                 int *li = lean_idx.p;
                 cplxf *lr = lean_rows.p, *lk = lean_rows.p + 2 * GL * NB;
-                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, (void *)&limit, &pivp, &stp, &sc.ps, &fl, &li, &lr,
-                                &lk};
+                int fls = lean_stride;
+                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, (void *)&limit, &pivp, &stp, &sc.ps, &fl, &fls, &li,
+                                &lr, &lk};
                 if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_lean, dim3(lean_g), dim3(kLeanThreads),
                                                          args, 0, stream()),
                              "lean panel launch"))
