@@ -1404,19 +1404,70 @@ __global__ void __launch_bounds__(256) k_panel_calu(cplxf *a, int n, int k0, int
 }
 
 // ---- row swaps outside the panel -------------------------------------
+static const int kLaswpCols = 32;  // columns per k_laswp block (shared memory 2 NB x 32 x 16 bytes at most)
+
 template <class T>
-__global__ void k_laswp(T *a, int n, int k0, int kb, const long long *piv, const Status *st) {
+__global__ void __launch_bounds__(256) k_laswp(T *a, int n, int k0, int kb, const long long *piv, const Status *st) {
+    // The kb interchanges (k, piv[k]) applied in order move at most 2 kb
+    // rows.  Warp 0 composes them into (destination, source) pairs; then the
+    // block stages its kLaswpCols columns of the source rows in shared memory
+    // (independent, coalesced loads) and writes them to the destinations.
+    // Same result as the sequential interchanges, one memory round trip.
+    extern __shared__ __align__(16) unsigned char laswp_smem[];
+    T *buf = reinterpret_cast<T *>(laswp_smem);  // [2 NB][kLaswpCols]
+    __shared__ int s_pos[2 * NB], s_src[2 * NB], s_cnt;
     if (st->code != 0) return;
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n || (j >= k0 && j < k0 + kb)) return;
-    for (int kk = 0; kk < kb; ++kk) {
-        int k = k0 + kk;
-        int p = (int)piv[k];
-        if (p != k) {
-            T t = a[(size_t)k * n + j];
-            a[(size_t)k * n + j] = a[(size_t)p * n + j];
-            a[(size_t)p * n + j] = t;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < 32) {
+        // positions k0 .. k0+kb-1 first, others appended as they appear
+        for (int t = lane; t < kb; t += 32) {
+            s_pos[t] = k0 + t;
+            s_src[t] = k0 + t;
         }
+        int cnt = kb;
+        __syncwarp();
+        for (int kk = 0; kk < kb; ++kk) {
+            const int k = k0 + kk, p = (int)piv[k];
+            if (p == k) continue;
+            int ip;
+            if (p < k0 + kb) {
+                ip = p - k0;
+            } else {
+                int f = -1;
+                for (int t = lane; t < cnt; t += 32)
+                    if (s_pos[t] == p) f = t;
+                const unsigned hit = __ballot_sync(0xffffffffu, f >= 0);
+                if (hit) {
+                    ip = __shfl_sync(0xffffffffu, f, __ffs(hit) - 1);
+                } else {
+                    ip = cnt;
+                    if (lane == 0) {
+                        s_pos[cnt] = p;
+                        s_src[cnt] = p;
+                    }
+                    ++cnt;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const int t = s_src[kk];
+                s_src[kk] = s_src[ip];
+                s_src[ip] = t;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) s_cnt = cnt;
+    }
+    __syncthreads();
+    const int cnt = s_cnt, j0 = blockIdx.x * kLaswpCols;
+    for (int e = tid; e < cnt * kLaswpCols; e += blockDim.x) {
+        const int r = e / kLaswpCols, jj = e % kLaswpCols, j = j0 + jj;
+        if (j < n && !(j >= k0 && j < k0 + kb)) buf[r * kLaswpCols + jj] = a[(size_t)s_src[r] * n + j];
+    }
+    __syncthreads();
+    for (int e = tid; e < cnt * kLaswpCols; e += blockDim.x) {
+        const int r = e / kLaswpCols, jj = e % kLaswpCols, j = j0 + jj;
+        if (j < n && !(j >= k0 && j < k0 + kb)) a[(size_t)s_pos[r] * n + j] = buf[r * kLaswpCols + jj];
     }
 }
 
@@ -1432,18 +1483,25 @@ __global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, int c
     __syncthreads();
     int j = c0 + blockIdx.x * blockDim.x + threadIdx.x;  // columns c0 .. c1-1 (all right of the panel)
     if (j >= c1) return;
+    // all loads first (independent), the substitution in registers, then the
+    // stores: the loads no longer wait behind the previous rows' stores
     T x[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+        if (i < kb) x[i] = a[(size_t)(k0 + i) * n + j];
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
         if (i < kb) {
-            T v = a[(size_t)(k0 + i) * n + j];
+            T v = x[i];
 #pragma unroll
             for (int m = 0; m < NB; ++m)
                 if (m < i) v = msub(v, L[i][m], x[m]);
             x[i] = v;
-            a[(size_t)(k0 + i) * n + j] = v;
         }
     }
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+        if (i < kb) a[(size_t)(k0 + i) * n + j] = x[i];
 }
 
 // ---- A22 -= L21 U12 --------------------------------------------------
@@ -2447,7 +2505,8 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
             PEEC_LAUNCH(k_panel<T>, 1, 1024, 0, d_a, n, k0, kb, limit, d_piv, d_st);
         }
         tm.mark(0);
-        PEEC_LAUNCH(k_laswp<T>, (n + 255) / 256, 256, 0, d_a, n, k0, kb, d_piv, d_st);
+        PEEC_LAUNCH(k_laswp<T>, (n + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(T), d_a, n, k0, kb,
+                    d_piv, d_st);
         int rest = n - (k0 + kb);
         if (rest > 0) {
             PEEC_LAUNCH(k_trsm<T>, (rest + 255) / 256, 256, 0, d_a, n, k0, kb, k0 + kb, n, d_st);
@@ -3052,7 +3111,8 @@ extern "C" int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double
         } else {
             PEEC_LAUNCH(k_panel<double>, 1, 1024, 0, d_a, ni, k0, kb, limit, d_piv, st);
         }
-        PEEC_LAUNCH(k_laswp<double>, (ni + 255) / 256, 256, 0, d_a, ni, k0, kb, d_piv, st);
+        PEEC_LAUNCH(k_laswp<double>, (ni + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(double), d_a,
+                    ni, k0, kb, d_piv, st);
         int rest = ni - (k0 + kb);
         if (rest > 0) {
             PEEC_LAUNCH(k_trsm<double>, (rest + 255) / 256, 256, 0, d_a, ni, k0, kb, k0 + kb, ni, st);
@@ -3669,7 +3729,8 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
                 PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
             }
             tm.mark(0);
-            PEEC_LAUNCH(k_laswp<cplxf>, (n + 255) / 256, 256, 0, a, n, k0, kb, piv.p, st.p);
+            PEEC_LAUNCH(k_laswp<cplxf>, (n + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(cplxf), a,
+                        n, k0, kb, piv.p, st.p);
             // the rest of the outer block's columns: U12 rows, then the narrow update
             const int rin = E - (k0 + kb);
             if (rin > 0) PEEC_LAUNCH(k_trsm<cplxf>, (rin + 255) / 256, 256, 0, a, n, k0, kb, k0 + kb, E, st.p);
