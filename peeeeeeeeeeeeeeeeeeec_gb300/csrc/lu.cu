@@ -739,14 +739,17 @@ struct ClSlot {
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-__global__ void __launch_bounds__(1024) k_panel_cl(cplxf *a, int n, int k0, int kb, int rows_per_cta, double limit,
-                                                   long long *piv, Status *st) {
+static const int kClMaxThreads = 640;  // rows per CTA at most (registers: 102 a thread)
+static const int kClStride = NB + 2;   // tile row stride (complex): 16-byte aligned rows
+
+__global__ void __launch_bounds__(kClMaxThreads) k_panel_cl(cplxf *a, int n, int k0, int kb, int rows_per_cta,
+                                                            double limit, long long *piv, Status *st) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char cl_smem[];
-    cplxf(*tile)[kPS] = reinterpret_cast<cplxf(*)[kPS]>(cl_smem);  // [rows_per_cta][kPS]
+    cplxf(*tile)[kClStride] = reinterpret_cast<cplxf(*)[kClStride]>(cl_smem);  // [rows_per_cta][kClStride]
     __shared__ ClSlot slot;
-    __shared__ cplxf s_prow[2][NB];
+    __shared__ __align__(16) cplxf s_prow[2][NB];
     __shared__ float s_wv[32], s_gb;
     __shared__ int s_wi[32], s_gc, s_p;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -807,10 +810,31 @@ __global__ void __launch_bounds__(1024) k_panel_cl(cplxf *a, int n, int k0, int 
         if (warp == 1 && k >= r0 && k < r1 && lane < kb) slot.krow[par][lane] = tile[k - r0][lane];
         __syncthreads();
         cluster_arrive();
-        // the previous column's deferred update, between arrive and wait
+        // the previous column's deferred update, between arrive and wait: the
+        // row in registers (16-byte shared-memory accesses, compile-time
+        // column indices), columns kk+1 .. kb-1 only
         if (kk > 0 && mine && i >= k) {
-#pragma unroll 4
-            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mreg, pprev[j]);
+            float4 *r4 = reinterpret_cast<float4 *>(row);
+            const float4 *p4 = reinterpret_cast<const float4 *>(pprev);
+#pragma unroll
+            for (int q = 0; q < NB / 2; ++q) {
+                if (2 * q + 1 <= kk || 2 * q >= kb) continue;
+                float4 r = r4[q];
+                const float4 u = p4[q];
+                if (2 * q > kk) {
+                    r.x = fmaf(-mreg.re, u.x, r.x);
+                    r.x = fmaf(mreg.im, u.y, r.x);
+                    r.y = fmaf(-mreg.re, u.y, r.y);
+                    r.y = fmaf(-mreg.im, u.x, r.y);
+                }
+                if (2 * q + 1 < kb) {
+                    r.z = fmaf(-mreg.re, u.z, r.z);
+                    r.z = fmaf(mreg.im, u.w, r.z);
+                    r.w = fmaf(-mreg.re, u.w, r.w);
+                    r.w = fmaf(-mreg.im, u.z, r.w);
+                }
+                r4[q] = r;
+            }
         }
         __syncwarp();
         cluster_wait();
@@ -919,7 +943,7 @@ static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long 
         cudaFuncSetAttribute(k_panel_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(16);
-        cfg.blockDim = dim3(1024);
+        cfg.blockDim = dim3(kClMaxThreads);
         cfg.dynamicSmemBytes = kMaxSmem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -936,8 +960,8 @@ static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long 
     if (max_c == 0) return false;
     const int C = max_c;
     const int rows = (m + C - 1) / C;
-    if (rows > 1024) return false;
-    const size_t smem = (size_t)rows * kPS * sizeof(cplxf);
+    if (rows > kClMaxThreads) return false;
+    const size_t smem = (size_t)rows * kClStride * sizeof(cplxf);
     if (smem > kMaxSmem) return false;
     const int threads = std::max(64, (rows + 31) / 32 * 32);
     cudaLaunchConfig_t cfg = {};
