@@ -77,6 +77,7 @@ struct RegionsDev {
     double *scale = nullptr;   // [n]     width w (inductance) or area S (potential); <= 0 marks a bad region
     int *same_obj = nullptr;   // [np]    object id for the reference's pointer test
     float4 *boxf = nullptr;    // [np*2]  box rounded to FP32: (lo, size), (hi, 0) -- the scan's far filter
+    int *axis = nullptr;       // [n]     0/1/2 when dir is exactly +-e_axis, else -1 (inductance)
     double cmax = 0.0;         // largest |corner coordinate| (scale of the rounding noise)
 };
 
@@ -156,22 +157,27 @@ __device__ __forceinline__ bool region_pair_skipped(const ScanArgs &s, int a, in
         if (!(a == lo && b == hi)) return true;
     }
     if (s.kind == KIND_INDUCTANCE) {
+        // axis-aligned directions: the FP64 dot product is exactly 0 or +-1
+        const int xa = s.R.axis[a], xb = s.R.axis[b];
+        if (xa >= 0 && xb >= 0) return (xa != xb ? 0.0 : 1.0) < s.dir_tol;
         double d = dot3(s.R.dir + 3 * a, s.R.dir + 3 * b);
         if (fabs(d) < s.dir_tol) return true;  // entry is exactly 0, no integral
     }
     return false;
 }
 
-// pass 0 counts, pass 1 writes (count[i] -> offsets in off[i])
+// pass 0 counts, pass 1 writes (count[i] -> offsets in off[i]).  One warp
+// per patch i, the lanes over consecutive partners j: the partners found in
+// a chunk of 32 are ranked by ballot, so the list keeps the j order.
 __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, NearRec *out,
                             unsigned long long *far_pairs) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int i = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
     const RegionsDev &R = s.R;
     if (i >= R.np) return;
-    int a = R.owner[i];
+    const int a = R.owner[i];
     const double *ci = R.corner + 12 * (size_t)i, *bi = R.box + 6 * (size_t)i;
-    double hi = R.size[i];
-    int w = pass ? off[i] : 0, found = 0;
+    const double hi = R.size[i];
     // FP32 filter: a pair whose FP32 gap exceeds the FP32 threshold by more
     // than the rounding of both (boxes rounded to FP32 move by <= 2^-24 cmax
     // per coordinate; the margins below are 4x the worst case) is FAR in the
@@ -180,45 +186,53 @@ __global__ void k_near_scan(ScanArgs s, int pass, int *count, const int *off, Ne
     const float nf = (float)s.near_factor;
     const float slack = (float)(9.5367431640625e-07 * R.cmax);  // 2^-20 cmax
     const int same_i = R.same_obj[i];
+    const int w = pass ? off[i] : 0;
+    int found = 0;
     unsigned long long nfar = 0;
     int b_prev = -1;
     bool skip_b = false;
-    for (int j = R.off[a]; j < R.np; ++j) {
-        int b = R.owner[j];
-        if (b == a && j < i) continue;
-        if (b != b_prev) {
-            skip_b = region_pair_skipped(s, a, b);
-            b_prev = b;
-        }
-        if (skip_b) {
-            j = R.off[b + 1] - 1;  // jump to the next region
-            continue;
-        }
-        const bool same = same_i == R.same_obj[j];
-        if (!same) {
-            const float4 lb = R.boxf[2 * j], hb4 = R.boxf[2 * j + 1];
-            float gx = fmaxf(0.0f, fmaxf(la.x - hb4.x, lb.x - ha4.x));
-            float gy = fmaxf(0.0f, fmaxf(la.y - hb4.y, lb.y - ha4.y));
-            float gz = fmaxf(0.0f, fmaxf(la.z - hb4.z, lb.z - ha4.z));
-            float gap = sqrtf(gx * gx + gy * gy + gz * gz);
-            float h = fmaxf(la.w, lb.w);
-            if (gap * (1.0f - 9.5367431640625e-07f) - slack > nf * h * (1.0f + 9.5367431640625e-07f)) {
-                ++nfar;
-                continue;
+    for (int jb = R.off[a]; jb < R.np; jb += 32) {
+        const int j = jb + lane;
+        bool near = false;
+        int cls = CLS_FAR;
+        if (j < R.np) {
+            const int b = R.owner[j];
+            if (b != b_prev) {
+                skip_b = region_pair_skipped(s, a, b);
+                b_prev = b;
+            }
+            if (!skip_b && !(b == a && j < i)) {
+                const bool same = same_i == R.same_obj[j];
+                bool far = false;
+                if (!same) {
+                    const float4 lb = R.boxf[2 * j], hb4 = R.boxf[2 * j + 1];
+                    float gx = fmaxf(0.0f, fmaxf(la.x - hb4.x, lb.x - ha4.x));
+                    float gy = fmaxf(0.0f, fmaxf(la.y - hb4.y, lb.y - ha4.y));
+                    float gz = fmaxf(0.0f, fmaxf(la.z - hb4.z, lb.z - ha4.z));
+                    float gap = sqrtf(gx * gx + gy * gy + gz * gz);
+                    float h = fmaxf(la.w, lb.w);
+                    far = gap * (1.0f - 9.5367431640625e-07f) - slack > nf * h * (1.0f + 9.5367431640625e-07f);
+                }
+                if (!far)
+                    cls = classify_pair(ci, bi, hi, R.corner + 12 * (size_t)j, R.box + 6 * (size_t)j, R.size[j],
+                                        s.near_factor, same);
+                if (cls == CLS_FAR)
+                    ++nfar;
+                else
+                    near = true;
             }
         }
-        int cls = classify_pair(ci, bi, hi, R.corner + 12 * (size_t)j, R.box + 6 * (size_t)j, R.size[j],
-                                s.near_factor, same);
-        if (cls == CLS_FAR) {
-            ++nfar;
-            continue;
-        }
-        if (pass) out[w + found] = NearRec{i, j, cls, 0};
-        ++found;
+        const unsigned bal = __ballot_sync(0xffffffffu, near);
+        if (pass && near) out[w + found + __popc(bal & ((1u << lane) - 1u))] = NearRec{i, j, cls, 0};
+        found += __popc(bal);
     }
     if (!pass) {
-        count[i] = found;
-        if (far_pairs && nfar) atomicAdd(far_pairs, nfar);
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) nfar += __shfl_xor_sync(0xffffffffu, nfar, sh);
+        if (lane == 0) {
+            count[i] = found;
+            if (far_pairs && nfar) atomicAdd(far_pairs, nfar);
+        }
     }
 }
 
@@ -1592,17 +1606,34 @@ struct DeviceRegions {
     DBuf<int> off, owner, same_obj;
     DBuf<double> corner, box, size, dir, scale;
     DBuf<float4> boxf;
+    DBuf<int> axis;
     RegionsDev view;
     bool upload(const HostRegions &H) {
         int np = H.off[H.n];
         if (!off.alloc(H.n + 1) || !owner.alloc(np) || !same_obj.alloc(np) || !corner.alloc(12 * (size_t)np) ||
             !box.alloc(6 * (size_t)np) || !size.alloc(np) || !scale.alloc(H.n) || !boxf.alloc(2 * (size_t)np) ||
+            !axis.alloc(H.n) ||
             !dir.alloc(H.dir.empty() ? 0 : H.dir.size()))
             return false;
         bool ok = off.upload(H.off.data(), H.off.size()) && scale.upload(H.scale.data(), H.scale.size());
         if (np) ok = ok && owner.upload(H.owner.data(), np) && same_obj.upload(H.same_obj.data(), np) &&
                      corner.upload(H.corner.data(), H.corner.size());
         if (!H.dir.empty()) ok = ok && dir.upload(H.dir.data(), H.dir.size());
+        {
+            // exact axis directions (one nonzero component of magnitude 1)
+            std::vector<int> ax(H.n, -1);
+            for (int r = 0; r < H.n && !H.dir.empty(); ++r) {
+                const double *d = H.dir.data() + 3 * (size_t)r;
+                int nz = 0, k = -1;
+                for (int q = 0; q < 3; ++q)
+                    if (d[q] != 0.0) {
+                        ++nz;
+                        k = q;
+                    }
+                if (nz == 1 && fabs(d[k]) == 1.0) ax[r] = k;
+            }
+            ok = ok && axis.upload(ax.data(), ax.size());
+        }
         view.n = H.n;
         view.np = np;
         view.off = off.p;
@@ -1612,6 +1643,7 @@ struct DeviceRegions {
         view.box = box.p;
         view.size = size.p;
         view.boxf = boxf.p;
+        view.axis = axis.p;
         view.dir = dir.p;
         view.scale = scale.p;
         view.cmax = 0.0;
@@ -1687,7 +1719,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
         long long tot = (long long)np * npts;
         PEEC_LAUNCH(k_far_points, (unsigned)((tot + 255) / 256), 256, 0, R, q, gl_row(q), pts.p, ptf.p);
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
-        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 0, count.p, nullptr, nullptr, farcount.p);
+        PEEC_LAUNCH(k_near_scan, (unsigned)(((long long)np * 32 + 255) / 256), 256, 0, s, 0, count.p, nullptr, nullptr,
+                    farcount.p);
         PEEC_LAUNCH(k_exclusive_scan, 1, 1024, 0, count.p, near_off.p, np);
     } else {
         cudaMemsetAsync(near_off.p, 0, sizeof(int), stream());
@@ -1711,7 +1744,8 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     const int *job_rec = nullptr;
     if (nrec) {
         ScanArgs s{R, kind, o.near_factor, o.dir_tol, only_a, only_b};
-        PEEC_LAUNCH(k_near_scan, (np + 127) / 128, 128, 0, s, 1, nullptr, near_off.p, rec.p, nullptr);
+        PEEC_LAUNCH(k_near_scan, (unsigned)(((long long)np * 32 + 255) / 256), 256, 0, s, 1, nullptr, near_off.p,
+                    rec.p, nullptr);
         if (near_reuse_enabled() && nrec > 1) {
             unsigned long long cap = 1;
             while (cap < 4ull * (unsigned long long)nrec) cap <<= 1;

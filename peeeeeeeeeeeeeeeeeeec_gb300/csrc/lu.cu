@@ -506,6 +506,14 @@ __device__ __forceinline__ void ld_relaxed_v2u64(const unsigned long long *p, un
     asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
 }
 
+// The largest FP32 value f with f <= x: for an FP32 g, g <= f exactly when
+// (double)g <= x, so the per-column pivot test needs no FP64 instruction.
+__device__ __forceinline__ float float_at_most(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = nextafterf(f, -INFINITY);
+    return f;
+}
+
 __device__ __forceinline__ float lean_mag(cplxf v, bool diag) {
     float m = hypotf(v.re, v.im);
     if (isnan(m)) m = diag ? INFINITY : -1.0f;  // NaN below the diagonal never wins; on it, +inf is rejected
@@ -526,6 +534,7 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
     const int r0 = k0 + c * kLeanThreads, r1 = min(n, r0 + kLeanThreads);
     const int nrows = r1 > r0 ? r1 - r0 : 0;
     if (st->code != 0) return;  // uniform across CTAs (set before launch)
+    const float limf = float_at_most(limit);
     const unsigned gen0 = *(volatile unsigned *)&ps->gen;
     for (int t = tid; t < nrows * kb; t += kLeanThreads) {
         const int ii = t / kb, j = t % kb;
@@ -641,7 +650,7 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
         }
         const int gc = s_gc;
         const float gb = s_fb;
-        if (gc < 0 || !isfinite(gb) || (double)gb <= limit) {
+        if (gc < 0 || !isfinite(gb) || gb <= limf) {
             if (c == 0 && tid == 0) {
                 st->code = 2;
                 st->column = k;
@@ -757,6 +766,7 @@ __global__ void __launch_bounds__(kClMaxThreads) k_panel_cl(cplxf *a, int n, int
     const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
     const int nrows = r1 > r0 ? r1 - r0 : 0;
     if (st->code != 0) return;  // uniform over the cluster (set before launch)
+    const float limf = float_at_most(limit);
     for (int t = tid; t < nrows * kb; t += blockDim.x) {
         const int ii = t / kb, j = t % kb;
         tile[ii][j] = a[(size_t)(r0 + ii) * n + k0 + j];
@@ -870,7 +880,7 @@ __global__ void __launch_bounds__(kClMaxThreads) k_panel_cl(cplxf *a, int n, int
         __syncthreads();
         const int gc = s_gc, p = s_p;
         const float gb = s_gb;
-        if (gc < 0 || !isfinite(gb) || (double)gb <= limit) {
+        if (gc < 0 || !isfinite(gb) || gb <= limf) {
             if (c == 0 && tid == 0) {
                 st->code = 2;
                 st->column = k;
