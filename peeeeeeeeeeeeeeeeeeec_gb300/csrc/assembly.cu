@@ -1376,6 +1376,15 @@ __device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *
     }
 }
 
+__device__ __forceinline__ f2 warp_sum_df2(f2 v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+        f2 o = {__shfl_xor_sync(0xffffffffu, v.h, m), __shfl_xor_sync(0xffffffffu, v.l, m)};
+        v = df_add(v, o);
+    }
+    return v;
+}
+
 __device__ __forceinline__ double warp_sum_df(f2 v) {
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) {
@@ -1455,7 +1464,13 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
             double dot = 0.0, sa = R.scale[a], sb = R.scale[b];
             bool skip = false;
             if (T.kind == KIND_INDUCTANCE) {
-                dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
+                const int xa = R.axis[a], xb = R.axis[b];
+                if (xa >= 0 && xb >= 0) {
+                    // axis directions: the dot product is exactly 0 or +-1
+                    dot = xa != xb ? 0.0 : R.dir[3 * a + xa] * R.dir[3 * b + xb];
+                } else {
+                    dot = dot3(R.dir + 3 * a, R.dir + 3 * b);
+                }
                 skip = fabs(dot) < T.dir_tol;
             }
             bool bad = false;
@@ -1510,17 +1525,22 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                 }
                 if (T.far_df == 1 || T.far_df == 2) {
                     fbad = __any_sync(0xffffffffu, fbad);
-                    double far = warp_sum_df(facc);
-                    if (fbad || !isfinite(far)) bad = true;
-                    integral += far;
+                    const f2 far2 = warp_sum_df2(facc);
+                    if (lane == 0) {  // the entry's FP64 epilogue on one lane
+                        const double far = (double)far2.h + (double)far2.l;
+                        if (fbad || !isfinite(far)) bad = true;
+                        integral += far;
+                    }
                 }
-                if (T.kind == KIND_INDUCTANCE)
-                    val = kMu0Over4Pi * dot * integral / (sa * sb);
-                else if (T.kind == KIND_POTENTIAL)
-                    val = kInv4PiEps0 * integral / (sa * sb);
-                else
-                    val = integral;
-                if (!isfinite(val)) bad = true;
+                if (lane == 0) {
+                    if (T.kind == KIND_INDUCTANCE)
+                        val = kMu0Over4Pi * dot * integral / (sa * sb);
+                    else if (T.kind == KIND_POTENTIAL)
+                        val = kInv4PiEps0 * integral / (sa * sb);
+                    else
+                        val = integral;
+                    if (!isfinite(val)) bad = true;
+                }
             }
             if (bad) {
                 if (lane == 0) atomicMin(T.err, (unsigned long long)a * (unsigned long long)n + b);
