@@ -326,6 +326,44 @@ def transient_leg(lib, ds, n_steps):
     return out
 
 
+def rcs_leg(lib, ds, x_mixed):
+    """RCS of the solved box (rcs.c:701-1140, dual-patch quadrature, order 6):
+    the monostatic direction (+z, the incident wave travels along -z) and a
+    360-direction bistatic sweep in the xy plane, for the plain FP64 and the
+    mixed solution at once (two solutions, one call); the mixed path's RCS
+    error against the FP64 LU solution is stated."""
+    n, ne = ds.n, ds.ne
+    lib.peec_gb300_copy_device(x_mixed + n * 16, ds.dx, n * 16)  # [mixed, plain]
+    ph = np.radians(np.arange(360.0))
+    dirs = np.concatenate([[[0.0, 0.0, 1.0]], np.stack([np.cos(ph), np.sin(ph), np.zeros_like(ph)], 1)])
+    dirs = np.ascontiguousarray(dirs)
+    out = np.zeros((dirs.shape[0], 2, 3), dtype=np.complex128)
+    k = ds.k0
+    args = (C.byref(ds.m.mesh), C.byref(ds.m.dual), x_mixed, 2, n, k, dirs.ctypes.data_as(ds.abi.c_double_p),
+            dirs.shape[0], 6, out.ctypes.data)
+    assert lib.peec_gb300_rcs_radiation_device(*args) == 0  # warm
+    ts = []
+    for _ in range(3):
+        t = time.perf_counter()
+        assert lib.peec_gb300_rcs_radiation_device(*args) == 0
+        ts.append(time.perf_counter() - t)
+    xs = np.zeros(2 * n, dtype=np.complex128)
+    lib.peec_gb300_copy_to_host(xs.ctypes.data, x_mixed, xs.nbytes)
+    Im, Ip = xs[:ne], xs[n:n + ne]
+    cur_err = float(np.max(np.abs(Im - Ip)) / np.max(np.abs(Ip)))
+    eta0 = np.sqrt(4e-7 * np.pi / 8.8541878128e-12)
+    T = dirs[:, None, :] * np.sum(dirs[:, None, :] * out, axis=2)[:, :, None] - out
+    sigma = k * k * eta0 * eta0 * np.sum(np.abs(T) ** 2, axis=2) / (4 * np.pi)  # E0 = 1 V/m
+    sm, sp = sigma[:, 0], sigma[:, 1]
+    return {"value": 1.0 / statistics.median(ts), "unit": "RCS sweeps/s",
+            "ms_per_sweep": 1e3 * statistics.median(ts), "directions": int(dirs.shape[0]), "solutions": 2,
+            "edges": ne, "surface_order": 6,
+            "monostatic_sigma_dbsm": {"plain_fp64": float(10 * np.log10(sp[0])), "mixed": float(10 * np.log10(sm[0]))},
+            "mixed_vs_fp64_max_rel_sigma_err": float(np.max(np.abs(sm - sp) / np.abs(sp))),
+            "mixed_vs_fp64_rel_radiation_err": float(np.max(np.abs(out[:, 0] - out[:, 1])) / np.max(np.abs(out[:, 1]))),
+            "edge_current_rel_err": cur_err}
+
+
 def retarded_leg(lib, ds):
     """The same box and frequency with the retarded kernel exp(-jkR)/R on Lp
     and P (complex assembly, complex MNA fill, mixed solve to the 1e-10
@@ -641,6 +679,11 @@ def main():
                  "phase_ms": {k: statistics.median(v) for k, v in ds.phase_ms_mixed.items()},
                  "precision": "FP32 far field (near field FP64), FP32 LU with split-BF16x3 tcgen05 trailing "
                               "update (FP32 accumulation), FP64 iterative refinement"}
+    # keep the mixed solution for the RCS comparison
+    x_mixed = None
+    if mixed is not None:
+        x_mixed = lib.peec_gb300_device_alloc(2 * ds.n * 16)
+        lib.peec_gb300_copy_device(x_mixed, ds.dx, ds.n * 16)
     # one more solve, outside the timed region, with the LU phase timing on
     lib.peec_gb300_lu_timing_enable(1)
     ds.step()
@@ -649,6 +692,10 @@ def main():
     lib.peec_gb300_lu_timing_enable(0)
     lu_phases = {"panel_ms": lu_t[0].value, "swap_trsm_ms": lu_t[1].value, "update_ms": lu_t[2].value,
                  "update_flops": lu_t[3].value}
+    rcs = None
+    if x_mixed:
+        rcs = rcs_leg(lib, ds, x_mixed)
+        lib.peec_gb300_device_free(x_mixed)
     p64, p32 = C.c_double(), C.c_double()
     lib.peec_gb300_pipe_peaks(C.byref(p64), C.byref(p32))
     transient = transient_leg(lib, ds, args.transient_steps) if args.transient_steps > 0 else None
@@ -719,6 +766,7 @@ def main():
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
                 "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "batched": batched, "transient": transient, "retarded": retarded,
+                "rcs": rcs,
                 "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
                                       "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
                 "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}

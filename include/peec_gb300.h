@@ -152,6 +152,21 @@ int peec_gb300_tc_gemm(const void *d_a, const void *d_b0, const void *d_b1, floa
 int peec_gb300_tc_gemm_cplx(const void *d_a, const void *d_br, const void *d_bi, float *d_c, int m,
                             int n, int k, int row0, int col0, long long ldc);
 
+/* ---- RCS radiation vectors (rcs.c:701-1000, dual-patch quadrature) ----
+ * For every direction d (directions: host [n_dir][3], unit vectors) and
+ * every solution s (edge currents on the device, solution s at
+ * d_current + s * current_stride, current_stride >= n_edges: e.g. the
+ * harmonic solution vectors, whose first n_edges entries are the edge
+ * currents), radiation[(d * n_rhs + s) * 3 + c] (host) =
+ * sum_e (I_e / w_e) G_e(d) e_hat_c with G_e the surface_order Gauss rule of
+ * exp(j k d.r) over the edge's dual patches, w_e = S_e / l_e; edges with
+ * l_e <= 0 or S_e <= 0 contribute nothing.  FP64; returns 0, or -1 on
+ * invalid input (k <= 0, unsupported order, mesh and dual mismatch). */
+int peec_gb300_rcs_radiation_device(const Mesh *mesh, const DualMesh *dual, const Complex *d_current,
+                                    size_t n_rhs, size_t current_stride, double wave_number,
+                                    const double *directions, size_t n_dir, int order,
+                                    Complex *radiation);
+
 /* ---- mixed precision complex solve ----
  * Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
  * another) to a componentwise backward error <= tol: row and column

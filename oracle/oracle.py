@@ -63,6 +63,8 @@ class Oracle:
              [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, D, D, D]),
             ("oracle_transient_rhs_stage1", C.c_int,
              [D, D, D, D, P(C.c_int), C.c_size_t, C.c_size_t, C.c_int, C.c_double, D, D, D, D, D]),
+            ("oracle_rcs_radiation_vector", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), P(abi.Complex), C.c_double, D, C.c_int, P(abi.Complex)]),
             ("oracle_lightning_current", C.c_double,
              [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
             ("oracle_transient_lightning", C.c_int,
@@ -161,6 +163,11 @@ class Oracle:
                                             out.ctypes.data_as(D))
         return s, out
 
+    def rcs_radiation(self, m, current, wave_number, directions, order=6):
+        """[n_dir][3] complex radiation vectors of one edge current vector."""
+        return _rcs(self.lib.oracle_rcs_radiation_vector, m, current, wave_number, directions,
+                    lambda f, cur, d, out: f(C.byref(m.mesh), C.byref(m.dual), cur, wave_number, d, order, out))
+
     def transient_matrix(self, L, P_, edges, R, scheme, dt):
         ne, nv = L.shape[0], P_.shape[0]
         nt = ne + nv
@@ -200,6 +207,26 @@ def _transient_lightning(fn, L, P_, edges, R, scheme, dt, source, n_steps, I, V,
     return s, I, V, probes
 
 
+def _rcs(fn, m, current, wave_number, directions, call):
+    cur = np.ascontiguousarray(current, dtype=np.complex128)
+    dirs = np.ascontiguousarray(directions, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((dirs.shape[0], 3), dtype=np.complex128)
+    cp = cur.ctypes.data_as(P(abi.Complex))
+    for q in range(dirs.shape[0]):
+        d = np.ascontiguousarray(dirs[q])
+        o = (abi.Complex * 3)()
+        s = call(fn, cp, _dp(d), o)
+        if s != 0:
+            return s, out
+        out[q] = [complex(o[c].re, o[c].im) for c in range(3)]
+    return 0, out
+
+
+class RcsOptions(C.Structure):
+    """rcs.h RcsOptions (integration 1 = dual-patch quadrature)."""
+    _fields_ = [("integration", C.c_int), ("surface_order", C.c_int), ("parallel_threads", C.c_int)]
+
+
 def reference_available():
     return os.path.exists(REF_PATH)
 
@@ -220,11 +247,22 @@ class Reference:
             ("dual_mesh_build", C.c_int, [P(abi.Mesh), P(abi.DualMesh)]),
         ]
         abi._bind(lib, extra)
+        f = lib.rcs_compute_radiation_vector
+        f.restype, f.argtypes = C.c_int, [P(abi.Mesh), P(abi.DualMesh), P(abi.Complex), C.c_double, D,
+                                          P(RcsOptions), P(abi.Complex)]
         f = lib.ref_transient_lightning
         f.restype, f.argtypes = C.c_int, [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, C.c_double,
               C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_size_t, D, D,
               P(C.c_int), C.c_size_t, P(C.c_int), C.c_size_t, D]
         self.lib = lib
+
+    def rcs_radiation(self, m, current, wave_number, directions, order=6):
+        """The reference's rcs_compute_radiation_vector (one thread: its
+        edge reduction is then sequential)."""
+        opt = RcsOptions(1, order, 1)
+        return _rcs(self.lib.rcs_compute_radiation_vector, m, current, wave_number, directions,
+                    lambda f, cur, d, out: f(C.byref(m.mesh), C.byref(m.dual), cur, wave_number, d,
+                                             C.byref(opt), out))
 
     def transient_lightning(self, L, P_, edges, R, scheme, dt, source, n_steps, I=None, V=None,
                             probe_nodes=(), probe_edges=()):

@@ -999,3 +999,87 @@ int oracle_retarded_matrix(const Mesh *mesh, const DualMesh *dual, int kind, con
     free(stat);
     return failed ? -1 : 0;
 }
+
+
+/* ------------------------------------------------------------------ */
+/* RCS radiation vector, dual-patch quadrature (rcs.c:238-1000)        */
+/* ------------------------------------------------------------------ */
+
+/* integral over triangle (p0, p1, p2) of exp(j k dir.r) dS by the
+ * collapsed-square Gauss rule of `order` (rcs.c:238-362): the points in
+ * (iu, iv) order, cos / sin of the phase, weight (0.5 w_u)(0.5 w_v) J. */
+static int rcs_triangle(const double p0[3], const double p1[3], const double p2[3], double k,
+                        const double dir[3], int order, double *re, double *im)
+{
+    double x[16], w[16];
+    if (order <= 0 || order > 16 || oracle_gauss_legendre_rule(order, x, w) != 0) return -1;
+    double a[3], b[3], c[3];
+    for (int d = 0; d < 3; ++d) {
+        a[d] = p1[d] - p0[d];
+        b[d] = p2[d] - p0[d];
+    }
+    v_cross(a, b, c);
+    const double area2 = v_norm(c);
+    double sr = 0.0, si = 0.0;
+    for (int iu = 0; iu < order; ++iu) {
+        const double u = 0.5 * (x[iu] + 1.0), wu = 0.5 * w[iu];
+        for (int iv = 0; iv < order; ++iv) {
+            const double v = 0.5 * (x[iv] + 1.0), wv = 0.5 * w[iv];
+            const double xi = u, eta = (1.0 - u) * v;
+            double r[3];
+            for (int d = 0; d < 3; ++d) r[d] = p0[d] + xi * a[d] + eta * b[d];
+            const double jac = area2 * (1.0 - u);
+            const double phase = k * v_dot(dir, r);
+            const double weight = wu * wv * jac;
+            sr += weight * cos(phase);
+            si += weight * sin(phase);
+        }
+    }
+    *re = sr;
+    *im = si;
+    return 0;
+}
+
+int oracle_rcs_radiation_vector(const Mesh *mesh, const DualMesh *dual, const Complex *current,
+                                double wave_number, const double dir[3], int order, Complex out[3])
+{
+    if (!mesh || !dual || !current || !dir || !out || !mesh->edge_vectors || !dual->edge_patches ||
+        !dual->edge_region_areas || dual->n_edges != mesh->n_edges)
+        return -1;
+    if (!isfinite(wave_number) || wave_number <= 0.0 || !order_ok(order)) return -1;
+    double F[6] = {0, 0, 0, 0, 0, 0};  /* x re, x im, y re, y im, z re, z im */
+    for (size_t e = 0; e < mesh->n_edges; ++e) {
+        const double *ev = mesh->edge_vectors + 3 * e;
+        const double len = v_norm(ev);
+        if (len <= 0.0) continue;                              /* rcs.c:801-806 */
+        const double ed[3] = {ev[0] / len, ev[1] / len, ev[2] / len};
+        const double area = dual->edge_region_areas[e];
+        if (area <= 0.0) continue;                             /* rcs.c:866-869 */
+        const double width = area / len;
+        /* G_e: patches in list order, triangles (0,1,2) then (0,2,3) */
+        double gr = 0.0, gi = 0.0;
+        const PatchList *list = &dual->edge_patches[e];
+        for (size_t q = 0; q < list->count; ++q) {
+            double p[4][3];
+            for (int i = 0; i < 4; ++i) corner(&list->patches[q], i, p[i]);
+            double r0, i0, r1, i1;
+            if (rcs_triangle(p[0], p[1], p[2], wave_number, dir, order, &r0, &i0) != 0 ||
+                rcs_triangle(p[0], p[2], p[3], wave_number, dir, order, &r1, &i1) != 0)
+                return -1;
+            gr += r0 + r1;
+            gi += i0 + i1;
+        }
+        /* (I_e / w_e) G_e along the edge direction (rcs.c:920-990) */
+        const double cr = current[e].re / width, ci = current[e].im / width;
+        const double sr = cr * gr - ci * gi, si = cr * gi + ci * gr;
+        for (int d = 0; d < 3; ++d) {
+            F[2 * d] += sr * ed[d];
+            F[2 * d + 1] += si * ed[d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        out[d].re = F[2 * d];
+        out[d].im = F[2 * d + 1];
+    }
+    return 0;
+}

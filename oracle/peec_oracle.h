@@ -119,6 +119,11 @@ int oracle_retarded_matrix(const Mesh *mesh, const DualMesh *dual, int kind, con
                            double near_factor, double direction_tolerance, double wave_number,
                            int threads, double *out);
 
+/* RCS radiation vector F(dir) = sum_e (I_e / w_e) G_e(dir) e_hat of one edge
+ * current vector, dual-patch quadrature of `order` (rcs.c:701-1000). */
+int oracle_rcs_radiation_vector(const Mesh *mesh, const DualMesh *dual, const Complex *current,
+                                double wave_number, const double dir[3], int order, Complex out[3]);
+
 #ifdef __cplusplus
 }
 #endif

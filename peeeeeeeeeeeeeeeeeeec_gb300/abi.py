@@ -231,6 +231,9 @@ EXT_SYMBOLS = [
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
       C.c_longlong]),
     ("peec_gb300_round_to_f32_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]),
+    ("peec_gb300_rcs_radiation_device", C.c_int,
+     [C.POINTER(Mesh), C.POINTER(DualMesh), C.c_void_p, C.c_size_t, C.c_size_t, C.c_double, c_double_p,
+      C.c_size_t, C.c_int, C.c_void_p]),
     ("peec_gb300_complex_solve_mixed_device", C.c_int,
      [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, c_double_p,
       c_int_p]),

@@ -273,6 +273,34 @@ def transient_case(R, name, n_steps, strike, ret, r_edge=1.0e-3):
     print("wrote transient_" + name, n_steps, "steps")
 
 
+# RCS radiation vectors (rcs.c:701-1000, dual-patch quadrature, one thread so
+# that the reference's edge reduction is sequential) of a seeded complex edge
+# current on the fixture's own mesh, for a few directions, wave numbers and
+# surface orders.
+RCS_K = (0.63, 6.3)
+RCS_ORDERS = (6, 4)
+
+
+def rcs_case(R, name):
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    f = np.load(os.path.join(HERE, name + ".npz"))
+    rng = np.random.default_rng(11)
+    with SynthMesh.from_arrays(f["xyz"], f["quads"]) as m:
+        ne = m.n_edges
+        cur = rng.standard_normal(ne) + 1j * rng.standard_normal(ne)
+        th, ph = np.arccos(rng.uniform(-1, 1, 6)), rng.uniform(0, 2 * np.pi, 6)
+        dirs = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+        dirs[0] = (0.0, 0.0, 1.0)
+        out = dict(current=cur, directions=dirs, k=np.array(RCS_K), orders=np.array(RCS_ORDERS))
+        for k in RCS_K:
+            for order in RCS_ORDERS:
+                s, F = R.rcs_radiation(m, cur, k, dirs, order)
+                assert s == 0
+                out["F_%g_%d" % (k, order)] = F
+    np.savez_compressed(os.path.join(HERE, "rcs_" + name + ".npz"), **out)
+    print("wrote rcs_" + name)
+
+
 def main():
     R = Reference()
     quadrature_cases(R)
@@ -283,6 +311,8 @@ def main():
     reference_case(R, *box_arrays(2.0, 1.0, 0.5, 40, 20, 10), "box_5cm_topology", with_matrices=False)
     transient_case(R, "plate4", 300, 0, 24)
     transient_case(R, "box421", 200, 0, 5)
+    rcs_case(R, "plate4")
+    rcs_case(R, "box421")
     plate_msh = os.path.join(REF_MESH_DIR, "plate.msh")
     if os.path.exists(plate_msh):
         gmsh_case(R, plate_msh, "plate_msh")

@@ -302,3 +302,25 @@ def test_retarded_oracle_limits(oracle):
         ratio = Pk[i, j] / P0[i, j]
         d = np.linalg.norm(m.array("xyz", (m.n_nodes, 3))[i] - m.array("xyz", (m.n_nodes, 3))[j])
         assert abs(ratio - np.exp(-1j * k * d)) < 2e-2
+
+
+@pytest.mark.parametrize("name", ["plate4", "box421"])
+def test_rcs_radiation_against_reference_fixtures(oracle, name):
+    """The oracle's RCS radiation vector (rcs.c:701-1000) equals the
+    reference's own output bit for bit on the fixture meshes."""
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    f, g = golden(name), golden("rcs_" + name)
+    with SynthMesh.from_arrays(f["xyz"], f["quads"]) as m:
+        for k in g["k"]:
+            for order in g["orders"]:
+                s, F = oracle.rcs_radiation(m, g["current"], float(k), g["directions"], int(order))
+                assert s == 0
+                assert np.array_equal(F, g["F_%g_%d" % (k, order)]), (k, order)
+
+
+def test_rcs_radiation_invalid_inputs(oracle):
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    with SynthMesh.plate(1.0, 1.0, 2, 2) as m:
+        cur = np.ones(m.n_edges, dtype=np.complex128)
+        assert oracle.rcs_radiation(m, cur, 0.0, [[0, 0, 1]])[0] == -1
+        assert oracle.rcs_radiation(m, cur, 1.0, [[0, 0, 1]], order=7)[0] == -1
