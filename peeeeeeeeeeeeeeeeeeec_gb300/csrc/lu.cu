@@ -1459,9 +1459,12 @@ __global__ void __launch_bounds__(256) k_laswp(T *a, int n, int k0, int kb, cons
             s_src[t] = k0 + t;
         }
         int cnt = kb;
+        // the kb pivots in one load (lane l holds piv[k0 + l]); the steps below
+        // take them by shuffle instead of one dependent load each
+        const int my_p = lane < kb ? (int)piv[k0 + lane] : 0;
         __syncwarp();
         for (int kk = 0; kk < kb; ++kk) {
-            const int k = k0 + kk, p = (int)piv[k];
+            const int k = k0 + kk, p = __shfl_sync(0xffffffffu, my_p, kk);
             if (p == k) continue;
             int ip;
             if (p < k0 + kb) {

@@ -398,6 +398,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Tile t of the persistent schedule in groups of kGroupM tile rows: the
+// tiles in flight at once (one per SM) cover ~kGroupM rows x 152/kGroupM
+// columns of C, so their A and B tiles stay in L2 while C streams.
+static const int kGroupM = 8;
+__device__ __forceinline__ void tile_of(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
+    const int per_group = kGroupM * tiles_n;
+    const int first = (t / per_group) * kGroupM;
+    const int gm = min(tiles_m - first, kGroupM);
+    const int r = t % per_group;
+    tm = first + r % gm;
+    tn = r / gm;
+}
+
 template <int BN, int S>
 __host__ __device__ constexpr size_t smem_bytes_persistent() {
     return (size_t)S * ((size_t)kBM * kBK * 2 + (size_t)2 * BN * kBK * 2) + (size_t)2 * kBM * 128 + 1024 + 256;
@@ -458,7 +471,10 @@ __global__ void __launch_bounds__(192, 1)
             long long it = 0;
             const uint64_t keep = policy_evict_last();
             for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
-                const int tm = (t / tiles_n) * kBM, tn = (t % tiles_n) * BN;
+                int tm, tn;
+                tile_of(t, tiles_m, tiles_n, tm, tn);
+                tm *= kBM;
+                tn *= BN;
                 for (int kt = 0; kt < ktiles; ++kt, ++it) {
                     const int s = (int)(it % kStages);
                     if (it >= kStages && !mbar_wait(&empty[s], (uint32_t)((it / kStages) - 1) & 1, abort_flag)) {
@@ -540,11 +556,16 @@ __global__ void __launch_bounds__(192, 1)
         // prefetch the first chunk
         if (leader && t < ntiles) {
             mbar_expect_tx(&cfull[0], chunk_bytes);
-            tma_load_2d_hint(cbuf, &map_c, 2 * ((t % tiles_n) * BN), (t / tiles_n) * kBM, &cfull[0], stream_c);
+            int tm0, tn0;
+            tile_of(t, tiles_m, tiles_n, tm0, tn0);
+            tma_load_2d_hint(cbuf, &map_c, 2 * (tn0 * BN), tm0 * kBM, &cfull[0], stream_c);
         }
         for (; t < ntiles; t += gridDim.x, ++lt) {
             const int b = lt & 1;
-            const int tm = (t / tiles_n) * kBM, tn = (t % tiles_n) * BN;
+            int tm, tn;
+            tile_of(t, tiles_m, tiles_n, tm, tn);
+            tm *= kBM;
+            tn *= BN;
             if (uniform_fail(mbar_wait(&tfull[b], (uint32_t)(lt >> 1) & 1, abort_flag))) break;
             fence_after_sync();
             const uint32_t acc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 2 * BN);
@@ -561,8 +582,10 @@ __global__ void __launch_bounds__(192, 1)
                     if (nt < ntiles) {
                         const int nb = (int)((gi + 1) & 1);
                         mbar_expect_tx(&cfull[nb], chunk_bytes);
-                        tma_load_2d_hint(cbuf + nb * chunk_bytes, &map_c, 2 * ((nt % tiles_n) * BN + nch * kEpiCols),
-                                         (nt / tiles_n) * kBM, &cfull[nb], stream_c);
+                        int ntm, ntn;
+                        tile_of(nt, tiles_m, tiles_n, ntm, ntn);
+                        tma_load_2d_hint(cbuf + nb * chunk_bytes, &map_c, 2 * (ntn * BN + nch * kEpiCols), ntm * kBM,
+                                         &cfull[nb], stream_c);
                     }
                 }
                 __syncwarp();
