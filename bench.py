@@ -373,6 +373,7 @@ def retarded_leg(lib, ds):
     al = lib.peec_gb300_device_alloc
     dLc, dPc = al(ds.ne * ds.ne * 16), al(ds.nv * ds.nv * 16)
     out = {}
+    prev = lib.peec_gb300_set_far_precision(2)  # the mixed path's FP32 far rule
     for rep in range(2):
         ev = [lib.peec_gb300_event_record()]
         assert lib.peec_gb300_inductance_retarded_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.lo), k, dLc,
@@ -396,13 +397,111 @@ def retarded_leg(lib, ds):
                "phase_ms": {"assemble_Lp_retarded": ms[0], "assemble_P_retarded": ms[1], "mna_fill_rhs": ms[2],
                             "mixed_solve": ms[3]},
                "backward_error": be.value, "refinement_iterations": it.value, "wave_number_per_m": k,
-               "kernel": "exp(-jkR)/R: static integral (FP64 near field, double-float far rule) + "
+               "kernel": "exp(-jkR)/R: static integral (FP64 near field, FP32 far rule) + "
                          "(exp(-jkR)-1)/R by the far product rule on the FP32 pipes"}
         for e in ev:
             lib.peec_gb300_event_destroy(e)
+    lib.peec_gb300_set_far_precision(prev)
     for p in (dLc, dPc):
         lib.peec_gb300_device_free(p)
     return out
+
+
+def config3(lib):
+    """The 2.5 cm box (80 x 40 x 20 cells: Ne 22400, Nv 11202, N 33602) at
+    100 MHz with retarded Lp / P (FP32 far rule, FP64 near field) and one
+    x-polarised plane wave from +z: the mixed solve (FP32 LU, split-BF16x3
+    tensor-core updates, FP64 refinement to the 1e-10 gate), then the plain
+    FP64 LU of the same Z as the reference for the current and RCS errors.
+    One JSON line; not part of the default run (the FP64 LU alone takes
+    about 1.5 minutes at this size)."""
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    m = SynthMesh.box(2.0, 1.0, 0.5, 80, 40, 20)
+    ds = DeviceSolve(lib, m)
+    n, ne, nv = ds.n, ds.ne, ds.nv
+    f = 100e6
+    k = 2 * np.pi * f / C0
+    al = lib.peec_gb300_device_alloc
+    dLc, dPc = al(ne * ne * 16), al(nv * nv * 16)
+    assert dLc and dPc
+    prev = lib.peec_gb300_set_far_precision(2)
+    ev = [lib.peec_gb300_event_record()]
+    st = ds.abi.PeecAssemblyStats(), ds.abi.PeecAssemblyStats()
+    assert lib.peec_gb300_inductance_retarded_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.lo), k, dLc,
+                                                     C.byref(st[0])) == 0
+    ev.append(lib.peec_gb300_event_record())
+    assert lib.peec_gb300_potential_retarded_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.po), k, dPc,
+                                                    C.byref(st[1])) == 0
+    ev.append(lib.peec_gb300_event_record())
+    assert lib.peec_gb300_harmonic_build_retarded_device(dLc, dPc, ds.dedges, None, ne, nv, f, ds.dZ) == 0
+    assert lib.peec_gb300_plane_wave_rhs_device(ds.dctr, ds.dvec, ne, nv, ds.kh, ds.eh, k, ds.db) == 0
+    ev.append(lib.peec_gb300_event_record())
+    lib.peec_gb300_set_far_precision(prev)
+    lib.peec_gb300_synchronize()
+    asm = [lib.peec_gb300_event_elapsed_ms(ev[i], ev[i + 1]) for i in range(3)]
+    for p in (dLc, dPc):
+        lib.peec_gb300_device_free(p)
+    be, it = C.c_double(), C.c_int()
+    runs = []
+    for rep in range(3):  # warm, timed, timed with the factorisation's phase timing
+        if rep == 2:
+            lib.peec_gb300_lu_timing_enable(1)
+        e0 = lib.peec_gb300_event_record()
+        s = lib.peec_gb300_complex_solve_mixed_device(ds.dZ, n, ds.db, ds.dx, 1, 1e-10, 30, C.byref(be), C.byref(it))
+        e1 = lib.peec_gb300_event_record()
+        lib.peec_gb300_synchronize()
+        assert s == 0, "mixed solve failed: %d" % s
+        runs.append(lib.peec_gb300_event_elapsed_ms(e0, e1))
+    mt = [C.c_double() for _ in range(4)]
+    lib.peec_gb300_lu_timing(*[C.byref(x) for x in mt])
+    tt = [C.c_double() for _ in range(2)]
+    lib.peec_gb300_lu_timing_trailing(*[C.byref(x) for x in tt])
+    lib.peec_gb300_lu_timing_enable(0)
+    mp, mf, mr = C.c_double(), C.c_double(), C.c_double()
+    lib.peec_gb300_mixed_timing(C.byref(mp), C.byref(mf), C.byref(mr))
+    x_mixed = al(2 * n * 16)
+    lib.peec_gb300_copy_device(x_mixed, ds.dx, n * 16)
+    # FP64 reference: the plain LU of the same Z
+    assert lib.peec_gb300_copy_device(ds.dLU, ds.dZ, n * n * 16) == 0
+    t0 = time.perf_counter()
+    scale, col = C.c_double(), C.c_int()
+    assert lib.peec_gb300_complex_lu_factor_device(ds.dLU, n, 1e-14, ds.dpiv, ds.dperm, ds.drow, ds.dcol,
+                                                   C.byref(scale), C.byref(col)) == 0
+    assert lib.peec_gb300_complex_lu_solve_device(ds.dLU, ds.dperm, ds.drow, ds.dcol, n, ds.db, ds.dx, 1) == 0
+    lib.peec_gb300_synchronize()
+    t_fp64 = time.perf_counter() - t0
+    out3 = (C.c_double * 3)()
+    assert lib.peec_gb300_backward_error_device(ds.dZ, n, ds.dx, ds.db, 1, out3) == 0
+    ds.k0 = k
+    rcs = rcs_leg(lib, ds, x_mixed)
+    lib.peec_gb300_device_free(x_mixed)
+    bf16 = 1933.8
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            bf16 = json.load(fh).get("bf16_tflops", bf16)
+    except Exception:
+        pass
+    tflops = tt[1].value / (tt[0].value * 1e-3) / 1e12 if tt[0].value > 0 else None
+    line = {"metric": "config 3 (2.5 cm box, 100 MHz, retarded Lp / P, 1 plane wave): mixed solve",
+            "value": 1000.0 / runs[1], "unit": "solves/s", "n_unknowns": n, "Ne": ne, "Nv": nv,
+            "assembly_ms": {"Lp_retarded": asm[0], "P_retarded": asm[1], "mna_fill_rhs": asm[2]},
+            "mixed_solve_ms": runs[1], "mixed_phase_ms": {"prepare": mp.value, "factor": mf.value, "refine": mr.value},
+            "backward_error": be.value, "refinement_iterations": it.value,
+            "lu_phases": {"panel_ms": mt[0].value, "swap_trsm_split_ms": mt[1].value, "tc_update_ms": mt[2].value,
+                          "trailing_gemm_ms": tt[0].value, "trailing_gemm_issued_bf16_flops": tt[1].value},
+            "trailing_gemm_roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",
+                                       "frac": tflops / bf16 if tflops else None,
+                                       "peak_source": "measured (MEASURED_PEAKS.json, cuBLAS BF16 burst)"},
+            "fp64_lu_reference_s": t_fp64, "fp64_backward_error": out3[0],
+            "errors_vs_fp64_lu": {"edge_current_rel": rcs["edge_current_rel_err"],
+                                  "radiation_vector_rel": rcs["mixed_vs_fp64_rel_radiation_err"],
+                                  "sigma_rel_max_over_361_directions": rcs["mixed_vs_fp64_max_rel_sigma_err"]},
+            "monostatic_sigma_dbsm": rcs["monostatic_sigma_dbsm"], "rcs_ms_per_sweep": rcs["ms_per_sweep"],
+            "near_pairs": {"Lp": st[0].near_pairs, "P": st[1].near_pairs},
+            "data": "synthetic (seeded box mesh, unit plane wave)", "dtype": "mixed (see metric)"}
+    print(json.dumps(line), flush=True)
+    ds.free()
+    m.close()
 
 
 def serving_leg(lib, window_s, workers):
@@ -601,6 +700,8 @@ def main():
     ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--batch", default="8x8", help="meshes x frequencies of the batched leg (0: skip)")
+    ap.add_argument("--config3", action="store_true",
+                    help="only the 2.5 cm retarded box (33602 unknowns): mixed solve + FP64 LU reference")
     args = ap.parse_args()
     if args.box:
         set_box(args.box)
@@ -621,6 +722,10 @@ def main():
     lib = abi.load_gpu_lib()
     if not lib.peec_gb300_device_ready():
         raise RuntimeError("no CUDA device")
+    if args.config3:
+        if rank == 0:
+            config3(lib)
+        return
     m = make_mesh()
     ds = DeviceSolve(lib, m)
     for _ in range(args.warmup):
