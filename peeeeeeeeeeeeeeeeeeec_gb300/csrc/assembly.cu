@@ -1315,6 +1315,10 @@ __device__ __forceinline__ f2 df_rsqrt(f2 x) {
 // partner patch is FP32; adding it into a (hi, lo) pair keeps the entry's
 // sum of ~16 k products at FP32 accuracy.  NaN propagates into `acc`.
 __device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF *pb, int npts, f2 &acc) {
+    // The reference skips R <= 0; two FAR patches of nonzero size are apart
+    // (their boxes have a positive gap), so no point pair coincides and the
+    // loop needs no test (patches of zero size are skipped by the caller:
+    // their weights are all zero).  NaN still propagates through rsqrt.
     const int lane = threadIdx.x & 31;
     for (int p = lane; p < npts; p += 32) {
         const float4 A = *reinterpret_cast<const float4 *>(pa + p);  // xh, yh, zh, wh
@@ -1324,19 +1328,16 @@ __device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF 
             const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
             const float4 B1 = *reinterpret_cast<const float4 *>(pb + q + 1);
             float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
-            float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (!(r2 <= 0.0f)) s0 = fmaf(B0.w, rsqrtf(r2), s0);
+            s0 = fmaf(B0.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
             dx = A.x - B1.x;
             dy = A.y - B1.y;
             dz = A.z - B1.z;
-            r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (!(r2 <= 0.0f)) s1 = fmaf(B1.w, rsqrtf(r2), s1);
+            s1 = fmaf(B1.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s1);
         }
         if (q < npts) {
             const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
-            float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
-            float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (!(r2 <= 0.0f)) s0 = fmaf(B0.w, rsqrtf(r2), s0);
+            const float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
+            s0 = fmaf(B0.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
         }
         acc = df_add(acc, two_sum(A.w * s0, A.w * s1));
     }
@@ -1511,7 +1512,9 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                                 continue;
                             }
                             if (T.far_df == 2) {
-                                far_pair_f32_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, facc);
+                                if (R.boxf[2 * i].w != 0.0f && R.boxf[2 * j].w != 0.0f)  // zero-size patches add 0
+                                    far_pair_f32_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts,
+                                                     facc);
                                 continue;
                             }
                             k = far_pair_fp64(T.pts + (size_t)i * T.npts, T.pts + (size_t)j * T.npts, T.npts);
