@@ -232,3 +232,44 @@ def test_box_against_oracle_with_reuse(gpu_lib, oracle):
         assert s == 0 and elem_rel_err(L, oracle.inductance(m)[1]) < TOL
         s, P = potential(gpu_lib, m)
         assert s == 0 and elem_rel_err(P, oracle.potential(m)[1]) < TOL
+
+
+_NEAR_FORMS_PROBE = r"""
+import sys
+import numpy as np
+sys.path.insert(0, {repo!r}); sys.path.insert(0, {tests!r})
+from helpers import inductance, potential
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+lib = abi.load_gpu_lib()
+with SynthMesh.box(0.4, 0.2, 0.1, 8, 4, 2) as m:
+    s1, L = inductance(lib, m)
+    s2, P = potential(lib, m)
+assert s1 == 0 and s2 == 0
+np.savez(sys.argv[1], L=L, P=P)
+"""
+
+
+def test_level_and_depth_first_near_fields_agree(tmp_path):
+    """The level-synchronous near field (default) and the depth-first warp
+    form (PEEC_GB300_NEAR_LEVELS=0) walk the same refinement trees; they sum
+    the accepted nodes in a different association (the reference's
+    recursion vs a running sum), so entries agree to rounding."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = _NEAR_FORMS_PROBE.format(repo=os.path.dirname(here), tests=here)
+    res = {}
+    for mode in ("1", "0"):
+        env = dict(os.environ)
+        env["PEEC_GB300_NEAR_LEVELS"] = mode
+        path = str(tmp_path / ("near_%s.npz" % mode))
+        r = subprocess.run([sys.executable, "-c", code, path], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res[mode] = np.load(path)
+    for key in ("L", "P"):
+        a, b = res["1"][key], res["0"][key]
+        assert np.array_equal(a == 0, b == 0)
+        nz = b != 0
+        assert np.max(np.abs(a[nz] - b[nz]) / np.abs(b[nz])) < 1e-13, key

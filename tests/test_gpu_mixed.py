@@ -206,3 +206,45 @@ def test_fp32_rounding_matches_ieee(gpu_lib):
         ref[np.abs(x) < 2.0 ** -1022] = np.copysign(np.float32(0.0), x[np.abs(x) < 2.0 ** -1022])
         assert np.array_equal(y.view(np.uint32)[~np.isnan(ref)], ref.view(np.uint32)[~np.isnan(ref)]), shift
         assert np.all(np.isnan(y[np.isnan(ref)]))
+
+
+_PANEL_FORMS_PROBE = r"""
+import sys
+import numpy as np
+sys.path.insert(0, {repo!r}); sys.path.insert(0, {tests!r})
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+from test_gpu_mixed import mixed_solve, backward_error
+lib = abi.load_gpu_lib()
+rng = np.random.default_rng(21)
+out = []
+for n in (700, 1900):
+    Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + n ** 0.5 * np.eye(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    s, x, be, it = mixed_solve(lib, Z, b)
+    assert s == 0 and be <= 1e-10 and backward_error(Z, x, b) <= 1e-10, (n, s, be)
+    out.append(x)
+np.save(sys.argv[1], np.concatenate(out))
+"""
+
+
+@pytest.mark.parametrize("form", ["lean", "coop", "calu"])
+def test_every_fp32_panel_form_reaches_the_gate(gpu_lib, form, tmp_path):
+    """The mixed solve with each FP32 panel form (PEEC_GB300_MIXED_PANEL:
+    cluster by default, lean grid, cooperative grid, tournament) reaches the
+    1e-10 gate, and the solutions agree with the default form's."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = _PANEL_FORMS_PROBE.format(repo=os.path.dirname(here), tests=here)
+    sols = {}
+    for f in ("default", form):
+        env = dict(os.environ)
+        env.pop("PEEC_GB300_MIXED_PANEL", None)
+        if f != "default":
+            env["PEEC_GB300_MIXED_PANEL"] = f
+        path = str(tmp_path / (f + ".npy"))
+        r = subprocess.run([sys.executable, "-c", code, path], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        sols[f] = np.load(path)
+    assert rel_err(sols[form], sols["default"]) < 1e-8
