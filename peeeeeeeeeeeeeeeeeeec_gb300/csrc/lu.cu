@@ -725,6 +725,212 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean(cplxf *a, int n, in
     if (c == 0 && tid == 0) atomicExch(&ps->gen, gen0 + (unsigned)kb);
 }
 
+// ---- lean FP64 panel (the plain LU) --------------------------------
+// The lean panel's structure for the FP64 factorisations, with the
+// reference's arithmetic kept bit for bit (FP64 |z|, first maximum wins,
+// NaN never wins, L = a / pivot by the same complex division, one msub per
+// pivot and element in pivot order): 64 rows per CTA, one per thread;
+// candidates published with an epoch-tagged flag carrying the magnitude
+// rounded to FP32 (monotonic: the FP32 maximum identifies the winner unless
+// several candidates share it, then their exact FP64 magnitudes decide);
+// the previous column's row update deferred to run while the flags travel.
+template <class T>
+__device__ __forceinline__ double lean64_mag(T v, bool diag) {
+    double m = mag_t(v);
+    if (isnan(m)) m = diag ? INFINITY : -1.0;
+    return m;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kLeanThreads) k_panel_lean64(T *a, int n, int k0, int kb, double limit,
+                                                               long long *piv, Status *st, PanelSlots *ps,
+                                                               unsigned long long *flag, int flag_stride,
+                                                               int *cand_idx, double *cand_val, T *cand_row,
+                                                               T *krow) {
+    __shared__ T tile[kLeanThreads][kPS];
+    __shared__ T s_prow[2][NB];
+    __shared__ double s_wv[2], s_gb;
+    __shared__ int s_wi[2], s_gc, s_p, s_timeout;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned G = gridDim.x;
+    const int c = blockIdx.x;
+    const int r0 = k0 + c * kLeanThreads, r1 = min(n, r0 + kLeanThreads);
+    const int nrows = r1 > r0 ? r1 - r0 : 0;
+    if (st->code != 0) return;  // uniform across CTAs (set before launch)
+    const unsigned gen0 = *(volatile unsigned *)&ps->gen;
+    for (int t = tid; t < nrows * kb; t += kLeanThreads) {
+        const int ii = t / kb, j = t % kb;
+        tile[ii][j] = a[(size_t)(r0 + ii) * n + k0 + j];
+    }
+    if (tid == 0) s_timeout = 0;
+    __syncthreads();
+    const int i = r0 + tid;
+    const bool mine = tid < nrows;
+    T *row = tile[tid];
+    double mv = mine ? lean64_mag(row[0], i == k0) : -1.0;
+    T mreg = T{};
+    for (int kk = 0; kk < kb; ++kk) {
+        const int k = k0 + kk, par = kk & 1;
+        const unsigned epoch = gen0 + (unsigned)kk + 1u;
+        const T *pprev = s_prow[par ^ 1];
+        double bv = (mine && i >= k) ? mv : -1.0;
+        int bi = bv >= 0.0 ? i : n;
+        for (int sh = 16; sh > 0; sh >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, bv, sh);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
+            if (ov > bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_wv[warp] = bv;
+            s_wi[warp] = bi;
+        }
+        __syncthreads();
+        if (s_wv[1] > s_wv[0] || (s_wv[1] == s_wv[0] && s_wi[1] < s_wi[0])) {
+            bv = s_wv[1];
+            bi = s_wi[1];
+        } else {
+            bv = s_wv[0];
+            bi = s_wi[0];
+        }
+        if (warp == 0 && bi < n && lane < kb) cand_row[((size_t)par * G + c) * NB + lane] = tile[bi - r0][lane];
+        if (warp == 1 && k >= r0 && k < r1 && lane < kb) krow[(size_t)par * NB + lane] = tile[k - r0][lane];
+        if (tid == 0) {
+            cand_idx[par * G + c] = bi;
+            cand_val[par * G + c] = bv;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_relaxed_u64(flag + (size_t)par * flag_stride + c,
+                           ((unsigned long long)epoch << 32) | __float_as_uint(bi < n ? (float)bv : -1.0f));
+        }
+        if (kk > 0 && mine && i >= k)
+            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], mreg, pprev[j]);
+        if (warp == 0) {
+            unsigned long long v[kLeanPoll];
+            unsigned pending = 0;
+#pragma unroll
+            for (int u = 0; u < kLeanPoll; ++u)
+                if (64 * (u >> 1) + 2 * lane + (u & 1) < (int)G) pending |= 1u << u;
+            for (long long spin = 0; pending && spin < kSpinLimit; ++spin) {
+#pragma unroll
+                for (int u = 0; u < kLeanPoll; u += 2)
+                    if (pending & (3u << u))
+                        ld_relaxed_v2u64(flag + (size_t)par * flag_stride + 64 * (u >> 1) + 2 * lane, v[u], v[u + 1]);
+#pragma unroll
+                for (int u = 0; u < kLeanPoll; ++u)
+                    if ((pending & (1u << u)) && (unsigned)(v[u] >> 32) == epoch) pending &= ~(1u << u);
+                if ((spin & 1023) == 1023 && *(volatile int *)&ps->timeout) break;
+            }
+            fence_acquire_gpu();
+            const bool ok = pending == 0;
+            // FP32 maximum, then the exact FP64 maximum among those sharing it
+            float fb = -2.0f;
+#pragma unroll
+            for (int u = 0; u < kLeanPoll; ++u) {
+                const int q = 64 * (u >> 1) + 2 * lane + (u & 1);
+                const float f = __uint_as_float((unsigned)v[u]);
+                if (ok && q < (int)G && f >= 0.0f && f > fb) fb = f;
+            }
+            for (int sh = 16; sh > 0; sh >>= 1) fb = fmaxf(fb, __shfl_xor_sync(0xffffffffu, fb, sh));
+            double eb = -1.0;
+            int eq = -1;
+#pragma unroll
+            for (int u = 0; u < kLeanPoll; ++u) {
+                const int q = 64 * (u >> 1) + 2 * lane + (u & 1);
+                if (!ok || q >= (int)G || fb < 0.0f || __uint_as_float((unsigned)v[u]) != fb) continue;
+                const double ev = ld_volatile(cand_val + par * G + q);
+                if (eq < 0 || ev > eb || (ev == eb && q < eq)) {
+                    eb = ev;
+                    eq = q;
+                }
+            }
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, eb, sh);
+                const int oq = __shfl_xor_sync(0xffffffffu, eq, sh);
+                if (oq >= 0 && (eq < 0 || ov > eb || (ov == eb && oq < eq))) {
+                    eb = ov;
+                    eq = oq;
+                }
+            }
+            if (!ok) atomicExch(&ps->timeout, 1);
+            const bool any_fail = __any_sync(0xffffffffu, !ok);
+            if (lane == 0) {
+                s_gc = eq;
+                s_gb = eb;
+                s_timeout = any_fail ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        if (s_timeout) {
+            if (tid == 0) atomicCAS(&st->code, 0, 6);
+            return;
+        }
+        const int gc = s_gc;
+        const double gb = s_gb;
+        if (gc < 0 || !isfinite(gb) || gb <= limit) {
+            if (c == 0 && tid == 0) {
+                st->code = 2;
+                st->column = k;
+                st->value = gc < 0 ? -1.0 : gb;
+            }
+            return;
+        }
+        T *pcur = s_prow[par];
+        T kval = T{};
+        if (gc == c) {
+            if (warp == 0 && lane < kb) pcur[lane] = tile[bi - r0][lane];
+            if (tid == 0) s_p = bi;
+            if (warp == 1 && bi != k && lane < kb) {
+                if (k >= r0 && k < r1) {
+                    kval = tile[k - r0][lane];
+                } else {
+                    kval = ld_volatile(krow + (size_t)par * NB + lane);
+                    if (kk > 0 && lane > kk) kval = msub(kval, ld_volatile(krow + (size_t)par * NB + kk - 1), pprev[lane]);
+                }
+            }
+        } else {
+            if (warp == 0 && lane < kb) {
+                const T *cr = cand_row + ((size_t)par * G + gc) * NB;
+                T vv = ld_volatile(cr + lane);
+                if (kk > 0 && lane > kk) vv = msub(vv, ld_volatile(cr + kk - 1), pprev[lane]);
+                pcur[lane] = vv;
+            }
+            if (warp == 1 && lane == 0) s_p = ld_volatile(cand_idx + par * G + gc);
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p != k) {
+            if (warp == 0 && k >= r0 && k < r1 && lane < kb) tile[k - r0][lane] = pcur[lane];
+            if (warp == 1 && gc == c && lane < kb) tile[p - r0][lane] = kval;
+        }
+        if (c == 0 && tid == 0) piv[k] = p;
+        __syncthreads();
+        if (k + 1 >= n) break;
+        if (mine && i > k) {
+            mreg = divide(row[kk], pcur[kk]);
+            row[kk] = mreg;
+            if (kk + 1 < kb) {
+                row[kk + 1] = msub(row[kk + 1], mreg, pcur[kk + 1]);
+                mv = lean64_mag(row[kk + 1], i == k + 1);
+            } else {
+                mv = -1.0;
+            }
+        } else {
+            mv = -1.0;
+        }
+    }
+    __syncthreads();
+    for (int t = tid; t < nrows * kb; t += kLeanThreads) {
+        const int ii = t / kb, j = t % kb;
+        a[(size_t)(r0 + ii) * n + k0 + j] = tile[ii][j];
+    }
+    if (c == 0 && tid == 0) atomicExch(&ps->gen, gen0 + (unsigned)kb);
+}
+
 // ---- cluster FP32 panel (the mixed path) ---------------------------
 // The lean panel's per-column exchange still crosses the GPU: measured on
 // GB300, a release store takes ~2 us to reach pollers on other SMs, while a
@@ -2429,6 +2635,27 @@ static int lean_panel_ctas(int m) {
     return g <= cap && g <= 32 * kLeanPoll ? g : 0;
 }
 
+// CTAs of the lean FP64 panel (k_panel_lean64) for m rows, 0 where it does
+// not apply (PEEC_GB300_PANEL=coop or =cluster selects another form).
+template <class T>
+static int lean64_panel_ctas(int m) {
+    static const int cap = [] {
+        const char *e = getenv("PEEC_GB300_PANEL");
+        if (e && (strcmp(e, "coop") == 0 || strcmp(e, "cluster") == 0)) return 0;
+        int dev = 0, sms = 0, coop = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (!coop ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_panel_lean64<T>, kLeanThreads, 0) != cudaSuccess)
+            return 0;
+        return per_sm * sms;
+    }();
+    if (m < 2 * kLeanThreads) return 0;
+    const int g = (m + kLeanThreads - 1) / kLeanThreads;
+    return g <= cap && g <= 32 * kLeanPoll ? g : 0;
+}
+
 // FP32 panels of the mixed path by tournament pivoting when
 // PEEC_GB300_MIXED_PANEL=calu; partial pivoting otherwise.  Measured on
 // GB300 (8402 unknowns) the tournament panel takes 75 ms per factorisation
@@ -2506,6 +2733,15 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
     if (tm.enabled) tm.reset();
     DBuf<unsigned char> scratch;
     PanelScratch sc;
+    // lean FP64 panel slots: ceil(n / 64) CTAs at most
+    const size_t GL = (size_t)(n + kLeanThreads - 1) / kLeanThreads;
+    const int lean_stride = (int)((GL + 63) / 64 * 64);
+    DBuf<unsigned long long> lean_flag(2 * (size_t)lean_stride);
+    DBuf<int> lean_idx(2 * GL);
+    DBuf<double> lean_val(2 * GL);
+    DBuf<T> lean_rows(2 * GL * NB + 2 * NB);
+    if (!lean_flag.p || !lean_idx.p || !lean_val.p || !lean_rows.p) return false;
+    cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
     {
         int sms = 0, dev = 0;
         cudaGetDevice(&dev);
@@ -2527,7 +2763,20 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
         int kb = std::min(NB, n - k0);
         tm.mark(2);
         CoopPlan<T> pl = coop_plan<T>(n - k0);
+        const int lean_g = lean64_panel_ctas<T>(n - k0);
         if (cluster_panel_enabled() && launch_cluster_panel<T>(d_a, n, k0, kb, limit, d_piv, d_st)) {
+        } else if (lean_g > 0) {
+            unsigned long long *fl = lean_flag.p;
+            int fls = lean_stride;
+            int *li = lean_idx.p;
+            double *lv = lean_val.p;
+            T *lr = lean_rows.p, *lk = lean_rows.p + 2 * GL * NB;
+            void *args[] = {&d_a, &n, (void *)&k0, &kb, &limit, &d_piv, &d_st, &sc.ps, &fl, &fls, &li, &lv, &lr, &lk};
+            if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_lean64<T>, dim3(lean_g), dim3(kLeanThreads),
+                                                     args, 0, stream()),
+                         "lean FP64 panel launch"))
+                return false;
+            note_launch();
         } else if (pl.G > 0) {
             int rows = pl.rows;
             T *cr = (T *)sc.cand_row, *kr = (T *)sc.krow;
