@@ -762,11 +762,18 @@ def main():
         for _ in range(args.warmup):
             ds.step_mixed()
         ds.phase_ms_mixed = {}
+        msteps = max(args.steps, 10)  # 0.15 s a solve: ten or more steps steady the mean
         lib.peec_gb300_synchronize()
-        m0 = lib.peec_gb300_event_record()
-        mbes = [ds.step_mixed() for _ in range(args.steps)]
-        m1 = lib.peec_gb300_event_record()
-        mixed_ms = lib.peec_gb300_event_elapsed_ms(m0, m1) / args.steps
+        marks = [lib.peec_gb300_event_record()]
+        mbes = []
+        for _ in range(msteps):
+            mbes.append(ds.step_mixed())
+            marks.append(lib.peec_gb300_event_record())
+        each = [lib.peec_gb300_event_elapsed_ms(marks[i], marks[i + 1]) for i in range(msteps)]
+        mixed_ms = lib.peec_gb300_event_elapsed_ms(marks[0], marks[-1]) / msteps
+        split_terms = lib.peec_gb300_mixed_split_terms()
+        for e in marks:
+            lib.peec_gb300_event_destroy(e)
         # one more mixed solve with the factorisation's phase timing on
         lib.peec_gb300_lu_timing_enable(1)
         ds.step_mixed()
@@ -778,12 +785,15 @@ def main():
         mixed_lu = {"panel_ms": mt[0].value, "swap_trsm_split_ms": mt[1].value, "tc_update_ms": mt[2].value,
                     "tc_update_issued_bf16_flops": mt[3].value, "trailing_gemm_ms": tt[0].value,
                     "trailing_gemm_issued_bf16_flops": tt[1].value}
-        mixed = {"value": world * 1000.0 / mixed_ms, "unit": "solves/s", "ms_per_step": mixed_ms,
+        mixed = {"value": world * 1000.0 / mixed_ms, "unit": "solves/s", "ms_per_step": mixed_ms, "steps": msteps,
+                 "ms_per_step_min": min(each), "ms_per_step_median": statistics.median(each),
                  "vs_plain_fp64_gpu": (1000.0 / mixed_ms) / (1000.0 / ms_step),
-                 "backward_error": max(mbes), "refinement_iterations": ds.mixed_iters, "lu_phases": mixed_lu,
+                 "backward_error": max(mbes), "refinement_iterations": ds.mixed_iters,
+                 "split_bf16_terms": split_terms, "lu_phases": mixed_lu,
                  "phase_ms": {k: statistics.median(v) for k, v in ds.phase_ms_mixed.items()},
                  "precision": "FP32 far field (near field FP64), FP32 LU with split-BF16x3 tcgen05 trailing "
-                              "update (FP32 accumulation), FP64 iterative refinement"}
+                              "update (FP32 accumulation; BF16x6 when refinement stalls), FP64 iterative "
+                              "refinement"}
     # keep the mixed solution for the RCS comparison
     x_mixed = None
     if mixed is not None:

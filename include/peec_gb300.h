@@ -168,23 +168,32 @@ int peec_gb300_rcs_radiation_device(const Mesh *mesh, const DualMesh *dual, cons
                                     Complex *radiation);
 
 /* ---- mixed precision complex solve ----
- * Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
- * another) to a componentwise backward error <= tol: row and column
- * equilibration by powers of two, FP32 LU whose trailing updates run on the tensor
- * cores as split-BF16x3 products (FP32 accumulation), then FP64 iterative
- * refinement r = B - Z X.  d_Z and d_b are not modified.  Returns 0 when
- * converged, 1 when max_iter refinements did not reach tol (X holds the last
- * iterate), -2 for a zero / non-finite row or column or a singular FP32
- * pivot, -1 on other errors.  backward_error / iterations may be NULL. */
-/* The FP32 rounding used by the mixed-precision solve's equilibration:
+ * The FP32 rounding used by the mixed-precision solve's equilibration:
  * d_y[i] = d_x[i] * 2^-shift rounded to the nearest FP32 (ties to even) by
  * integer operations on the FP64 bits; results below 2^-126 flush to zero,
  * beyond the FP32 range give +-inf, NaN stays NaN. */
 int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, size_t count, int shift);
 
+/* Solves Z X = B (n x n FP64 complex, nrhs right-hand sides stored one after
+ * another) to a componentwise backward error <= tol: row and column
+ * equilibration by powers of two, FP32 LU whose trailing updates run on the
+ * tensor cores as split-BF16x3 products (FP32 accumulation), then FP64
+ * iterative refinement r = B - Z X from X = 0.  When the refinement stalls
+ * (a backward error that is not finite, or a smallest backward error so far
+ * not a factor 4 below the smallest three sweeps earlier) or the FP32 pivots
+ * break down, the FP32 copy of Z is factored again with split-BF16x6
+ * products (three-part operands, FP32-equivalent) and refined again from
+ * X = 0, until the gate, max_iter sweeps, or no factor 2 of progress over
+ * six sweeps.  d_Z and d_b are not modified.  Returns 0 when converged, 1
+ * when the refinement did not reach tol (X holds the last iterate), -2 for a zero /
+ * non-finite row or column or a singular FP32 pivot, -1 on other errors.
+ * backward_error / iterations (sweeps of all attempts) may be NULL. */
 int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Complex *d_b,
                                           Complex *d_x, size_t nrhs, double tol, int max_iter,
                                           double *backward_error, int *iterations);
+/* Split-BF16 product terms (3 or 6) of the last mixed solve's final
+ * factorisation on this host thread. */
+int peec_gb300_mixed_split_terms(void);
 /* FP64 iterative refinement of d_x (in: a solution, out: the refined one)
  * with an FP64 factor of Z from peec_gb300_complex_lu_factor_device:
  * r = b - Z x, x += (LU)^-1 r until the componentwise backward error

@@ -2017,7 +2017,12 @@ __global__ void k_perm(const long long *piv, int n, int *perm, const Status *st)
 // precomputed inverse of its diagonal block (k_diag_inverse) as one more
 // tile and publishes x with a per-block ready flag.  The inverse turns the
 // 64-step dependent substitution, which on one warp would run at a quarter
-// of the SM's small FP64 rate, into a product spread over all warps.
+// of the SM's small FP64 rate, into a product spread over all warps.  The
+// FP32 factor of the mixed path (WaveArgs::subst) solves its upper blocks by
+// substitution instead, one warp per right-hand side: an FP32 inverse of an
+// ill-conditioned upper block (condition numbers near 1e7 at kHz
+// frequencies) is not backward stable, and iterative refinement from it
+// stalls; unit lower blocks with |l_ij| <= 1 keep the inverse.
 // Every task waits only on earlier tasks of the global order (forward
 // 0..nb-1, then backward nb-1..0) and each CTA runs its tasks in that order,
 // so with all CTAs co-resident the earliest unfinished task can always
@@ -2040,6 +2045,7 @@ struct WaveArgs {
     T *out;                   // unscaled copy (col_scale set), else unused
     unsigned *flags;          // [nchunks][2][nb], zero on entry
     int *error;
+    int subst;                // upper blocks by substitution (dinv's upper half from k_diag_copy_upper)
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -2122,6 +2128,25 @@ __global__ void __launch_bounds__(128) k_diag_inverse(const T *lu, int n, T *din
     }
 }
 
+// The upper diagonal blocks of a packed LU factor for substitution, over
+// the U_bb^-1 half of dinv, transposed (column j of a block is row j of its
+// copy): the strict upper part of U_bb with 1 / u_jj on the diagonal, zeros
+// elsewhere and outside the matrix.  One CTA per block.
+template <class T>
+__global__ void __launch_bounds__(256) k_diag_copy_upper(const T *lu, int n, T *dinv) {
+    const int b = blockIdx.x, r0 = b * kRB, nrow = min(kRB, n - r0);
+    T *du = dinv + ((size_t)b * 2 + 1) * kRB * kRB;
+    for (int t = threadIdx.x; t < kRB * kRB; t += blockDim.x) {
+        const int j = t / kRB, i = t % kRB;  // entry (i, j) of the block goes to du[j][i]
+        T u = zero_t<T>();
+        if (i < nrow && j < nrow && i <= j) {
+            const T v = lu[(size_t)(r0 + i) * n + r0 + j];
+            u = i < j ? v : divide(one_t(T{}), v);
+        }
+        du[t] = u;
+    }
+}
+
 // bounded wait for *flag != 0 by one thread; false on timeout / abort
 __device__ __forceinline__ bool wave_wait(const unsigned *flag, int *error) {
     long long spins = 0;
@@ -2158,6 +2183,16 @@ __device__ __forceinline__ T shfl_xor_t(T v, int m) {
     unsigned *pr = reinterpret_cast<unsigned *>(&r);
 #pragma unroll
     for (int w = 0; w < (int)(sizeof(T) / 4); ++w) pr[w] = __shfl_xor_sync(0xffffffffu, pv[w], m);
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ T shfl_t(T v, int src) {
+    T r;
+    const unsigned *pv = reinterpret_cast<const unsigned *>(&v);
+    unsigned *pr = reinterpret_cast<unsigned *>(&r);
+#pragma unroll
+    for (int w = 0; w < (int)(sizeof(T) / 4); ++w) pr[w] = __shfl_sync(0xffffffffu, pv[w], src);
     return r;
 }
 
@@ -2268,6 +2303,42 @@ __device__ bool wave_block(const WaveArgs<T> &A, int blk, int c0, int nr, unsign
     }
     cp_async_wait_all();
     __syncthreads();
+    if (!LOWER && A.subst) {
+        // x_b from U_b x_b = y by substitution, warp q for right-hand side q,
+        // lane l holding rows l and l + 32; S.dinv holds U_b transposed
+        // (k_diag_copy_upper), so step j reads column j as one conflict-free row
+        if (warp < nr) {
+            const int q = warp;
+            T v0 = S.y[q][lane], v1 = S.y[q][lane + 32];
+            for (int j = nrow - 1; j >= 0; --j) {
+                const T *col = S.dinv + j * kDS;
+                const T xj = mac(zero_t<T>(), shfl_t(j < 32 ? v0 : v1, j & 31), col[j]);
+                v0 = msub(v0, col[lane], xj);
+                v1 = msub(v1, col[lane + 32], xj);
+                if (lane == (j & 31)) {  // row j is final: x_j (its own update above is discarded)
+                    if (j < 32)
+                        v0 = xj;
+                    else
+                        v1 = xj;
+                }
+            }
+            T *xq = A.x + (size_t)(c0 + q) * n + r0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int row = lane + 32 * h;
+                const T v = h ? v1 : v0;
+                if (row < nrow) {
+                    xq[row] = v;
+                    if (A.col_scale)
+                        A.out[(size_t)(c0 + q) * n + r0 + row] = scale_div(v, A.col_scale[r0 + row]);
+                }
+            }
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release_u32(flags + blk, 1u);
+        return true;
+    }
     // x_b = D_b^-1 y: four threads per row, interleaved columns qq + 4k
     for (int q = 0; q < nr; ++q) {
         T v = zero_t<T>();
@@ -2328,15 +2399,18 @@ static size_t wave_dinv_count(int n) {
     return (size_t)nb * 2 * kRB * kRB;
 }
 
-// Computes the diagonal-block inverses of the factor into dinv.
+// Computes the diagonal-block inverses of the factor into dinv; with subst
+// the upper half then holds the transposed upper blocks for substitution
+// (WaveArgs::subst).
 template <class T>
-static bool wave_prepare(const T *lu, int n, T *dinv) {
+static bool wave_prepare(const T *lu, int n, T *dinv, bool subst = false) {
     constexpr size_t smem = (size_t)3 * kRB * kRS * sizeof(T);
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_diag_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (!cuda_ok(attr, "diagonal block inverse smem attribute")) return false;
     int nb = (n + kRB - 1) / kRB;
     PEEC_LAUNCH(k_diag_inverse<T>, nb, 128, smem, lu, n, dinv);
+    if (subst) PEEC_LAUNCH(k_diag_copy_upper<T>, nb, 256, 0, lu, n, dinv);
     return launch_ok("diagonal block inverses");
 }
 
@@ -2603,6 +2677,16 @@ static bool cluster_panel_enabled() {
         return e && strcmp(e, "cluster") == 0;
     }();
     return on;
+}
+
+// Split-BF16 terms the mixed path's first factorisation uses: 3 (BF16x3),
+// or 6 (BF16x6) with PEEC_GB300_MIXED_SPLIT=6.
+static int mixed_split_terms() {
+    static const int t = [] {
+        const char *e = getenv("PEEC_GB300_MIXED_SPLIT");
+        return e && strcmp(e, "6") == 0 ? 6 : 3;
+    }();
+    return t;
 }
 
 // FP32 panel of the mixed path: the cluster panel (k_panel_cl) where the
@@ -3568,42 +3652,66 @@ __global__ void k_eq2_to_float(const cplx *z, int n, const int *er, const int *e
     }
 }
 
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &h, __nv_bfloat16 &l) {
-    h = __float2bfloat16_rn(x);
-    l = __float2bfloat16_rn(x - __bfloat162float(h));
+// x = h + m (+ l): each part the BF16 rounding of what the earlier parts
+// leave (x - h and x - h - m are exact in FP32).
+template <int P>
+__device__ __forceinline__ void split_parts(float x, __nv_bfloat16 (&v)[P]) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        v[p] = __float2bfloat16_rn(x);
+        x -= __bfloat162float(v[p]);
+    }
 }
 
-// Split-BF16x3 operands of one complex trailing update C -= L U, K = 6 KW:
+// The products of one split-BF16 real product a b: T = 3 terms (BF16x3,
+// two-part operands: h h + h m + m h, about 16 bits) or T = 6 terms (BF16x6,
+// three-part operands: h h + h m + m h + h l + m m + l h, the products the
+// FP32 rounding of a b keeps).  Term t multiplies part split_pa(t) of a by
+// part split_pb(t) of b.
+template <int T> struct SplitScheme {
+    static constexpr int parts = T == 3 ? 2 : 3;
+    static constexpr int planes = 2 * T;  // K = planes x KW
+    __host__ __device__ static constexpr int pa(int t) { return t == 2 || t == 4 ? 1 : t == 5 ? 2 : 0; }
+    __host__ __device__ static constexpr int pb(int t) { return t == 1 || t == 4 ? 1 : t == 3 ? 2 : 0; }
+};
+
+// Split operands of one complex trailing update C -= L U, K = 2 T KW:
 // A' row r (0..m-1) <- L[row0 + r][col0 .. col0+kw-1] (zero-padded to KW) as
-// the planes [re_h | re_h | re_l | im_h | im_h | im_l], KW wide each.
+// 2 T planes KW wide, [re part pa(0) .. re part pa(T-1) | im part pa(0) ..],
+// e.g. [re_h | re_h | re_l | im_h | im_h | im_l] for T = 3.
+template <int T>
 __global__ void k_split_a(const cplxf *a, int n, int row0, int m, int col0, int kw, int KW, __nv_bfloat16 *out) {
+    using S = SplitScheme<T>;
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)m * KW) return;
     int r = (int)(t / KW), c = (int)(t % KW);
     cplxf x = c < kw ? a[(size_t)(row0 + r) * n + col0 + c] : cplxf{0.0f, 0.0f};
-    __nv_bfloat16 rh, rl, ih, il;
-    split_bf16(x.re, rh, rl);
-    split_bf16(x.im, ih, il);
-    __nv_bfloat16 *row = out + (size_t)r * 6 * KW;
-    row[c] = rh;
-    row[KW + c] = rh;
-    row[2 * KW + c] = rl;
-    row[3 * KW + c] = ih;
-    row[4 * KW + c] = ih;
-    row[5 * KW + c] = il;
+    __nv_bfloat16 re[S::parts], im[S::parts];
+    split_parts(x.re, re);
+    split_parts(x.im, im);
+    __nv_bfloat16 *row = out + (size_t)r * S::planes * KW;
+#pragma unroll
+    for (int q = 0; q < T; ++q) {
+        row[q * KW + c] = re[S::pa(q)];
+        row[(T + q) * KW + c] = im[S::pa(q)];
+    }
 }
 
-// Br', Bi' row j (0..nc-1) <- U[row0 .. row0+kw-1][col0 + j]:
-// Br' = [re_h | re_l | re_h | -im_h | -im_l | -im_h], Bi' = [im_h | im_l | im_h | re_h | re_l | re_h],
-// so that A' Br' = Re(L U) and A' Bi' = Im(L U) to FP32 accuracy.
+// Br', Bi' row j (0..nc-1) <- U[row0 .. row0+kw-1][col0 + j] as 2 T planes:
+// Br' = [re part pb(q) | -im part pb(q)], Bi' = [im part pb(q) | re part pb(q)]
+// (q = 0 .. T-1), so that A' Br' = Re(L U) and A' Bi' = Im(L U); for T = 3
+// Br' = [re_h | re_l | re_h | -im_h | -im_l | -im_h].
 // A 64 (K) x 32 (columns) tile per CTA goes through shared memory: rows of U
-// are read along the columns (coalesced), the four BF16 parts are kept as
+// are read along the columns (coalesced), the BF16 parts are kept as
 // K-contiguous planes, and the K-major outputs are written as 128-byte
 // segments of 16-byte stores.  grid (ceil(nc / 32), ceil(KW / 64)), 256 threads.
 static const int kSbK = 64, kSbJ = 32, kSbPad = 72;  // plane row: 72 BF16 = 144 bytes (16-byte aligned)
+template <int T>
 __global__ void __launch_bounds__(256) k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int col0, int nc,
                                                  __nv_bfloat16 *br, __nv_bfloat16 *bi) {
-    __shared__ __align__(16) __nv_bfloat16 pl[4][kSbJ][kSbPad];  // re_h, re_l, im_h, im_l
+    using S = SplitScheme<T>;
+    constexpr int NP = S::parts;
+    __shared__ __align__(16) __nv_bfloat16 pl[2 * NP][kSbJ][kSbPad];  // re parts, then im parts
     const int t = threadIdx.x, j0 = blockIdx.x * kSbJ, c0 = blockIdx.y * kSbK;
     {
         const int j = t & 31;
@@ -3611,31 +3719,33 @@ __global__ void __launch_bounds__(256) k_split_b(const cplxf *a, int n, int row0
             const int c = rr * 8 + (t >> 5);
             cplxf x = (c0 + c < kw && j0 + j < nc) ? a[(size_t)(row0 + c0 + c) * n + col0 + j0 + j]
                                                    : cplxf{0.0f, 0.0f};
-            __nv_bfloat16 rh, rl, ih, il;
-            split_bf16(x.re, rh, rl);
-            split_bf16(x.im, ih, il);
-            pl[0][j][c] = rh;
-            pl[1][j][c] = rl;
-            pl[2][j][c] = ih;
-            pl[3][j][c] = il;
+            __nv_bfloat16 re[NP], im[NP];
+            split_parts(x.re, re);
+            split_parts(x.im, im);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                pl[p][j][c] = re[p];
+                pl[NP + p][j][c] = im[p];
+            }
         }
     }
     __syncthreads();
-    // output segment seg (0..11): br planes 0..5, bi planes 6..11; within
-    // six, parts (h, l, h) of the first then the second component
-    for (int q = t; q < 12 * kSbJ * (kSbK / 8); q += blockDim.x) {
+    // output segment seg (0 .. 4T-1): br planes 0..2T-1, then bi planes;
+    // within 2T planes, the parts pb(q) of the first then the second component
+    for (int q = t; q < 2 * S::planes * kSbJ * (kSbK / 8); q += blockDim.x) {
         const int e = q & 7, j = (q >> 3) & (kSbJ - 1), seg = q >> 8;
         const int c = c0 + 8 * e;
         if (j0 + j >= nc || c >= KW) continue;
-        const int s6 = seg % 6, second = s6 / 3, lo = (s6 % 3) == 1;
-        const int imag = (seg < 6) ? second : 1 - second;
-        uint4 v = *reinterpret_cast<const uint4 *>(&pl[2 * imag + lo][j][8 * e]);
-        const unsigned m = (seg < 6 && second) ? 0x80008000u : 0u;
+        const bool is_bi = seg >= S::planes;
+        const int p = seg % S::planes, second = p / T, part = S::pb(p % T);
+        const int imag = is_bi ? 1 - second : second;
+        uint4 v = *reinterpret_cast<const uint4 *>(&pl[NP * imag + part][j][8 * e]);
+        const unsigned m = (!is_bi && second) ? 0x80008000u : 0u;
         v.x ^= m;
         v.y ^= m;
         v.z ^= m;
         v.w ^= m;
-        __nv_bfloat16 *out = (seg < 6 ? br : bi) + (size_t)(j0 + j) * 6 * KW + (seg % 6) * KW + c;
+        __nv_bfloat16 *out = (is_bi ? bi : br) + (size_t)(j0 + j) * S::planes * KW + p * KW + c;
         *reinterpret_cast<uint4 *>(out) = v;
     }
 }
@@ -3804,7 +3914,7 @@ __global__ void k_add_cplx(cplx *x, const cplx *dx, size_t count) {
 
 struct MixedTiming {
     double ms_prepare = 0, ms_factor = 0, ms_refine = 0;
-    int iterations = 0;
+    int iterations = 0, split_terms = 3;
 };
 static thread_local MixedTiming g_mixed_timing;  // last mixed solve of this host thread
 
@@ -3872,7 +3982,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     // two-level blocking: 32-column panels inside 256-column outer blocks, so
     // the bulk of the trailing update runs with K = 6 x 256 on the tensor cores
     const int OB = 256;
-    DBuf<__nv_bfloat16> ap((size_t)n * 6 * OB), bpr((size_t)n * 6 * OB), bpi((size_t)n * 6 * OB);
+    DBuf<__nv_bfloat16> ap((size_t)n * 12 * OB), bpr((size_t)n * 12 * OB), bpi((size_t)n * 12 * OB);
     DBuf<cplxf> linv((size_t)OB * OB);  // I - L11^-1 of one outer block
     // tournament panel scratch (nominees of every CTA and group, the pivot block)
     const int kMaxCta = kCaluMaxRows / NB * kCaluGroup;
@@ -3941,205 +4051,275 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     if (!isfinite(scale) || scale <= 0.0) return -2;
     const double limit = 1e-14 * scale;
     cudaEventRecord(ev[1], stream());
-    // FP32 factorisation, trailing updates on the tensor cores
     cplxf *a = f.p;
     LuTiming &tm = g_lu_timing;
-    if (tm.enabled) tm.reset();
-    // C[row0.., col0..] -= L[row0.., kc..kc+kw) U[kc..kc+kw, col0..), split-BF16x3
-    // (the L operand may come from another matrix: lsrc with leading dimension
-    // ld, its rows lrow0.., columns lcol0..)
-    auto tc_update_from = [&](const cplxf *lsrc, int ld, int lrow0, int lcol0, int row0, int m, int col0, int nc,
-                              int kc, int kw) -> bool {
-        if (m <= 0 || nc <= 0) return true;
-        const int KW = (kw + 31) / 32 * 32;
-        PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
-                    ap.p);
-        PEEC_LAUNCH(k_split_b, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
-                    bpr.p, bpi.p);
-        if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
-        return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
-    };
-    auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw, bool outer = false) -> bool {
-        if (m <= 0 || nc <= 0) return true;
-        const int KW = (kw + 31) / 32 * 32;
-        PEEC_LAUNCH(k_split_a, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
-        PEEC_LAUNCH(k_split_b, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
-                    bpr.p, bpi.p);
-        if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);  // issued BF16 tensor flops
-        if (!outer) return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
-        tm.mark(2);
-        if (tm.enabled) tm.flops_outer += 2.0 * 2.0 * (double)m * nc * (6.0 * KW);
-        const bool ok = tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 6 * KW, row0, col0, n, err.p);
-        tm.mark(3);
-        return ok;
-    };
-    for (int K0 = 0; K0 < n; K0 += OB) {
-        const int E = std::min(n, K0 + OB);  // the outer block is columns [K0, E)
-        for (int k0 = K0; k0 < E; k0 += NB) {
-            const int kb = std::min(NB, E - k0);
+    // split-BF16 terms of the trailing update products: BF16x3 first (about
+    // 16 bits), BF16x6 (FP32-equivalent) when refinement from the BF16x3
+    // factor stalls; PEEC_GB300_MIXED_SPLIT=6 starts with BF16x6
+    int T = mixed_split_terms();
+    // FP32 factorisation of f, trailing updates on the tensor cores: 0, -2 on
+    // a pivot breakdown, -1 on errors
+    auto factor = [&]() -> int {
+        if (tm.enabled) tm.reset();
+        // C[row0.., col0..] -= L[row0.., kc..kc+kw) U[kc..kc+kw, col0..), split-BF16 with T terms
+        // (the L operand may come from another matrix: lsrc with leading dimension
+        // ld, its rows lrow0.., columns lcol0..)
+        auto tc_update_from = [&](const cplxf *lsrc, int ld, int lrow0, int lcol0, int row0, int m, int col0, int nc,
+                                  int kc, int kw) -> bool {
+            if (m <= 0 || nc <= 0) return true;
+            const int KW = (kw + 31) / 32 * 32;
+            if (T == 6)
+                PEEC_LAUNCH(k_split_a<6>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
+                        ap.p);
+            else
+                PEEC_LAUNCH(k_split_a<3>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
+                        ap.p);
+            if (T == 6)
+                PEEC_LAUNCH(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                        bpr.p, bpi.p);
+            else
+                PEEC_LAUNCH(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                        bpr.p, bpi.p);
+            if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (2.0 * T * KW);  // issued BF16 tensor flops
+            return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 2 * T * KW, row0, col0, n, err.p);
+        };
+        auto tc_update = [&](int row0, int m, int col0, int nc, int kc, int kw, bool outer = false) -> bool {
+            if (m <= 0 || nc <= 0) return true;
+            const int KW = (kw + 31) / 32 * 32;
+            if (T == 6)
+                PEEC_LAUNCH(k_split_a<6>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
+            else
+                PEEC_LAUNCH(k_split_a<3>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
+            if (T == 6)
+                PEEC_LAUNCH(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                        bpr.p, bpi.p);
+            else
+                PEEC_LAUNCH(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                        bpr.p, bpi.p);
+            if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (2.0 * T * KW);  // issued BF16 tensor flops
+            if (!outer) return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 2 * T * KW, row0, col0, n, err.p);
             tm.mark(2);
-            CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
-            const int lean_g = lean_panel_ctas(n - k0);
-            if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
-            } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
-            } else if (cl_panel_enabled() && launch_cl_panel(a, n, k0, kb, limit, piv.p, st.p)) {
-            } else if (lean_g > 0) {
-                Status *stp = st.p;
-                long long *pivp = piv.p;
-                int kbv = kb;
-                unsigned long long *fl = lean_flag.p;
-                int *li = lean_idx.p;
-                cplxf *lr = lean_rows.p, *lk = lean_rows.p + 2 * GL * NB;
-                int fls = lean_stride;
-                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, (void *)&limit, &pivp, &stp, &sc.ps, &fl, &fls, &li,
-                                &lr, &lk};
-                if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_lean, dim3(lean_g), dim3(kLeanThreads),
-                                                         args, 0, stream()),
-                             "lean panel launch"))
-                    return -1;
-                note_launch();
-            } else if (pl.G > 0) {
-                int rows = pl.rows;
-                cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
-                Status *stp = st.p;
-                long long *pivp = piv.p;
-                int kbv = kb;
-                void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, &rows, (void *)&limit, &pivp, &stp, &sc.ps,
-                                &sc.cand_val, &sc.cand_idx, &cr, &kr};
-                if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<cplxf>, dim3(pl.G), dim3(256),
-                                                         args, pl.smem, stream()),
-                             "cooperative panel launch"))
-                    return -1;
-                note_launch();
-            } else {
-                PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
+            if (tm.enabled) tm.flops_outer += 2.0 * 2.0 * (double)m * nc * (2.0 * T * KW);
+            const bool ok = tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 2 * T * KW, row0, col0, n, err.p);
+            tm.mark(3);
+            return ok;
+        };
+        for (int K0 = 0; K0 < n; K0 += OB) {
+            const int E = std::min(n, K0 + OB);  // the outer block is columns [K0, E)
+            for (int k0 = K0; k0 < E; k0 += NB) {
+                const int kb = std::min(NB, E - k0);
+                tm.mark(2);
+                CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
+                const int lean_g = lean_panel_ctas(n - k0);
+                if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
+                } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
+                } else if (cl_panel_enabled() && launch_cl_panel(a, n, k0, kb, limit, piv.p, st.p)) {
+                } else if (lean_g > 0) {
+                    Status *stp = st.p;
+                    long long *pivp = piv.p;
+                    int kbv = kb;
+                    unsigned long long *fl = lean_flag.p;
+                    int *li = lean_idx.p;
+                    cplxf *lr = lean_rows.p, *lk = lean_rows.p + 2 * GL * NB;
+                    int fls = lean_stride;
+                    void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, (void *)&limit, &pivp, &stp, &sc.ps, &fl, &fls, &li,
+                                    &lr, &lk};
+                    if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_lean, dim3(lean_g), dim3(kLeanThreads),
+                                                             args, 0, stream()),
+                                 "lean panel launch"))
+                        return -1;
+                    note_launch();
+                } else if (pl.G > 0) {
+                    int rows = pl.rows;
+                    cplxf *cr = (cplxf *)sc.cand_row, *kr = (cplxf *)sc.krow;
+                    Status *stp = st.p;
+                    long long *pivp = piv.p;
+                    int kbv = kb;
+                    void *args[] = {&a, (void *)&n, (void *)&k0, &kbv, &rows, (void *)&limit, &pivp, &stp, &sc.ps,
+                                    &sc.cand_val, &sc.cand_idx, &cr, &kr};
+                    if (!cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_coop<cplxf>, dim3(pl.G), dim3(256),
+                                                             args, pl.smem, stream()),
+                                 "cooperative panel launch"))
+                        return -1;
+                    note_launch();
+                } else {
+                    PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
+                }
+                tm.mark(0);
+                PEEC_LAUNCH(k_laswp<cplxf>, (n + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(cplxf), a,
+                            n, k0, kb, piv.p, st.p);
+                // the rest of the outer block's columns: U12 rows, then the narrow update
+                const int rin = E - (k0 + kb);
+                if (rin > 0) PEEC_LAUNCH(k_trsm<cplxf>, (rin + 255) / 256, 256, 0, a, n, k0, kb, k0 + kb, E, st.p);
+                tm.mark(1);
+                if (!tc_update(k0 + kb, n - (k0 + kb), k0 + kb, rin, k0, kb)) return -1;
             }
-            tm.mark(0);
-            PEEC_LAUNCH(k_laswp<cplxf>, (n + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(cplxf), a,
-                        n, k0, kb, piv.p, st.p);
-            // the rest of the outer block's columns: U12 rows, then the narrow update
-            const int rin = E - (k0 + kb);
-            if (rin > 0) PEEC_LAUNCH(k_trsm<cplxf>, (rin + 255) / 256, 256, 0, a, n, k0, kb, k0 + kb, E, st.p);
-            tm.mark(1);
-            if (!tc_update(k0 + kb, n - (k0 + kb), k0 + kb, rin, k0, kb)) return -1;
+            if (E < n) {
+                // U12 of the outer block for the columns right of it in one
+                // tensor-core update: U12 = L11^-1 A12 = A12 - (I - L11^-1) A12
+                const int kw = E - K0;
+                static const cudaError_t li_attr = cudaFuncSetAttribute(
+                    k_lower_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k_lower_inv_smem());
+                if (!cuda_ok(li_attr, "lower-inverse smem attribute")) return -1;
+                PEEC_LAUNCH(k_lower_inv, dim3((kw + 31) / 32, 4), 256, k_lower_inv_smem(), a, n, K0, kw, linv.p);
+                tm.mark(1);
+                if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
+                tm.mark(2);
+                // trailing update with K = 6 x (E - K0)
+                if (!tc_update(E, n - E, E, n - E, K0, E - K0, true)) return -1;
+            }
         }
-        if (E < n) {
-            // U12 of the outer block for the columns right of it in one
-            // tensor-core update: U12 = L11^-1 A12 = A12 - (I - L11^-1) A12
-            const int kw = E - K0;
-            static const cudaError_t li_attr = cudaFuncSetAttribute(
-                k_lower_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k_lower_inv_smem());
-            if (!cuda_ok(li_attr, "lower-inverse smem attribute")) return -1;
-            PEEC_LAUNCH(k_lower_inv, dim3((kw + 31) / 32, 4), 256, k_lower_inv_smem(), a, n, K0, kw, linv.p);
-            tm.mark(1);
-            if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
-            tm.mark(2);
-            // trailing update with K = 6 x (E - K0)
-            if (!tc_update(E, n - E, E, n - E, K0, E - K0, true)) return -1;
+        tm.mark(2);
+        tm.finish();
+        PEEC_LAUNCH(k_check_diag<cplxf>, (n + 255) / 256, 256, 0, a, n, limit, st.p);
+        size_t perm_smem = n_ * sizeof(int);
+        if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+        PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, piv.p, n, perm.p, st.p);
+        int herr = 0;
+        cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+        cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
+        if (!launch_ok("mixed factorisation") || !sync("mixed factorisation")) return -1;
+        if (herr) {
+            set_error("tcgen05 trailing update: a pipeline wait timed out");
+            return -1;
         }
-    }
-    tm.mark(2);
-    tm.finish();
-    PEEC_LAUNCH(k_check_diag<cplxf>, (n + 255) / 256, 256, 0, a, n, limit, st.p);
-    size_t perm_smem = n_ * sizeof(int);
-    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
-    PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, piv.p, n, perm.p, st.p);
-    int herr = 0;
-    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
-    cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
-    cudaEventRecord(ev[2], stream());
-    if (!launch_ok("mixed factorisation") || !sync("mixed factorisation")) return -1;
-    if (herr) {
-        set_error("tcgen05 trailing update: a pipeline wait timed out");
-        return -1;
-    }
-    if (hs.code == 6) {
-        set_error("LU panel synchronisation timed out");
-        return -1;
-    }
-    if (hs.code != 0) return -2;
-    // FP64 iterative refinement
-    cudaMemsetAsync(x, 0, nv * sizeof(cplx), stream());
-    cudaMemcpyAsync(r.p, b, nv * sizeof(cplx), cudaMemcpyDeviceToDevice, stream());
-    double eta = INFINITY;
-    int it = 0;
+        if (hs.code == 6) {
+            set_error("LU panel synchronisation timed out");
+            return -1;
+        }
+        if (hs.code != 0) return -2;
+        return 0;
+    };
+    // FP64 iterative refinement from x = 0: 0 at the gate; 1 when max_iter
+    // sweeps end or the refinement stalls (a backward error that is not
+    // finite, or a smallest backward error so far that is not a factor 4
+    // below the smallest three sweeps earlier with BF16x3 -- the BF16x6
+    // factor is the better choice then -- or a factor 2 below the smallest
+    // six sweeps earlier with BF16x6); -1 on errors
     DBuf<unsigned> wflags(wave_flag_count<cplxf>(n, nrhs));
     DBuf<int> werr(1);
     DBuf<cplxf> wdinv(wave_dinv_count(n));
     DBuf<float> absx(nv);
     if (!wflags.p || !werr.p || !wdinv.p || !absx.p) return -1;
-    cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
-    if (!wave_prepare(a, n, wdinv.p)) return -1;
-    // one refinement sweep (FP32 correction solve, FP64 update, FP64
-    // residual + backward error): captured once as a CUDA graph and
-    // replayed per iteration
-    auto sweep = [&]() {
-        PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
-        WaveArgs<cplxf> W{};
-        W.lu = a;
-        W.dinv = wdinv.p;
-        W.n = n;
-        W.nrhs = nrhs;
-        W.b = y.p;  // already permuted and row-scaled by k_mix_rhs
-        W.x = y.p;
-        W.flags = wflags.p;
-        W.error = werr.p;
-        wave_solve(W);
-        PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs, absx.p);
-        cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
-        PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, b, n, nrhs, r.p,
-                    be.p);
-    };
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    if (!sync("refinement setup")) return -1;
-    unsigned long long sweep_launches = 0;
-    if (cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        unsigned long long l0 = launch_count();
-        sweep();
-        sweep_launches = launch_count() - l0;
-        if (cudaStreamEndCapture(stream(), &graph) != cudaSuccess ||
-            cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {
-            gexec = nullptr;
-        }
-    }
-    cudaGetLastError();  // a failed capture falls back to direct launches
-    for (it = 1; it <= max_iter; ++it) {
-        if (gexec) {
-            if (!cuda_ok(cudaGraphLaunch(gexec, stream()), "refinement graph")) break;
-            note_launch((int)sweep_launches);  // the replayed kernels
-        } else {
+    double eta = INFINITY;
+    int total_it = 0;
+    auto refine = [&]() -> int {
+        cudaMemsetAsync(x, 0, nv * sizeof(cplx), stream());
+        cudaMemcpyAsync(r.p, b, nv * sizeof(cplx), cudaMemcpyDeviceToDevice, stream());
+        cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
+        if (!wave_prepare(a, n, wdinv.p, true)) return -1;
+        // one refinement sweep (FP32 correction solve, FP64 update, FP64
+        // residual + backward error): captured once as a CUDA graph and
+        // replayed per iteration
+        auto sweep = [&]() {
+            PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
+            WaveArgs<cplxf> W{};
+            W.lu = a;
+            W.dinv = wdinv.p;
+            W.n = n;
+            W.nrhs = nrhs;
+            W.b = y.p;  // already permuted and row-scaled by k_mix_rhs
+            W.x = y.p;
+            W.flags = wflags.p;
+            W.error = werr.p;
+            W.subst = 1;  // backward stable for ill-conditioned diagonal blocks of the FP32 factor
+            wave_solve(W);
+            PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs, absx.p);
+            cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+            PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, b, n, nrhs, r.p,
+                        be.p);
+        };
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t gexec = nullptr;
+        if (!sync("refinement setup")) return -1;
+        unsigned long long sweep_launches = 0;
+        if (cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            unsigned long long l0 = launch_count();
             sweep();
+            sweep_launches = launch_count() - l0;
+            if (cudaStreamEndCapture(stream(), &graph) != cudaSuccess ||
+                cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {
+                gexec = nullptr;
+            }
         }
-        unsigned long long hb = 0;
-        int hw = 0;
-        cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
-        cudaMemcpyAsync(&hw, werr.p, sizeof(hw), cudaMemcpyDeviceToHost, stream());
-        if (!launch_ok("refinement") || !sync("refinement") || hw) {
-            if (hw) set_error("triangular solve: a wait for an earlier row block timed out");
-            if (gexec) cudaGraphExecDestroy(gexec);
-            if (graph) cudaGraphDestroy(graph);
-            return -1;
+        cudaGetLastError();  // a failed capture falls back to direct launches
+        const int window = T == 6 ? 6 : 3;
+        const double gain = T == 6 ? 0.5 : 0.25;
+        double best = INFINITY, back[6];  // back[it % window]: the best after sweep it - window
+        for (double &v : back) v = INFINITY;
+        int out = 1, it = 1;
+        eta = INFINITY;
+        for (; it <= max_iter; ++it) {
+            if (gexec) {
+                if (!cuda_ok(cudaGraphLaunch(gexec, stream()), "refinement graph")) {
+                    out = -1;
+                    break;
+                }
+                note_launch((int)sweep_launches);  // the replayed kernels
+            } else {
+                sweep();
+            }
+            unsigned long long hb = 0;
+            int hw = 0;
+            cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
+            cudaMemcpyAsync(&hw, werr.p, sizeof(hw), cudaMemcpyDeviceToHost, stream());
+            if (!launch_ok("refinement") || !sync("refinement") || hw) {
+                if (hw) set_error("triangular solve: a wait for an earlier row block timed out");
+                out = -1;
+                break;
+            }
+            memcpy(&eta, &hb, sizeof(eta));
+            if (eta <= tol) {
+                out = 0;
+                break;
+            }
+            if (!isfinite(eta)) break;
+            best = fmin(best, eta);
+            if (best > gain * back[it % window]) break;
+            back[it % window] = best;
         }
-        memcpy(&eta, &hb, sizeof(eta));
-        if (eta <= tol) break;
+        total_it += it > max_iter ? max_iter : it;
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        return out;
+    };
+    float t01 = -1.0f, ms_factor = 0.0f, ms_refine = 0.0f;
+    int outcome;
+    for (;;) {
+        outcome = factor();
+        cudaEventRecord(ev[2], stream());
+        if (outcome == 0) outcome = refine();
+        cudaEventRecord(ev[3], stream());
+        cudaEventSynchronize(ev[3]);
+        if (t01 < 0.0f) cudaEventElapsedTime(&t01, ev[0], ev[1]);
+        float t12 = 0.0f, t23 = 0.0f;
+        cudaEventElapsedTime(&t12, ev[1], ev[2]);
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        ms_factor += t12;
+        ms_refine += t23;
+        if (outcome == -1 || outcome == 0 || T == 6) break;
+        // stalled (or an FP32 pivot breakdown) with BF16x3: factor the FP32
+        // copy of the equilibrated Z again with BF16x6 products
+        T = 6;
+        cudaEventRecord(ev[1], stream());
+        cudaMemsetAsync(scratch.p, 0, sbytes, stream());
+        cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
+        cudaMemsetAsync(err.p, 0, sizeof(int), stream());
+        cudaMemsetAsync(calu_ps.p, 0, sizeof(PanelSlots), stream());
+        cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
+        PEEC_LAUNCH(k_eq2_to_float, 152 * 16, 256, 0, Z, n, er.p, ec.p, f.p, (float *)nullptr);
     }
-    if (gexec) cudaGraphExecDestroy(gexec);
-    if (graph) cudaGraphDestroy(graph);
-    cudaEventRecord(ev[3], stream());
-    cudaEventSynchronize(ev[3]);
-    float t01, t12, t23;
-    cudaEventElapsedTime(&t01, ev[0], ev[1]);
-    cudaEventElapsedTime(&t12, ev[1], ev[2]);
-    cudaEventElapsedTime(&t23, ev[2], ev[3]);
-    g_mixed_timing.ms_prepare = t01;
-    g_mixed_timing.ms_factor = t12;
-    g_mixed_timing.ms_refine = t23;
-    g_mixed_timing.iterations = it > max_iter ? max_iter : it;
     for (auto &e : ev) cudaEventDestroy(e);
+    if (outcome == -1) return -1;
+    g_mixed_timing.ms_prepare = t01;
+    g_mixed_timing.ms_factor = ms_factor;
+    g_mixed_timing.ms_refine = ms_refine;
+    g_mixed_timing.iterations = total_it;
+    g_mixed_timing.split_terms = T;
     if (backward_error) *backward_error = eta;
-    if (iterations) *iterations = it > max_iter ? max_iter : it;
-    return eta <= tol ? 0 : 1;
+    if (iterations) *iterations = total_it;
+    if (outcome == -2) return -2;
+    return outcome == 0 ? 0 : 1;
 }
 
 namespace peec {
@@ -4158,6 +4338,8 @@ extern "C" int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, siz
     PEEC_LAUNCH(k_round_f32, 152 * 4, 256, 0, d_x, d_y, count, shift);
     return sync("FP32 rounding") ? 0 : -1;
 }
+
+extern "C" int peec_gb300_mixed_split_terms(void) { return peec::g_mixed_timing.split_terms; }
 
 extern "C" int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine) {
     if (ms_prepare) *ms_prepare = peec::g_mixed_timing.ms_prepare;

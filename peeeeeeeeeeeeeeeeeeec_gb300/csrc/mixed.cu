@@ -170,9 +170,9 @@ bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c
         set_error("tcgen05 GEMM: K must be a positive multiple of 64");
         return false;
     }
-    // the LU's K is 192: three stages, 64-column tiles -> two CTAs per SM
-    // narrow updates (the panel's K = 6 x 32 columns): 64-column tiles
-    const bool narrow = k <= 192;
+    // narrow updates (the panel's K = 6 or 12 x 32, at most 256 columns):
+    // 64-column tiles
+    const bool narrow = k <= 192 || (k <= 384 && n <= 256);
     if (persistent_enabled() && persistent_ok(c, ldc, row0, col0))
         return narrow ? launch_tc_persistent<64, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err)
                       : launch_tc_persistent<128, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err);

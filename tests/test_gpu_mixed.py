@@ -105,6 +105,111 @@ def test_peec_box_system_matches_plain_fp64(gpu_lib):
     assert rel_err(x, xp) < 1e-7
 
 
+def mna_matrix(lib, m, freq):
+    """The harmonic MNA matrix of mesh m at freq, assembled on the GPU."""
+    ne, nv = m.n_edges, m.n_nodes
+    n = ne + nv
+    lo = abi.InductanceOptions()
+    lib.inductance_options_default(C.byref(lo), 1)
+    po = abi.PotentialOptions()
+    lib.potential_options_default(C.byref(po), 1)
+    dL = lib.peec_gb300_device_alloc(ne * ne * 8)
+    dP = lib.peec_gb300_device_alloc(nv * nv * 8)
+    dZ = lib.peec_gb300_device_alloc(n * n * 16)
+    dE = dev_put(lib, np.ascontiguousarray(m.edges()))
+    assert lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(lo), dL, None) == 0
+    assert lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(po), dP, None) == 0
+    assert lib.peec_gb300_harmonic_build_device(dL, dP, dE, None, ne, nv, freq, dZ) == 0
+    Z = np.zeros((n, n), dtype=np.complex128)
+    lib.peec_gb300_copy_to_host(Z.ctypes.data, dZ, Z.nbytes)
+    for p in (dL, dP, dZ, dE):
+        lib.peec_gb300_device_free(p)
+    return Z
+
+
+def plate_system(lib, freq):
+    """Plate 1.41 x 1.12 m, 18 x 15 cells (877 unknowns) at freq, excited by an
+    x-polarised unit plane wave at normal incidence (U_e = E . l_e)."""
+    with SynthMesh.plate(1.41, 1.12, 18, 15) as m:
+        ne = m.n_edges
+        Z = mna_matrix(lib, m, freq)
+        vec = m.array("edge_vectors", (ne, 3))
+    b = np.zeros(Z.shape[0], dtype=np.complex128)
+    b[:ne] = -vec[:, 0]
+    return Z, b
+
+
+def test_bf16x3_factor_suffices_at_30mhz(gpu_lib):
+    Z, b = plate_system(gpu_lib, 30e6)
+    s, x, be, it = mixed_solve(gpu_lib, Z, b)
+    assert s == 0, (be, it)
+    assert backward_error(Z, x, b) <= 1e-10
+    assert gpu_lib.peec_gb300_mixed_split_terms() == 3
+
+
+def test_split_escalates_when_refinement_stalls(gpu_lib):
+    """At 1 kHz the equilibrated MNA matrix of the plate has a condition
+    number near 2e8: refinement from the BF16x3 factor (about 16-bit trailing
+    updates) stalls and the solve factors the FP32 matrix again with BF16x6
+    products.  Whether that reaches the gate depends on the system (the
+    serving loop falls back to an FP64 LU when it does not): the solve
+    returns 0 with the gate met, or 1 with a finite last iterate."""
+    Z, b = plate_system(gpu_lib, 1e3)
+    s, x, be, it = mixed_solve(gpu_lib, Z, b)
+    assert gpu_lib.peec_gb300_mixed_split_terms() == 6
+    assert s in (0, 1), (s, be, it)
+    assert np.all(np.isfinite(x))
+    if s == 0:
+        assert backward_error(Z, x, b) <= 1e-10
+
+
+BF16X6_SCRIPT = """
+import ctypes as C, json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+lib = abi.load_gpu_lib()
+rng = np.random.default_rng(1)
+n = 700
+Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 3 * np.eye(n)
+b = rng.standard_normal(n) + 0j
+def put(a):
+    p = lib.peec_gb300_device_alloc(a.nbytes)
+    lib.peec_gb300_copy_to_device(p, a.ctypes.data, a.nbytes)
+    return p
+dZ, db, dx = put(Z), put(b), lib.peec_gb300_device_alloc(b.nbytes)
+be, it = C.c_double(), C.c_int()
+s = lib.peec_gb300_complex_solve_mixed_device(dZ, n, db, dx, 1, 1e-10, 30, C.byref(be), C.byref(it))
+x = np.zeros_like(b)
+lib.peec_gb300_copy_to_host(x.ctypes.data, dx, x.nbytes)
+r = Z @ x - b
+print(json.dumps({"status": s, "iterations": it.value, "terms": lib.peec_gb300_mixed_split_terms(),
+                  "backward_error": float(np.max(np.abs(r) / (np.abs(Z) @ np.abs(x) + np.abs(b))))}))
+"""
+
+
+def test_bf16x6_from_the_start():
+    """PEEC_GB300_MIXED_SPLIT=6 factors with BF16x6 products from the start
+    (a fresh process: the switch is read once): the gate is reached, in no
+    more sweeps than the BF16x3 factor needs."""
+    import json
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for terms in ("3", "6"):
+        env = dict(os.environ, PEEC_GB300_MIXED_SPLIT=terms)
+        r = subprocess.run([sys.executable, "-c", BF16X6_SCRIPT, repo], env=env, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        out[terms] = json.loads(r.stdout.strip().splitlines()[-1])
+    for terms in ("3", "6"):
+        assert out[terms]["status"] == 0 and out[terms]["backward_error"] <= 1e-10
+        assert out[terms]["terms"] == int(terms)
+    assert out["6"]["iterations"] <= out["3"]["iterations"]
+
+
 def test_singular_and_bad_input(gpu_lib):
     Z = np.eye(40, dtype=np.complex128)
     Z[5, :] = 0

@@ -100,12 +100,13 @@ def run_cplx(lib, m, n, k, row0, col0, ldc, rows, seed):
 
 
 # (m, n, k, row0, col0, ldc, rows): even ldc and an aligned block take the
-# persistent kernel (128-column tiles, or 64-column tiles for K <= 192;
+# persistent kernel (128-column tiles, or 64-column tiles for K <= 192 and
+# for K <= 384 with at most 256 columns;
 # several tiles per CTA at the larger sizes, ragged edges); odd ldc takes
 # the one-tile-per-CTA kernels.
 @pytest.mark.parametrize("m,n,k,row0,col0,ldc,rows", [
     (128, 128, 384, 0, 0, 128, 128), (300, 260, 1536, 5, 6, 600, 320), (1000, 700, 768, 2, 4, 800, 1010),
     (4000, 2600, 256, 32, 64, 2700, 4040), (200, 150, 384, 1, 3, 301, 210), (500, 100, 192, 0, 32, 200, 510),
-    (8000, 224, 192, 40, 64, 600, 8040), (300, 90, 192, 1, 3, 301, 310)])
+    (8000, 224, 192, 40, 64, 600, 8040), (300, 90, 192, 1, 3, 301, 310), (2000, 224, 384, 8, 32, 400, 2040)])
 def test_tc_gemm_cplx_block(gpu_lib, m, n, k, row0, col0, ldc, rows):
     run_cplx(gpu_lib, m, n, k, row0, col0, ldc, rows, seed=m + n + k)
