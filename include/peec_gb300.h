@@ -184,8 +184,11 @@ int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, size_t count, 
  * break down, the FP32 copy of Z is factored again with split-BF16x6
  * products (three-part operands, FP32-equivalent) and refined again from
  * X = 0, until the gate, max_iter sweeps, or no factor 2 of progress over
- * six sweeps.  d_Z and d_b are not modified.  Returns 0 when converged, 1
- * when the refinement did not reach tol (X holds the last iterate), -2 for a zero /
+ * six sweeps.  If that stalls too, FGMRES-IR with the BF16x6 factor as the
+ * preconditioner (per right-hand side from X = 0: FP64 residual, inner
+ * flexible GMRES on the row-equilibrated correction equation to 1e-6
+ * relative or 40 steps, at most 10 outer steps).  d_Z and d_b are not modified.  Returns 0 when converged, 1 when
+ * the refinement did not reach tol (X holds the last iterate), -2 for a zero /
  * non-finite row or column or a singular FP32 pivot, -1 on other errors.
  * backward_error / iterations (sweeps of all attempts) may be NULL. */
 int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Complex *d_b,
@@ -194,6 +197,9 @@ int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Co
 /* Split-BF16 product terms (3 or 6) of the last mixed solve's final
  * factorisation on this host thread. */
 int peec_gb300_mixed_split_terms(void);
+/* Inner FGMRES steps of the last mixed solve on this host thread (0 unless
+ * refinement from the BF16x6 factor stalled and FGMRES-IR ran). */
+int peec_gb300_mixed_gmres_iterations(void);
 /* FP64 iterative refinement of d_x (in: a solution, out: the refined one)
  * with an FP64 factor of Z from peec_gb300_complex_lu_factor_device:
  * r = b - Z x, x += (LU)^-1 r until the componentwise backward error

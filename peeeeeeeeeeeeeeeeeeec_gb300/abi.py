@@ -242,6 +242,7 @@ EXT_SYMBOLS = [
       C.c_size_t, C.c_double, C.c_int, c_double_p, c_int_p]),
     ("peec_gb300_mixed_timing", C.c_int, [c_double_p, c_double_p, c_double_p]),
     ("peec_gb300_mixed_split_terms", C.c_int, []),
+    ("peec_gb300_mixed_gmres_iterations", C.c_int, []),
     ("peec_gb300_harmonic_build_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_double,
       C.c_void_p]),

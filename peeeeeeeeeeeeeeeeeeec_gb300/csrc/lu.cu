@@ -26,6 +26,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <complex>
 #include <list>
 #include <mutex>
 #include <type_traits>
@@ -3912,9 +3913,129 @@ __global__ void k_add_cplx(cplx *x, const cplx *dx, size_t count) {
     x[t].im += dx[t].im;
 }
 
+// ---- FGMRES-IR: flexible GMRES on D_r^-1 Z d = D_r^-1 r, preconditioned by
+// the FP32 factor applied in FP32 (Arioli and Duff, "Using FGMRES to obtain
+// backward stability in mixed precision", ETNA 33, 2009) ----
+
+// y = D_r^-1 Z v in FP64, one warp per row
+__global__ void k_zmv_scaled(const cplx *Z, const cplx *v, const double *rs, int n, cplx *y) {
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const cplx *row = Z + (size_t)warp * n;
+    double yr = 0.0, yi = 0.0;
+    for (int j = lane; j < n; j += 32) {
+        const cplx z = row[j], u = v[j];
+        yr = fma(z.re, u.re, yr);
+        yr = fma(-z.im, u.im, yr);
+        yi = fma(z.re, u.im, yi);
+        yi = fma(z.im, u.re, yi);
+    }
+    yr = warp_sum(yr);
+    yi = warp_sum(yi);
+    if (lane == 0) y[warp] = cplx{yr / rs[warp], yi / rs[warp]};
+}
+
+// y = P v rounded to FP32 (v already row-scaled)
+__global__ void k_perm_f32(const cplx *v, const int *perm, int n, cplxf *y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cplx u = v[perm[i]];
+    y[i] = cplxf{(float)u.re, (float)u.im};
+}
+
+// v = D_r^-1 r
+__global__ void k_scale_rows(const cplx *r, const double *rs, int n, cplx *v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = cplx{r[i].re / rs[i], r[i].im / rs[i]};
+}
+
+// w = D_c^-1 y: the FP32 correction solve's result in FP64
+__global__ void k_mix_out(const cplxf *y, const double *cs, int n, cplx *w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = cplx{(double)y[i].re / cs[i], (double)y[i].im / cs[i]};
+}
+
+// h[j] = v_j^H w for j < k (V column-major, leading dimension n), one CTA per
+// j, a fixed reduction order
+__global__ void __launch_bounds__(256) k_gs_dots(const cplx *V, int n, const cplx *w, cplx *h) {
+    __shared__ double sr[8], si[8];
+    const cplx *v = V + (size_t)blockIdx.x * n;
+    double re = 0.0, im = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) {
+        const cplx a = v[i], b = w[i];
+        re = fma(a.re, b.re, re);
+        re = fma(a.im, b.im, re);
+        im = fma(a.re, b.im, im);
+        im = fma(-a.im, b.re, im);
+    }
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if ((threadIdx.x & 31) == 0) {
+        sr[threadIdx.x >> 5] = re;
+        si[threadIdx.x >> 5] = im;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            a += sr[q];
+            b += si[q];
+        }
+        h[blockIdx.x] = cplx{a, b};
+    }
+}
+
+// w -= sum_{j<k} h_j v_j
+__global__ void k_gs_update(const cplx *V, int n, int k, const cplx *h, cplx *w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cplx s = w[i];
+    for (int j = 0; j < k; ++j) {
+        const cplx hj = h[j], v = V[(size_t)j * n + i];
+        s.re -= hj.re * v.re - hj.im * v.im;
+        s.im -= hj.re * v.im + hj.im * v.re;
+    }
+    w[i] = s;
+}
+
+// out = ||w||_2, one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) k_norm2(const cplx *w, int n, double *out) {
+    __shared__ double part[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 1024) s = fma(w[i].re, w[i].re, fma(w[i].im, w[i].im, s));
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 32; ++q) t += part[q];
+        *out = sqrt(t);
+    }
+}
+
+// v = w * scale
+__global__ void k_cscale(const cplx *w, int n, double scale, cplx *v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = cplx{w[i].re * scale, w[i].im * scale};
+}
+
+// x += sum_{j<k} y_j z_j
+__global__ void k_gmres_update(const cplx *V, int n, int k, const cplx *y, cplx *x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cplx s = x[i];
+    for (int j = 0; j < k; ++j) {
+        const cplx a = y[j], v = V[(size_t)j * n + i];
+        s.re += a.re * v.re - a.im * v.im;
+        s.im += a.re * v.im + a.im * v.re;
+    }
+    x[i] = s;
+}
+
 struct MixedTiming {
     double ms_prepare = 0, ms_factor = 0, ms_refine = 0;
-    int iterations = 0, split_terms = 3;
+    int iterations = 0, split_terms = 3, gmres_iterations = 0;
 };
 static thread_local MixedTiming g_mixed_timing;  // last mixed solve of this host thread
 
@@ -4283,6 +4404,137 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         if (graph) cudaGraphDestroy(graph);
         return out;
     };
+    // FGMRES-IR with the BF16x6 factor, the last rung: per right-hand side
+    // from x = 0, outer FP64 residuals r = b - Z x and inner flexible GMRES
+    // on D_r^-1 Z d = D_r^-1 r (the equilibrated rows), preconditioned by the
+    // FP32 factor in FP32 (z_k = D_c^-1 U^-1 L^-1 P v_k, kept for the update
+    // d = Z_k y since the preconditioner is not exactly linear); classical
+    // Gram-Schmidt twice, Givens rotations on the host; 1e-6 relative
+    // residual or 40 steps per inner solve.  Stops at the gate, after 10
+    // outer steps, or when the backward error no longer halves.  0 at the
+    // gate, 1 when not, -1 on errors.
+    int gmres_total = 0;
+    auto gmres_ir = [&]() -> int {
+        constexpr int m = 40;
+        DBuf<cplx> V((size_t)(m + 1) * n), Zk((size_t)m * n), w(n), hd(2 * (m + 1)), yd(m);
+        DBuf<double> nrm(1);
+        if (!V.p || !Zk.p || !w.p || !hd.p || !yd.p || !nrm.p) return -1;
+        const unsigned gn = (unsigned)((n + 255) / 256), gw = (unsigned)(((size_t)n * 32 + 255) / 256);
+        // z = D_c^-1 U^-1 L^-1 P v in FP32, returned in FP64
+        auto precondition = [&](const cplx *v, cplx *z) -> bool {
+            PEEC_LAUNCH(k_perm_f32, gn, 256, 0, v, perm.p, n, y.p);
+            WaveArgs<cplxf> W{};
+            W.lu = a;
+            W.dinv = wdinv.p;
+            W.n = n;
+            W.nrhs = 1;
+            W.b = y.p;
+            W.x = y.p;
+            W.flags = wflags.p;
+            W.error = werr.p;
+            W.subst = 1;
+            if (!wave_solve(W)) return false;
+            PEEC_LAUNCH(k_mix_out, gn, 256, 0, y.p, cs.p, n, z);
+            return true;
+        };
+        auto host_sync = [&](const char *what) -> bool {
+            int hw = 0;
+            cudaMemcpyAsync(&hw, werr.p, sizeof(hw), cudaMemcpyDeviceToHost, stream());
+            if (!launch_ok(what) || !sync(what)) return false;
+            if (hw) set_error("triangular solve: a wait for an earlier row block timed out");
+            return hw == 0;
+        };
+        double eta_max = 0.0;
+        for (int q = 0; q < nrhs; ++q) {
+            cplx *xq = x + (size_t)q * n;
+            const cplx *bq = b + (size_t)q * n;
+            cudaMemsetAsync(xq, 0, (size_t)n * sizeof(cplx), stream());
+            double eta_q = INFINITY, prev = INFINITY;
+            for (int outer = 0; outer < 10; ++outer) {
+                cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+                PEEC_LAUNCH(k_abs_x, gn, 256, 0, xq, (size_t)n, absx.p);
+                PEEC_LAUNCH(k_residual, gw, 256, 0, Z, absZ.p, xq, absx.p, bq, n, 1, r.p, be.p);
+                PEEC_LAUNCH(k_scale_rows, gn, 256, 0, r.p, rs.p, n, V.p);
+                PEEC_LAUNCH(k_norm2, 1, 1024, 0, V.p, n, nrm.p);
+                unsigned long long hb = 0;
+                double beta = 0.0;
+                cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
+                cudaMemcpyAsync(&beta, nrm.p, sizeof(beta), cudaMemcpyDeviceToHost, stream());
+                if (!host_sync("GMRES-IR residual")) return -1;
+                memcpy(&eta_q, &hb, sizeof(eta_q));
+                if (eta_q <= tol || !isfinite(eta_q) || eta_q > 0.5 * prev) break;
+                prev = eta_q;
+                if (!(beta > 0.0) || !isfinite(beta)) break;
+                PEEC_LAUNCH(k_cscale, gn, 256, 0, V.p, n, 1.0 / beta, V.p);
+                using zc = std::complex<double>;
+                std::vector<zc> H((size_t)(m + 1) * m), g(m + 1, zc(0.0)), sn(m);
+                std::vector<double> c(m);
+                std::vector<cplx> hh(2 * (m + 1));
+                g[0] = beta;
+                int kk = 0;
+                for (int k = 0; k < m; ++k) {
+                    cplx *zk = Zk.p + (size_t)k * n;
+                    if (!precondition(V.p + (size_t)k * n, zk)) return -1;
+                    PEEC_LAUNCH(k_zmv_scaled, gw, 256, 0, Z, zk, rs.p, n, w.p);
+                    for (int pass = 0; pass < 2; ++pass) {
+                        PEEC_LAUNCH(k_gs_dots, (unsigned)(k + 1), 256, 0, V.p, n, w.p, hd.p + pass * (m + 1));
+                        PEEC_LAUNCH(k_gs_update, gn, 256, 0, V.p, n, k + 1, hd.p + pass * (m + 1), w.p);
+                    }
+                    PEEC_LAUNCH(k_norm2, 1, 1024, 0, w.p, n, nrm.p);
+                    double hn = 0.0;
+                    cudaMemcpyAsync(hh.data(), hd.p, hh.size() * sizeof(cplx), cudaMemcpyDeviceToHost, stream());
+                    cudaMemcpyAsync(&hn, nrm.p, sizeof(hn), cudaMemcpyDeviceToHost, stream());
+                    if (!host_sync("GMRES-IR step")) return -1;
+                    ++gmres_total;
+                    zc *col = &H[(size_t)k * (m + 1)];
+                    for (int j = 0; j <= k; ++j)
+                        col[j] = zc(hh[j].re + hh[m + 1 + j].re, hh[j].im + hh[m + 1 + j].im);
+                    if (hn > 0.0 && isfinite(hn))
+                        PEEC_LAUNCH(k_cscale, gn, 256, 0, w.p, n, 1.0 / hn, V.p + (size_t)(k + 1) * n);
+                    // earlier rotations, then a new one zeroing the subdiagonal hn
+                    for (int j = 0; j < k; ++j) {
+                        const zc u = c[j] * col[j] + sn[j] * col[j + 1];
+                        col[j + 1] = -std::conj(sn[j]) * col[j] + c[j] * col[j + 1];
+                        col[j] = u;
+                    }
+                    const double aa = std::abs(col[k]), rr = std::hypot(aa, hn);
+                    if (aa == 0.0) {
+                        c[k] = 0.0;
+                        sn[k] = 1.0;
+                        col[k] = hn;
+                    } else {
+                        const zc ph = col[k] / aa;
+                        c[k] = aa / rr;
+                        sn[k] = ph * (hn / rr);
+                        col[k] = ph * rr;
+                    }
+                    g[k + 1] = -std::conj(sn[k]) * g[k];
+                    g[k] = c[k] * g[k];
+                    kk = k + 1;
+                    if (!(hn > 0.0) || !isfinite(hn) || std::abs(g[k + 1]) <= 1e-6 * beta) break;
+                }
+                // y from the triangular H, x += Z_k y
+                std::vector<zc> yv(kk);
+                for (int i = kk - 1; i >= 0; --i) {
+                    zc sum = g[i];
+                    for (int j = i + 1; j < kk; ++j) sum -= H[(size_t)j * (m + 1) + i] * yv[j];
+                    yv[i] = sum / H[(size_t)i * (m + 1) + i];
+                }
+                std::vector<cplx> yh(kk);
+                for (int i = 0; i < kk; ++i) yh[i] = cplx{yv[i].real(), yv[i].imag()};
+                cudaMemcpyAsync(yd.p, yh.data(), kk * sizeof(cplx), cudaMemcpyHostToDevice, stream());
+                PEEC_LAUNCH(k_gmres_update, gn, 256, 0, Zk.p, n, kk, yd.p, xq);
+                if (!host_sync("GMRES-IR update")) return -1;
+            }
+            if (!(eta_q <= tol)) {
+                eta = eta_q;
+                return 1;
+            }
+            eta_max = std::max(eta_max, eta_q);
+        }
+        eta = eta_max;
+        return 0;
+    };
     float t01 = -1.0f, ms_factor = 0.0f, ms_refine = 0.0f;
     int outcome;
     for (;;) {
@@ -4309,8 +4561,20 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
         PEEC_LAUNCH(k_eq2_to_float, 152 * 16, 256, 0, Z, n, er.p, ec.p, f.p, (float *)nullptr);
     }
+    if (outcome == 1 && T == 6) {
+        // still stalled with BF16x6: GMRES-IR with the same factor
+        cudaEventRecord(ev[2], stream());
+        outcome = gmres_ir();
+        cudaEventRecord(ev[3], stream());
+        cudaEventSynchronize(ev[3]);
+        float t23 = 0.0f;
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        ms_refine += t23;
+        total_it += gmres_total;
+    }
     for (auto &e : ev) cudaEventDestroy(e);
     if (outcome == -1) return -1;
+    g_mixed_timing.gmres_iterations = gmres_total;
     g_mixed_timing.ms_prepare = t01;
     g_mixed_timing.ms_factor = ms_factor;
     g_mixed_timing.ms_refine = ms_refine;
@@ -4340,6 +4604,8 @@ extern "C" int peec_gb300_round_to_f32_device(const double *d_x, float *d_y, siz
 }
 
 extern "C" int peec_gb300_mixed_split_terms(void) { return peec::g_mixed_timing.split_terms; }
+
+extern "C" int peec_gb300_mixed_gmres_iterations(void) { return peec::g_mixed_timing.gmres_iterations; }
 
 extern "C" int peec_gb300_mixed_timing(double *ms_prepare, double *ms_factor, double *ms_refine) {
     if (ms_prepare) *ms_prepare = peec::g_mixed_timing.ms_prepare;
