@@ -364,6 +364,41 @@ def rcs_leg(lib, ds, x_mixed):
             "edge_current_rel_err": cur_err}
 
 
+def incidence_leg(lib, ds, reps=5):
+    """The incidence products (incidence.h) on the resident P and edge list:
+    P A^T (Nv x Ne), A P A^T (Ne x Ne), A S (Ne x Nv).  Gathers from P, so
+    HBM-bound: algorithmic bytes = the output written + P read once.  Each
+    call is timed with events around the device-resident API (its final
+    synchronisation included), best of `reps`."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm = json.load(f).get("hbm_gbs", 6800.0)
+    except (OSError, ValueError):
+        hbm = 6800.0
+    ne, nv = ds.ne, ds.nv
+    out = lib.peec_gb300_device_alloc(max(ne * ne, ne * nv) * 8)
+    bad = C.c_longlong()
+    calls = {"P_AT": (lambda: lib.peec_gb300_pat_device(ds.dP, ds.dedges, nv, ne, out, C.byref(bad)), nv * ne),
+             "A_P_AT": (lambda: lib.peec_gb300_apat_device(ds.dP, ds.dedges, nv, ne, out), ne * ne),
+             "A_S": (lambda: lib.peec_gb300_as_device(ds.dP, ds.dedges, nv, ne, out), ne * nv)}
+    res = {}
+    for name, (call, count) in calls.items():
+        best = float("inf")
+        for _ in range(reps):
+            e0 = lib.peec_gb300_event_record()
+            assert call() == 0, name
+            e1 = lib.peec_gb300_event_record()
+            best = min(best, lib.peec_gb300_event_elapsed_ms(e0, e1))
+            lib.peec_gb300_event_destroy(e0)
+            lib.peec_gb300_event_destroy(e1)
+        nbytes = 8.0 * (count + nv * nv)
+        res[name] = {"ms": best, "output_entries": count, "algorithmic_bytes": nbytes,
+                     "GB_s": nbytes / best / 1e6, "frac_of_hbm": nbytes / best / 1e6 / hbm}
+    lib.peec_gb300_device_free(out)
+    res["note"] = "time of the device-resident call including its final synchronisation; peak = measured HBM copy"
+    return res
+
+
 def retarded_leg(lib, ds):
     """The same box and frequency with the retarded kernel exp(-jkR)/R on Lp
     and P (complex assembly, complex MNA fill, mixed solve to the 1e-10
@@ -811,6 +846,7 @@ def main():
     if x_mixed:
         rcs = rcs_leg(lib, ds, x_mixed)
         lib.peec_gb300_device_free(x_mixed)
+    incidence = incidence_leg(lib, ds)
     p64, p32 = C.c_double(), C.c_double()
     lib.peec_gb300_pipe_peaks(C.byref(p64), C.byref(p32))
     transient = transient_leg(lib, ds, args.transient_steps) if args.transient_steps > 0 else None
@@ -881,7 +917,7 @@ def main():
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
                 "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "batched": batched, "transient": transient, "retarded": retarded,
-                "rcs": rcs,
+                "rcs": rcs, "incidence": incidence,
                 "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
                                       "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
                 "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}

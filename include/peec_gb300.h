@@ -167,6 +167,25 @@ int peec_gb300_rcs_radiation_device(const Mesh *mesh, const DualMesh *dual, cons
                                     const double *directions, size_t n_dir, int order,
                                     Complex *radiation);
 
+/* ---- incidence products (incidence.h) on device-resident P ----
+ * d_P: nv x nv FP64 row-major; d_edges: [2 ne] (a, b) node pairs, current
+ * a -> b.  Outputs are device arrays, row-major, bit-identical to the
+ * reference's expressions.
+ * P A^T (nv x ne): d_out[j][e] = P[j][b] - P[j][a], NaN for an edge with a
+ * node out of range; returns 0, 1 when an entry is not finite (*first_bad =
+ * its row-major index, else -1; may be NULL), -1 on invalid arguments. */
+int peec_gb300_pat_device(const double *d_P, const int *d_edges, size_t nv, size_t ne, double *d_out,
+                          long long *first_bad);
+/* A P A^T (ne x ne): d_K[e][f] = P[a][c] - P[a][d] - P[b][c] + P[b][d] for
+ * e <= f, mirrored.  Returns 0, or -1 on invalid arguments or a node index
+ * out of range. */
+int peec_gb300_apat_device(const double *d_P, const int *d_edges, size_t nv, size_t ne, double *d_K);
+/* A S (ne x nv): d_AS[e][a] = (P[b][a] - P[a'][a]) / P[a][a] for edge
+ * e = a' -> b.  Returns 0, 1 when a P[a][a] is not finite or <= 0 (those
+ * entries NaN), -1 on invalid arguments or edges (a node out of range or
+ * a' == b). */
+int peec_gb300_as_device(const double *d_P, const int *d_edges, size_t nv, size_t ne, double *d_AS);
+
 /* ---- mixed precision complex solve ----
  * The FP32 rounding used by the mixed-precision solve's equilibration:
  * d_y[i] = d_x[i] * 2^-shift rounded to the nearest FP32 (ties to even) by

@@ -71,6 +71,9 @@ class Oracle:
              [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, C.c_double,
               C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_size_t, D, D,
               P(C.c_int), C.c_size_t, P(C.c_int), C.c_size_t, D]),
+            ("oracle_incidence_apat", None, [D, P(C.c_int), C.c_size_t, C.c_size_t, D]),
+            ("oracle_incidence_pat", C.c_int, [D, P(C.c_int), C.c_size_t, C.c_size_t, D, P(C.c_longlong)]),
+            ("oracle_incidence_as", C.c_int, [D, P(C.c_int), C.c_size_t, C.c_size_t, D]),
         ]
         for name, res, args in sig:
             f = getattr(lib, name)
@@ -153,6 +156,27 @@ class Oracle:
                                              lu.shape[0], b.ctypes.data_as(D), x.ctypes.data_as(D))
         return s, x
 
+    def incidence_apat(self, P_, edges):
+        Pc, e, K = _incidence_oracle(P_, edges, (len(edges), len(edges)))
+        self.lib.oracle_incidence_apat(Pc.ctypes.data_as(D), e.ctypes.data_as(P(C.c_int)), Pc.shape[0], len(e),
+                                       K.ctypes.data_as(D))
+        return K
+
+    def incidence_pat(self, P_, edges):
+        """(status, PAT, first non-finite row-major index or -1)"""
+        Pc, e, out = _incidence_oracle(P_, edges, (P_.shape[0], len(edges)))
+        bad = C.c_longlong()
+        s = self.lib.oracle_incidence_pat(Pc.ctypes.data_as(D), e.ctypes.data_as(P(C.c_int)), Pc.shape[0], len(e),
+                                          out.ctypes.data_as(D), C.byref(bad))
+        return s, out, bad.value
+
+    def incidence_as(self, P_, edges):
+        """(status, AS)"""
+        Pc, e, out = _incidence_oracle(P_, edges, (len(edges), P_.shape[0]))
+        s = self.lib.oracle_incidence_as(Pc.ctypes.data_as(D), e.ctypes.data_as(P(C.c_int)), Pc.shape[0], len(e),
+                                         out.ctypes.data_as(D))
+        return s, out
+
     def retarded(self, m, kind, wave_number, orders=(4, 10, 12, 8), near_factor=0.5, tol=1e-10,
                  threads=None):
         """kind 0: Lp, 1: P with the exp(-jkR)/R kernel (complex n x n)."""
@@ -225,6 +249,42 @@ def _rcs(fn, m, current, wave_number, directions, call):
 class RcsOptions(C.Structure):
     """rcs.h RcsOptions (integration 1 = dual-patch quadrature)."""
     _fields_ = [("integration", C.c_int), ("surface_order", C.c_int), ("parallel_threads", C.c_int)]
+
+
+def _incidence_oracle(P_, edges, shape):
+    Pc = np.ascontiguousarray(P_, dtype=np.float64)
+    e = np.ascontiguousarray(np.asarray(edges).reshape(-1, 2), dtype=np.int32)
+    return Pc, e, np.zeros(shape)
+
+
+def incidence_products(lib, mesh, P_, threads=1):
+    """Call the incidence.h functions of a library with the drop-in ABI (the
+    reference's own, or the GB300 one) on a Mesh struct and a dense P:
+    {"A", "APAT", "PAT", "AS"} as numpy arrays, or the int status of the
+    first call that failed under that key."""
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    nv = P_.shape[0]
+    Pc = np.ascontiguousarray(P_, dtype=np.float64)
+    Pm = abi.PotentialMatrix(nv, Pc.ctypes.data_as(D))
+    out = {}
+    A = abi.IncidenceMatrix()
+    s = lib.incidence_build(C.byref(mesh), C.byref(A))
+    if s != 0:
+        return {"A": s}
+    out["A"] = np.ctypeslib.as_array(A.data, shape=(A.rows, A.cols)).copy()
+    for name, call in (("APAT", lambda M: lib.incidence_build_APAT(C.byref(mesh), C.byref(Pm), C.byref(M), threads)),
+                       ("PAT", lambda M: lib.incidence_build_PAT(C.byref(mesh), C.byref(Pm), C.byref(M), threads)),
+                       ("AS", lambda M: lib.incidence_build_AS(C.byref(A), C.byref(Pm), C.byref(M), threads))):
+        M = abi.Matrix()
+        s = call(M)
+        if s != 0:
+            out[name] = s
+            continue
+        out[name] = np.ctypeslib.as_array(M.data, shape=(M.rows, M.cols)).copy()
+        libc.free(C.cast(M.data, C.c_void_p))
+    libc.free(C.cast(A.data, C.c_void_p))
+    return out
 
 
 def reference_available():

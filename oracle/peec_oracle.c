@@ -1083,3 +1083,59 @@ int oracle_rcs_radiation_vector(const Mesh *mesh, const DualMesh *dual, const Co
     }
     return 0;
 }
+
+/* ---- incidence products (incidence.c:242-741), test oracle ---- */
+
+/* incidence.c:298-330: K[e][f] = P[a][c] - P[a][d] - P[b][c] + P[b][d] for
+ * e <= f, written to both triangles */
+void oracle_incidence_apat(const double *P, const int *edges, size_t nv, size_t ne, double *K) {
+    for (size_t e = 0; e < ne; ++e) {
+        const size_t a = (size_t)edges[2 * e], b = (size_t)edges[2 * e + 1];
+        for (size_t f = e; f < ne; ++f) {
+            const size_t c = (size_t)edges[2 * f], d = (size_t)edges[2 * f + 1];
+            const double v = P[a * nv + c] - P[a * nv + d] - P[b * nv + c] + P[b * nv + d];
+            K[e * ne + f] = v;
+            K[f * ne + e] = v;
+        }
+    }
+}
+
+/* incidence.c:475-589: PAT[j][e] = P[j][b] - P[j][a], NaN for an edge out of
+ * range; the first non-finite entry in row-major order fails the call */
+int oracle_incidence_pat(const double *P, const int *edges, size_t nv, size_t ne, double *out,
+                         long long *first_bad) {
+    for (size_t j = 0; j < nv; ++j)
+        for (size_t e = 0; e < ne; ++e) {
+            const int a = edges[2 * e], b = edges[2 * e + 1];
+            out[j * ne + e] = (a < 0 || b < 0 || (size_t)a >= nv || (size_t)b >= nv)
+                                  ? NAN
+                                  : P[j * nv + (size_t)b] - P[j * nv + (size_t)a];
+        }
+    *first_bad = -1;
+    for (size_t t = 0; t < nv * ne; ++t)
+        if (!isfinite(out[t])) {
+            *first_bad = (long long)t;
+            return -1;
+        }
+    return 0;
+}
+
+/* incidence.c:641-729 with node_minus / node_plus = the edge's (a, b):
+ * AS[e][k] = (P[b][k] - P[a][k]) / P[k][k]; NaN and failure where P[k][k] is
+ * not finite or <= 0 */
+int oracle_incidence_as(const double *P, const int *edges, size_t nv, size_t ne, double *AS) {
+    int status = 0;
+    for (size_t e = 0; e < ne; ++e) {
+        const size_t m = (size_t)edges[2 * e], n = (size_t)edges[2 * e + 1];
+        for (size_t k = 0; k < nv; ++k) {
+            const double pkk = P[k * nv + k];
+            if (!isfinite(pkk) || pkk <= 0.0) {
+                AS[e * nv + k] = NAN;
+                status = -1;
+                continue;
+            }
+            AS[e * nv + k] = (P[n * nv + k] - P[m * nv + k]) / pkk;
+        }
+    }
+    return status;
+}

@@ -128,4 +128,14 @@ int oracle_rcs_radiation_vector(const Mesh *mesh, const DualMesh *dual, const Co
 }
 #endif
 
+/* Incidence products from an edge list (a, b), current a -> b
+ * (incidence.c:242-415, 417-591, 593-741): K = A P A^T (ne x ne, e <= f
+ * evaluated, mirrored); PAT = P A^T (nv x ne, NaN for an edge out of range;
+ * returns -1 with *first_bad = the row-major index of the first non-finite
+ * entry); AS = A S (ne x nv; returns -1 if a P[a][a] is not finite or <= 0). */
+void oracle_incidence_apat(const double *P, const int *edges, size_t nv, size_t ne, double *K);
+int oracle_incidence_pat(const double *P, const int *edges, size_t nv, size_t ne, double *out,
+                         long long *first_bad);
+int oracle_incidence_as(const double *P, const int *edges, size_t nv, size_t ne, double *AS);
+
 #endif

@@ -74,6 +74,14 @@ class PotentialMatrix(C.Structure):
     _fields_ = [("n", C.c_size_t), ("data", c_double_p)]
 
 
+class Matrix(C.Structure):
+    _fields_ = [("rows", C.c_size_t), ("cols", C.c_size_t), ("data", c_double_p)]
+
+
+class IncidenceMatrix(C.Structure):
+    _fields_ = [("rows", C.c_size_t), ("cols", C.c_size_t), ("data", c_double_p)]
+
+
 class LUOptions(C.Structure):
     _fields_ = [("parallel_threads", C.c_int), ("pivot_tolerance", C.c_double),
                 ("parallel_threshold", C.c_size_t)]
@@ -102,6 +110,15 @@ P = C.POINTER
 # Every symbol the drop-in headers declare, with its ctypes signature.
 # (name, restype, argtypes)
 DROP_IN_SYMBOLS = [
+    # incidence.h
+    ("incidence_init", None, [P(IncidenceMatrix)]),
+    ("incidence_free", None, [P(IncidenceMatrix)]),
+    ("incidence_build", C.c_int, [P(Mesh), P(IncidenceMatrix)]),
+    ("incidence_check_row_sum", C.c_double, [P(IncidenceMatrix)]),
+    ("incidence_print_info", None, [P(IncidenceMatrix)]),
+    ("incidence_build_APAT", C.c_int, [P(Mesh), P(PotentialMatrix), P(Matrix), C.c_int]),
+    ("incidence_build_PAT", C.c_int, [P(Mesh), P(PotentialMatrix), P(Matrix), C.c_int]),
+    ("incidence_build_AS", C.c_int, [P(IncidenceMatrix), P(PotentialMatrix), P(Matrix), C.c_int]),
     # quadrature.h
     ("gauss_legendre_rule", C.c_int, [C.c_int, c_double_p, c_double_p]),
     ("triangle_area", C.c_double, [c_double_p, c_double_p, c_double_p]),
@@ -242,6 +259,10 @@ EXT_SYMBOLS = [
       C.c_size_t, C.c_double, C.c_int, c_double_p, c_int_p]),
     ("peec_gb300_mixed_timing", C.c_int, [c_double_p, c_double_p, c_double_p]),
     ("peec_gb300_mixed_split_terms", C.c_int, []),
+    ("peec_gb300_pat_device", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.POINTER(C.c_longlong)]),
+    ("peec_gb300_apat_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p]),
+    ("peec_gb300_as_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p]),
     ("peec_gb300_mixed_gmres_iterations", C.c_int, []),
     ("peec_gb300_harmonic_build_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_double,

@@ -301,7 +301,27 @@ def rcs_case(R, name):
     print("wrote rcs_" + name)
 
 
+# incidence.c:34-741: A, A P A^T, P A^T and A S of the fixture's mesh and
+# its reference P, from the reference's own functions.
+def incidence_case(R, name):
+    from oracle import incidence_products
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    f = np.load(os.path.join(HERE, name + ".npz"))
+    with SynthMesh.from_arrays(f["xyz"], f["quads"]) as m:
+        assert np.array_equal(m.edges(), f["edges"])
+        out = incidence_products(R.lib, m.mesh, f["P"])
+    for k, v in out.items():
+        assert not isinstance(v, int), (k, v)
+    np.savez_compressed(os.path.join(HERE, "incidence_" + name + ".npz"), **out)
+    print("wrote incidence_" + name)
+
+
 def main():
+    if sys.argv[1:] == ["incidence"]:
+        R = Reference()
+        incidence_case(R, "plate4")
+        incidence_case(R, "box421")
+        return
     R = Reference()
     quadrature_cases(R)
     lu_cases(R)
@@ -313,6 +333,8 @@ def main():
     transient_case(R, "box421", 200, 0, 5)
     rcs_case(R, "plate4")
     rcs_case(R, "box421")
+    incidence_case(R, "plate4")
+    incidence_case(R, "box421")
     plate_msh = os.path.join(REF_MESH_DIR, "plate.msh")
     if os.path.exists(plate_msh):
         gmsh_case(R, plate_msh, "plate_msh")

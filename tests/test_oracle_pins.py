@@ -324,3 +324,55 @@ def test_rcs_radiation_invalid_inputs(oracle):
         cur = np.ones(m.n_edges, dtype=np.complex128)
         assert oracle.rcs_radiation(m, cur, 0.0, [[0, 0, 1]])[0] == -1
         assert oracle.rcs_radiation(m, cur, 1.0, [[0, 0, 1]], order=7)[0] == -1
+
+
+# ---------------------------------------------------------------------
+# incidence products (incidence.c:242-741) against the reference's outputs
+# ---------------------------------------------------------------------
+@pytest.mark.parametrize("name", ["plate4", "box421"])
+def test_oracle_incidence_matches_reference_fixtures(oracle, name):
+    f, g = golden(name), golden("incidence_" + name)
+    P_, edges = f["P"], f["edges"]
+    ne, nv = edges.shape[0], P_.shape[0]
+    A = np.zeros((ne, nv))
+    A[np.arange(ne), edges[:, 0]] = -1.0
+    A[np.arange(ne), edges[:, 1]] = 1.0
+    assert np.array_equal(A, g["A"])
+    assert np.array_equal(oracle.incidence_apat(P_, edges), g["APAT"])
+    s, pat, bad = oracle.incidence_pat(P_, edges)
+    assert s == 0 and bad == -1 and np.array_equal(pat, g["PAT"])
+    s, as_ = oracle.incidence_as(P_, edges)
+    assert s == 0 and np.array_equal(as_, g["AS"])
+
+
+def test_oracle_incidence_failures():
+    from oracle import Oracle
+    o = Oracle()
+    P_ = np.array([[2.0, 1.0, 0.5], [1.0, 3.0, 0.25], [0.5, 0.25, 4.0]])
+    edges = np.array([[0, 1], [1, 2]], dtype=np.int32)
+    bad_edges = np.array([[0, 1], [1, 7]], dtype=np.int32)
+    s, pat, bad = o.incidence_pat(P_, bad_edges)
+    assert s == -1 and bad == 1 and np.isnan(pat[:, 1]).all()
+    Pn = P_.copy()
+    Pn[2, 2] = -1.0
+    s, as_ = o.incidence_as(Pn, edges)
+    assert s == -1 and np.isnan(as_[:, 2]).all()
+
+
+@pytest.mark.skipif(not __import__("oracle").reference_available(), reason="reference library not built here")
+def test_incidence_oracle_against_reference_library(oracle):
+    """Larger case straight against the reference's incidence.c (a symmetric
+    P with a positive diagonal on a 6 x 5 plate's edge list)."""
+    from oracle import Reference, incidence_products
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    R = Reference()
+    rng = np.random.default_rng(3)
+    with SynthMesh.plate(0.6, 0.5, 6, 5) as m:
+        nv = m.n_nodes
+        X = rng.standard_normal((nv, nv))
+        P_ = X @ X.T + nv * np.eye(nv)
+        ref = incidence_products(R.lib, m.mesh, P_, threads=4)
+        edges = m.edges()
+    assert np.array_equal(oracle.incidence_apat(P_, edges), ref["APAT"])
+    assert np.array_equal(oracle.incidence_pat(P_, edges)[1], ref["PAT"])
+    assert np.array_equal(oracle.incidence_as(P_, edges)[1], ref["AS"])
