@@ -82,6 +82,10 @@ class IncidenceMatrix(C.Structure):
     _fields_ = [("rows", C.c_size_t), ("cols", C.c_size_t), ("data", c_double_p)]
 
 
+class ResistanceMatrix(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("diagonal", c_double_p)]
+
+
 class LUOptions(C.Structure):
     _fields_ = [("parallel_threads", C.c_int), ("pivot_tolerance", C.c_double),
                 ("parallel_threshold", C.c_size_t)]
@@ -119,6 +123,12 @@ DROP_IN_SYMBOLS = [
     ("incidence_build_APAT", C.c_int, [P(Mesh), P(PotentialMatrix), P(Matrix), C.c_int]),
     ("incidence_build_PAT", C.c_int, [P(Mesh), P(PotentialMatrix), P(Matrix), C.c_int]),
     ("incidence_build_AS", C.c_int, [P(IncidenceMatrix), P(PotentialMatrix), P(Matrix), C.c_int]),
+    # matrix_export.h
+    ("matrix_export_dense_mtx", C.c_int, [C.c_char_p, c_double_p, C.c_size_t, C.c_size_t]),
+    ("matrix_export_incidence_mtx", C.c_int, [C.c_char_p, P(Mesh)]),
+    ("matrix_export_resistance_mtx", C.c_int, [C.c_char_p, P(ResistanceMatrix)]),
+    ("matrix_export_peec_set", C.c_int,
+     [C.c_char_p, P(Mesh), P(InductanceMatrix), P(PotentialMatrix), P(Matrix), P(ResistanceMatrix)]),
     # quadrature.h
     ("gauss_legendre_rule", C.c_int, [C.c_int, c_double_p, c_double_p]),
     ("triangle_area", C.c_double, [c_double_p, c_double_p, c_double_p]),

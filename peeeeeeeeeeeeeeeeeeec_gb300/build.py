@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, "include")
 ORACLE = os.path.join(REPO, "oracle")
 REFERENCE = os.environ.get("PEEC_REFERENCE_DIR", "/root/reference")
 
-CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu"]
+CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu", "matrix_export.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17", "--fmad=false",

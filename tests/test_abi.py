@@ -8,7 +8,7 @@ import subprocess
 from peeeeeeeeeeeeeeeeeeec_gb300 import abi
 
 INCLUDE = os.path.join(abi.REPO_DIR, "include")
-DROP_IN = ["quadrature.h", "inductance.h", "potential.h", "lu.h", "complex_lu.h", "incidence.h", "peec_gb300.h"]
+DROP_IN = ["quadrature.h", "inductance.h", "potential.h", "lu.h", "complex_lu.h", "incidence.h", "matrix_export.h", "peec_gb300.h"]
 
 
 def declared_functions(header):
