@@ -583,13 +583,18 @@ def batched_leg(lib, n_meshes, n_freqs, workers):
     """Many meshes x many frequencies (config-4 shape, scaled): seeded boxes /
     plates of 300-4000 unknowns, each at n_freqs log-spaced frequencies from
     1 kHz to 100 MHz with 4 plane waves, all submitted at once to one server
-    (its Lp / P cache warmed first), mixed solve then plain FP64 LU.
+    (its Lp / P cache warmed first), mixed solve then plain FP64 LU.  The
+    sweep is submitted largest system first, lowest frequency first within a
+    mesh (longest-processing-time order, the same for both arms), so that the
+    costliest solves start early and overlap the rest.
     Throughput = systems reaching the 1e-10 gate / makespan."""
     from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
     from peeeeeeeeeeeeeeeeeeec_gb300.server import Server
     pool = W.serving_meshes(seed=11, count=n_meshes, lo=300, hi=4000)
     systems = W.batch_systems(seed=13, n_meshes=n_meshes, n_freqs=n_freqs)
-    out = {"systems": "%d meshes x %d frequencies (1 kHz - 100 MHz, log) x 4 plane waves" % (n_meshes, n_freqs),
+    size = [m.n_edges + m.n_nodes for m, _ in pool]
+    systems.sort(key=lambda t: (-size[t[0]], t[1]))
+    out = {"systems": "%d meshes x %d frequencies (1 kHz - 100 MHz, log) x 4 plane waves, largest system first" % (n_meshes, n_freqs),
            "unknowns": [m.n_edges + m.n_nodes for m, _ in pool], "workers": workers}
     with Server(150 << 30, workers) as srv:
         for t in [srv.submit(m, i, 30e6, [[0.0, 0.0, -1.0]], [[1.0, 0.0, 0.0]]) for i, (m, _) in enumerate(pool)]:
