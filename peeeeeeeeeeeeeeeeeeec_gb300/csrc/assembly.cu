@@ -1192,7 +1192,7 @@ __global__ void k_round_resolve(int nrec, const int *failed, const RoundSlot *ta
     }
 }
 
-// representatives integrated in round 1 take their own value
+// representatives integrated in the first reuse pass take their own value
 __global__ void k_round_self(int nrec, const int *rep_pos, int *src) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < nrec && rep_pos[r] >= 0) src[r] = r;
@@ -1844,7 +1844,7 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
                 !fcode.alloc(nrec) || !failed.alloc(nrec) || !slot_of2.alloc(nrec) || !isnew.alloc(nrec) ||
                 !off2.alloc(nrec + 1) || !key2.alloc(nrec) || !tab2.alloc(cap))
                 return -1;
-            // round 1: the representatives just integrated decide for themselves
+            // first reuse pass: the representatives just integrated decide for themselves
             PEEC_LAUNCH(k_fill_int, g, 256, 0, src.p, (long long)nrec, 1, -1);
             PEEC_LAUNCH(k_fill_int, g, 256, 0, rpos.p, (long long)nrec, 1, -1);
             cudaMemsetAsync(evalf.p, 0, (size_t)nrec * sizeof(int), stream());
