@@ -1362,9 +1362,11 @@ __device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *
                 f2 dx = df_sub(ax, f2{B.xh, B.xl});
                 f2 dy = df_sub(ay, f2{B.yh, B.yl});
                 f2 dz = df_sub(az, f2{B.zh, B.zl});
+                // no R <= 0 test: FAR patches of nonzero size never share a
+                // point (the caller skips zero-size patches, whose weights are
+                // zero), and a NaN reaches the entry's sum, which the epilogue
+                // checks
                 f2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-                if (r2.h <= 0.0f) continue;  // the reference skips R <= 0
-                if (!(r2.h == r2.h) || !(B.wh == B.wh)) bad = true;
                 f2 t = df_mul(f2{B.wh, B.wl}, df_rsqrt(r2));
                 if (u == 0)
                     s0 = df_add(s0, t);
@@ -1372,7 +1374,6 @@ __device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *
                     s1 = df_add(s1, t);
             }
         }
-        if (!(A.wh == A.wh)) bad = true;
         acc = df_add(acc, df_mul(f2{A.wh, A.wl}, df_add(s0, s1)));
     }
 }
@@ -1507,8 +1508,9 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                         }
                         if (!near) {
                             if (T.far_df == 1) {
-                                far_pair_df_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts, facc,
-                                                fbad);
+                                if (R.boxf[2 * i].w != 0.0f && R.boxf[2 * j].w != 0.0f)  // zero-size patches add 0
+                                    far_pair_df_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts,
+                                                    facc, fbad);
                                 continue;
                             }
                             if (T.far_df == 2) {
