@@ -1347,8 +1347,8 @@ __device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF 
 // entry's far part is reduced across lanes once, after all its patch pairs):
 // every point difference, square, the reciprocal square root and the sums
 // carry ~48 significant bits on the FP32 pipes; two independent partial sums
-// per lane keep the dependent add chains short.  `bad` is set for a NaN.
-__device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *pb, int npts, f2 &acc, bool &bad) {
+// per lane keep the dependent add chains short.  A NaN propagates into `acc`.
+__device__ __forceinline__ void far_pair_df_acc(const FarPtF *pa, const FarPtF *pb, int npts, f2 &acc) {
     const int lane = threadIdx.x & 31;
     for (int p = lane; p < npts; p += 32) {
         FarPtF A = pa[p];
@@ -1483,7 +1483,6 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                 // are reduced across the warp once per entry; near pairs (and
                 // the other modes) add in the reference's (i, j) order
                 f2 facc = {0.0f, 0.0f};
-                bool fbad = false;
                 for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i) {
                     // i's near partners are sorted by j (the scan's list):
                     // a cursor from the first partner in region b
@@ -1510,7 +1509,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                             if (T.far_df == 1) {
                                 if (R.boxf[2 * i].w != 0.0f && R.boxf[2 * j].w != 0.0f)  // zero-size patches add 0
                                     far_pair_df_acc(T.ptf + (size_t)i * T.npts, T.ptf + (size_t)j * T.npts, T.npts,
-                                                    facc, fbad);
+                                                    facc);
                                 continue;
                             }
                             if (T.far_df == 2) {
@@ -1529,11 +1528,10 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                     }
                 }
                 if (T.far_df == 1 || T.far_df == 2) {
-                    fbad = __any_sync(0xffffffffu, fbad);
                     const f2 far2 = warp_sum_df2(facc);
                     if (lane == 0) {  // the entry's FP64 epilogue on one lane
                         const double far = (double)far2.h + (double)far2.l;
-                        if (fbad || !isfinite(far)) bad = true;
+                        if (!isfinite(far)) bad = true;
                         integral += far;
                     }
                 }
