@@ -19,6 +19,8 @@ from peeeeeeeeeeeeeeeeeeec_gb300 import abi  # noqa: E402  (struct layouts)
 
 ORACLE_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libpeec_ref.so")
+# the same sources built with the reference's own release flags (CPU baseline)
+REF_NATIVE_PATH = os.path.join(HERE, "_ref", "libpeec_ref_native.so")
 
 D = abi.c_double_p
 S = abi.c_size_t_p
@@ -211,6 +213,10 @@ def _ip(a):
     return a.ctypes.data_as(P(C.c_int))
 
 
+def _cp(a):
+    return a.ctypes.data_as(P(abi.Complex))
+
+
 def _transient_lightning(fn, L, P_, edges, R, scheme, dt, source, n_steps, I, V, probe_nodes,
                          probe_edges):
     """source = (K, alpha, beta, delay, strike_node, return_node).  Returns
@@ -287,6 +293,54 @@ def incidence_products(lib, mesh, P_, threads=1):
     return out
 
 
+# ---------------------------------------------------------------------
+# synthetic mesh arrays (the same numbering as the library's mesher)
+# ---------------------------------------------------------------------
+def plate_arrays(lx, ly, nx, ny):
+    xyz = np.zeros(((nx + 1) * (ny + 1), 3))
+    for j in range(ny + 1):
+        for i in range(nx + 1):
+            xyz[j * (nx + 1) + i] = (lx * i / nx, ly * j / ny, 0.0)
+    quads = []
+    for j in range(ny):
+        for i in range(nx):
+            v = j * (nx + 1) + i
+            quads.append((v, v + 1, v + 1 + nx + 1, v + nx + 1))
+    return xyz, np.array(quads, dtype=np.int32)
+
+
+def box_arrays(lx, ly, lz, nx, ny, nz):
+    # same construction as the library's peec_synth_box (outward winding,
+    # first-seen vertex numbering over the faces -z, +z, -y, +y, -x, +x)
+    ids, xyz, quads = {}, [], []
+
+    def v(i, j, k):
+        if (i, j, k) not in ids:
+            ids[(i, j, k)] = len(xyz)
+            xyz.append((lx * i / nx, ly * j / ny, lz * k / nz))
+        return ids[(i, j, k)]
+
+    for j in range(ny):
+        for i in range(nx):
+            quads.append((v(i, j, 0), v(i, j + 1, 0), v(i + 1, j + 1, 0), v(i + 1, j, 0)))
+    for j in range(ny):
+        for i in range(nx):
+            quads.append((v(i, j, nz), v(i + 1, j, nz), v(i + 1, j + 1, nz), v(i, j + 1, nz)))
+    for k in range(nz):
+        for i in range(nx):
+            quads.append((v(i, 0, k), v(i + 1, 0, k), v(i + 1, 0, k + 1), v(i, 0, k + 1)))
+    for k in range(nz):
+        for i in range(nx):
+            quads.append((v(i, ny, k), v(i, ny, k + 1), v(i + 1, ny, k + 1), v(i + 1, ny, k)))
+    for k in range(nz):
+        for j in range(ny):
+            quads.append((v(0, j, k), v(0, j, k + 1), v(0, j + 1, k + 1), v(0, j + 1, k)))
+    for k in range(nz):
+        for j in range(ny):
+            quads.append((v(nx, j, k), v(nx, j + 1, k), v(nx, j + 1, k + 1), v(nx, j, k + 1)))
+    return np.array(xyz), np.array(quads, dtype=np.int32)
+
+
 def reference_available():
     return os.path.exists(REF_PATH)
 
@@ -314,7 +368,79 @@ class Reference:
         f.restype, f.argtypes = C.c_int, [D, D, P(C.c_int), D, C.c_size_t, C.c_size_t, C.c_int, C.c_double, C.c_double,
               C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_size_t, D, D,
               P(C.c_int), C.c_size_t, P(C.c_int), C.c_size_t, D]
+        Cp = P(abi.Complex)
+        harmonic = [
+            ("ref_plane_wave_excitation", C.c_int,
+             [P(abi.Mesh), C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, Cp, D, D]),
+            ("ref_harmonic_build", C.c_int, [P(abi.Mesh), D, D, D, C.c_double, C.c_int, Cp]),
+            ("ref_harmonic_residual", C.c_int,
+             [Cp, C.c_size_t, C.c_size_t, C.c_double, D, Cp, Cp, C.c_int, D]),
+            ("ref_harmonic_pipeline", C.c_int,
+             [P(abi.Mesh), P(abi.DualMesh), C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int,
+              D, D, D, Cp, Cp, Cp, S, D, D, D, D]),
+        ]
+        abi._bind(lib, harmonic)
         self.lib = lib
+
+    # ---- harmonic scattering chain (oracle/ref_harmonic.c) ----
+    def plane_wave_excitation(self, m, frequency, theta_deg=0.0, phi_deg=0.0, polarization=1, analytic=True,
+                              threads=1):
+        """(U_inc [Ne] complex, k_hat [3], E0 [3]) of a unit COMPLEX plane
+        wave (polarization 1 vertical, 0 horizontal)."""
+        U = np.zeros(m.n_edges, dtype=np.complex128)
+        kh, e0 = np.zeros(3), np.zeros(3)
+        s = self.lib.ref_plane_wave_excitation(C.byref(m.mesh), frequency, theta_deg, phi_deg, polarization,
+                                               1 if analytic else 0, threads, _cp(U), _dp(kh), _dp(e0))
+        if s != 0:
+            raise RuntimeError("reference excitation failed: %d" % s)
+        return U, kh, e0
+
+    def harmonic_build(self, m, L, P_, R, frequency, threads=1):
+        """Z of the reference's harmonic_build_system from given Lp, P, R."""
+        n = m.n_edges + m.n_nodes
+        Z = np.zeros((n, n), dtype=np.complex128)
+        L = np.ascontiguousarray(L, dtype=np.float64)
+        P_ = np.ascontiguousarray(P_, dtype=np.float64)
+        Rp = None if R is None else _dp(np.ascontiguousarray(R, dtype=np.float64))
+        s = self.lib.ref_harmonic_build(C.byref(m.mesh), _dp(L), _dp(P_), Rp, frequency, threads, _cp(Z))
+        if s != 0:
+            raise RuntimeError("reference harmonic_build_system failed: %d" % s)
+        return Z
+
+    def harmonic_residual(self, Z, ne, nv, frequency, P_, U, x, threads=1):
+        """The 7 fields of the reference's harmonic_compute_residual."""
+        out = np.zeros(7)
+        Z = np.ascontiguousarray(Z, dtype=np.complex128)
+        P_ = np.ascontiguousarray(P_, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.complex128)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        s = self.lib.ref_harmonic_residual(_cp(Z), ne, nv, frequency, _dp(P_), _cp(U), _cp(x), threads, _dp(out))
+        if s != 0:
+            raise RuntimeError("reference harmonic_compute_residual failed: %d" % s)
+        return out
+
+    def harmonic_pipeline(self, m, frequency, theta_deg=0.0, phi_deg=0.0, polarization=1, sheet_resistance=0.0,
+                          threads=1, matrices=True):
+        """The reference's whole harmonic scattering chain on one mesh: a dict
+        with x, U, R, pivots, row / column scales, residual[7], times[8] and,
+        with matrices=True, L, P and Z."""
+        ne, nv = m.n_edges, m.n_nodes
+        n = ne + nv
+        out = {"x": np.zeros(n, dtype=np.complex128), "U": np.zeros(ne, dtype=np.complex128), "R": np.zeros(ne),
+               "pivots": np.zeros(n, dtype=np.uintp), "row_scale": np.zeros(n), "column_scale": np.zeros(n),
+               "residual": np.zeros(7), "times": np.zeros(8)}
+        if matrices:
+            out.update(L=np.zeros((ne, ne)), P=np.zeros((nv, nv)), Z=np.zeros((n, n), dtype=np.complex128))
+        g = out.get
+        s = self.lib.ref_harmonic_pipeline(
+            C.byref(m.mesh), C.byref(m.dual), frequency, theta_deg, phi_deg, polarization, sheet_resistance,
+            threads, _dp(g("L")) if matrices else None, _dp(g("P")) if matrices else None, _dp(out["R"]),
+            _cp(g("Z")) if matrices else None, _cp(out["U"]), _cp(out["x"]), out["pivots"].ctypes.data_as(S),
+            _dp(out["row_scale"]), _dp(out["column_scale"]), _dp(out["residual"]), _dp(out["times"]))
+        if s != 0:
+            raise RuntimeError("reference harmonic chain failed: %d" % s)
+        out["pivots"] = out["pivots"].astype(np.int64)
+        return out
 
     def rcs_radiation(self, m, current, wave_number, directions, order=6):
         """The reference's rcs_compute_radiation_vector (one thread: its
@@ -328,3 +454,99 @@ class Reference:
                             probe_nodes=(), probe_edges=()):
         return _transient_lightning(self.lib.ref_transient_lightning, L, P_, edges, R, scheme, dt,
                                     source, n_steps, I, V, probe_nodes, probe_edges)
+
+
+# ---------------------------------------------------------------------
+# harmonic system around the hot path (numpy restatement)
+# ---------------------------------------------------------------------
+def harmonic_system(L, P_, edges, R, frequency):
+    """Z = [R + j w L, A; -P A^T, j w I] as harmonic_build_system
+    (src/solver/harmonic.c:175-372) writes it: re = R_ii on the diagonal of
+    the top-left block, im = w L_ij; A[e, a] = -1, A[e, b] = +1
+    (incidence.c:34-110); -(P[i, b] - P[i, a]) from incidence_build_PAT
+    (incidence.c:417-592); j w on the diagonal of the bottom-right block.
+    Elementwise, so bit-identical to the reference."""
+    L = np.asarray(L, dtype=np.float64)
+    P_ = np.asarray(P_, dtype=np.float64)
+    e = np.asarray(edges).reshape(-1, 2)
+    ne, nv = L.shape[0], P_.shape[0]
+    n = ne + nv
+    w = 2.0 * np.pi * frequency
+    Z = np.zeros((n, n), dtype=np.complex128)
+    zr, zi = Z.real, Z.imag          # views into Z
+    zi[:ne, :ne] = w * L
+    if R is not None:
+        zr[np.arange(ne), np.arange(ne)] = np.asarray(R, dtype=np.float64)
+    A = np.zeros((ne, nv))
+    A[np.arange(ne), e[:, 0]] = -1.0
+    A[np.arange(ne), e[:, 1]] = 1.0
+    zr[:ne, ne:] = A
+    zr[ne:, :ne] = -(P_[:, e[:, 1]] - P_[:, e[:, 0]])
+    zi[np.arange(ne, n), np.arange(ne, n)] = w
+    return Z
+
+
+def plane_wave_field(frequency, theta_deg, phi_deg, polarization, amplitude=1.0):
+    """(k_hat, E0, wave number) of a harmonic plane wave, as
+    incident_field_configure_harmonic builds them (incident_field.c:110-230,
+    312-423): k_hat = -(sin t cos p, sin t sin p, cos t); E0 = amplitude *
+    e_theta (polarization 1, vertical) or e_phi (0, horizontal); each
+    vector normalised by its Euclidean norm; k0 = 2 pi f / c0."""
+    c0 = 299792458.0
+    t = theta_deg * np.pi / 180.0
+    p = phi_deg * np.pi / 180.0
+    k_hat = np.array([-np.sin(t) * np.cos(p), -np.sin(t) * np.sin(p), -np.cos(t)])
+    e_theta = np.array([np.cos(t) * np.cos(p), np.cos(t) * np.sin(p), -np.sin(t)])
+    e_phi = np.array([-np.sin(p), np.cos(p), 0.0])
+
+    def unit(v):
+        return v / np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+
+    k_hat, e_theta, e_phi = unit(k_hat), unit(e_theta), unit(e_phi)
+    E0 = amplitude * (e_theta if polarization == 1 else e_phi)
+    return k_hat, E0, 2.0 * np.pi * frequency / c0
+
+
+def plane_wave_excitation(centers, vectors, k_hat, E0, wave_number, analytic=True):
+    """U_inc per edge (scattering.c:140-336): E(r_c) = E0 exp(-j k0 k_hat.r_c)
+    (incident_field.c:754-830, zero phase), projected on the edge vector; the
+    analytic edge integral multiplies by sinc(k0 k_hat.l / 2), with the
+    reference's series 1 - x^2/6 + x^4/120 below |x| = 1e-4."""
+    c = np.asarray(centers, dtype=np.float64).reshape(-1, 3)
+    v = np.asarray(vectors, dtype=np.float64).reshape(-1, 3)
+    kr = k_hat[0] * c[:, 0] + k_hat[1] * c[:, 1] + k_hat[2] * c[:, 2]
+    gamma = -wave_number * kr + 0.0
+    cs, sn = np.cos(gamma), np.sin(gamma)
+    re = (E0[0] * cs) * v[:, 0] + (E0[1] * cs) * v[:, 1] + (E0[2] * cs) * v[:, 2]
+    im = (E0[0] * sn) * v[:, 0] + (E0[1] * sn) * v[:, 1] + (E0[2] * sn) * v[:, 2]
+    if analytic:
+        x = 0.5 * (wave_number * (k_hat[0] * v[:, 0] + k_hat[1] * v[:, 1] + k_hat[2] * v[:, 2]))
+        x2 = x * x
+        small = np.abs(x) < 1.0e-4
+        f = np.where(small, 1.0 - x2 / 6.0 + (x2 * x2) / 120.0, np.sin(x) / np.where(small, 1.0, x))
+        re, im = re * f, im * f
+    return re + 1j * im
+
+
+def harmonic_rhs(U, nv):
+    """b = [-U_e ; 0] (harmonic_build_rhs, harmonic.c:436-552, no node current)."""
+    U = np.asarray(U, dtype=np.complex128)
+    return np.concatenate([-U, np.zeros(nv, dtype=np.complex128)])
+
+
+def harmonic_residual(Z, ne, U, x):
+    """The fields of harmonic_compute_residual (harmonic.c:720-1080) as
+    [absolute, rhs-relative, backward error, edge absolute, node absolute,
+    edge backward error, node backward error]; backward error =
+    max_i |r_i| / (sum_j |Z_ij||x_j| + |b_i|).  Summation order differs from
+    the reference's, so values agree to rounding, not bit for bit."""
+    Z = np.asarray(Z, dtype=np.complex128)
+    n = Z.shape[0]
+    b = harmonic_rhs(U, n - ne)
+    r = Z @ x - b
+    ra, ba = np.hypot(r.real, r.imag), np.hypot(b.real, b.imag)
+    den = np.hypot(Z.real, Z.imag) @ np.hypot(x.real, x.imag) + ba
+    eta = np.where(den > 0, ra / np.where(den > 0, den, 1.0), ra)
+    bmax = ba.max()
+    return np.array([ra.max(), ra.max() / bmax if bmax > 0 else ra.max(), eta.max(), ra[:ne].max(),
+                     ra[ne:].max(), eta[:ne].max(), eta[ne:].max()])

@@ -512,6 +512,43 @@ int oracle_potential_matrix(const Mesh *mesh, const DualMesh *dual, const int or
                                  mesh->n_nodes, data);
 }
 
+/* Rows of Lp (kind 0) or P (kind 1) for a timing sample: the upper-
+ * triangle pairs (a, b >= a) of the given rows with the default orders
+ * (4, 10, 12, 8), near factor 0.5 and direction tolerance 1e-10, the pairs
+ * of all sampled rows spread over `threads` threads.  out[k * n + b]
+ * receives row rows[k].  Returns 0, or -1 when a pair fails. */
+int oracle_sample_rows(const Mesh *mesh, const DualMesh *dual, int kind, const size_t *rows, size_t nrows,
+                       int threads, double *out)
+{
+    static const int orders[4] = {4, 10, 12, 8};
+    size_t n = kind == 0 ? mesh->n_edges : mesh->n_nodes;
+    size_t *start = malloc((nrows + 1) * sizeof(size_t));
+    if (!start) return -1;
+    start[0] = 0;
+    for (size_t k = 0; k < nrows; ++k) start[k + 1] = start[k] + (rows[k] < n ? n - rows[k] : 0);
+    int failed = 0;
+    long long total = (long long)start[nrows];
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+    for (long long t = 0; t < total; ++t) {
+        size_t lo = 0, hi = nrows;
+        while (hi - lo > 1) {
+            size_t mid = (lo + hi) / 2;
+            if (start[mid] <= (size_t)t) lo = mid; else hi = mid;
+        }
+        size_t a = rows[lo], b = a + ((size_t)t - start[lo]);
+        double v = 0.0;
+        int st = kind == 0 ? oracle_inductance_pair(mesh, dual, a, b, orders, 0.5, 1e-10, &v)
+                           : oracle_potential_pair(mesh, dual, a, b, orders, 0.5, &v);
+        if (st != 0) {
+#pragma omp atomic write
+            failed = 1;
+        }
+        out[lo * n + b] = v;
+    }
+    free(start);
+    return failed ? -1 : 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* real LU (lu.c:194-479, 494-653)                                     */
 /* ------------------------------------------------------------------ */

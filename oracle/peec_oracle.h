@@ -51,6 +51,10 @@ int oracle_inductance_rows(const Mesh *mesh, const DualMesh *dual, const int ord
 /* potential.c:139-253 and :261-395 */
 int oracle_potential_pair(const Mesh *mesh, const DualMesh *dual, size_t i, size_t j,
                           const int orders[4], double near_factor, double *value);
+/* Upper-triangle pairs of sampled rows of Lp (kind 0) or P (kind 1), default
+ * options, for the CPU timing sample; out[k * n + b] = row rows[k]. */
+int oracle_sample_rows(const Mesh *mesh, const DualMesh *dual, int kind, const size_t *rows,
+                       size_t nrows, int threads, double *out);
 int oracle_potential_matrix(const Mesh *mesh, const DualMesh *dual, const int orders[4],
                             double near_factor, int threads, double *data);
 int oracle_potential_rows(const Mesh *mesh, const DualMesh *dual, const int orders[4],

@@ -2,8 +2,10 @@
 
   libpeec_gb300.so   the sm_103a drop-in library (nvcc, one -gencode)
   libpeec_mesh.so    host-only synthetic mesher (gcc)
-  oracle/liboracle.so and, when the reference sources are present,
-  oracle/_ref/libpeec_ref.so   the CPU checkers (make -C oracle)
+  oracle/liboracle.so and, when the reference's sources are present (staged
+  into baseline/_ref/ by `make -C oracle stage`, which travels with the
+  working tree), oracle/_ref/libpeec_ref*.so   the CPU checkers and the
+  reference's own CPU build (make -C oracle)
 
 Translation units compile in parallel; no cmake.  Host code is portable C
 (no -march=native), so the same sources build on x86-64 and aarch64.
@@ -20,9 +22,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(REPO, "include")
 ORACLE = os.path.join(REPO, "oracle")
-REFERENCE = os.environ.get("PEEC_REFERENCE_DIR", "/root/reference")
+STAGED_REFERENCE = os.path.join(REPO, "baseline", "_ref")
 
-CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu", "matrix_export.cu"]
+CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu", "matrix_export.cu", "sweep.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17", "--fmad=false",
@@ -92,8 +94,12 @@ def build_mesh_lib():
 
 def build_oracle():
     _run(["make", "-s", "-C", ORACLE, "all"])
-    if os.path.isdir(os.path.join(REFERENCE, "src")):
-        _run(["make", "-s", "-C", ORACLE, "ref", "REF=" + REFERENCE])
+    # refresh the staged copy where the reference is readable (the recipe
+    # knows where), then build the reference from the staged copy
+    ref = os.environ.get("PEEC_REFERENCE_DIR")
+    _run(["make", "-s", "-C", ORACLE, "stage"] + (["REF=" + ref] if ref else []))
+    if os.path.isdir(os.path.join(STAGED_REFERENCE, "src")):
+        _run(["make", "-s", "-C", ORACLE, "ref"])
 
 
 def build_all(verbose=False):

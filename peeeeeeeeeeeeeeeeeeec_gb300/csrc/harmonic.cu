@@ -8,6 +8,7 @@
 //           [ -P A^T      j w I  ]      (P A^T)[i,e] = P[i,b] - P[i,a] (incidence.c:417-592)
 //   src/solver/harmonic.c:436-552    harmonic_build_rhs: [-U_e ; P I_s]
 //   src/physics/scattering.c:263-336 U_e = (E(r_c) . l) sinc(k_hat.l k0 / 2)
+//   src/physics/incident_field.c:754-830  E(r) = E0 exp(-j k0 k_hat.r)
 //   src/solver/harmonic.c:720-1080   backward error max_i |r_i| / (sum_j |Z_ij||x_j| + |b_i|)
 // All byte-bound: one pass over Z per kernel.
 #include <math.h>
@@ -24,7 +25,8 @@ struct cpx {
 
 // One thread per entry of row-block rows; coalesced 16-byte stores.
 __global__ void k_harmonic_fill(const double *L, const double *P, const int *edges, const double *R, int ne, int nv,
-                                double omega, cpx *Z) {
+                                double omega, const double *omega_dev, cpx *Z) {
+    if (omega_dev) omega = *omega_dev;  // the batched sweep's graph: the frequency lives in device memory
     const long long n = (long long)ne + nv;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n * n;
          t += (long long)gridDim.x * blockDim.x) {
@@ -85,26 +87,52 @@ __global__ void k_harmonic_fill_complex(const cpx *L, const cpx *P, const int *e
     }
 }
 
-// U_e for a unit plane wave E(r) = e_hat exp(-j k0 k_hat.r): field at the
-// edge centre projected on the edge vector, times sinc(q/2), q = k0 k_hat.l;
-// the right-hand side is [-U_e ; 0].
+// U_e for a plane wave E(r) = e_hat exp(-j k0 k_hat.r) in the operation
+// order of the reference (incident_field.c:754-830, scattering.c:140-336):
+// E_k = (e_k cos g, e_k sin g) with g = -k0 (k_hat.r_c) + 0, projected on
+// the edge vector term by term, times sinc(k0 (k_hat.l) / 2) with the
+// series 1 - x^2/6 + x^4/120 below |x| = 1e-4; the right-hand side is
+// [-U_e ; 0].  The library is built without FMA contraction, so only the
+// device sin / cos can differ from the host's (by an ulp).
+__device__ __forceinline__ cpx plane_wave_edge(const double *c, const double *l, double kx, double ky, double kz,
+                                               double ex, double ey, double ez, double k0) {
+    double kr = kx * c[0] + ky * c[1] + kz * c[2];
+    double g = -k0 * kr + 0.0;
+    double s, co;
+    sincos(g, &s, &co);
+    double ure = (ex * co) * l[0] + (ey * co) * l[1] + (ez * co) * l[2];
+    double uim = (ex * s) * l[0] + (ey * s) * l[1] + (ez * s) * l[2];
+    double x = 0.5 * (k0 * (kx * l[0] + ky * l[1] + kz * l[2]));
+    double f;
+    if (fabs(x) < 1.0e-4) {
+        double x2 = x * x;
+        f = 1.0 - x2 / 6.0 + (x2 * x2) / 120.0;
+    } else {
+        f = sin(x) / x;
+    }
+    return cpx{-(ure * f), -(uim * f)};
+}
+
 __global__ void k_plane_wave_rhs(const double *centers, const double *vectors, int ne, int nv, double kx, double ky,
                                  double kz, double ex, double ey, double ez, double k0, cpx *rhs) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ne + nv) return;
-    if (i >= ne) {
-        rhs[i] = cpx{0.0, 0.0};
-        return;
-    }
-    const double *c = centers + 3 * i, *l = vectors + 3 * i;
-    double phase = -k0 * (kx * c[0] + ky * c[1] + kz * c[2]);
-    double s, co;
-    sincos(phase, &s, &co);
-    double proj = ex * l[0] + ey * l[1] + ez * l[2];
-    double q = k0 * (kx * l[0] + ky * l[1] + kz * l[2]);
-    double h = 0.5 * q;
-    double sinc = fabs(h) < 1e-8 ? 1.0 - h * h / 6.0 : sin(h) / h;
-    rhs[i] = cpx{-proj * co * sinc, -proj * s * sinc};
+    rhs[i] = i >= ne ? cpx{0.0, 0.0}
+                     : plane_wave_edge(centers + 3 * i, vectors + 3 * i, kx, ky, kz, ex, ey, ez, k0);
+}
+
+// nrhs waves at once (directions and polarisations in device memory, k0
+// from *k0_dev when set): rhs[q][i].
+__global__ void k_plane_waves(const double *centers, const double *vectors, int ne, int nv, int nrhs,
+                              const double *k_hat, const double *e_hat, double k0, const double *k0_dev, cpx *rhs) {
+    const long long n = (long long)ne + nv;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n * nrhs) return;
+    if (k0_dev) k0 = *k0_dev;
+    const int q = (int)(t / n), i = (int)(t % n);
+    const double *kq = k_hat + 3 * q, *eq = e_hat + 3 * q;
+    rhs[t] = i >= ne ? cpx{0.0, 0.0}
+                     : plane_wave_edge(centers + 3 * i, vectors + 3 * i, kq[0], kq[1], kq[2], eq[0], eq[1], eq[2], k0);
 }
 
 // |z| in FP32 for the denominator sum |Z||x| + |b| of the backward error (a
@@ -150,7 +178,7 @@ __global__ void k_backward_error(const cpx *Z, const cpx *x, const float *absx, 
     if (lane == 0) {
         cpx bi = b[(size_t)rr * n + i];
         double res = hypot(yr - bi.re, yi - bi.im);
-        double babs = hypot(bi.re, bi.im);
+        double babs = hypot_cr(bi.re, bi.im);
         double d = (double)den + babs;
         double eta = d > 0.0 ? res / d : res;
         if (!isfinite(eta)) eta = INFINITY;
@@ -158,6 +186,24 @@ __global__ void k_backward_error(const cpx *Z, const cpx *x, const float *absx, 
         atomicMax(out + 1, (unsigned long long)__double_as_longlong(isfinite(res) ? res : INFINITY));
         atomicMax(out + 2, (unsigned long long)__double_as_longlong(babs));
     }
+}
+
+// Launchers for the batched sweep (sweep.cu): omega / k0 read from device
+// memory by the kernels, so that a recorded graph serves every frequency.
+bool launch_harmonic_fill_dev(const double *L, const double *P, const int *edges, const double *R, int ne, int nv,
+                              const double *omega_dev, void *Z) {
+    long long n = (long long)ne + nv, total = n * n;
+    int grid = (int)((total + 255) / 256 < 152LL * 32 ? (total + 255) / 256 : 152LL * 32);
+    PEEC_LAUNCH(k_harmonic_fill, grid, 256, 0, L, P, edges, R, ne, nv, 0.0, omega_dev, (cpx *)Z);
+    return launch_ok("harmonic fill");
+}
+
+bool launch_plane_waves_dev(const double *centers, const double *vectors, int ne, int nv, int nrhs,
+                            const double *d_k_hat, const double *d_e_hat, const double *k0_dev, void *rhs) {
+    long long total = ((long long)ne + nv) * nrhs;
+    PEEC_LAUNCH(k_plane_waves, (unsigned)((total + 255) / 256), 256, 0, centers, vectors, ne, nv, nrhs, d_k_hat,
+                d_e_hat, 0.0, k0_dev, (cpx *)rhs);
+    return launch_ok("plane waves");
 }
 
 }  // namespace peec
@@ -177,7 +223,7 @@ int peec_gb300_harmonic_build_device(const double *d_L, const double *d_P, const
     long long total = n * n;
     int grid = (int)((total + 255) / 256 < 152LL * 32 ? (total + 255) / 256 : 152LL * 32);
     PEEC_LAUNCH(k_harmonic_fill, grid, 256, 0, d_L, d_P, d_edges, d_R, (int)n_edges, (int)n_nodes, omega,
-                (cpx *)d_Z);
+                (const double *)nullptr, (cpx *)d_Z);
     return launch_ok("harmonic fill") ? 0 : -1;
 }
 

@@ -5,7 +5,8 @@ oracle/_ref/libpeec_ref.so (`make -C oracle ref`), on small seeded inputs and
 stores inputs and outputs as .npz files.  The GPU machine has no copy of the
 reference, so the tests there compare against these files.
 
-    python tests/golden/make_golden.py        (needs oracle/_ref/libpeec_ref.so)
+    python tests/golden/make_golden.py            (needs oracle/_ref/libpeec_ref.so)
+    python tests/golden/make_golden.py harmonic   (only the harmonic chain)
 """
 import ctypes as C
 import os
@@ -19,9 +20,10 @@ sys.path.insert(0, REPO)
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 from peeeeeeeeeeeeeeeeeeec_gb300 import abi  # noqa: E402
-from oracle import Reference  # noqa: E402
+from oracle import Reference, box_arrays, plate_arrays  # noqa: E402
 
-REF_MESH_DIR = os.environ.get("PEEC_REFERENCE_DIR", "/root/reference") + "/meshes"
+# the reference's meshes, from the copy `make -C oracle stage` keeps
+REF_MESH_DIR = os.path.join(REPO, "baseline", "_ref", "meshes")
 
 _libc = C.CDLL(None)
 _libc.malloc.restype = C.c_void_p
@@ -38,19 +40,6 @@ def _arr(ptr, shape, dtype):
     n = int(np.prod(shape))
     ctype = C.c_double if dtype == np.float64 else C.c_int
     return np.frombuffer(C.cast(ptr, C.POINTER(ctype * n)).contents, dtype=dtype).reshape(shape).copy()
-
-
-def plate_arrays(lx, ly, nx, ny):
-    xyz = np.zeros(((nx + 1) * (ny + 1), 3))
-    for j in range(ny + 1):
-        for i in range(nx + 1):
-            xyz[j * (nx + 1) + i] = (lx * i / nx, ly * j / ny, 0.0)
-    quads = []
-    for j in range(ny):
-        for i in range(nx):
-            v = j * (nx + 1) + i
-            quads.append((v, v + 1, v + 1 + nx + 1, v + nx + 1))
-    return xyz, np.array(quads, dtype=np.int32)
 
 
 def reference_case(R, xyz, quads, name, with_matrices=True):
@@ -94,38 +83,6 @@ def reference_case(R, xyz, quads, name, with_matrices=True):
         out["P"] = np.ctypeslib.as_array(Pm.data, shape=(nv, nv)).copy()
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print("wrote", name, "Ne=%d Nv=%d" % (ne, nv))
-
-
-def box_arrays(lx, ly, lz, nx, ny, nz):
-    # same construction as the library's peec_synth_box (outward winding,
-    # first-seen vertex numbering over the faces -z, +z, -y, +y, -x, +x)
-    ids, xyz, quads = {}, [], []
-
-    def v(i, j, k):
-        if (i, j, k) not in ids:
-            ids[(i, j, k)] = len(xyz)
-            xyz.append((lx * i / nx, ly * j / ny, lz * k / nz))
-        return ids[(i, j, k)]
-
-    for j in range(ny):
-        for i in range(nx):
-            quads.append((v(i, j, 0), v(i, j + 1, 0), v(i + 1, j + 1, 0), v(i + 1, j, 0)))
-    for j in range(ny):
-        for i in range(nx):
-            quads.append((v(i, j, nz), v(i + 1, j, nz), v(i + 1, j + 1, nz), v(i, j + 1, nz)))
-    for k in range(nz):
-        for i in range(nx):
-            quads.append((v(i, 0, k), v(i + 1, 0, k), v(i + 1, 0, k + 1), v(i, 0, k + 1)))
-    for k in range(nz):
-        for i in range(nx):
-            quads.append((v(i, ny, k), v(i, ny, k + 1), v(i + 1, ny, k + 1), v(i + 1, ny, k)))
-    for k in range(nz):
-        for j in range(ny):
-            quads.append((v(0, j, k), v(0, j, k + 1), v(0, j + 1, k + 1), v(0, j + 1, k)))
-    for k in range(nz):
-        for j in range(ny):
-            quads.append((v(nx, j, k), v(nx, j + 1, k), v(nx, j + 1, k + 1), v(nx, j, k + 1)))
-    return np.array(xyz), np.array(quads, dtype=np.int32)
 
 
 def gmsh_case(R, path, name):
@@ -316,7 +273,57 @@ def incidence_case(R, name):
     print("wrote incidence_" + name)
 
 
+# The reference's harmonic scattering chain (oracle/ref_harmonic.c, the calls
+# of main.c's solve_harmonic_scattering): Lp, P, P A^T, R, the analytic
+# plane-wave excitation, harmonic_build_system, harmonic_factorize,
+# harmonic_solve and harmonic_compute_residual, at 30 MHz with a unit
+# x-polarised wave from +z (theta 0, phi 0, vertical).  Small cases keep
+# every matrix; the 2102-unknown box keeps the solution, pivots, scales and
+# residual.  Also: an oblique wave's excitation (theta 60, phi 30,
+# horizontal) and the residual of a perturbed solution, whose backward error
+# is far above rounding so that implementations can be compared on it.
+SIGMA_SHEET = 1.0 / (5.8e7 * 1.0e-3)   # 1 mm copper sheet, ohms per square
+HARMONIC_FREQ = 30.0e6
+
+
+def harmonic_case(R, xyz, quads, name, sheet_resistance, matrices):
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    threads = os.cpu_count()
+    with SynthMesh.from_arrays(xyz, quads) as m:
+        ne, nv = m.n_edges, m.n_nodes
+        out = R.harmonic_pipeline(m, HARMONIC_FREQ, 0.0, 0.0, 1, sheet_resistance, threads, matrices=True)
+        U1, kh1, e01 = R.plane_wave_excitation(m, HARMONIC_FREQ, 0.0, 0.0, 1, True, threads)
+        assert np.array_equal(U1, out["U"])
+        U2, kh2, e02 = R.plane_wave_excitation(m, HARMONIC_FREQ, 60.0, 30.0, 0, True, threads)
+        rng = np.random.default_rng(17)
+        x = out["x"]
+        xp = x * (1.0 + 1e-6 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size)))
+        res_p = R.harmonic_residual(out["Z"], ne, nv, HARMONIC_FREQ, out["P"], out["U"], xp, threads)
+        edges = m.edges()
+        centers = m.array("edge_centers", (ne, 3))
+        vectors = m.array("edge_vectors", (ne, 3))
+    keep = dict(xyz=xyz, quads=quads, edges=edges, edge_centers=centers, edge_vectors=vectors,
+                frequency=HARMONIC_FREQ, sheet_resistance=sheet_resistance, x=x, U=out["U"], R=out["R"],
+                pivots=out["pivots"], row_scale=out["row_scale"], column_scale=out["column_scale"],
+                residual=out["residual"], k_hat=kh1, E0=e01, U_oblique=U2, k_hat_oblique=kh2, E0_oblique=e02,
+                x_perturbed=xp, residual_perturbed=res_p, cpu_seconds=out["times"], threads=threads)
+    if matrices:
+        keep.update(L=out["L"], P=out["P"], Z=out["Z"])
+    np.savez_compressed(os.path.join(HERE, "harmonic_" + name + ".npz"), **keep)
+    print("wrote harmonic_%s Ne=%d Nv=%d backward error %.3g, %.1f s" % (name, ne, nv, out["residual"][2],
+                                                                        out["times"].sum()))
+
+
+def harmonic_cases(R):
+    harmonic_case(R, *plate_arrays(1.0, 1.0, 4, 4), "plate4", SIGMA_SHEET, True)
+    harmonic_case(R, *box_arrays(0.4, 0.2, 0.1, 4, 2, 1), "box421", 0.0, True)
+    harmonic_case(R, *box_arrays(1.0, 0.5, 0.25, 20, 10, 5), "box1m_5cm", 0.0, False)
+
+
 def main():
+    if sys.argv[1:] == ["harmonic"]:
+        harmonic_cases(Reference())
+        return
     if sys.argv[1:] == ["incidence"]:
         R = Reference()
         incidence_case(R, "plate4")
@@ -338,6 +345,7 @@ def main():
     plate_msh = os.path.join(REF_MESH_DIR, "plate.msh")
     if os.path.exists(plate_msh):
         gmsh_case(R, plate_msh, "plate_msh")
+    harmonic_cases(R)
 
 
 if __name__ == "__main__":

@@ -129,3 +129,35 @@ def elem_rel_err(a, b):
     if np.any(a[~nz] != 0):
         return float("inf")
     return float(np.max(np.abs(a[nz] - b[nz]) / np.abs(b[nz]))) if nz.any() else 0.0
+
+
+class DeviceBuffers:
+    """Device copies of numpy arrays for the extension API; freed on exit."""
+
+    def __init__(self, lib):
+        self.lib, self.ptrs = lib, []
+
+    def put(self, arr):
+        arr = np.ascontiguousarray(arr)
+        p = self.alloc(arr.nbytes)
+        assert self.lib.peec_gb300_copy_to_device(p, arr.ctypes.data, arr.nbytes) == 0
+        return p
+
+    def alloc(self, nbytes):
+        p = self.lib.peec_gb300_device_alloc(max(int(nbytes), 16))
+        assert p, "device allocation failed"
+        self.ptrs.append(p)
+        return p
+
+    def get(self, p, shape, dtype):
+        out = np.zeros(shape, dtype=dtype)
+        assert self.lib.peec_gb300_copy_to_host(out.ctypes.data, p, out.nbytes) == 0
+        return out
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        for p in self.ptrs:
+            self.lib.peec_gb300_device_free(p)
+        self.ptrs = []

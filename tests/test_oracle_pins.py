@@ -376,3 +376,61 @@ def test_incidence_oracle_against_reference_library(oracle):
     assert np.array_equal(oracle.incidence_apat(P_, edges), ref["APAT"])
     assert np.array_equal(oracle.incidence_pat(P_, edges)[1], ref["PAT"])
     assert np.array_equal(oracle.incidence_as(P_, edges)[1], ref["AS"])
+
+
+# ---- harmonic system (oracle restatement vs the reference's own outputs) ----
+@pytest.mark.parametrize("name", ["plate4", "box421"])
+def test_harmonic_fill_restatement_bit_exact(name):
+    """The numpy MNA fill equals the reference's harmonic_build_system bit
+    for bit (fixtures written by the reference from its own Lp, P, R)."""
+    from oracle import harmonic_system
+    g = golden("harmonic_" + name)
+    Z = harmonic_system(g["L"], g["P"], g["edges"], g["R"], float(g["frequency"]))
+    assert np.array_equal(Z.view(np.uint64), g["Z"].view(np.uint64))
+
+
+@pytest.mark.parametrize("name", ["plate4", "box421", "box1m_5cm"])
+def test_plane_wave_restatement_matches_reference(name):
+    """k_hat, E0 and U_inc of the reference's incident_field_configure_
+    harmonic + scattering_build_harmonic_excitation (analytic edge integral),
+    for the +z wave and an oblique horizontally polarised one."""
+    from oracle import plane_wave_excitation, plane_wave_field
+    g = golden("harmonic_" + name)
+    f = float(g["frequency"])
+    for (th, ph, pol), suffix in (((0.0, 0.0, 1), ""), ((60.0, 30.0, 0), "_oblique")):
+        kh, e0, k0 = plane_wave_field(f, th, ph, pol)
+        assert np.array_equal(kh, g["k_hat" + suffix]) and np.array_equal(e0, g["E0" + suffix])
+        U = plane_wave_excitation(g["edge_centers"], g["edge_vectors"], kh, e0, k0)
+        ref = g["U" + suffix]
+        assert np.max(np.abs(U - ref)) <= 1e-15 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("name", ["plate4", "box421"])
+def test_harmonic_residual_restatement(name):
+    """The backward error and residual norms of harmonic_compute_residual
+    (a perturbed solution, so that the values sit far above rounding).  The
+    node rows sum terms ~1e5 times their residual, so the summation order
+    moves the residual norms by up to ~1e-10 of themselves: rtol 1e-9."""
+    from oracle import harmonic_residual
+    g = golden("harmonic_" + name)
+    ne = g["L"].shape[0]
+    res = harmonic_residual(g["Z"], ne, g["U"], g["x_perturbed"])
+    assert np.allclose(res, g["residual_perturbed"], rtol=1e-9, atol=0)
+    res0 = harmonic_residual(g["Z"], ne, g["U"], g["x"])
+    assert res0[2] <= 1e-10 and g["residual"][2] <= 1e-10
+
+
+def test_harmonic_fixture_reproduced_by_reference():
+    """The fixture generator is the reference's chain: rerunning it on the
+    plate gives the stored solution (same machine, same build)."""
+    from oracle import reference_available
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
+    if not reference_available():
+        pytest.skip("reference library not built here")
+    from oracle import Reference
+    g = golden("harmonic_plate4")
+    with SynthMesh.from_arrays(g["xyz"], g["quads"]) as m:
+        out = Reference().harmonic_pipeline(m, float(g["frequency"]), 0.0, 0.0, 1, float(g["sheet_resistance"]),
+                                           int(g["threads"]))
+    assert np.array_equal(out["pivots"], g["pivots"])
+    assert np.max(np.abs(out["x"] - g["x"])) <= 1e-13 * np.max(np.abs(g["x"]))
