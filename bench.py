@@ -16,9 +16,10 @@ Lp and P are quasi-static (the reference has no retardation).
           inductance_compute_matrix, potential_compute_matrix, host MNA
           fill (what the reference's harmonic driver does), complex_lu_
           factorize, complex_lu_solve, host backward error
-  --impl reference   the reference algorithm on the host cores (the CPU
-          oracle, a restatement bit-exact with the reference's sources), on
-          a bounded sample extrapolated to one solve
+  --impl reference   the reference's own CPU code on the host cores (its
+          sources built here with its release flags; the bit-exact oracle
+          port where they are absent), on a bounded sample extrapolated to
+          one solve (oracle/cpu_baseline.py)
 Multi-GPU: the path does not shard; --gpus N runs N independent replicas
 (one process per GPU) and reports the aggregate.
 """
@@ -200,7 +201,8 @@ class DeviceSolve:
         ev.append(lib.peec_gb300_event_record())
         assert lib.peec_gb300_harmonic_build_device(self.dL, self.dP, self.dedges, None, self.ne, self.nv, FREQ,
                                                     self.dZ) == 0
-        assert lib.peec_gb300_copy_device(self.dLU, self.dZ, n * n * 16) == 0
+        ev.append(lib.peec_gb300_event_record())
+        assert lib.peec_gb300_copy_device(self.dLU, self.dZ, n * n * 16) == 0  # Z stays for the residual
         ev.append(lib.peec_gb300_event_record())
         scale, col = C.c_double(), C.c_int()
         s = lib.peec_gb300_complex_lu_factor_device(self.dLU, n, 1e-14, self.dpiv, self.dperm, self.drow, self.dcol,
@@ -215,7 +217,8 @@ class DeviceSolve:
         out = (C.c_double * 3)()
         assert lib.peec_gb300_backward_error_device(self.dZ, n, self.dx, self.db, 1, out) == 0
         ev.append(lib.peec_gb300_event_record())
-        names = ["assemble_Lp", "assemble_P", "mna_fill", "complex_lu", "rhs_solve", "backward_error"]
+        names = ["assemble_Lp", "assemble_P", "mna_fill", "copy_Z_for_factor", "complex_lu", "rhs_solve",
+                 "backward_error"]
         for k, name in enumerate(names):
             self.phase_ms.setdefault(name, []).append(lib.peec_gb300_event_elapsed_ms(ev[k], ev[k + 1]))
         for tag, st in (("Lp", self.stL), ("P", self.stP)):
@@ -442,6 +445,82 @@ def retarded_leg(lib, ds):
     return out
 
 
+def far_precision_leg(lib, ds):
+    """Lp + P assembly of the same box with each far-rule arithmetic: native
+    FP64 (the reference's), double-float on the FP32 pipes (the plain path's
+    default) and FP32 (the mixed path's), CUDA-event timed after a warm
+    pass; entry errors against the native FP64 matrices."""
+    m = ds.m
+    out, ref = {}, None
+    prev = lib.peec_gb300_set_far_precision(0)
+    for mode, name in ((0, "fp64_native"), (1, "double_float"), (2, "fp32")):
+        lib.peec_gb300_set_far_precision(mode)
+        for rep in range(2):
+            e0 = lib.peec_gb300_event_record()
+            assert lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.lo), ds.dL,
+                                                    C.byref(ds.stL)) == 0
+            e1 = lib.peec_gb300_event_record()
+            assert lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.po), ds.dP,
+                                                   C.byref(ds.stP)) == 0
+            e2 = lib.peec_gb300_event_record()
+            lib.peec_gb300_synchronize()
+            ms = (lib.peec_gb300_event_elapsed_ms(e0, e1), lib.peec_gb300_event_elapsed_ms(e1, e2))
+            for e in (e0, e1, e2):
+                lib.peec_gb300_event_destroy(e)
+        L = np.zeros((ds.ne, ds.ne))
+        P = np.zeros((ds.nv, ds.nv))
+        lib.peec_gb300_copy_to_host(L.ctypes.data, ds.dL, L.nbytes)
+        lib.peec_gb300_copy_to_host(P.ctypes.data, ds.dP, P.nbytes)
+        out[name] = {"Lp_ms": ms[0], "P_ms": ms[1], "Lp_far_ms": ds.stL.ms_far, "P_far_ms": ds.stP.ms_far}
+        if ref is None:
+            ref = (L, P)
+        else:
+            for tag, a, b in (("Lp", L, ref[0]), ("P", P, ref[1])):
+                nz = b != 0
+                out[name][tag + "_max_rel_err_vs_fp64"] = float(np.max(np.abs(a[nz] - b[nz]) / np.abs(b[nz])))
+    lib.peec_gb300_set_far_precision(prev)
+    out["note"] = ("the plain path (value) uses double_float: FP32-pipe arithmetic carrying ~48 bits, within 1e-12 "
+                   "of the reference; fp64_native is the same rule on the FP64 pipe")
+    return out
+
+
+def retarded_plain_leg(lib, ds):
+    """One plain FP64 solve of the retarded system (complex Lp / P with
+    exp(-jkR)/R: static part double-float far rule + FP64 near field,
+    retardation correction on the FP32 pipes; complex FP64 LU), after the
+    mixed retarded leg has warmed the kernels.  CUDA-event timed."""
+    m, n = ds.m, ds.n
+    k = 2 * np.pi * FREQ / C0
+    al = lib.peec_gb300_device_alloc
+    dLc, dPc = al(ds.ne * ds.ne * 16), al(ds.nv * ds.nv * 16)
+    ev = [lib.peec_gb300_event_record()]
+    assert lib.peec_gb300_inductance_retarded_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.lo), k, dLc,
+                                                     None) == 0
+    assert lib.peec_gb300_potential_retarded_device(C.byref(m.mesh), C.byref(m.dual), C.byref(ds.po), k, dPc,
+                                                    None) == 0
+    ev.append(lib.peec_gb300_event_record())
+    assert lib.peec_gb300_harmonic_build_retarded_device(dLc, dPc, ds.dedges, None, ds.ne, ds.nv, FREQ, ds.dZ) == 0
+    assert lib.peec_gb300_copy_device(ds.dLU, ds.dZ, n * n * 16) == 0
+    assert lib.peec_gb300_plane_wave_rhs_device(ds.dctr, ds.dvec, ds.ne, ds.nv, ds.kh, ds.eh, ds.k0, ds.db) == 0
+    ev.append(lib.peec_gb300_event_record())
+    scale, col = C.c_double(), C.c_int()
+    assert lib.peec_gb300_complex_lu_factor_device(ds.dLU, n, 1e-14, ds.dpiv, ds.dperm, ds.drow, ds.dcol,
+                                                   C.byref(scale), C.byref(col)) == 0
+    assert lib.peec_gb300_complex_lu_solve_device(ds.dLU, ds.dperm, ds.drow, ds.dcol, n, ds.db, ds.dx, 1) == 0
+    ev.append(lib.peec_gb300_event_record())
+    out3 = (C.c_double * 3)()
+    assert lib.peec_gb300_backward_error_device(ds.dZ, n, ds.dx, ds.db, 1, out3) == 0
+    ms = [lib.peec_gb300_event_elapsed_ms(ev[i], ev[i + 1]) for i in range(3)]
+    for e in ev:
+        lib.peec_gb300_event_destroy(e)
+    for p in (dLc, dPc):
+        lib.peec_gb300_device_free(p)
+    return {"value": 1000.0 / sum(ms), "unit": "solves/s", "ms_per_step": sum(ms),
+            "phase_ms": {"assemble_Lp_P_retarded": ms[0], "fill_copy_rhs": ms[1], "complex_lu_solve": ms[2]},
+            "backward_error": out3[0], "precision": "plain: FP64 LU; static far rule double-float, near field FP64, "
+                                                    "retardation correction FP32 pipes"}
+
+
 def config3(lib):
     """The 2.5 cm box (80 x 40 x 20 cells: Ne 22400, Nv 11202, N 33602) at
     100 MHz with retarded Lp / P (FP32 far rule, FP64 near field) and one
@@ -539,43 +618,221 @@ def config3(lib):
     m.close()
 
 
-def serving_leg(lib, window_s, workers):
-    """Poisson arrivals at 200 requests/s over window_s of harmonic requests
-    (seeded boxes / plates of 500-12000 unknowns, 1-100 MHz, 1-64 plane
-    waves), replayed once with the mixed-precision solve and once with the
-    plain FP64 LU through one server (150 GB budget) whose Lp / P cache was
-    warmed first.  Latency = completion - submission on the server clock."""
+def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
+    """Config 4: n_meshes seeded boxes / plates (sides U(0.2, 2.0) m, cell size
+    chosen for N = Ne + Nv ~ U(300, 4000)), each at n_freqs log-spaced
+    frequencies from 1 kHz to 100 MHz with nrhs plane waves.  Both arms run
+    the meshes largest first on `workers` host threads (one CUDA stream each)
+    and time the whole arm on the wall clock: Lp / P assembly included.
+      mixed  a sweep plan per mesh (peec_gb300_sweep_*): the autotuner at
+             three probe frequencies (lowest, middle, highest) picks split
+             terms, refinement sweeps and tile width; the mixed solve
+             recorded once into a CUDA graph is replayed for every frequency;
+             systems above the gate are solved again by the precision
+             ladder, then the FP64 LU with FP64 refinement
+      plain  per system: MNA fill, FP64 complex LU, solve, FP64 iterative
+             refinement with that factor to the same gate (every
+             plain_stride-th frequency; throughput over the systems run)
+    Throughput = systems whose componentwise backward error <= 1e-10 / wall
+    time."""
+    import concurrent.futures as cf
     from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
+    pool = W.serving_meshes(seed=11, count=n_meshes, lo=300, hi=4000)
+    order = sorted(range(len(pool)), key=lambda i: -(pool[i][0].n_edges + pool[i][0].n_nodes))
+    freqs = np.logspace(3.0, 8.0, n_freqs)
+    waves = [W.plane_waves(np.random.default_rng(100 + i), nrhs) for i in range(len(pool))]
+    lo, po = ds_opts(lib)
+
+    def assemble(m):
+        ne, nv = m.n_edges, m.n_nodes
+        al = lib.peec_gb300_device_alloc
+        d = {"L": al(ne * ne * 8), "P": al(nv * nv * 8), "e": al(ne * 8), "c": al(ne * 24), "v": al(ne * 24)}
+        assert lib.peec_gb300_inductance_device(C.byref(m.mesh), C.byref(m.dual), C.byref(lo), d["L"], None) == 0
+        assert lib.peec_gb300_potential_device(C.byref(m.mesh), C.byref(m.dual), C.byref(po), d["P"], None) == 0
+        for key, arr in (("e", np.ascontiguousarray(m.edges(), dtype=np.int32)),
+                         ("c", m.array("edge_centers", (ne, 3))), ("v", m.array("edge_vectors", (ne, 3)))):
+            assert lib.peec_gb300_copy_to_device(d[key], np.ascontiguousarray(arr).ctypes.data, arr.nbytes) == 0
+        return d
+
+    def free(d):
+        for p in d.values():
+            lib.peec_gb300_device_free(p)
+
+    def mixed_mesh(i):
+        m = pool[i][0]
+        ne, nv = m.n_edges, m.n_nodes
+        n = ne + nv
+        d = assemble(m)
+        kh, eh = (np.ascontiguousarray(a) for a in waves[i])
+        plan = lib.peec_gb300_sweep_create(d["L"], d["P"], d["e"], None, d["c"], d["v"], ne, nv, nrhs,
+                                           kh.ctypes.data_as(ds_abi().c_double_p),
+                                           eh.ctypes.data_as(ds_abi().c_double_p), None)
+        assert plan, "sweep plan"
+        t = ds_abi().PeecSweepTuning()
+        ms = C.c_double()
+        probes = np.ascontiguousarray(freqs[[0, len(freqs) // 2, len(freqs) - 1]])
+        assert lib.peec_gb300_sweep_tune(plan, probes.ctypes.data_as(ds_abi().c_double_p), 3, C.byref(t),
+                                         C.byref(ms)) == 0
+        dX = lib.peec_gb300_device_alloc(len(freqs) * nrhs * n * 16)
+        be = np.zeros(len(freqs))
+        fb = np.zeros(len(freqs), dtype=np.int32)
+        f = np.ascontiguousarray(freqs)
+        s = lib.peec_gb300_sweep_run(plan, f.ctypes.data_as(ds_abi().c_double_p), len(freqs), 1e-10, dX,
+                                     be.ctypes.data_as(ds_abi().c_double_p), fb.ctypes.data_as(ds_abi().c_int_p))
+        assert s >= 0, "sweep run failed"
+        lib.peec_gb300_sweep_destroy(plan)
+        lib.peec_gb300_device_free(dX)
+        free(d)
+        return {"n": n, "be": be, "fb": fb, "tuning": (t.split_terms, t.sweeps, t.tile_bn), "graph_ms": ms.value}
+
+    def plain_mesh(i):
+        m = pool[i][0]
+        ne, nv = m.n_edges, m.n_nodes
+        n = ne + nv
+        d = assemble(m)
+        al = lib.peec_gb300_device_alloc
+        dZ, dLU, dB, dX = al(n * n * 16), al(n * n * 16), al(nrhs * n * 16), al(nrhs * n * 16)
+        dpiv, dperm, drs, dcs = al(n * 8), al(n * 4), al(n * 8), al(n * 8)
+        kh, eh = waves[i]
+        bes = []
+        for fr in freqs[::plain_stride]:
+            assert lib.peec_gb300_harmonic_build_device(d["L"], d["P"], d["e"], None, ne, nv, fr, dZ) == 0
+            assert lib.peec_gb300_copy_device(dLU, dZ, n * n * 16) == 0
+            scale, col = C.c_double(), C.c_int()
+            s = lib.peec_gb300_complex_lu_factor_device(dLU, n, 1e-14, dpiv, dperm, drs, dcs, C.byref(scale),
+                                                        C.byref(col))
+            if s != 0:
+                bes.append(np.inf)
+                continue
+            for q in range(nrhs):
+                kq, eq = (C.c_double * 3)(*kh[q]), (C.c_double * 3)(*eh[q])
+                assert lib.peec_gb300_plane_wave_rhs_device(d["c"], d["v"], ne, nv, kq, eq, 2 * np.pi * fr / C0,
+                                                            dB + q * n * 16) == 0
+            assert lib.peec_gb300_complex_lu_solve_device(dLU, dperm, drs, dcs, n, dB, dX, nrhs) == 0
+            be, it = C.c_double(), C.c_int()
+            r = lib.peec_gb300_complex_refine_device(dZ, dLU, dperm, drs, dcs, n, dB, dX, nrhs, 1e-10, 10,
+                                                     C.byref(be), C.byref(it))
+            bes.append(be.value if r >= 0 else np.inf)
+        for p in (dZ, dLU, dB, dX, dpiv, dperm, drs, dcs):
+            lib.peec_gb300_device_free(p)
+        free(d)
+        return {"n": n, "be": np.array(bes)}
+
+    out = {"systems": "%d meshes x %d frequencies (1 kHz - 100 MHz, log) x %d plane waves = %d"
+                      % (len(pool), len(freqs), nrhs, len(pool) * len(freqs)),
+           "unknowns": sorted(m.n_edges + m.n_nodes for m, _ in pool), "workers": workers}
+    for arm, fn in (("mixed", mixed_mesh), ("plain", plain_mesh)):
+        lib.peec_gb300_synchronize()
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+            res = list(ex.map(fn, order))
+        span = time.perf_counter() - t0
+        be = np.concatenate([r["be"] for r in res])
+        ok = int(np.sum(be <= 1e-10))
+        out[arm] = {"value": ok / span, "unit": "systems/s", "systems": int(be.size), "at_gate": ok,
+                    "wall_s": span, "max_backward_error": float(np.max(be))}
+        if arm == "mixed":
+            fb = np.concatenate([r["fb"] for r in res])
+            out[arm]["graph_replays_at_gate"] = int(np.sum(fb == 0))
+            out[arm]["fallback_mixed_ladder"] = int(np.sum(fb == 1))
+            out[arm]["fallback_fp64"] = int(np.sum(fb == 2))
+            out[arm]["tuning"] = {str(r["n"]): {"split_terms": r["tuning"][0], "sweeps": r["tuning"][1],
+                                                "tile_bn": r["tuning"][2], "graph_ms_per_system": r["graph_ms"]}
+                                  for r in res}
+        else:
+            out[arm]["frequency_stride"] = plain_stride
+    out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
+    for m, _ in pool:
+        m.close()
+    return out
+
+
+def ds_abi():
+    from peeeeeeeeeeeeeeeeeeec_gb300 import abi
+    return abi
+
+
+def ds_opts(lib):
+    abi = ds_abi()
+    lo, po = abi.InductanceOptions(), abi.PotentialOptions()
+    lib.inductance_options_default(C.byref(lo), 1)
+    lib.potential_options_default(C.byref(po), 1)
+    return lo, po
+
+
+def serving_leg(lib, window_s, workers, lightning_steps=4096):
+    """Poisson arrivals at 200 requests/s over window_s, two request types:
+    70% harmonic requests (seeded boxes / plates of 500-12000 unknowns,
+    1-100 MHz, 1-64 plane waves) and 30% lightning runs on the 5 cm box
+    (10/350 us 100 kA stroke at a seeded top-face node, returned at node 0,
+    lightning_steps trapezoidal steps of 0.1 us on the device-resident
+    factor).  Replayed once with the mixed-precision harmonic solve and once
+    with the plain FP64 LU through one server (150 GB budget) whose Lp / P
+    and transient caches were warmed first.  Latency = completion -
+    submission on the server clock, per request type."""
+    from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
+    from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
     from peeeeeeeeeeeeeeeeeeec_gb300.server import Server
     pool = W.serving_meshes(seed=5, count=6)
-    reqs = W.harmonic_requests(seed=7, n_meshes=len(pool), rate_hz=200.0, window_s=window_s)
-    out = {"arrivals": "Poisson 200/s over %.2f s: %d requests" % (window_s, len(reqs)),
-           "meshes": ["%s, N=%d" % (d, m.n_edges + m.n_nodes) for m, d in pool], "workers": workers,
-           "hbm_budget_gb": 150}
+    box = SynthMesh.box(*BOX)
+    box_key = 1000
+    xyz = box.array("xyz", (box.n_nodes, 3))
+    top = np.flatnonzero(xyz[:, 2] >= xyz[:, 2].max() - 1e-12)
+    reqs = W.serving_mix(seed=7, n_meshes=len(pool), rate_hz=200.0, window_s=window_s, top_nodes=top)
+    LW = W.LIGHTNING_10_350
+    n_l = sum(1 for r in reqs if r[0] == "lightning")
+    out = {"arrivals": "Poisson 200/s over %.2f s: %d requests (%d harmonic, %d lightning)"
+                       % (window_s, len(reqs), len(reqs) - n_l, n_l),
+           "meshes": ["%s, N=%d" % (d, m.n_edges + m.n_nodes) for m, d in pool],
+           "lightning": "box %gx%gx%g m (N=%d), %d steps, dt 0.1 us, trapezoidal, 10/350 us 100 kA"
+                        % (BOX[0], BOX[1], BOX[2], box.n_edges + box.n_nodes, lightning_steps),
+           "workers": workers, "hbm_budget_gb": 150}
+
+    def lightning(srv, strike, steps):
+        return srv.submit_transient(box, box_key, steps, (LW["K"], LW["alpha"], LW["beta"], LW["delay"], strike, 0),
+                                    scheme=2, dt=1e-7, probe_nodes=[strike])
+
     with Server(150 << 30, workers) as srv:
         warm = [srv.submit(m, i, 30e6, [[0.0, 0.0, -1.0]], [[1.0, 0.0, 0.0]], mixed=True)
                 for i, (m, _) in enumerate(pool)]
+        warm.append(lightning(srv, int(top[0]), 8))
         for t in warm:
             srv.wait(t)
         for mode in ("mixed", "plain"):
             t0 = time.perf_counter()
             tickets = []
-            for (ta, mi, f, k, e) in reqs:
-                d = t0 + ta - time.perf_counter()
+            for r in reqs:
+                d = t0 + r[1] - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
-                tickets.append(srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed")))
-            res = [srv.wait(t)[1] for t in tickets]
-            lat = np.array([r["t_end"] - r["t_submit"] for r in res])
-            span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
-            ok = sum(1 for r in res if r["status"] == 0 and r["backward_error"] <= 1e-10)
-            out[mode] = {"value": ok / span, "unit": "solves/s", "completed_at_gate": ok, "requests": len(res),
-                         "p50_latency_s": float(np.percentile(lat, 50)),
-                         "p99_latency_s": float(np.percentile(lat, 99)), "makespan_s": span,
-                         "max_backward_error": max(r["backward_error"] for r in res)}
+                if r[0] == "lightning":
+                    tickets.append(("lightning", lightning(srv, r[2], lightning_steps)))
+                else:
+                    _, _, mi, f, k, e = r
+                    tickets.append(("harmonic", srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed"))))
+            res = [(kind, srv.wait(t)[1]) for kind, t in tickets]
+            span = max(r["t_end"] for _, r in res) - min(r["t_submit"] for _, r in res)
+            ok_h = sum(1 for k, r in res if k == "harmonic" and r["status"] == 0 and r["backward_error"] <= 1e-10)
+            ok_l = sum(1 for k, r in res if k == "lightning" and r["status"] == 0)
+            per = {}
+            for kind in ("harmonic", "lightning"):
+                lat = np.array([r["t_end"] - r["t_submit"] for k, r in res if k == kind])
+                if lat.size:
+                    per[kind] = {"requests": int(lat.size), "p50_latency_s": float(np.percentile(lat, 50)),
+                                 "p99_latency_s": float(np.percentile(lat, 99))}
+            lat_all = np.array([r["t_end"] - r["t_submit"] for _, r in res])
+            hb = [r["backward_error"] for k, r in res if k == "harmonic"]
+            out[mode] = {"value": ok_h / span, "unit": "harmonic solves/s", "completed_at_gate": ok_h,
+                         "lightning_runs_completed": ok_l, "lightning_runs_per_s": ok_l / span,
+                         "requests_per_s": (ok_h + ok_l) / span, "requests": len(res),
+                         "p50_latency_s": float(np.percentile(lat_all, 50)),
+                         "p99_latency_s": float(np.percentile(lat_all, 99)), "per_type": per, "makespan_s": span,
+                         "fallbacks_to_fp64": sum(r.get("fallback", 0) for k, r in res if k == "harmonic"),
+                         "max_backward_error": max(hb) if hb else None}
     out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
     for m, _ in pool:
         m.close()
+    box.close()
     return out
 
 
@@ -654,74 +911,50 @@ def geometry_bytes(m):
 
 
 # ---------------------------------------------------------------------
-# CPU: the reference algorithm (oracle) on a bounded sample
+# CPU: the reference's own code (or the oracle port) on a bounded sample
 # ---------------------------------------------------------------------
-def cpu_sample_solve_seconds(m, threads, budget_rows=(48, 48), lu_n=1600):
-    """Seconds for one full solve on `threads` host cores, extrapolated from
-    a sample: the first rows of the Lp and P upper triangles (scaled by the
-    number of entry pairs), and a complex LU + solve of size lu_n (scaled by
-    (N/lu_n)^3 and (N/lu_n)^2)."""
+def cpu_reference(prefer="reference"):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    from oracle import Oracle
-    orc = Oracle()
-    ne, nv = m.n_edges, m.n_nodes
-    n = ne + nv
-    parts = {}
-    t = time.perf_counter()
-    s, _ = orc.inductance(m, threads=threads, rows=(0, budget_rows[0]))
-    tl = time.perf_counter() - t
-    assert s == 0
-    pairs_s = sum(ne - a for a in range(budget_rows[0]))
-    parts["Lp"] = tl * (ne * (ne + 1) / 2) / pairs_s
-    t = time.perf_counter()
-    s, _ = orc.potential(m, threads=threads, rows=(0, budget_rows[1]))
-    tp = time.perf_counter() - t
-    assert s == 0
-    pairs_s = sum(nv - a for a in range(budget_rows[1]))
-    parts["P"] = tp * (nv * (nv + 1) / 2) / pairs_s
-    rng = np.random.default_rng(0)
-    a = rng.standard_normal((lu_n, lu_n)) + 1j * rng.standard_normal((lu_n, lu_n))
-    t = time.perf_counter()
-    s, lu, piv, _, _, rs, cs = orc.complex_lu_factorize(a, threads=threads)
-    tf = time.perf_counter() - t
-    t = time.perf_counter()
-    orc.complex_lu_solve(lu, piv, rs, cs, a[0])
-    ts = time.perf_counter() - t
-    parts["complex_lu"] = tf * (n / lu_n) ** 3
-    parts["solve"] = ts * (n / lu_n) ** 2
-    sample_s = tl + tp + tf + ts
-    desc = ("Lp rows 0-%d and P rows 0-%d of the upper triangle (scaled by entry-pair count), complex LU + "
-            "solve at n=%d (scaled by (N/n)^3, (N/n)^2); oracle restatement, %d threads"
-            % (budget_rows[0], budget_rows[1], lu_n, threads))
-    return sum(parts.values()), parts, sample_s, desc
+    from cpu_baseline import CpuReference
+    return CpuReference(prefer)
 
 
-# ---------------------------------------------------------------------
 def run_reference(args, rank, world):
+    """The reference's CPU path on this host's cores (rank 0 only): each step
+    is one bounded sample of the 5 cm box solve (oracle/cpu_baseline.py),
+    extrapolated to one full solve; value = 1 / median extrapolated seconds.
+    ms_per_step is the measured wall time of one sample.  After the timed
+    steps, one smaller sample on one thread."""
     if rank != 0:
         return
-    m = make_mesh()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from cpu_baseline import run_steps
+    impl = cpu_reference()
     threads = os.cpu_count()
-    times = []
-    last = None
-    for i in range(args.warmup + args.steps):
-        sec, parts, sample_s, desc = cpu_sample_solve_seconds(m, threads, budget_rows=(16, 16), lu_n=1000)
-        if i >= args.warmup:
-            times.append(sec)
-        last = (parts, sample_s, desc)
-    t = statistics.median(times)
-    v = 1.0 / t
-    ref_kind = "reference" if os.path.exists(os.path.join(REPO, "oracle", "_ref", "libpeec_ref.so")) else "port"
+    t0 = time.perf_counter()
+    impl.mesh(BOX)
+    impl.solve_chain(FREQ, threads)  # set-up: the 2102-unknown system's Lp / P
+    setup_s = time.perf_counter() - t0
+    sec, parts, measured, desc = run_steps(impl, BOX, FREQ, threads, args.steps, args.warmup)
+    sec1, parts1, measured1, desc1 = run_steps(impl, BOX, FREQ, 1, 1, 0, rows=(8, 8))
+    v = 1.0 / sec
+    m = impl.mesh(BOX)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": measured * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n_unknowns": m.n_edges + m.n_nodes, "Ne": m.n_edges,
-                       "Nv": m.n_nodes, "frequency_hz": FREQ, "parallelism": "cpu",
-                       "note": "bounded sample per step extrapolated to one full solve"},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": last[2], "phase_seconds": last[0]},
+                       "Nv": m.n_nodes, "frequency_hz": FREQ, "parallelism": "cpu (%d threads)" % threads,
+                       "note": "each step: one bounded sample (ms_per_step is its measured wall time), "
+                               "extrapolated to one full solve (value = 1 / median extrapolated seconds)"},
+            "solve_seconds_extrapolated": sec, "setup_seconds": setup_s,
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": impl.kind,
+                             "library": os.path.relpath(impl.path, REPO), "sample": desc,
+                             "phase_seconds": {k: round(x, 3) for k, x in parts.items()},
+                             "one_thread": {"value": 1.0 / sec1, "unit": "solves/s", "cores": 1,
+                                            "solve_seconds_extrapolated": sec1,
+                                            "phase_seconds": {k: round(x, 3) for k, x in parts1.items()},
+                                            "sample": desc1, "sample_seconds": measured1}},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    line["cpu_baseline"]["kind"] = "port" if ref_kind == "port" else "port"
     print(json.dumps(line))
 
 
@@ -740,6 +973,9 @@ def main():
     ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--batch", default="8x8", help="meshes x frequencies of the batched leg (0: skip)")
+    ap.add_argument("--config4", default=None,
+                    help="only the batched sweep, meshes x frequencies (e.g. 48x64): sweep graphs vs plain FP64 LU")
+    ap.add_argument("--config4-plain-stride", type=int, default=1)
     ap.add_argument("--config3", action="store_true",
                     help="only the 2.5 cm retarded box (33602 unknowns): mixed solve + FP64 LU reference")
     args = ap.parse_args()
@@ -765,6 +1001,14 @@ def main():
     if args.config3:
         if rank == 0:
             config3(lib)
+        return
+    if args.config4:
+        if rank == 0:
+            nm, nf = (int(v) for v in args.config4.split("x"))
+            res = config4(lib, nm, nf, workers=args.serve_workers, plain_stride=args.config4_plain_stride)
+            print(json.dumps({"metric": "config 4 batched sweep: systems/s at <=1e-10 backward error",
+                              "value": res["mixed"]["value"], "unit": "systems/s", "batched": res,
+                              "data": "synthetic (seeded meshes and plane waves)"}), flush=True)
         return
     m = make_mesh()
     ds = DeviceSolve(lib, m)
@@ -856,6 +1100,9 @@ def main():
     lib.peec_gb300_pipe_peaks(C.byref(p64), C.byref(p32))
     transient = transient_leg(lib, ds, args.transient_steps) if args.transient_steps > 0 else None
     retarded = None if args.no_retarded else retarded_leg(lib, ds)
+    if retarded is not None:
+        retarded["plain_fp64_solve"] = retarded_plain_leg(lib, ds)
+    far_precision = far_precision_leg(lib, ds)
     ds.free()
     serving = serving_leg(lib, args.serve_window, args.serve_workers) if args.serve_window > 0 else None
     batched = None
@@ -880,9 +1127,13 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        sec, parts, sample_s, desc = cpu_sample_solve_seconds(m, os.cpu_count())
-        cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": desc, "sample_seconds": round(sample_s, 2),
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        from cpu_baseline import run_steps
+        impl = cpu_reference()
+        sec, parts, measured, desc = run_steps(impl, BOX, FREQ, os.cpu_count(), 1, 0)
+        cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": os.cpu_count(), "kind": impl.kind,
+               "library": os.path.relpath(impl.path, REPO), "sample": desc,
+               "sample_seconds": round(measured, 2),
                "phase_seconds": {k: round(v, 2) for k, v in parts.items()}}
 
     roofs = roofline(phases, lu_phases, m, p64.value, p32.value, ds.work)
@@ -922,7 +1173,7 @@ def main():
                 "phase_ms": phases, "work": ds.work, "backward_error": max(bes), "gpu_launches": int(launches),
                 "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
                 "lu_phases": lu_phases, "mixed": mixed, "serving": serving, "batched": batched, "transient": transient, "retarded": retarded,
-                "rcs": rcs, "incidence": incidence,
+                "rcs": rcs, "incidence": incidence, "far_precision": far_precision,
                 "pipe_peaks_tflops": {"fp64": p64.value, "fp32": p32.value,
                                       "how": "FMA loops on this GPU (the pool's measured peaks cover HBM and BF16)"},
                 "rooflines": roofs, "roofline": max(roofs, key=lambda r: r["ms"]) if roofs else None}
@@ -979,7 +1230,7 @@ def roofline(phases, lu, m, fp64_peak, fp32_peak, work):
                         "peak_source": "measured FP32 FMA rate / %d FP32 instructions per point pair"
                                        % DF_FP32_INSTR_PER_PAIR})
     if phases.get("mna_fill"):
-        b = 16.0 * n * n + 8.0 * ne * ne
+        b = 16.0 * n * n + 8.0 * ne * ne + 8.0 * nv * nv  # Z written, Lp read, P read (its rows gathered)
         a = b / (phases["mna_fill"] * 1e-3) / 1e9
         out.append({"kernel": "k_harmonic_fill (MNA matrix Z)", "bound": "hbm", "achieved": a, "peak": hbm,
                     "unit": "GB/s", "frac": a / hbm, "ms": phases["mna_fill"], "traffic": traffic.get("k_harmonic_fill"),

@@ -14,6 +14,9 @@ reference's).
   directions and transverse polarisations, Poisson arrival times.
 * batch_systems: every mesh of a pool at log-spaced frequencies with a
   fixed number of plane waves (the many-meshes x many-frequencies sweep).
+* serving_mix: the two request types of the serving workload on one Poisson
+  arrival stream: a fraction of lightning runs (a seeded strike node on the
+  box's top face) and harmonic requests as harmonic_requests draws them.
 """
 import numpy as np
 
@@ -106,3 +109,23 @@ def batch_systems(seed, n_meshes, n_freqs, f_lo=1e3, f_hi=1e8, nrhs=4):
             k, e = plane_waves(rng, nrhs)
             out.append((mi, float(f), k, e))
     return out
+
+
+def serving_mix(seed, n_meshes, rate_hz, window_s, top_nodes, lightning_fraction=0.3, max_rhs=64):
+    """Poisson arrivals over window_s of both request types:
+    [("harmonic", t, mesh index, frequency, k_hat, e_hat)] and
+    [("lightning", t, strike node)] merged in arrival order; each arrival
+    is a lightning run with probability lightning_fraction."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    top_nodes = np.asarray(top_nodes)
+    while True:
+        t += rng.exponential(1.0 / rate_hz)
+        if t > window_s:
+            return out
+        if rng.random() < lightning_fraction:
+            out.append(("lightning", t, int(rng.choice(top_nodes))))
+            continue
+        q = int(rng.integers(1, max_rhs + 1))
+        k, e = plane_waves(rng, q)
+        out.append(("harmonic", t, int(rng.integers(0, n_meshes)), float(rng.uniform(1e6, 100e6)), k, e))
