@@ -3,8 +3,8 @@
  * edge e = a -> b) and the dense products the PEEC systems use.  The O(N^2)
  * products run on the GPU (csrc/incidence.cu); results are host arrays as in
  * the reference.  Device-resident forms are in peec_gb300.h. */
-#ifndef PEEC_GB300_INCIDENCE_H
-#define PEEC_GB300_INCIDENCE_H
+#ifndef PEEC_INCIDENCE_H
+#define PEEC_INCIDENCE_H
 
 #include <stddef.h>
 

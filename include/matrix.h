@@ -3,8 +3,8 @@
  * owned by the caller and released with the reference's matrix_free
  * (free(data), then zero the struct).  The incidence products of
  * incidence.h fill one; the library allocates data with calloc. */
-#ifndef PEEC_GB300_MATRIX_H
-#define PEEC_GB300_MATRIX_H
+#ifndef PEEC_MATRIX_H
+#define PEEC_MATRIX_H
 
 #include <stddef.h>
 

@@ -5,8 +5,8 @@
  * byte-identical to the reference's; dense values are formatted by parallel
  * host threads and written in order.  Return 0, or -1 on NULL / empty input
  * or a file that cannot be opened. */
-#ifndef PEEC_GB300_MATRIX_EXPORT_H
-#define PEEC_GB300_MATRIX_EXPORT_H
+#ifndef PEEC_MATRIX_EXPORT_H
+#define PEEC_MATRIX_EXPORT_H
 
 #include <stddef.h>
 

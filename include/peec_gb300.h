@@ -110,10 +110,23 @@ int peec_gb300_complex_lu_factor_device(Complex *d_a, size_t n, double pivot_tol
  * up the array's device address with that device current: make that first
  * call before any stream capture.  Every call reuses the same array and
  * clears it on entry, so calls that overlap on the GPU (for instance from two
- * host threads) race with each other: serialise them. */
+ * host threads) race with each other: serialise them.  The call synchronises
+ * the library stream before returning (it reads the matrix scale and the
+ * status back).  The device address is looked up once per device and kept,
+ * so do not keep using the library on a device after cudaDeviceReset. */
 int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double pivot_tolerance,
                                         long long *d_piv, int *d_perm,
                                         double *matrix_scale, int *failed_column);
+/* Device copies of host factorisations (lu_factorize / complex_lu_factorize
+ * results) stay registered for later lu_solve / complex_lu_solve calls.
+ * trust = 0 (default): every solve uploads the caller's current host factor
+ * into the registered buffers, so edits of the factor between calls are
+ * seen.  trust = 1: a registered copy is reused without re-reading the host
+ * factor while the pointer, size, pivots, scales, diagonal and a strided
+ * sample of 4093 entries are unchanged; set it only if no factor is edited
+ * between solves.  Returns the previous setting. */
+int peec_gb300_set_factor_cache(int trust);
+
 /* nrhs right-hand sides stored one after another; d_b != d_x. */
 int peec_gb300_lu_solve_device(const double *d_lu, const int *d_perm, size_t n,
                                const double *d_b, double *d_x, size_t nrhs);
@@ -240,8 +253,11 @@ int peec_gb300_harmonic_build_device(const double *d_L, const double *d_P,
                                      const int *d_edges, const double *d_R,
                                      size_t n_edges, size_t n_nodes, double frequency,
                                      Complex *d_Z);
-/* [-U_e; 0] for a unit plane wave e_hat exp(-j k0 k_hat.r), U_e the field at
- * the edge centre projected on the edge vector times sinc(k0 k_hat.l / 2). */
+/* [-U_e; 0] for a plane wave e_hat exp(-j k0 k_hat.r), U_e the field at the
+ * edge centre projected on the edge vector times sinc(k0 k_hat.l / 2): the
+ * reference's scattering_build_harmonic_excitation with the analytic edge
+ * integral (scattering.c:140-336) for a COMPLEX wave of zero phase whose
+ * k_hat and E0 (= e_hat) come from incident_field_configure_harmonic. */
 int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
                                      const double *d_edge_vectors, size_t n_edges,
                                      size_t n_nodes, const double k_hat[3],
@@ -253,6 +269,45 @@ int peec_gb300_plane_wave_rhs_device(const double *d_edge_centers,
  * out[2] = max |b_i|. */
 int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex *d_x,
                                      const Complex *d_b, size_t nrhs, double out[3]);
+
+/* ---- batched frequency sweep (no reference counterpart) ----
+ * The harmonic systems of one mesh at many frequencies, each with nrhs
+ * plane waves, solved by the mixed-precision solve recorded once into a
+ * CUDA graph and replayed per frequency (omega and k0 are device data of the
+ * graph).  A plan keeps pointers to the caller's device Lp, P, edge list,
+ * resistance diagonal (NULL: PEC), edge centres and edge vectors (keep them
+ * valid while it lives) and copies the waves (k_hat, e_hat: host [nrhs][3]).
+ * Different meshes' plans run from different host threads to overlap. */
+typedef struct
+{
+    int split_terms; /* split-BF16 products of the FP32 factorisation: 3 or 6 */
+    int sweeps;      /* FP64 refinement sweeps recorded in the graph        */
+    int tile_bn;     /* width of the wide tensor-core update tiles: 64, 128, or 0 (by shape) */
+} PeecSweepTuning;
+
+/* NULL on invalid input or allocation failure.  tuning NULL: {3, 4, 0}. */
+void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R,
+                              const double *d_edge_centers, const double *d_edge_vectors, size_t n_edges,
+                              size_t n_nodes, size_t nrhs, const double *k_hat, const double *e_hat,
+                              const PeecSweepTuning *tuning);
+/* Autotuner: solves the systems at the probe frequencies with the adaptive
+ * mixed solve to learn the split terms and sweeps they need (plus one sweep
+ * of margin), then records and times the graph with 128- and 64-column
+ * tiles for the wide updates at the middle probe and keeps the faster.
+ * chosen / ms_per_system (graph replay time of one system) may be NULL. */
+int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_probe,
+                          PeecSweepTuning *chosen, double *ms_per_system);
+/* Solves every frequency: d_X (device) [n_freq][nrhs][Ne + Nv].  A system
+ * whose backward error after the recorded sweeps is above tol is solved
+ * again outside the graph (mixed solve with its precision ladder; then the
+ * FP64 LU with FP64 refinement).  backward_error[f] (host) is its final
+ * componentwise backward error; fallback[f] 0 graph, 1 mixed ladder, 2 FP64.
+ * Returns 0 when every system reached tol, 1 when some did not, -1 on
+ * errors. */
+int peec_gb300_sweep_run(void *plan, const double *frequencies, size_t n_freq, double tol,
+                         Complex *d_X, double *backward_error, int *fallback);
+int peec_gb300_sweep_tuning(void *plan, PeecSweepTuning *tuning);
+void peec_gb300_sweep_destroy(void *plan);
 
 /* ---- retarded Lp / P (no reference counterpart: the reference's
  * retardation.c is empty) ----

@@ -212,6 +212,10 @@ class PeecRequestResult(C.Structure):
                 ("t_submit", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double)]
 
 
+class PeecSweepTuning(C.Structure):
+    _fields_ = [("split_terms", C.c_int), ("sweeps", C.c_int), ("tile_bn", C.c_int)]
+
+
 # include/peec_gb300.h
 EXT_SYMBOLS = [
     ("peec_gb300_device_ready", C.c_int, []),
@@ -247,6 +251,15 @@ EXT_SYMBOLS = [
     ("peec_gb300_complex_lu_solve_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
       C.c_size_t]),
+    ("peec_gb300_set_factor_cache", C.c_int, [C.c_int]),
+    ("peec_gb300_sweep_create", C.c_void_p,
+     [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t,
+      c_double_p, c_double_p, P(PeecSweepTuning)]),
+    ("peec_gb300_sweep_tune", C.c_int, [C.c_void_p, c_double_p, C.c_size_t, P(PeecSweepTuning), c_double_p]),
+    ("peec_gb300_sweep_run", C.c_int,
+     [C.c_void_p, c_double_p, C.c_size_t, C.c_double, C.c_void_p, c_double_p, c_int_p]),
+    ("peec_gb300_sweep_tuning", C.c_int, [C.c_void_p, P(PeecSweepTuning)]),
+    ("peec_gb300_sweep_destroy", None, [C.c_void_p]),
     ("peec_gb300_lu_timing_enable", None, [C.c_int]),
     ("peec_gb300_lu_timing", C.c_int, [c_double_p, c_double_p, c_double_p, c_double_p]),
     ("peec_gb300_lu_timing_trailing", C.c_int, [c_double_p, c_double_p]),

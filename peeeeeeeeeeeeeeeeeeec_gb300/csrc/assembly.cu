@@ -1930,7 +1930,11 @@ static int run_assembly(DeviceRegions &D, int kind, const AssemblyOptions &o, do
     T.pts = pts.p;
     T.ptf = ptf.p;
     T.npts = npts;
-    T.far_df = far_mode_df();
+    // The double-float and FP32 far loops carry no R <= 0 test, which relies
+    // on FAR patches being apart: true for near_factor > 0 (a positive box
+    // gap).  With near_factor == 0 overlapping patches are FAR, so the FP64
+    // form, which skips R <= 0 as the reference does, takes them.
+    T.far_df = o.near_factor > 0.0 ? far_mode_df() : 0;
     T.near_off = near_off.p;
     T.near_rec = rec.p;
     T.near_k = kval.p;

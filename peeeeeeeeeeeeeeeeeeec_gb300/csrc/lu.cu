@@ -26,6 +26,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <complex>
 #include <list>
 #include <mutex>
@@ -33,6 +34,7 @@
 #include <vector>
 
 #include "../../include/complex_lu.h"
+#include "mixed_capture.cuh"
 #include "../../include/lu.h"
 #include "../../include/peec_gb300.h"
 #include <cooperative_groups.h>
@@ -52,7 +54,7 @@ struct cplx {
 
 // ---- scalar traits --------------------------------------------------
 __device__ __forceinline__ double mag(double v) { return fabs(v); }
-__device__ __forceinline__ double mag(cplx v) { return hypot(v.re, v.im); }
+__device__ __forceinline__ double mag(cplx v) { return hypot_cr(v.re, v.im); }
 __device__ __forceinline__ double divide(double a, double b) { return a / b; }
 // complex_lu.c:168-190: (a conj(b)) / |b|^2 without scaling
 __device__ __forceinline__ cplx divide(cplx a, cplx b) {
@@ -259,7 +261,7 @@ struct MagType<cplxf> {
     using type = float;
 };
 __device__ __forceinline__ double mag_t(double v) { return fabs(v); }
-__device__ __forceinline__ double mag_t(cplx v) { return hypot(v.re, v.im); }
+__device__ __forceinline__ double mag_t(cplx v) { return hypot_cr(v.re, v.im); }
 __device__ __forceinline__ float mag_t(cplxf v) { return hypotf(v.re, v.im); }
 
 struct PanelSlots {
@@ -1935,7 +1937,7 @@ __global__ void k_row_scale(const cplx *in, cplx *out, int n, double *row_scale,
     double s = 0.0;
     int bad = 0;
     for (int j = lane; j < n; j += 32) {
-        double m = hypot(row[j].re, row[j].im);
+        double m = hypot_cr(row[j].re, row[j].im);
         if (!isfinite(m)) bad = 1;
         s = fmax(s, m);
     }
@@ -1964,7 +1966,7 @@ __global__ void __launch_bounds__(256) k_col_max(const cplx *a, int n, double *c
     const int j = blockIdx.x * 32 + lane;
     double s = 0.0;
     if (j < n)
-        for (int i = warp; i < n; i += 8) s = fmax(s, hypot(a[(size_t)i * n + j].re, a[(size_t)i * n + j].im));
+        for (int i = warp; i < n; i += 8) s = fmax(s, hypot_cr(a[(size_t)i * n + j].re, a[(size_t)i * n + j].im));
     part[warp][lane] = s;
     __syncthreads();
     if (warp == 0 && j < n) {
@@ -2047,6 +2049,8 @@ struct WaveArgs {
     unsigned *flags;          // [nchunks][2][nb], zero on entry
     int *error;
     int subst;                // upper blocks by substitution (dinv's upper half from k_diag_copy_upper)
+    const int *refine_blocks;  // if set: [nb][2] (lower, upper), 1 = that diagonal block's solve takes one
+                               // step of iterative refinement after the inverse (k_diag_flags)
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -2145,6 +2149,63 @@ __global__ void __launch_bounds__(256) k_diag_copy_upper(const T *lu, int n, T *
             u = i < j ? v : divide(one_t(T{}), v);
         }
         du[t] = u;
+    }
+}
+
+// FP64 factors: the diagonal blocks whose inverse would cost the solve its
+// backward stability take one step of refinement after the inverse
+// (wave_block).  Per block and triangle, kappa = ||T||_inf ||T^-1||_inf
+// (|re| + |im| for complex entries); applying a computed inverse perturbs
+// the block's solution by up to about 64 kappa eps relative (7e-15 kappa),
+// so blocks with kappa above kRefineCondition = 1e3 (or a non-finite one)
+// get flag 1 (the step costs two more 64 x 64 products on the solve's
+// critical path, where FP64 runs at 2 FMA per clock per SM):
+// flag[2 b] for the unit lower block, flag[2 b + 1] for the upper.
+static const double kRefineCondition = 1.0e3;
+
+__device__ __forceinline__ double abs1(double v) { return fabs(v); }
+__device__ __forceinline__ double abs1(cplx v) { return fabs(v.re) + fabs(v.im); }
+
+template <class T>
+__global__ void __launch_bounds__(256) k_diag_flags(const T *lu, int n, const T *dinv, int *flag) {
+    __shared__ double nrm[4][kRB];  // row sums: |L|, |L^-1|, |U|, |U^-1|
+    const int b = blockIdx.x, r0 = b * kRB, nrow = min(kRB, n - r0);
+    const T *dl = dinv + (size_t)b * 2 * kRB * kRB, *du = dl + kRB * kRB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = warp; i < kRB; i += 8) {
+        double sl = 0.0, sli = 0.0, su = 0.0, sui = 0.0;
+        if (i < nrow)
+            for (int j = lane; j < nrow; j += 32) {
+                const double a = abs1(lu[(size_t)(r0 + i) * n + r0 + j]);
+                if (j < i) sl += a;
+                if (j == i) sl += 1.0;
+                if (j >= i) su += a;
+                sli += abs1(dl[i * kRB + j]);
+                sui += abs1(du[i * kRB + j]);
+            }
+        for (int d = 16; d > 0; d >>= 1) {
+            sl += __shfl_xor_sync(0xffffffffu, sl, d);
+            sli += __shfl_xor_sync(0xffffffffu, sli, d);
+            su += __shfl_xor_sync(0xffffffffu, su, d);
+            sui += __shfl_xor_sync(0xffffffffu, sui, d);
+        }
+        if (lane == 0) {
+            nrm[0][i] = sl;
+            nrm[1][i] = sli;
+            nrm[2][i] = su;
+            nrm[3][i] = sui;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        const int t = threadIdx.x;  // 0 lower, 1 upper
+        double a = 0.0, ai = 0.0;
+        for (int i = 0; i < nrow; ++i) {
+            a = fmax(a, nrm[2 * t][i]);
+            ai = fmax(ai, nrm[2 * t + 1][i]);
+        }
+        const double kappa = a * ai;
+        flag[2 * b + t] = !(kappa <= kRefineCondition);
     }
 }
 
@@ -2340,6 +2401,59 @@ __device__ bool wave_block(const WaveArgs<T> &A, int blk, int c0, int nr, unsign
         if (threadIdx.x == 0) st_release_u32(flags + blk, 1u);
         return true;
     }
+    if (A.refine_blocks && A.refine_blocks[2 * blk + (LOWER ? 0 : 1)]) {
+        // ill-conditioned diagonal block: x0 = D_b^-1 y, r = y - T_b x0 with
+        // the block T_b of the factor (unit lower or upper), x = x0 + D_b^-1 r
+        // -- one step of refinement makes the inverse-based block solve
+        // backward stable (its error shrinks by kappa(T_b) eps per step).
+        // S.part is free here: x0 in part[q][i][0], r in part[q][i][1].
+        for (int q = 0; q < nr; ++q) {
+            T v = zero_t<T>();
+#pragma unroll
+            for (int k = 0; k < kRB / 4; ++k) v = mac(v, S.dinv[row * kDS + qq + 4 * k], S.y[q][qq + 4 * k]);
+            v = addv(v, shfl_xor_t(v, 1));
+            v = addv(v, shfl_xor_t(v, 2));
+            if (qq == 0) S.part[q][row][0] = row < nrow ? v : zero_t<T>();
+        }
+        __syncthreads();
+        const T *trow = A.lu + (size_t)(r0 + (row < nrow ? row : 0)) * n + r0;
+        for (int q = 0; q < nr; ++q) {
+            T v = zero_t<T>();
+#pragma unroll
+            for (int k = 0; k < kRB / 4; ++k) {
+                const int c = qq + 4 * k;
+                if (row < nrow && c < nrow) {
+                    T t = zero_t<T>();
+                    if (LOWER)
+                        t = c < row ? trow[c] : (c == row ? one_t(T{}) : zero_t<T>());
+                    else if (c >= row)
+                        t = trow[c];
+                    v = mac(v, t, S.part[q][c][0]);
+                }
+            }
+            v = addv(v, shfl_xor_t(v, 1));
+            v = addv(v, shfl_xor_t(v, 2));
+            if (qq == 0) S.part[q][row][1] = row < nrow ? addv(S.y[q][row], neg_t(v)) : zero_t<T>();
+        }
+        __syncthreads();
+        for (int q = 0; q < nr; ++q) {
+            T v = zero_t<T>();
+#pragma unroll
+            for (int k = 0; k < kRB / 4; ++k) v = mac(v, S.dinv[row * kDS + qq + 4 * k], S.part[q][qq + 4 * k][1]);
+            v = addv(v, shfl_xor_t(v, 1));
+            v = addv(v, shfl_xor_t(v, 2));
+            if (qq == 0 && row < nrow) {
+                v = addv(S.part[q][row][0], v);
+                A.x[(size_t)(c0 + q) * n + r0 + row] = v;
+                if (!LOWER && A.col_scale)
+                    A.out[(size_t)(c0 + q) * n + r0 + row] = scale_div(v, A.col_scale[r0 + row]);
+            }
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release_u32(flags + blk, 1u);
+        return true;
+    }
     // x_b = D_b^-1 y: four threads per row, interleaved columns qq + 4k
     for (int q = 0; q < nr; ++q) {
         T v = zero_t<T>();
@@ -2395,14 +2509,24 @@ static size_t wave_flag_count(int n, int nrhs) {
 }
 
 // Elements of the diagonal-block inverses of an n x n factor.
+// Elements (of 8 bytes or more) of the diagonal-block inverses of an n x n
+// factor, followed by 2 nb ints: the per-block refinement flags of the FP64
+// solves (k_diag_flags).
 static size_t wave_dinv_count(int n) {
     int nb = (n + kRB - 1) / kRB;
-    return (size_t)nb * 2 * kRB * kRB;
+    return (size_t)nb * 2 * kRB * kRB + ((size_t)2 * nb * sizeof(int) + 7) / 8;
+}
+
+template <class T>
+static int *wave_refine_flags(T *dinv, int n) {
+    int nb = (n + kRB - 1) / kRB;
+    return reinterpret_cast<int *>(dinv + (size_t)nb * 2 * kRB * kRB);
 }
 
 // Computes the diagonal-block inverses of the factor into dinv; with subst
 // the upper half then holds the transposed upper blocks for substitution
-// (WaveArgs::subst).
+// (WaveArgs::subst).  FP64 factors also get the per-block refinement flags
+// (k_diag_flags; WaveArgs::refine_blocks = wave_refine_flags(dinv)).
 template <class T>
 static bool wave_prepare(const T *lu, int n, T *dinv, bool subst = false) {
     constexpr size_t smem = (size_t)3 * kRB * kRS * sizeof(T);
@@ -2411,7 +2535,12 @@ static bool wave_prepare(const T *lu, int n, T *dinv, bool subst = false) {
     if (!cuda_ok(attr, "diagonal block inverse smem attribute")) return false;
     int nb = (n + kRB - 1) / kRB;
     PEEC_LAUNCH(k_diag_inverse<T>, nb, 128, smem, lu, n, dinv);
-    if (subst) PEEC_LAUNCH(k_diag_copy_upper<T>, nb, 256, 0, lu, n, dinv);
+    if (subst) {
+        PEEC_LAUNCH(k_diag_copy_upper<T>, nb, 256, 0, lu, n, dinv);
+    } else if constexpr (sizeof(T) == sizeof(double) || sizeof(T) == sizeof(cplx)) {
+        if constexpr (!std::is_same<T, cplxf>::value)
+            PEEC_LAUNCH(k_diag_flags<T>, nb, 256, 0, lu, n, dinv, wave_refine_flags(dinv, n));
+    }
     return launch_ok("diagonal block inverses");
 }
 
@@ -2452,6 +2581,7 @@ bool wave_solve_real(const double *lu, const double *dinv, const int *perm, int 
     WaveArgs<double> A{};
     A.lu = lu;
     A.dinv = dinv;
+    A.refine_blocks = wave_refine_flags(const_cast<double *>(dinv), n);
     A.n = n;
     A.nrhs = nrhs;
     A.perm = perm;
@@ -2477,6 +2607,15 @@ struct Resident {
     unsigned long long fingerprint = 0;
     size_t bytes = 0;
 };
+
+// Reuse of device factor copies across *_solve calls without re-reading the
+// host factor (peec_gb300_set_factor_cache): off by default, so every solve
+// uploads the caller's current host factor into the registered device
+// buffers.  When on, a registered copy is reused while the host pointer,
+// size, pivots, scales, diagonal and a strided sample of the factor are
+// unchanged, which is only safe for callers that never edit a factor's
+// other entries between solves.
+static std::atomic<int> g_trust_factor_cache{0};
 
 static std::mutex g_reg_mu;
 static std::list<Resident> g_reg;
@@ -2537,11 +2676,20 @@ static void registry_put(Resident r) {
     g_reg.push_front(r);
 }
 
-static bool registry_get(const void *host_data, size_t n, bool cx, unsigned long long fp, Resident &out) {
+static void registry_set_fingerprint(const void *host_data, unsigned long long fp) {
+    std::lock_guard<std::mutex> g(g_reg_mu);
+    for (auto &r : g_reg)
+        if (r.host_data == host_data) r.fingerprint = fp;
+}
+
+// The registered copy of host_data with this size and type; with
+// any_content false its fingerprint must also equal fp.
+static bool registry_get(const void *host_data, size_t n, bool cx, unsigned long long fp, bool any_content,
+                         Resident &out) {
     std::lock_guard<std::mutex> g(g_reg_mu);
     for (auto it = g_reg.begin(); it != g_reg.end(); ++it)
         if (it->host_data == host_data) {
-            if (it->n != n || it->complex_ != cx || it->fingerprint != fp) return false;
+            if (it->n != n || it->complex_ != cx || (!any_content && it->fingerprint != fp)) return false;
             g_reg.splice(g_reg.begin(), g_reg, it);
             out = *it;
             return true;
@@ -2920,6 +3068,7 @@ static bool solve_device(const T *d_lu, const int *d_perm, const double *d_row, 
     WaveArgs<T> A{};
     A.lu = d_lu;
     A.dinv = dinv.p;
+    A.refine_blocks = wave_refine_flags(dinv.p, n);
     A.n = n;
     A.nrhs = nrhs;
     A.perm = d_perm;
@@ -2949,6 +3098,8 @@ using namespace peec;
 // C ABI: lu.h
 // =====================================================================
 extern "C" {
+
+int peec_gb300_set_factor_cache(int trust) { return g_trust_factor_cache.exchange(trust ? 1 : 0); }
 
 void lu_options_default(LUOptions *options, int parallel_threads) {
     if (!options) return;
@@ -3099,14 +3250,48 @@ static int factorize_common(const T *input, size_t n, double pivot_tolerance, bo
     return 0;
 }
 
-// Device copy of a host factorisation: the registry's if the fingerprint
-// matches, else uploaded now (and registered).
+template <class T>
+static bool upload_factor(Resident &r, const T *data, const size_t *pivots, const double *rs, const double *cs,
+                          size_t n, bool cx) {
+    std::vector<long long> piv(n);
+    for (size_t k = 0; k < n; ++k) {
+        if (pivots[k] >= n) return false;
+        piv[k] = (long long)pivots[k];
+    }
+    bool ok = cuda_ok(cudaMemcpyAsync(r.d_lu, data, n * n * sizeof(T), cudaMemcpyHostToDevice, stream()), "factor upload") &&
+              cuda_ok(cudaMemcpyAsync(r.d_piv, piv.data(), n * sizeof(long long), cudaMemcpyHostToDevice, stream()),
+                      "pivot upload");
+    if (cx && ok)
+        ok = cuda_ok(cudaMemcpyAsync(r.d_row, rs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload") &&
+             cuda_ok(cudaMemcpyAsync(r.d_col, cs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload");
+    size_t perm_smem = n * sizeof(int);
+    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
+    if (ok) PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, (int)n, r.d_perm, (const Status *)nullptr);
+    return ok && sync("factor upload");
+}
+
+// Device copy of a host factorisation: the registered buffers, refreshed
+// from the host factor (or reused unread when the cache is trusted and the
+// fingerprint matches), else new buffers uploaded now and registered.
 template <class T>
 static bool resident_for(const T *data, const size_t *pivots, const double *rs, const double *cs, size_t n, bool cx,
                          Resident &out) {
     unsigned long long fp = fingerprint(data, pivots, rs, cs, n, cx);
-    if (registry_get(data, n, cx, fp, out)) return true;
     Resident r;
+    if (registry_get(data, n, cx, g_trust_factor_cache.load() ? fp : 0, !g_trust_factor_cache.load(), r)) {
+        if (g_trust_factor_cache.load()) {
+            out = r;
+            return true;
+        }
+        if (!upload_factor<T>(r, data, pivots, rs, cs, n, cx)) {
+            registry_drop(data);
+            return false;
+        }
+        registry_set_fingerprint(data, fp);
+        out = r;
+        return true;
+    }
+    r = Resident();
     r.host_data = data;
     r.n = n;
     r.complex_ = cx;
@@ -3119,28 +3304,8 @@ static bool resident_for(const T *data, const size_t *pivots, const double *rs, 
         r.d_row = (double *)dalloc(n * sizeof(double));
         r.d_col = (double *)dalloc(n * sizeof(double));
     }
-    if (!r.d_lu || !r.d_piv || !r.d_perm || (cx && (!r.d_row || !r.d_col))) {
-        release(r);
-        return false;
-    }
-    std::vector<long long> piv(n);
-    for (size_t k = 0; k < n; ++k) {
-        if (pivots[k] >= n) {
-            release(r);
-            return false;
-        }
-        piv[k] = (long long)pivots[k];
-    }
-    bool ok = cuda_ok(cudaMemcpyAsync(r.d_lu, data, n * n * sizeof(T), cudaMemcpyHostToDevice, stream()), "factor upload") &&
-              cuda_ok(cudaMemcpyAsync(r.d_piv, piv.data(), n * sizeof(long long), cudaMemcpyHostToDevice, stream()),
-                      "pivot upload");
-    if (cx && ok)
-        ok = cuda_ok(cudaMemcpyAsync(r.d_row, rs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload") &&
-             cuda_ok(cudaMemcpyAsync(r.d_col, cs, n * sizeof(double), cudaMemcpyHostToDevice, stream()), "scale upload");
-    size_t perm_smem = n * sizeof(int);
-    if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
-    if (ok) PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, r.d_piv, (int)n, r.d_perm, (const Status *)nullptr);
-    if (!ok || !sync("factor upload")) {
+    if (!r.d_lu || !r.d_piv || !r.d_perm || (cx && (!r.d_row || !r.d_col)) ||
+        !upload_factor<T>(r, data, pivots, rs, cs, n, cx)) {
         release(r);
         return false;
     }
@@ -4083,10 +4248,16 @@ extern "C" int peec_gb300_complex_refine_device(const Complex *d_Z, const Comple
     return eta <= tol ? 0 : 1;
 }
 
-extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x,
-                                                     size_t nrhs_, double tol, int max_iter, double *backward_error,
-                                                     int *iterations) {
-    using namespace peec;
+namespace peec {
+
+__global__ void k_capture_status(const Status *st, const int *werr, const unsigned long long *be,
+                                 unsigned long long *eta_out, int *status_out) {
+    *status_out = st->code ? st->code : (*werr ? 6 : 0);
+    *eta_out = *be;
+}
+
+int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x, size_t nrhs_, double tol,
+                     int max_iter, double *backward_error, int *iterations, const MixedCapture *cap) {
     if (!d_Z || !d_b || !d_x || n_ == 0 || nrhs_ == 0 || n_ > (size_t)0x7fffffff || max_iter < 1) return -1;
     const int n = (int)n_, nrhs = (int)nrhs_;
     const size_t nn = n_ * n_, nv = n_ * nrhs_;
@@ -4127,9 +4298,11 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         !lean_flag.p || !lean_idx.p || !lean_rows.p)
         return -1;
     cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
-    cudaEvent_t ev[4];
-    for (auto &e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], stream());
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (!cap) {
+        for (auto &e : ev) cudaEventCreate(&e);
+        cudaEventRecord(ev[0], stream());
+    }
     cudaMemsetAsync(scratch.p, 0, sbytes, stream());
     cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
     cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
@@ -4163,21 +4336,23 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     PEEC_LAUNCH(k_max_mag<cplxf>, 152 * 8, 256, 0, f.p, nn, mx.p);
     unsigned long long bits = 0;
     Status hs;
-    cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
-    cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
-    if (!sync("mixed equilibration")) return -1;
-    if (hs.code != 0) return -2;
-    double scale;
-    memcpy(&scale, &bits, sizeof(scale));
-    if (!isfinite(scale) || scale <= 0.0) return -2;
+    double scale = 1.0;
+    if (!cap) {
+        cudaMemcpyAsync(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, stream());
+        cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
+        if (!sync("mixed equilibration")) return -1;
+        if (hs.code != 0) return -2;
+        memcpy(&scale, &bits, sizeof(scale));
+        if (!isfinite(scale) || scale <= 0.0) return -2;
+        cudaEventRecord(ev[1], stream());
+    }
     const double limit = 1e-14 * scale;
-    cudaEventRecord(ev[1], stream());
     cplxf *a = f.p;
     LuTiming &tm = g_lu_timing;
     // split-BF16 terms of the trailing update products: BF16x3 first (about
     // 16 bits), BF16x6 (FP32-equivalent) when refinement from the BF16x3
     // factor stalls; PEEC_GB300_MIXED_SPLIT=6 starts with BF16x6
-    int T = mixed_split_terms();
+    int T = cap ? cap->split_terms : mixed_split_terms();
     // FP32 factorisation of f, trailing updates on the tensor cores: 0, -2 on
     // a pivot breakdown, -1 on errors
     auto factor = [&]() -> int {
@@ -4296,6 +4471,7 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
         size_t perm_smem = n_ * sizeof(int);
         if (perm_smem > 48 * 1024) cudaFuncSetAttribute(k_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)perm_smem);
         PEEC_LAUNCH(k_perm, 1, 1024, perm_smem, piv.p, n, perm.p, st.p);
+        if (cap) return launch_ok("mixed factorisation") ? 0 : -1;
         int herr = 0;
         cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, stream());
         cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream());
@@ -4350,6 +4526,11 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
             PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, b, n, nrhs, r.p,
                         be.p);
         };
+        if (cap) {
+            for (int it = 0; it < cap->sweeps; ++it) sweep();
+            total_it = cap->sweeps;
+            return launch_ok("refinement") ? 0 : -1;
+        }
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t gexec = nullptr;
         if (!sync("refinement setup")) return -1;
@@ -4537,6 +4718,13 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     };
     float t01 = -1.0f, ms_factor = 0.0f, ms_refine = 0.0f;
     int outcome;
+    if (cap) {
+        outcome = factor();
+        if (outcome == 0) outcome = refine();
+        if (outcome != 0) return -1;
+        PEEC_LAUNCH(k_capture_status, 1, 1, 0, st.p, werr.p, be.p, cap->d_eta_bits, cap->d_status);
+        return launch_ok("mixed solve (graph form)") ? 0 : -1;
+    }
     for (;;) {
         outcome = factor();
         cudaEventRecord(ev[2], stream());
@@ -4584,6 +4772,14 @@ extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t 
     if (iterations) *iterations = total_it;
     if (outcome == -2) return -2;
     return outcome == 0 ? 0 : 1;
+}
+
+}  // namespace peec
+
+extern "C" int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x,
+                                                     size_t nrhs_, double tol, int max_iter, double *backward_error,
+                                                     int *iterations) {
+    return peec::mixed_solve_impl(d_Z, n_, d_b, d_x, nrhs_, tol, max_iter, backward_error, iterations, nullptr);
 }
 
 namespace peec {

@@ -2,8 +2,8 @@
 // include/matrix_export.h; host code).
 //
 // Reference (paths inside the reference project):
-//   src/io/matrix_export.c:11-69     directory creation, parents first, 0755
-//   src/io/matrix_export.c:71-103    "<directory>/<file>" within 4096 bytes
+//   src/io/matrix_export.c:11-103    the directory (parents too, 0755) and
+//                                    the file paths inside it
 //   src/io/matrix_export.c:105-176   dense "array real general", values column
 //                                    by column, one "%.17e" per line
 //   src/io/matrix_export.c:178-258   incidence as 2 Ne 1-based coordinates
@@ -15,12 +15,11 @@
 // slow part (25 bytes of decimal text per value, 31 M values for the 5 cm
 // box's Lp): columns are formatted in parallel host threads, a block of
 // columns at a time, and the blocks are written in order.
-#include <errno.h>
 #include <stdio.h>
 #include <string.h>
-#include <sys/stat.h>
 
 #include <algorithm>
+#include <filesystem>
 #include <string>
 #include <thread>
 #include <vector>
@@ -29,29 +28,29 @@
 
 namespace {
 
+namespace fs = std::filesystem;
+
+// The directory and its missing parents (permissions 0755 as the
+// reference's exporter creates them); an existing directory is fine.
 int ensure_directory(const char *directory) {
     if (!directory || directory[0] == '\0') return -1;
-    char buffer[4096];
-    const size_t length = strlen(directory);
-    if (length >= sizeof(buffer)) return -1;
-    memcpy(buffer, directory, length + 1);
-    for (size_t i = 1; i <= length; ++i) {
-        if (buffer[i] != '/' && buffer[i] != '\0') continue;
-        const char saved = buffer[i];
-        buffer[i] = '\0';
-        if (buffer[0] != '\0' && mkdir(buffer, 0755) != 0 && errno != EEXIST) {
-            fprintf(stderr, "ERROR: cannot create directory '%s': %s\n", buffer, strerror(errno));
-            return -1;
-        }
-        buffer[i] = saved;
+    std::error_code ec;
+    const fs::path dir(directory);
+    if (fs::is_directory(dir, ec)) return 0;
+    fs::create_directories(dir, ec);
+    if (ec) {
+        fprintf(stderr, "ERROR: cannot create directory '%s': %s\n", directory, ec.message().c_str());
+        return -1;
     }
+    fs::permissions(dir, fs::perms::owner_all | fs::perms::group_read | fs::perms::group_exec |
+                             fs::perms::others_read | fs::perms::others_exec, ec);
     return 0;
 }
 
-int make_path(char *buffer, size_t size, const char *directory, const char *file) {
-    if (!buffer || size == 0 || !directory || !file) return -1;
-    const int written = snprintf(buffer, size, "%s/%s", directory, file);
-    return (written < 0 || (size_t)written >= size) ? -1 : 0;
+// directory / file, or an empty string when a path argument is missing.
+std::string join_path(const char *directory, const char *file) {
+    if (!directory || !file) return std::string();
+    return (fs::path(directory) / file).string();
 }
 
 // "%.17e\n" of data[row * cols + col] for rows 0.. of columns [c0, c1),
@@ -137,16 +136,14 @@ int matrix_export_peec_set(const char *directory, const Mesh *mesh, const Induct
                            const PotentialMatrix *P, const Matrix *PAT, const ResistanceMatrix *R) {
     if (!directory || !mesh || !L || !P || !PAT || !R) return -1;
     if (ensure_directory(directory) != 0) return -1;
-    char path[4096];
-    if (make_path(path, sizeof(path), directory, "L.mtx") != 0 || matrix_export_dense_mtx(path, L->data, L->n, L->n))
+    const std::string l = join_path(directory, "L.mtx"), a = join_path(directory, "A.mtx"),
+                      p = join_path(directory, "P.mtx"), pat = join_path(directory, "PAT.mtx"),
+                      r = join_path(directory, "R.mtx");
+    if (matrix_export_dense_mtx(l.c_str(), L->data, L->n, L->n) || matrix_export_incidence_mtx(a.c_str(), mesh) ||
+        matrix_export_dense_mtx(p.c_str(), P->data, P->n, P->n) ||
+        matrix_export_dense_mtx(pat.c_str(), PAT->data, PAT->rows, PAT->cols) ||
+        matrix_export_resistance_mtx(r.c_str(), R))
         return -1;
-    if (make_path(path, sizeof(path), directory, "A.mtx") != 0 || matrix_export_incidence_mtx(path, mesh)) return -1;
-    if (make_path(path, sizeof(path), directory, "P.mtx") != 0 || matrix_export_dense_mtx(path, P->data, P->n, P->n))
-        return -1;
-    if (make_path(path, sizeof(path), directory, "PAT.mtx") != 0 ||
-        matrix_export_dense_mtx(path, PAT->data, PAT->rows, PAT->cols))
-        return -1;
-    if (make_path(path, sizeof(path), directory, "R.mtx") != 0 || matrix_export_resistance_mtx(path, R)) return -1;
     printf("PEEC matrices saved : %s\n", directory);
     return 0;
 }

@@ -162,6 +162,16 @@ static bool persistent_enabled() {
     return on;
 }
 
+// Tile width of the wide (trailing) updates on this host thread: 0 picks by
+// shape (128 columns), 64 or 128 forces it.  The batched sweep's autotuner
+// sets it while it records a graph, so the choice is baked into the graph.
+static thread_local int g_tc_wide_bn = 0;
+int set_tc_wide_tile(int bn) {
+    const int prev = g_tc_wide_bn;
+    g_tc_wide_bn = (bn == 64 || bn == 128) ? bn : 0;
+    return prev;
+}
+
 // Complex C (interleaved FP32, leading dimension ldc complex elements)
 // [row0.., col0..] -= (A Br^T) + j (A Bi^T).
 bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c, int m, int n, int k, int row0,
@@ -172,7 +182,7 @@ bool tc_gemm_update_cplx(const void *a, const void *br, const void *bi, float *c
     }
     // narrow updates (the panel's K = 6 or 12 x 32, at most 256 columns):
     // 64-column tiles
-    const bool narrow = k <= 192 || (k <= 384 && n <= 256);
+    const bool narrow = k <= 192 || (k <= 384 && n <= 256) || (g_tc_wide_bn == 64);
     if (persistent_enabled() && persistent_ok(c, ldc, row0, col0))
         return narrow ? launch_tc_persistent<64, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err)
                       : launch_tc_persistent<128, 4>(a, br, bi, c, m, n, k, row0, col0, ldc, d_err);

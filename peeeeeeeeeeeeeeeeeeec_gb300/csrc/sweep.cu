@@ -1,0 +1,346 @@
+// Batched frequency sweep: the harmonic systems of one mesh at many
+// frequencies, each solved by the mixed-precision solve in its graph form.
+//
+// The whole per-frequency sequence -- MNA fill Z = [R + j w L, A; -P A^T,
+// j w I] (harmonic.c:175-372), the nrhs plane-wave right-hand sides
+// (scattering.c:263-336), power-of-two equilibration, FP32 LU with
+// split-BF16 tcgen05 trailing updates, a fixed number of FP64 refinement
+// sweeps -- is recorded once into a CUDA graph (its scratch as graph
+// allocations) and replayed for every frequency; omega and k0 live in
+// device memory and are copied in before each replay, so one graph serves
+// the whole sweep.  Different meshes run their plans from different host
+// threads (each thread has its own stream), so their graphs overlap on the
+// device.  Systems whose backward error is above the tolerance after the
+// fixed sweeps are solved again outside the graph: by the mixed solve with
+// its full precision ladder, then, if that does not reach the gate, by the
+// FP64 LU with FP64 refinement.
+//
+// The autotuner picks, per plan, the split-BF16 terms (3 or 6), the number
+// of refinement sweeps and the tile width of the wide tensor-core updates
+// (64 or 128 columns): the adaptive solve at the probe frequencies tells
+// the terms and sweeps it needed; each tile width is recorded and timed
+// by replays at the middle probe frequency; the fastest is kept.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/peec_gb300.h"
+#include "common.cuh"
+#include "mixed_capture.cuh"
+
+namespace peec {
+
+bool launch_harmonic_fill_dev(const double *L, const double *P, const int *edges, const double *R, int ne, int nv,
+                              const double *omega_dev, void *Z);
+bool launch_plane_waves_dev(const double *centers, const double *vectors, int ne, int nv, int nrhs,
+                            const double *d_k_hat, const double *d_e_hat, const double *k0_dev, void *rhs);
+int set_tc_wide_tile(int bn);
+
+static const double kC0 = 299792458.0;
+
+struct SweepPlan {
+    const double *L, *P, *R, *centers, *vectors;
+    const int *edges;
+    int ne, nv, n, nrhs;
+    PeecSweepTuning tuning;
+    double *d_params = nullptr;     // omega, k0
+    double *h_params = nullptr;     // pinned: one (omega, k0) pair per frequency of a run
+    size_t h_params_cap = 0;
+    double *d_dirs = nullptr;       // k_hat [nrhs][3], e_hat [nrhs][3]
+    Complex *d_Z = nullptr, *d_b = nullptr, *d_x = nullptr;
+    unsigned long long *d_eta = nullptr;  // per graph replay
+    int *d_status = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long graph_launches = 0;  // kernels per replay
+};
+
+static void drop_graph(SweepPlan &p) {
+    if (p.exec) cudaGraphExecDestroy(p.exec);
+    p.exec = nullptr;
+}
+
+// Record the per-frequency sequence with the plan's tuning.
+static bool record(SweepPlan &p) {
+    drop_graph(p);
+    if (!sync("sweep: before recording")) return false;
+    const int prev_bn = set_tc_wide_tile(p.tuning.tile_bn);
+    cudaGraph_t g = nullptr;
+    bool ok = cuda_ok(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal), "sweep: begin capture");
+    if (ok) {
+        const unsigned long long l0 = launch_count();
+        MixedCapture cap{p.tuning.split_terms, p.tuning.sweeps, p.d_eta, p.d_status};
+        bool body = launch_harmonic_fill_dev(p.L, p.P, p.edges, p.R, p.ne, p.nv, p.d_params, p.d_Z) &&
+                    launch_plane_waves_dev(p.centers, p.vectors, p.ne, p.nv, p.nrhs, p.d_dirs, p.d_dirs + 3 * p.nrhs,
+                                           p.d_params + 1, p.d_b) &&
+                    mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, p.d_x, (size_t)p.nrhs, 0.0, 1, nullptr, nullptr,
+                                     &cap) == 0;
+        p.graph_launches = launch_count() - l0;
+        const bool ended = cuda_ok(cudaStreamEndCapture(stream(), &g), "sweep: end capture");
+        ok = body && ended && g &&
+             cuda_ok(cudaGraphInstantiate(&p.exec, g, 0), "sweep: graph instantiation");
+    }
+    if (g) cudaGraphDestroy(g);
+    set_tc_wide_tile(prev_bn);
+    if (!ok) {
+        cudaGetLastError();
+        drop_graph(p);
+    }
+    return ok;
+}
+
+static bool ensure_params(SweepPlan &p, size_t n_freq) {
+    if (p.h_params_cap >= n_freq) return true;
+    if (p.h_params) cudaFreeHost(p.h_params);
+    p.h_params = nullptr;
+    p.h_params_cap = 0;
+    if (!cuda_ok(cudaMallocHost((void **)&p.h_params, 2 * n_freq * sizeof(double)), "sweep: pinned parameters"))
+        return false;
+    p.h_params_cap = n_freq;
+    return true;
+}
+
+// Replays of the graph for freqs[0..n_freq): X, eta bits and status per
+// frequency into device arrays (copied after each replay).
+static bool replay(SweepPlan &p, const double *freqs, size_t n_freq, Complex *d_X, unsigned long long *d_eta_all,
+                   int *d_status_all) {
+    if (!ensure_params(p, n_freq)) return false;
+    for (size_t f = 0; f < n_freq; ++f) {
+        const double w = 2.0 * M_PI * freqs[f];
+        p.h_params[2 * f] = w;
+        p.h_params[2 * f + 1] = w / kC0;
+    }
+    const size_t xs = (size_t)p.n * p.nrhs;
+    for (size_t f = 0; f < n_freq; ++f) {
+        if (!cuda_ok(cudaMemcpyAsync(p.d_params, p.h_params + 2 * f, 2 * sizeof(double), cudaMemcpyHostToDevice,
+                                     stream()),
+                     "sweep: parameters") ||
+            !cuda_ok(cudaGraphLaunch(p.exec, stream()), "sweep: graph launch"))
+            return false;
+        note_launch((int)p.graph_launches);
+        if (!cuda_ok(cudaMemcpyAsync(d_X + f * xs, p.d_x, xs * sizeof(Complex), cudaMemcpyDeviceToDevice, stream()),
+                     "sweep: solution copy") ||
+            !cuda_ok(cudaMemcpyAsync(d_eta_all + f, p.d_eta, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                     stream()),
+                     "sweep: backward error copy") ||
+            !cuda_ok(cudaMemcpyAsync(d_status_all + f, p.d_status, sizeof(int), cudaMemcpyDeviceToDevice, stream()),
+                     "sweep: status copy"))
+            return false;
+    }
+    return true;
+}
+
+// One system outside the graph: the mixed solve with its precision ladder,
+// then the FP64 LU with FP64 refinement.  0 at the gate (fallback 1 or 2),
+// 1 when neither reached it, -1 on errors.
+static int solve_fallback(SweepPlan &p, double freq, double tol, Complex *d_X, double *eta, int *fallback) {
+    const double w = 2.0 * M_PI * freq, params[2] = {w, w / kC0};
+    if (!cuda_ok(cudaMemcpyAsync(p.d_params, params, sizeof(params), cudaMemcpyHostToDevice, stream()),
+                 "sweep: parameters") ||
+        !launch_harmonic_fill_dev(p.L, p.P, p.edges, p.R, p.ne, p.nv, p.d_params, p.d_Z) ||
+        !launch_plane_waves_dev(p.centers, p.vectors, p.ne, p.nv, p.nrhs, p.d_dirs, p.d_dirs + 3 * p.nrhs,
+                                p.d_params + 1, p.d_b) ||
+        !sync("sweep: fallback set-up"))
+        return -1;
+    int it = 0;
+    int s = mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, d_X, (size_t)p.nrhs, tol, 30, eta, &it, nullptr);
+    if (s == 0) {
+        *fallback = 1;
+        return 0;
+    }
+    if (s == -1) return -1;
+    // FP64 LU of Z with FP64 refinement of the mixed solution (or from zero)
+    const size_t nn = (size_t)p.n * p.n;
+    DBuf<Complex> lu(nn);
+    DBuf<long long> piv(p.n);
+    DBuf<int> perm(p.n);
+    DBuf<double> rs(p.n), cs(p.n);
+    if (!lu.p || !piv.p || !perm.p || !rs.p || !cs.p) return -1;
+    if (!cuda_ok(cudaMemcpyAsync(lu.p, p.d_Z, nn * sizeof(Complex), cudaMemcpyDeviceToDevice, stream()), "sweep: Z"))
+        return -1;
+    double scale = 0.0;
+    int col = -1;
+    if (peec_gb300_complex_lu_factor_device(lu.p, (size_t)p.n, 1e-14, piv.p, perm.p, rs.p, cs.p, &scale, &col) != 0)
+        return -1;
+    if (s != 1 &&
+        peec_gb300_complex_lu_solve_device(lu.p, perm.p, rs.p, cs.p, (size_t)p.n, p.d_b, d_X, (size_t)p.nrhs) != 0)
+        return -1;
+    int r = peec_gb300_complex_refine_device(p.d_Z, lu.p, perm.p, rs.p, cs.p, (size_t)p.n, p.d_b, d_X,
+                                             (size_t)p.nrhs, tol, 10, eta, &it);
+    if (r < 0) return -1;
+    *fallback = 2;
+    return r;
+}
+
+}  // namespace peec
+
+using namespace peec;
+
+extern "C" {
+
+void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R,
+                              const double *d_edge_centers, const double *d_edge_vectors, size_t n_edges,
+                              size_t n_nodes, size_t nrhs, const double *k_hat, const double *e_hat,
+                              const PeecSweepTuning *tuning) {
+    if (!d_L || !d_P || !d_edges || !d_edge_centers || !d_edge_vectors || !k_hat || !e_hat || n_edges == 0 ||
+        n_nodes == 0 || nrhs == 0 || n_edges + n_nodes > 0x7fffffff || nrhs > 4096)
+        return nullptr;
+    SweepPlan *p = new SweepPlan();
+    p->L = d_L;
+    p->P = d_P;
+    p->R = d_R;
+    p->edges = d_edges;
+    p->centers = d_edge_centers;
+    p->vectors = d_edge_vectors;
+    p->ne = (int)n_edges;
+    p->nv = (int)n_nodes;
+    p->n = p->ne + p->nv;
+    p->nrhs = (int)nrhs;
+    p->tuning = tuning ? *tuning : PeecSweepTuning{3, 4, 0};
+    const size_t n = (size_t)p->n;
+    bool ok = cuda_ok(cudaMalloc((void **)&p->d_params, 2 * sizeof(double)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_dirs, 6 * nrhs * sizeof(double)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_Z, n * n * sizeof(Complex)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_b, n * nrhs * sizeof(Complex)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_x, n * nrhs * sizeof(Complex)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_eta, sizeof(unsigned long long)), "sweep plan") &&
+              cuda_ok(cudaMalloc((void **)&p->d_status, sizeof(int)), "sweep plan");
+    if (ok) {
+        std::vector<double> dirs(6 * nrhs);
+        memcpy(dirs.data(), k_hat, 3 * nrhs * sizeof(double));
+        memcpy(dirs.data() + 3 * nrhs, e_hat, 3 * nrhs * sizeof(double));
+        ok = cuda_ok(cudaMemcpyAsync(p->d_dirs, dirs.data(), dirs.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                     stream()),
+                     "sweep plan") &&
+             sync("sweep plan");
+    }
+    if (!ok) {
+        peec_gb300_sweep_destroy(p);
+        return nullptr;
+    }
+    return p;
+}
+
+int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_probe, PeecSweepTuning *chosen,
+                          double *ms_per_system) {
+    if (!plan || !probe_frequencies || n_probe == 0) return -1;
+    SweepPlan &p = *static_cast<SweepPlan *>(plan);
+    const size_t xs = (size_t)p.n * p.nrhs;
+    DBuf<Complex> x(xs);
+    if (!x.p) return -1;
+    // 1. what the adaptive solve needs at the probe frequencies
+    int terms = 3, sweeps = 1;
+    for (size_t f = 0; f < n_probe; ++f) {
+        double eta = 0.0;
+        int fb = 0;
+        const double w = 2.0 * M_PI * probe_frequencies[f], params[2] = {w, w / kC0};
+        if (!cuda_ok(cudaMemcpyAsync(p.d_params, params, sizeof(params), cudaMemcpyHostToDevice, stream()),
+                     "sweep: parameters") ||
+            !launch_harmonic_fill_dev(p.L, p.P, p.edges, p.R, p.ne, p.nv, p.d_params, p.d_Z) ||
+            !launch_plane_waves_dev(p.centers, p.vectors, p.ne, p.nv, p.nrhs, p.d_dirs, p.d_dirs + 3 * p.nrhs,
+                                    p.d_params + 1, p.d_b))
+            return -1;
+        int it = 0;
+        const int s = mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, x.p, (size_t)p.nrhs, 1e-10, 30, &eta, &it, nullptr);
+        (void)fb;
+        if (s < 0 && s != -2) return -1;
+        if (s == 0) {
+            terms = std::max(terms, peec_gb300_mixed_split_terms());
+            // the sweeps of the last rung: all of them when it started at BF16x6
+            sweeps = std::max(sweeps, peec_gb300_mixed_split_terms() == 6 && terms == 6 ? std::min(it, 8) : it);
+        }
+    }
+    sweeps = std::min(sweeps + 1, 10);  // one sweep of margin
+    // 2. record and time each tile width at the middle probe frequency
+    const double fmid = probe_frequencies[n_probe / 2];
+    DBuf<unsigned long long> eta_all(3);
+    DBuf<int> st_all(3);
+    DBuf<Complex> X3(3 * xs);
+    if (!eta_all.p || !st_all.p || !X3.p) return -1;
+    const double fr[3] = {fmid, fmid, fmid};
+    PeecSweepTuning best = {terms, sweeps, 128};
+    double best_ms = INFINITY;
+    for (int bn : {128, 64}) {
+        p.tuning = PeecSweepTuning{terms, sweeps, bn};
+        if (!record(p)) continue;
+        if (!replay(p, fr, 1, X3.p, eta_all.p, st_all.p) || !sync("sweep: tuning warm-up")) return -1;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream());
+        const bool ok = replay(p, fr, 3, X3.p, eta_all.p, st_all.p);
+        cudaEventRecord(e1, stream());
+        float ms = 0.0f;
+        const bool synced = sync("sweep: tuning");
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (!ok || !synced) return -1;
+        if (ms / 3.0 < best_ms) {
+            best_ms = ms / 3.0;
+            best = p.tuning;
+        }
+    }
+    if (!isfinite(best_ms)) return -1;
+    p.tuning = best;
+    if (!record(p)) return -1;
+    if (chosen) *chosen = best;
+    if (ms_per_system) *ms_per_system = best_ms;
+    return 0;
+}
+
+int peec_gb300_sweep_run(void *plan, const double *frequencies, size_t n_freq, double tol, Complex *d_X,
+                         double *backward_error, int *fallback) {
+    if (!plan || !frequencies || n_freq == 0 || !d_X) return -1;
+    SweepPlan &p = *static_cast<SweepPlan *>(plan);
+    if (!p.exec && !record(p)) return -1;
+    DBuf<unsigned long long> eta_all(n_freq);
+    DBuf<int> st_all(n_freq);
+    if (!eta_all.p || !st_all.p) return -1;
+    if (!replay(p, frequencies, n_freq, d_X, eta_all.p, st_all.p)) return -1;
+    std::vector<unsigned long long> eb(n_freq);
+    std::vector<int> sb(n_freq);
+    cudaMemcpyAsync(eb.data(), eta_all.p, n_freq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream());
+    cudaMemcpyAsync(sb.data(), st_all.p, n_freq * sizeof(int), cudaMemcpyDeviceToHost, stream());
+    if (!sync("sweep: results")) return -1;
+    const size_t xs = (size_t)p.n * p.nrhs;
+    int worst = 0;
+    for (size_t f = 0; f < n_freq; ++f) {
+        double eta;
+        memcpy(&eta, &eb[f], sizeof(eta));
+        int fb = 0;
+        if (sb[f] == 6) {
+            set_error("sweep: a triangular-solve wait timed out in the graph");
+            return -1;
+        }
+        if (sb[f] != 0 || !(eta <= tol)) {
+            const int s = solve_fallback(p, frequencies[f], tol, d_X + f * xs, &eta, &fb);
+            if (s < 0) return -1;
+            worst = std::max(worst, s);
+        }
+        if (backward_error) backward_error[f] = eta;
+        if (fallback) fallback[f] = fb;
+    }
+    return worst;
+}
+
+int peec_gb300_sweep_tuning(void *plan, PeecSweepTuning *tuning) {
+    if (!plan || !tuning) return -1;
+    *tuning = static_cast<SweepPlan *>(plan)->tuning;
+    return 0;
+}
+
+void peec_gb300_sweep_destroy(void *plan) {
+    if (!plan) return;
+    SweepPlan *p = static_cast<SweepPlan *>(plan);
+    sync("sweep: destroy");
+    drop_graph(*p);
+    for (void *d : {(void *)p->d_params, (void *)p->d_dirs, (void *)p->d_Z, (void *)p->d_b, (void *)p->d_x,
+                    (void *)p->d_eta, (void *)p->d_status})
+        if (d) cudaFree(d);
+    if (p->h_params) cudaFreeHost(p->h_params);
+    delete p;
+}
+
+}  // extern "C"

@@ -273,3 +273,31 @@ def test_level_and_depth_first_near_fields_agree(tmp_path):
         assert np.array_equal(a == 0, b == 0)
         nz = b != 0
         assert np.max(np.abs(a[nz] - b[nz]) / np.abs(b[nz])) < 1e-13, key
+
+
+def test_near_factor_zero_overlapping_plates(gpu_lib, oracle):
+    """near_factor = 0 makes overlapping patches of two coincident-plane
+    plates (shifted by a third of a cell, no shared vertex) FAR; the far
+    rule must then keep the reference's R <= 0 skip (the FP64 form is used)
+    and the entries match the oracle."""
+    xyz, quads = [], []
+    for dx in (0.0, 1.0 / 12.0):
+        base = len(xyz)
+        for j in range(5):
+            for i in range(5):
+                xyz.append((0.25 * i + dx, 0.25 * j, 0.0))
+        for j in range(4):
+            for i in range(4):
+                v = base + j * 5 + i
+                quads.append((v, v + 1, v + 6, v + 5))
+    with SynthMesh.from_arrays(np.array(xyz), np.array(quads, dtype=np.int32)) as m:
+        s, L = inductance(gpu_lib, m, near_factor=0.0)
+        assert s == 0
+        so, Lo = oracle.inductance(m, near_factor=0.0)
+        assert so == 0
+        assert elem_rel_err(L, Lo) < TOL
+        s, P = potential(gpu_lib, m, near_factor=0.0)
+        assert s == 0
+        so, Po = oracle.potential(m, near_factor=0.0)
+        assert so == 0
+        assert elem_rel_err(P, Po) < TOL

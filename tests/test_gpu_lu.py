@@ -181,6 +181,35 @@ def test_solve_with_caller_built_factor(gpu_lib):
     f.free()
 
 
+def test_edited_factor_entry_is_seen_by_solve(gpu_lib, oracle):
+    """A complex_lu_factorize result whose one off-diagonal entry (outside
+    the cache's sampled fingerprint) is edited between two solves: the
+    second solve uses the edited factor (it equals the oracle's solve with
+    that factor), not a stale device copy."""
+    import ctypes as C
+    from helpers import cp
+    rng = np.random.default_rng(21)
+    n = 300
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    f = ComplexLU(gpu_lib, a)
+    assert f.status == 0
+    s, x0 = f.solve(b)
+    assert s == 0
+    i, j = 5, 17                          # double index 2 (5 n + 17) is off the 4093-point sample grid
+    step = (2 * n * n) // 4093 + 1
+    assert (2 * (i * n + j)) % step and (2 * (i * n + j) + 1) % step
+    raw = np.ctypeslib.as_array(C.cast(f.f.data, C.POINTER(C.c_double)), shape=(2 * n * n,))
+    raw[2 * (i * n + j)] += 0.25
+    lu, piv, rs, cs = f.factors()
+    s, x1 = f.solve(b)
+    assert s == 0
+    _, xo = oracle.complex_lu_solve(np.ascontiguousarray(lu), piv.astype(np.uintp), rs, cs, b)
+    assert rel_err(x1, xo) < 1e-12
+    assert rel_err(x1, x0) > 1e-6
+    f.free()
+
+
 _PANEL_PROBE = r"""
 import ctypes as C, hashlib, sys
 import numpy as np
