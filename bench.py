@@ -20,6 +20,10 @@ Lp and P are quasi-static (the reference has no retardation).
           sources built here with its release flags; the bit-exact oracle
           port where they are absent), on a bounded sample extrapolated to
           one solve (oracle/cpu_baseline.py)
+Legs beside the headline: the mixed-precision solve, serving (config 5:
+Poisson harmonic and lightning requests), the config-4 sweep at a reduced
+size (--batch), transient, retarded, RCS, incidence and far-rule precision;
+--config3 and --config4 run those configurations alone.
 Multi-GPU: the path does not shard; --gpus N runs N independent replicas
 (one process per GPU) and reports the aggregate.
 """
@@ -130,26 +134,58 @@ def plane_wave(m):
     return b
 
 
+def _row_blocks(n, fn, threads=None):
+    """fn(r0, r1) over row blocks on the host's cores (numpy releases the
+    GIL inside its array operations)."""
+    import concurrent.futures as cf
+    threads = threads or os.cpu_count() or 1
+    step = max(64, (n + 4 * threads - 1) // (4 * threads))
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda r0: fn(r0, min(n, r0 + step)), range(0, n, step)))
+
+
 def host_mna(L, P, edges, freq):
     """Z = [jwL, A; -P A^T, jw I] on the host, as the reference's
-    harmonic_build_system does (PEC: R = 0)."""
+    harmonic_build_system does (PEC: R = 0), row blocks on all host cores."""
     ne, nv = L.shape[0], P.shape[0]
     n = ne + nv
     w = 2 * np.pi * freq
-    Z = np.zeros((n, n), dtype=np.complex128)
-    Z[:ne, :ne] = 1j * w * L
-    idx = np.arange(ne)
-    Z[idx, ne + edges[:, 0]] = -1.0
-    Z[idx, ne + edges[:, 1]] = 1.0
-    Z[ne:, :ne] = -(P[:, edges[:, 1]] - P[:, edges[:, 0]])
-    Z[np.arange(ne, n), np.arange(ne, n)] = 1j * w
+    Z = np.empty((n, n), dtype=np.complex128)
+    ea, eb = edges[:, 0], edges[:, 1]
+
+    def fill(r0, r1):
+        blk = Z[r0:r1]
+        blk[:] = 0.0
+        e0, e1 = min(r0, ne), min(r1, ne)
+        if e1 > e0:
+            blk[:e1 - e0, :ne].imag = w * L[e0:e1]
+            idx = np.arange(e0, e1)
+            blk[idx - r0, ne + ea[e0:e1]] = -1.0
+            blk[idx - r0, ne + eb[e0:e1]] = 1.0
+        v0, v1 = max(r0, ne) - ne, max(r1, ne) - ne
+        if v1 > v0:
+            sub = blk[max(r0, ne) - r0:]
+            sub[:, :ne].real = -(P[v0:v1, eb] - P[v0:v1, ea])
+            sub[np.arange(v1 - v0), ne + np.arange(v0, v1)] = 1j * w
+
+    _row_blocks(n, fill)
     return Z
 
 
 def host_backward_error(Z, x, b):
-    r = Z @ x - b
-    den = np.abs(Z) @ np.abs(x) + np.abs(b)
-    return float(np.max(np.abs(r) / np.where(den > 0, den, 1)))
+    """max_i |Z x - b|_i / (sum_j |Z_ij||x_j| + |b_i|), row blocks on all
+    host cores."""
+    n = Z.shape[0]
+    ax = np.abs(x)
+    out = []
+
+    def part(r0, r1):
+        r = Z[r0:r1] @ x - b[r0:r1]
+        den = np.abs(Z[r0:r1]) @ ax + np.abs(b[r0:r1])
+        out.append(float(np.max(np.abs(r) / np.where(den > 0, den, 1))))
+
+    _row_blocks(n, part)
+    return max(out)
 
 
 class DeviceSolve:
@@ -521,23 +557,27 @@ def retarded_plain_leg(lib, ds):
                                                     "retardation correction FP32 pipes"}
 
 
-def config3(lib):
-    """The 2.5 cm box (80 x 40 x 20 cells: Ne 22400, Nv 11202, N 33602) at
-    100 MHz with retarded Lp / P (FP32 far rule, FP64 near field) and one
-    x-polarised plane wave from +z: the mixed solve (FP32 LU, split-BF16x3
-    tensor-core updates, FP64 refinement to the 1e-10 gate), then the plain
-    FP64 LU of the same Z as the reference for the current and RCS errors.
-    One JSON line; not part of the default run (the FP64 LU alone takes
-    about 1.5 minutes at this size)."""
+def config3(lib, nrhs=720, box=(2.0, 1.0, 0.5, 80, 40, 20)):
+    """Config 3: the 2.5 cm box (80 x 40 x 20 cells: Ne 22400, Nv 11202,
+    N 33602) at 100 MHz with retarded Lp / P (FP32 far rule, FP64 near
+    field) and nrhs plane waves: theta = 90 deg, phi at 1-degree steps,
+    theta and phi polarisations (720 = 360 x 2; incident_field.c:110-230
+    basis).  The mixed solve of all right-hand sides at once (FP32 LU,
+    split-BF16x3 tensor-core updates, blocked many-right-hand-side FP32
+    substitution, FP64 refinement with a GEMM-form residual, to the 1e-10
+    gate), then the plain FP64 LU of the same Z and its solve of every
+    right-hand side as the reference for the current and RCS errors.  One
+    JSON line; not part of the default run."""
     from peeeeeeeeeeeeeeeeeeec_gb300.mesh import SynthMesh
-    m = SynthMesh.box(2.0, 1.0, 0.5, 80, 40, 20)
+    m = SynthMesh.box(*box)
     ds = DeviceSolve(lib, m)
     n, ne, nv = ds.n, ds.ne, ds.nv
     f = 100e6
     k = 2 * np.pi * f / C0
     al = lib.peec_gb300_device_alloc
     dLc, dPc = al(ne * ne * 16), al(nv * nv * 16)
-    assert dLc and dPc
+    dB, dX, dXr = al(nrhs * n * 16), al(nrhs * n * 16), al(nrhs * n * 16)
+    assert dLc and dPc and dB and dX and dXr
     prev = lib.peec_gb300_set_far_precision(2)
     ev = [lib.peec_gb300_event_record()]
     st = ds.abi.PeecAssemblyStats(), ds.abi.PeecAssemblyStats()
@@ -548,7 +588,15 @@ def config3(lib):
                                                     C.byref(st[1])) == 0
     ev.append(lib.peec_gb300_event_record())
     assert lib.peec_gb300_harmonic_build_retarded_device(dLc, dPc, ds.dedges, None, ne, nv, f, ds.dZ) == 0
-    assert lib.peec_gb300_plane_wave_rhs_device(ds.dctr, ds.dvec, ne, nv, ds.kh, ds.eh, k, ds.db) == 0
+    phis = np.radians(np.arange(nrhs // 2, dtype=np.float64))
+    waves = []
+    for ph in phis:  # theta = 90 deg: k_hat = -(cos phi, sin phi, 0)
+        kh = (-np.cos(ph), -np.sin(ph), -0.0)
+        waves.append((kh, (0.0, 0.0, -1.0)))               # e_theta
+        waves.append((kh, (-np.sin(ph), np.cos(ph), 0.0)))  # e_phi
+    for q, (kh, eh) in enumerate(waves[:nrhs]):
+        assert lib.peec_gb300_plane_wave_rhs_device(ds.dctr, ds.dvec, ne, nv, (C.c_double * 3)(*kh),
+                                                    (C.c_double * 3)(*eh), k, dB + q * n * 16) == 0
     ev.append(lib.peec_gb300_event_record())
     lib.peec_gb300_set_far_precision(prev)
     lib.peec_gb300_synchronize()
@@ -556,16 +604,13 @@ def config3(lib):
     for p in (dLc, dPc):
         lib.peec_gb300_device_free(p)
     be, it = C.c_double(), C.c_int()
-    runs = []
-    for rep in range(3):  # warm, timed, timed with the factorisation's phase timing
-        if rep == 2:
-            lib.peec_gb300_lu_timing_enable(1)
-        e0 = lib.peec_gb300_event_record()
-        s = lib.peec_gb300_complex_solve_mixed_device(ds.dZ, n, ds.db, ds.dx, 1, 1e-10, 30, C.byref(be), C.byref(it))
-        e1 = lib.peec_gb300_event_record()
-        lib.peec_gb300_synchronize()
-        assert s == 0, "mixed solve failed: %d" % s
-        runs.append(lib.peec_gb300_event_elapsed_ms(e0, e1))
+    lib.peec_gb300_lu_timing_enable(1)
+    e0 = lib.peec_gb300_event_record()
+    s = lib.peec_gb300_complex_solve_mixed_device(ds.dZ, n, dB, dX, nrhs, 1e-10, 30, C.byref(be), C.byref(it))
+    e1 = lib.peec_gb300_event_record()
+    lib.peec_gb300_synchronize()
+    assert s == 0, "mixed solve failed: %d (backward error %g)" % (s, be.value)
+    mixed_ms = lib.peec_gb300_event_elapsed_ms(e0, e1)
     mt = [C.c_double() for _ in range(4)]
     lib.peec_gb300_lu_timing(*[C.byref(x) for x in mt])
     tt = [C.c_double() for _ in range(2)]
@@ -573,22 +618,35 @@ def config3(lib):
     lib.peec_gb300_lu_timing_enable(0)
     mp, mf, mr = C.c_double(), C.c_double(), C.c_double()
     lib.peec_gb300_mixed_timing(C.byref(mp), C.byref(mf), C.byref(mr))
-    x_mixed = al(2 * n * 16)
-    lib.peec_gb300_copy_device(x_mixed, ds.dx, n * 16)
-    # FP64 reference: the plain LU of the same Z
+    # FP64 reference: the plain LU of the same Z, every right-hand side
     assert lib.peec_gb300_copy_device(ds.dLU, ds.dZ, n * n * 16) == 0
     t0 = time.perf_counter()
     scale, col = C.c_double(), C.c_int()
     assert lib.peec_gb300_complex_lu_factor_device(ds.dLU, n, 1e-14, ds.dpiv, ds.dperm, ds.drow, ds.dcol,
                                                    C.byref(scale), C.byref(col)) == 0
-    assert lib.peec_gb300_complex_lu_solve_device(ds.dLU, ds.dperm, ds.drow, ds.dcol, n, ds.db, ds.dx, 1) == 0
+    lib.peec_gb300_synchronize()
+    t_fp64_factor = time.perf_counter() - t0
+    assert lib.peec_gb300_complex_lu_solve_device(ds.dLU, ds.dperm, ds.drow, ds.dcol, n, dB, dXr, nrhs) == 0
     lib.peec_gb300_synchronize()
     t_fp64 = time.perf_counter() - t0
     out3 = (C.c_double * 3)()
-    assert lib.peec_gb300_backward_error_device(ds.dZ, n, ds.dx, ds.db, 1, out3) == 0
+    assert lib.peec_gb300_backward_error_device(ds.dZ, n, dXr, dB, nrhs, out3) == 0
+    X = np.zeros((nrhs, n), dtype=np.complex128)
+    Xr = np.zeros((nrhs, n), dtype=np.complex128)
+    lib.peec_gb300_copy_to_host(X.ctypes.data, dX, X.nbytes)
+    lib.peec_gb300_copy_to_host(Xr.ctypes.data, dXr, Xr.nbytes)
+    cur = np.max(np.abs(X[:, :ne] - Xr[:, :ne]), axis=1) / np.max(np.abs(Xr[:, :ne]), axis=1)
+    pot = np.max(np.abs(X[:, ne:] - Xr[:, ne:]), axis=1) / np.max(np.abs(Xr[:, ne:]), axis=1)
+    # RCS of the first two right-hand sides (theta and phi polarisation at
+    # phi = 0) in 361 directions, mixed against FP64
+    x_pair = al(4 * n * 16)
+    lib.peec_gb300_copy_device(x_pair, dX, n * 16)
+    lib.peec_gb300_copy_device(ds.dx, dXr, n * 16)
     ds.k0 = k
-    rcs = rcs_leg(lib, ds, x_mixed)
-    lib.peec_gb300_device_free(x_mixed)
+    rcs = rcs_leg(lib, ds, x_pair)
+    lib.peec_gb300_device_free(x_pair)
+    for p in (dB, dX, dXr):
+        lib.peec_gb300_device_free(p)
     bf16 = 1933.8
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
@@ -596,26 +654,33 @@ def config3(lib):
     except Exception:
         pass
     tflops = tt[1].value / (tt[0].value * 1e-3) / 1e12 if tt[0].value > 0 else None
-    line = {"metric": "config 3 (2.5 cm box, 100 MHz, retarded Lp / P, 1 plane wave): mixed solve",
-            "value": 1000.0 / runs[1], "unit": "solves/s", "n_unknowns": n, "Ne": ne, "Nv": nv,
+    line = {"metric": "config 3 (box %gx%gx%g m, %dx%dx%d cells, 100 MHz, retarded Lp / P, %d plane waves): "
+                      "mixed solve" % (box + (nrhs,)),
+            "value": nrhs * 1000.0 / mixed_ms, "unit": "right-hand sides solved to the gate per second",
+            "n_unknowns": n, "Ne": ne, "Nv": nv, "nrhs": nrhs,
             "assembly_ms": {"Lp_retarded": asm[0], "P_retarded": asm[1], "mna_fill_rhs": asm[2]},
-            "mixed_solve_ms": runs[1], "mixed_phase_ms": {"prepare": mp.value, "factor": mf.value, "refine": mr.value},
+            "mixed_solve_ms": mixed_ms, "mixed_phase_ms": {"prepare": mp.value, "factor": mf.value,
+                                                           "refine": mr.value},
             "backward_error": be.value, "refinement_iterations": it.value,
             "lu_phases": {"panel_ms": mt[0].value, "swap_trsm_split_ms": mt[1].value, "tc_update_ms": mt[2].value,
                           "trailing_gemm_ms": tt[0].value, "trailing_gemm_issued_bf16_flops": tt[1].value},
             "trailing_gemm_roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",
                                        "frac": tflops / bf16 if tflops else None,
                                        "peak_source": "measured (MEASURED_PEAKS.json, cuBLAS BF16 burst)"},
-            "fp64_lu_reference_s": t_fp64, "fp64_backward_error": out3[0],
-            "errors_vs_fp64_lu": {"edge_current_rel": rcs["edge_current_rel_err"],
+            "fp64_lu_reference_s": {"factor": t_fp64_factor, "factor_and_solve_all_rhs": t_fp64},
+            "fp64_backward_error": out3[0],
+            "mixed_vs_fp64_time": t_fp64 / (mixed_ms * 1e-3),
+            "errors_vs_fp64_lu": {"edge_current_rel_max_over_rhs": float(cur.max()),
+                                  "edge_current_rel_median": float(np.median(cur)),
+                                  "node_potential_rel_max_over_rhs": float(pot.max()),
                                   "radiation_vector_rel": rcs["mixed_vs_fp64_rel_radiation_err"],
                                   "sigma_rel_max_over_361_directions": rcs["mixed_vs_fp64_max_rel_sigma_err"]},
-            "monostatic_sigma_dbsm": rcs["monostatic_sigma_dbsm"], "rcs_ms_per_sweep": rcs["ms_per_sweep"],
             "near_pairs": {"Lp": st[0].near_pairs, "P": st[1].near_pairs},
-            "data": "synthetic (seeded box mesh, unit plane wave)", "dtype": "mixed (see metric)"}
+            "data": "synthetic (seeded box mesh, unit plane waves)", "dtype": "mixed (see metric)"}
     print(json.dumps(line), flush=True)
     ds.free()
     m.close()
+
 
 
 def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
@@ -625,9 +690,10 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
     the meshes largest first on `workers` host threads (one CUDA stream each)
     and time the whole arm on the wall clock: Lp / P assembly included.
       mixed  a sweep plan per mesh (peec_gb300_sweep_*): the autotuner at
-             three probe frequencies (lowest, middle, highest) picks split
-             terms, refinement sweeps and tile width; the mixed solve
-             recorded once into a CUDA graph is replayed for every frequency;
+             eight probe frequencies across the band picks the frequency
+             below which the robust graph (BF16x6) runs, the fast graph's
+             sweeps and the tile width; the mixed solve recorded into CUDA
+             graphs is replayed for every frequency;
              systems above the gate are solved again by the precision
              ladder, then the FP64 LU with FP64 refinement
       plain  per system: MNA fill, FP64 complex LU, solve, FP64 iterative
@@ -670,9 +736,11 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
         assert plan, "sweep plan"
         t = ds_abi().PeecSweepTuning()
         ms = C.c_double()
-        probes = np.ascontiguousarray(freqs[[0, len(freqs) // 2, len(freqs) - 1]])
-        assert lib.peec_gb300_sweep_tune(plan, probes.ctypes.data_as(ds_abi().c_double_p), 3, C.byref(t),
+        probes = np.ascontiguousarray(freqs[np.linspace(0, len(freqs) - 1, 8).round().astype(int)])
+        assert lib.peec_gb300_sweep_tune(plan, probes.ctypes.data_as(ds_abi().c_double_p), len(probes), C.byref(t),
                                          C.byref(ms)) == 0
+        fsplit, rob = C.c_double(), ds_abi().PeecSweepTuning()
+        lib.peec_gb300_sweep_split(plan, C.byref(fsplit), C.byref(rob))
         dX = lib.peec_gb300_device_alloc(len(freqs) * nrhs * n * 16)
         be = np.zeros(len(freqs))
         fb = np.zeros(len(freqs), dtype=np.int32)
@@ -683,7 +751,8 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
         lib.peec_gb300_sweep_destroy(plan)
         lib.peec_gb300_device_free(dX)
         free(d)
-        return {"n": n, "be": be, "fb": fb, "tuning": (t.split_terms, t.sweeps, t.tile_bn), "graph_ms": ms.value}
+        return {"n": n, "be": be, "fb": fb, "tuning": (t.split_terms, t.sweeps, t.tile_bn), "graph_ms": ms.value,
+                "split_hz": fsplit.value, "robust": (rob.split_terms, rob.sweeps)}
 
     def plain_mesh(i):
         m = pool[i][0]
@@ -737,7 +806,9 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
             out[arm]["fallback_mixed_ladder"] = int(np.sum(fb == 1))
             out[arm]["fallback_fp64"] = int(np.sum(fb == 2))
             out[arm]["tuning"] = {str(r["n"]): {"split_terms": r["tuning"][0], "sweeps": r["tuning"][1],
-                                                "tile_bn": r["tuning"][2], "graph_ms_per_system": r["graph_ms"]}
+                                                "tile_bn": r["tuning"][2], "graph_ms_per_system": r["graph_ms"],
+                                                "robust_below_hz": r["split_hz"],
+                                                "robust_terms_sweeps": list(r["robust"])}
                                   for r in res}
         else:
             out[arm]["frequency_stride"] = plain_stride
@@ -833,43 +904,6 @@ def serving_leg(lib, window_s, workers, lightning_steps=4096):
     for m, _ in pool:
         m.close()
     box.close()
-    return out
-
-
-def batched_leg(lib, n_meshes, n_freqs, workers):
-    """Many meshes x many frequencies (config-4 shape, scaled): seeded boxes /
-    plates of 300-4000 unknowns, each at n_freqs log-spaced frequencies from
-    1 kHz to 100 MHz with 4 plane waves, all submitted at once to one server
-    (its Lp / P cache warmed first), mixed solve then plain FP64 LU.  The
-    sweep is submitted largest system first, lowest frequency first within a
-    mesh (longest-processing-time order, the same for both arms), so that the
-    costliest solves start early and overlap the rest.
-    Throughput = systems reaching the 1e-10 gate / makespan."""
-    from peeeeeeeeeeeeeeeeeeec_gb300 import workloads as W
-    from peeeeeeeeeeeeeeeeeeec_gb300.server import Server
-    pool = W.serving_meshes(seed=11, count=n_meshes, lo=300, hi=4000)
-    systems = W.batch_systems(seed=13, n_meshes=n_meshes, n_freqs=n_freqs)
-    size = [m.n_edges + m.n_nodes for m, _ in pool]
-    systems.sort(key=lambda t: (-size[t[0]], t[1]))
-    out = {"systems": "%d meshes x %d frequencies (1 kHz - 100 MHz, log) x 4 plane waves, largest system first" % (n_meshes, n_freqs),
-           "unknowns": [m.n_edges + m.n_nodes for m, _ in pool], "workers": workers}
-    with Server(150 << 30, workers) as srv:
-        for t in [srv.submit(m, i, 30e6, [[0.0, 0.0, -1.0]], [[1.0, 0.0, 0.0]]) for i, (m, _) in enumerate(pool)]:
-            srv.wait(t)
-        for mode in ("mixed", "plain"):
-            tickets = [srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed")) for (mi, f, k, e) in systems]
-            res = [srv.wait(t)[1] for t in tickets]
-            span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
-            ok = sum(1 for r in res if r["status"] == 0 and r["backward_error"] <= 1e-10)
-            lat = np.array([r["t_end"] - r["t_submit"] for r in res])
-            out[mode] = {"value": ok / span, "unit": "systems/s", "at_gate": ok, "systems": len(res),
-                         "makespan_s": span, "fallbacks_to_fp64": sum(r.get("fallback", 0) for r in res),
-                         "p50_latency_s": float(np.percentile(lat, 50)),
-                         "p99_latency_s": float(np.percentile(lat, 99)),
-                         "max_backward_error": max(r["backward_error"] for r in res)}
-    out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
-    for m, _ in pool:
-        m.close()
     return out
 
 
@@ -972,10 +1006,16 @@ def main():
     ap.add_argument("--no-retarded", action="store_true")
     ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=4)
-    ap.add_argument("--batch", default="8x8", help="meshes x frequencies of the batched leg (0: skip)")
+    ap.add_argument("--batch", default="12x16",
+                    help="meshes x frequencies of the batched leg, the config-4 sweep at a reduced size (0: skip)")
     ap.add_argument("--config4", default=None,
                     help="only the batched sweep, meshes x frequencies (e.g. 48x64): sweep graphs vs plain FP64 LU")
     ap.add_argument("--config4-plain-stride", type=int, default=1)
+    ap.add_argument("--config4-workers", type=int, default=8, help="host threads (streams) of both config-4 arms")
+    ap.add_argument("--config3-box", default="2.0,1.0,0.5,80,40,20",
+                    help="lx,ly,lz,nx,ny,nz of --config3 (a smaller box for profiling runs)")
+    ap.add_argument("--config3-rhs", type=int, default=720)
+    ap.add_argument("--no-far", action="store_true", help="skip the far-rule precision leg")
     ap.add_argument("--config3", action="store_true",
                     help="only the 2.5 cm retarded box (33602 unknowns): mixed solve + FP64 LU reference")
     args = ap.parse_args()
@@ -1000,12 +1040,13 @@ def main():
         raise RuntimeError("no CUDA device")
     if args.config3:
         if rank == 0:
-            config3(lib)
+            v = args.config3_box.split(",")
+            config3(lib, args.config3_rhs, (float(v[0]), float(v[1]), float(v[2]), int(v[3]), int(v[4]), int(v[5])))
         return
     if args.config4:
         if rank == 0:
             nm, nf = (int(v) for v in args.config4.split("x"))
-            res = config4(lib, nm, nf, workers=args.serve_workers, plain_stride=args.config4_plain_stride)
+            res = config4(lib, nm, nf, workers=args.config4_workers, plain_stride=args.config4_plain_stride)
             print(json.dumps({"metric": "config 4 batched sweep: systems/s at <=1e-10 backward error",
                               "value": res["mixed"]["value"], "unit": "systems/s", "batched": res,
                               "data": "synthetic (seeded meshes and plane waves)"}), flush=True)
@@ -1102,13 +1143,13 @@ def main():
     retarded = None if args.no_retarded else retarded_leg(lib, ds)
     if retarded is not None:
         retarded["plain_fp64_solve"] = retarded_plain_leg(lib, ds)
-    far_precision = far_precision_leg(lib, ds)
+    far_precision = None if args.no_far else far_precision_leg(lib, ds)
     ds.free()
     serving = serving_leg(lib, args.serve_window, args.serve_workers) if args.serve_window > 0 else None
     batched = None
     if args.batch not in ("0", ""):
         bm, bf = (int(v) for v in args.batch.split("x"))
-        batched = batched_leg(lib, bm, bf, args.serve_workers)
+        batched = config4(lib, bm, bf, workers=args.config4_workers)
 
     # end to end through the drop-in ABI, host buffers
     e2e = None

@@ -281,20 +281,23 @@ int peec_gb300_backward_error_device(const Complex *d_Z, size_t n, const Complex
 typedef struct
 {
     int split_terms; /* split-BF16 products of the FP32 factorisation: 3 or 6 */
-    int sweeps;      /* FP64 refinement sweeps recorded in the graph        */
+    int sweeps;      /* FP64 refinement sweeps recorded in the graph (at most; a
+                        sweep after the one that reaches 1e-10 does nothing) */
     int tile_bn;     /* width of the wide tensor-core update tiles: 64, 128, or 0 (by shape) */
 } PeecSweepTuning;
 
-/* NULL on invalid input or allocation failure.  tuning NULL: {3, 4, 0}. */
+/* NULL on invalid input or allocation failure.  tuning NULL: {3, 10, 0}. */
 void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R,
                               const double *d_edge_centers, const double *d_edge_vectors, size_t n_edges,
                               size_t n_nodes, size_t nrhs, const double *k_hat, const double *e_hat,
                               const PeecSweepTuning *tuning);
-/* Autotuner: solves the systems at the probe frequencies with the adaptive
- * mixed solve to learn the split terms and sweeps they need (plus one sweep
- * of margin), then records and times the graph with 128- and 64-column
- * tiles for the wide updates at the middle probe and keeps the faster.
- * chosen / ms_per_system (graph replay time of one system) may be NULL. */
+/* Autotuner: replays a fast graph (BF16x3, up to 10 sweeps; sweeps after
+ * the one that reaches 1e-10 do nothing) at the probe frequencies (at most
+ * 64); the lowest frequency from which every probe reaches 1e-10 becomes
+ * the split frequency, below which a robust graph (BF16x6, up to 16 sweeps)
+ * runs; the 128- and 64-column tiles of the wide updates are timed at the
+ * top probe and the faster kept.  chosen (the fast graph's tuning) and
+ * ms_per_system (its replay time) may be NULL. */
 int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_probe,
                           PeecSweepTuning *chosen, double *ms_per_system);
 /* Solves every frequency: d_X (device) [n_freq][nrhs][Ne + Nv].  A system
@@ -307,6 +310,9 @@ int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_
 int peec_gb300_sweep_run(void *plan, const double *frequencies, size_t n_freq, double tol,
                          Complex *d_X, double *backward_error, int *fallback);
 int peec_gb300_sweep_tuning(void *plan, PeecSweepTuning *tuning);
+/* The frequency below which the plan replays its robust graph (BF16x6, more
+ * sweeps; 0 when it has none) and that graph's tuning. */
+int peec_gb300_sweep_split(void *plan, double *split_frequency, PeecSweepTuning *robust);
 void peec_gb300_sweep_destroy(void *plan);
 
 /* ---- retarded Lp / P (no reference counterpart: the reference's

@@ -259,6 +259,7 @@ EXT_SYMBOLS = [
     ("peec_gb300_sweep_run", C.c_int,
      [C.c_void_p, c_double_p, C.c_size_t, C.c_double, C.c_void_p, c_double_p, c_int_p]),
     ("peec_gb300_sweep_tuning", C.c_int, [C.c_void_p, P(PeecSweepTuning)]),
+    ("peec_gb300_sweep_split", C.c_int, [C.c_void_p, c_double_p, P(PeecSweepTuning)]),
     ("peec_gb300_sweep_destroy", None, [C.c_void_p]),
     ("peec_gb300_lu_timing_enable", None, [C.c_int]),
     ("peec_gb300_lu_timing", C.c_int, [c_double_p, c_double_p, c_double_p, c_double_p]),

@@ -24,7 +24,7 @@ INCLUDE = os.path.join(REPO, "include")
 ORACLE = os.path.join(REPO, "oracle")
 STAGED_REFERENCE = os.path.join(REPO, "baseline", "_ref")
 
-CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu", "matrix_export.cu", "sweep.cu"]
+CUDA_SOURCES = ["runtime.cu", "assembly.cu", "lu.cu", "potential_helpers.cu", "harmonic.cu", "mixed.cu", "server.cu", "transient.cu", "rcs.cu", "incidence.cu", "matrix_export.cu", "sweep.cu", "multirhs.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17", "--fmad=false",

@@ -41,7 +41,6 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
-#include "solve.cuh"
 
 namespace peec {
 
@@ -1199,452 +1198,6 @@ static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long 
     return cuda_ok(cudaLaunchKernelEx(&cfg, k_panel_cl, a, n, k0, kb, rows, limit, piv, st), "cluster FP32 panel launch");
 }
 
-// ---- cluster panel ----------------------------------------------------
-// The same partial-pivoting panel (first maximum wins, NaN never wins, the
-// same swaps and updates, so the same pivots as the reference) on one
-// thread-block cluster of up to 16 CTAs: the panel rows sit in the CTAs'
-// shared memory, candidates are exchanged through distributed shared memory
-// and each column costs one hardware cluster barrier instead of a grid
-// barrier through global memory.  Slots alternate by column parity, so a
-// CTA that runs ahead never overwrites a slot another CTA still reads (it
-// cannot pass the next barrier before the slower one arrives).  Used while
-// the panel fits (rows per CTA x 32 elements in shared memory).
-template <class T>
-struct ClusterSlot {
-    T cand_row[2][NB];  // this CTA's candidate row, by column parity
-    T krow[2][NB];      // row k when owned here
-    double val[2];      // candidate magnitude (as double: exact for float)
-    int idx[2];         // candidate row, n if none
-};
-
-template <class T>
-__global__ void __launch_bounds__(256) k_panel_cluster(T *a, int n, int k0, int kb, int rows_per_cta, double limit,
-                                                       long long *piv, Status *st) {
-    namespace cg = cooperative_groups;
-    cg::cluster_group cluster = cg::this_cluster();
-    using M = typename MagType<T>::type;
-    extern __shared__ __align__(16) unsigned char cl_smem[];
-    ClusterSlot<T> &slot = *reinterpret_cast<ClusterSlot<T> *>(cl_smem);
-    T *tile = reinterpret_cast<T *>(cl_smem + ((sizeof(ClusterSlot<T>) + 15) & ~(size_t)15));  // [rows][NB]
-    __shared__ T s_prow[NB];
-    __shared__ M s_val[8];
-    __shared__ int s_idx[8];
-    __shared__ int s_p, s_pc, s_fail;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int C = (int)cluster.num_blocks(), c = (int)cluster.block_rank();
-    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
-    const int nrows = r1 > r0 ? r1 - r0 : 0;
-    if (st->code != 0) return;  // uniform across the cluster (set before launch)
-    for (int t = tid; t < nrows * kb; t += blockDim.x) {
-        int i = t / kb, j = t % kb;
-        tile[i * NB + j] = a[(size_t)(r0 + i) * n + k0 + j];
-    }
-    __syncthreads();
-    for (int kk = 0; kk < kb; ++kk) {
-        const int k = k0 + kk, par = kk & 1;
-        M best = -1;
-        int bi = n;
-        for (int i = max(r0, k) + tid; i < r1; i += blockDim.x) {
-            M m = mag_t(tile[(i - r0) * NB + kk]);
-            if (i == k && isnan(m)) m = INFINITY;
-            if (isnan(m)) continue;
-            if (m > best || (m == best && i < bi)) {
-                best = m;
-                bi = i;
-            }
-        }
-        for (int sh = 16; sh > 0; sh >>= 1) {
-            M ov = __shfl_xor_sync(0xffffffffu, best, sh);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
-            if (ov > best || (ov == best && oi < bi)) {
-                best = ov;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            s_val[warp] = best;
-            s_idx[warp] = bi;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-                if (s_val[w] > best || (s_val[w] == best && s_idx[w] < bi)) {
-                    best = s_val[w];
-                    bi = s_idx[w];
-                }
-            slot.val[par] = (double)best;
-            slot.idx[par] = bi;
-            s_idx[0] = bi;
-        }
-        __syncthreads();
-        bi = s_idx[0];
-        if (bi < n)
-            for (int j = tid; j < kb; j += blockDim.x) slot.cand_row[par][j] = tile[(bi - r0) * NB + j];
-        if (k >= r0 && k < r1)
-            for (int j = tid; j < kb; j += blockDim.x) slot.krow[par][j] = tile[(k - r0) * NB + j];
-        cluster.sync();
-        // global pivot from the C slots (distributed shared memory)
-        if (warp == 0) {
-            double gb = -1.0;
-            int gi = n, gc = -1;
-            if (lane < C) {
-                ClusterSlot<T> *rs = cluster.map_shared_rank(&slot, lane);
-                int ix = rs->idx[par];
-                double v = rs->val[par];
-                if (ix < n) {
-                    gb = v;
-                    gi = ix;
-                    gc = lane;
-                }
-            }
-            for (int sh = 16; sh > 0; sh >>= 1) {
-                double ov = __shfl_xor_sync(0xffffffffu, gb, sh);
-                int oi = __shfl_xor_sync(0xffffffffu, gi, sh);
-                int oc = __shfl_xor_sync(0xffffffffu, gc, sh);
-                if (ov > gb || (ov == gb && oi < gi)) {
-                    gb = ov;
-                    gi = oi;
-                    gc = oc;
-                }
-            }
-            if (lane == 0) {
-                s_fail = 0;
-                if (gc < 0 || !isfinite(gb) || gb <= limit) {
-                    s_fail = 1;
-                    if (c == 0) {
-                        st->code = 2;
-                        st->column = k;
-                        st->value = gb;
-                    }
-                } else if (c == 0) {
-                    piv[k] = gi;
-                }
-                s_p = gi;
-                s_pc = gc;
-            }
-        }
-        __syncthreads();
-        if (s_fail) {  // identical decision in every CTA of the cluster
-            cluster.sync();  // every CTA has read the slots before any leaves
-            return;
-        }
-        const int p = s_p, pc = s_pc;
-        {
-            ClusterSlot<T> *ps = cluster.map_shared_rank(&slot, pc);
-            for (int j = tid; j < kb; j += blockDim.x) s_prow[j] = ps->cand_row[par][j];
-        }
-        __syncthreads();
-        if (p != k) {
-            if (k >= r0 && k < r1)
-                for (int j = tid; j < kb; j += blockDim.x) tile[(k - r0) * NB + j] = s_prow[j];
-            if (p >= r0 && p < r1) {
-                const int kc = (k - k0) / rows_per_cta;  // owner of row k
-                ClusterSlot<T> *ks = cluster.map_shared_rank(&slot, kc);
-                for (int j = tid; j < kb; j += blockDim.x) tile[(p - r0) * NB + j] = ks->krow[par][j];
-            }
-        }
-        __syncthreads();
-        if (k + 1 >= n) break;
-        const T pivot = s_prow[kk];
-        for (int i = max(r0, k + 1) + tid; i < r1; i += blockDim.x) {
-            T *row = tile + (i - r0) * NB;
-            T m = divide(row[kk], pivot);
-            row[kk] = m;
-            for (int j = kk + 1; j < kb; ++j) row[j] = msub(row[j], m, s_prow[j]);
-        }
-        __syncthreads();
-    }
-    for (int t = tid; t < nrows * kb; t += blockDim.x) {
-        int i = t / kb, j = t % kb;
-        a[(size_t)(r0 + i) * n + k0 + j] = tile[i * NB + j];
-    }
-    cluster.sync();  // no CTA leaves while another may still read its slots
-}
-
-// ---- tournament-pivoting panel (mixed path) ----------------------------
-// Communication-avoiding LU of the FP32 panel (rows k0..n-1, columns
-// k0..k0+kb-1) with tournament pivoting: each CTA factors its own rows with
-// partial pivoting and nominates the rows it picked; groups of 8 CTAs
-// merge their nominees the same way, then CTA 0 merges the group winners and
-// factors the final pivot rows.  Four bounded grid barriers per panel
-// instead of one per column (plus one before the panel is written back).
-// The pivots differ from partial pivoting (so
-// this is used only by the FP32 factorisation, whose result is refined in
-// FP64); every non-pivot row becomes L21 = A21 U11^-1 from its original
-// values.  piv[] receives the equivalent sequential swaps.
-static const int kCaluGroup = 8;          // CTAs whose nominees one leader merges
-static const int kCaluRows = 256;         // rows per CTA in the first two phases (local rows, group nominees)
-static const int kCaluMaxRows = 640;      // group winners merged by CTA 0 (up to 160 CTAs)
-
-struct CaluScratch {
-    PanelSlots *ps;
-    cplxf *cand;     // [G][NB][NB] nominated rows (original values)
-    int *cand_idx;   // [G][NB] their rows, -1 = none
-    cplxf *cand2;    // [groups][NB][NB]
-    int *cand2_idx;  // [groups][NB]
-    cplxf *top;      // [NB][NB] factored pivot rows (L11 \ U11)
-    int *fpiv;       // [NB] final pivot rows in order
-};
-
-// Partial-pivoting LU of the m x kb block W (rows of NB in shared memory,
-// ids[] the rows they came from): after the call the first min(m, kb) rows
-// are the chosen pivot rows in order (ids permuted with them).  NaN never
-// wins; a row whose magnitude is NaN at the diagonal counts as +inf (as the
-// reference's panel).  All threads of the CTA call it.
-__device__ void calu_block_lu(cplxf *W, int *ids, int m, int kb) {
-    __shared__ float s_v[8];
-    __shared__ int s_i[8];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int steps = min(m, kb);
-    for (int j = 0; j < steps; ++j) {
-        float best = -1.0f;
-        int bi = m;
-        for (int r = j + tid; r < m; r += blockDim.x) {
-            float v = mag_t(W[r * kPS + j]);
-            if (r == j && isnan(v)) v = INFINITY;
-            if (isnan(v)) continue;
-            if (v > best || (v == best && r < bi)) {
-                best = v;
-                bi = r;
-            }
-        }
-        for (int sh = 16; sh > 0; sh >>= 1) {
-            float ov = __shfl_xor_sync(0xffffffffu, best, sh);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, sh);
-            if (ov > best || (ov == best && oi < bi)) {
-                best = ov;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            s_v[warp] = best;
-            s_i[warp] = bi;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-                if (s_v[w] > best || (s_v[w] == best && s_i[w] < bi)) {
-                    best = s_v[w];
-                    bi = s_i[w];
-                }
-            s_i[0] = bi < m ? bi : j;  // no candidate (all NaN): keep row j
-        }
-        __syncthreads();
-        const int p = s_i[0];
-        if (p != j) {
-            for (int c = tid; c < NB; c += blockDim.x) {
-                cplxf t = W[j * kPS + c];
-                W[j * kPS + c] = W[p * kPS + c];
-                W[p * kPS + c] = t;
-            }
-            if (tid == 0) {
-                int t = ids[j];
-                ids[j] = ids[p];
-                ids[p] = t;
-            }
-        }
-        __syncthreads();
-        const cplxf piv = W[j * kPS + j];
-        for (int r = j + 1 + tid; r < m; r += blockDim.x) {
-            cplxf *row = W + r * kPS;
-            cplxf l = divide(row[j], piv);
-            row[j] = l;
-            for (int c = j + 1; c < kb; ++c) row[c] = msub(row[c], l, W[j * kPS + c]);
-        }
-        __syncthreads();
-    }
-}
-
-__global__ void __launch_bounds__(256) k_panel_calu(cplxf *a, int n, int k0, int kb, int rows_per_cta, double limit,
-                                                    long long *piv, Status *st, CaluScratch S) {
-    extern __shared__ __align__(16) unsigned char calu_smem[];
-    // W: work rows; O: the same rows' original values (phases 1-2 only, so
-    // phase 3 may use the whole buffer for W)
-    cplxf *W = reinterpret_cast<cplxf *>(calu_smem);                 // [kCaluMaxRows][kPS]
-    cplxf *O = W + kCaluRows * kPS;                                  // [kCaluRows][kPS]
-    int *ids = reinterpret_cast<int *>(W + kCaluMaxRows * kPS);      // [kCaluMaxRows]
-    __shared__ int s_prow[2 * NB], s_pos[2 * NB], s_nt;              // touched rows and where they end
-    __shared__ cplxf s_top[NB * NB];
-    const int tid = threadIdx.x;
-    const unsigned G = gridDim.x;
-    const int c = blockIdx.x;
-    const int r0 = k0 + c * rows_per_cta, r1 = min(n, r0 + rows_per_cta);
-    const int nrows = r1 > r0 ? r1 - r0 : 0;
-    if (st->code != 0) return;  // uniform (set before launch)
-    unsigned int gen = *(volatile unsigned int *)&S.ps->gen;
-    // 1. local partial pivoting on this CTA's rows, nominate its pivot rows
-    for (int t = tid; t < nrows * NB; t += blockDim.x) {
-        int i = t / NB, j = t % NB;
-        cplxf v = j < kb ? a[(size_t)(r0 + i) * n + k0 + j] : cplxf{0.0f, 0.0f};
-        W[i * kPS + j] = v;
-        O[i * kPS + j] = v;
-    }
-    for (int i = tid; i < nrows; i += blockDim.x) ids[i] = i;  // local index into O
-    __syncthreads();
-    calu_block_lu(W, ids, nrows, kb);
-    const int nc = min(nrows, kb);
-    for (int t = tid; t < NB * NB; t += blockDim.x) {
-        int i = t / NB, j = t % NB;
-        S.cand[((size_t)c * NB + i) * NB + j] = i < nc ? O[ids[i] * kPS + j] : cplxf{0.0f, 0.0f};
-    }
-    for (int i = tid; i < NB; i += blockDim.x) S.cand_idx[c * NB + i] = i < nc ? r0 + ids[i] : -1;
-    if (!grid_barrier(S.ps, G, gen)) {
-        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
-        return;
-    }
-    // 2. group leaders merge the nominees of their 8 CTAs
-    const int groups = (int)((G + kCaluGroup - 1) / kCaluGroup);
-    __shared__ int s_off[kCaluMaxRows / NB + 1];  // compaction offsets (phase 2: CTAs, phase 3: groups)
-    __shared__ int s_gr[kCaluMaxRows];  // global row of each gathered candidate
-    if (c % kCaluGroup == 0) {
-        const int g = c / kCaluGroup, nq = min((int)G, c + kCaluGroup) - c;
-        // valid nominees of CTA q are its first count(q) slots: compaction offsets
-        if (tid < nq) {
-            int cnt = 0;
-            for (int i = 0; i < NB; ++i) cnt += ld_volatile(S.cand_idx + (c + tid) * NB + i) >= 0;
-            s_off[tid + 1] = cnt;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            s_off[0] = 0;
-            for (int q = 0; q < nq; ++q) s_off[q + 1] += s_off[q];
-        }
-        __syncthreads();
-        const int m = s_off[nq];
-        for (int t = tid; t < nq * NB * NB; t += blockDim.x) {
-            const int q = t / (NB * NB), i = (t / NB) % NB, j = t % NB;
-            if (i < s_off[q + 1] - s_off[q]) {
-                cplxf v = ld_volatile(S.cand + ((size_t)(c + q) * NB + i) * NB + j);
-                W[(s_off[q] + i) * kPS + j] = v;
-                O[(s_off[q] + i) * kPS + j] = v;
-                if (j == 0) s_gr[s_off[q] + i] = ld_volatile(S.cand_idx + (c + q) * NB + i);
-            }
-        }
-        for (int i = tid; i < m; i += blockDim.x) ids[i] = i;
-        __syncthreads();
-        calu_block_lu(W, ids, m, kb);
-        const int w2 = min(m, kb);
-        for (int t = tid; t < NB * NB; t += blockDim.x) {
-            int i = t / NB, j = t % NB;
-            S.cand2[((size_t)g * NB + i) * NB + j] = i < w2 ? O[ids[i] * kPS + j] : cplxf{0.0f, 0.0f};
-        }
-        for (int i = tid; i < NB; i += blockDim.x) S.cand2_idx[g * NB + i] = i < w2 ? s_gr[ids[i]] : -1;
-    }
-    if (!grid_barrier(S.ps, G, gen)) {
-        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
-        return;
-    }
-    // 3. CTA 0 merges the group winners and factors the pivot rows
-    if (c == 0) {
-        if (tid < groups) {
-            int cnt = 0;
-            for (int i = 0; i < NB; ++i) cnt += ld_volatile(S.cand2_idx + tid * NB + i) >= 0;
-            s_off[tid + 1] = cnt;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            s_off[0] = 0;
-            for (int q = 0; q < groups; ++q) s_off[q + 1] += s_off[q];
-        }
-        __syncthreads();
-        const int m = s_off[groups];
-        for (int t = tid; t < groups * NB * NB; t += blockDim.x) {
-            const int q = t / (NB * NB), i = (t / NB) % NB, j = t % NB;
-            if (i < s_off[q + 1] - s_off[q]) {
-                W[(s_off[q] + i) * kPS + j] = ld_volatile(S.cand2 + ((size_t)q * NB + i) * NB + j);
-                if (j == 0) s_gr[s_off[q] + i] = ld_volatile(S.cand2_idx + q * NB + i);
-            }
-        }
-        for (int i = tid; i < m; i += blockDim.x) ids[i] = i;
-        __syncthreads();
-        calu_block_lu(W, ids, m, kb);
-        if (tid == 0) {
-            for (int i = 0; i < kb; ++i) {
-                const double dm = i < m ? (double)mag_t(W[i * kPS + i]) : 0.0;
-                if (i >= m || !isfinite(dm) || dm <= limit) {
-                    st->code = 2;
-                    st->column = k0 + i;
-                    st->value = dm;
-                    break;
-                }
-            }
-        }
-        __syncthreads();
-        for (int t = tid; t < NB * NB; t += blockDim.x) S.top[t] = W[(t / NB) * kPS + t % NB];
-        for (int i = tid; i < NB; i += blockDim.x) S.fpiv[i] = i < kb && i < m ? s_gr[ids[i]] : -1;
-    }
-    if (!grid_barrier(S.ps, G, gen)) {
-        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
-        return;
-    }
-    if (ld_volatile(&st->code) != 0) return;  // a singular pivot block: every CTA leaves here
-    // the merges overwrote the shared buffers: reload this CTA's original
-    // rows (nothing has written the panel yet) before anyone writes it
-    cplxf *Own = W;
-    for (int t = tid; t < nrows * NB; t += blockDim.x) {
-        int i = t / NB, j = t % NB;
-        Own[i * kPS + j] = j < kb ? a[(size_t)(r0 + i) * n + k0 + j] : cplxf{0.0f, 0.0f};
-    }
-    // 4. sequential swaps equivalent to moving fpiv[i] to row k0 + i (piv[]),
-    //    and where every touched row ends: entries (row s_prow[t] at
-    //    position s_pos[t]); untouched rows stay where they are
-    if (tid == 0) {
-        int nt = 0;
-        for (int i = 0; i < kb; ++i) {
-            const int r = ld_volatile(S.fpiv + i), p = k0 + i;
-            int tr = -1, tp = -1;
-            for (int t = 0; t < nt; ++t) {
-                if (s_prow[t] == r) tr = t;
-                if (s_pos[t] == p) tp = t;
-            }
-            const int q = tr >= 0 ? s_pos[tr] : r;  // current position of row r
-            if (c == 0) piv[p] = q;
-            if (q == p) continue;
-            const int rp = tp >= 0 ? s_prow[tp] : p;  // the row now at p moves to q
-            if (tr < 0) {
-                tr = nt++;
-                s_prow[tr] = r;
-            }
-            if (tp < 0) {
-                tp = nt++;
-                s_prow[tp] = rp;
-            }
-            s_pos[tr] = p;
-            s_pos[tp] = q;
-        }
-        s_nt = nt;
-    }
-    for (int t = tid; t < NB * NB; t += blockDim.x) s_top[t] = ld_volatile(S.top + t);
-    if (!grid_barrier(S.ps, G, gen)) {  // every CTA holds its originals
-        if (c == 0 && tid == 0) atomicCAS(&st->code, 0, 6);
-        return;
-    }
-    // 5. write this CTA's original rows at their final positions: pivot rows
-    //    get L11 \ U11 (from CTA 0's factorisation), the others
-    //    L21 = A21 U11^-1 (forward substitution along the row)
-    for (int i = tid; i < nrows; i += blockDim.x) {
-        const int r = r0 + i;
-        int pos = r;
-        for (int t = 0; t < s_nt; ++t)
-            if (s_prow[t] == r) pos = s_pos[t];
-        cplxf *dst = a + (size_t)pos * n + k0;
-        if (pos < k0 + kb) {
-            const cplxf *src = s_top + (pos - k0) * NB;
-            for (int j = 0; j < kb; ++j) dst[j] = src[j];
-        } else {
-            cplxf x[NB];
-#pragma unroll
-            for (int j = 0; j < NB; ++j) {
-                if (j < kb) {
-                    cplxf v = Own[i * kPS + j];
-                    for (int q = 0; q < j; ++q) v = msub(v, x[q], s_top[q * NB + j]);
-                    x[j] = divide(v, s_top[j * NB + j]);
-                    dst[j] = x[j];
-                }
-            }
-        }
-    }
-}
 
 // ---- row swaps outside the panel -------------------------------------
 static const int kLaswpCols = 32;  // columns per k_laswp block (shared memory 2 NB x 32 x 16 bytes at most)
@@ -2051,6 +1604,7 @@ struct WaveArgs {
     int subst;                // upper blocks by substitution (dinv's upper half from k_diag_copy_upper)
     const int *refine_blocks;  // if set: [nb][2] (lower, upper), 1 = that diagonal block's solve takes one
                                // step of iterative refinement after the inverse (k_diag_flags)
+    const int *skip;           // if set and *skip != 0 the launch does nothing (a converged graph sweep)
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -2474,6 +2028,7 @@ __device__ bool wave_block(const WaveArgs<T> &A, int blk, int c0, int nr, unsign
 
 template <class T, int NR>
 __global__ void __launch_bounds__(256) k_trsv_wave(WaveArgs<T> A) {
+    if (A.skip && *A.skip) return;  // uniform: written before the launch
     extern __shared__ __align__(16) unsigned char wave_smem[];
     WaveSmem<T, NR> &S = *reinterpret_cast<WaveSmem<T, NR> *>(wave_smem);
     __shared__ int s_ok;
@@ -2572,25 +2127,6 @@ static bool wave_solve(WaveArgs<T> A) {
                    "triangular solve launch");
 }
 
-size_t wave_flag_words_real(int n, int nrhs) { return wave_flag_count<double>(n, nrhs); }
-size_t wave_dinv_words_real(int n) { return wave_dinv_count(n); }
-bool wave_prepare_real(const double *lu, int n, double *dinv) { return wave_prepare(lu, n, dinv); }
-
-bool wave_solve_real(const double *lu, const double *dinv, const int *perm, int n, const double *b, double *x,
-                     int nrhs, unsigned *flags, int *err) {
-    WaveArgs<double> A{};
-    A.lu = lu;
-    A.dinv = dinv;
-    A.refine_blocks = wave_refine_flags(const_cast<double *>(dinv), n);
-    A.n = n;
-    A.nrhs = nrhs;
-    A.perm = perm;
-    A.b = b;
-    A.x = x;
-    A.flags = flags;
-    A.error = err;
-    return wave_solve(A);
-}
 
 // ---------------------------------------------------------------------
 // registry: device copies of factorisations, keyed by the host data
@@ -2709,85 +2245,6 @@ struct CoopPlan {
     size_t smem = 0;
 };
 
-// Tournament panel for the FP32 factorisation: G CTAs (one per SM) when the
-// panel has enough rows; false when it does not apply.
-static bool launch_calu_panel(cplxf *a, int n, int k0, int kb, double limit, long long *piv, Status *st,
-                              const CaluScratch &S, int sms) {
-    const int m = n - k0;
-    if (m < 2 * 64) return false;
-    const int G = std::min(sms, std::min(kCaluMaxRows / NB * kCaluGroup, (m + NB - 1) / NB));
-    const int rows = (m + G - 1) / G;
-    if (rows > kCaluRows) return false;
-    constexpr size_t smem = (size_t)kCaluMaxRows * kPS * sizeof(cplxf) + kCaluMaxRows * sizeof(int);
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k_panel_calu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (attr != cudaSuccess) return false;
-    static const int per_sm = [] {
-        int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_panel_calu, 256, smem);
-        return v;
-    }();
-    if (per_sm < 1) return false;
-    int rows_v = rows, kb_v = kb, n_v = n, k0_v = k0;
-    double lim = limit;
-    CaluScratch sv = S;
-    void *args[] = {&a, &n_v, &k0_v, &kb_v, &rows_v, &lim, &piv, &st, &sv};
-    note_launch();
-    return cuda_ok(cudaLaunchCooperativeKernel((const void *)k_panel_calu, dim3(G), dim3(256), args, smem, stream()),
-                   "tournament panel launch");
-}
-
-// Cluster panel: C CTAs (16 where the device allows non-portable clusters,
-// else 8) when the m panel rows fit their shared memory.  Returns false
-// when the cluster panel does not apply; the caller then uses the
-// cooperative grid panel.
-template <class T>
-static bool launch_cluster_panel(T *a, int n, int k0, int kb, double limit, long long *piv, Status *st) {
-    const int m = n - k0;
-    if (m < 2 * 64) return false;  // small panels: one CTA is faster
-    static const size_t kMaxSmem = 220 * 1024;
-    static const size_t head = (sizeof(ClusterSlot<T>) + 15) & ~(size_t)15;
-    static const int max_c = [] {
-        cudaFuncSetAttribute(k_panel_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-        cudaFuncSetAttribute(k_panel_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(16);
-        cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = kMaxSmem;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = 16;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int c = 0;
-        if (cudaOccupancyMaxPotentialClusterSize(&c, k_panel_cluster<T>, &cfg) != cudaSuccess) c = 0;
-        cudaGetLastError();
-        return c >= 16 ? 16 : c >= 8 ? 8 : 0;
-    }();
-    if (max_c == 0) return false;
-    const int C = max_c;
-    const int rows = (m + C - 1) / C;
-    const size_t smem = head + (size_t)rows * NB * sizeof(T);
-    if (smem > kMaxSmem) return false;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(C);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream();
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = C;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    note_launch();
-    return cuda_ok(cudaLaunchKernelEx(&cfg, k_panel_cluster<T>, a, n, k0, kb, rows, limit, piv, st),
-                   "cluster panel launch");
-}
-
 template <class T>
 static CoopPlan<T> coop_plan(int m) {
     CoopPlan<T> pl;
@@ -2813,21 +2270,6 @@ static CoopPlan<T> coop_plan(int m) {
     return pl;
 }
 
-// Panel form: the cooperative grid panel by default; PEEC_GB300_PANEL=cluster
-// selects the 16-CTA cluster panel where it fits.  Measured on GB300 (8402
-// unknowns) the cluster form is slower -- the mixed panel 68 ms against 55 ms,
-// the plain 116 ms against 105 ms: its dependent distributed-shared-memory
-// reads and the larger per-CTA row count cost more per column than the grid
-// barrier saves -- so it stays an alternative, checked to give the same
-// factors bit for bit.
-static bool cluster_panel_enabled() {
-    static const bool on = [] {
-        const char *e = getenv("PEEC_GB300_PANEL");
-        return e && strcmp(e, "cluster") == 0;
-    }();
-    return on;
-}
-
 // Split-BF16 terms the mixed path's first factorisation uses: 3 (BF16x3),
 // or 6 (BF16x6) with PEEC_GB300_MIXED_SPLIT=6.
 static int mixed_split_terms() {
@@ -2840,11 +2282,11 @@ static int mixed_split_terms() {
 
 // FP32 panel of the mixed path: the cluster panel (k_panel_cl) where the
 // panel fits one cluster's shared memory, else the lean grid panel, else the
-// cooperative one.  PEEC_GB300_MIXED_PANEL=lean / coop / calu selects a form.
+// cooperative one.  PEEC_GB300_MIXED_PANEL=lean / coop selects a form.
 static bool cl_panel_enabled() {
     static const bool on = [] {
         const char *e = getenv("PEEC_GB300_MIXED_PANEL");
-        return !(e && (strcmp(e, "lean") == 0 || strcmp(e, "coop") == 0 || strcmp(e, "calu") == 0));
+        return !(e && (strcmp(e, "lean") == 0 || strcmp(e, "coop") == 0));
     }();
     return on;
 }
@@ -2869,12 +2311,12 @@ static int lean_panel_ctas(int m) {
 }
 
 // CTAs of the lean FP64 panel (k_panel_lean64) for m rows, 0 where it does
-// not apply (PEEC_GB300_PANEL=coop or =cluster selects another form).
+// not apply (PEEC_GB300_PANEL=coop selects the cooperative grid panel).
 template <class T>
 static int lean64_panel_ctas(int m) {
     static const int cap = [] {
         const char *e = getenv("PEEC_GB300_PANEL");
-        if (e && (strcmp(e, "coop") == 0 || strcmp(e, "cluster") == 0)) return 0;
+        if (e && strcmp(e, "coop") == 0) return 0;
         int dev = 0, sms = 0, coop = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -2887,21 +2329,6 @@ static int lean64_panel_ctas(int m) {
     if (m < 2 * kLeanThreads) return 0;
     const int g = (m + kLeanThreads - 1) / kLeanThreads;
     return g <= cap && g <= 32 * kLeanPoll ? g : 0;
-}
-
-// FP32 panels of the mixed path by tournament pivoting when
-// PEEC_GB300_MIXED_PANEL=calu; partial pivoting otherwise.  Measured on
-// GB300 (8402 unknowns) the tournament panel takes 75 ms per factorisation
-// against 49 ms for the cooperative partial-pivoting panel: its four grid
-// barriers per panel are cheaper than 32, but every CTA's local LU of 256+
-// rows and the two merge levels serialise more FP32 work than the barriers
-// save at 32-column panels.
-static bool calu_panel_enabled() {
-    static const bool on = [] {
-        const char *e = getenv("PEEC_GB300_MIXED_PANEL");
-        return e && strcmp(e, "calu") == 0;
-    }();
-    return on;
 }
 
 // Complex trailing update form: the direct 4-product form (default; it keeps
@@ -2997,8 +2424,7 @@ static bool factor_device(T *d_a, int n, double limit, long long *d_piv, Status 
         tm.mark(2);
         CoopPlan<T> pl = coop_plan<T>(n - k0);
         const int lean_g = lean64_panel_ctas<T>(n - k0);
-        if (cluster_panel_enabled() && launch_cluster_panel<T>(d_a, n, k0, kb, limit, d_piv, d_st)) {
-        } else if (lean_g > 0) {
+        if (lean_g > 0) {
             unsigned long long *fl = lean_flag.p;
             int fls = lean_stride;
             int *li = lean_idx.p;
@@ -4002,7 +3428,9 @@ __global__ void __launch_bounds__(256) k_lower_inv(const cplxf *a, int n, int K0
 }
 
 // y = P D_r^-1 r in FP32 (the permuted, row-scaled residual)
-__global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int n, int nrhs, cplxf *y) {
+__global__ void k_mix_rhs(const cplx *r, const int *perm, const double *rs, int n, int nrhs, cplxf *y,
+                          const int *skip) {
+    if (skip && *skip) return;
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)n * nrhs) return;
     int q = (int)(t / n), i = (int)(t % n), src = perm[i];
@@ -4017,7 +3445,9 @@ __global__ void k_abs_matrix(const cplx *Z, size_t count, float *out) {
 }
 
 // x += D_c^-1 y  (FP64 accumulation of the FP32 correction)
-__global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs, float *absx) {
+__global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, int nrhs, float *absx,
+                             const int *skip) {
+    if (skip && *skip) return;
     size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (t >= (size_t)n * nrhs) return;
     int i = (int)(t % n);
@@ -4033,7 +3463,8 @@ __global__ void k_mix_update(cplx *x, const cplxf *y, const double *cs, int n, i
 // componentwise backward error |r_i| / (sum_j |Z_ij||x_j| + |b_i|), the
 // denominator from FP32 magnitudes, max-reduced as IEEE bits.
 __global__ void k_residual(const cplx *Z, const float *absZ, const cplx *x, const float *absx, const cplx *b, int n,
-                           int nrhs, cplx *r, unsigned long long *be) {
+                           int nrhs, cplx *r, unsigned long long *be, const int *skip) {
+    if (skip && *skip) return;
     long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= (long long)n * nrhs) return;
@@ -4064,6 +3495,18 @@ __global__ void k_residual(const cplx *Z, const float *absZ, const cplx *x, cons
         if (!isfinite(eta)) eta = INFINITY;
         atomicMax(be, (unsigned long long)__double_as_longlong(eta));
     }
+}
+
+// A graph sweep's convergence flag: *done = (backward error <= tol); the
+// backward error accumulator is zeroed for the next residual unless done.
+__global__ void k_sweep_done(const unsigned long long *be, double tol, int *done) {
+    if (*done) return;
+    double eta;
+    memcpy(&eta, be, sizeof(eta));
+    *done = eta <= tol;
+}
+__global__ void k_zero_unless_done(unsigned long long *be, const int *done) {
+    if (!*done) *be = 0ull;
 }
 
 __global__ void k_abs_x(const cplx *x, size_t count, float *absx) {
@@ -4233,7 +3676,7 @@ extern "C" int peec_gb300_complex_refine_device(const Complex *d_Z, const Comple
         cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
         PEEC_LAUNCH(k_abs_x, (unsigned)((nv + 255) / 256), 256, 0, x, nv, absx.p);
         PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, (const cplx *)d_b, n,
-                    nrhs, r.p, be.p);
+                    nrhs, r.p, be.p, (const int *)nullptr);
         unsigned long long hb = 0;
         cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
         if (!launch_ok("refinement") || !sync("refinement")) return -1;
@@ -4256,6 +3699,14 @@ __global__ void k_capture_status(const Status *st, const int *werr, const unsign
     *eta_out = *be;
 }
 
+bool mrhs_sweep(const void *Z, const float *absZ, const void *lu, const int *perm, const double *rs,
+                const double *cs, int n, int nrhs, const void *b, void *x, void *r, void *Y, float *absx,
+                unsigned long long *be);
+// from this many right-hand sides on, the refinement sweeps use the blocked
+// many-right-hand-side form (multirhs.cu) instead of the wavefront solve
+// (NR right-hand sides per pass) and the per-row residual
+static const int kManyRhs = 32;
+
 int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex *d_x, size_t nrhs_, double tol,
                      int max_iter, double *backward_error, int *iterations, const MixedCapture *cap) {
     if (!d_Z || !d_b || !d_x || n_ == 0 || nrhs_ == 0 || n_ > (size_t)0x7fffffff || max_iter < 1) return -1;
@@ -4276,11 +3727,6 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     const int OB = 256;
     DBuf<__nv_bfloat16> ap((size_t)n * 12 * OB), bpr((size_t)n * 12 * OB), bpi((size_t)n * 12 * OB);
     DBuf<cplxf> linv((size_t)OB * OB);  // I - L11^-1 of one outer block
-    // tournament panel scratch (nominees of every CTA and group, the pivot block)
-    const int kMaxCta = kCaluMaxRows / NB * kCaluGroup;
-    DBuf<cplxf> calu_rows((size_t)(kMaxCta + kMaxCta / kCaluGroup + 1) * NB * NB);
-    DBuf<int> calu_idx((size_t)(kMaxCta + kMaxCta / kCaluGroup + 1) * NB);
-    DBuf<PanelSlots> calu_ps(1);
     DBuf<unsigned char> scratch;
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -4294,7 +3740,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     DBuf<int> lean_idx(2 * GL);
     DBuf<cplxf> lean_rows(2 * GL * NB + 2 * NB);
     if (!f.p || !y.p || !r.p || !rs.p || !cs.p || !piv.p || !perm.p || !err.p || !st.p || !mx.p || !be.p || !ap.p ||
-        !bpr.p || !bpi.p || !linv.p || !calu_rows.p || !calu_idx.p || !calu_ps.p || !scratch.alloc(sbytes) ||
+        !bpr.p || !bpi.p || !linv.p || !scratch.alloc(sbytes) ||
         !lean_flag.p || !lean_idx.p || !lean_rows.p)
         return -1;
     cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
@@ -4307,15 +3753,6 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
     cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), stream());
     cudaMemsetAsync(err.p, 0, sizeof(int), stream());
-    cudaMemsetAsync(calu_ps.p, 0, sizeof(PanelSlots), stream());
-    CaluScratch cs_calu;
-    cs_calu.ps = calu_ps.p;
-    cs_calu.cand = calu_rows.p;
-    cs_calu.cand_idx = calu_idx.p;
-    cs_calu.cand2 = calu_rows.p + (size_t)kMaxCta * NB * NB;
-    cs_calu.cand2_idx = calu_idx.p + (size_t)kMaxCta * NB;
-    cs_calu.top = cs_calu.cand2 + (size_t)(kMaxCta / kCaluGroup) * NB * NB;
-    cs_calu.fpiv = cs_calu.cand2_idx + (size_t)(kMaxCta / kCaluGroup) * NB;
     PanelScratch sc;
     {
         unsigned char *bb = scratch.p;
@@ -4352,7 +3789,10 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     // split-BF16 terms of the trailing update products: BF16x3 first (about
     // 16 bits), BF16x6 (FP32-equivalent) when refinement from the BF16x3
     // factor stalls; PEEC_GB300_MIXED_SPLIT=6 starts with BF16x6
-    int T = cap ? cap->split_terms : mixed_split_terms();
+    // (many right-hand sides: BF16x6 from the start -- the factorisation is
+    // a small part of such a solve, every refinement sweep reads Z for all
+    // right-hand sides, and the BF16x6 factor needs fewer sweeps)
+    int T = cap ? cap->split_terms : (nrhs >= kManyRhs ? 6 : mixed_split_terms());
     // FP32 factorisation of f, trailing updates on the tensor cores: 0, -2 on
     // a pivot breakdown, -1 on errors
     auto factor = [&]() -> int {
@@ -4407,9 +3847,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
                 tm.mark(2);
                 CoopPlan<cplxf> pl = coop_plan<cplxf>(n - k0);
                 const int lean_g = lean_panel_ctas(n - k0);
-                if (calu_panel_enabled() && launch_calu_panel(a, n, k0, kb, limit, piv.p, st.p, cs_calu, sms)) {
-                } else if (cluster_panel_enabled() && launch_cluster_panel<cplxf>(a, n, k0, kb, limit, piv.p, st.p)) {
-                } else if (cl_panel_enabled() && launch_cl_panel(a, n, k0, kb, limit, piv.p, st.p)) {
+                if (cl_panel_enabled() && launch_cl_panel(a, n, k0, kb, limit, piv.p, st.p)) {
                 } else if (lean_g > 0) {
                     Status *stp = st.p;
                     long long *pivp = piv.p;
@@ -4494,7 +3932,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     // factor is the better choice then -- or a factor 2 below the smallest
     // six sweeps earlier with BF16x6); -1 on errors
     DBuf<unsigned> wflags(wave_flag_count<cplxf>(n, nrhs));
-    DBuf<int> werr(1);
+    DBuf<int> werr(1), done(1);  // done: a graph sweep converged (later sweeps are no-ops)
     DBuf<cplxf> wdinv(wave_dinv_count(n));
     DBuf<float> absx(nv);
     if (!wflags.p || !werr.p || !wdinv.p || !absx.p) return -1;
@@ -4509,8 +3947,17 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
         // residual + backward error): captured once as a CUDA graph and
         // replayed per iteration
         auto sweep = [&]() {
-            PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p);
+            if (nrhs >= kManyRhs) {
+                // many right-hand sides: blocked substitution with GEMM updates
+                // and the residual in GEMM form (multirhs.cu)
+                cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+                mrhs_sweep(Z, absZ.p, a, perm.p, rs.p, cs.p, n, nrhs, b, x, r.p, y.p, absx.p, be.p);
+                return;
+            }
+            const int *skip = cap ? done.p : nullptr;
+            PEEC_LAUNCH(k_mix_rhs, (unsigned)((nv + 255) / 256), 256, 0, r.p, perm.p, rs.p, n, nrhs, y.p, skip);
             WaveArgs<cplxf> W{};
+            W.skip = skip;
             W.lu = a;
             W.dinv = wdinv.p;
             W.n = n;
@@ -4521,12 +3968,17 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             W.error = werr.p;
             W.subst = 1;  // backward stable for ill-conditioned diagonal blocks of the FP32 factor
             wave_solve(W);
-            PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs, absx.p);
-            cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
+            PEEC_LAUNCH(k_mix_update, (unsigned)((nv + 255) / 256), 256, 0, x, y.p, cs.p, n, nrhs, absx.p, skip);
+            if (cap)
+                PEEC_LAUNCH(k_zero_unless_done, 1, 1, 0, be.p, (const int *)done.p);
+            else
+                cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
             PEEC_LAUNCH(k_residual, (unsigned)((nv * 32 + 255) / 256), 256, 0, Z, absZ.p, x, absx.p, b, n, nrhs, r.p,
-                        be.p);
+                        be.p, skip);
+            if (cap) PEEC_LAUNCH(k_sweep_done, 1, 1, 0, (const unsigned long long *)be.p, cap->tol, done.p);
         };
         if (cap) {
+            cudaMemsetAsync(done.p, 0, sizeof(int), stream());
             for (int it = 0; it < cap->sweeps; ++it) sweep();
             total_it = cap->sweeps;
             return launch_ok("refinement") ? 0 : -1;
@@ -4634,7 +4086,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             for (int outer = 0; outer < 10; ++outer) {
                 cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
                 PEEC_LAUNCH(k_abs_x, gn, 256, 0, xq, (size_t)n, absx.p);
-                PEEC_LAUNCH(k_residual, gw, 256, 0, Z, absZ.p, xq, absx.p, bq, n, 1, r.p, be.p);
+                PEEC_LAUNCH(k_residual, gw, 256, 0, Z, absZ.p, xq, absx.p, bq, n, 1, r.p, be.p, (const int *)nullptr);
                 PEEC_LAUNCH(k_scale_rows, gn, 256, 0, r.p, rs.p, n, V.p);
                 PEEC_LAUNCH(k_norm2, 1, 1024, 0, V.p, n, nrm.p);
                 unsigned long long hb = 0;
@@ -4745,7 +4197,6 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
         cudaMemsetAsync(scratch.p, 0, sbytes, stream());
         cudaMemsetAsync(st.p, 0, sizeof(Status), stream());
         cudaMemsetAsync(err.p, 0, sizeof(int), stream());
-        cudaMemsetAsync(calu_ps.p, 0, sizeof(PanelSlots), stream());
         cudaMemsetAsync(lean_flag.p, 0, lean_flag.n * sizeof(unsigned long long), stream());
         PEEC_LAUNCH(k_eq2_to_float, 152 * 16, 256, 0, Z, n, er.p, ec.p, f.p, (float *)nullptr);
     }

@@ -63,10 +63,11 @@ struct Job {
     bool done = false;
 };
 
-// factor + A S + diagonal-block inverses + vectors of a transient system
+// a transient system at its peak (the factor and the inverse formed from
+// it, before the factor is freed) + A S + vectors
 static size_t transient_system_bytes(size_t ne, size_t nv) {
-    size_t nt = ne + nv, nb = (nt + 63) / 64;
-    return 8 * nt * nt + 8 * ne * nv + 8 * nb * 2 * 64 * 64 + 64 * nt + 16 * ne;
+    size_t nt = ne + nv;
+    return 16 * nt * nt + 8 * ne * nv + 64 * nt + 16 * ne;
 }
 
 class Server {
@@ -391,14 +392,15 @@ class Server {
             status = peec_gb300_complex_lu_factor_device(W.p, n, 1e-14, piv.p, perm.p, rs.p, cs.p, &scale, &col);
             if (status == 0)
                 status = peec_gb300_complex_lu_solve_device(W.p, perm.p, rs.p, cs.p, n, B.p, X.p, nrhs);
-            if (status == 0 && j.res.fallback) {
-                // the fallback refines in FP64 with the FP64 factor to the gate
+            if (status == 0) {
+                // FP64 iterative refinement with the FP64 factor up to the
+                // gate: the mixed path's fallback, and the plain path's
+                // answer when the LU solution itself misses the gate (very
+                // low frequencies), so that both paths deliver the same
+                // accuracy
                 double tol = r.tolerance > 0.0 ? r.tolerance : 1e-10;
                 status = peec_gb300_complex_refine_device(Z.p, W.p, perm.p, rs.p, cs.p, n, B.p, X.p, nrhs, tol, 5,
                                                           &be, &iters);
-            } else {
-                double out[3];
-                if (status == 0 && peec_gb300_backward_error_device(Z.p, n, X.p, B.p, nrhs, out) == 0) be = out[0];
             }
         }
         j.res.backward_error = be;

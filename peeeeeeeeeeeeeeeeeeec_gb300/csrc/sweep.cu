@@ -15,11 +15,15 @@
 // its full precision ladder, then, if that does not reach the gate, by the
 // FP64 LU with FP64 refinement.
 //
-// The autotuner picks, per plan, the split-BF16 terms (3 or 6), the number
-// of refinement sweeps and the tile width of the wide tensor-core updates
-// (64 or 128 columns): the adaptive solve at the probe frequencies tells
-// the terms and sweeps it needed; each tile width is recorded and timed
-// by replays at the middle probe frequency; the fastest is kept.
+// A plan holds two graphs: a fast one (split-BF16x3 products, up to 10
+// refinement sweeps) and a robust one (BF16x6, up to 16) for the
+// low-frequency end of the band, where the systems are worst conditioned;
+// in both, the sweeps after the one that reaches 1e-10 are no-ops (a device
+// flag), so the bound costs little.  The autotuner replays the fast graph
+// at the probe frequencies and finds the lowest frequency from which every
+// probe reaches the gate (the split frequency: below it the robust graph
+// runs), and times the wide tensor-core update tiles (64 or 128 columns) on
+// the fast graph at the top probe, keeping the faster.
 #include <math.h>
 #include <string.h>
 
@@ -44,7 +48,11 @@ struct SweepPlan {
     const double *L, *P, *R, *centers, *vectors;
     const int *edges;
     int ne, nv, n, nrhs;
-    PeecSweepTuning tuning;
+    PeecSweepTuning tuning;         // the fast graph's
+    PeecSweepTuning robust = {6, 16, 0};
+    double f_split = 0.0;           // frequencies below use the robust graph
+    cudaGraphExec_t exec_robust = nullptr;
+    unsigned long long robust_launches = 0;
     double *d_params = nullptr;     // omega, k0
     double *h_params = nullptr;     // pinned: one (omega, k0) pair per frequency of a run
     size_t h_params_cap = 0;
@@ -56,39 +64,40 @@ struct SweepPlan {
     unsigned long long graph_launches = 0;  // kernels per replay
 };
 
-static void drop_graph(SweepPlan &p) {
-    if (p.exec) cudaGraphExecDestroy(p.exec);
-    p.exec = nullptr;
+static void drop(cudaGraphExec_t &e) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
 }
 
-// Record the per-frequency sequence with the plan's tuning.
-static bool record(SweepPlan &p) {
-    drop_graph(p);
+// Record the per-frequency sequence with tuning t into exec.
+static bool record(SweepPlan &p, const PeecSweepTuning &t, cudaGraphExec_t &exec, unsigned long long &launches) {
+    drop(exec);
     if (!sync("sweep: before recording")) return false;
-    const int prev_bn = set_tc_wide_tile(p.tuning.tile_bn);
+    const int prev_bn = set_tc_wide_tile(t.tile_bn);
     cudaGraph_t g = nullptr;
     bool ok = cuda_ok(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal), "sweep: begin capture");
     if (ok) {
         const unsigned long long l0 = launch_count();
-        MixedCapture cap{p.tuning.split_terms, p.tuning.sweeps, p.d_eta, p.d_status};
+        MixedCapture cap{t.split_terms, t.sweeps, 1e-10, p.d_eta, p.d_status};
         bool body = launch_harmonic_fill_dev(p.L, p.P, p.edges, p.R, p.ne, p.nv, p.d_params, p.d_Z) &&
                     launch_plane_waves_dev(p.centers, p.vectors, p.ne, p.nv, p.nrhs, p.d_dirs, p.d_dirs + 3 * p.nrhs,
                                            p.d_params + 1, p.d_b) &&
                     mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, p.d_x, (size_t)p.nrhs, 0.0, 1, nullptr, nullptr,
                                      &cap) == 0;
-        p.graph_launches = launch_count() - l0;
+        launches = launch_count() - l0;
         const bool ended = cuda_ok(cudaStreamEndCapture(stream(), &g), "sweep: end capture");
-        ok = body && ended && g &&
-             cuda_ok(cudaGraphInstantiate(&p.exec, g, 0), "sweep: graph instantiation");
+        ok = body && ended && g && cuda_ok(cudaGraphInstantiate(&exec, g, 0), "sweep: graph instantiation");
     }
     if (g) cudaGraphDestroy(g);
     set_tc_wide_tile(prev_bn);
     if (!ok) {
         cudaGetLastError();
-        drop_graph(p);
+        drop(exec);
     }
     return ok;
 }
+
+static bool record(SweepPlan &p) { return record(p, p.tuning, p.exec, p.graph_launches); }
 
 static bool ensure_params(SweepPlan &p, size_t n_freq) {
     if (p.h_params_cap >= n_freq) return true;
@@ -113,12 +122,13 @@ static bool replay(SweepPlan &p, const double *freqs, size_t n_freq, Complex *d_
     }
     const size_t xs = (size_t)p.n * p.nrhs;
     for (size_t f = 0; f < n_freq; ++f) {
+        const bool robust = p.exec_robust && freqs[f] < p.f_split;
         if (!cuda_ok(cudaMemcpyAsync(p.d_params, p.h_params + 2 * f, 2 * sizeof(double), cudaMemcpyHostToDevice,
                                      stream()),
                      "sweep: parameters") ||
-            !cuda_ok(cudaGraphLaunch(p.exec, stream()), "sweep: graph launch"))
+            !cuda_ok(cudaGraphLaunch(robust ? p.exec_robust : p.exec, stream()), "sweep: graph launch"))
             return false;
-        note_launch((int)p.graph_launches);
+        note_launch((int)(robust ? p.robust_launches : p.graph_launches));
         if (!cuda_ok(cudaMemcpyAsync(d_X + f * xs, p.d_x, xs * sizeof(Complex), cudaMemcpyDeviceToDevice, stream()),
                      "sweep: solution copy") ||
             !cuda_ok(cudaMemcpyAsync(d_eta_all + f, p.d_eta, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
@@ -197,7 +207,7 @@ void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d
     p->nv = (int)n_nodes;
     p->n = p->ne + p->nv;
     p->nrhs = (int)nrhs;
-    p->tuning = tuning ? *tuning : PeecSweepTuning{3, 4, 0};
+    p->tuning = tuning ? *tuning : PeecSweepTuning{3, 10, 0};
     const size_t n = (size_t)p->n;
     bool ok = cuda_ok(cudaMalloc((void **)&p->d_params, 2 * sizeof(double)), "sweep plan") &&
               cuda_ok(cudaMalloc((void **)&p->d_dirs, 6 * nrhs * sizeof(double)), "sweep plan") &&
@@ -224,69 +234,92 @@ void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d
 
 int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_probe, PeecSweepTuning *chosen,
                           double *ms_per_system) {
-    if (!plan || !probe_frequencies || n_probe == 0) return -1;
+    if (!plan || !probe_frequencies || n_probe == 0 || n_probe > 64) return -1;
     SweepPlan &p = *static_cast<SweepPlan *>(plan);
+    std::vector<double> probes(probe_frequencies, probe_frequencies + n_probe);
+    std::sort(probes.begin(), probes.end());
     const size_t xs = (size_t)p.n * p.nrhs;
-    DBuf<Complex> x(xs);
-    if (!x.p) return -1;
-    // 1. what the adaptive solve needs at the probe frequencies
-    int terms = 3, sweeps = 1;
-    for (size_t f = 0; f < n_probe; ++f) {
-        double eta = 0.0;
-        int fb = 0;
-        const double w = 2.0 * M_PI * probe_frequencies[f], params[2] = {w, w / kC0};
-        if (!cuda_ok(cudaMemcpyAsync(p.d_params, params, sizeof(params), cudaMemcpyHostToDevice, stream()),
-                     "sweep: parameters") ||
-            !launch_harmonic_fill_dev(p.L, p.P, p.edges, p.R, p.ne, p.nv, p.d_params, p.d_Z) ||
-            !launch_plane_waves_dev(p.centers, p.vectors, p.ne, p.nv, p.nrhs, p.d_dirs, p.d_dirs + 3 * p.nrhs,
-                                    p.d_params + 1, p.d_b))
-            return -1;
-        int it = 0;
-        const int s = mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, x.p, (size_t)p.nrhs, 1e-10, 30, &eta, &it, nullptr);
-        (void)fb;
-        if (s < 0 && s != -2) return -1;
-        if (s == 0) {
-            terms = std::max(terms, peec_gb300_mixed_split_terms());
-            // the sweeps of the last rung: all of them when it started at BF16x6
-            sweeps = std::max(sweeps, peec_gb300_mixed_split_terms() == 6 && terms == 6 ? std::min(it, 8) : it);
+    DBuf<unsigned long long> eta_all(n_probe);
+    DBuf<int> st_all(n_probe);
+    DBuf<Complex> X(n_probe * xs);
+    if (!eta_all.p || !st_all.p || !X.p) return -1;
+    // the fast graph's backward errors at the probes; false on errors
+    auto try_probes = [&](std::vector<double> &eta) -> bool {
+        std::vector<unsigned long long> eb(n_probe);
+        std::vector<int> sb(n_probe);
+        if (!replay(p, probes.data(), n_probe, X.p, eta_all.p, st_all.p)) return false;
+        cudaMemcpyAsync(eb.data(), eta_all.p, n_probe * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        stream());
+        cudaMemcpyAsync(sb.data(), st_all.p, n_probe * sizeof(int), cudaMemcpyDeviceToHost, stream());
+        if (!sync("sweep: tuning probes")) return false;
+        eta.resize(n_probe);
+        for (size_t f = 0; f < n_probe; ++f) {
+            memcpy(&eta[f], &eb[f], sizeof(double));
+            if (sb[f] != 0) eta[f] = INFINITY;
         }
+        return true;
+    };
+    const double tol = 1e-10;
+    drop(p.exec_robust);
+    p.f_split = 0.0;
+    // 1. fast graph: BF16x3, up to 10 sweeps; the split frequency
+    p.tuning = PeecSweepTuning{3, 10, 128};
+    std::vector<double> eta;
+    if (!record(p) || !try_probes(eta)) return -1;
+    size_t first_ok = n_probe;  // every probe from here on passes
+    for (size_t f = n_probe; f-- > 0;) {
+        if (!(eta[f] <= tol)) break;
+        first_ok = f;
     }
-    sweeps = std::min(sweeps + 1, 10);  // one sweep of margin
-    // 2. record and time each tile width at the middle probe frequency
-    const double fmid = probe_frequencies[n_probe / 2];
-    DBuf<unsigned long long> eta_all(3);
-    DBuf<int> st_all(3);
-    DBuf<Complex> X3(3 * xs);
-    if (!eta_all.p || !st_all.p || !X3.p) return -1;
-    const double fr[3] = {fmid, fmid, fmid};
-    PeecSweepTuning best = {terms, sweeps, 128};
+    if (first_ok > 0) {  // the low end needs the robust graph
+        p.f_split = first_ok < n_probe ? probes[first_ok] : INFINITY;
+        if (!record(p, p.robust, p.exec_robust, p.robust_launches)) return -1;
+    }
+    // 2. tile width of the wide updates, timed on the fast graph at the top probe
+    const double ftop = probes.back(), fr[3] = {ftop, ftop, ftop};
     double best_ms = INFINITY;
+    int best_bn = 128;
     for (int bn : {128, 64}) {
-        p.tuning = PeecSweepTuning{terms, sweeps, bn};
+        p.tuning.tile_bn = bn;
         if (!record(p)) continue;
-        if (!replay(p, fr, 1, X3.p, eta_all.p, st_all.p) || !sync("sweep: tuning warm-up")) return -1;
+        const double f_split = p.f_split;
+        p.f_split = 0.0;  // time the fast graph
+        bool ok = replay(p, fr, 1, X.p, eta_all.p, st_all.p) && sync("sweep: tuning warm-up");
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream());
-        const bool ok = replay(p, fr, 3, X3.p, eta_all.p, st_all.p);
+        ok = ok && replay(p, fr, 3, X.p, eta_all.p, st_all.p);
         cudaEventRecord(e1, stream());
         float ms = 0.0f;
-        const bool synced = sync("sweep: tuning");
+        ok = sync("sweep: tuning") && ok;
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        if (!ok || !synced) return -1;
+        p.f_split = f_split;
+        if (!ok) return -1;
         if (ms / 3.0 < best_ms) {
             best_ms = ms / 3.0;
-            best = p.tuning;
+            best_bn = bn;
         }
     }
     if (!isfinite(best_ms)) return -1;
-    p.tuning = best;
+    p.tuning.tile_bn = best_bn;
     if (!record(p)) return -1;
-    if (chosen) *chosen = best;
+    if (p.exec_robust) {
+        p.robust.tile_bn = best_bn;
+        if (!record(p, p.robust, p.exec_robust, p.robust_launches)) return -1;
+    }
+    if (chosen) *chosen = p.tuning;
     if (ms_per_system) *ms_per_system = best_ms;
+    return 0;
+}
+
+int peec_gb300_sweep_split(void *plan, double *split_frequency, PeecSweepTuning *robust) {
+    if (!plan) return -1;
+    SweepPlan &p = *static_cast<SweepPlan *>(plan);
+    if (split_frequency) *split_frequency = p.exec_robust ? p.f_split : 0.0;
+    if (robust) *robust = p.robust;
     return 0;
 }
 
@@ -335,7 +368,8 @@ void peec_gb300_sweep_destroy(void *plan) {
     if (!plan) return;
     SweepPlan *p = static_cast<SweepPlan *>(plan);
     sync("sweep: destroy");
-    drop_graph(*p);
+    drop(p->exec);
+    drop(p->exec_robust);
     for (void *d : {(void *)p->d_params, (void *)p->d_dirs, (void *)p->d_Z, (void *)p->d_b, (void *)p->d_x,
                     (void *)p->d_eta, (void *)p->d_status})
         if (d) cudaFree(d);

@@ -5,11 +5,18 @@
 // and transient_solve_step (transient.c:2068-2097).
 //
 // The system matrix M = [L/dt + theta R, theta AS; -theta A^T, F/dt] is
-// filled and LU-factorised once on the device and stays resident; every step
-// then reads Lp and AS once (the right-hand side, an HBM-bound GEMV with the
-// node rows gathered through a node -> edge adjacency instead of the dense
-// incidence) and the factor once (one cooperative wavefront solve).  The
-// state x = [I; V] never leaves HBM between steps.
+// filled and LU-factorised once on the device (the reference's pivoting),
+// and its inverse is formed from the factor once (blocked substitution of
+// the permuted identity, about 2 n^3 FP64 flops); the factor is then freed
+// and the inverse stays resident.  Every step is HBM-bound matrix-vector
+// work, all runs of a batch at once: the right-hand side (Lp and AS read
+// once, the node rows gathered through a node -> edge adjacency instead of
+// the dense incidence), x0 = M^-1 b, the residual r = b - M x0 (Lp and AS
+// again) and x = x0 + M^-1 r -- one step of iterative refinement, which
+// keeps the step backward stable like the reference's LU solve
+// (transient_solve_step) while reading 2 (n^2 + Ne^2 + Ne Nv) doubles
+// instead of walking a chain of dependent triangular blocks.  The state
+// x = [I; V] never leaves HBM between steps.
 #include <math.h>
 #include <string.h>
 
@@ -17,23 +24,25 @@
 
 #include "../../include/peec_gb300.h"
 #include "common.cuh"
-#include "solve.cuh"
 
 namespace peec {
+
+bool inverse_from_lu_real(const double *lu, const int *perm, int n, double *Minv);
 
 struct TransientSystem {
     int ne = 0, nv = 0, nt = 0, scheme = 0;
     double theta = 0.0, dt = 0.0;
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
+    double *minv = nullptr;  // M^-1, nt x nt row-major
     long long *piv = nullptr;
     int *perm = nullptr, *edges = nullptr;
     int *adj_ptr = nullptr, *adj = nullptr;  // node j: edges +(e+1) entering (b = j), -(e+1) leaving (a = j)
     void release() {
-        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)piv, (void *)perm,
-                        (void *)edges, (void *)adj_ptr, (void *)adj})
+        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)piv,
+                        (void *)perm, (void *)edges, (void *)adj_ptr, (void *)adj})
             dfree(p);
-        R = F = AS = lu = dinv = nullptr;
+        R = F = AS = lu = dinv = minv = nullptr;
         piv = nullptr;
         perm = edges = adj_ptr = adj = nullptr;
     }
@@ -216,6 +225,58 @@ __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
     A.rhs[(size_t)r * nt + A.ne + j] = v;
 }
 
+// y[r][i] = y0[r][i] (when set) + sum_q Minv[i][q] v[r][q] for every run,
+// one warp per row of M^-1 (streamed once for all runs).
+template <int R>
+__global__ void __launch_bounds__(256) k_minv_apply(const double *Minv, int nt, const double *v, const double *y0,
+                                                    double *y, int nrun) {
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= nt) return;
+    double acc[R];
+    row_dot_runs<R>(Minv + (size_t)i * nt, v, nt, nt, lane, acc);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const double s = warp_sum(acc[r]);
+        if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s;
+    }
+}
+
+// res = b - M x for every run (M of k_transient_fill applied from its
+// blocks: Lp / dt, theta R, theta AS, -theta A^T through the adjacency,
+// F / dt), rows split as in k_transient_rhs.
+template <int R>
+__global__ void __launch_bounds__(256) k_transient_resid(StepArgs A, const double *b, double *res, int eb) {
+    const int nt = A.ne + A.nv;
+    if ((int)blockIdx.x < eb) {
+        const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+        if (i >= A.ne) return;
+        double s[R], sa[R];
+        row_dot_runs<R>(A.L + (size_t)i * A.ne, A.x, nt, A.ne, lane, s);
+        row_dot_runs<R>(A.AS + (size_t)i * A.nv, A.x + A.ne, nt, A.nv, lane, sa);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const double ls = warp_sum(s[r]), as = warp_sum(sa[r]);
+            if (lane == 0 && r < A.nrun) {
+                const double *x = A.x + (size_t)r * nt;
+                const double mx = ls / A.dt + A.theta * A.R[i] * x[i] + A.theta * as;
+                res[(size_t)r * nt + i] = b[(size_t)r * nt + i] - mx;
+            }
+        }
+        return;
+    }
+    const int t = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
+    if (t >= A.nv * A.nrun) return;
+    const int r = t / A.nv, j = t % A.nv;
+    const double *x = A.x + (size_t)r * nt;
+    double at = 0.0;  // (A^T I)_j
+    for (int k = A.adj_ptr[j]; k < A.adj_ptr[j + 1]; ++k) {
+        int e = A.adj[k];
+        at += e > 0 ? x[e - 1] : -x[-e - 1];
+    }
+    const double mx = -A.theta * at + A.F[j] * x[A.ne + j] / A.dt;
+    res[(size_t)r * nt + A.ne + j] = b[(size_t)r * nt + A.ne + j] - mx;
+}
+
 __global__ void k_transient_probe(StepArgs A) { record_probes(A, A.record_row); }
 
 static int create(const double *d_L, const double *d_P, const int *d_edges, const double *d_R, size_t ne_, size_t nv_,
@@ -290,9 +351,11 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     int col;
     int s = peec_gb300_lu_factor_device(S.lu, nt, 1.0e-14, S.piv, S.perm, &scale, &col);
     if (s != 0) return s == -2 ? -2 : -1;
-    // diagonal-block inverses for the per-step solves, once per factor
-    S.dinv = static_cast<double *>(dalloc(sizeof(double) * wave_dinv_words_real(nt)));
-    if (!S.dinv || !wave_prepare_real(S.lu, nt, S.dinv) || !sync("transient factor")) return -1;
+    // M^-1 from the factor, once; the factor is not needed afterwards
+    S.minv = static_cast<double *>(dalloc(sizeof(double) * (size_t)nt * nt));
+    if (!S.minv || !inverse_from_lu_real(S.lu, S.perm, nt, S.minv) || !sync("transient inverse")) return -1;
+    dfree(S.lu);
+    S.lu = nullptr;
     return 0;
 }
 
@@ -314,14 +377,14 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     // the right-hand-side kernel is instantiated for 1, 2, 4 or 8 runs and
     // reads that many states: pad with zero states
     const int cap = nrun <= 1 ? 1 : nrun <= 2 ? 2 : nrun <= 4 ? 4 : 8;
-    DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * nrun);
-    DBuf<unsigned> flags(wave_flag_words_real(nt, nrun));
-    DBuf<int> err(1);
-    if (!x.p || !rhs.p || !flags.p || !err.p) return -1;
+    DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
+    if (!x.p || !rhs.p || !x0.p || !res.p) return -1;
     cudaStream_t st = stream();
-    if (cap > nrun) cudaMemsetAsync(x.p + (size_t)nt * nrun, 0, sizeof(double) * nt * (cap - nrun), st);
+    if (cap > nrun) {
+        for (double *p : {x.p, rhs.p, x0.p, res.p})
+            cudaMemsetAsync(p + (size_t)nt * nrun, 0, sizeof(double) * nt * (cap - nrun), st);
+    }
     cudaMemcpyAsync(x.p, d_X, sizeof(double) * nt * nrun, cudaMemcpyDeviceToDevice, st);
-    cudaMemsetAsync(err.p, 0, sizeof(int), st);
     StepArgs A{};
     A.L = S.L;
     A.R = S.R;
@@ -343,11 +406,36 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     A.n_probe_edges = n_probe_edges;
     A.probes = (n_probe_nodes + n_probe_edges) > 0 ? probes : nullptr;
     const int eb = (ne + 7) / 8, grid = eb + (nv * nrun + 255) / 256;
+    const int mgrid = (nt + 7) / 8;
+    StepArgs Ares = A;  // the residual reads x0 as its state
+    Ares.x = x0.p;
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
         A.record_row = k - 1;
         launch_rhs(A, grid, eb);
-        if (!wave_solve_real(S.lu, S.dinv, S.perm, nt, rhs.p, x.p, nrun, flags.p, err.p)) return -1;
+        // x0 = M^-1 b; r = b - M x0; x = x0 + M^-1 r
+        switch (cap) {
+            case 1:
+                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_transient_resid<1>, grid, 256, 0, Ares, rhs.p, res.p, eb);
+                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                break;
+            case 2:
+                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_transient_resid<2>, grid, 256, 0, Ares, rhs.p, res.p, eb);
+                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                break;
+            case 4:
+                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_transient_resid<4>, grid, 256, 0, Ares, rhs.p, res.p, eb);
+                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                break;
+            default:
+                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_transient_resid<8>, grid, 256, 0, Ares, rhs.p, res.p, eb);
+                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                break;
+        }
         if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
     }
     if (A.probes && n_steps > 0) {
@@ -355,13 +443,7 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
         PEEC_LAUNCH(k_transient_probe, 1, 256, 0, A);
     }
     cudaMemcpyAsync(d_X, x.p, sizeof(double) * nt * nrun, cudaMemcpyDeviceToDevice, st);
-    int herr = 0;
-    cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (!launch_ok("transient steps") || !sync("transient steps")) return -1;
-    if (herr) {
-        set_error("transient: a triangular-solve wait timed out");
-        return -1;
-    }
     return 0;
 }
 

@@ -231,23 +231,24 @@ print(h.hexdigest())
 """
 
 
-def test_cluster_and_grid_panels_agree():
-    """The cooperative grid panel (default) and the thread-block-cluster
-    panel (PEEC_GB300_PANEL=cluster) make the same pivot choices and the same
-    arithmetic: the factors agree bit for bit."""
+def test_lean_and_grid_panels_agree():
+    """The lean FP64 panel (default: flag-published candidates, no grid
+    barrier) and the cooperative grid panel (PEEC_GB300_PANEL=coop) make the
+    same pivot choices and the same arithmetic: the factors agree bit for
+    bit."""
     import os
     import subprocess
     import sys
     here = os.path.dirname(os.path.abspath(__file__))
     code = _PANEL_PROBE.format(repo=os.path.dirname(here), tests=here)
     out = {}
-    for mode in ("cluster", "grid"):
+    for mode in ("coop", "lean"):
         env = dict(os.environ)
-        if mode == "cluster":
-            env["PEEC_GB300_PANEL"] = "cluster"
+        if mode == "coop":
+            env["PEEC_GB300_PANEL"] = "coop"
         else:
             env.pop("PEEC_GB300_PANEL", None)
         r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
         out[mode] = r.stdout.strip()
-    assert out["cluster"] == out["grid"]
+    assert out["coop"] == out["lean"]

@@ -69,6 +69,24 @@ def test_multiple_right_hand_sides(gpu_lib):
         assert backward_error(Z, X[q], B[q]) <= 1e-10
 
 
+@pytest.mark.parametrize("n,k", [(300, 40), (1000, 96)])
+def test_many_right_hand_sides(gpu_lib, n, k):
+    """32 or more right-hand sides take the blocked form (GEMM updates in the
+    triangular solves, the FP64 residual as a GEMM): every right-hand side
+    reaches the gate and agrees with LAPACK."""
+    rng = np.random.default_rng(n + k)
+    Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + n ** 0.5 * np.eye(n)
+    Z *= np.logspace(-3, 3, n)[:, None]
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    s, X, be, it = mixed_solve(gpu_lib, Z, B)
+    assert s == 0, (be, it)
+    assert be <= 1e-10
+    Xr = np.linalg.solve(Z, B.T).T
+    for q in range(k):
+        assert backward_error(Z, X[q], B[q]) <= 1e-10
+        assert rel_err(X[q], Xr[q]) < 1e-8
+
+
 def test_peec_box_system_matches_plain_fp64(gpu_lib):
     """Harmonic MNA matrix of a small PEC box at 30 MHz (assembled on the
     GPU): the mixed solve reaches the 1e-10 gate and agrees with the plain
@@ -329,11 +347,11 @@ np.save(sys.argv[1], np.concatenate(out))
 """
 
 
-@pytest.mark.parametrize("form", ["lean", "coop", "calu"])
+@pytest.mark.parametrize("form", ["lean", "coop"])
 def test_every_fp32_panel_form_reaches_the_gate(gpu_lib, form, tmp_path):
     """The mixed solve with each FP32 panel form (PEEC_GB300_MIXED_PANEL:
-    cluster by default, lean grid, cooperative grid, tournament) reaches the
-    1e-10 gate, and the solutions agree with the default form's."""
+    cluster by default, lean grid, cooperative grid) reaches the 1e-10
+    gate, and the solutions agree with the default form's."""
     import os
     import subprocess
     import sys
