@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <complex>
 #include <list>
 #include <mutex>
@@ -2270,6 +2271,25 @@ static CoopPlan<T> coop_plan(int m) {
     return pl;
 }
 
+// Host-side phase trace of the mixed solve on stderr (PEEC_GB300_TRACE set):
+// wall milliseconds since the previous mark, after synchronising the stream.
+static bool trace_enabled() {
+    static const bool on = getenv("PEEC_GB300_TRACE") != nullptr;
+    return on;
+}
+
+struct PhaseTrace {
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char *what) {
+        if (!trace_enabled()) return;
+        cudaStreamSynchronize(stream());
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "[peec trace] %-32s %10.3f ms\n", what,
+                std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
+
 // Split-BF16 terms the mixed path's first factorisation uses: 3 (BF16x3),
 // or 6 (BF16x6) with PEEC_GB300_MIXED_SPLIT=6.
 static int mixed_split_terms() {
@@ -3699,9 +3719,9 @@ __global__ void k_capture_status(const Status *st, const int *werr, const unsign
     *eta_out = *be;
 }
 
-bool mrhs_sweep(const void *Z, const float *absZ, const void *lu, const int *perm, const double *rs,
-                const double *cs, int n, int nrhs, const void *b, void *x, void *r, void *Y, float *absx,
-                unsigned long long *be);
+bool mrhs_split_z(const void *Z, size_t count, void *Zs);
+bool mrhs_sweep(const void *Zs, const void *lu, const int *perm, const double *rs, const double *cs, int n, int nrhs,
+                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be);
 // from this many right-hand sides on, the refinement sweeps use the blocked
 // many-right-hand-side form (multirhs.cu) instead of the wavefront solve
 // (NR right-hand sides per pass) and the per-row residual
@@ -3936,22 +3956,29 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     DBuf<cplxf> wdinv(wave_dinv_count(n));
     DBuf<float> absx(nv);
     if (!wflags.p || !werr.p || !wdinv.p || !absx.p) return -1;
+    // many right-hand sides: Z and x as float pairs for the double-float residual
+    const bool many = nrhs >= kManyRhs;
+    DBuf<float4> zsp(many ? nn : 0), xsp(many ? nv : 0);
+    if (many && (!zsp.p || !xsp.p)) return -1;
     double eta = INFINITY;
     int total_it = 0;
     auto refine = [&]() -> int {
+        PhaseTrace tr;
         cudaMemsetAsync(x, 0, nv * sizeof(cplx), stream());
         cudaMemcpyAsync(r.p, b, nv * sizeof(cplx), cudaMemcpyDeviceToDevice, stream());
         cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
         if (!wave_prepare(a, n, wdinv.p, true)) return -1;
+        if (many && !mrhs_split_z(Z, nn, zsp.p)) return -1;
+        if (!cap) tr.mark("refine: set-up");
         // one refinement sweep (FP32 correction solve, FP64 update, FP64
         // residual + backward error): captured once as a CUDA graph and
         // replayed per iteration
         auto sweep = [&]() {
-            if (nrhs >= kManyRhs) {
+            if (many) {
                 // many right-hand sides: blocked substitution with GEMM updates
                 // and the residual in GEMM form (multirhs.cu)
                 cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
-                mrhs_sweep(Z, absZ.p, a, perm.p, rs.p, cs.p, n, nrhs, b, x, r.p, y.p, absx.p, be.p);
+                mrhs_sweep(zsp.p, a, perm.p, rs.p, cs.p, n, nrhs, b, x, r.p, y.p, xsp.p, be.p);
                 return;
             }
             const int *skip = cap ? done.p : nullptr;
@@ -3997,6 +4024,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             }
         }
         cudaGetLastError();  // a failed capture falls back to direct launches
+        tr.mark(gexec ? "refine: sweep graph recorded" : "refine: capture failed");
         const int window = T == 6 ? 6 : 3;
         const double gain = T == 6 ? 0.5 : 0.25;
         double best = INFINITY, back[6];  // back[it % window]: the best after sweep it - window
@@ -4023,6 +4051,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
                 break;
             }
             memcpy(&eta, &hb, sizeof(eta));
+            tr.mark("refine: sweep");
             if (eta <= tol) {
                 out = 0;
                 break;

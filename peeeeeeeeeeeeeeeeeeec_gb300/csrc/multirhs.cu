@@ -55,9 +55,10 @@ __global__ void __launch_bounds__(256) k_permute_in(const c64 *r, const int *per
     }
 }
 
-// x[q][i] += Y[i][q] / cs[i] (FP64 accumulation), absx[q][i] = |x| in FP32.
+// x[q][i] += Y[i][q] / cs[i] (FP64 accumulation); xs[q][i] = x as float
+// pairs (re.h, re.l, im.h, im.l) for the residual.
 __global__ void __launch_bounds__(256) k_update_out(c64 *x, const c32 *Y, const double *cs, int n, int nrhs,
-                                                    float *absx) {
+                                                    float4 *xs) {
     __shared__ c32 t[32][33];
     const int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -75,8 +76,8 @@ __global__ void __launch_bounds__(256) k_update_out(c64 *x, const c32 *Y, const 
             v.re += (double)y.re / s;
             v.im += (double)y.im / s;
             x[(size_t)q * n + i] = v;
-            const float ar = fminf(fabsf((float)v.re), 1e19f), ai = fminf(fabsf((float)v.im), 1e19f);
-            absx[(size_t)q * n + i] = sqrtf(fmaf(ar, ar, ai * ai));
+            const float rh = (float)v.re, ih = (float)v.im;
+            xs[(size_t)q * n + i] = make_float4(rh, (float)(v.re - (double)rh), ih, (float)(v.im - (double)ih));
         }
     }
 }
@@ -294,106 +295,127 @@ __global__ void k_permuted_identity(const int *perm, int n, double *Y) {
 
 // ---- double-float residual: the same product on the FP32 pipes ----
 // A double-float value is an unevaluated sum hi + lo of two floats (~48
-// significant bits).  Products use the exact FMA product of the high parts
-// plus the cross terms; sums use the error-free two-sum of the high parts
-// (Dekker 1971, Knuth TAOCP 4.2.2).  On GB300 the FP32 pipe issues ~60x the
-// FP64 pipe's rate, so ~15 FP32 operations per real multiply-add still run
-// ~4x faster than one FP64 FMA.
+// significant bits).  The products below take the exact FMA product of the
+// high parts plus the two cross terms; the running sum of the high parts
+// uses the error-free two-sum (Dekker 1971, Knuth TAOCP 4.2.2), and every
+// low-order term (product errors, cross terms, two-sum errors) goes into a
+// second FP32 accumulator that is folded in once, at the end.  On GB300 the
+// FP32 pipe issues ~60x the FP64 pipe's rate, so the 12 FP32 operations of
+// one real multiply-add still run ~5x faster than one FP64 FMA.
+//
+// The complex product uses Gauss's three real products: with s_z = re + im
+// of Z and s_x = re + im of X (both double-float sums formed as the tiles
+// are staged), T1 = sum re*re, T2 = sum im*im, T3 = sum s_z*s_x, and
+// Re = T1 - T2, Im = T3 - T1 - T2 in FP64 at the end.  The error stays a
+// few units of 2^-48 of sum |Z_ij||X_j|, the residual's own scale.
 
-struct df {
+// Z as float pairs (re.h, re.l, im.h, im.l), once per solve: the residual
+// tiles then stage no FP64 instructions.
+__global__ void k_split_z(const c64 *Z, size_t count, float4 *Zs) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const c64 z = Z[t];
+    const float rh = (float)z.re, ih = (float)z.im;
+    Zs[t] = make_float4(rh, (float)(z.re - (double)rh), ih, (float)(z.im - (double)ih));
+}
+
+struct dacc {  // running sum: h (two-summed high parts) + l (low-order terms)
     float h, l;
 };
 
-__device__ __forceinline__ df df_split(double v) {
-    const float h = (float)v;
-    return df{h, (float)(v - (double)h)};
+// s += (ah + al)(bh + bl), dropping al bl
+__device__ __forceinline__ void dmac(dacc &s, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    const float t = s.h + p;
+    const float bp = t - s.h;
+    const float err = (s.h - (t - bp)) + (p - bp);
+    s.h = t;
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    s.l += e + err;
 }
 
-// s + a b
-__device__ __forceinline__ df df_mac(df s, df a, df b) {
-    const float ph = a.h * b.h;
-    float pl = fmaf(a.h, b.h, -ph);
-    pl = fmaf(a.h, b.l, pl);
-    pl = fmaf(a.l, b.h, pl);
-    const float t = s.h + ph;
-    const float bb = t - s.h;
-    float e = (s.h - (t - bb)) + (ph - bb);
-    e += s.l + pl;
-    const float hh = t + e;
-    return df{hh, e - (hh - t)};
+// (h, l) of a + b for two float pairs (two-sum of the high parts)
+__device__ __forceinline__ float2 pair_sum(float ah, float al, float bh, float bl) {
+    const float t = ah + bh;
+    const float bp = t - ah;
+    const float err = (ah - (t - bp)) + (bh - bp);
+    const float l = err + al + bl;
+    const float h = t + l;
+    return make_float2(h, l - (h - t));
 }
-
-struct df4 {
-    df re, im;
-};
 
 // R[q][i] = B[q][i] - sum_j Z[i][j] X[q][j] for all right-hand sides, with
 // the componentwise backward error |R_qi| / (sum_j |Z_ij||X_qj| + |B_qi|)
-// (the denominator from FP32 magnitudes absZ, absx) max-reduced into *be as
-// IEEE bits.  64 rows x 32 right-hand sides per CTA, 256 threads of 4 rows
-// x 2 right-hand sides, K in chunks of 16 in shared memory: Z is read once
-// per 32 right-hand sides.  The tiles of Z and X are split into float pairs
-// as they are staged (each split serves 32 right-hand sides or 64 rows),
-// the 8 complex accumulators of a thread are double-float, and the residual
-// is formed in FP64 from them at the end.
-__global__ void __launch_bounds__(256) k_residual_gemm_df(const c64 *Z, const float *absZ, const c64 *X,
-                                                          const float *absx, const c64 *B, int n, int nrhs, c64 *R,
-                                                          unsigned long long *be) {
-    __shared__ df4 Zs[16][64 + 1];
-    __shared__ float Za[16][64 + 1];
-    __shared__ df4 Xs[16][32 + 1];
-    __shared__ float Xa[16][32 + 1];
+// (the denominator in FP32 from the high parts) max-reduced into *be as
+// IEEE bits.  Zs, Xs: Z and X as float pairs (k_split_z, k_update_out).
+// 64 rows x 32 right-hand sides per CTA, 256 threads of 4 rows x 2
+// right-hand sides, K in chunks of 16 in shared memory: Z is read once per
+// 32 right-hand sides.  Each staged element holds its re and im pairs, its
+// re + im pair and its FP32 magnitude, so the inner loop is FP32 only.
+static const int kRK = 16;
+struct RTile {  // rows padded by one element: the transposing stores are conflict-free
+    float4 z[kRK][64 + 1];   // re.h, re.l, im.h, im.l
+    float4 zs[kRK][64 + 1];  // (re + im).h, (re + im).l, |z|, 0
+    float4 x[kRK][32 + 1];
+    float4 xs[kRK][32 + 1];
+};
+
+__global__ void __launch_bounds__(256) k_residual_gemm_df(const float4 *Zs, const float4 *Xs, const c64 *B, int n,
+                                                          int nrhs, c64 *R, unsigned long long *be) {
+    extern __shared__ __align__(16) unsigned char rsm[];
+    RTile &S = *reinterpret_cast<RTile *>(rsm);
     const int i0 = blockIdx.y * 64, q0 = blockIdx.x * 32;
     const int tr = threadIdx.x >> 4, tq = threadIdx.x & 15;
-    df4 acc[4][2];
+    dacc t1[4][2], t2[4][2], t3[4][2];
     float den[4][2];
 #pragma unroll
     for (int x = 0; x < 4; ++x)
 #pragma unroll
         for (int y = 0; y < 2; ++y) {
-            acc[x][y] = df4{{0.0f, 0.0f}, {0.0f, 0.0f}};
+            t1[x][y] = t2[x][y] = t3[x][y] = dacc{0.0f, 0.0f};
             den[x][y] = 0.0f;
         }
-    for (int j0 = 0; j0 < n; j0 += 16) {
-        for (int t = threadIdx.x; t < 64 * 16; t += 256) {
-            const int r = t >> 4, k = t & 15;
-            const bool ok = i0 + r < n && j0 + k < n;
-            const c64 z = ok ? Z[(size_t)(i0 + r) * n + j0 + k] : c64{0.0, 0.0};
-            Zs[k][r] = df4{df_split(z.re), df_split(z.im)};
-            Za[k][r] = ok ? absZ[(size_t)(i0 + r) * n + j0 + k] : 0.0f;
+    for (int j0 = 0; j0 < n; j0 += kRK) {
+        for (int t = threadIdx.x; t < 64 * kRK; t += 256) {
+            const int r = t / kRK, k = t % kRK;
+            float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (i0 + r < n && j0 + k < n) z = Zs[(size_t)(i0 + r) * n + j0 + k];
+            const float2 sz = pair_sum(z.x, z.y, z.z, z.w);
+            S.z[k][r] = z;
+            S.zs[k][r] = make_float4(sz.x, sz.y, sqrtf(fmaf(z.x, z.x, z.z * z.z)), 0.0f);
         }
-        for (int t = threadIdx.x; t < 32 * 16; t += 256) {
-            const int c = t >> 4, k = t & 15;
-            const bool ok = q0 + c < nrhs && j0 + k < n;
-            const c64 v = ok ? X[(size_t)(q0 + c) * n + j0 + k] : c64{0.0, 0.0};
-            Xs[k][c] = df4{df_split(v.re), df_split(v.im)};
-            Xa[k][c] = ok ? absx[(size_t)(q0 + c) * n + j0 + k] : 0.0f;
+        for (int t = threadIdx.x; t < 32 * kRK; t += 256) {
+            const int c = t / kRK, k = t % kRK;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (q0 + c < nrhs && j0 + k < n) v = Xs[(size_t)(q0 + c) * n + j0 + k];
+            const float2 sv = pair_sum(v.x, v.y, v.z, v.w);
+            S.x[k][c] = v;
+            S.xs[k][c] = make_float4(sv.x, sv.y, sqrtf(fmaf(v.x, v.x, v.z * v.z)), 0.0f);
         }
         __syncthreads();
-#pragma unroll 4
-        for (int k = 0; k < 16; ++k) {
-            df4 z[4], v[2];
-            float za[4], va[2];
+#pragma unroll 2
+        for (int k = 0; k < kRK; ++k) {
+            float4 z[4], zs[4], v[2], vs[2];
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
-                z[x] = Zs[k][tr + 16 * x];
-                za[x] = Za[k][tr + 16 * x];
+                z[x] = S.z[k][tr + 16 * x];
+                zs[x] = S.zs[k][tr + 16 * x];
             }
 #pragma unroll
             for (int y = 0; y < 2; ++y) {
-                v[y] = Xs[k][tq + 16 * y];
-                va[y] = Xa[k][tq + 16 * y];
+                v[y] = S.x[k][tq + 16 * y];
+                vs[y] = S.xs[k][tq + 16 * y];
             }
 #pragma unroll
             for (int x = 0; x < 4; ++x)
 #pragma unroll
                 for (int y = 0; y < 2; ++y) {
-                    const df nzi = {-z[x].im.h, -z[x].im.l};
-                    acc[x][y].re = df_mac(acc[x][y].re, z[x].re, v[y].re);
-                    acc[x][y].re = df_mac(acc[x][y].re, nzi, v[y].im);
-                    acc[x][y].im = df_mac(acc[x][y].im, z[x].re, v[y].im);
-                    acc[x][y].im = df_mac(acc[x][y].im, z[x].im, v[y].re);
-                    den[x][y] = fmaf(za[x], va[y], den[x][y]);
+                    dmac(t1[x][y], z[x].x, z[x].y, v[y].x, v[y].y);
+                    dmac(t2[x][y], z[x].z, z[x].w, v[y].z, v[y].w);
+                    dmac(t3[x][y], zs[x].x, zs[x].y, vs[y].x, vs[y].y);
+                    den[x][y] = fmaf(zs[x].z, vs[y].z, den[x][y]);
                 }
         }
         __syncthreads();
@@ -408,9 +430,10 @@ __global__ void __launch_bounds__(256) k_residual_gemm_df(const c64 *Z, const fl
             const int q = q0 + tq + 16 * y;
             if (q >= nrhs) continue;
             const c64 b = B[(size_t)q * n + i];
-            const double yre = (double)acc[x][y].re.h + (double)acc[x][y].re.l;
-            const double yim = (double)acc[x][y].im.h + (double)acc[x][y].im.l;
-            const c64 r = c64{b.re - yre, b.im - yim};
+            const double a1 = (double)t1[x][y].h + (double)t1[x][y].l;
+            const double a2 = (double)t2[x][y].h + (double)t2[x][y].l;
+            const double a3 = (double)t3[x][y].h + (double)t3[x][y].l;
+            const c64 r = c64{b.re - (a1 - a2), b.im - (a3 - a1 - a2)};
             R[(size_t)q * n + i] = r;
             const double res = sqrt(fma(r.re, r.re, r.im * r.im));
             const double babs = hypot(b.re, b.im);
@@ -451,15 +474,26 @@ bool inverse_from_lu_real(const double *lu, const int *perm, int n, double *Minv
     return launch_ok("inverse from the LU factor");
 }
 
+// Z (count complex FP64 entries) as float pairs into Zs (16 bytes an entry),
+// once per solve, for the residual of mrhs_sweep.
+bool mrhs_split_z(const void *Z, size_t count, void *Zs) {
+    using namespace mrhs;
+    PEEC_LAUNCH(k_split_z, (unsigned)((count + 255) / 256), 256, 0, (const c64 *)Z, count, (float4 *)Zs);
+    return launch_ok("many-right-hand-side split of Z");
+}
+
 // One correction of the many-right-hand-side refinement, all on the
 // calling thread's stream: Y = P D_r^-1 r (FP32, [n][nrhs]); forward and
 // backward block substitution on the FP32 factor lu (diagonal blocks per
-// right-hand side, the rest as GEMMs); x += D_c^-1 Y; r = b - Z x (FP64) and
+// right-hand side, the rest as GEMMs); x += D_c^-1 Y (FP64) and its float
+// pairs xs; r = b - Z x in double-float from the split Zs (mrhs_split_z) and
 // the backward error into *be (IEEE bits; the caller zeroes it).
-bool mrhs_sweep(const void *Z, const float *absZ, const void *lu, const int *perm, const double *rs,
-                const double *cs, int n, int nrhs, const void *b, void *x, void *r, void *Y, float *absx,
-                unsigned long long *be) {
+bool mrhs_sweep(const void *Zs, const void *lu, const int *perm, const double *rs, const double *cs, int n, int nrhs,
+                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be) {
     using namespace mrhs;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_residual_gemm_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RTile));
+    if (!cuda_ok(attr, "residual GEMM shared memory attribute")) return false;
     const c32 *F = (const c32 *)lu;
     c32 *Yt = (c32 *)Y;
     const dim3 tgrid((n + 31) / 32, (nrhs + 31) / 32);
@@ -480,9 +514,9 @@ bool mrhs_sweep(const void *Z, const float *absZ, const void *lu, const int *per
             PEEC_LAUNCH(k_cgemm_sub, dim3((nrhs + 63) / 64, (r0 + 63) / 64), 256, 0, F + r0, n,
                         Yt + (size_t)r0 * nrhs, Yt, nrhs, r0, nrhs, nrow);
     }
-    PEEC_LAUNCH(k_update_out, tgrid, 256, 0, (c64 *)x, Yt, cs, n, nrhs, absx);
-    PEEC_LAUNCH(k_residual_gemm_df, dim3((nrhs + 31) / 32, (n + 63) / 64), 256, 0, (const c64 *)Z, absZ,
-                (const c64 *)x, absx, (const c64 *)b, n, nrhs, (c64 *)r, be);
+    PEEC_LAUNCH(k_update_out, tgrid, 256, 0, (c64 *)x, Yt, cs, n, nrhs, (float4 *)xs);
+    PEEC_LAUNCH(k_residual_gemm_df, dim3((nrhs + 31) / 32, (n + 63) / 64), 256, sizeof(RTile), (const float4 *)Zs,
+                (const float4 *)xs, (const c64 *)b, n, nrhs, (c64 *)r, be);
     return launch_ok("many-right-hand-side sweep");
 }
 

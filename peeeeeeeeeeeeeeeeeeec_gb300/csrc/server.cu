@@ -110,8 +110,10 @@ class Server {
         j->mesh_bytes = mesh_bytes(ne, nv);
         // Z + working copy (mixed: FP32 LU + FP32 |Z| + BF16 splits, or the
         // FP64 LU of a fallback, whichever is larger; plain: FP64 LU) +
-        // vectors + scratch
-        j->bytes = 32 * n * n + (r->mixed ? 9216 * n : 0) + 96 * n * r->nrhs + (64 << 20);
+        // vectors + scratch; a mixed solve of 32 or more right-hand sides
+        // also keeps Z as float pairs for its residual
+        j->bytes = 32 * n * n + (r->mixed ? 9216 * n : 0) + (r->mixed && r->nrhs >= 32 ? 16 * n * n : 0) +
+                   112 * n * r->nrhs + (64 << 20);
         return enqueue(j);
     }
 
