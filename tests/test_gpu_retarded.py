@@ -2,9 +2,11 @@
 against the oracle's FP64 restatement of the same formula.
 
 The static part is the quasi-static pipeline itself (parity 1e-12); the
-correction D_k = integral of (exp(-jkR) - 1)/R runs on the FP32 pipes.  The
-tolerance stated here: |GPU - oracle| <= 1e-12 |entry| + 1e-5 max|D_k| per
-entry.  k = 0 must give the static matrices bit for bit."""
+correction D_k = integral of (exp(-jkR) - 1)/R runs on the FP32 pipes, with
+the product rule's order lowered to 3 or 2 for patch pairs far apart
+relative to their size and the wavelength; the oracle applies the far order
+to every pair.  The tolerance stated here: |GPU - oracle| <= 1e-12 |entry| +
+1e-5 max|D_k| per entry.  k = 0 must give the static matrices bit for bit."""
 import ctypes as C
 
 import numpy as np
@@ -37,9 +39,12 @@ def retarded(lib, m, kind, k):
         lib.peec_gb300_device_free(d)
 
 
+# box_fine: 5 cm cells, so that patch pairs of all three correction orders
+# (2, 3 and the far order) occur at 30 and 100 MHz
 MESHES = {"plate4": lambda: SynthMesh.plate(1.0, 1.0, 4, 4),
           "box421": lambda: SynthMesh.box(0.4, 0.2, 0.1, 4, 2, 1),
-          "box_2m": lambda: SynthMesh.box(2.0, 1.0, 0.5, 8, 4, 2)}
+          "box_2m": lambda: SynthMesh.box(2.0, 1.0, 0.5, 8, 4, 2),
+          "box_fine": lambda: SynthMesh.box(0.5, 0.25, 0.125, 10, 5, 3)}
 
 
 @pytest.mark.parametrize("name", list(MESHES))
