@@ -691,9 +691,10 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
     and time the whole arm on the wall clock: Lp / P assembly included.
       mixed  a sweep plan per mesh (peec_gb300_sweep_*): the autotuner at
              eight probe frequencies across the band picks the frequency
-             below which the robust graph (BF16x6) runs, the fast graph's
-             sweeps and the tile width; the mixed solve recorded into CUDA
-             graphs is replayed for every frequency;
+             below which the robust graph (BF16x6) runs and the tile width
+             of the wide tensor-core updates; the mixed solve recorded into
+             CUDA graphs (refinement sweeps past the gate are no-ops) is
+             replayed for every frequency;
              systems above the gate are solved again by the precision
              ladder, then the FP64 LU with FP64 refinement
       plain  per system: MNA fill, FP64 complex LU, solve, FP64 iterative
@@ -1202,6 +1203,36 @@ def main():
                       "ms": ml["tc_update_ms"], "traffic": None,
                       "peak_source": "measured (MEASURED_PEAKS.json, cuBLAS BF16 burst)",
                       "note": "issued BF16 flops: 2 accumulators x 2 x m x n x 6 x (block width)"})
+    if mixed and mixed.get("phase_ms"):
+        # the mixed path's FP32 far rule against its issue bound: one MUFU
+        # reciprocal square root per point pair, 16 per clock per SM against
+        # 128 FP32 FMA lanes
+        for tag in ("Lp", "P"):
+            ms = mixed["phase_ms"].get(tag + "_far")
+            pairs = ds.work.get(tag + "_far_point_pairs")
+            if ms and pairs and p32.value:
+                a = pairs / (ms * 1e-3) / 1e9
+                pk = p32.value * 1e12 / 2 / 8 / 1e9
+                roofs.append({"kernel": "k_assemble_tiles far rule, %s (FP32, mixed path)" % tag, "bound": "mufu",
+                              "achieved": a, "peak": pk, "unit": "Gpoint-pairs/s", "frac": a / pk, "ms": ms,
+                              "traffic": None,
+                              "peak_source": "measured FP32 FMA rate / 8 (MUFU rsqrt rate, one per point pair)"})
+    if transient and transient.get("ms_per_step"):
+        ne_, nv_ = m.n_edges, m.n_nodes
+        nt_ = ne_ + nv_
+        b = 16.0 * nt_ * nt_ + 16.0 * (ne_ * ne_ + ne_ * nv_)  # two M^-1 applies; Lp and A S read twice
+        a = b / (transient["ms_per_step"] * 1e-3) / 1e9
+        hbm_pk = 6800.0
+        try:
+            with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+                hbm_pk = json.load(f).get("hbm_gbs", hbm_pk)
+        except Exception:
+            pass
+        roofs.append({"kernel": "transient step (k_transient_rhs, 2 x k_minv_apply, k_transient_resid)",
+                      "bound": "hbm", "achieved": a, "peak": hbm_pk, "unit": "GB/s", "frac": a / hbm_pk,
+                      "ms": transient["ms_per_step"], "traffic": load_traffic().get("k_minv_apply"),
+                      "peak_source": "measured (MEASURED_PEAKS.json)",
+                      "note": "algorithmic bytes per step: 16 N^2 (M^-1 twice) + 16 (Ne^2 + Ne Nv) (Lp, A S twice)"})
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -1297,11 +1297,22 @@ __device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
     e = fmaf(a.l, b.h, e);
     return quick_two_sum(p, e);
 }
+// The hardware reciprocal square root as one instruction: rsqrtf() wraps it
+// in a rescaling for subnormal inputs, which the far rule never sees (a FAR
+// point pair is at least near_factor patch sizes apart) and which would
+// otherwise add ~5 instructions to a loop body of 9.  Subnormal inputs
+// flush to zero (result +inf, which the entry's finiteness check reports).
+__device__ __forceinline__ float rsqrt_hw(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // 1/sqrt(x) for x > 0 to ~1e-14 relative: hardware rsqrtf seed y, residual
 // r = 1 - x y^2 in double-float, one Halley step y (1 + r/2 + 3 r^2 / 8)
 // (third-order convergence from the 2^-22 seed).
 __device__ __forceinline__ f2 df_rsqrt(f2 x) {
-    float y = rsqrtf(x.h);
+    float y = rsqrt_hw(x.h);
     float yy = y * y;
     f2 y2 = f2{yy, fmaf(y, y, -yy)};
     f2 t = df_mul(x, y2);
@@ -1328,16 +1339,16 @@ __device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF 
             const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
             const float4 B1 = *reinterpret_cast<const float4 *>(pb + q + 1);
             float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
-            s0 = fmaf(B0.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
+            s0 = fmaf(B0.w, rsqrt_hw(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
             dx = A.x - B1.x;
             dy = A.y - B1.y;
             dz = A.z - B1.z;
-            s1 = fmaf(B1.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s1);
+            s1 = fmaf(B1.w, rsqrt_hw(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s1);
         }
         if (q < npts) {
             const float4 B0 = *reinterpret_cast<const float4 *>(pb + q);
             const float dx = A.x - B0.x, dy = A.y - B0.y, dz = A.z - B0.z;
-            s0 = fmaf(B0.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
+            s0 = fmaf(B0.w, rsqrt_hw(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s0);
         }
         acc = df_add(acc, two_sum(A.w * s0, A.w * s1));
     }
@@ -1359,7 +1370,7 @@ __device__ __forceinline__ void far_pair_f32_acc32(const FarPtF *pa, const FarPt
     for (int q = 0; q < 32; ++q) {
         const float4 B = slot[q];
         const float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        s[q & 3] = fmaf(B.w, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s[q & 3]);
+        s[q & 3] = fmaf(B.w, rsqrt_hw(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s[q & 3]);
     }
     acc = df_add(acc, two_sum(A.w * (s[0] + s[1]), A.w * (s[2] + s[3])));
 }
@@ -2075,7 +2086,7 @@ __device__ __forceinline__ void retard_point_pair(const float4 A, const float4 B
     const float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     if (r2 > 0.0f) {
-        float inv = rsqrtf(r2), sn, cs;
+        float inv = rsqrt_hw(r2), sn, cs;
         sincosf(0.5f * k * (r2 * inv), &sn, &cs);
         const float wi = w * inv;
         sr = fmaf(wi, -2.0f * sn * sn, sr);
