@@ -1204,19 +1204,23 @@ def main():
                       "peak_source": "measured (MEASURED_PEAKS.json, cuBLAS BF16 burst)",
                       "note": "issued BF16 flops: 2 accumulators x 2 x m x n x 6 x (block width)"})
     if mixed and mixed.get("phase_ms"):
-        # the mixed path's FP32 far rule against its issue bound: one MUFU
-        # reciprocal square root per point pair, 16 per clock per SM against
-        # 128 FP32 FMA lanes
+        # the mixed path's FP32 far rule against the issue bound of its point
+        # loop: 7.25 warp instructions per 32 point pairs (a shared-memory
+        # broadcast, an add, three FMAs, the reciprocal square root, the
+        # weighted FMA, a quarter of the weights' load) at one warp
+        # instruction per clock per SM sub-partition (the FP32 FMA probe's
+        # rate / 32 lanes); ncu shows the MUFU pipe at a quarter of its peak
         for tag in ("Lp", "P"):
             ms = mixed["phase_ms"].get(tag + "_far")
             pairs = ds.work.get(tag + "_far_point_pairs")
             if ms and pairs and p32.value:
                 a = pairs / (ms * 1e-3) / 1e9
-                pk = p32.value * 1e12 / 2 / 8 / 1e9
-                roofs.append({"kernel": "k_assemble_tiles far rule, %s (FP32, mixed path)" % tag, "bound": "mufu",
+                pk = p32.value * 1e12 / 2 / 32 * (32 / 7.25) / 1e9
+                roofs.append({"kernel": "k_assemble_tiles far rule, %s (FP32, mixed path)" % tag, "bound": "issue",
                               "achieved": a, "peak": pk, "unit": "Gpoint-pairs/s", "frac": a / pk, "ms": ms,
                               "traffic": None,
-                              "peak_source": "measured FP32 FMA rate / 8 (MUFU rsqrt rate, one per point pair)"})
+                              "peak_source": "measured FP32 FMA rate / 2 / 32 lanes x 32 / 7.25 point pairs per "
+                                             "warp instruction (the point loop's instruction count)"})
     if transient and transient.get("ms_per_step"):
         ne_, nv_ = m.n_edges, m.n_nodes
         nt_ = ne_ + nv_

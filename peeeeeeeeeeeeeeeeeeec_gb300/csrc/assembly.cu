@@ -1354,25 +1354,95 @@ __device__ __forceinline__ void far_pair_f32_acc(const FarPtF *pa, const FarPtF 
     }
 }
 
-// The FP32 form at the far order 4 (32 points a patch, one per lane): the
-// partner's points are staged in the warp's shared slot by one coalesced
-// load and read back as broadcasts, and four partial sums per lane keep
-// the dependent FMA chains short.
+// The FP32 form at the far order 4 (32 points a patch, one per lane), in
+// coordinates local to the pair: with O = the first point of patch A (its
+// float pair), a = A - O and b = B - O are formed from the float pairs (so
+// they carry FP32 accuracy relative to the patch size and the distance, not
+// to the absolute position), and R^2 = |a|^2 + |b|^2 - 2 a.b takes one add
+// and three FMAs per point pair.  Its rounding stays a few units of 2^-24 of
+// (|a| + |b|)^2 <= (R + 2h)^2, i.e. below 1.5e-6 of R^2 at the closest FAR
+// pairs (R >= near_factor h with the default 0.5) -- the absolute-coordinate
+// form it replaces rounded each difference to 2^-24 of the coordinate.
+// Lane q prepares (b, |b|^2) and the weight of partner point q in the warp's
+// shared slot; every lane then reads them as broadcasts.
 __device__ __forceinline__ void far_pair_f32_acc32(const FarPtF *pa, const FarPtF *pb, float4 *slot, f2 &acc) {
     const int lane = threadIdx.x & 31;
-    const float4 A = *reinterpret_cast<const float4 *>(pa + lane);  // xh, yh, zh, wh
-    const float4 Bl = *reinterpret_cast<const float4 *>(pb + lane);
+    const FarPtF A = pa[lane];
+    const FarPtF B = pb[lane];
+    const float oxh = __shfl_sync(0xffffffffu, A.xh, 0), oxl = __shfl_sync(0xffffffffu, A.xl, 0);
+    const float oyh = __shfl_sync(0xffffffffu, A.yh, 0), oyl = __shfl_sync(0xffffffffu, A.yl, 0);
+    const float ozh = __shfl_sync(0xffffffffu, A.zh, 0), ozl = __shfl_sync(0xffffffffu, A.zl, 0);
+    const float bx = (B.xh - oxh) + (B.xl - oxl), by = (B.yh - oyh) + (B.yl - oyl), bz = (B.zh - ozh) + (B.zl - ozl);
+    const float ax = (A.xh - oxh) + (A.xl - oxl), ay = (A.yh - oyh) + (A.yl - oyl), az = (A.zh - ozh) + (A.zl - ozl);
+    const float a2 = fmaf(az, az, fmaf(ay, ay, ax * ax));
+    const float mx = -2.0f * ax, my = -2.0f * ay, mz = -2.0f * az;
     __syncwarp();  // the slot's previous partner is read by every lane
-    slot[lane] = Bl;
+    slot[lane] = make_float4(bx, by, bz, fmaf(bz, bz, fmaf(by, by, bx * bx)));
+    reinterpret_cast<float *>(slot + 32)[lane] = B.wh;
     __syncwarp();
     float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int q = 0; q < 32; ++q) {
-        const float4 B = slot[q];
-        const float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        s[q & 3] = fmaf(B.w, rsqrt_hw(fmaf(dz, dz, fmaf(dy, dy, dx * dx))), s[q & 3]);
+    for (int q4 = 0; q4 < 8; ++q4) {
+        const float4 w = slot[32 + q4];
+        const float ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float4 b = slot[4 * q4 + u];
+            const float r2 = fmaf(mz, b.z, fmaf(my, b.y, fmaf(mx, b.x, a2 + b.w)));
+            s[u] = fmaf(ws[u], rsqrt_hw(r2), s[u]);
+        }
     }
-    acc = df_add(acc, two_sum(A.w * (s[0] + s[1]), A.w * (s[2] + s[3])));
+    acc = df_add(acc, two_sum(A.wh * (s[0] + s[1]), A.wh * (s[2] + s[3])));
+}
+
+// The FP32 far rule of a whole entry at the far order 4 (regions of at most
+// four patches a side), after its near pairs: farmask bit 4 ii + jj marks the
+// far patch pair (off[a] + ii, off[b] + jj).  One origin O for the entry (the
+// first point of the entry's first A patch) lets every partner patch be
+// staged once per entry and every A point be prepared once per A patch; the
+// point loop is far_pair_f32_acc32's.  With |a| below the region size s and
+// R >= near_factor s_patch, the rounding of R^2 stays below ~3e-6 of R^2 at
+// the closest FAR pairs (typically 1e-7).  slot: 4 x 40 float4 of the warp.
+__device__ __forceinline__ void far_entry_f32(const FarPtF *ptf, int i0, int ni, int j0, int nj, unsigned farmask,
+                                              float4 *slot, f2 &acc) {
+    const int lane = threadIdx.x & 31;
+    const FarPtF O = ptf[(size_t)i0 * 32];  // the same address in every lane: one broadcast load
+    __syncwarp();  // the previous entry's partner points are read by every lane
+    for (int jj = 0; jj < nj; ++jj) {
+        if (!((farmask >> jj) & 0x1111u)) continue;  // no far pair with this partner patch
+        const FarPtF B = ptf[(size_t)(j0 + jj) * 32 + lane];
+        const float bx = (B.xh - O.xh) + (B.xl - O.xl), by = (B.yh - O.yh) + (B.yl - O.yl),
+                    bz = (B.zh - O.zh) + (B.zl - O.zl);
+        slot[40 * jj + lane] = make_float4(bx, by, bz, fmaf(bz, bz, fmaf(by, by, bx * bx)));
+        reinterpret_cast<float *>(slot + 40 * jj + 32)[lane] = B.wh;
+    }
+    __syncwarp();
+    for (int ii = 0; ii < ni; ++ii) {
+        const unsigned row = (farmask >> (4 * ii)) & 0xFu;
+        if (!row) continue;
+        const FarPtF A = ptf[(size_t)(i0 + ii) * 32 + lane];
+        const float ax = (A.xh - O.xh) + (A.xl - O.xl), ay = (A.yh - O.yh) + (A.yl - O.yl),
+                    az = (A.zh - O.zh) + (A.zl - O.zl);
+        const float a2 = fmaf(az, az, fmaf(ay, ay, ax * ax));
+        const float mx = -2.0f * ax, my = -2.0f * ay, mz = -2.0f * az;
+        for (int jj = 0; jj < nj; ++jj) {
+            if (!((row >> jj) & 1u)) continue;
+            const float4 *bs = slot + 40 * jj;
+            float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int q4 = 0; q4 < 8; ++q4) {
+                const float4 w = bs[32 + q4];
+                const float ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4 b = bs[4 * q4 + u];
+                    const float r2 = fmaf(mz, b.z, fmaf(my, b.y, fmaf(mx, b.x, a2 + b.w)));
+                    s4[u] = fmaf(ws[u], rsqrt_hw(r2), s4[u]);
+                }
+            }
+            acc = df_add(acc, two_sum(A.wh * (s4[0] + s4[1]), A.wh * (s4[2] + s4[3])));
+        }
+    }
 }
 
 // The double-float form at the far order 4, with the partner's points
@@ -1510,7 +1580,7 @@ __device__ __forceinline__ bool near_lookup(const TileArgs &T, int i, int j, dou
 
 __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) {
     __shared__ double tile[kTile][kTile + 1];
-    __shared__ float4 stage[kTileWarps][64];  // one partner patch's far points per warp
+    __shared__ float4 stage[kTileWarps][160];  // partner patches' far points, per warp
     const int ta = blockIdx.y, tb = blockIdx.x;
     if (tb < ta) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1546,6 +1616,11 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                 // are reduced across the warp once per entry; near pairs (and
                 // the other modes) add in the reference's (i, j) order
                 f2 facc = {0.0f, 0.0f};
+                // FP32 far rule at order 4 with regions of at most 4 patches:
+                // far pairs are collected in farmask and run per entry below
+                const int ni = R.off[a + 1] - R.off[a], nj = R.off[b + 1] - R.off[b];
+                const bool per_entry = T.far_df == 2 && T.npts == 32 && ni <= 4 && nj <= 4;
+                unsigned farmask = 0;
                 for (int i = R.off[a]; i < R.off[a + 1] && !bad; ++i) {
                     // i's near partners are sorted by j (the scan's list):
                     // a cursor from the first partner in region b
@@ -1582,7 +1657,9 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                             }
                             if (T.far_df == 2) {
                                 if (R.boxf[2 * i].w != 0.0f && R.boxf[2 * j].w != 0.0f) {  // zero-size patches add 0
-                                    if (T.npts == 32)
+                                    if (per_entry)
+                                        farmask |= 1u << (4 * (i - R.off[a]) + (j - R.off[b]));
+                                    else if (T.npts == 32)
                                         far_pair_f32_acc32(T.ptf + (size_t)i * 32, T.ptf + (size_t)j * 32,
                                                            stage[warp], facc);
                                     else
@@ -1600,6 +1677,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_assemble_tiles(TileArgs T) 
                         integral += k;
                     }
                 }
+                if (farmask && !bad) far_entry_f32(T.ptf, R.off[a], ni, R.off[b], nj, farmask, stage[warp], facc);
                 if (T.far_df == 1 || T.far_df == 2) {
                     const f2 far2 = warp_sum_df2(facc);
                     if (lane == 0) {  // the entry's FP64 epilogue on one lane

@@ -938,8 +938,8 @@ __global__ void __launch_bounds__(kLeanThreads) k_panel_lean64(T *a, int n, int 
 // The lean panel's per-column exchange still crosses the GPU: measured on
 // GB300, a release store takes ~2 us to reach pollers on other SMs, while a
 // thread-block cluster barrier takes 0.2 us and a distributed-shared-memory
-// load 0.1 us.  Here the whole panel lives in one cluster of C (16) CTAs,
-// one row per thread (up to 1024 rows per CTA), candidates in each CTA's
+// load 0.1 us.  Here the whole panel lives in one cluster of C (1-16) CTAs,
+// one row per thread (up to 640 rows per CTA), candidates in each CTA's
 // shared memory: per column a CTA argmax, one split cluster barrier (the
 // previous column's deferred update runs between arrive and wait), the
 // winner read from its CTA's shared memory, the swap, and the multiplier
@@ -1151,11 +1151,12 @@ __global__ void __launch_bounds__(kClMaxThreads) k_panel_cl(cplxf *a, int n, int
 }
 
 
-// Cluster FP32 panel for m rows: C = 16 CTAs (8 where 16 is not
-// available), one row per thread; false when it does not apply.
+// Cluster FP32 panel for m rows: one CTA up to 640 rows, else C = 16 CTAs
+// (8 where 16 is not available), one row per thread; false when it does
+// not apply.
 static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long long *piv, Status *st) {
     const int m = n - k0;
-    if (m < 2 * 64) return false;
+    if (m < 1) return false;
     static const size_t kMaxSmem = 200 * 1024;
     static const int max_c = [] {
         cudaFuncSetAttribute(k_panel_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
@@ -1177,7 +1178,13 @@ static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long 
         return c >= 16 ? 16 : c >= 8 ? 8 : 0;
     }();
     if (max_c == 0) return false;
-    const int C = max_c;
+    // a panel of up to kClMaxThreads rows fits one CTA: a cluster of one,
+    // whose barriers are the CTA's own (measured: the tail panels of a small
+    // system take ~30 us instead of ~240 us with the single-CTA global-
+    // memory panel, and the SMs left free serve the other streams of a
+    // batched sweep).  Larger panels take the widest cluster: intermediate
+    // sizes (2-8 CTAs) made the 8402-unknown factorisation 2 ms slower.
+    const int C = m <= kClMaxThreads ? 1 : max_c;
     const int rows = (m + C - 1) / C;
     if (rows > kClMaxThreads) return false;
     const size_t smem = (size_t)rows * kClStride * sizeof(cplxf);
