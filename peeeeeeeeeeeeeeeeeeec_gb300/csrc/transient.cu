@@ -34,7 +34,7 @@ struct TransientSystem {
     double theta = 0.0, dt = 0.0;
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
-    double *minv = nullptr;  // M^-1, nt x nt row-major
+    float2 *minv = nullptr;  // M^-1 as float pairs (hi, lo), nt x nt row-major
     long long *piv = nullptr;
     int *perm = nullptr, *edges = nullptr;
     int *adj_ptr = nullptr, *adj = nullptr;  // node j: edges +(e+1) entering (b = j), -(e+1) leaving (a = j)
@@ -42,7 +42,8 @@ struct TransientSystem {
         for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)piv,
                         (void *)perm, (void *)edges, (void *)adj_ptr, (void *)adj})
             dfree(p);
-        R = F = AS = lu = dinv = minv = nullptr;
+        R = F = AS = lu = dinv = nullptr;
+        minv = nullptr;
         piv = nullptr;
         perm = edges = adj_ptr = adj = nullptr;
     }
@@ -225,18 +226,96 @@ __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
     A.rhs[(size_t)r * nt + A.ne + j] = v;
 }
 
+// M^-1 is applied in double-float arithmetic on the FP32 pipes: one FP64
+// FMA per matrix element would hold the GEMV to GB300's FP64 rate (two per
+// clock per SM, ~110 us for the 5 cm box's 70.6 M elements) where the HBM
+// read of the matrix takes ~85 us.  M^-1 is stored as float pairs (8 B an
+// element, as FP64) and the vectors are split before each apply; the sum is
+// exact to ~2^-48 of sum |M^-1||v|, and the FP64 residual r = b - M x0
+// (k_transient_resid) with the second apply restores FP64 accuracy.
+
+__global__ void k_split_pairs(const double *v, size_t count, float2 *out) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const double x = v[t];
+    const float h = (float)x;
+    out[t] = make_float2(h, (float)(x - (double)h));
+}
+
+// s += (a.x + a.y)(b.x + b.y) with the high parts two-summed into s.x and
+// every low-order term in s.y (a.y b.y dropped)
+__device__ __forceinline__ void pair_mac(float2 &s, float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    const float t = s.x + p;
+    const float bp = t - s.x;
+    const float err = (s.x - (t - bp)) + (p - bp);
+    s.x = t;
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    s.y += e + err;
+}
+
 // y[r][i] = y0[r][i] (when set) + sum_q Minv[i][q] v[r][q] for every run,
-// one warp per row of M^-1 (streamed once for all runs).
+// one warp per row of M^-1 (streamed once for all runs); vs: v as float
+// pairs (k_split_pairs), [run][nt].  Each lane reads two elements at a time
+// (16 B) and keeps kApplyDepth such loads in flight: a warp streams 4 KB of
+// its row per iteration, so that the memory system, not each warp's
+// load-to-use latency, sets the apply's pace.
+static constexpr int kApplyDepth = 8;
 template <int R>
-__global__ void __launch_bounds__(256) k_minv_apply(const double *Minv, int nt, const double *v, const double *y0,
+__global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, const float2 *vs, const double *y0,
                                                     double *y, int nrun) {
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= nt) return;
-    double acc[R];
-    row_dot_runs<R>(Minv + (size_t)i * nt, v, nt, nt, lane, acc);
+    const float2 *row = Minv + (size_t)i * nt;
+    float2 acc[2][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[0][r] = acc[1][r] = make_float2(0.0f, 0.0f);
+    // rows start 8-byte aligned; the 16-byte loads begin at the first even
+    // element of the row (nt odd: every other row starts at an odd one)
+    const int head = (int)(((size_t)i * nt) & 1);
+    if (head && lane == 0) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) pair_mac(acc[0][r], row[0], vs[(size_t)r * nt]);
+    }
+    const int body = (nt - head) / 2;  // float4 pairs of elements after the head
+    const float4 *row4 = reinterpret_cast<const float4 *>(row + head);
+    int t = lane;
+    for (; t + 32 * (kApplyDepth - 1) < body; t += 32 * kApplyDepth) {
+        float4 m[kApplyDepth];
+#pragma unroll
+        for (int u = 0; u < kApplyDepth; ++u) m[u] = __ldcs(row4 + t + 32 * u);
+#pragma unroll
+        for (int u = 0; u < kApplyDepth; ++u) {
+            const int j = head + 2 * (t + 32 * u);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float2 *v = vs + (size_t)r * nt + j;
+                pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), v[0]);
+                pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), v[1]);
+            }
+        }
+    }
+    for (; t < body; t += 32) {
+        const float4 m = __ldcs(row4 + t);
+        const int j = head + 2 * t;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float2 *v = vs + (size_t)r * nt + j;
+            pair_mac(acc[0][r], make_float2(m.x, m.y), v[0]);
+            pair_mac(acc[0][r], make_float2(m.z, m.w), v[1]);
+        }
+    }
+    const int tail = head + 2 * body;  // one element left when nt - head is odd
+    if (tail < nt && lane == 1) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) pair_mac(acc[1][r], row[tail], vs[(size_t)r * nt + tail]);
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        const double s = warp_sum(acc[r]);
+        const double part = ((double)acc[0][r].x + (double)acc[1][r].x) + ((double)acc[0][r].y + (double)acc[1][r].y);
+        const double s = warp_sum(part);
         if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s;
     }
 }
@@ -351,12 +430,24 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     int col;
     int s = peec_gb300_lu_factor_device(S.lu, nt, 1.0e-14, S.piv, S.perm, &scale, &col);
     if (s != 0) return s == -2 ? -2 : -1;
-    // M^-1 from the factor, once; the factor is not needed afterwards
-    S.minv = static_cast<double *>(dalloc(sizeof(double) * (size_t)nt * nt));
-    if (!S.minv || !inverse_from_lu_real(S.lu, S.perm, nt, S.minv) || !sync("transient inverse")) return -1;
+    // M^-1 from the factor, once (the factor is not needed afterwards), kept
+    // as float pairs for the double-float applies
+    const size_t nn = (size_t)nt * nt;
+    double *inv = static_cast<double *>(dalloc(sizeof(double) * nn));
+    if (!inv || !inverse_from_lu_real(S.lu, S.perm, nt, inv) || !sync("transient inverse")) {
+        dfree(inv);
+        return -1;
+    }
     dfree(S.lu);
     S.lu = nullptr;
-    return 0;
+    S.minv = static_cast<float2 *>(dalloc(sizeof(float2) * nn));
+    if (!S.minv) {
+        dfree(inv);
+        return -1;
+    }
+    PEEC_LAUNCH(k_split_pairs, (unsigned)((nn + 255) / 256), 256, 0, inv, nn, S.minv);
+    dfree(inv);
+    return launch_ok("transient inverse") && sync("transient inverse") ? 0 : -1;
 }
 
 static void launch_rhs(const StepArgs &A, int grid, int eb) {
@@ -378,7 +469,8 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     // reads that many states: pad with zero states
     const int cap = nrun <= 1 ? 1 : nrun <= 2 ? 2 : nrun <= 4 ? 4 : 8;
     DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
-    if (!x.p || !rhs.p || !x0.p || !res.p) return -1;
+    DBuf<float2> vs((size_t)nt * cap);  // the vector of an apply as float pairs
+    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p) return -1;
     cudaStream_t st = stream();
     if (cap > nrun) {
         for (double *p : {x.p, rhs.p, x0.p, res.p})
@@ -414,26 +506,32 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
         A.record_row = k - 1;
         launch_rhs(A, grid, eb);
         // x0 = M^-1 b; r = b - M x0; x = x0 + M^-1 r
+        const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
+        PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, rhs.p, (size_t)nt * cap, vs.p);
         switch (cap) {
             case 1:
-                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
                 PEEC_LAUNCH(k_transient_resid<1>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
+                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             case 2:
-                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
                 PEEC_LAUNCH(k_transient_resid<2>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
+                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             case 4:
-                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
                 PEEC_LAUNCH(k_transient_resid<4>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
+                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             default:
-                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, rhs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
                 PEEC_LAUNCH(k_transient_resid<8>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, res.p, x0.p, x.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
+                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
         }
         if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
