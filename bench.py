@@ -883,6 +883,19 @@ def serving_leg(lib, window_s, workers, lightning_steps=4096):
                     _, _, mi, f, k, e = r
                     tickets.append(("harmonic", srv.submit(pool[mi][0], mi, f, k, e, mixed=(mode == "mixed"))))
             res = [(kind, srv.wait(t)[1]) for kind, t in tickets]
+            # per request: type, unknowns, right-hand sides (harmonic), frequency
+            # MHz (harmonic), queue wait and service time (s), refinement
+            # iterations or steps, fallback rung
+            detail = []
+            for (kind, r), q in zip(res, reqs):
+                if kind == "harmonic":
+                    m_ = pool[q[2]][0]
+                    detail.append(["h", m_.n_edges + m_.n_nodes, len(q[4]), round(q[3] / 1e6, 2),
+                                   round(r["t_start"] - r["t_submit"], 3), round(r["t_end"] - r["t_start"], 3),
+                                   r.get("iterations"), r.get("fallback", 0)])
+                else:
+                    detail.append(["l", box.n_edges + box.n_nodes, 1, None, round(r["t_start"] - r["t_submit"], 3),
+                                   round(r["t_end"] - r["t_start"], 3), r.get("iterations"), 0])
             span = max(r["t_end"] for _, r in res) - min(r["t_submit"] for _, r in res)
             ok_h = sum(1 for k, r in res if k == "harmonic" and r["status"] == 0 and r["backward_error"] <= 1e-10)
             ok_l = sum(1 for k, r in res if k == "lightning" and r["status"] == 0)
@@ -900,7 +913,9 @@ def serving_leg(lib, window_s, workers, lightning_steps=4096):
                          "p50_latency_s": float(np.percentile(lat_all, 50)),
                          "p99_latency_s": float(np.percentile(lat_all, 99)), "per_type": per, "makespan_s": span,
                          "fallbacks_to_fp64": sum(r.get("fallback", 0) for k, r in res if k == "harmonic"),
-                         "max_backward_error": max(hb) if hb else None}
+                         "max_backward_error": max(hb) if hb else None,
+                         "per_request": {"fields": ["type", "unknowns", "rhs", "MHz", "wait_s", "service_s",
+                                                    "iterations", "fallback"], "rows": detail}}
     out["mixed_vs_plain"] = out["mixed"]["value"] / out["plain"]["value"]
     for m, _ in pool:
         m.close()

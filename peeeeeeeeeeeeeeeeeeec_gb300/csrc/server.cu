@@ -27,11 +27,18 @@
 
 namespace peec {
 
+int transient_lightning_runs(void *system, int nrun, const double *K, const double *alpha, const double *beta,
+                             const double *delay, const size_t *strike_node, const size_t *return_node,
+                             const long long *start, size_t step0, size_t n_steps, double *d_X,
+                             const int *d_probe_nodes, size_t n_probe_nodes, const int *d_probe_edges,
+                             size_t n_probe_edges, double *d_probes);
+
 struct TransientEntry {
     void *sys = nullptr;
     size_t bytes = 0;
     bool ready = false;
     int status = 0;
+    int session_room = 0;  // free run slots of the stepping sessions on this system
 };
 
 struct MeshEntry {
@@ -64,10 +71,11 @@ struct Job {
 };
 
 // a transient system at its peak (the factor and the inverse formed from
-// it, before the factor is freed) + A S + vectors
+// it, before the factor is freed) + Lp and A S as float pairs (+ the FP64
+// A S while they are formed) + vectors
 static size_t transient_system_bytes(size_t ne, size_t nv) {
     size_t nt = ne + nv;
-    return 16 * nt * nt + 8 * ne * nv + 64 * nt + 16 * ne;
+    return 16 * nt * nt + 8 * ne * ne + 16 * ne * nv + 64 * nt + 16 * ne;
 }
 
 class Server {
@@ -193,6 +201,16 @@ class Server {
         m.edges = nullptr;
     }
 
+    // a lightning run that a stepping session of its system has room for
+    // (it joins that session at its next chunk boundary)
+    bool steered(const Job &j) {
+        if (j.kind != 1) return false;
+        auto it = meshes_.find(j.mesh_key);
+        if (it == meshes_.end()) return false;
+        auto ti = it->second.transient.find({j.treq.scheme, j.treq.dt});
+        return ti != it->second.transient.end() && ti->second.session_room > 0;
+    }
+
     // bytes the job needs now: its own, plus the mesh and the transient
     // system when they are not cached
     size_t need(const Job &j) {
@@ -228,17 +246,22 @@ class Server {
             bool build_mesh = false, build_sys = false;
             {
                 std::unique_lock<std::mutex> g(mu_);
+                auto pick = queue_.end();
                 for (;;) {
                     if (stop_ && queue_.empty()) return;
-                    if (!queue_.empty()) {
-                        size_t nb = need(*queue_.front());
-                        make_room(nb, queue_.front()->mesh_key);
+                    // the first request in arrival order, passing over lightning
+                    // runs that a stepping session of their system will admit
+                    pick = queue_.begin();
+                    while (pick != queue_.end() && steered(**pick)) ++pick;
+                    if (pick != queue_.end()) {
+                        size_t nb = need(**pick);
+                        make_room(nb, (*pick)->mesh_key);
                         if (used_ + nb <= budget_) break;
                     }
                     cv_.wait(g);
                 }
-                j = queue_.front();
-                queue_.pop_front();
+                j = *pick;
+                queue_.erase(pick);
                 auto it = meshes_.find(j->mesh_key);
                 if (it == meshes_.end()) {
                     MeshEntry e;
@@ -265,26 +288,7 @@ class Server {
                 me->last_use = ++tick_;
                 used_ += j->bytes;
                 j->res.t_start = clock();
-                if (j->kind == 1) {
-                    // continuous batching of lightning runs: queued runs on the
-                    // same system with the same length and probes join this one
-                    // (up to 8 runs per step), as far as the budget allows
-                    for (auto q = queue_.begin(); q != queue_.end() && batch.size() < 7;) {
-                        const Job &o = **q;
-                        if (o.kind == 1 && o.mesh_key == j->mesh_key && o.treq.scheme == j->treq.scheme &&
-                            o.treq.dt == j->treq.dt && o.treq.n_steps == j->treq.n_steps &&
-                            o.probe_nodes == j->probe_nodes && o.probe_edges == j->probe_edges &&
-                            used_ + o.bytes <= budget_) {
-                            used_ += o.bytes;
-                            me->users++;
-                            (*q)->res.t_start = j->res.t_start;
-                            batch.push_back(*q);
-                            q = queue_.erase(q);
-                        } else {
-                            ++q;
-                        }
-                    }
-                }
+                if (j->kind == 1) admit_runs(*j, me, batch, 7, j->res.t_start);  // start with j
             }
             cv_.notify_all();
             if (build_mesh) {
@@ -315,24 +319,23 @@ class Server {
                 status = te->status;
             }
             batch.insert(batch.begin(), j);
-            if (status == 0) status = j->kind == 0 ? solve(*me, *j) : run_transient(*me, *te, batch);
+            if (j->kind == 1) {
+                // the stepping session finishes every run it steps: those of
+                // batch and those it admits on the way
+                run_session(me, *te, batch, status);
+            } else {
+                if (status == 0) status = solve(*me, *j);
+                std::lock_guard<std::mutex> g(mu_);
+                finish(me, j, status);
+            }
             {
                 std::lock_guard<std::mutex> g(mu_);
-                for (auto &b : batch) {
-                    b->res.status = status;
-                    b->res.t_end = clock();
-                    b->res.iterations = j->kind == 1 ? (int)b->treq.n_steps : b->res.iterations;
-                    used_ -= b->bytes;
-                    me->users--;
-                    if (b != j) b->done = true;
-                }
                 if ((me->status != 0 || (te && te->status != 0)) && me->users == 0) {
                     // a failed assembly or factorisation is not kept
                     used_ -= me->bytes;
                     free_mesh(*me);
                     meshes_.erase(me->key);
                 }
-                j->done = true;
             }
             cv_.notify_all();
             done_cv_.notify_all();
@@ -412,47 +415,174 @@ class Server {
         return status;
     }
 
-    // the lightning runs of `jobs` (same system, length and probes) stepped
-    // together; each job gets its own waveforms and final state
-    int run_transient(const MeshEntry &e, const TransientEntry &t, const std::vector<std::shared_ptr<Job>> &jobs) {
-        const Job &j0 = *jobs[0];
-        const int nrun = (int)jobs.size();
-        const size_t nt = e.ne + e.nv, n_steps = j0.treq.n_steps;
-        const size_t npn = j0.probe_nodes.size(), npe = j0.probe_edges.size(), np = npn + npe;
-        DBuf<double> X(nt * nrun), probes(n_steps * nrun * np);
-        DBuf<int> pn(npn), pe(npe);
-        if (!X.p || (np && !probes.p) || (npn && !pn.p) || (npe && !pe.p)) return -1;
-        cudaMemsetAsync(X.p, 0, 8 * nt * nrun, stream());
-        if ((npn && !pn.upload(j0.probe_nodes.data(), npn)) || (npe && !pe.upload(j0.probe_edges.data(), npe)))
-            return -1;
-        std::vector<double> K(nrun), al(nrun), be(nrun), de(nrun);
-        std::vector<size_t> sk(nrun), rt(nrun);
-        for (int r = 0; r < nrun; ++r) {
-            const PeecTransientRequest &q = jobs[r]->treq;
-            K[r] = q.K;
-            al[r] = q.alpha;
-            be[r] = q.beta;
-            de[r] = q.delay;
-            sk[r] = q.strike_node;
-            rt[r] = q.return_node;
+    // a finished request (the caller holds mu_)
+    void finish(MeshEntry *me, const std::shared_ptr<Job> &b, int status) {
+        b->res.status = status;
+        b->res.t_end = clock();
+        if (b->kind == 1) b->res.iterations = (int)b->treq.n_steps;
+        used_ -= b->bytes;
+        me->users--;
+        b->done = true;
+    }
+
+    // queued lightning runs that can join a stepping batch of j's system
+    // (same mesh, scheme and time step), up to `room` of them and as far as
+    // the budget allows; the caller holds mu_
+    void admit_runs(const Job &j, MeshEntry *me, std::vector<std::shared_ptr<Job>> &out, size_t room,
+                    double t_start) {
+        for (auto q = queue_.begin(); q != queue_.end() && out.size() < room;) {
+            const Job &o = **q;
+            if (o.kind == 1 && o.mesh_key == j.mesh_key && o.treq.scheme == j.treq.scheme &&
+                o.treq.dt == j.treq.dt && used_ + o.bytes <= budget_) {
+                used_ += o.bytes;
+                me->users++;
+                me->last_use = ++tick_;
+                (*q)->res.t_start = t_start;
+                out.push_back(*q);
+                q = queue_.erase(q);
+            } else {
+                ++q;
+            }
         }
-        int s = peec_gb300_transient_lightning_batch(t.sys, nrun, K.data(), al.data(), be.data(), de.data(),
-                                                     sk.data(), rt.data(), 0, n_steps, X.p, pn.p, npn, pe.p, npe,
-                                                     probes.p);
-        if (s != 0) return s;
-        std::vector<double> hx(nt * nrun), hp(n_steps * nrun * np);
-        if (!X.download(hx.data(), nt * nrun) || (np && !probes.download(hp.data(), hp.size())) ||
-            !sync("transient result"))
-            return -1;
-        for (int r = 0; r < nrun; ++r) {
-            const PeecTransientRequest &q = jobs[r]->treq;
-            if (np && q.probes)
-                for (size_t k = 0; k < n_steps; ++k)
-                    memcpy(q.probes + k * np, hp.data() + (k * nrun + r) * np, np * sizeof(double));
-            if (q.I) memcpy(q.I, hx.data() + r * nt, e.ne * sizeof(double));
-            if (q.V) memcpy(q.V, hx.data() + r * nt + e.ne, e.nv * sizeof(double));
+    }
+
+    // Continuous batching of lightning runs on one transient system: up to 8
+    // runs step together, in chunks of at most kChunk steps; between chunks
+    // the runs that reached their length leave (waveforms and final state
+    // copied out, the request finished) and queued runs of the same system
+    // join with their state at rest and their own step 0 at the current
+    // step.  While the session has free slots, workers leave that system's
+    // queued runs to it (steered()).  Each run keeps its own probe lists:
+    // a chunk records the concatenation of all runs' lists for every run,
+    // and each request takes its own columns.  A run's arithmetic does not
+    // depend on its slot or on the other runs, so its results equal a run
+    // alone bit for bit.
+    static constexpr size_t kChunk = 256;
+    struct Slot {
+        std::shared_ptr<Job> job;
+        long long start = 0;  // the session step of its own step 0
+        size_t done = 0;      // its steps so far
+    };
+    void run_session(MeshEntry *me, TransientEntry &t, const std::vector<std::shared_ptr<Job>> &first, int status) {
+        const size_t nt = me->ne + me->nv;
+        const Job &j0 = *first[0];
+        std::vector<Slot> slots;
+        for (auto &b : first) slots.push_back(Slot{b, 0, 0});
+        int room = 0;  // this session's share of t.session_room
+        auto set_room = [&](int r) {  // the caller holds mu_
+            t.session_room += r - room;
+            room = r;
+        };
+        DBuf<double> X(nt * 8), probes;
+        DBuf<int> pn, pe;
+        if (status == 0 && !X.p) status = -1;
+        if (status == 0) {
+            cudaMemsetAsync(X.p, 0, 8 * nt * slots.size(), stream());
+            std::lock_guard<std::mutex> g(mu_);
+            set_room(8 - (int)slots.size());
         }
-        return 0;
+        std::vector<double> hp, hx(nt);
+        std::vector<int> cn, ce;  // the chunk's concatenated probe lists
+        std::vector<size_t> on, oe;  // each slot's offsets in them
+        long long step = 0;
+        while (status == 0 && !slots.empty()) {
+            const int nrun = (int)slots.size();
+            size_t chunk = kChunk;
+            for (auto &sl : slots) chunk = std::min(chunk, (size_t)sl.job->treq.n_steps - sl.done);
+            std::vector<double> K(nrun), al(nrun), be(nrun), de(nrun);
+            std::vector<size_t> sk(nrun), rt(nrun);
+            std::vector<long long> st(nrun);
+            cn.clear();
+            ce.clear();
+            on.assign(nrun, 0);
+            oe.assign(nrun, 0);
+            for (int r = 0; r < nrun; ++r) {
+                const Job &jr = *slots[r].job;
+                const PeecTransientRequest &q = jr.treq;
+                K[r] = q.K;
+                al[r] = q.alpha;
+                be[r] = q.beta;
+                de[r] = q.delay;
+                sk[r] = q.strike_node;
+                rt[r] = q.return_node;
+                st[r] = slots[r].start;
+                on[r] = cn.size();
+                oe[r] = ce.size();
+                cn.insert(cn.end(), jr.probe_nodes.begin(), jr.probe_nodes.end());
+                ce.insert(ce.end(), jr.probe_edges.begin(), jr.probe_edges.end());
+            }
+            const size_t npn = cn.size(), npe = ce.size(), np = npn + npe;
+            if ((npn > pn.n && !pn.alloc(npn)) || (npe > pe.n && !pe.alloc(npe)) ||
+                (np * chunk * nrun > probes.n && !probes.alloc(np * kChunk * 8)) ||
+                (npn && !pn.upload(cn.data(), npn)) || (npe && !pe.upload(ce.data(), npe))) {
+                status = -1;
+                break;
+            }
+            status = transient_lightning_runs(t.sys, nrun, K.data(), al.data(), be.data(), de.data(), sk.data(),
+                                              rt.data(), st.data(), (size_t)step, chunk, X.p, pn.p, npn, pe.p, npe,
+                                              probes.p);
+            if (status != 0) break;
+            hp.resize(chunk * nrun * np);
+            if (np && (!probes.download(hp.data(), hp.size()) || !sync("transient probes"))) {
+                status = -1;
+                break;
+            }
+            for (int r = 0; r < nrun; ++r) {  // rows [k][run][np] -> each request's own columns
+                const Job &jr = *slots[r].job;
+                const size_t rn = jr.probe_nodes.size(), re = jr.probe_edges.size();
+                if ((rn + re) && jr.treq.probes)
+                    for (size_t k = 0; k < chunk; ++k) {
+                        const double *row = hp.data() + (k * nrun + r) * np;
+                        double *dst = jr.treq.probes + (slots[r].done + k) * (rn + re);
+                        memcpy(dst, row + on[r], rn * sizeof(double));
+                        memcpy(dst + rn, row + npn + oe[r], re * sizeof(double));
+                    }
+                slots[r].done += chunk;
+            }
+            step += (long long)chunk;
+            // runs that reached their length leave, the last slot moving into
+            // each freed one
+            std::vector<std::shared_ptr<Job>> finished;
+            for (int r = nrun - 1; r >= 0; --r) {
+                if (slots[r].done < slots[r].job->treq.n_steps) continue;
+                const PeecTransientRequest &q = slots[r].job->treq;
+                if (cudaMemcpyAsync(hx.data(), X.p + (size_t)r * nt, 8 * nt, cudaMemcpyDeviceToHost, stream()) !=
+                        cudaSuccess ||
+                    !sync("transient result")) {
+                    status = -1;
+                    break;
+                }
+                if (q.I) memcpy(q.I, hx.data(), me->ne * sizeof(double));
+                if (q.V) memcpy(q.V, hx.data() + me->ne, me->nv * sizeof(double));
+                finished.push_back(slots[r].job);
+                const int last = (int)slots.size() - 1;
+                if (r != last) {
+                    cudaMemcpyAsync(X.p + (size_t)r * nt, X.p + (size_t)last * nt, 8 * nt, cudaMemcpyDeviceToDevice,
+                                    stream());
+                    slots[r] = slots[last];
+                }
+                slots.pop_back();
+            }
+            std::vector<std::shared_ptr<Job>> joined;
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                for (auto &b : finished) finish(me, b, 0);
+                if (status == 0) admit_runs(j0, me, joined, 8 - slots.size(), clock());
+                set_room(status == 0 && slots.size() + joined.size() > 0 ? 8 - (int)(slots.size() + joined.size())
+                                                                         : 0);
+            }
+            if (!finished.empty()) done_cv_.notify_all();
+            for (auto &b : joined) {  // at rest, own step 0 at the current step
+                cudaMemsetAsync(X.p + slots.size() * nt, 0, 8 * nt, stream());
+                slots.push_back(Slot{b, step, 0});
+            }
+        }
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            set_room(0);
+            for (auto &sl : slots) finish(me, sl.job, status == 0 ? -1 : status);
+        }
+        cv_.notify_all();  // runs passed over for this session are open to every worker again
     }
 };
 

@@ -35,15 +35,17 @@ struct TransientSystem {
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
     float2 *minv = nullptr;  // M^-1 as float pairs (hi, lo), nt x nt row-major
+    float2 *Lf = nullptr, *ASf = nullptr;  // Lp (ne x ne) and A S (ne x nv) as float pairs
     long long *piv = nullptr;
     int *perm = nullptr, *edges = nullptr;
     int *adj_ptr = nullptr, *adj = nullptr;  // node j: edges +(e+1) entering (b = j), -(e+1) leaving (a = j)
     void release() {
-        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)piv,
+        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)Lf,
+                        (void *)ASf, (void *)piv,
                         (void *)perm, (void *)edges, (void *)adj_ptr, (void *)adj})
             dfree(p);
         R = F = AS = lu = dinv = nullptr;
-        minv = nullptr;
+        minv = Lf = ASf = nullptr;
         piv = nullptr;
         perm = edges = adj_ptr = adj = nullptr;
     }
@@ -99,6 +101,7 @@ __global__ void k_transient_fill(const double *L, const double *R, const double 
 struct LightningArgs {
     double K, alpha, beta, delay;
     int strike, ret;
+    long long start;  // the global step at which this run's own step 0 falls
 };
 
 // lightning.c:184-212
@@ -109,13 +112,16 @@ __device__ __forceinline__ double lightning_current(const LightningArgs &s, doub
 }
 
 // Several lightning runs on one system are stepped together (up to kMaxRuns):
-// the right-hand-side kernel reads each Lp / A S row once for all runs and
-// the wavefront solve takes the runs as right-hand sides, so the factor is
-// read once per step for all of them.
+// every matrix of a step (Lp and A S in the right-hand side and the
+// residual, M^-1 twice) is read once for all of them.  A run may join a
+// batch mid-way: its source time counts from its own start step, and its
+// state starts at rest.
 static const int kMaxRuns = 8;
 
 struct StepArgs {
-    const double *L, *R, *AS, *F;
+    const double *R, *F;
+    const float2 *Lf, *ASf;  // Lp and A S as float pairs
+    const float2 *xs;        // the states x as float pairs
     const int *adj_ptr, *adj;
     int ne, nv, nrun;
     double theta, dt;
@@ -147,92 +153,15 @@ __device__ __forceinline__ void record_probes(const StepArgs &A, long long row) 
     }
 }
 
-// this lane's part of row . x_r for every run r < nrun: each row element is
-// loaded once (streamed from HBM), two loads in flight per lane; the states
-// stay in L1 / L2
-template <int R>
-__device__ __forceinline__ void row_dot_runs(const double *row, const double *x, size_t ldx, int n, int lane,
-                                             double *acc) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) acc[r] = 0.0;
-    int j = lane;
-    for (; j + 32 < n; j += 64) {
-        const double a0 = __ldcs(row + j), a1 = __ldcs(row + j + 32);
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            acc[r] = fma(a0, x[r * ldx + j], acc[r]);
-            acc[r] = fma(a1, x[r * ldx + j + 32], acc[r]);
-        }
-    }
-    for (; j < n; j += 32) {
-        const double a0 = row[j];
-#pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] = fma(a0, x[r * ldx + j], acc[r]);
-    }
-}
-
-// Right-hand side of one step for every run (transient.c:1421-1631, edge
-// voltages absent): blocks [0, eb) take the edge rows, one warp per row and
-// all runs; the rest the (node, run) pairs.
-template <int R>
-__global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
-    const double omt = 1.0 - A.theta;
-    const int nt = A.ne + A.nv;
-    if (blockIdx.x == 0 && A.probes && A.record_row >= 0) record_probes(A, A.record_row);
-    if ((int)blockIdx.x < eb) {
-        const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-        if (i >= A.ne) return;
-        double s[R], sa[R];
-        row_dot_runs<R>(A.L + (size_t)i * A.ne, A.x, nt, A.ne, lane, s);
-        if (omt != 0.0)
-            row_dot_runs<R>(A.AS + (size_t)i * A.nv, A.x + A.ne, nt, A.nv, lane, sa);
-        else
-#pragma unroll
-            for (int r = 0; r < R; ++r) sa[r] = 0.0;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const double ls = warp_sum(s[r]), as = omt != 0.0 ? warp_sum(sa[r]) : 0.0;
-            if (lane == 0 && r < A.nrun) {
-                const double *I = A.x + (size_t)r * nt;
-                A.rhs[(size_t)r * nt + i] = ls / A.dt - omt * A.R[i] * I[i] - omt * as;
-            }
-        }
-        return;
-    }
-    const int t = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
-    if (t >= A.nv * A.nrun) return;
-    const int r = t / A.nv, j = t % A.nv;
-    const double *x = A.x + (size_t)r * nt;
-    const LightningArgs &src = A.src[r];
-    const double tn = (double)A.step * A.dt, tnp1 = (double)(A.step + 1) * A.dt;
-    double jn = 0.0, jnp1 = 0.0;
-    if (j == src.strike || j == src.ret) {
-        jn = lightning_current(src, tn);
-        jnp1 = lightning_current(src, tnp1);
-        if (j == src.ret) {
-            jn = -jn;
-            jnp1 = -jnp1;
-        }
-    }
-    double v = A.F[j] * x[A.ne + j] / A.dt;
-    double at = 0.0;  // (A^T I)_j
-    for (int k = A.adj_ptr[j]; k < A.adj_ptr[j + 1]; ++k) {
-        int e = A.adj[k];
-        at += e > 0 ? x[e - 1] : -x[-e - 1];
-    }
-    v += omt * at;
-    v += omt * jn;
-    v += A.theta * jnp1;
-    A.rhs[(size_t)r * nt + A.ne + j] = v;
-}
-
-// M^-1 is applied in double-float arithmetic on the FP32 pipes: one FP64
-// FMA per matrix element would hold the GEMV to GB300's FP64 rate (two per
-// clock per SM, ~110 us for the 5 cm box's 70.6 M elements) where the HBM
-// read of the matrix takes ~85 us.  M^-1 is stored as float pairs (8 B an
-// element, as FP64) and the vectors are split before each apply; the sum is
-// exact to ~2^-48 of sum |M^-1||v|, and the FP64 residual r = b - M x0
-// (k_transient_resid) with the second apply restores FP64 accuracy.
+// The step's matrix-vector products (M^-1, Lp, A S against every run's
+// vector) run in double-float arithmetic on the FP32 pipes, the matrices
+// stored as float pairs (8 B an element, as FP64): one FP64 FMA per element
+// and run would hold them to GB300's FP64 rate (two per clock per SM), so a
+// batch of 8 runs would cost 8x one run; here a batch streams each matrix
+// once at about the cost of one run.  Each sum is exact to ~2^-48 of
+// sum |a||v|; the FP64 residual of the refinement step and the FP64
+// diagonal and adjacency terms keep the step's result to ~1e-14 of the
+// FP64 recursion (the waveforms stay within 1e-11 of the reference's).
 
 __global__ void k_split_pairs(const double *v, size_t count, float2 *out) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -256,44 +185,39 @@ __device__ __forceinline__ void pair_mac(float2 &s, float2 a, float2 b) {
     s.y += e + err;
 }
 
-// y[r][i] = y0[r][i] (when set) + sum_q Minv[i][q] v[r][q] for every run,
-// one warp per row of M^-1 (streamed once for all runs); vs: v as float
-// pairs (k_split_pairs), [run][nt].  Each lane reads two elements at a time
-// (16 B) and keeps kApplyDepth such loads in flight: a warp streams 4 KB of
-// its row per iteration, so that the memory system, not each warp's
-// load-to-use latency, sets the apply's pace.
-static constexpr int kApplyDepth = 8;
+// out[r] = sum_j row[j] v[r][j] (j < n) for every run r < R, by the whole
+// warp (every lane returns the sums).  Each lane reads two elements at a
+// time (16 B) and keeps kDotDepth such loads in flight (4 KB per warp and
+// iteration), so the memory system, not each warp's load-to-use latency,
+// sets the pace.  v: run r's vector at v + r ldv (float pairs).
+static constexpr int kDotDepth = 8;
 template <int R>
-__global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, const float2 *vs, const double *y0,
-                                                    double *y, int nrun) {
-    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (i >= nt) return;
-    const float2 *row = Minv + (size_t)i * nt;
+__device__ __forceinline__ void row_dot_df(const float2 *row, int n, const float2 *v, size_t ldv, int lane,
+                                           double *out) {
     float2 acc[2][R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[0][r] = acc[1][r] = make_float2(0.0f, 0.0f);
-    // rows start 8-byte aligned; the 16-byte loads begin at the first even
-    // element of the row (nt odd: every other row starts at an odd one)
-    const int head = (int)(((size_t)i * nt) & 1);
+    // 16-byte loads start at the first 16-byte aligned element of the row
+    const int head = n > 0 && (reinterpret_cast<uintptr_t>(row) & 8) ? 1 : 0;
     if (head && lane == 0) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) pair_mac(acc[0][r], row[0], vs[(size_t)r * nt]);
+        for (int r = 0; r < R; ++r) pair_mac(acc[0][r], row[0], v[(size_t)r * ldv]);
     }
-    const int body = (nt - head) / 2;  // float4 pairs of elements after the head
+    const int body = (n - head) / 2;  // float4 pairs of elements after the head
     const float4 *row4 = reinterpret_cast<const float4 *>(row + head);
     int t = lane;
-    for (; t + 32 * (kApplyDepth - 1) < body; t += 32 * kApplyDepth) {
-        float4 m[kApplyDepth];
+    for (; t + 32 * (kDotDepth - 1) < body; t += 32 * kDotDepth) {
+        float4 m[kDotDepth];
 #pragma unroll
-        for (int u = 0; u < kApplyDepth; ++u) m[u] = __ldcs(row4 + t + 32 * u);
+        for (int u = 0; u < kDotDepth; ++u) m[u] = __ldcs(row4 + t + 32 * u);
 #pragma unroll
-        for (int u = 0; u < kApplyDepth; ++u) {
+        for (int u = 0; u < kDotDepth; ++u) {
             const int j = head + 2 * (t + 32 * u);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float2 *v = vs + (size_t)r * nt + j;
-                pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), v[0]);
-                pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), v[1]);
+                const float2 *vr = v + (size_t)r * ldv + j;
+                pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), vr[0]);
+                pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), vr[1]);
             }
         }
     }
@@ -302,22 +226,90 @@ __global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, 
         const int j = head + 2 * t;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const float2 *v = vs + (size_t)r * nt + j;
-            pair_mac(acc[0][r], make_float2(m.x, m.y), v[0]);
-            pair_mac(acc[0][r], make_float2(m.z, m.w), v[1]);
+            const float2 *vr = v + (size_t)r * ldv + j;
+            pair_mac(acc[0][r], make_float2(m.x, m.y), vr[0]);
+            pair_mac(acc[0][r], make_float2(m.z, m.w), vr[1]);
         }
     }
-    const int tail = head + 2 * body;  // one element left when nt - head is odd
-    if (tail < nt && lane == 1) {
+    const int tail = head + 2 * body;  // one element left when n - head is odd
+    if (tail < n && lane == 1) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) pair_mac(acc[1][r], row[tail], vs[(size_t)r * nt + tail]);
+        for (int r = 0; r < R; ++r) pair_mac(acc[1][r], row[tail], v[(size_t)r * ldv + tail]);
     }
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const double part = ((double)acc[0][r].x + (double)acc[1][r].x) + ((double)acc[0][r].y + (double)acc[1][r].y);
-        const double s = warp_sum(part);
-        if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s;
+    for (int r = 0; r < R; ++r)
+        out[r] = warp_sum(((double)acc[0][r].x + (double)acc[1][r].x) + ((double)acc[0][r].y + (double)acc[1][r].y));
+}
+
+// Right-hand side of one step for every run (transient.c:1421-1631, edge
+// voltages absent): blocks [0, eb) take the edge rows, one warp per row and
+// all runs; the rest the (node, run) pairs.
+template <int R>
+__global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
+    const double omt = 1.0 - A.theta;
+    const int nt = A.ne + A.nv;
+    if (blockIdx.x == 0 && A.probes && A.record_row >= 0) record_probes(A, A.record_row);
+    if ((int)blockIdx.x < eb) {
+        const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+        if (i >= A.ne) return;
+        double s[R], sa[R];
+        row_dot_df<R>(A.Lf + (size_t)i * A.ne, A.ne, A.xs, nt, lane, s);
+        if (omt != 0.0)
+            row_dot_df<R>(A.ASf + (size_t)i * A.nv, A.nv, A.xs + A.ne, nt, lane, sa);
+        else
+#pragma unroll
+            for (int r = 0; r < R; ++r) sa[r] = 0.0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const double ls = s[r], as = sa[r];
+            if (lane == 0 && r < A.nrun) {
+                const double *I = A.x + (size_t)r * nt;
+                A.rhs[(size_t)r * nt + i] = ls / A.dt - omt * A.R[i] * I[i] - omt * as;
+            }
+        }
+        return;
     }
+    const int t = (blockIdx.x - eb) * blockDim.x + threadIdx.x;
+    if (t >= A.nv * A.nrun) return;
+    const int r = t / A.nv, j = t % A.nv;
+    const double *x = A.x + (size_t)r * nt;
+    const LightningArgs &src = A.src[r];
+    const long long own = A.step - src.start;  // the run's own step number
+    const double tn = (double)own * A.dt, tnp1 = (double)(own + 1) * A.dt;
+    double jn = 0.0, jnp1 = 0.0;
+    if (j == src.strike || j == src.ret) {
+        jn = lightning_current(src, tn);
+        jnp1 = lightning_current(src, tnp1);
+        if (j == src.ret) {
+            jn = -jn;
+            jnp1 = -jnp1;
+        }
+    }
+    double v = A.F[j] * x[A.ne + j] / A.dt;
+    double at = 0.0;  // (A^T I)_j
+    for (int k = A.adj_ptr[j]; k < A.adj_ptr[j + 1]; ++k) {
+        int e = A.adj[k];
+        at += e > 0 ? x[e - 1] : -x[-e - 1];
+    }
+    v += omt * at;
+    v += omt * jn;
+    v += A.theta * jnp1;
+    A.rhs[(size_t)r * nt + A.ne + j] = v;
+}
+
+// y[r][i] = y0[r][i] (when set) + sum_q Minv[i][q] v[r][q] for every run,
+// one warp per row of M^-1 (streamed once for all runs); vs: v as float
+// pairs (k_split_pairs), [run][nt].
+template <int R>
+__global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, const float2 *vs, const double *y0,
+                                                    double *y, int nrun) {
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= nt) return;
+    double s[R];
+    row_dot_df<R>(Minv + (size_t)i * nt, nt, vs, nt, lane, s);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s[r];
 }
 
 // res = b - M x for every run (M of k_transient_fill applied from its
@@ -330,11 +322,11 @@ __global__ void __launch_bounds__(256) k_transient_resid(StepArgs A, const doubl
         const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
         if (i >= A.ne) return;
         double s[R], sa[R];
-        row_dot_runs<R>(A.L + (size_t)i * A.ne, A.x, nt, A.ne, lane, s);
-        row_dot_runs<R>(A.AS + (size_t)i * A.nv, A.x + A.ne, nt, A.nv, lane, sa);
+        row_dot_df<R>(A.Lf + (size_t)i * A.ne, A.ne, A.xs, nt, lane, s);
+        row_dot_df<R>(A.ASf + (size_t)i * A.nv, A.nv, A.xs + A.ne, nt, lane, sa);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const double ls = warp_sum(s[r]), as = warp_sum(sa[r]);
+            const double ls = s[r], as = sa[r];
             if (lane == 0 && r < A.nrun) {
                 const double *x = A.x + (size_t)r * nt;
                 const double mx = ls / A.dt + A.theta * A.R[i] * x[i] + A.theta * as;
@@ -426,6 +418,16 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
         set_error("transient: invalid diagonal of P (non-finite or not positive)");
         return -1;
     }
+    // Lp and A S as float pairs for the steps' double-float products; the
+    // FP64 A S served the fill only
+    S.Lf = static_cast<float2 *>(dalloc(sizeof(float2) * (size_t)ne * ne));
+    S.ASf = static_cast<float2 *>(dalloc(sizeof(float2) * nas));
+    if (!S.Lf || !S.ASf) return -1;
+    PEEC_LAUNCH(k_split_pairs, (unsigned)(((size_t)ne * ne + 255) / 256), 256, 0, d_L, (size_t)ne * ne, S.Lf);
+    PEEC_LAUNCH(k_split_pairs, (unsigned)((nas + 255) / 256), 256, 0, S.AS, nas, S.ASf);
+    if (!launch_ok("transient split") || !sync("transient split")) return -1;
+    dfree(S.AS);
+    S.AS = nullptr;
     double scale;
     int col;
     int s = peec_gb300_lu_factor_device(S.lu, nt, 1.0e-14, S.piv, S.perm, &scale, &col);
@@ -469,8 +471,10 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     // reads that many states: pad with zero states
     const int cap = nrun <= 1 ? 1 : nrun <= 2 ? 2 : nrun <= 4 ? 4 : 8;
     DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
-    DBuf<float2> vs((size_t)nt * cap);  // the vector of an apply as float pairs
-    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p) return -1;
+    // float pairs of the vectors: of an apply (vs), of the state x (xs) and of
+    // x0 (x0s) for the right-hand side and the residual products
+    DBuf<float2> vs((size_t)nt * cap), xs((size_t)nt * cap), x0s((size_t)nt * cap);
+    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p || !xs.p || !x0s.p) return -1;
     cudaStream_t st = stream();
     if (cap > nrun) {
         for (double *p : {x.p, rhs.p, x0.p, res.p})
@@ -478,10 +482,11 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     }
     cudaMemcpyAsync(x.p, d_X, sizeof(double) * nt * nrun, cudaMemcpyDeviceToDevice, st);
     StepArgs A{};
-    A.L = S.L;
     A.R = S.R;
-    A.AS = S.AS;
     A.F = S.F;
+    A.Lf = S.Lf;
+    A.ASf = S.ASf;
+    A.xs = xs.p;
     A.adj_ptr = S.adj_ptr;
     A.adj = S.adj;
     A.ne = ne;
@@ -501,34 +506,40 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     const int mgrid = (nt + 7) / 8;
     StepArgs Ares = A;  // the residual reads x0 as its state
     Ares.x = x0.p;
+    Ares.xs = x0s.p;
+    const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
         A.record_row = k - 1;
+        PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x.p, (size_t)nt * cap, xs.p);
         launch_rhs(A, grid, eb);
         // x0 = M^-1 b; r = b - M x0; x = x0 + M^-1 r
-        const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
         PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, rhs.p, (size_t)nt * cap, vs.p);
         switch (cap) {
             case 1:
                 PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
                 PEEC_LAUNCH(k_transient_resid<1>, grid, 256, 0, Ares, rhs.p, res.p, eb);
                 PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
                 PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             case 2:
                 PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
                 PEEC_LAUNCH(k_transient_resid<2>, grid, 256, 0, Ares, rhs.p, res.p, eb);
                 PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
                 PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             case 4:
                 PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
                 PEEC_LAUNCH(k_transient_resid<4>, grid, 256, 0, Ares, rhs.p, res.p, eb);
                 PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
                 PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
                 break;
             default:
                 PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
+                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
                 PEEC_LAUNCH(k_transient_resid<8>, grid, 256, 0, Ares, rhs.p, res.p, eb);
                 PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
                 PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
@@ -551,6 +562,42 @@ static bool source_ok(const TransientSystem &S, double K, double alpha, double b
     return isfinite(K) && K > 0.0 && isfinite(alpha) && isfinite(beta) && alpha > 0.0 && beta > 0.0 &&
            beta > alpha && isfinite(delay) && delay >= 0.0 && strike < (size_t)S.nv && ret < (size_t)S.nv &&
            strike != ret;
+}
+
+// The batch entry with each run's start step (null: all 0); the server's
+// continuous batching admits runs into a stepping batch at chunk
+// boundaries with start = the current global step.
+int transient_lightning_runs(void *system, int nrun, const double *K, const double *alpha, const double *beta,
+                             const double *delay, const size_t *strike_node, const size_t *return_node,
+                             const long long *start, size_t step0, size_t n_steps, double *d_X,
+                             const int *d_probe_nodes, size_t n_probe_nodes, const int *d_probe_edges,
+                             size_t n_probe_edges, double *d_probes) {
+    auto *S = static_cast<TransientSystem *>(system);
+    if (!S || !d_X || nrun < 1 || nrun > kMaxRuns || !K || !alpha || !beta || !delay || !strike_node ||
+        !return_node) {
+        set_error("transient: missing system, state or sources (1 to 8 runs)");
+        return -1;
+    }
+    LightningArgs src[kMaxRuns];
+    for (int r = 0; r < nrun; ++r) {
+        if (!source_ok(*S, K[r], alpha[r], beta[r], delay[r], strike_node[r], return_node[r])) {
+            set_error("transient: invalid lightning source (K > 0, 0 < alpha < beta, delay >= 0, two distinct nodes)");
+            return -1;
+        }
+        if (start && (start[r] < 0 || start[r] > (long long)step0)) {
+            set_error("transient: a run's start step lies after the batch's first step");
+            return -1;
+        }
+        src[r] = LightningArgs{K[r], alpha[r], beta[r], delay[r], (int)strike_node[r], (int)return_node[r],
+                               start ? start[r] : 0};
+    }
+    if ((n_probe_nodes && !d_probe_nodes) || (n_probe_edges && !d_probe_edges) ||
+        ((n_probe_nodes || n_probe_edges) && !d_probes) || n_probe_nodes + n_probe_edges > (1u << 20)) {
+        set_error("transient: probe arrays missing");
+        return -1;
+    }
+    return run_lightning(*S, src, nrun, (long long)step0, (long long)n_steps, d_X, d_probe_nodes, (int)n_probe_nodes,
+                         d_probe_edges, (int)n_probe_edges, d_probes);
 }
 
 }  // namespace peec
@@ -603,27 +650,9 @@ int peec_gb300_transient_lightning_batch(void *system, int nrun, const double *K
                                          const size_t *return_node, size_t step0, size_t n_steps, double *d_X,
                                          const int *d_probe_nodes, size_t n_probe_nodes, const int *d_probe_edges,
                                          size_t n_probe_edges, double *d_probes) {
-    auto *S = static_cast<TransientSystem *>(system);
-    if (!S || !d_X || nrun < 1 || nrun > kMaxRuns || !K || !alpha || !beta || !delay || !strike_node ||
-        !return_node) {
-        set_error("transient: missing system, state or sources (1 to 8 runs)");
-        return -1;
-    }
-    LightningArgs src[kMaxRuns];
-    for (int r = 0; r < nrun; ++r) {
-        if (!source_ok(*S, K[r], alpha[r], beta[r], delay[r], strike_node[r], return_node[r])) {
-            set_error("transient: invalid lightning source (K > 0, 0 < alpha < beta, delay >= 0, two distinct nodes)");
-            return -1;
-        }
-        src[r] = LightningArgs{K[r], alpha[r], beta[r], delay[r], (int)strike_node[r], (int)return_node[r]};
-    }
-    if ((n_probe_nodes && !d_probe_nodes) || (n_probe_edges && !d_probe_edges) ||
-        ((n_probe_nodes || n_probe_edges) && !d_probes) || n_probe_nodes + n_probe_edges > (1u << 20)) {
-        set_error("transient: probe arrays missing");
-        return -1;
-    }
-    return run_lightning(*S, src, nrun, (long long)step0, (long long)n_steps, d_X, d_probe_nodes, (int)n_probe_nodes,
-                         d_probe_edges, (int)n_probe_edges, d_probes);
+    return peec::transient_lightning_runs(system, nrun, K, alpha, beta, delay, strike_node, return_node, nullptr,
+                                          step0, n_steps, d_X, d_probe_nodes, n_probe_nodes, d_probe_edges,
+                                          n_probe_edges, d_probes);
 }
 
 void peec_gb300_transient_destroy(void *system) {

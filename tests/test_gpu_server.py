@@ -215,3 +215,36 @@ def test_queued_transient_runs_are_batched(gpu_lib, meshes):
         assert rb["status"] == 0
     for ((pb, Ib, Vb), rb), (s, I, V, p) in zip(outs, ref):
         assert np.array_equal(pb, p) and np.array_equal(Ib, I) and np.array_equal(Vb, V)
+
+
+def test_lightning_runs_join_a_running_batch(gpu_lib, meshes):
+    """A lightning run submitted while another run on the same system is
+    stepping joins that batch at a chunk boundary (one worker: it starts
+    before the first run ends), with its own probe lists, and both equal
+    their direct runs bit for bit."""
+    import time
+    from test_gpu_transient import DeviceTransient
+    from helpers import inductance, potential
+    m = meshes[0]
+    runs = [((102900.0, 1500.0, 1.0e6, 0.0, 3, 20), 20000, [0, 3, 20], [1, 5]),
+            ((6.0e4, 1800.0, 4.0e5, 1e-7, 12, 25), 700, [12], [2, 7, 9])]
+    s1, L = inductance(gpu_lib, m)
+    s2, P = potential(gpu_lib, m)
+    direct = DeviceTransient(gpu_lib, L, P, m.edges(), None, 2, 1e-7)
+    try:
+        ref = [direct.run(src, n, probe_nodes=pn, probe_edges=pe) for src, n, pn, pe in runs]
+    finally:
+        direct.close()
+    with Server(8 * GB, 1) as srv:
+        src, n, pn, pe = runs[0]
+        ta = srv.submit_transient(m, 0, n, src, probe_nodes=pn, probe_edges=pe)
+        time.sleep(0.05)
+        src, n, pn, pe = runs[1]
+        tb = srv.submit_transient(m, 0, n, src, probe_nodes=pn, probe_edges=pe)
+        (pa, Ia, Va), ra = srv.wait(ta)
+        (pb, Ib, Vb), rb = srv.wait(tb)
+    assert ra["status"] == 0 and rb["status"] == 0
+    assert rb["t_start"] < ra["t_end"]  # it joined, not queued behind the first run
+    for (p, I, V), (s, Ir, Vr, pr) in zip(((pa, Ia, Va), (pb, Ib, Vb)), ref):
+        assert s == 0
+        assert np.array_equal(p, pr) and np.array_equal(I, Ir) and np.array_equal(V, Vr)
