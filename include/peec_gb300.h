@@ -366,10 +366,9 @@ int peec_gb300_transient_lightning(void *system, double K, double alpha, double 
 /* nrun (1 to 8) lightning runs on one system stepped together: run r has
  * its own source (K[r], alpha[r], beta[r], delay[r], strike_node[r],
  * return_node[r]) and state d_X + r (Ne + Nv) = [I; V] (in and out); every
- * step reads Lp, A S and the factor once for all runs (the runs are the
- * right-hand sides of one wavefront solve).  d_probes:
+ * step reads Lp, A S and the system's inverse once for all runs.  d_probes:
  * [n_steps][nrun][n_probe_nodes + n_probe_edges].  Each run's result is the
- * one a single run gives, to rounding. */
+ * one a single run gives, bit for bit. */
 int peec_gb300_transient_lightning_batch(void *system, int nrun, const double *K,
                                          const double *alpha, const double *beta,
                                          const double *delay, const size_t *strike_node,

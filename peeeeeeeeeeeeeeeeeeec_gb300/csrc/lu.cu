@@ -2299,12 +2299,23 @@ struct PhaseTrace {
 
 // Split-BF16 terms the mixed path's first factorisation uses: 3 (BF16x3),
 // or 6 (BF16x6) with PEEC_GB300_MIXED_SPLIT=6.
+static thread_local int g_start_terms = 0;  // set_mixed_start_terms
 static int mixed_split_terms() {
     static const int t = [] {
         const char *e = getenv("PEEC_GB300_MIXED_SPLIT");
         return e && strcmp(e, "6") == 0 ? 6 : 3;
     }();
-    return t;
+    return g_start_terms ? g_start_terms : t;
+}
+
+// The split terms this host thread's next mixed solves start with (3 or 6;
+// 0: the default).  The batched sweep starts its fallback solves with
+// BF16x6: a system its graph did not bring to the gate gains nothing from
+// another BF16x3 attempt.  Returns the previous setting.
+int set_mixed_start_terms(int t) {
+    const int prev = g_start_terms;
+    g_start_terms = (t == 3 || t == 6) ? t : 0;
+    return prev;
 }
 
 // FP32 panel of the mixed path: the cluster panel (k_panel_cl) where the

@@ -288,7 +288,7 @@ class Server {
                 me->last_use = ++tick_;
                 used_ += j->bytes;
                 j->res.t_start = clock();
-                if (j->kind == 1) admit_runs(*j, me, batch, 7, j->res.t_start);  // start with j
+                if (j->kind == 1) admit_runs(*j, me, batch, kMaxSlots - 1, j->res.t_start);  // start with j
             }
             cv_.notify_all();
             if (build_mesh) {
@@ -446,8 +446,8 @@ class Server {
         }
     }
 
-    // Continuous batching of lightning runs on one transient system: up to 8
-    // runs step together, in chunks of at most kChunk steps; between chunks
+    // Continuous batching of lightning runs on one transient system: up to
+    // kMaxSlots runs step together, in chunks of at most kChunk steps; between chunks
     // the runs that reached their length leave (waveforms and final state
     // copied out, the request finished) and queued runs of the same system
     // join with their state at rest and their own step 0 at the current
@@ -458,6 +458,7 @@ class Server {
     // depend on its slot or on the other runs, so its results equal a run
     // alone bit for bit.
     static constexpr size_t kChunk = 256;
+    static constexpr int kMaxSlots = 8;
     struct Slot {
         std::shared_ptr<Job> job;
         long long start = 0;  // the session step of its own step 0
@@ -473,13 +474,13 @@ class Server {
             t.session_room += r - room;
             room = r;
         };
-        DBuf<double> X(nt * 8), probes;
+        DBuf<double> X(nt * kMaxSlots), probes;
         DBuf<int> pn, pe;
         if (status == 0 && !X.p) status = -1;
         if (status == 0) {
             cudaMemsetAsync(X.p, 0, 8 * nt * slots.size(), stream());
             std::lock_guard<std::mutex> g(mu_);
-            set_room(8 - (int)slots.size());
+            set_room(kMaxSlots - (int)slots.size());
         }
         std::vector<double> hp, hx(nt);
         std::vector<int> cn, ce;  // the chunk's concatenated probe lists
@@ -513,7 +514,7 @@ class Server {
             }
             const size_t npn = cn.size(), npe = ce.size(), np = npn + npe;
             if ((npn > pn.n && !pn.alloc(npn)) || (npe > pe.n && !pe.alloc(npe)) ||
-                (np * chunk * nrun > probes.n && !probes.alloc(np * kChunk * 8)) ||
+                (np * chunk * nrun > probes.n && !probes.alloc(np * kChunk * kMaxSlots)) ||
                 (npn && !pn.upload(cn.data(), npn)) || (npe && !pe.upload(ce.data(), npe))) {
                 status = -1;
                 break;
@@ -567,9 +568,10 @@ class Server {
             {
                 std::lock_guard<std::mutex> g(mu_);
                 for (auto &b : finished) finish(me, b, 0);
-                if (status == 0) admit_runs(j0, me, joined, 8 - slots.size(), clock());
-                set_room(status == 0 && slots.size() + joined.size() > 0 ? 8 - (int)(slots.size() + joined.size())
-                                                                         : 0);
+                if (status == 0) admit_runs(j0, me, joined, kMaxSlots - slots.size(), clock());
+                set_room(status == 0 && slots.size() + joined.size() > 0
+                             ? kMaxSlots - (int)(slots.size() + joined.size())
+                             : 0);
             }
             if (!finished.empty()) done_cv_.notify_all();
             for (auto &b : joined) {  // at rest, own step 0 at the current step

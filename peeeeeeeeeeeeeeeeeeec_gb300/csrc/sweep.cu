@@ -11,9 +11,9 @@
 // the whole sweep.  Different meshes run their plans from different host
 // threads (each thread has its own stream), so their graphs overlap on the
 // device.  Systems whose backward error is above the tolerance after the
-// fixed sweeps are solved again outside the graph: by the mixed solve with
-// its full precision ladder, then, if that does not reach the gate, by the
-// FP64 LU with FP64 refinement.
+// fixed sweeps are solved again outside the graph: by the mixed solve from
+// its BF16x6 rung (then FGMRES-IR), then, if that does not reach the gate,
+// by the FP64 LU with FP64 refinement.
 //
 // A plan holds two graphs: a fast one (split-BF16x3 products, up to 10
 // refinement sweeps) and a robust one (BF16x6, up to 16) for the
@@ -41,6 +41,7 @@ bool launch_harmonic_fill_dev(const double *L, const double *P, const int *edges
 bool launch_plane_waves_dev(const double *centers, const double *vectors, int ne, int nv, int nrhs,
                             const double *d_k_hat, const double *d_e_hat, const double *k0_dev, void *rhs);
 int set_tc_wide_tile(int bn);
+int set_mixed_start_terms(int t);
 
 static const double kC0 = 299792458.0;
 
@@ -154,7 +155,11 @@ static int solve_fallback(SweepPlan &p, double freq, double tol, Complex *d_X, d
         !sync("sweep: fallback set-up"))
         return -1;
     int it = 0;
+    // straight to BF16x6 (then FGMRES-IR if that stalls): the graph's own
+    // attempt already showed BF16x3 (or BF16x6 refinement alone) short
+    const int prev_terms = set_mixed_start_terms(6);
     int s = mixed_solve_impl(p.d_Z, (size_t)p.n, p.d_b, d_X, (size_t)p.nrhs, tol, 30, eta, &it, nullptr);
+    set_mixed_start_terms(prev_terms);
     if (s == 0) {
         *fallback = 1;
         return 0;

@@ -187,13 +187,15 @@ __device__ __forceinline__ void pair_mac(float2 &s, float2 a, float2 b) {
 
 // out[r] = sum_j row[j] v[r][j] (j < n) for every run r < R, by the whole
 // warp (every lane returns the sums).  Each lane reads two elements at a
-// time (16 B) and keeps kDotDepth such loads in flight (4 KB per warp and
+// time (16 B) and keeps up to 8 such loads in flight (4 KB per warp and
 // iteration), so the memory system, not each warp's load-to-use latency,
 // sets the pace.  v: run r's vector at v + r ldv (float pairs).
-static constexpr int kDotDepth = 8;
 template <int R>
 __device__ __forceinline__ void row_dot_df(const float2 *row, int n, const float2 *v, size_t ldv, int lane,
                                            double *out) {
+    // loads in flight: fewer with more runs, whose products give each load
+    // more work (and whose accumulators need the registers)
+    constexpr int kDotDepth = R >= 8 ? 4 : 8;
     float2 acc[2][R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[0][r] = acc[1][r] = make_float2(0.0f, 0.0f);
@@ -452,14 +454,24 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     return launch_ok("transient inverse") && sync("transient inverse") ? 0 : -1;
 }
 
-static void launch_rhs(const StepArgs &A, int grid, int eb) {
-    switch (A.nrun) {
-        case 1: PEEC_LAUNCH(k_transient_rhs<1>, grid, 256, 0, A, eb); break;
-        case 2: PEEC_LAUNCH(k_transient_rhs<2>, grid, 256, 0, A, eb); break;
-        case 3:
-        case 4: PEEC_LAUNCH(k_transient_rhs<4>, grid, 256, 0, A, eb); break;
-        default: PEEC_LAUNCH(k_transient_rhs<8>, grid, 256, 0, A, eb); break;
-    }
+// One step for R run slots (the states padded with zero runs): split x,
+// right-hand side, x0 = M^-1 b, split x0, r = b - M x0, x = x0 + M^-1 r.
+struct StepBuffers {
+    double *x, *rhs, *x0, *res;
+    float2 *vs, *xs, *x0s;
+};
+template <int R>
+static void launch_step(const TransientSystem &S, const StepArgs &A, const StepArgs &Ares, const StepBuffers &b,
+                        int grid, int eb, int mgrid, unsigned sgrid, size_t nvec, int nrun) {
+    const int nt = S.nt;
+    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x, nvec, b.xs);
+    PEEC_LAUNCH(k_transient_rhs<R>, grid, 256, 0, A, eb);
+    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.rhs, nvec, b.vs);
+    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, b.vs, (const double *)nullptr, b.x0, nrun);
+    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x0, nvec, b.x0s);
+    PEEC_LAUNCH(k_transient_resid<R>, grid, 256, 0, Ares, b.rhs, b.res, eb);
+    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.res, nvec, b.vs);
+    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, b.vs, b.x0, b.x, nrun);
 }
 
 // nrun runs (states d_X[r] = [I; V], sources src[r]) stepped together
@@ -467,8 +479,9 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
                          long long n_steps, double *d_X, const int *probe_nodes, int n_probe_nodes,
                          const int *probe_edges, int n_probe_edges, double *probes) {
     const int ne = S.ne, nv = S.nv, nt = S.nt;
-    // the right-hand-side kernel is instantiated for 1, 2, 4 or 8 runs and
-    // reads that many states: pad with zero states
+    // the step kernels are instantiated for 1, 2, 4 or 8 runs and read that
+    // many states: pad with zero states (measured: a 16-run instantiation
+    // stepped 16 runs slower than two batches of 8)
     const int cap = nrun <= 1 ? 1 : nrun <= 2 ? 2 : nrun <= 4 ? 4 : 8;
     DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
     // float pairs of the vectors: of an apply (vs), of the state x (xs) and of
@@ -508,42 +521,16 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     Ares.x = x0.p;
     Ares.xs = x0s.p;
     const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
+    const StepBuffers bufs{x.p, rhs.p, x0.p, res.p, vs.p, xs.p, x0s.p};
+    const size_t nvec = (size_t)nt * cap;
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
         A.record_row = k - 1;
-        PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x.p, (size_t)nt * cap, xs.p);
-        launch_rhs(A, grid, eb);
-        // x0 = M^-1 b; r = b - M x0; x = x0 + M^-1 r
-        PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, rhs.p, (size_t)nt * cap, vs.p);
         switch (cap) {
-            case 1:
-                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
-                PEEC_LAUNCH(k_transient_resid<1>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
-                PEEC_LAUNCH(k_minv_apply<1>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
-                break;
-            case 2:
-                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
-                PEEC_LAUNCH(k_transient_resid<2>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
-                PEEC_LAUNCH(k_minv_apply<2>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
-                break;
-            case 4:
-                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
-                PEEC_LAUNCH(k_transient_resid<4>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
-                PEEC_LAUNCH(k_minv_apply<4>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
-                break;
-            default:
-                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, (const double *)nullptr, x0.p, nrun);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, x0.p, (size_t)nt * cap, x0s.p);
-                PEEC_LAUNCH(k_transient_resid<8>, grid, 256, 0, Ares, rhs.p, res.p, eb);
-                PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, res.p, (size_t)nt * cap, vs.p);
-                PEEC_LAUNCH(k_minv_apply<8>, mgrid, 256, 0, S.minv, nt, vs.p, x0.p, x.p, nrun);
-                break;
+            case 1: launch_step<1>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
+            case 2: launch_step<2>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
+            case 4: launch_step<4>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
+            default: launch_step<8>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
         }
         if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
     }

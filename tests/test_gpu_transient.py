@@ -170,9 +170,9 @@ def test_invalid_inputs(gpu_lib):
 
 
 def test_batched_runs_equal_single_runs(gpu_lib):
-    """Three runs with different sources stepped together (one right-hand
-    side kernel and one wavefront solve per step for all) give each run's
-    single-run waveforms bit for bit; bad sources and run counts are refused."""
+    """Three runs with different sources stepped together (every matrix of a
+    step read once for all) give each run's single-run waveforms bit for
+    bit; bad run counts are refused."""
     f, g = golden("box421"), golden("transient_box421")
     ne, nv = f["L"].shape[0], f["P"].shape[0]
     nt = ne + nv
@@ -199,8 +199,12 @@ def test_batched_runs_equal_single_runs(gpu_lib):
             assert s == 0
             assert np.array_equal(probes[:, r, :], p1)
             assert np.array_equal(X[r, :ne], I) and np.array_equal(X[r, ne:], V)
-        bad = gpu_lib.peec_gb300_transient_lightning_batch(t.h, 9, col(0), col(1), col(2), col(3), sz(4), sz(5), 0, 5,
-                                                           dX, None, 0, None, 0, None)
+        # more runs than a batch takes (8): refused before any array is read
+        big = 9
+        colb = lambda k: (C.c_double * big)(*([s[k] for s in srcs] * 6)[:big])
+        szb = lambda k: (C.c_size_t * big)(*([s[k] for s in srcs] * 6)[:big])
+        bad = gpu_lib.peec_gb300_transient_lightning_batch(t.h, big, colb(0), colb(1), colb(2), colb(3), szb(4),
+                                                           szb(5), 0, 5, dX, None, 0, None, 0, None)
         assert bad == -1
     finally:
         t.close()
