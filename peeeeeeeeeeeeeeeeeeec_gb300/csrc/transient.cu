@@ -35,17 +35,20 @@ struct TransientSystem {
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
     float2 *minv = nullptr;  // M^-1 as float pairs (hi, lo), nt x nt row-major
+    float *minv_hi = nullptr;  // their high parts alone, for the correction's FP32 apply
     float2 *Lf = nullptr, *ASf = nullptr;  // Lp (ne x ne) and A S (ne x nv) as float pairs
     long long *piv = nullptr;
     int *perm = nullptr, *edges = nullptr;
     int *adj_ptr = nullptr, *adj = nullptr;  // node j: edges +(e+1) entering (b = j), -(e+1) leaving (a = j)
     void release() {
-        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)Lf,
+        for (void *p : {(void *)R, (void *)F, (void *)AS, (void *)lu, (void *)dinv, (void *)minv, (void *)minv_hi,
+                        (void *)Lf,
                         (void *)ASf, (void *)piv,
                         (void *)perm, (void *)edges, (void *)adj_ptr, (void *)adj})
             dfree(p);
         R = F = AS = lu = dinv = nullptr;
         minv = Lf = ASf = nullptr;
+        minv_hi = nullptr;
         piv = nullptr;
         perm = edges = adj_ptr = adj = nullptr;
     }
@@ -314,6 +317,89 @@ __global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, 
         if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s[r];
 }
 
+// out[r] = sum_j row[j] v[r][j].x (j < n) in FP32 (FP64 across the warp),
+// for the correction x = x0 + M^-1 r of the refinement step: r is ~2^-48
+// of b, so the correction needs only a few correct digits, and its FP32
+// apply streams half the bytes (the high parts alone).
+template <int R>
+__device__ __forceinline__ void row_dot_f32(const float *row, int n, const float2 *v, size_t ldv, int lane,
+                                            double *out) {
+    float acc[2][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[0][r] = acc[1][r] = 0.0f;
+    // 16-byte loads from the first 16-byte aligned element of the row
+    const int head = min(n, (int)((4 - ((reinterpret_cast<uintptr_t>(row) >> 2) & 3)) & 3));
+    if (lane < head) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[0][r] = fmaf(row[lane], v[(size_t)r * ldv + lane].x, acc[0][r]);
+    }
+    const int body = (n - head) / 4;  // float4 groups after the head
+    const float4 *row4 = reinterpret_cast<const float4 *>(row + head);
+    constexpr int kDepth = 4;
+    int t = lane;
+    for (; t + 32 * (kDepth - 1) < body; t += 32 * kDepth) {
+        float4 m[kDepth];
+#pragma unroll
+        for (int u = 0; u < kDepth; ++u) m[u] = __ldcs(row4 + t + 32 * u);
+#pragma unroll
+        for (int u = 0; u < kDepth; ++u) {
+            const int j = head + 4 * (t + 32 * u);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float2 *vr = v + (size_t)r * ldv + j;
+                float a = acc[u & 1][r];
+                a = fmaf(m[u].x, vr[0].x, a);
+                a = fmaf(m[u].y, vr[1].x, a);
+                a = fmaf(m[u].z, vr[2].x, a);
+                a = fmaf(m[u].w, vr[3].x, a);
+                acc[u & 1][r] = a;
+            }
+        }
+    }
+    for (; t < body; t += 32) {
+        const float4 m = __ldcs(row4 + t);
+        const int j = head + 4 * t;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float2 *vr = v + (size_t)r * ldv + j;
+            float a = acc[0][r];
+            a = fmaf(m.x, vr[0].x, a);
+            a = fmaf(m.y, vr[1].x, a);
+            a = fmaf(m.z, vr[2].x, a);
+            a = fmaf(m.w, vr[3].x, a);
+            acc[0][r] = a;
+        }
+    }
+    const int tail0 = head + 4 * body;  // up to 3 elements left
+    if (tail0 + lane < n) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            acc[1][r] = fmaf(row[tail0 + lane], v[(size_t)r * ldv + tail0 + lane].x, acc[1][r]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[r] = warp_sum((double)acc[0][r] + (double)acc[1][r]);
+}
+
+// y[r][i] = y0[r][i] + sum_q Minv_hi[i][q] v[r][q].x for every run (the
+// refinement step's correction), one warp per row.
+template <int R>
+__global__ void __launch_bounds__(256) k_minv_apply_hi(const float *Mh, int nt, const float2 *vs, const double *y0,
+                                                       double *y, int nrun) {
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= nt) return;
+    double s[R];
+    row_dot_f32<R>(Mh + (size_t)i * nt, nt, vs, nt, lane, s);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = y0[(size_t)r * nt + i] + s[r];
+}
+
+// high parts of float pairs, for the FP32 apply
+__global__ void k_pairs_hi(const float2 *in, size_t count, float *out) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) out[t] = in[t].x;
+}
+
 // res = b - M x for every run (M of k_transient_fill applied from its
 // blocks: Lp / dt, theta R, theta AS, -theta A^T through the adjacency,
 // F / dt), rows split as in k_transient_rhs.
@@ -451,11 +537,15 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     }
     PEEC_LAUNCH(k_split_pairs, (unsigned)((nn + 255) / 256), 256, 0, inv, nn, S.minv);
     dfree(inv);
+    S.minv_hi = static_cast<float *>(dalloc(sizeof(float) * nn));
+    if (!S.minv_hi) return -1;
+    PEEC_LAUNCH(k_pairs_hi, (unsigned)((nn + 255) / 256), 256, 0, S.minv, nn, S.minv_hi);
     return launch_ok("transient inverse") && sync("transient inverse") ? 0 : -1;
 }
 
 // One step for R run slots (the states padded with zero runs): split x,
-// right-hand side, x0 = M^-1 b, split x0, r = b - M x0, x = x0 + M^-1 r.
+// right-hand side, x0 = M^-1 b (double-float), split x0, r = b - M x0
+// (double-float), x = x0 + M^-1 r (FP32: the correction is ~2^-48 of x).
 struct StepBuffers {
     double *x, *rhs, *x0, *res;
     float2 *vs, *xs, *x0s;
@@ -471,7 +561,7 @@ static void launch_step(const TransientSystem &S, const StepArgs &A, const StepA
     PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x0, nvec, b.x0s);
     PEEC_LAUNCH(k_transient_resid<R>, grid, 256, 0, Ares, b.rhs, b.res, eb);
     PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.res, nvec, b.vs);
-    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, b.vs, b.x0, b.x, nrun);
+    PEEC_LAUNCH(k_minv_apply_hi<R>, mgrid, 256, 0, S.minv_hi, nt, b.vs, b.x0, b.x, nrun);
 }
 
 // nrun runs (states d_X[r] = [I; V], sources src[r]) stepped together
