@@ -1027,7 +1027,7 @@ def main():
     ap.add_argument("--config4", default=None,
                     help="only the batched sweep, meshes x frequencies (e.g. 48x64): sweep graphs vs plain FP64 LU")
     ap.add_argument("--config4-plain-stride", type=int, default=1)
-    ap.add_argument("--config4-workers", type=int, default=16, help="host threads (streams) of both config-4 arms")
+    ap.add_argument("--config4-workers", type=int, default=32, help="host threads (streams) of both config-4 arms")
     ap.add_argument("--config3-box", default="2.0,1.0,0.5,80,40,20",
                     help="lx,ly,lz,nx,ny,nz of --config3 (a smaller box for profiling runs)")
     ap.add_argument("--config3-rhs", type=int, default=720)
