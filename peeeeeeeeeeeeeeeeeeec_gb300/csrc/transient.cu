@@ -31,10 +31,11 @@ bool inverse_from_lu_real(const double *lu, const int *perm, int n, double *Minv
 
 struct TransientSystem {
     int ne = 0, nv = 0, nt = 0, scheme = 0;
+    int ldm = 0;  // row stride of M^-1's copies: nt rounded up to 4 (16-byte aligned rows, zero padding)
     double theta = 0.0, dt = 0.0;
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
-    float2 *minv = nullptr;  // M^-1 as float pairs (hi, lo), nt x nt row-major
+    float2 *minv = nullptr;  // M^-1 as float pairs (hi, lo), nt rows of ldm
     float *minv_hi = nullptr;  // their high parts alone, for the correction's FP32 apply
     float2 *Lf = nullptr, *ASf = nullptr;  // Lp (ne x ne) and A S (ne x nv) as float pairs
     long long *piv = nullptr;
@@ -174,6 +175,28 @@ __global__ void k_split_pairs(const double *v, size_t count, float2 *out) {
     out[t] = make_float2(h, (float)(x - (double)h));
 }
 
+// rows x cols FP64 -> float pairs with row stride ld (ld >= cols, the pad
+// columns zero); hi (optional): the high parts alone, same layout
+__global__ void k_split_rows(const double *v, int rows, int cols, int ld, float2 *out, float *hi) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)rows * ld) return;
+    const int r = (int)(t / ld), c = (int)(t % ld);
+    float2 p = make_float2(0.0f, 0.0f);
+    if (c < cols) {
+        const double x = v[(size_t)r * cols + c];
+        const float h = (float)x;
+        p = make_float2(h, (float)(x - (double)h));
+    }
+    out[t] = p;
+    if (hi) hi[t] = p.x;
+}
+
+// the high parts of float pairs
+__global__ void k_pairs_hi(const float2 *in, size_t count, float *out) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) out[t] = in[t].x;
+}
+
 // s += (a.x + a.y)(b.x + b.y) with the high parts two-summed into s.x and
 // every low-order term in s.y (a.y b.y dropped)
 __device__ __forceinline__ void pair_mac(float2 &s, float2 a, float2 b) {
@@ -192,8 +215,10 @@ __device__ __forceinline__ void pair_mac(float2 &s, float2 a, float2 b) {
 // warp (every lane returns the sums).  Each lane reads two elements at a
 // time (16 B) and keeps up to 8 such loads in flight (4 KB per warp and
 // iteration), so the memory system, not each warp's load-to-use latency,
-// sets the pace.  v: run r's vector at v + r ldv (float pairs).
-template <int R>
+// sets the pace.  v: run r's vector at v + r ldv (float pairs); ALIGNED:
+// row and v + r ldv 16-byte aligned and n even (M^-1's padded layout), the
+// vector then read two pairs at a time too.
+template <int R, bool ALIGNED = false>
 __device__ __forceinline__ void row_dot_df(const float2 *row, int n, const float2 *v, size_t ldv, int lane,
                                            double *out) {
     // loads in flight: fewer with more runs, whose products give each load
@@ -221,8 +246,14 @@ __device__ __forceinline__ void row_dot_df(const float2 *row, int n, const float
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const float2 *vr = v + (size_t)r * ldv + j;
-                pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), vr[0]);
-                pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), vr[1]);
+                if constexpr (ALIGNED) {  // both pairs in one 16-byte load
+                    const float4 w = *reinterpret_cast<const float4 *>(vr);
+                    pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), make_float2(w.x, w.y));
+                    pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), make_float2(w.z, w.w));
+                } else {
+                    pair_mac(acc[u & 1][r], make_float2(m[u].x, m[u].y), vr[0]);
+                    pair_mac(acc[u & 1][r], make_float2(m[u].z, m[u].w), vr[1]);
+                }
             }
         }
     }
@@ -304,37 +335,33 @@ __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
 
 // y[r][i] = y0[r][i] (when set) + sum_q Minv[i][q] v[r][q] for every run,
 // one warp per row of M^-1 (streamed once for all runs); vs: v as float
-// pairs (k_split_pairs), [run][nt].
+// pairs (k_split_rows), [run][ldm] with zero padding.
 template <int R>
-__global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, const float2 *vs, const double *y0,
-                                                    double *y, int nrun) {
+__global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, int ldm, const float2 *vs,
+                                                    const double *y0, double *y, int nrun) {
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= nt) return;
     double s[R];
-    row_dot_df<R>(Minv + (size_t)i * nt, nt, vs, nt, lane, s);
+    row_dot_df<R, true>(Minv + (size_t)i * ldm, ldm, vs, ldm, lane, s);
 #pragma unroll
     for (int r = 0; r < R; ++r)
         if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = (y0 ? y0[(size_t)r * nt + i] : 0.0) + s[r];
 }
 
-// out[r] = sum_j row[j] v[r][j].x (j < n) in FP32 (FP64 across the warp),
+// out[r] = sum_j row[j] v[r][j] (j < n) in FP32 (FP64 across the warp),
 // for the correction x = x0 + M^-1 r of the refinement step: r is ~2^-48
 // of b, so the correction needs only a few correct digits, and its FP32
-// apply streams half the bytes (the high parts alone).
+// apply streams half the bytes (the high parts alone).  row and v + r ldv
+// 16-byte aligned, n a multiple of 4 (M^-1's padded layout): matrix and
+// vector are read four elements at a time.
 template <int R>
-__device__ __forceinline__ void row_dot_f32(const float *row, int n, const float2 *v, size_t ldv, int lane,
+__device__ __forceinline__ void row_dot_f32(const float *row, int n, const float *v, size_t ldv, int lane,
                                             double *out) {
     float acc[2][R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[0][r] = acc[1][r] = 0.0f;
-    // 16-byte loads from the first 16-byte aligned element of the row
-    const int head = min(n, (int)((4 - ((reinterpret_cast<uintptr_t>(row) >> 2) & 3)) & 3));
-    if (lane < head) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) acc[0][r] = fmaf(row[lane], v[(size_t)r * ldv + lane].x, acc[0][r]);
-    }
-    const int body = (n - head) / 4;  // float4 groups after the head
-    const float4 *row4 = reinterpret_cast<const float4 *>(row + head);
+    const int body = n / 4;
+    const float4 *row4 = reinterpret_cast<const float4 *>(row);
     constexpr int kDepth = 4;
     int t = lane;
     for (; t + 32 * (kDepth - 1) < body; t += 32 * kDepth) {
@@ -343,61 +370,48 @@ __device__ __forceinline__ void row_dot_f32(const float *row, int n, const float
         for (int u = 0; u < kDepth; ++u) m[u] = __ldcs(row4 + t + 32 * u);
 #pragma unroll
         for (int u = 0; u < kDepth; ++u) {
-            const int j = head + 4 * (t + 32 * u);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float2 *vr = v + (size_t)r * ldv + j;
+                const float4 w = reinterpret_cast<const float4 *>(v + (size_t)r * ldv)[t + 32 * u];
                 float a = acc[u & 1][r];
-                a = fmaf(m[u].x, vr[0].x, a);
-                a = fmaf(m[u].y, vr[1].x, a);
-                a = fmaf(m[u].z, vr[2].x, a);
-                a = fmaf(m[u].w, vr[3].x, a);
+                a = fmaf(m[u].x, w.x, a);
+                a = fmaf(m[u].y, w.y, a);
+                a = fmaf(m[u].z, w.z, a);
+                a = fmaf(m[u].w, w.w, a);
                 acc[u & 1][r] = a;
             }
         }
     }
     for (; t < body; t += 32) {
         const float4 m = __ldcs(row4 + t);
-        const int j = head + 4 * t;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const float2 *vr = v + (size_t)r * ldv + j;
+            const float4 w = reinterpret_cast<const float4 *>(v + (size_t)r * ldv)[t];
             float a = acc[0][r];
-            a = fmaf(m.x, vr[0].x, a);
-            a = fmaf(m.y, vr[1].x, a);
-            a = fmaf(m.z, vr[2].x, a);
-            a = fmaf(m.w, vr[3].x, a);
+            a = fmaf(m.x, w.x, a);
+            a = fmaf(m.y, w.y, a);
+            a = fmaf(m.z, w.z, a);
+            a = fmaf(m.w, w.w, a);
             acc[0][r] = a;
         }
-    }
-    const int tail0 = head + 4 * body;  // up to 3 elements left
-    if (tail0 + lane < n) {
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-            acc[1][r] = fmaf(row[tail0 + lane], v[(size_t)r * ldv + tail0 + lane].x, acc[1][r]);
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) out[r] = warp_sum((double)acc[0][r] + (double)acc[1][r]);
 }
 
-// y[r][i] = y0[r][i] + sum_q Minv_hi[i][q] v[r][q].x for every run (the
-// refinement step's correction), one warp per row.
+// y[r][i] = y0[r][i] + sum_q Minv_hi[i][q] v[r][q] for every run (the
+// refinement step's correction), one warp per row; vh: the high parts of
+// the vector, [run][ldm] with zero padding.
 template <int R>
-__global__ void __launch_bounds__(256) k_minv_apply_hi(const float *Mh, int nt, const float2 *vs, const double *y0,
-                                                       double *y, int nrun) {
+__global__ void __launch_bounds__(256) k_minv_apply_hi(const float *Mh, int nt, int ldm, const float *vh,
+                                                       const double *y0, double *y, int nrun) {
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= nt) return;
     double s[R];
-    row_dot_f32<R>(Mh + (size_t)i * nt, nt, vs, nt, lane, s);
+    row_dot_f32<R>(Mh + (size_t)i * ldm, ldm, vh, ldm, lane, s);
 #pragma unroll
     for (int r = 0; r < R; ++r)
         if (lane == 0 && r < nrun) y[(size_t)r * nt + i] = y0[(size_t)r * nt + i] + s[r];
-}
-
-// high parts of float pairs, for the FP32 apply
-__global__ void k_pairs_hi(const float2 *in, size_t count, float *out) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < count) out[t] = in[t].x;
 }
 
 // res = b - M x for every run (M of k_transient_fill applied from its
@@ -530,16 +544,18 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     }
     dfree(S.lu);
     S.lu = nullptr;
-    S.minv = static_cast<float2 *>(dalloc(sizeof(float2) * nn));
+    S.ldm = (nt + 3) & ~3;
+    const size_t np_ = (size_t)nt * S.ldm;
+    S.minv = static_cast<float2 *>(dalloc(sizeof(float2) * np_));
     if (!S.minv) {
         dfree(inv);
         return -1;
     }
-    PEEC_LAUNCH(k_split_pairs, (unsigned)((nn + 255) / 256), 256, 0, inv, nn, S.minv);
-    dfree(inv);
-    S.minv_hi = static_cast<float *>(dalloc(sizeof(float) * nn));
+    PEEC_LAUNCH(k_split_rows, (unsigned)((np_ + 255) / 256), 256, 0, inv, nt, nt, S.ldm, S.minv, (float *)nullptr);
+    dfree(inv);  // before the high parts' copy: the peak stays at two FP64 matrices
+    S.minv_hi = static_cast<float *>(dalloc(sizeof(float) * np_));
     if (!S.minv_hi) return -1;
-    PEEC_LAUNCH(k_pairs_hi, (unsigned)((nn + 255) / 256), 256, 0, S.minv, nn, S.minv_hi);
+    PEEC_LAUNCH(k_pairs_hi, (unsigned)((np_ + 255) / 256), 256, 0, S.minv, np_, S.minv_hi);
     return launch_ok("transient inverse") && sync("transient inverse") ? 0 : -1;
 }
 
@@ -548,7 +564,8 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
 // (double-float), x = x0 + M^-1 r (FP32: the correction is ~2^-48 of x).
 struct StepBuffers {
     double *x, *rhs, *x0, *res;
-    float2 *vs, *xs, *x0s;
+    float2 *vs, *xs, *x0s;  // vs: [run][ldm] (the applies); xs, x0s: [run][nt]
+    float *vh;              // the high parts of vs
 };
 template <int R>
 static void launch_step(const TransientSystem &S, const StepArgs &A, const StepArgs &Ares, const StepBuffers &b,
@@ -556,12 +573,14 @@ static void launch_step(const TransientSystem &S, const StepArgs &A, const StepA
     const int nt = S.nt;
     PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x, nvec, b.xs);
     PEEC_LAUNCH(k_transient_rhs<R>, grid, 256, 0, A, eb);
-    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.rhs, nvec, b.vs);
-    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, b.vs, (const double *)nullptr, b.x0, nrun);
+    const int ldm = S.ldm;
+    const unsigned pgrid = (unsigned)(((size_t)R * ldm + 255) / 256);
+    PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.rhs, R, nt, ldm, b.vs, (float *)nullptr);
+    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, ldm, b.vs, (const double *)nullptr, b.x0, nrun);
     PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x0, nvec, b.x0s);
     PEEC_LAUNCH(k_transient_resid<R>, grid, 256, 0, Ares, b.rhs, b.res, eb);
-    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.res, nvec, b.vs);
-    PEEC_LAUNCH(k_minv_apply_hi<R>, mgrid, 256, 0, S.minv_hi, nt, b.vs, b.x0, b.x, nrun);
+    PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.res, R, nt, ldm, b.vs, b.vh);
+    PEEC_LAUNCH(k_minv_apply_hi<R>, mgrid, 256, 0, S.minv_hi, nt, ldm, (const float *)b.vh, b.x0, b.x, nrun);
 }
 
 // nrun runs (states d_X[r] = [I; V], sources src[r]) stepped together
@@ -576,8 +595,9 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
     // float pairs of the vectors: of an apply (vs), of the state x (xs) and of
     // x0 (x0s) for the right-hand side and the residual products
-    DBuf<float2> vs((size_t)nt * cap), xs((size_t)nt * cap), x0s((size_t)nt * cap);
-    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p || !xs.p || !x0s.p) return -1;
+    DBuf<float2> vs((size_t)S.ldm * cap), xs((size_t)nt * cap), x0s((size_t)nt * cap);
+    DBuf<float> vh((size_t)S.ldm * cap);
+    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p || !xs.p || !x0s.p || !vh.p) return -1;
     cudaStream_t st = stream();
     if (cap > nrun) {
         for (double *p : {x.p, rhs.p, x0.p, res.p})
@@ -611,7 +631,7 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     Ares.x = x0.p;
     Ares.xs = x0s.p;
     const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
-    const StepBuffers bufs{x.p, rhs.p, x0.p, res.p, vs.p, xs.p, x0s.p};
+    const StepBuffers bufs{x.p, rhs.p, x0.p, res.p, vs.p, xs.p, x0s.p, vh.p};
     const size_t nvec = (size_t)nt * cap;
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
