@@ -32,6 +32,7 @@ bool inverse_from_lu_real(const double *lu, const int *perm, int n, double *Minv
 struct TransientSystem {
     int ne = 0, nv = 0, nt = 0, scheme = 0;
     int ldm = 0;  // row stride of M^-1's copies: nt rounded up to 4 (16-byte aligned rows, zero padding)
+    int lde = 0, ldn = 0;  // row strides of Lf and ASf: ne and nv rounded up to 2 (zero padding)
     double theta = 0.0, dt = 0.0;
     const double *L = nullptr;  // caller's Lp (kept by pointer)
     double *R = nullptr, *F = nullptr, *AS = nullptr, *lu = nullptr, *dinv = nullptr;
@@ -125,7 +126,8 @@ static const int kMaxRuns = 8;
 struct StepArgs {
     const double *R, *F;
     const float2 *Lf, *ASf;  // Lp and A S as float pairs
-    const float2 *xs;        // the states x as float pairs
+    const float2 *xI, *xV;   // the states' I and V parts as float pairs, [run][lde] / [run][ldn]
+    int lde, ldn;
     const int *adj_ptr, *adj;
     int ne, nv, nrun;
     double theta, dt;
@@ -189,6 +191,27 @@ __global__ void k_split_rows(const double *v, int rows, int cols, int ld, float2
     }
     out[t] = p;
     if (hi) hi[t] = p.x;
+}
+
+// the states x [run][nt] (FP64) as float pairs in two padded parts: the
+// currents [run][lde] and the potentials [run][ldn] (pad entries zero), so
+// that Lp and A S rows meet 16-byte aligned vectors
+__global__ void k_split_state(const double *x, int runs, int ne, int nv, int lde, int ldn, float2 *xI, float2 *xV) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, per = lde + ldn;
+    if (t >= runs * per) return;
+    const int r = t / per, c = t % per;
+    const bool cur = c < lde;
+    const int j = cur ? c : c - lde;
+    float2 p = make_float2(0.0f, 0.0f);
+    if (j < (cur ? ne : nv)) {
+        const double v = x[(size_t)r * (ne + nv) + (cur ? j : ne + j)];
+        const float h = (float)v;
+        p = make_float2(h, (float)(v - (double)h));
+    }
+    if (cur)
+        xI[(size_t)r * lde + j] = p;
+    else
+        xV[(size_t)r * ldn + j] = p;
 }
 
 // the high parts of float pairs
@@ -289,9 +312,9 @@ __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
         const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
         if (i >= A.ne) return;
         double s[R], sa[R];
-        row_dot_df<R>(A.Lf + (size_t)i * A.ne, A.ne, A.xs, nt, lane, s);
+        row_dot_df<R, true>(A.Lf + (size_t)i * A.lde, A.lde, A.xI, A.lde, lane, s);
         if (omt != 0.0)
-            row_dot_df<R>(A.ASf + (size_t)i * A.nv, A.nv, A.xs + A.ne, nt, lane, sa);
+            row_dot_df<R, true>(A.ASf + (size_t)i * A.ldn, A.ldn, A.xV, A.ldn, lane, sa);
         else
 #pragma unroll
             for (int r = 0; r < R; ++r) sa[r] = 0.0;
@@ -424,8 +447,8 @@ __global__ void __launch_bounds__(256) k_transient_resid(StepArgs A, const doubl
         const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
         if (i >= A.ne) return;
         double s[R], sa[R];
-        row_dot_df<R>(A.Lf + (size_t)i * A.ne, A.ne, A.xs, nt, lane, s);
-        row_dot_df<R>(A.ASf + (size_t)i * A.nv, A.nv, A.xs + A.ne, nt, lane, sa);
+        row_dot_df<R, true>(A.Lf + (size_t)i * A.lde, A.lde, A.xI, A.lde, lane, s);
+        row_dot_df<R, true>(A.ASf + (size_t)i * A.ldn, A.ldn, A.xV, A.ldn, lane, sa);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const double ls = s[r], as = sa[r];
@@ -522,11 +545,15 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
     }
     // Lp and A S as float pairs for the steps' double-float products; the
     // FP64 A S served the fill only
-    S.Lf = static_cast<float2 *>(dalloc(sizeof(float2) * (size_t)ne * ne));
-    S.ASf = static_cast<float2 *>(dalloc(sizeof(float2) * nas));
+    S.lde = (ne + 1) & ~1;
+    S.ldn = (nv + 1) & ~1;
+    S.Lf = static_cast<float2 *>(dalloc(sizeof(float2) * (size_t)ne * S.lde));
+    S.ASf = static_cast<float2 *>(dalloc(sizeof(float2) * (size_t)ne * S.ldn));
     if (!S.Lf || !S.ASf) return -1;
-    PEEC_LAUNCH(k_split_pairs, (unsigned)(((size_t)ne * ne + 255) / 256), 256, 0, d_L, (size_t)ne * ne, S.Lf);
-    PEEC_LAUNCH(k_split_pairs, (unsigned)((nas + 255) / 256), 256, 0, S.AS, nas, S.ASf);
+    PEEC_LAUNCH(k_split_rows, (unsigned)(((size_t)ne * S.lde + 255) / 256), 256, 0, d_L, ne, ne, S.lde, S.Lf,
+                (float *)nullptr);
+    PEEC_LAUNCH(k_split_rows, (unsigned)(((size_t)ne * S.ldn + 255) / 256), 256, 0, S.AS, ne, nv, S.ldn, S.ASf,
+                (float *)nullptr);
     if (!launch_ok("transient split") || !sync("transient split")) return -1;
     dfree(S.AS);
     S.AS = nullptr;
@@ -564,20 +591,22 @@ static int create(const double *d_L, const double *d_P, const int *d_edges, cons
 // (double-float), x = x0 + M^-1 r (FP32: the correction is ~2^-48 of x).
 struct StepBuffers {
     double *x, *rhs, *x0, *res;
-    float2 *vs, *xs, *x0s;  // vs: [run][ldm] (the applies); xs, x0s: [run][nt]
+    float2 *vs;             // [run][ldm]: the applies' vector
+    float2 *xI, *xV, *x0I, *x0V;  // x's and x0's parts: [run][lde], [run][ldn]
     float *vh;              // the high parts of vs
 };
 template <int R>
 static void launch_step(const TransientSystem &S, const StepArgs &A, const StepArgs &Ares, const StepBuffers &b,
-                        int grid, int eb, int mgrid, unsigned sgrid, size_t nvec, int nrun) {
+                        int grid, int eb, int mgrid, int nrun) {
     const int nt = S.nt;
-    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x, nvec, b.xs);
+    const unsigned xgrid = (unsigned)(((size_t)R * (S.lde + S.ldn) + 255) / 256);
+    PEEC_LAUNCH(k_split_state, xgrid, 256, 0, b.x, R, S.ne, S.nv, S.lde, S.ldn, b.xI, b.xV);
     PEEC_LAUNCH(k_transient_rhs<R>, grid, 256, 0, A, eb);
     const int ldm = S.ldm;
     const unsigned pgrid = (unsigned)(((size_t)R * ldm + 255) / 256);
     PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.rhs, R, nt, ldm, b.vs, (float *)nullptr);
     PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, ldm, b.vs, (const double *)nullptr, b.x0, nrun);
-    PEEC_LAUNCH(k_split_pairs, sgrid, 256, 0, b.x0, nvec, b.x0s);
+    PEEC_LAUNCH(k_split_state, xgrid, 256, 0, b.x0, R, S.ne, S.nv, S.lde, S.ldn, b.x0I, b.x0V);
     PEEC_LAUNCH(k_transient_resid<R>, grid, 256, 0, Ares, b.rhs, b.res, eb);
     PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.res, R, nt, ldm, b.vs, b.vh);
     PEEC_LAUNCH(k_minv_apply_hi<R>, mgrid, 256, 0, S.minv_hi, nt, ldm, (const float *)b.vh, b.x0, b.x, nrun);
@@ -595,9 +624,10 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     DBuf<double> x((size_t)nt * cap), rhs((size_t)nt * cap), x0((size_t)nt * cap), res((size_t)nt * cap);
     // float pairs of the vectors: of an apply (vs), of the state x (xs) and of
     // x0 (x0s) for the right-hand side and the residual products
-    DBuf<float2> vs((size_t)S.ldm * cap), xs((size_t)nt * cap), x0s((size_t)nt * cap);
+    DBuf<float2> vs((size_t)S.ldm * cap), xI((size_t)S.lde * cap), xV((size_t)S.ldn * cap),
+        x0I((size_t)S.lde * cap), x0V((size_t)S.ldn * cap);
     DBuf<float> vh((size_t)S.ldm * cap);
-    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p || !xs.p || !x0s.p || !vh.p) return -1;
+    if (!x.p || !rhs.p || !x0.p || !res.p || !vs.p || !xI.p || !xV.p || !x0I.p || !x0V.p || !vh.p) return -1;
     cudaStream_t st = stream();
     if (cap > nrun) {
         for (double *p : {x.p, rhs.p, x0.p, res.p})
@@ -609,7 +639,10 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     A.F = S.F;
     A.Lf = S.Lf;
     A.ASf = S.ASf;
-    A.xs = xs.p;
+    A.xI = xI.p;
+    A.xV = xV.p;
+    A.lde = S.lde;
+    A.ldn = S.ldn;
     A.adj_ptr = S.adj_ptr;
     A.adj = S.adj;
     A.ne = ne;
@@ -629,18 +662,17 @@ static int run_lightning(const TransientSystem &S, const LightningArgs *src, int
     const int mgrid = (nt + 7) / 8;
     StepArgs Ares = A;  // the residual reads x0 as its state
     Ares.x = x0.p;
-    Ares.xs = x0s.p;
-    const unsigned sgrid = (unsigned)(((size_t)nt * cap + 255) / 256);
-    const StepBuffers bufs{x.p, rhs.p, x0.p, res.p, vs.p, xs.p, x0s.p, vh.p};
-    const size_t nvec = (size_t)nt * cap;
+    Ares.xI = x0I.p;
+    Ares.xV = x0V.p;
+    const StepBuffers bufs{x.p, rhs.p, x0.p, res.p, vs.p, xI.p, xV.p, x0I.p, x0V.p, vh.p};
     for (long long k = 0; k < n_steps; ++k) {
         A.step = step0 + k;
         A.record_row = k - 1;
         switch (cap) {
-            case 1: launch_step<1>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
-            case 2: launch_step<2>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
-            case 4: launch_step<4>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
-            default: launch_step<8>(S, A, Ares, bufs, grid, eb, mgrid, sgrid, nvec, nrun); break;
+            case 1: launch_step<1>(S, A, Ares, bufs, grid, eb, mgrid, nrun); break;
+            case 2: launch_step<2>(S, A, Ares, bufs, grid, eb, mgrid, nrun); break;
+            case 4: launch_step<4>(S, A, Ares, bufs, grid, eb, mgrid, nrun); break;
+            default: launch_step<8>(S, A, Ares, bufs, grid, eb, mgrid, nrun); break;
         }
         if ((k & 255) == 255 && !launch_ok("transient step")) return -1;
     }
