@@ -690,7 +690,7 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
     the meshes largest first on `workers` host threads (one CUDA stream each)
     and time the whole arm on the wall clock: Lp / P assembly included.
       mixed  a sweep plan per mesh (peec_gb300_sweep_*): the autotuner at
-             eight probe frequencies across the band picks the frequency
+             six probe frequencies across the band picks the frequency
              below which the robust graph (BF16x6) runs and the tile width
              of the wide tensor-core updates; the mixed solve recorded into
              CUDA graphs (refinement sweeps past the gate are no-ops) is
@@ -737,7 +737,7 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
         assert plan, "sweep plan"
         t = ds_abi().PeecSweepTuning()
         ms = C.c_double()
-        probes = np.ascontiguousarray(freqs[np.linspace(0, len(freqs) - 1, 8).round().astype(int)])
+        probes = np.ascontiguousarray(freqs[np.linspace(0, len(freqs) - 1, 6).round().astype(int)])
         assert lib.peec_gb300_sweep_tune(plan, probes.ctypes.data_as(ds_abi().c_double_p), len(probes), C.byref(t),
                                          C.byref(ms)) == 0
         fsplit, rob = C.c_double(), ds_abi().PeecSweepTuning()
