@@ -3739,7 +3739,8 @@ __global__ void k_capture_status(const Status *st, const int *werr, const unsign
 
 bool mrhs_split_z(const void *Z, size_t count, void *Zs);
 bool mrhs_sweep(const void *Zs, const void *lu, const int *perm, const double *rs, const double *cs, int n, int nrhs,
-                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be);
+                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be, unsigned long long *be_q,
+                int *done, double tol);
 // from this many right-hand sides on, the refinement sweeps use the blocked
 // many-right-hand-side form (multirhs.cu) instead of the wavefront solve
 // (NR right-hand sides per pass) and the per-row residual
@@ -3977,7 +3978,9 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     // many right-hand sides: Z and x as float pairs for the double-float residual
     const bool many = nrhs >= kManyRhs;
     DBuf<float4> zsp(many ? nn : 0), xsp(many ? nv : 0);
-    if (many && (!zsp.p || !xsp.p)) return -1;
+    DBuf<unsigned long long> be_q(many ? nrhs_ : 0);  // per right-hand side backward errors
+    DBuf<int> rhs_done(many ? nrhs_ : 0);             // right-hand sides at the gate
+    if (many && (!zsp.p || !xsp.p || !be_q.p || !rhs_done.p)) return -1;
     double eta = INFINITY;
     int total_it = 0;
     auto refine = [&]() -> int {
@@ -3987,6 +3990,7 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
         cudaMemsetAsync(werr.p, 0, sizeof(int), stream());
         if (!wave_prepare(a, n, wdinv.p, true)) return -1;
         if (many && !mrhs_split_z(Z, nn, zsp.p)) return -1;
+        if (many) cudaMemsetAsync(rhs_done.p, 0, nrhs_ * sizeof(int), stream());
         if (!cap) tr.mark("refine: set-up");
         // one refinement sweep (FP32 correction solve, FP64 update, FP64
         // residual + backward error): captured once as a CUDA graph and
@@ -3996,7 +4000,8 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
                 // many right-hand sides: blocked substitution with GEMM updates
                 // and the residual in GEMM form (multirhs.cu)
                 cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
-                mrhs_sweep(zsp.p, a, perm.p, rs.p, cs.p, n, nrhs, b, x, r.p, y.p, xsp.p, be.p);
+                mrhs_sweep(zsp.p, a, perm.p, rs.p, cs.p, n, nrhs, b, x, r.p, y.p, xsp.p, be.p, be_q.p, rhs_done.p,
+                           tol);
                 return;
             }
             const int *skip = cap ? done.p : nullptr;
@@ -4082,6 +4087,20 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
         total_it += it > max_iter ? max_iter : it;
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
+        if (many && out != -1) {
+            // the last backward error of every right-hand side (those that
+            // stopped earlier were not recomputed in the last sweeps)
+            std::vector<unsigned long long> hq(nrhs_);
+            if (!be_q.download(hq.data(), nrhs_) || !sync("per right-hand side errors")) return -1;
+            double worst = 0.0;
+            for (unsigned long long bits : hq) {
+                double e;
+                memcpy(&e, &bits, sizeof(e));
+                worst = fmax(worst, e);
+            }
+            eta = worst;
+            out = eta <= tol ? 0 : 1;
+        }
         return out;
     };
     // FGMRES-IR with the BF16x6 factor, the last rung: per right-hand side

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) k_permute_in(const c64 *r, const int *per
 // x[q][i] += Y[i][q] / cs[i] (FP64 accumulation); xs[q][i] = x as float
 // pairs (re.h, re.l, im.h, im.l) for the residual.
 __global__ void __launch_bounds__(256) k_update_out(c64 *x, const c32 *Y, const double *cs, int n, int nrhs,
-                                                    float4 *xs) {
+                                                    float4 *xs, const int *done) {
     __shared__ c32 t[32][33];
     const int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) k_update_out(c64 *x, const c32 *Y, const 
     __syncthreads();
     for (int k = ty; k < 32; k += 8) {
         const int q = q0 + k, i = i0 + tx;
-        if (q < nrhs && i < n) {
+        if (q < nrhs && i < n && !done[q]) {
             const c32 y = t[tx][k];
             const double s = cs[i];
             c64 v = x[(size_t)q * n + i];
@@ -99,7 +99,8 @@ __device__ __forceinline__ c32 msub_c32(c32 c, c32 a, c32 b) {  // c - a b
 }
 
 template <bool LOWER>
-__global__ void __launch_bounds__(256) k_trsm_diag(const c32 *lu, int n, int r0, int nrow, c32 *Y, int nrhs) {
+__global__ void __launch_bounds__(256) k_trsm_diag(const c32 *lu, int n, int r0, int nrow, c32 *Y, int nrhs,
+                                                   const int *done) {
     __shared__ c32 B[kDB][kDB + 1];
     for (int t = threadIdx.x; t < kDB * kDB; t += blockDim.x) {
         const int i = t / kDB, j = t % kDB;
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(256) k_trsm_diag(const c32 *lu, int n, int r0,
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (q >= nrhs) return;
+    if (q >= nrhs || done[q]) return;  // converged right-hand sides keep their solution
     c32 v0 = lane < nrow ? Y[(size_t)(r0 + lane) * nrhs + q] : c32{0.0f, 0.0f};
     c32 v1 = lane + 32 < nrow ? Y[(size_t)(r0 + lane + 32) * nrhs + q] : c32{0.0f, 0.0f};
     if (LOWER) {
@@ -144,10 +145,13 @@ __global__ void __launch_bounds__(256) k_trsm_diag(const c32 *lu, int n, int r0,
 // leading dimension ldb.  64 x 64 output tiles, 256 threads, 4 x 4 outputs
 // per thread, K in chunks of 16 staged in shared memory.
 __global__ void __launch_bounds__(256) k_cgemm_sub(const c32 *A, int lda, const c32 *Bm, c32 *C, int ldb, int M,
-                                                   int NC, int K) {
+                                                   int NC, int K, const int *done) {
     __shared__ c32 As[16][64 + 1];
     __shared__ c32 Bs[16][64];
     const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    // a tile whose 64 right-hand sides have all converged has nothing to do
+    const int qc = n0 + (threadIdx.x & 63);
+    if (__syncthreads_and(qc >= NC || done[qc])) return;
     const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;  // 16 x 16 threads
     c32 acc[4][4];
 #pragma unroll
@@ -363,10 +367,14 @@ struct RTile {  // rows padded by one element: the transposing stores are confli
 };
 
 __global__ void __launch_bounds__(256) k_residual_gemm_df(const float4 *Zs, const float4 *Xs, const c64 *B, int n,
-                                                          int nrhs, c64 *R, unsigned long long *be) {
+                                                          int nrhs, c64 *R, unsigned long long *be,
+                                                          unsigned long long *be_q, const int *done) {
     extern __shared__ __align__(16) unsigned char rsm[];
     RTile &S = *reinterpret_cast<RTile *>(rsm);
     const int i0 = blockIdx.y * 64, q0 = blockIdx.x * 32;
+    // 32 converged right-hand sides: their residuals and errors stand
+    const int qc = q0 + (threadIdx.x & 31);
+    if (__syncthreads_and(qc >= nrhs || done[qc])) return;
     const int tr = threadIdx.x >> 4, tq = threadIdx.x & 15;
     dacc t1[4][2], t2[4][2], t3[4][2];
     float den[4][2];
@@ -420,7 +428,7 @@ __global__ void __launch_bounds__(256) k_residual_gemm_df(const float4 *Zs, cons
         }
         __syncthreads();
     }
-    double worst = 0.0;
+    double worst = 0.0, worst_q[2] = {0.0, 0.0};
 #pragma unroll
     for (int x = 0; x < 4; ++x) {
         const int i = i0 + tr + 16 * x;
@@ -441,9 +449,27 @@ __global__ void __launch_bounds__(256) k_residual_gemm_df(const float4 *Zs, cons
             double eta = d > 0.0 ? res / d : res;
             if (!isfinite(eta)) eta = INFINITY;
             worst = fmax(worst, eta);
+            worst_q[y] = fmax(worst_q[y], eta);
         }
     }
     atomicMax(be, (unsigned long long)__double_as_longlong(worst));
+#pragma unroll
+    for (int y = 0; y < 2; ++y) {  // lanes l and l + 16 share a right-hand side
+        const double w = fmax(worst_q[y], __shfl_xor_sync(0xffffffffu, worst_q[y], 16));
+        const int q = q0 + tq + 16 * y;
+        if ((threadIdx.x & 16) == 0 && q < nrhs) atomicMax(be_q + q, (unsigned long long)__double_as_longlong(w));
+    }
+}
+
+// per right-hand side, before a sweep: the error maxima of the ones still
+// refined start at zero; after it: the ones at the gate are marked done
+__global__ void k_be_reset(unsigned long long *be_q, const int *done, int nrhs) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nrhs && !done[q]) be_q[q] = 0ull;
+}
+__global__ void k_mark_done(const unsigned long long *be_q, int *done, int nrhs, double tol) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nrhs && !done[q] && __longlong_as_double((long long)be_q[q]) <= tol) done[q] = 1;
 }
 
 }  // namespace mrhs
@@ -487,9 +513,14 @@ bool mrhs_split_z(const void *Z, size_t count, void *Zs) {
 // backward block substitution on the FP32 factor lu (diagonal blocks per
 // right-hand side, the rest as GEMMs); x += D_c^-1 Y (FP64) and its float
 // pairs xs; r = b - Z x in double-float from the split Zs (mrhs_split_z) and
-// the backward error into *be (IEEE bits; the caller zeroes it).
+// the backward error into *be (IEEE bits; the caller zeroes it).  Right-
+// hand sides refine until their own backward error reaches tol: done[q]
+// (zeroed by the caller before the first sweep) then stops their updates,
+// and tiles of done right-hand sides are skipped; be_q[q] holds each one's
+// last backward error.
 bool mrhs_sweep(const void *Zs, const void *lu, const int *perm, const double *rs, const double *cs, int n, int nrhs,
-                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be) {
+                const void *b, void *x, void *r, void *Y, void *xs, unsigned long long *be, unsigned long long *be_q,
+                int *done, double tol) {
     using namespace mrhs;
     static const cudaError_t attr = cudaFuncSetAttribute(
         k_residual_gemm_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RTile));
@@ -497,26 +528,29 @@ bool mrhs_sweep(const void *Zs, const void *lu, const int *perm, const double *r
     const c32 *F = (const c32 *)lu;
     c32 *Yt = (c32 *)Y;
     const dim3 tgrid((n + 31) / 32, (nrhs + 31) / 32);
+    const unsigned qgrid = (unsigned)((nrhs + 255) / 256);
+    PEEC_LAUNCH(k_be_reset, qgrid, 256, 0, be_q, (const int *)done, nrhs);
     PEEC_LAUNCH(k_permute_in, tgrid, 256, 0, (const c64 *)r, perm, rs, n, nrhs, Yt);
     const int nb = (n + kDB - 1) / kDB;
     const unsigned dgrid = (unsigned)((nrhs + 7) / 8);
     for (int blk = 0; blk < nb; ++blk) {  // forward: unit lower
         const int r0 = blk * kDB, nrow = min(kDB, n - r0), r1 = r0 + nrow;
-        PEEC_LAUNCH(k_trsm_diag<true>, dgrid, 256, 0, F, n, r0, nrow, Yt, nrhs);
+        PEEC_LAUNCH(k_trsm_diag<true>, dgrid, 256, 0, F, n, r0, nrow, Yt, nrhs, (const int *)done);
         if (r1 < n)
             PEEC_LAUNCH(k_cgemm_sub, dim3((nrhs + 63) / 64, (n - r1 + 63) / 64), 256, 0, F + (size_t)r1 * n + r0, n,
-                        Yt + (size_t)r0 * nrhs, Yt + (size_t)r1 * nrhs, nrhs, n - r1, nrhs, nrow);
+                        Yt + (size_t)r0 * nrhs, Yt + (size_t)r1 * nrhs, nrhs, n - r1, nrhs, nrow, (const int *)done);
     }
     for (int blk = nb - 1; blk >= 0; --blk) {  // backward: upper
         const int r0 = blk * kDB, nrow = min(kDB, n - r0);
-        PEEC_LAUNCH(k_trsm_diag<false>, dgrid, 256, 0, F, n, r0, nrow, Yt, nrhs);
+        PEEC_LAUNCH(k_trsm_diag<false>, dgrid, 256, 0, F, n, r0, nrow, Yt, nrhs, (const int *)done);
         if (r0 > 0)
             PEEC_LAUNCH(k_cgemm_sub, dim3((nrhs + 63) / 64, (r0 + 63) / 64), 256, 0, F + r0, n,
-                        Yt + (size_t)r0 * nrhs, Yt, nrhs, r0, nrhs, nrow);
+                        Yt + (size_t)r0 * nrhs, Yt, nrhs, r0, nrhs, nrow, (const int *)done);
     }
-    PEEC_LAUNCH(k_update_out, tgrid, 256, 0, (c64 *)x, Yt, cs, n, nrhs, (float4 *)xs);
+    PEEC_LAUNCH(k_update_out, tgrid, 256, 0, (c64 *)x, Yt, cs, n, nrhs, (float4 *)xs, (const int *)done);
     PEEC_LAUNCH(k_residual_gemm_df, dim3((nrhs + 31) / 32, (n + 63) / 64), 256, sizeof(RTile), (const float4 *)Zs,
-                (const float4 *)xs, (const c64 *)b, n, nrhs, (c64 *)r, be);
+                (const float4 *)xs, (const c64 *)b, n, nrhs, (c64 *)r, be, be_q, (const int *)done);
+    PEEC_LAUNCH(k_mark_done, qgrid, 256, 0, (const unsigned long long *)be_q, done, nrhs, tol);
     return launch_ok("many-right-hand-side sweep");
 }
 
