@@ -695,7 +695,8 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
              of the wide tensor-core updates; the mixed solve recorded into
              CUDA graphs (refinement sweeps past the gate are no-ops) is
              replayed for every frequency;
-             systems above the gate are solved again by the precision
+             systems the fast graph leaves above the gate are replayed
+             with the robust graph, then solved again by the precision
              ladder, then the FP64 LU with FP64 refinement
       plain  per system: MNA fill, FP64 complex LU, solve, FP64 iterative
              refinement with that factor to the same gate (every
@@ -804,6 +805,7 @@ def config4(lib, n_meshes=48, n_freqs=64, nrhs=4, workers=4, plain_stride=1):
         if arm == "mixed":
             fb = np.concatenate([r["fb"] for r in res])
             out[arm]["graph_replays_at_gate"] = int(np.sum(fb == 0))
+            out[arm]["robust_graph_after_fast"] = int(np.sum(fb == 3))
             out[arm]["fallback_mixed_ladder"] = int(np.sum(fb == 1))
             out[arm]["fallback_fp64"] = int(np.sum(fb == 2))
             out[arm]["tuning"] = {str(r["n"]): {"split_terms": r["tuning"][0], "sweeps": r["tuning"][1],

@@ -106,14 +106,12 @@ int peec_gb300_complex_lu_factor_device(Complex *d_a, size_t n, double pivot_tol
  * scratch (status, scale reduction, panel exchange slots) lives in one
  * 256 KiB static device array that every GPU loading the library keeps until
  * the process exits; n is limited to 50000 (larger n returns -1 with a
- * message, see peec_gb300_last_error).  The first call on each device looks
- * up the array's device address with that device current: make that first
- * call before any stream capture.  Every call reuses the same array and
+ * message, see peec_gb300_last_error).  Each call looks up the array's
+ * device address on the current device.  Every call reuses the same array and
  * clears it on entry, so calls that overlap on the GPU (for instance from two
  * host threads) race with each other: serialise them.  The call synchronises
  * the library stream before returning (it reads the matrix scale and the
- * status back).  The device address is looked up once per device and kept,
- * so do not keep using the library on a device after cudaDeviceReset. */
+ * status back). */
 int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double pivot_tolerance,
                                         long long *d_piv, int *d_perm,
                                         double *matrix_scale, int *failed_column);
@@ -301,12 +299,13 @@ void *peec_gb300_sweep_create(const double *d_L, const double *d_P, const int *d
 int peec_gb300_sweep_tune(void *plan, const double *probe_frequencies, size_t n_probe,
                           PeecSweepTuning *chosen, double *ms_per_system);
 /* Solves every frequency: d_X (device) [n_freq][nrhs][Ne + Nv].  A system
- * whose backward error after the recorded sweeps is above tol is solved
- * again outside the graph (mixed solve with its precision ladder; then the
+ * that the fast graph leaves above tol is replayed with the robust graph
+ * (recorded then if the tuner did not need it); one still above tol is solved
+ * again outside the graphs (mixed solve with its precision ladder; then the
  * FP64 LU with FP64 refinement).  backward_error[f] (host) is its final
- * componentwise backward error; fallback[f] 0 graph, 1 mixed ladder, 2 FP64.
- * Returns 0 when every system reached tol, 1 when some did not, -1 on
- * errors. */
+ * componentwise backward error; fallback[f] 0 graph, 3 robust graph after
+ * the fast one, 1 mixed ladder, 2 FP64.  Returns 0 when every system reached
+ * tol, 1 when some did not, -1 on errors. */
 int peec_gb300_sweep_run(void *plan, const double *frequencies, size_t n_freq, double tol,
                          Complex *d_X, double *backward_error, int *fallback);
 int peec_gb300_sweep_tuning(void *plan, PeecSweepTuning *tuning);

@@ -2034,20 +2034,35 @@ __device__ bool wave_block(const WaveArgs<T> &A, int blk, int c0, int nr, unsign
     return true;
 }
 
+// Tasks in ticket order: per chunk of NR right-hand sides, the forward
+// blocks 0..nb-1, then the backward blocks nb-1..0.  A CTA takes the next
+// ticket from a counter when it is free and every task waits only on tasks
+// of lower tickets, all taken by CTAs already running, so the solve needs no
+// co-residency: it is an ordinary launch, which starts on whatever SMs are
+// free (under concurrent streams a cooperative launch waits until the whole
+// grid fits at once).
 template <class T, int NR>
 __global__ void __launch_bounds__(256) k_trsv_wave(WaveArgs<T> A) {
     if (A.skip && *A.skip) return;  // uniform: written before the launch
     extern __shared__ __align__(16) unsigned char wave_smem[];
     WaveSmem<T, NR> &S = *reinterpret_cast<WaveSmem<T, NR> *>(wave_smem);
-    __shared__ int s_ok;
+    __shared__ int s_ok, s_task;
     const int nb = A.nb;
-    for (int c0 = 0, chunk = 0; c0 < A.nrhs; c0 += NR, ++chunk) {
+    const int nchunks = (A.nrhs + NR - 1) / NR, total = nchunks * 2 * nb;
+    unsigned *ticket = A.flags + (size_t)nchunks * 2 * nb;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (int)atomicAdd(ticket, 1u);
+        __syncthreads();
+        const int t = s_task;
+        __syncthreads();  // every thread has read s_task before the next ticket
+        if (t >= total) return;
+        const int chunk = t / (2 * nb), u = t - chunk * 2 * nb, c0 = chunk * NR;
         const int nr = min(NR, A.nrhs - c0);
         unsigned *ff = A.flags + (size_t)chunk * 2 * nb, *bf = ff + nb;
-        for (int blk = blockIdx.x; blk < nb; blk += gridDim.x)
-            if (!wave_block<T, NR, true>(A, blk, c0, nr, ff, S, &s_ok)) return;
-        for (int q = blockIdx.x; q < nb; q += gridDim.x) {
-            const int blk = nb - 1 - q;
+        if (u < nb) {
+            if (!wave_block<T, NR, true>(A, u, c0, nr, ff, S, &s_ok)) return;
+        } else {
+            const int blk = 2 * nb - 1 - u;
             // the last block's backward step also needs the whole forward pass
             if (blk == nb - 1) {
                 if (threadIdx.x == 0) s_ok = wave_wait(ff + nb - 1, A.error);
@@ -2064,11 +2079,12 @@ static constexpr int wave_nr() {  // right-hand sides per wave: 8-byte scalars 4
     return sizeof(T) == 8 ? 4 : 2;
 }
 
-// Flag words of one wavefront solve of n unknowns and nrhs right-hand sides.
+// Flag words of one wavefront solve of n unknowns and nrhs right-hand sides
+// (one per block and direction, then the ticket counter).
 template <class T>
 static size_t wave_flag_count(int n, int nrhs) {
     int nb = (n + kRB - 1) / kRB;
-    return (size_t)((nrhs + wave_nr<T>() - 1) / wave_nr<T>()) * 2 * nb;
+    return (size_t)((nrhs + wave_nr<T>() - 1) / wave_nr<T>()) * 2 * nb + 1;
 }
 
 // Elements of the diagonal-block inverses of an n x n factor.
@@ -2126,13 +2142,11 @@ static bool wave_solve(WaveArgs<T> A) {
         return false;
     }
     A.nb = (A.n + kRB - 1) / kRB;
-    int grid = std::min(A.nb, capacity);
+    const int tasks = (A.nrhs + NR - 1) / NR * 2 * A.nb;
+    const int grid = std::min(tasks, capacity);
     cudaMemsetAsync(A.flags, 0, wave_flag_count<T>(A.n, A.nrhs) * sizeof(unsigned), stream());
-    void *args[] = {&A};
-    note_launch();
-    return cuda_ok(cudaLaunchCooperativeKernel((const void *)k_trsv_wave<T, NR>, dim3(grid), dim3(256), args,
-                                               sizeof(WaveSmem<T, NR>), stream()),
-                   "triangular solve launch");
+    PEEC_LAUNCH((k_trsv_wave<T, NR>), grid, 256, sizeof(WaveSmem<T, NR>), A);
+    return launch_ok("triangular solve launch");
 }
 
 
@@ -3027,24 +3041,17 @@ static const size_t kNoAllocScratchBytes = 256 * 1024;
 static const size_t kNoAllocMaxN = 50000;  // the permutation kernel keeps n ints in shared memory
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-static std::mutex g_noalloc_mu;
-static void *g_noalloc_ptr[64];  // device address of g_noalloc_scratch, per device ordinal
-
-// Host-side name of the array is not a device address: resolve it once per
-// device with that device current.
-static unsigned char *noalloc_scratch(int dev) {
-    if (dev < 0 || dev >= 64) return nullptr;
-    std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            set_error("cudaGetSymbolAddress of the static LU scratch failed: %s", cudaGetErrorString(e));
-            return nullptr;
-        }
-        g_noalloc_ptr[dev] = p;
+// Host-side name of the array is not a device address: resolve it on every
+// call with the caller's device current (no allocation, and no address kept
+// across a device reset or a reload of the module).
+static unsigned char *noalloc_scratch() {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        set_error("cudaGetSymbolAddress of the static LU scratch failed: %s", cudaGetErrorString(e));
+        return nullptr;
     }
-    return (unsigned char *)g_noalloc_ptr[dev];
+    return (unsigned char *)p;
 }
 
 }  // namespace peec
@@ -3071,7 +3078,7 @@ extern "C" int peec_gb300_lu_factor_device_noalloc(double *d_a, size_t n, double
                   kNoAllocScratchBytes);
         return -1;
     }
-    unsigned char *base = noalloc_scratch(dev);
+    unsigned char *base = noalloc_scratch();
     if (!base) return -1;
     Status *st = (Status *)base;
     unsigned long long *mx = (unsigned long long *)(base + off_mx);

@@ -10,10 +10,11 @@
 // device memory and are copied in before each replay, so one graph serves
 // the whole sweep.  Different meshes run their plans from different host
 // threads (each thread has its own stream), so their graphs overlap on the
-// device.  Systems whose backward error is above the tolerance after the
-// fixed sweeps are solved again outside the graph: by the mixed solve from
-// its BF16x6 rung (then FGMRES-IR), then, if that does not reach the gate,
-// by the FP64 LU with FP64 refinement.
+// device.  Systems that the fast graph leaves above the tolerance are
+// replayed with the robust graph; those still above it are solved again
+// outside the graphs: by the mixed solve from its BF16x6 rung (then
+// FGMRES-IR), then, if that does not reach the gate, by the FP64 LU with
+// FP64 refinement.
 //
 // A plan holds two graphs: a fast one (split-BF16x3 products, up to 10
 // refinement sweeps) and a robust one (BF16x6, up to 16) for the
@@ -112,9 +113,10 @@ static bool ensure_params(SweepPlan &p, size_t n_freq) {
 }
 
 // Replays of the graph for freqs[0..n_freq): X, eta bits and status per
-// frequency into device arrays (copied after each replay).
+// frequency into device arrays (copied after each replay).  The robust graph
+// runs below the split frequency, or for every frequency with all_robust.
 static bool replay(SweepPlan &p, const double *freqs, size_t n_freq, Complex *d_X, unsigned long long *d_eta_all,
-                   int *d_status_all) {
+                   int *d_status_all, bool all_robust = false) {
     if (!ensure_params(p, n_freq)) return false;
     for (size_t f = 0; f < n_freq; ++f) {
         const double w = 2.0 * M_PI * freqs[f];
@@ -123,7 +125,7 @@ static bool replay(SweepPlan &p, const double *freqs, size_t n_freq, Complex *d_
     }
     const size_t xs = (size_t)p.n * p.nrhs;
     for (size_t f = 0; f < n_freq; ++f) {
-        const bool robust = p.exec_robust && freqs[f] < p.f_split;
+        const bool robust = p.exec_robust && (all_robust || freqs[f] < p.f_split);
         if (!cuda_ok(cudaMemcpyAsync(p.d_params, p.h_params + 2 * f, 2 * sizeof(double), cudaMemcpyHostToDevice,
                                      stream()),
                      "sweep: parameters") ||
@@ -351,16 +353,65 @@ int peec_gb300_sweep_run(void *plan, const double *frequencies, size_t n_freq, d
     cudaMemcpyAsync(sb.data(), st_all.p, n_freq * sizeof(int), cudaMemcpyDeviceToHost, stream());
     if (!sync("sweep: results")) return -1;
     const size_t xs = (size_t)p.n * p.nrhs;
-    int worst = 0;
-    for (size_t f = 0; f < n_freq; ++f) {
+    auto missed = [&](size_t f) {
         double eta;
         memcpy(&eta, &eb[f], sizeof(eta));
-        int fb = 0;
+        return sb[f] != 0 || !(eta <= tol);
+    };
+    for (size_t f = 0; f < n_freq; ++f)
         if (sb[f] == 6) {
             set_error("sweep: a triangular-solve wait timed out in the graph");
             return -1;
         }
-        if (sb[f] != 0 || !(eta <= tol)) {
+    // systems the fast graph left above tol: the robust graph first (recorded
+    // here if the tuner did not need it), replayed for all of them
+    std::vector<double> rf;
+    std::vector<size_t> ri;
+    for (size_t f = 0; f < n_freq; ++f)
+        if (missed(f) && !(p.exec_robust && frequencies[f] < p.f_split)) {
+            rf.push_back(frequencies[f]);
+            ri.push_back(f);
+        }
+    std::vector<int> rescued(n_freq, 0);
+    if (!ri.empty()) {
+        if (!p.exec_robust) {
+            p.robust.tile_bn = p.tuning.tile_bn;
+            if (!record(p, p.robust, p.exec_robust, p.robust_launches)) return -1;
+        }
+        const size_t m = ri.size();
+        DBuf<Complex> X2(m * xs);
+        DBuf<unsigned long long> eta2(m);
+        DBuf<int> st2(m);
+        if (!X2.p || !eta2.p || !st2.p || !replay(p, rf.data(), m, X2.p, eta2.p, st2.p, true)) return -1;
+        std::vector<unsigned long long> e2(m);
+        std::vector<int> s2(m);
+        cudaMemcpyAsync(e2.data(), eta2.p, m * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream());
+        cudaMemcpyAsync(s2.data(), st2.p, m * sizeof(int), cudaMemcpyDeviceToHost, stream());
+        if (!sync("sweep: robust replays")) return -1;
+        for (size_t j = 0; j < m; ++j) {
+            double eta;
+            memcpy(&eta, &e2[j], sizeof(eta));
+            if (s2[j] == 6) {
+                set_error("sweep: a triangular-solve wait timed out in the graph");
+                return -1;
+            }
+            if (s2[j] != 0 || !(eta <= tol)) continue;
+            const size_t f = ri[j];
+            if (!cuda_ok(cudaMemcpyAsync(d_X + f * xs, X2.p + j * xs, xs * sizeof(Complex), cudaMemcpyDeviceToDevice,
+                                         stream()),
+                         "sweep: solution copy"))
+                return -1;
+            eb[f] = e2[j];
+            sb[f] = 0;
+            rescued[f] = 1;
+        }
+    }
+    int worst = 0;
+    for (size_t f = 0; f < n_freq; ++f) {
+        double eta;
+        memcpy(&eta, &eb[f], sizeof(eta));
+        int fb = rescued[f] ? 3 : 0;
+        if (missed(f)) {
             const int s = solve_fallback(p, frequencies[f], tol, d_X + f * xs, &eta, &fb);
             if (s < 0) return -1;
             worst = std::max(worst, s);
