@@ -228,7 +228,8 @@ int peec_gb300_complex_solve_mixed_device(const Complex *d_Z, size_t n, const Co
  * factorisation on this host thread. */
 int peec_gb300_mixed_split_terms(void);
 /* Inner FGMRES steps of the last mixed solve on this host thread (0 unless
- * refinement from the BF16x6 factor stalled and FGMRES-IR ran). */
+ * refinement from the BF16x6 factor stalled and FGMRES-IR ran); one step
+ * serves up to 8 right-hand sides in lockstep. */
 int peec_gb300_mixed_gmres_iterations(void);
 /* FP64 iterative refinement of d_x (in: a solution, out: the refined one)
  * with an FP64 factor of Z from peec_gb300_complex_lu_factor_device:

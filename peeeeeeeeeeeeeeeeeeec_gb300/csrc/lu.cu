@@ -3570,31 +3570,53 @@ __global__ void k_add_cplx(cplx *x, const cplx *dx, size_t count) {
 // the FP32 factor applied in FP32 (Arioli and Duff, "Using FGMRES to obtain
 // backward stability in mixed precision", ETNA 33, 2009) ----
 
-// y = D_r^-1 Z v in FP64, one warp per row
-__global__ void k_zmv_scaled(const cplx *Z, const cplx *v, const double *rs, int n, cplx *y) {
+// The right-hand sides of one FGMRES chunk run in lockstep: every vector
+// argument below is nq column blocks of n (block q at offset q n), nq <=
+// kGmresChunk, and each block sees the arithmetic of a solve of its own.
+static const int kGmresChunk = 8;
+struct GmresScalars {
+    double v[kGmresChunk];
+};
+struct GmresCounts {
+    int v[kGmresChunk];
+};
+
+// y_q = D_r^-1 Z v_q in FP64, one warp per row (Z read once for all q)
+__global__ void k_zmv_scaled(const cplx *Z, const cplx *v, const double *rs, int n, int nq, cplx *y) {
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n) return;
     const cplx *row = Z + (size_t)warp * n;
-    double yr = 0.0, yi = 0.0;
+    double yr[kGmresChunk], yi[kGmresChunk];
+#pragma unroll
+    for (int q = 0; q < kGmresChunk; ++q) yr[q] = yi[q] = 0.0;
     for (int j = lane; j < n; j += 32) {
-        const cplx z = row[j], u = v[j];
-        yr = fma(z.re, u.re, yr);
-        yr = fma(-z.im, u.im, yr);
-        yi = fma(z.re, u.im, yi);
-        yi = fma(z.im, u.re, yi);
+        const cplx z = row[j];
+#pragma unroll
+        for (int q = 0; q < kGmresChunk; ++q) {
+            if (q >= nq) break;
+            const cplx u = v[(size_t)q * n + j];
+            yr[q] = fma(z.re, u.re, yr[q]);
+            yr[q] = fma(-z.im, u.im, yr[q]);
+            yi[q] = fma(z.re, u.im, yi[q]);
+            yi[q] = fma(z.im, u.re, yi[q]);
+        }
     }
-    yr = warp_sum(yr);
-    yi = warp_sum(yi);
-    if (lane == 0) y[warp] = cplx{yr / rs[warp], yi / rs[warp]};
+#pragma unroll
+    for (int q = 0; q < kGmresChunk; ++q) {
+        if (q >= nq) break;
+        const double a = warp_sum(yr[q]), c = warp_sum(yi[q]);
+        if (lane == 0) y[(size_t)q * n + warp] = cplx{a / rs[warp], c / rs[warp]};
+    }
 }
 
-// y = P v rounded to FP32 (v already row-scaled)
+// y_q = P v_q rounded to FP32 (v already row-scaled); grid.y = q
 __global__ void k_perm_f32(const cplx *v, const int *perm, int n, cplxf *y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const cplx u = v[perm[i]];
-    y[i] = cplxf{(float)u.re, (float)u.im};
+    const size_t o = (size_t)blockIdx.y * n;
+    const cplx u = v[o + perm[i]];
+    y[o + i] = cplxf{(float)u.re, (float)u.im};
 }
 
 // v = D_r^-1 r
@@ -3603,20 +3625,23 @@ __global__ void k_scale_rows(const cplx *r, const double *rs, int n, cplx *v) {
     if (i < n) v[i] = cplx{r[i].re / rs[i], r[i].im / rs[i]};
 }
 
-// w = D_c^-1 y: the FP32 correction solve's result in FP64
+// w_q = D_c^-1 y_q: the FP32 correction solve's result in FP64; grid.y = q
 __global__ void k_mix_out(const cplxf *y, const double *cs, int n, cplx *w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) w[i] = cplx{(double)y[i].re / cs[i], (double)y[i].im / cs[i]};
+    if (i >= n) return;
+    const size_t o = (size_t)blockIdx.y * n;
+    w[o + i] = cplx{(double)y[o + i].re / cs[i], (double)y[o + i].im / cs[i]};
 }
 
-// h[j] = v_j^H w for j < k (V column-major, leading dimension n), one CTA per
-// j, a fixed reduction order
-__global__ void __launch_bounds__(256) k_gs_dots(const cplx *V, int n, const cplx *w, cplx *h) {
+// h_q[j] = v_{j,q}^H w_q for j < k (basis vector j of block q at V + (j nq +
+// q) n), one CTA per (j, q), a fixed reduction order; h_q at h + q ld
+__global__ void __launch_bounds__(256) k_gs_dots(const cplx *V, int n, int nq, const cplx *w, cplx *h, int ld) {
     __shared__ double sr[8], si[8];
-    const cplx *v = V + (size_t)blockIdx.x * n;
+    const int q = blockIdx.y;
+    const cplx *v = V + ((size_t)blockIdx.x * nq + q) * n, *wq = w + (size_t)q * n;
     double re = 0.0, im = 0.0;
     for (int i = threadIdx.x; i < n; i += 256) {
-        const cplx a = v[i], b = w[i];
+        const cplx a = v[i], b = wq[i];
         re = fma(a.re, b.re, re);
         re = fma(a.im, b.im, re);
         im = fma(a.re, b.im, im);
@@ -3631,59 +3656,68 @@ __global__ void __launch_bounds__(256) k_gs_dots(const cplx *V, int n, const cpl
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0.0, b = 0.0;
-        for (int q = 0; q < 8; ++q) {
-            a += sr[q];
-            b += si[q];
+        for (int t = 0; t < 8; ++t) {
+            a += sr[t];
+            b += si[t];
         }
-        h[blockIdx.x] = cplx{a, b};
+        h[(size_t)q * ld + blockIdx.x] = cplx{a, b};
     }
 }
 
-// w -= sum_{j<k} h_j v_j
-__global__ void k_gs_update(const cplx *V, int n, int k, const cplx *h, cplx *w) {
+// w_q -= sum_{j<k} h_q[j] v_{j,q}; grid.y = q
+__global__ void k_gs_update(const cplx *V, int n, int nq, int k, const cplx *h, int ld, cplx *w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    cplx s = w[i];
+    const int q = blockIdx.y;
+    const cplx *hq = h + (size_t)q * ld;
+    cplx s = w[(size_t)q * n + i];
     for (int j = 0; j < k; ++j) {
-        const cplx hj = h[j], v = V[(size_t)j * n + i];
+        const cplx hj = hq[j], v = V[((size_t)j * nq + q) * n + i];
         s.re -= hj.re * v.re - hj.im * v.im;
         s.im -= hj.re * v.im + hj.im * v.re;
     }
-    w[i] = s;
+    w[(size_t)q * n + i] = s;
 }
 
-// out = ||w||_2, one CTA of 1024 threads
+// out[q] = ||w_q||_2, one CTA of 1024 threads per q
 __global__ void __launch_bounds__(1024) k_norm2(const cplx *w, int n, double *out) {
     __shared__ double part[32];
+    const cplx *wq = w + (size_t)blockIdx.x * n;
     double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += 1024) s = fma(w[i].re, w[i].re, fma(w[i].im, w[i].im, s));
+    for (int i = threadIdx.x; i < n; i += 1024) s = fma(wq[i].re, wq[i].re, fma(wq[i].im, wq[i].im, s));
     s = warp_sum(s);
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int q = 0; q < 32; ++q) t += part[q];
-        *out = sqrt(t);
+        out[blockIdx.x] = sqrt(t);
     }
 }
 
-// v = w * scale
-__global__ void k_cscale(const cplx *w, int n, double scale, cplx *v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = cplx{w[i].re * scale, w[i].im * scale};
-}
-
-// x += sum_{j<k} y_j z_j
-__global__ void k_gmres_update(const cplx *V, int n, int k, const cplx *y, cplx *x) {
+// v_q = w_q * scale_q; grid.y = q
+__global__ void k_cscale(const cplx *w, int n, GmresScalars scale, cplx *v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    cplx s = x[i];
-    for (int j = 0; j < k; ++j) {
-        const cplx a = y[j], v = V[(size_t)j * n + i];
+    const size_t o = (size_t)blockIdx.y * n;
+    const double sc = scale.v[blockIdx.y];
+    v[o + i] = cplx{w[o + i].re * sc, w[o + i].im * sc};
+}
+
+// x_q += sum_{j<k_q} y_q[j] z_{j,q} (z_{j,q} at Zk + (j nq + q) n, y_q at y + q
+// ld); grid.y = q
+__global__ void k_gmres_update(const cplx *Zk, int n, int nq, GmresCounts k, const cplx *y, int ld, cplx *x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int q = blockIdx.y;
+    const cplx *yq = y + (size_t)q * ld;
+    cplx s = x[(size_t)q * n + i];
+    for (int j = 0; j < k.v[q]; ++j) {
+        const cplx a = yq[j], v = Zk[((size_t)j * nq + q) * n + i];
         s.re += a.re * v.re - a.im * v.im;
         s.im += a.re * v.im + a.im * v.re;
     }
-    x[i] = s;
+    x[(size_t)q * n + i] = s;
 }
 
 struct MixedTiming {
@@ -4116,33 +4150,24 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
     // FP32 factor in FP32 (z_k = D_c^-1 U^-1 L^-1 P v_k, kept for the update
     // d = Z_k y since the preconditioner is not exactly linear); classical
     // Gram-Schmidt twice, Givens rotations on the host; 1e-6 relative
-    // residual or 40 steps per inner solve.  Stops at the gate, after 10
-    // outer steps, or when the backward error no longer halves.  0 at the
-    // gate, 1 when not, -1 on errors.
+    // residual or 40 steps per inner solve.  A right-hand side stops at the
+    // gate, after 10 outer steps, or when its backward error no longer
+    // halves.  Up to kGmresChunk right-hand sides run in lockstep: one
+    // triangular solve, one pass over Z and one host round trip per step
+    // serve them all, each with its own Krylov basis, rotations and stopping
+    // (a finished one rides along on zero vectors).  0 at the gate, 1 when
+    // not, -1 on errors.
     int gmres_total = 0;
     auto gmres_ir = [&]() -> int {
-        constexpr int m = 40;
-        DBuf<cplx> V((size_t)(m + 1) * n), Zk((size_t)m * n), w(n), hd(2 * (m + 1)), yd(m);
-        DBuf<double> nrm(1);
-        if (!V.p || !Zk.p || !w.p || !hd.p || !yd.p || !nrm.p) return -1;
+        constexpr int m = 40, ld = m + 1;
+        const int Q = std::min(nrhs, kGmresChunk);
+        DBuf<cplx> V((size_t)(m + 1) * Q * n), Zk((size_t)m * Q * n), w((size_t)Q * n), hd((size_t)2 * Q * ld),
+            yd((size_t)Q * ld);
+        DBuf<double> nrm(Q);
+        DBuf<unsigned long long> beq(Q);
+        if (!V.p || !Zk.p || !w.p || !hd.p || !yd.p || !nrm.p || !beq.p) return -1;
         const unsigned gn = (unsigned)((n + 255) / 256), gw = (unsigned)(((size_t)n * 32 + 255) / 256);
-        // z = D_c^-1 U^-1 L^-1 P v in FP32, returned in FP64
-        auto precondition = [&](const cplx *v, cplx *z) -> bool {
-            PEEC_LAUNCH(k_perm_f32, gn, 256, 0, v, perm.p, n, y.p);
-            WaveArgs<cplxf> W{};
-            W.lu = a;
-            W.dinv = wdinv.p;
-            W.n = n;
-            W.nrhs = 1;
-            W.b = y.p;
-            W.x = y.p;
-            W.flags = wflags.p;
-            W.error = werr.p;
-            W.subst = 1;
-            if (!wave_solve(W)) return false;
-            PEEC_LAUNCH(k_mix_out, gn, 256, 0, y.p, cs.p, n, z);
-            return true;
-        };
+        using zc = std::complex<double>;
         auto host_sync = [&](const char *what) -> bool {
             int hw = 0;
             cudaMemcpyAsync(&hw, werr.p, sizeof(hw), cudaMemcpyDeviceToHost, stream());
@@ -4151,92 +4176,149 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             return hw == 0;
         };
         double eta_max = 0.0;
-        for (int q = 0; q < nrhs; ++q) {
-            cplx *xq = x + (size_t)q * n;
-            const cplx *bq = b + (size_t)q * n;
-            cudaMemsetAsync(xq, 0, (size_t)n * sizeof(cplx), stream());
-            double eta_q = INFINITY, prev = INFINITY;
+        for (int q0 = 0; q0 < nrhs; q0 += Q) {
+            const int nq = std::min(Q, nrhs - q0);
+            const dim3 gq(gn, (unsigned)nq);
+            // z_q = D_c^-1 U^-1 L^-1 P v_q in FP32, returned in FP64, for all q at once
+            auto precondition = [&](const cplx *v, cplx *z) -> bool {
+                PEEC_LAUNCH(k_perm_f32, gq, 256, 0, v, perm.p, n, y.p);
+                WaveArgs<cplxf> W{};
+                W.lu = a;
+                W.dinv = wdinv.p;
+                W.n = n;
+                W.nrhs = nq;
+                W.b = y.p;
+                W.x = y.p;
+                W.flags = wflags.p;
+                W.error = werr.p;
+                W.subst = 1;
+                if (!wave_solve(W)) return false;
+                PEEC_LAUNCH(k_mix_out, gq, 256, 0, y.p, cs.p, n, z);
+                return true;
+            };
+            cplx *xc = x + (size_t)q0 * n;
+            const cplx *bc = b + (size_t)q0 * n;
+            cudaMemsetAsync(xc, 0, (size_t)nq * n * sizeof(cplx), stream());
+            std::vector<double> eta_q(nq, INFINITY), prev(nq, INFINITY), beta(nq), hn(nq);
+            std::vector<unsigned long long> hb(nq);
+            std::vector<char> live(nq, 1);  // still iterating (outer)
             for (int outer = 0; outer < 10; ++outer) {
-                cudaMemsetAsync(be.p, 0, sizeof(unsigned long long), stream());
-                PEEC_LAUNCH(k_abs_x, gn, 256, 0, xq, (size_t)n, absx.p);
-                PEEC_LAUNCH(k_residual, gw, 256, 0, Z, absZ.p, xq, absx.p, bq, n, 1, r.p, be.p, (const int *)nullptr);
-                PEEC_LAUNCH(k_scale_rows, gn, 256, 0, r.p, rs.p, n, V.p);
-                PEEC_LAUNCH(k_norm2, 1, 1024, 0, V.p, n, nrm.p);
-                unsigned long long hb = 0;
-                double beta = 0.0;
-                cudaMemcpyAsync(&hb, be.p, sizeof(hb), cudaMemcpyDeviceToHost, stream());
-                cudaMemcpyAsync(&beta, nrm.p, sizeof(beta), cudaMemcpyDeviceToHost, stream());
+                cudaMemsetAsync(beq.p, 0, nq * sizeof(unsigned long long), stream());
+                for (int q = 0; q < nq; ++q) {
+                    const size_t o = (size_t)q * n;
+                    PEEC_LAUNCH(k_abs_x, gn, 256, 0, xc + o, (size_t)n, absx.p + o);
+                    PEEC_LAUNCH(k_residual, gw, 256, 0, Z, absZ.p, xc + o, absx.p + o, bc + o, n, 1, r.p + o,
+                                beq.p + q, (const int *)nullptr);
+                    PEEC_LAUNCH(k_scale_rows, gn, 256, 0, r.p + o, rs.p, n, V.p + o);
+                }
+                PEEC_LAUNCH(k_norm2, nq, 1024, 0, V.p, n, nrm.p);
+                cudaMemcpyAsync(hb.data(), beq.p, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream());
+                cudaMemcpyAsync(beta.data(), nrm.p, nq * sizeof(double), cudaMemcpyDeviceToHost, stream());
                 if (!host_sync("GMRES-IR residual")) return -1;
-                memcpy(&eta_q, &hb, sizeof(eta_q));
-                if (eta_q <= tol || !isfinite(eta_q) || eta_q > 0.5 * prev) break;
-                prev = eta_q;
-                if (!(beta > 0.0) || !isfinite(beta)) break;
-                PEEC_LAUNCH(k_cscale, gn, 256, 0, V.p, n, 1.0 / beta, V.p);
-                using zc = std::complex<double>;
-                std::vector<zc> H((size_t)(m + 1) * m), g(m + 1, zc(0.0)), sn(m);
-                std::vector<double> c(m);
-                std::vector<cplx> hh(2 * (m + 1));
-                g[0] = beta;
-                int kk = 0;
-                for (int k = 0; k < m; ++k) {
-                    cplx *zk = Zk.p + (size_t)k * n;
-                    if (!precondition(V.p + (size_t)k * n, zk)) return -1;
-                    PEEC_LAUNCH(k_zmv_scaled, gw, 256, 0, Z, zk, rs.p, n, w.p);
-                    for (int pass = 0; pass < 2; ++pass) {
-                        PEEC_LAUNCH(k_gs_dots, (unsigned)(k + 1), 256, 0, V.p, n, w.p, hd.p + pass * (m + 1));
-                        PEEC_LAUNCH(k_gs_update, gn, 256, 0, V.p, n, k + 1, hd.p + pass * (m + 1), w.p);
+                GmresScalars sc0{};
+                bool any = false;
+                for (int q = 0; q < nq; ++q) {
+                    if (!live[q]) continue;
+                    memcpy(&eta_q[q], &hb[q], sizeof(double));
+                    if (eta_q[q] <= tol || !isfinite(eta_q[q]) || eta_q[q] > 0.5 * prev[q] || !(beta[q] > 0.0) ||
+                        !isfinite(beta[q])) {
+                        live[q] = 0;
+                        continue;
                     }
-                    PEEC_LAUNCH(k_norm2, 1, 1024, 0, w.p, n, nrm.p);
-                    double hn = 0.0;
+                    prev[q] = eta_q[q];
+                    sc0.v[q] = 1.0 / beta[q];
+                    any = true;
+                }
+                if (!any) break;
+                PEEC_LAUNCH(k_cscale, gq, 256, 0, V.p, n, sc0, V.p);
+                std::vector<std::vector<zc>> H(nq, std::vector<zc>((size_t)(m + 1) * m)), g(nq), sn(nq);
+                std::vector<std::vector<double>> c(nq, std::vector<double>(m));
+                std::vector<cplx> hh((size_t)2 * Q * ld);
+                std::vector<char> inner(live);
+                GmresCounts kk{};
+                for (int q = 0; q < nq; ++q) {
+                    g[q].assign(m + 1, zc(0.0));
+                    sn[q].assign(m, zc(0.0));
+                    g[q][0] = beta[q];
+                }
+                for (int k = 0; k < m; ++k) {
+                    cplx *zk = Zk.p + (size_t)k * nq * n;
+                    const cplx *vk = V.p + (size_t)k * nq * n;
+                    if (!precondition(vk, zk)) return -1;
+                    PEEC_LAUNCH(k_zmv_scaled, gw, 256, 0, Z, zk, rs.p, n, nq, w.p);
+                    for (int pass = 0; pass < 2; ++pass) {
+                        PEEC_LAUNCH(k_gs_dots, dim3((unsigned)(k + 1), (unsigned)nq), 256, 0, V.p, n, nq, w.p,
+                                    hd.p + (size_t)pass * Q * ld, ld);
+                        PEEC_LAUNCH(k_gs_update, gq, 256, 0, V.p, n, nq, k + 1, hd.p + (size_t)pass * Q * ld, ld, w.p);
+                    }
+                    PEEC_LAUNCH(k_norm2, nq, 1024, 0, w.p, n, nrm.p);
                     cudaMemcpyAsync(hh.data(), hd.p, hh.size() * sizeof(cplx), cudaMemcpyDeviceToHost, stream());
-                    cudaMemcpyAsync(&hn, nrm.p, sizeof(hn), cudaMemcpyDeviceToHost, stream());
+                    cudaMemcpyAsync(hn.data(), nrm.p, nq * sizeof(double), cudaMemcpyDeviceToHost, stream());
                     if (!host_sync("GMRES-IR step")) return -1;
                     ++gmres_total;
-                    zc *col = &H[(size_t)k * (m + 1)];
-                    for (int j = 0; j <= k; ++j)
-                        col[j] = zc(hh[j].re + hh[m + 1 + j].re, hh[j].im + hh[m + 1 + j].im);
-                    if (hn > 0.0 && isfinite(hn))
-                        PEEC_LAUNCH(k_cscale, gn, 256, 0, w.p, n, 1.0 / hn, V.p + (size_t)(k + 1) * n);
-                    // earlier rotations, then a new one zeroing the subdiagonal hn
-                    for (int j = 0; j < k; ++j) {
-                        const zc u = c[j] * col[j] + sn[j] * col[j + 1];
-                        col[j + 1] = -std::conj(sn[j]) * col[j] + c[j] * col[j + 1];
-                        col[j] = u;
+                    GmresScalars sck{};
+                    bool more = false;
+                    for (int q = 0; q < nq; ++q) {
+                        if (!inner[q]) continue;
+                        zc *col = &H[q][(size_t)k * (m + 1)];
+                        const cplx *h0 = &hh[(size_t)q * ld], *h1 = &hh[(size_t)(Q + q) * ld];
+                        for (int j = 0; j <= k; ++j) col[j] = zc(h0[j].re + h1[j].re, h0[j].im + h1[j].im);
+                        const double hq = hn[q];
+                        if (hq > 0.0 && isfinite(hq)) sck.v[q] = 1.0 / hq;
+                        // earlier rotations, then a new one zeroing the subdiagonal hq
+                        for (int j = 0; j < k; ++j) {
+                            const zc u = c[q][j] * col[j] + sn[q][j] * col[j + 1];
+                            col[j + 1] = -std::conj(sn[q][j]) * col[j] + c[q][j] * col[j + 1];
+                            col[j] = u;
+                        }
+                        const double aa = std::abs(col[k]), rr = std::hypot(aa, hq);
+                        if (aa == 0.0) {
+                            c[q][k] = 0.0;
+                            sn[q][k] = 1.0;
+                            col[k] = hq;
+                        } else {
+                            const zc ph = col[k] / aa;
+                            c[q][k] = aa / rr;
+                            sn[q][k] = ph * (hq / rr);
+                            col[k] = ph * rr;
+                        }
+                        g[q][k + 1] = -std::conj(sn[q][k]) * g[q][k];
+                        g[q][k] = c[q][k] * g[q][k];
+                        kk.v[q] = k + 1;
+                        if (!(hq > 0.0) || !isfinite(hq) || std::abs(g[q][k + 1]) <= 1e-6 * beta[q]) {
+                            inner[q] = 0;
+                            sck.v[q] = 0.0;
+                        } else {
+                            more = true;
+                        }
                     }
-                    const double aa = std::abs(col[k]), rr = std::hypot(aa, hn);
-                    if (aa == 0.0) {
-                        c[k] = 0.0;
-                        sn[k] = 1.0;
-                        col[k] = hn;
-                    } else {
-                        const zc ph = col[k] / aa;
-                        c[k] = aa / rr;
-                        sn[k] = ph * (hn / rr);
-                        col[k] = ph * rr;
+                    PEEC_LAUNCH(k_cscale, gq, 256, 0, w.p, n, sck, V.p + (size_t)(k + 1) * nq * n);
+                    if (!more) break;
+                }
+                // y_q from the triangular H_q, x_q += Z_k y_q
+                std::vector<cplx> yh((size_t)Q * ld, cplx{0.0, 0.0});
+                for (int q = 0; q < nq; ++q) {
+                    if (!live[q]) continue;
+                    const int kq = kk.v[q];
+                    std::vector<zc> yv(kq);
+                    for (int i = kq - 1; i >= 0; --i) {
+                        zc sum = g[q][i];
+                        for (int j = i + 1; j < kq; ++j) sum -= H[q][(size_t)j * (m + 1) + i] * yv[j];
+                        yv[i] = sum / H[q][(size_t)i * (m + 1) + i];
                     }
-                    g[k + 1] = -std::conj(sn[k]) * g[k];
-                    g[k] = c[k] * g[k];
-                    kk = k + 1;
-                    if (!(hn > 0.0) || !isfinite(hn) || std::abs(g[k + 1]) <= 1e-6 * beta) break;
+                    for (int i = 0; i < kq; ++i) yh[(size_t)q * ld + i] = cplx{yv[i].real(), yv[i].imag()};
                 }
-                // y from the triangular H, x += Z_k y
-                std::vector<zc> yv(kk);
-                for (int i = kk - 1; i >= 0; --i) {
-                    zc sum = g[i];
-                    for (int j = i + 1; j < kk; ++j) sum -= H[(size_t)j * (m + 1) + i] * yv[j];
-                    yv[i] = sum / H[(size_t)i * (m + 1) + i];
-                }
-                std::vector<cplx> yh(kk);
-                for (int i = 0; i < kk; ++i) yh[i] = cplx{yv[i].real(), yv[i].imag()};
-                cudaMemcpyAsync(yd.p, yh.data(), kk * sizeof(cplx), cudaMemcpyHostToDevice, stream());
-                PEEC_LAUNCH(k_gmres_update, gn, 256, 0, Zk.p, n, kk, yd.p, xq);
+                cudaMemcpyAsync(yd.p, yh.data(), yh.size() * sizeof(cplx), cudaMemcpyHostToDevice, stream());
+                PEEC_LAUNCH(k_gmres_update, gq, 256, 0, Zk.p, n, nq, kk, yd.p, ld, xc);
                 if (!host_sync("GMRES-IR update")) return -1;
             }
-            if (!(eta_q <= tol)) {
-                eta = eta_q;
-                return 1;
+            for (int q = 0; q < nq; ++q) {
+                if (!(eta_q[q] <= tol)) {
+                    eta = eta_q[q];
+                    return 1;
+                }
+                eta_max = std::max(eta_max, eta_q[q]);
             }
-            eta_max = std::max(eta_max, eta_q);
         }
         eta = eta_max;
         return 0;
