@@ -1052,6 +1052,10 @@ def main():
             dist.destroy_process_group()
         return
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    # the serving and sweep legs run up to 32 host threads, one stream each:
+    # as many hardware work queues, so independent streams do not share one
+    # (read when the CUDA context is created)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     from peeeeeeeeeeeeeeeeeeec_gb300 import abi
     lib = abi.load_gpu_lib()
     if not lib.peec_gb300_device_ready():
