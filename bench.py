@@ -22,8 +22,9 @@ Lp and P are quasi-static (the reference has no retardation).
           port where they are absent), on a bounded sample extrapolated to
           one solve (oracle/cpu_baseline.py)
 Legs beside the headline: the mixed-precision solve, serving (config 5:
-Poisson harmonic and lightning requests), the config-4 sweep at a reduced
-size (--batch), transient, retarded, RCS, incidence and far-rule precision;
+Poisson harmonic and lightning requests), the config-4 sweep on 12 of its
+48 meshes (--batch), transient, retarded, RCS, incidence and far-rule
+precision;
 --config3 and --config4 run those configurations alone.
 Multi-GPU: the path does not shard; --gpus N runs N independent replicas
 (one process per GPU) and reports the aggregate.
@@ -1018,11 +1019,12 @@ def main():
     ap.add_argument("--no-retarded", action="store_true")
     ap.add_argument("--serve-window", type=float, default=0.2, help="seconds of Poisson arrivals (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=8)
-    ap.add_argument("--batch", default="12x16",
-                    help="meshes x frequencies of the batched leg, the config-4 sweep at a reduced size (0: skip)")
+    ap.add_argument("--batch", default="12x64",
+                    help="meshes x frequencies of the batched leg, the config-4 sweep on fewer meshes (0: skip)")
     ap.add_argument("--config4", default=None,
                     help="only the batched sweep, meshes x frequencies (e.g. 48x64): sweep graphs vs plain FP64 LU")
-    ap.add_argument("--config4-plain-stride", type=int, default=1)
+    ap.add_argument("--config4-plain-stride", type=int, default=4,
+                    help="the plain arm of the sweep legs solves every k-th frequency (throughput over those)")
     ap.add_argument("--config4-workers", type=int, default=32, help="host threads (streams) of both config-4 arms")
     ap.add_argument("--config3-box", default="2.0,1.0,0.5,80,40,20",
                     help="lx,ly,lz,nx,ny,nz of --config3 (a smaller box for profiling runs)")
@@ -1165,7 +1167,7 @@ def main():
     batched = None
     if args.batch not in ("0", ""):
         bm, bf = (int(v) for v in args.batch.split("x"))
-        batched = config4(lib, bm, bf, workers=args.config4_workers)
+        batched = config4(lib, bm, bf, workers=args.config4_workers, plain_stride=args.config4_plain_stride)
 
     # end to end through the drop-in ABI, host buffers
     e2e = None
