@@ -172,6 +172,31 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Programmatic dependent launch: a kernel launched by pdl_launch may be
+// scheduled while the previous kernel on the stream still runs; it calls
+// pdl_wait() before touching any data, which returns once that kernel has
+// completed and its memory is visible, and pdl_trigger() to let the next
+// kernel be scheduled early in turn.  Both are no-ops in a kernel launched
+// without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream();
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);  // an error stays the thread's last error (launch_ok)
+    note_launch();
+}
+
 }  // namespace peec
 
 #define PEEC_LAUNCH(kernel, grid, block, smem, ...)                              \

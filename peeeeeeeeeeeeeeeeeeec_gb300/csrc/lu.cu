@@ -962,6 +962,8 @@ static const int kClStride = NB + 2;   // tile row stride (complex): 16-byte ali
 
 __global__ void __launch_bounds__(kClMaxThreads) k_panel_cl(cplxf *a, int n, int k0, int kb, int rows_per_cta,
                                                             double limit, long long *piv, Status *st) {
+    pdl_wait();
+    pdl_trigger();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char cl_smem[];
@@ -1195,13 +1197,15 @@ static bool launch_cl_panel(cplxf *a, int n, int k0, int kb, double limit, long 
     cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream();
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = C;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // a programmatic dependent (pdl_wait)
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     note_launch();
     return cuda_ok(cudaLaunchKernelEx(&cfg, k_panel_cl, a, n, k0, kb, rows, limit, piv, st), "cluster FP32 panel launch");
 }
@@ -1212,6 +1216,8 @@ static const int kLaswpCols = 32;  // columns per k_laswp block (shared memory 2
 
 template <class T>
 __global__ void __launch_bounds__(256) k_laswp(T *a, int n, int k0, int kb, const long long *piv, const Status *st) {
+    pdl_wait();
+    pdl_trigger();
     // The kb interchanges (k, piv[k]) applied in order move at most 2 kb
     // rows.  Warp 0 composes them into (destination, source) pairs; then the
     // block stages its kLaswpCols columns of the source rows in shared memory
@@ -1281,6 +1287,8 @@ __global__ void __launch_bounds__(256) k_laswp(T *a, int n, int k0, int kb, cons
 // ---- U12 = L11^-1 A12 ------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(256) k_trsm(T *a, int n, int k0, int kb, int c0, int c1, const Status *st) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ T L[NB][NB];
     if (st->code != 0) return;
     for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
@@ -3318,6 +3326,8 @@ template <int T> struct SplitScheme {
 // e.g. [re_h | re_h | re_l | im_h | im_h | im_l] for T = 3.
 template <int T>
 __global__ void k_split_a(const cplxf *a, int n, int row0, int m, int col0, int kw, int KW, __nv_bfloat16 *out) {
+    pdl_wait();
+    pdl_trigger();
     using S = SplitScheme<T>;
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)m * KW) return;
@@ -3346,6 +3356,8 @@ static const int kSbK = 64, kSbJ = 32, kSbPad = 72;  // plane row: 72 BF16 = 144
 template <int T>
 __global__ void __launch_bounds__(256) k_split_b(const cplxf *a, int n, int row0, int kw, int KW, int col0, int nc,
                                                  __nv_bfloat16 *br, __nv_bfloat16 *bi) {
+    pdl_wait();
+    pdl_trigger();
     using S = SplitScheme<T>;
     constexpr int NP = S::parts;
     __shared__ __align__(16) __nv_bfloat16 pl[2 * NP][kSbJ][kSbPad];  // re parts, then im parts
@@ -3400,6 +3412,8 @@ static constexpr size_t k_lower_inv_smem() {
     return sizeof(cplxf) * ((size_t)8 * 32 * kLiPad + 256 * kLiX + 32 * kLiRow + 32 * kLiX);
 }
 __global__ void __launch_bounds__(256) k_lower_inv(const cplxf *a, int n, int K0, int kw, cplxf *N) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(16) unsigned char li_smem[];
     cplxf *blk = reinterpret_cast<cplxf *>(li_smem);  // [8][32][kLiPad]: L_ii, then L_ii^-1
     cplxf *X = blk + 8 * 32 * kLiPad;                 // [256][kLiX]: rows 32 jb.., this CTA's 8 columns
@@ -3885,16 +3899,16 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             if (m <= 0 || nc <= 0) return true;
             const int KW = (kw + 31) / 32 * 32;
             if (T == 6)
-                PEEC_LAUNCH(k_split_a<6>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
+                pdl_launch(k_split_a<6>, dim3((unsigned)(((long long)m * KW + 255) / 256)), dim3(256), 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
                         ap.p);
             else
-                PEEC_LAUNCH(k_split_a<3>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
+                pdl_launch(k_split_a<3>, dim3((unsigned)(((long long)m * KW + 255) / 256)), dim3(256), 0, lsrc, ld, lrow0, m, lcol0, kw, KW,
                         ap.p);
             if (T == 6)
-                PEEC_LAUNCH(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                pdl_launch(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), dim3(256), 0, a, n, kc, kw, KW, col0, nc,
                         bpr.p, bpi.p);
             else
-                PEEC_LAUNCH(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                pdl_launch(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), dim3(256), 0, a, n, kc, kw, KW, col0, nc,
                         bpr.p, bpi.p);
             if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (2.0 * T * KW);  // issued BF16 tensor flops
             return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 2 * T * KW, row0, col0, n, err.p);
@@ -3903,14 +3917,14 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
             if (m <= 0 || nc <= 0) return true;
             const int KW = (kw + 31) / 32 * 32;
             if (T == 6)
-                PEEC_LAUNCH(k_split_a<6>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
+                pdl_launch(k_split_a<6>, dim3((unsigned)(((long long)m * KW + 255) / 256)), dim3(256), 0, a, n, row0, m, kc, kw, KW, ap.p);
             else
-                PEEC_LAUNCH(k_split_a<3>, (unsigned)(((long long)m * KW + 255) / 256), 256, 0, a, n, row0, m, kc, kw, KW, ap.p);
+                pdl_launch(k_split_a<3>, dim3((unsigned)(((long long)m * KW + 255) / 256)), dim3(256), 0, a, n, row0, m, kc, kw, KW, ap.p);
             if (T == 6)
-                PEEC_LAUNCH(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                pdl_launch(k_split_b<6>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), dim3(256), 0, a, n, kc, kw, KW, col0, nc,
                         bpr.p, bpi.p);
             else
-                PEEC_LAUNCH(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), 256, 0, a, n, kc, kw, KW, col0, nc,
+                pdl_launch(k_split_b<3>, dim3((nc + kSbJ - 1) / kSbJ, (KW + kSbK - 1) / kSbK), dim3(256), 0, a, n, kc, kw, KW, col0, nc,
                         bpr.p, bpi.p);
             if (tm.enabled) tm.flops_update += 2.0 * 2.0 * (double)m * nc * (2.0 * T * KW);  // issued BF16 tensor flops
             if (!outer) return tc_gemm_update_cplx(ap.p, bpr.p, bpi.p, (float *)a, m, nc, 2 * T * KW, row0, col0, n, err.p);
@@ -3960,11 +3974,14 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
                     PEEC_LAUNCH(k_panel<cplxf>, 1, 1024, 0, a, n, k0, kb, limit, piv.p, st.p);
                 }
                 tm.mark(0);
-                PEEC_LAUNCH(k_laswp<cplxf>, (n + kLaswpCols - 1) / kLaswpCols, 256, 2 * NB * kLaswpCols * sizeof(cplxf), a,
-                            n, k0, kb, piv.p, st.p);
+                pdl_launch(k_laswp<cplxf>, dim3((n + kLaswpCols - 1) / kLaswpCols), dim3(256),
+                           2 * NB * kLaswpCols * sizeof(cplxf), a, n, k0, kb, (const long long *)piv.p,
+                           (const Status *)st.p);
                 // the rest of the outer block's columns: U12 rows, then the narrow update
                 const int rin = E - (k0 + kb);
-                if (rin > 0) PEEC_LAUNCH(k_trsm<cplxf>, (rin + 255) / 256, 256, 0, a, n, k0, kb, k0 + kb, E, st.p);
+                if (rin > 0)
+                    pdl_launch(k_trsm<cplxf>, dim3((rin + 255) / 256), dim3(256), 0, a, n, k0, kb, k0 + kb, E,
+                               (const Status *)st.p);
                 tm.mark(1);
                 if (!tc_update(k0 + kb, n - (k0 + kb), k0 + kb, rin, k0, kb)) return -1;
             }
@@ -3975,7 +3992,8 @@ int mixed_solve_impl(const Complex *d_Z, size_t n_, const Complex *d_b, Complex 
                 static const cudaError_t li_attr = cudaFuncSetAttribute(
                     k_lower_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k_lower_inv_smem());
                 if (!cuda_ok(li_attr, "lower-inverse smem attribute")) return -1;
-                PEEC_LAUNCH(k_lower_inv, dim3((kw + 31) / 32, 4), 256, k_lower_inv_smem(), a, n, K0, kw, linv.p);
+                pdl_launch(k_lower_inv, dim3((kw + 31) / 32, 4), dim3(256), k_lower_inv_smem(), (const cplxf *)a, n, K0,
+                           kw, linv.p);
                 tm.mark(1);
                 if (!tc_update_from(linv.p, kw, 0, 0, K0, kw, E, n - E, K0, kw)) return -1;
                 tm.mark(2);

@@ -149,7 +149,7 @@ static bool launch_tc_persistent(const void *a, const void *br, const void *bi, 
     const long long tiles = (long long)((m + tc::kBM - 1) / tc::kBM) * ((n + BN - 1) / BN);
     const int grid = (int)std::min<long long>(tiles, sms);
     tc::PersistentArgs g{m, n, k, d_err};
-    PEEC_LAUNCH((tc::k_tc_gemm_cplx_persistent<BN, S>), grid, 192, smem, ma, mbr, mbi, mc, g);
+    pdl_launch(tc::k_tc_gemm_cplx_persistent<BN, S>, dim3(grid), dim3(192), smem, ma, mbr, mbi, mc, g);
     return launch_tc_ok();
 }
 

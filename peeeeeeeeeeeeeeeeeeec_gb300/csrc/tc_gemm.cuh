@@ -426,6 +426,10 @@ __global__ void __launch_bounds__(192, 1)
     k_tc_gemm_cplx_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_br,
                               const __grid_constant__ CUtensorMap map_bi, const __grid_constant__ CUtensorMap map_c,
                               PersistentArgs args) {
+    // launched as a programmatic dependent: wait for the split kernels
+    // before the barriers, TMEM or any load
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr size_t a_bytes = (size_t)kBM * kBK * 2, b_bytes = (size_t)BN * kBK * 2;
