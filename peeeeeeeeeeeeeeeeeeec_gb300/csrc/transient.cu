@@ -180,6 +180,8 @@ __global__ void k_split_pairs(const double *v, size_t count, float2 *out) {
 // rows x cols FP64 -> float pairs with row stride ld (ld >= cols, the pad
 // columns zero); hi (optional): the high parts alone, same layout
 __global__ void k_split_rows(const double *v, int rows, int cols, int ld, float2 *out, float *hi) {
+    pdl_wait();
+    pdl_trigger();
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)rows * ld) return;
     const int r = (int)(t / ld), c = (int)(t % ld);
@@ -197,6 +199,8 @@ __global__ void k_split_rows(const double *v, int rows, int cols, int ld, float2
 // currents [run][lde] and the potentials [run][ldn] (pad entries zero), so
 // that Lp and A S rows meet 16-byte aligned vectors
 __global__ void k_split_state(const double *x, int runs, int ne, int nv, int lde, int ldn, float2 *xI, float2 *xV) {
+    pdl_wait();
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x, per = lde + ldn;
     if (t >= runs * per) return;
     const int r = t / per, c = t % per;
@@ -305,6 +309,8 @@ __device__ __forceinline__ void row_dot_df(const float2 *row, int n, const float
 // all runs; the rest the (node, run) pairs.
 template <int R>
 __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
+    pdl_wait();
+    pdl_trigger();
     const double omt = 1.0 - A.theta;
     const int nt = A.ne + A.nv;
     if (blockIdx.x == 0 && A.probes && A.record_row >= 0) record_probes(A, A.record_row);
@@ -362,6 +368,8 @@ __global__ void __launch_bounds__(256) k_transient_rhs(StepArgs A, int eb) {
 template <int R>
 __global__ void __launch_bounds__(256) k_minv_apply(const float2 *Minv, int nt, int ldm, const float2 *vs,
                                                     const double *y0, double *y, int nrun) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= nt) return;
     double s[R];
@@ -428,6 +436,8 @@ __device__ __forceinline__ void row_dot_f32(const float *row, int n, const float
 template <int R>
 __global__ void __launch_bounds__(256) k_minv_apply_hi(const float *Mh, int nt, int ldm, const float *vh,
                                                        const double *y0, double *y, int nrun) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= nt) return;
     double s[R];
@@ -442,6 +452,8 @@ __global__ void __launch_bounds__(256) k_minv_apply_hi(const float *Mh, int nt, 
 // F / dt), rows split as in k_transient_rhs.
 template <int R>
 __global__ void __launch_bounds__(256) k_transient_resid(StepArgs A, const double *b, double *res, int eb) {
+    pdl_wait();
+    pdl_trigger();
     const int nt = A.ne + A.nv;
     if ((int)blockIdx.x < eb) {
         const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -600,16 +612,22 @@ static void launch_step(const TransientSystem &S, const StepArgs &A, const StepA
                         int grid, int eb, int mgrid, int nrun) {
     const int nt = S.nt;
     const unsigned xgrid = (unsigned)(((size_t)R * (S.lde + S.ldn) + 255) / 256);
-    PEEC_LAUNCH(k_split_state, xgrid, 256, 0, b.x, R, S.ne, S.nv, S.lde, S.ldn, b.xI, b.xV);
-    PEEC_LAUNCH(k_transient_rhs<R>, grid, 256, 0, A, eb);
+    // the step's chain as programmatic dependents: each kernel waits for the
+    // one before it (pdl_wait) and lets the next be scheduled at once
+    pdl_launch(k_split_state, dim3(xgrid), dim3(256), 0, (const double *)b.x, R, S.ne, S.nv, S.lde, S.ldn, b.xI,
+               b.xV);
+    pdl_launch(k_transient_rhs<R>, dim3(grid), dim3(256), 0, A, eb);
     const int ldm = S.ldm;
     const unsigned pgrid = (unsigned)(((size_t)R * ldm + 255) / 256);
-    PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.rhs, R, nt, ldm, b.vs, (float *)nullptr);
-    PEEC_LAUNCH(k_minv_apply<R>, mgrid, 256, 0, S.minv, nt, ldm, b.vs, (const double *)nullptr, b.x0, nrun);
-    PEEC_LAUNCH(k_split_state, xgrid, 256, 0, b.x0, R, S.ne, S.nv, S.lde, S.ldn, b.x0I, b.x0V);
-    PEEC_LAUNCH(k_transient_resid<R>, grid, 256, 0, Ares, b.rhs, b.res, eb);
-    PEEC_LAUNCH(k_split_rows, pgrid, 256, 0, b.res, R, nt, ldm, b.vs, b.vh);
-    PEEC_LAUNCH(k_minv_apply_hi<R>, mgrid, 256, 0, S.minv_hi, nt, ldm, (const float *)b.vh, b.x0, b.x, nrun);
+    pdl_launch(k_split_rows, dim3(pgrid), dim3(256), 0, (const double *)b.rhs, R, nt, ldm, b.vs, (float *)nullptr);
+    pdl_launch(k_minv_apply<R>, dim3(mgrid), dim3(256), 0, (const float2 *)S.minv, nt, ldm, (const float2 *)b.vs,
+               (const double *)nullptr, b.x0, nrun);
+    pdl_launch(k_split_state, dim3(xgrid), dim3(256), 0, (const double *)b.x0, R, S.ne, S.nv, S.lde, S.ldn, b.x0I,
+               b.x0V);
+    pdl_launch(k_transient_resid<R>, dim3(grid), dim3(256), 0, Ares, (const double *)b.rhs, b.res, eb);
+    pdl_launch(k_split_rows, dim3(pgrid), dim3(256), 0, (const double *)b.res, R, nt, ldm, b.vs, b.vh);
+    pdl_launch(k_minv_apply_hi<R>, dim3(mgrid), dim3(256), 0, (const float *)S.minv_hi, nt, ldm,
+               (const float *)b.vh, (const double *)b.x0, b.x, nrun);
 }
 
 // nrun runs (states d_X[r] = [I; V], sources src[r]) stepped together
